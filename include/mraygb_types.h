@@ -1,0 +1,89 @@
+/*
+ * Plain-old-data mirrors of the parameter and camera types that mray's moment
+ * raymarcher API takes (TobiasRp/mray).  Field order, types and meaning follow
+ * the reference field for field so that a shim around the reference's C++
+ * signatures is a member-wise copy:
+ *
+ *   mraygb_camera                 <- cut::Camera            (src/cut/camera.h:39-55)
+ *   mraygb_generation_params      <- GenerationParameters   (src/parameters.h:49-70)
+ *   mraygb_reconstruction_params  <- ReconstructionParameters (src/parameters.h:231-247)
+ *
+ * C++ `bool` members are stored as uint8_t (same size and alignment under the
+ * Itanium and AAPCS64 ABIs).  No CUDA or torch types appear here.
+ */
+#ifndef MRAYGB_TYPES_H
+#define MRAYGB_TYPES_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* cut::Camera (src/cut/camera.h:39-55).  transform is row-major, m[row][col],
+ * exactly as cut::Mat4f stores it.  The inverse view transform of the
+ * reference is not needed on this path and is not mirrored. */
+typedef struct mraygb_camera
+{
+    float transform[4][4];
+    float position[3];
+    float right[3];
+    float up[3];
+    float dir[3];
+    float scale;
+    float aspect;
+    float znear;
+    int32_t orthographic;
+} mraygb_camera;
+
+/* GenerationParameters (src/parameters.h:49-70), same defaults. */
+typedef struct mraygb_generation_params
+{
+    float step_size;               /* 1.0  */
+    float step_size_write_samples; /* 1.5  (unused on this path) */
+    float data_min;                /* 0.0  */
+    float data_max;                /* 1.0  */
+    float error_threshold;         /* 1.0  */
+    float bias;                    /* 1e-4 */
+    uint8_t compact_image;         /* 1 */
+    uint8_t prediction_coding;     /* 1 */
+    uint8_t compress;              /* 0 (file format; not on this path) */
+    uint8_t entropy_coding;        /* 0 (file format; not on this path) */
+    uint8_t quantization_bits;     /* 32 */
+    uint8_t pad0[3];
+    int32_t coding_warp;           /* 0 = CODING_WARP_DEFAULT_TRANSFORMED, 1 = CODING_WARP_NONE */
+    int32_t quantization_curve_sampling; /* 64 (unused on this path) */
+    uint8_t transform_to_bounds;   /* 0 */
+    uint8_t pad1[3];
+    float transform_bound_eps;     /* 0.01 */
+} mraygb_generation_params;
+
+/* ReconstructionParameters (src/parameters.h:231-247), same defaults.  The
+ * single-scattering block is out of scope; ss_enable must be 0. */
+typedef struct mraygb_reconstruction_params
+{
+    float bias;                    /* 1e-6 */
+    float medium_emission;         /* 0.1  */
+    float medium_scattering;       /* 0.1  */
+    float early_ray_termination;   /* 0.95 */
+    float data_min;                /* 0.0  */
+    float data_max;                /* 1.0  */
+    float step_size;               /* 0.01 */
+    float step_size_write_samples; /* 1.5 (unused on this path) */
+    uint8_t use_truncated_fourier; /* 0 (must be 0: MESE only) */
+    uint8_t ss_enable;             /* 0 (must be 0) */
+    uint8_t pad0[2];
+} mraygb_reconstruction_params;
+
+/* Coding warps (src/coding_params.h:35-42). */
+enum
+{
+    MRAYGB_CODING_WARP_DEFAULT_TRANSFORMED = 0,
+    MRAYGB_CODING_WARP_NONE = 1
+};
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MRAYGB_TYPES_H */

@@ -1,0 +1,174 @@
+"""Seeded synthetic inputs that stand in for the reference's datasets.
+
+The reference evaluates on NetCDF / H5Part datasets (Marschner-Lobb, mixing layers, SPH runs) that are not
+available here; these generators produce fields of the same shapes, sizes and value ranges:
+
+* :func:`marschner_lobb`   -- the analytic Marschner-Lobb test function on [-1, 1]^3, sampled at the
+  reference's corner-aligned voxel positions x_i = -1 + 2 i / N (src/volume.h:97-123 maps voxel i to
+  min + i/N (max - min)).
+* :func:`mixing_layer`     -- rho = 0.5 (1 + tanh((z - z0 - h(x, y)) / 0.02)) on [0, 1]^3, h a sum of seeded
+  Fourier modes (wavenumbers 1..32, amplitude ~ k^(-5/3)), plus 5 % seeded Gaussian noise.
+* :func:`transfer_function` -- a 256-entry RGBA table: extinction and emission each the sum of 4 seeded
+  Gaussian bumps.
+* cameras: a seeded orthographic view of the unit-diagonal cube and a perspective view.
+
+Volumes are float32 arrays indexed ``[z, y, x]`` (x fastest in memory, as ``RegularGrid::read``).
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+
+import numpy as np
+
+from .types import Camera, GenerationParameters, ReconstructionParameters
+
+
+def marschner_lobb(n: int, alpha: float = 0.25, f_m: float = 6.0) -> np.ndarray:
+    """rho(x,y,z) = (1 - sin(pi z / 2) + alpha (1 + cos(2 pi f_M cos(pi r / 2)))) / (2 (1 + alpha)),
+    r = sqrt(x^2 + y^2), on [-1, 1]^3."""
+    c = (-1.0 + 2.0 * np.arange(n, dtype=np.float64) / n)
+    z = c[:, None, None]
+    y = c[None, :, None]
+    x = c[None, None, :]
+    r = np.sqrt(x * x + y * y)
+    rho = (1.0 - np.sin(np.pi * z / 2.0) + alpha * (1.0 + np.cos(2.0 * np.pi * f_m * np.cos(np.pi * r / 2.0))))
+    rho = rho / (2.0 * (1.0 + alpha))
+    return np.ascontiguousarray(np.broadcast_to(rho, (n, n, n)), dtype=np.float32)
+
+
+def mixing_layer(n: int, modes: int = 64, seed: int = 1, noise: float = 0.05, z0: float = 0.5,
+                 amplitude: float = 0.08, width: float = 0.02) -> np.ndarray:
+    """A mixing-layer-like field on [0, 1]^3 (see the module docstring)."""
+    rng = np.random.default_rng(seed)
+    k = rng.uniform(1.0, 32.0, size=modes)
+    theta = rng.uniform(0.0, 2.0 * np.pi, size=modes)
+    phase = rng.uniform(0.0, 2.0 * np.pi, size=modes)
+    amp = k ** (-5.0 / 3.0)
+    amp *= amplitude / np.sqrt(np.sum(amp * amp) / 2.0)
+    c = np.arange(n, dtype=np.float64) / n
+    xx, yy = np.meshgrid(c, c, indexing="xy")  # [y, x]
+    h = np.zeros((n, n), dtype=np.float64)
+    for i in range(modes):
+        kx, ky = k[i] * np.cos(theta[i]), k[i] * np.sin(theta[i])
+        h += amp[i] * np.cos(2.0 * np.pi * (kx * xx + ky * yy) + phase[i])
+    h32 = h.astype(np.float32)
+    out = np.empty((n, n, n), dtype=np.float32)
+    zc = c.astype(np.float32)
+    inv_w = np.float32(1.0 / width)
+    for iz in range(n):
+        np.tanh((zc[iz] - np.float32(z0) - h32) * inv_w, out=out[iz])
+    out += np.float32(1.0)
+    out *= np.float32(0.5)
+    if noise > 0.0:
+        nrng = np.random.default_rng(seed + 1000003)
+        chunk = max(1, (1 << 24) // (n * n))
+        for z in range(0, n, chunk):
+            out[z:z + chunk] += np.float32(noise) * nrng.standard_normal(out[z:z + chunk].shape, dtype=np.float32)
+    return out
+
+
+def transfer_function(seed: int = 7, bumps: int = 4) -> np.ndarray:
+    """A 256 x RGBA float table: alpha (extinction) and rgb (emission) are sums of seeded Gaussian bumps."""
+    rng = np.random.default_rng(seed)
+    s = np.arange(256, dtype=np.float64) / 256.0
+    tf = np.zeros((256, 4), dtype=np.float64)
+    for _ in range(bumps):
+        c, w, a = rng.uniform(0.15, 0.9), rng.uniform(0.02, 0.08), rng.uniform(0.3, 1.0)
+        tf[:, 3] += a * np.exp(-0.5 * ((s - c) / w) ** 2)
+    tf[:, 3] /= tf[:, 3].max()
+    for _ in range(bumps):
+        c, w = rng.uniform(0.1, 0.95), rng.uniform(0.03, 0.12)
+        col = rng.uniform(0.2, 1.0, size=3)
+        tf[:, :3] += col[None, :] * np.exp(-0.5 * ((s - c) / w) ** 2)[:, None]
+    tf[:, :3] /= max(1.0, tf[:, :3].max())
+    return tf.astype(np.float32)
+
+
+def _unit(v):
+    v = np.asarray(v, dtype=np.float64)
+    return v / np.linalg.norm(v)
+
+
+def ortho_camera(seed: int, center=(0.0, 0.0, 0.0), half_extent: float = math.sqrt(3.0),
+                 distance: float = 3.0) -> Camera:
+    """A seeded orthographic view: unit direction d, right/up orthogonal to d spanning +-half_extent,
+    position = center - distance * d."""
+    rng = np.random.default_rng(seed)
+    d = _unit(rng.normal(size=3))
+    helper = np.array([0.0, 0.0, 1.0]) if abs(d[2]) < 0.9 else np.array([1.0, 0.0, 0.0])
+    right = _unit(np.cross(d, helper))
+    up = _unit(np.cross(right, d))
+    pos = np.asarray(center, dtype=np.float64) - distance * d
+    return Camera.orthographic_camera(pos, right * half_extent, up * half_extent, d)
+
+
+def look_at_transform(eye, target, up=(0.0, 0.0, 1.0)) -> np.ndarray:
+    """Camera->world matrix (row-major) for a camera at ``eye`` looking at ``target``; the camera looks
+    along -z in camera space (src/cut/raytracing.h:39-49)."""
+    eye = np.asarray(eye, dtype=np.float64)
+    f = _unit(np.asarray(target, dtype=np.float64) - eye)
+    r = _unit(np.cross(f, up))
+    u = np.cross(r, f)
+    m = np.eye(4)
+    m[:3, 0] = r
+    m[:3, 1] = u
+    m[:3, 2] = -f
+    m[:3, 3] = eye
+    return m
+
+
+def perspective_camera(eye, target, fov_deg: float, aspect: float = 1.0, znear: float = 0.0) -> Camera:
+    return Camera.perspective_camera(look_at_transform(eye, target), math.tan(math.radians(fov_deg) / 2.0),
+                                     aspect, znear)
+
+
+@dataclasses.dataclass
+class Workload:
+    """One configuration of the path: volume, view, image, moments and the two parameter blocks."""
+
+    name: str
+    volume: np.ndarray
+    domain_min: tuple
+    domain_max: tuple
+    width: int
+    height: int
+    num_moments: int
+    camera: Camera
+    gen: GenerationParameters
+    rec: ReconstructionParameters
+    tf1d: np.ndarray
+    tf_step: float  # step_size * preintegration_step_size_factor (main.cpp:100-105)
+
+    @property
+    def num_rays(self) -> int:
+        return self.width * self.height
+
+
+def ml_workload(n: int = 64, width: int = 512, height: int = 512, num_moments: int = 31, seed: int = 11,
+                name: str = "ml64_512sq_m31_ortho") -> Workload:
+    """Marschner-Lobb n^3 on [-1,1]^3, orthographic seeded view, 0.5-voxel steps, bounded moments
+    (transform_to_bounds, eps 0.005), compaction with threshold 0, no prediction coding, bias 5e-5,
+    emission 1.0, early termination 0.99 (eval/marschner_lobb/marschner_lobb.json)."""
+    step = 0.5 * 2.0 / n
+    gen = GenerationParameters(step_size=step, error_threshold=0.0, bias=5e-5, compact_image=1,
+                               prediction_coding=0, transform_to_bounds=1, transform_bound_eps=0.005)
+    rec = ReconstructionParameters(step_size=step, bias=5e-5, medium_emission=1.0, early_ray_termination=0.99)
+    return Workload(name, marschner_lobb(n), (-1.0, -1.0, -1.0), (1.0, 1.0, 1.0), width, height, num_moments,
+                    ortho_camera(seed), gen, rec, transfer_function(seed + 1), tf_step=0.05)
+
+
+def mixing_layer_workload(n: int = 512, width: int = 1024, height: int = 1024, num_moments: int = 64,
+                          modes: int = 64, seed: int = 21, prediction_coding: bool = False,
+                          name: str | None = None) -> Workload:
+    """Mixing layer n^3 on [0,1]^3, perspective view, 0.5-voxel steps."""
+    step = 0.5 / n
+    gen = GenerationParameters(step_size=step, error_threshold=0.0, bias=5e-5, compact_image=1,
+                               prediction_coding=1 if prediction_coding else 0, transform_to_bounds=1,
+                               transform_bound_eps=0.005, quantization_bits=10 if prediction_coding else 32,
+                               coding_warp=0)
+    rec = ReconstructionParameters(step_size=step, bias=5e-5, medium_emission=1.0, early_ray_termination=0.99)
+    cam = perspective_camera(eye=(1.9, -1.1, 1.45), target=(0.5, 0.5, 0.5), fov_deg=38.0, aspect=width / height)
+    name = name or f"mixing_layer{n}_{width}x{height}_m{num_moments}_persp"
+    return Workload(name, mixing_layer(n, modes=modes, seed=seed), (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), width,
+                    height, num_moments, cam, gen, rec, transfer_function(seed + 1), tf_step=0.05 * (512.0 / n))

@@ -1,0 +1,307 @@
+"""ORACLE -- test infrastructure only.
+
+ctypes front end of the C restatement of the reference's CPU path (``oracle/mray_oracle.c``, built by
+``oracle/Makefile`` into ``oracle/_build/liboracle.so``) and, where it was built, of the reference's own CPU
+code (``oracle/_ref/libmrayref.so``).  Imported by ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline
+leg of ``bench.py`` only; the product never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+REF_LIB_PATH = os.path.join(HERE, "_ref", "libmrayref.so")
+
+_lock = threading.Lock()
+_lib = None
+_ref = None
+
+fp = np.ctypeslib.ndpointer
+
+
+class Options(C.Structure):
+    _fields_ = [("exact_atan", C.c_int), ("nthreads", C.c_int), ("row_begin", C.c_int), ("row_end", C.c_int),
+                ("row_step", C.c_int)]
+
+
+class Grid(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+                ("dmin", C.c_float * 3), ("dmax", C.c_float * 3)]
+
+
+def build(force: bool = False) -> None:
+    """Compile liboracle.so (and the reference library when its sources exist)."""
+    if force or not os.path.exists(LIB_PATH):
+        subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
+
+
+def build_ref() -> bool:
+    """Compile the reference's own CPU path into oracle/_ref (only where the reference sources exist)."""
+    src = os.environ.get("MRAY_REFERENCE_SRC", "/root/reference/src")
+    if not os.path.isdir(src):
+        return False
+    subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={src}"], check=True)
+    return os.path.exists(REF_LIB_PATH)
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is None:
+            build()
+            _lib = C.CDLL(LIB_PATH)
+            _declare(_lib)
+        return _lib
+
+
+def ref_lib():
+    """The reference's own CPU code, or None where it cannot be built."""
+    global _ref
+    with _lock:
+        if _ref is None:
+            if not os.path.exists(REF_LIB_PATH) and not build_ref():
+                return None
+            _ref = C.CDLL(REF_LIB_PATH)
+        return _ref
+
+
+def _declare(L):
+    from mray_gb300.types import Camera, GenerationParameters, ReconstructionParameters
+
+    P = C.POINTER
+    for sfx, R in (("f32", C.c_float), ("f64", C.c_double)):
+        f = getattr(L, f"oracle_generate_moments_{sfx}")
+        f.argtypes = [P(Camera), P(GenerationParameters), P(Grid), C.c_int, C.c_int, C.c_int, C.c_void_p,
+                      C.c_void_p, C.c_void_p, P(Options)]
+        f.restype = None
+        f = getattr(L, f"oracle_prepare_moments_{sfx}")
+        f.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_float,
+                      C.c_void_p, P(Options)]
+        f.restype = None
+        f = getattr(L, f"oracle_reconstruct_{sfx}")
+        f.argtypes = [P(Camera), P(ReconstructionParameters), C.c_int, C.c_int, C.c_int, C.c_float * 3,
+                      C.c_float * 3, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, P(Options)]
+        f.restype = None
+        getattr(L, f"oracle_evaluate_mese_{sfx}").restype = R
+        getattr(L, f"oracle_evaluate_mese_{sfx}").argtypes = [C.c_int, R, C.c_void_p, C.c_int]
+        getattr(L, f"oracle_fast_atan_{sfx}").restype = R
+        getattr(L, f"oracle_fast_atan_{sfx}").argtypes = [R]
+        getattr(L, f"oracle_determine_best_number_moments_{sfx}").argtypes = [C.c_int, C.c_void_p, R]
+        getattr(L, f"oracle_determine_best_number_moments_{sfx}").restype = C.c_int
+        getattr(L, f"oracle_rmse_{sfx}").argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+        getattr(L, f"oracle_rmse_{sfx}").restype = R
+        getattr(L, f"oracle_transform_quantization_real_{sfx}").argtypes = [C.c_int, C.c_void_p, R, C.c_void_p]
+        getattr(L, f"oracle_grid_sample_{sfx}").argtypes = [P(Grid), C.c_void_p]
+        getattr(L, f"oracle_grid_sample_{sfx}").restype = R
+        getattr(L, f"oracle_tf_sample_{sfx}").argtypes = [C.c_void_p, R, R, C.c_void_p]
+    L.oracle_compact.restype = C.c_uint64
+    L.oracle_compact.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.oracle_prediction_encode.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_uint64, C.c_int,
+                                           C.c_float, C.c_void_p, P(Options)]
+    L.oracle_find_coding_transform_parameters.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                                          C.c_uint64, C.c_void_p]
+    L.oracle_quantize.restype = C.c_uint32
+    L.oracle_quantize.argtypes = [C.c_float, C.c_int, C.c_float, C.c_float]
+    L.oracle_dequantize.restype = C.c_float
+    L.oracle_dequantize.argtypes = [C.c_uint32, C.c_int, C.c_float, C.c_float]
+    L.oracle_quantize_prediction_coding.restype = C.c_uint64
+    L.oracle_quantize_prediction_coding.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                    C.c_void_p]
+    L.oracle_dequantize_prediction_coding.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                                      C.c_void_p, C.c_uint64, C.c_void_p]
+    L.oracle_preintegrate.argtypes = [C.c_void_p, C.c_float, C.c_void_p]
+    L.oracle_rgba_to_u8.argtypes = [C.c_uint64, C.c_void_p, C.c_void_p]
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _grid(volume, dmin, dmax):
+    g = Grid()
+    v = np.ascontiguousarray(volume, dtype=np.float32)
+    g.data = v.ctypes.data
+    g.nz, g.ny, g.nx = v.shape
+    for i in range(3):
+        g.dmin[i] = dmin[i]
+        g.dmax[i] = dmax[i]
+    return g, v
+
+
+def options(nthreads=0, rows=None, exact_atan=False):
+    o = Options()
+    o.exact_atan = int(exact_atan)
+    o.nthreads = int(nthreads)
+    if rows is None:
+        o.row_begin, o.row_end, o.row_step = 0, 0, 1
+    else:
+        o.row_begin, o.row_end, o.row_step = rows
+    return o
+
+
+def _dt(precision):
+    return np.float32 if precision == "f32" else np.float64
+
+
+# --------------------------------------------------------------------------------------------------------------
+# pipeline stages
+# --------------------------------------------------------------------------------------------------------------
+
+def generate_moments(cam, gp, volume, dmin, dmax, width, height, m, precision="f32", nthreads=0, rows=None):
+    """generate_host's per-pixel loop: returns (moments[H,W,m], bounds[H,W,2] u16, counts[H,W] u32)."""
+    L = lib()
+    dt = _dt(precision)
+    g, keep = _grid(volume, dmin, dmax)
+    moments = np.zeros((height, width, m), dtype=dt)
+    bounds = np.zeros((height, width, 2), dtype=np.uint16)
+    counts = np.zeros((height, width), dtype=np.uint32)
+    o = options(nthreads, rows)
+    getattr(L, f"oracle_generate_moments_{precision}")(C.byref(cam), C.byref(gp), C.byref(g), width, height, m,
+                                                       _ptr(moments), _ptr(bounds), _ptr(counts), C.byref(o))
+    del keep
+    return moments, bounds, counts
+
+
+def compact(counts, moments):
+    """MomentImageHost::compact: returns (index[W*H+1] u32, data[total] f32)."""
+    L = lib()
+    h, w, m = moments.shape
+    counts = np.ascontiguousarray(counts, dtype=np.uint32)
+    mo = np.ascontiguousarray(moments, dtype=np.float32)
+    index = np.zeros(w * h + 1, dtype=np.uint32)
+    total = int(L.oracle_compact(w, h, m, _ptr(counts), _ptr(mo), _ptr(index), None))
+    data = np.zeros(max(total, 1), dtype=np.float32)[:total]
+    if total:
+        L.oracle_compact(w, h, m, _ptr(counts), _ptr(mo), _ptr(index), _ptr(data))
+    return index, data
+
+
+def prediction_encode(width, height, m, index, data, coding_warp=0, bias=1e-4, nthreads=0):
+    """MomentImageHost::prediction_encode on a copy; returns (data, coding_params u16[2(m-1)])."""
+    L = lib()
+    d = np.array(data, dtype=np.float32, copy=True)
+    cp = np.zeros(max(2 * (m - 1), 1), dtype=np.uint16)
+    o = options(nthreads)
+    L.oracle_prediction_encode(width, height, m, _ptr(np.ascontiguousarray(index, dtype=np.uint32)), _ptr(d),
+                               d.size, coding_warp, bias, _ptr(cp), C.byref(o))
+    return d, cp[:2 * (m - 1)]
+
+
+def find_coding_transform_parameters(width, height, m, index, data):
+    L = lib()
+    d = np.ascontiguousarray(data, dtype=np.float32)
+    out = np.zeros(max(2 * (m - 1), 1), dtype=np.float32)
+    L.oracle_find_coding_transform_parameters(width, height, m, _ptr(np.ascontiguousarray(index, dtype=np.uint32)),
+                                              _ptr(d), d.size, _ptr(out))
+    return out[:2 * (m - 1)]
+
+
+def quantize_prediction_coding(width, height, m, index, data, table):
+    L = lib()
+    idx = np.ascontiguousarray(index, dtype=np.uint32)
+    d = np.ascontiguousarray(data, dtype=np.float32)
+    t = np.ascontiguousarray(table, dtype=np.uint8)
+    n = int(L.oracle_quantize_prediction_coding(width, height, m, _ptr(idx), _ptr(d), _ptr(t), None))
+    out = np.zeros(max(n, 1), dtype=np.uint8)
+    L.oracle_quantize_prediction_coding(width, height, m, _ptr(idx), _ptr(d), _ptr(t), _ptr(out))
+    return out[:n]
+
+
+def dequantize_prediction_coding(width, height, m, index, table, packed, size):
+    L = lib()
+    out = np.zeros(max(size, 1), dtype=np.float32)
+    b = np.ascontiguousarray(packed, dtype=np.uint8)
+    L.oracle_dequantize_prediction_coding(width, height, m, _ptr(np.ascontiguousarray(index, dtype=np.uint32)),
+                                          _ptr(np.ascontiguousarray(table, dtype=np.uint8)), _ptr(b), b.size,
+                                          _ptr(out))
+    return out[:size]
+
+
+def default_quantization_table(m, bits):
+    return np.array([16] + [bits] * (m - 1), dtype=np.uint8)[:m]
+
+
+def prepare_moments(width, height, m, index, data, prediction_code=False, coding_warp=0, coding_params=None,
+                    bias=1e-6, precision="f32", nthreads=0, rows=None):
+    """MomentImageHost::prepare_moments for every pixel; returns the Lagrange multipliers in the data layout."""
+    L = lib()
+    d = np.ascontiguousarray(data, dtype=np.float32)
+    out = np.zeros(max(d.size, 1), dtype=_dt(precision))
+    cp = None if coding_params is None else np.ascontiguousarray(coding_params, dtype=np.uint16)
+    idx = None if index is None else np.ascontiguousarray(index, dtype=np.uint32)
+    o = options(nthreads, rows)
+    getattr(L, f"oracle_prepare_moments_{precision}")(width, height, m, _ptr(idx), _ptr(d), int(prediction_code),
+                                                      coding_warp, _ptr(cp), bias, _ptr(out), C.byref(o))
+    return out[:d.size]
+
+
+def reconstruct(cam, rp, width, height, m, dmin, dmax, index, pmoments, bounds, tf_table, precision="f32",
+                nthreads=0, rows=None, exact_atan=False):
+    """reconstruct_host with float RGBA: returns rgba[H,W,4]."""
+    L = lib()
+    dt = _dt(precision)
+    pm = np.ascontiguousarray(pmoments, dtype=dt)
+    idx = None if index is None else np.ascontiguousarray(index, dtype=np.uint32)
+    b = None if bounds is None else np.ascontiguousarray(bounds, dtype=np.uint16)
+    t = np.ascontiguousarray(tf_table, dtype=np.float32)
+    out = np.zeros((height, width, 4), dtype=dt)
+    o = options(nthreads, rows, exact_atan)
+    getattr(L, f"oracle_reconstruct_{precision}")(C.byref(cam), C.byref(rp), width, height, m,
+                                                  (C.c_float * 3)(*dmin), (C.c_float * 3)(*dmax), _ptr(idx),
+                                                  _ptr(pm), _ptr(b), _ptr(t), _ptr(out), C.byref(o))
+    return out
+
+
+def preintegrate(tf1d, step_size):
+    L = lib()
+    src = np.ascontiguousarray(tf1d, dtype=np.float32)
+    out = np.zeros((256, 4), dtype=np.float32)
+    L.oracle_preintegrate(_ptr(src), step_size, _ptr(out))
+    return out
+
+
+def rgba_to_u8(rgba):
+    L = lib()
+    src = np.ascontiguousarray(rgba, dtype=np.float32)
+    out = np.zeros(src.shape, dtype=np.uint8)
+    L.oracle_rgba_to_u8(src.size // 4, _ptr(src), _ptr(out))
+    return out
+
+
+def generate(cam, gp, volume, dmin, dmax, width, height, m, precision="f32", nthreads=0):
+    """The whole reference ``generate()`` on the CPU (moment_raymarcher.cpp:121-166): per-pixel moments, counts,
+    compaction and prediction coding as the parameters ask.  Returns a dict like a MomentImageHost."""
+    moments, bounds, counts = generate_moments(cam, gp, volume, dmin, dmax, width, height, m, precision, nthreads)
+    res = {"width": width, "height": height, "num_moments": m, "bounds": bounds if gp.transform_to_bounds else None,
+           "raw_moments": moments, "counts": counts, "is_compact": bool(gp.compact_image),
+           "prediction_code": False, "coding_warp": int(gp.coding_warp), "coding_params": None}
+    if gp.compact_image:
+        index, data = compact(counts, moments.astype(np.float32))
+        res["index"], res["data"] = index, data
+        if gp.prediction_coding:
+            d, cp = prediction_encode(width, height, m, index, data, gp.coding_warp, gp.bias, nthreads)
+            res["data"], res["prediction_code"] = d, True
+            res["coding_params"] = cp if gp.coding_warp == 0 else None
+    else:
+        res["index"], res["data"] = None, moments.reshape(-1)
+    return res
+
+
+def workload_generate(wl, precision="f32", nthreads=0):
+    return generate(wl.camera, wl.gen, wl.volume, wl.domain_min, wl.domain_max, wl.width, wl.height,
+                    wl.num_moments, precision, nthreads)
+
+
+def workload_reconstruct(wl, mi, precision="f32", nthreads=0, exact_atan=False):
+    """prepare + MESE re-march of a moment image from :func:`generate`."""
+    tf = preintegrate(wl.tf1d, wl.tf_step)
+    pm = prepare_moments(wl.width, wl.height, wl.num_moments, mi["index"], mi["data"], mi["prediction_code"],
+                         mi["coding_warp"], mi["coding_params"], wl.rec.bias, precision, nthreads)
+    return reconstruct(wl.camera, wl.rec, wl.width, wl.height, wl.num_moments, wl.domain_min, wl.domain_max,
+                       mi["index"], pm, mi["bounds"], tf, precision, nthreads, exact_atan=exact_atan)

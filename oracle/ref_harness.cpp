@@ -1,0 +1,459 @@
+/*
+ * ORACLE — test infrastructure only.
+ *
+ * A C-ABI harness around the reference's OWN CPU implementation (TobiasRp/mray, compiled from its sources
+ * where they lie by oracle/Makefile into oracle/_ref/).  It is used in the development container to pin
+ * the C restatement (mray_oracle.c) and to write the golden fixtures under tests/golden/.  It only calls
+ * the reference's functions; it computes nothing of its own except copying data in and out and, for the
+ * float colour output, the per-pixel loop of reconstruct_host (moment_raymarcher.cpp:283-327) without its
+ * final u8 store.
+ */
+#include "../include/mraygb_types.h"
+
+#include "moment_raymarcher.h"
+#include "raymarch_generate.h"
+#include "raymarch_reconstruct.h"
+#include "moment_compaction.h"
+#include "moment_image.h"
+#include "moment_quantization.h"
+#include "coding_transform.h"
+#include "moment_prediction_coding.h"
+#include "mese/MESE_dynamic.h"
+#include "mese/MESE_4_10.h"
+#include "transfer_function.h"
+#include "color_image.h"
+#include "volume.h"
+#include "cut/raytracing.h"
+
+#include <cstring>
+
+/* defined in transfer_function.cpp without a header declaration */
+TransferFunction preintegrate(const array<Vec4f, TransferFunction::RESOLUTION> &tf1d, float step_size);
+
+namespace
+{
+cut::Camera to_camera(const mraygb_camera *c)
+{
+    cut::Camera cam;
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j)
+            cam.transform[i][j] = c->transform[i][j];
+    cam.position = Vec3f(c->position[0], c->position[1], c->position[2]);
+    cam.right = Vec3f(c->right[0], c->right[1], c->right[2]);
+    cam.up = Vec3f(c->up[0], c->up[1], c->up[2]);
+    cam.dir = Vec3f(c->dir[0], c->dir[1], c->dir[2]);
+    cam.scale = c->scale;
+    cam.aspect = c->aspect;
+    cam.znear = c->znear;
+    cam.orthographic = c->orthographic != 0;
+    return cam;
+}
+
+GenerationParameters to_gen(const mraygb_generation_params *g)
+{
+    GenerationParameters p;
+    p.step_size = g->step_size;
+    p.step_size_write_samples = g->step_size_write_samples;
+    p.data_min = g->data_min;
+    p.data_max = g->data_max;
+    p.error_threshold = g->error_threshold;
+    p.bias = g->bias;
+    p.compact_image = g->compact_image != 0;
+    p.prediction_coding = g->prediction_coding != 0;
+    p.compress = g->compress != 0;
+    p.entropy_coding = g->entropy_coding != 0;
+    p.quantization_bits = g->quantization_bits;
+    p.coding_warp = g->coding_warp;
+    p.quantization_curve_sampling = g->quantization_curve_sampling;
+    p.transform_to_bounds = g->transform_to_bounds != 0;
+    p.transform_bound_eps = g->transform_bound_eps;
+    return p;
+}
+
+ReconstructionParameters to_rec(const mraygb_reconstruction_params *r)
+{
+    ReconstructionParameters p;
+    p.bias = r->bias;
+    p.medium_emission = r->medium_emission;
+    p.medium_scattering = r->medium_scattering;
+    p.early_ray_termination = r->early_ray_termination;
+    p.data_min = r->data_min;
+    p.data_max = r->data_max;
+    p.step_size = r->step_size;
+    p.step_size_write_samples = r->step_size_write_samples;
+    p.use_truncated_fourier = r->use_truncated_fourier != 0;
+    return p;
+}
+
+Range<Vec3f> to_range(const float *mn, const float *mx)
+{
+    return Range<Vec3f>(Vec3f(mn[0], mn[1], mn[2]), Vec3f(mx[0], mx[1], mx[2]));
+}
+
+/* A MomentImageHost from flat arrays (compact when index != nullptr). */
+MomentImageHost make_mi(int w, int h, int m, const uint32_t *index, const float *data, uint64_t data_size,
+                        const uint16_t *bounds, int prediction_code, int coding_warp, const uint16_t *coding_params,
+                        const float *dmin, const float *dmax)
+{
+    MomentImageHost mi(w, h, m, index != nullptr, bounds != nullptr);
+    if (index)
+    {
+        std::memcpy(mi.index.data(), index, sizeof(uint32_t) * (size_t(w) * h + 1));
+        mi.is_compact = true;
+    }
+    mi.data.assign(data, data + data_size);
+    if (bounds)
+        for (size_t i = 0; i < size_t(w) * h; ++i)
+        {
+            mi.bounds[i].lower = bounds[2 * i];
+            mi.bounds[i].upper = bounds[2 * i + 1];
+        }
+    mi.prediction_code = prediction_code != 0;
+    mi.coding_warp = static_cast<CodingWarpType>(coding_warp);
+    if (prediction_code && coding_warp == CODING_WARP_DEFAULT_TRANSFORMED && coding_params)
+        for (int i = 0; i < m - 1; ++i)
+            mi.coding_params.push_back(CodingParamType{coding_params[2 * i], coding_params[2 * i + 1]});
+    if (dmin)
+        mi.domain = to_range(dmin, dmax);
+    return mi;
+}
+
+TransferFunction make_tf(const float *row)
+{
+    TransferFunction tf;
+    for (int y = 0; y < TransferFunction::RESOLUTION; ++y)
+        for (int x = 0; x < TransferFunction::RESOLUTION; ++x)
+            tf.data[y * TransferFunction::RESOLUTION + x] =
+                Vec4f(row[4 * x], row[4 * x + 1], row[4 * x + 2], row[4 * x + 3]);
+    return tf;
+}
+} // namespace
+
+extern "C" {
+
+/* generate() -> generate_host (moment_raymarcher.cpp:121-183) with the MomentImageHost that main.cpp:300
+ * builds.  out_data needs W*H*m floats. */
+int ref_generate_grid(const mraygb_camera *c, const mraygb_generation_params *g, const float *vol, int nx, int ny,
+                      int nz, const float *dmin, const float *dmax, int w, int h, int m, float *out_data,
+                      uint32_t *out_index, uint16_t *out_bounds, uint16_t *out_coding_params, uint64_t *out_size,
+                      int *out_flags)
+{
+    auto gp = to_gen(g);
+    RegularGrid grid(Vec3i(nx, ny, nz), to_range(dmin, dmax), std::vector<float>(vol, vol + size_t(nx) * ny * nz),
+                     RegularGrid::DataType::F32);
+    MomentImageHost mi(w, h, m, gp.compact_image, gp.transform_to_bounds);
+    mi.domain = grid.domain;
+    generate(to_camera(c), grid, mi, gp);
+    std::memcpy(out_data, mi.data.data(), sizeof(float) * mi.data.size());
+    *out_size = mi.data.size();
+    if (out_index && !mi.index.empty())
+        std::memcpy(out_index, mi.index.data(), sizeof(uint32_t) * mi.index.size());
+    if (out_bounds && mi.has_bounds())
+        for (size_t i = 0; i < mi.bounds.size(); ++i)
+        {
+            out_bounds[2 * i] = mi.bounds[i].lower;
+            out_bounds[2 * i + 1] = mi.bounds[i].upper;
+        }
+    if (out_coding_params)
+        for (size_t i = 0; i < mi.coding_params.size(); ++i)
+        {
+            out_coding_params[2 * i] = mi.coding_params[i].param1;
+            out_coding_params[2 * i + 1] = mi.coding_params[i].param2;
+        }
+    out_flags[0] = mi.is_compact;
+    out_flags[1] = mi.prediction_code;
+    out_flags[2] = mi.coding_warp;
+    out_flags[3] = mi.has_bounds();
+    return 0;
+}
+
+/* reconstruct() -> reconstruct_host (moment_raymarcher.cpp:283-337): u8 RGBA as the reference stores it. */
+int ref_reconstruct_u8(const mraygb_camera *c, const mraygb_reconstruction_params *r, int w, int h, int m,
+                       const uint32_t *index, const float *data, uint64_t data_size, const uint16_t *bounds,
+                       int prediction_code, int coding_warp, const uint16_t *coding_params, const float *dmin,
+                       const float *dmax, const float *tf_row, uint8_t *out_rgba8)
+{
+    auto mi = make_mi(w, h, m, index, data, data_size, bounds, prediction_code, coding_warp, coding_params, dmin,
+                      dmax);
+    auto tf = make_tf(tf_row);
+    ColorImageHost img(w, h);
+    reconstruct(to_camera(c), mi, tf, img, to_rec(r));
+    std::memcpy(out_rgba8, img.rgba.data(), 4 * size_t(w) * h);
+    return 0;
+}
+
+/* The per-pixel body of reconstruct_host (moment_raymarcher.cpp:296-325, MESE branch) keeping the float colour. */
+int ref_reconstruct_float(const mraygb_camera *c, const mraygb_reconstruction_params *r, int w, int h, int m,
+                          const uint32_t *index, const float *data, uint64_t data_size, const uint16_t *bounds,
+                          int prediction_code, int coding_warp, const uint16_t *coding_params, const float *dmin,
+                          const float *dmax, const float *tf_row, float *out_rgba)
+{
+    auto mi = make_mi(w, h, m, index, data, data_size, bounds, prediction_code, coding_warp, coding_params, dmin,
+                      dmax);
+    auto tf = make_tf(tf_row);
+    auto cam = to_camera(c);
+    auto params = to_rec(r);
+    NoSingleScattering ss;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int y = 0; y < h; ++y)
+        for (int x = 0; x < w; ++x)
+        {
+            Vec2f ndc(x / static_cast<float>(w) * 2.f - 1.f, y / static_cast<float>(h) * 2.f - 1.f);
+            Vec4f color;
+            if (mi.get_num_moments(x, y) == 0)
+                color = reconstruct_zero_ray(tf);
+            else
+            {
+                auto pm = mi.prepare_moments(x, y, params.bias);
+                MESEReconstructionDefault rec(pm.size(), pm.data(), mi.get_bounds(x, y));
+                color = reconstruct_ray(cut::get_eye_ray(cam, ndc), mi.domain, cam.znear, rec, tf, ss, params);
+            }
+            float *o = out_rgba + 4 * (size_t(y) * w + x);
+            o[0] = color.x;
+            o[1] = color.y;
+            o[2] = color.z;
+            o[3] = color.w;
+        }
+    return 0;
+}
+
+/* MomentImageHost::prepare_moments (moment_image.cpp:154-183) for every pixel; output in the data layout. */
+int ref_prepare_moments(int w, int h, int m, const uint32_t *index, const float *data, uint64_t data_size,
+                        int prediction_code, int coding_warp, const uint16_t *coding_params, float bias, float *out)
+{
+    auto mi =
+        make_mi(w, h, m, index, data, data_size, nullptr, prediction_code, coding_warp, coding_params, nullptr, nullptr);
+    for (int y = 0; y < h; ++y)
+        for (int x = 0; x < w; ++x)
+        {
+            if (mi.get_num_moments(x, y) == 0)
+                continue;
+            auto pm = mi.prepare_moments(x, y, bias);
+            std::memcpy(out + mi.get_idx(x, y), pm.data(), sizeof(float) * pm.size());
+        }
+    return 0;
+}
+
+/* MomentImageHost::prediction_encode (moment_image.cpp:96-152), in place. */
+int ref_prediction_encode(int w, int h, int m, const uint32_t *index, float *data, uint64_t data_size, int warp,
+                          float bias, uint16_t *out_coding_params)
+{
+    auto mi = make_mi(w, h, m, index, data, data_size, nullptr, 0, warp, nullptr, nullptr, nullptr);
+    mi.prediction_encode(warp, bias);
+    std::memcpy(data, mi.data.data(), sizeof(float) * data_size);
+    if (out_coding_params)
+        for (size_t i = 0; i < mi.coding_params.size(); ++i)
+        {
+            out_coding_params[2 * i] = mi.coding_params[i].param1;
+            out_coding_params[2 * i + 1] = mi.coding_params[i].param2;
+        }
+    return 0;
+}
+
+/* find_coding_transform_parameters (coding_transform.h:37-68). */
+int ref_find_coding_transform_parameters(int w, int h, int m, const uint32_t *index, const float *data,
+                                         uint64_t data_size, float *out)
+{
+    auto mi = make_mi(w, h, m, index, data, data_size, nullptr, 0, 0, nullptr, nullptr, nullptr);
+    auto p = find_coding_transform_parameters(mi);
+    std::memcpy(out, p.data(), sizeof(float) * p.size());
+    return 0;
+}
+
+/* moment_quantization::quantize_prediction_coding (moment_quantization.cpp:239-276).  Returns the byte count;
+ * out may be nullptr. */
+uint64_t ref_quantize_prediction_coding(int w, int h, int m, const uint32_t *index, const float *data,
+                                        uint64_t data_size, const uint8_t *table, uint8_t *out)
+{
+    auto mi = make_mi(w, h, m, index, data, data_size, nullptr, 1, 0, nullptr, nullptr, nullptr);
+    std::vector<Byte> t(table, table + m);
+    auto bytes = moment_quantization::quantize_prediction_coding(mi, t);
+    if (out)
+        std::memcpy(out, bytes.data(), bytes.size());
+    return bytes.size();
+}
+
+/* ---- MESE primitives (mese/MESE_dynamic.h) ---- */
+void ref_trig_to_exp(int n, const float *trig, float *exp_out)
+{
+    trigonometricToExponentialMoments(n, reinterpret_cast<float_complex *>(exp_out), trig);
+}
+void ref_exp_to_trig(int n, const float *exp_in, float *trig_out)
+{
+    exponentialToTrigonometricMoments(n, reinterpret_cast<float_complex *>(trig_out),
+                                      const_cast<float_complex *>(reinterpret_cast<const float_complex *>(exp_in)));
+}
+void ref_levinson(int n, const float *col, float *sol)
+{
+    std::vector<float_complex> tmp(n);
+    levinsonsAlgorithm(n, reinterpret_cast<float_complex *>(sol), const_cast<float_complex *>(reinterpret_cast<const float_complex *>(col)),
+                       tmp.data());
+}
+void ref_prepare_lagrange(int n, const float *trig, float *out)
+{
+    std::vector<float_complex> a(n), b(n), c(n);
+    prepareMESELagrange(n, out, trig, a.data(), b.data(), c.data());
+}
+float ref_evaluate_mese(int n, float phase, const float *lagrange) { return evaluateMESELagrange(n, phase, lagrange); }
+float ref_fast_atan(float x) { return fast_atan(x); }
+void ref_autocorrelation(int n, const float *sig, float *out)
+{
+    computeAutocorrelation(n, reinterpret_cast<float_complex *>(out), const_cast<float_complex *>(reinterpret_cast<const float_complex *>(sig)));
+}
+void ref_correlation(int n, const float *lhs, const float *rhs, float *out)
+{
+    computeCorrelation(n, reinterpret_cast<float_complex *>(out), const_cast<float_complex *>(reinterpret_cast<const float_complex *>(lhs)),
+                       const_cast<float_complex *>(reinterpret_cast<const float_complex *>(rhs)));
+}
+void ref_imaginary_correlation(int n, const float *lhs, const float *rhs, float *out)
+{
+    computeImaginaryCorrelation(n, out, const_cast<float_complex *>(reinterpret_cast<const float_complex *>(lhs)),
+                                const_cast<float_complex *>(reinterpret_cast<const float_complex *>(rhs)));
+}
+void ref_encode(int n, const float *exp_in, float *code)
+{
+    std::vector<float_complex> poly(n), tmp(n);
+    encode(n, const_cast<float_complex *>(reinterpret_cast<const float_complex *>(exp_in)), reinterpret_cast<float_complex *>(code), poly.data(),
+           tmp.data());
+}
+void ref_decode(int n, const float *code, float *exp_out, float *poly)
+{
+    std::vector<float_complex> tmp(n);
+    decode(n, const_cast<float_complex *>(reinterpret_cast<const float_complex *>(code)), reinterpret_cast<float_complex *>(exp_out),
+           reinterpret_cast<float_complex *>(poly), tmp.data());
+}
+void ref_transform_quantization_real(int n, const float *code, float c0, float *out)
+{
+    transform_quantization_real(n, const_cast<float_complex *>(reinterpret_cast<const float_complex *>(code)), c0, out);
+}
+void ref_transform_dequantization_real(int n, const float *in, float *code, int warp, const float *params)
+{
+    transform_dequantization_real(n, in, reinterpret_cast<float_complex *>(code), WarpParameters{warp, params});
+}
+int ref_determine_best_number_moments(int n, const float *moments, float thr)
+{
+    std::vector<float_complex> a(n), b(n), c(n);
+    return determine_best_number_moments(n, moments, thr, a.data(), b.data(), c.data());
+}
+void ref_evaluate_unknown_moments(int n, const float *exp_in, int max_moments, float *new_exp)
+{
+    std::vector<float_complex> lev(max_moments);
+    evaluate_unknown_moments(n, const_cast<float_complex *>(reinterpret_cast<const float_complex *>(exp_in)), max_moments,
+                             reinterpret_cast<float_complex *>(new_exp), lev.data());
+}
+void ref_exponential_to_bounded_moments(int n, const float *exp_in, float *bounded, int known)
+{
+    exponential_to_bounded_moments(n, const_cast<float_complex *>(reinterpret_cast<const float_complex *>(exp_in)),
+                                   reinterpret_cast<float_complex *>(bounded), known);
+}
+float ref_rmse(int n, int m, const float *pred, const float *target)
+{
+    return rmse(n, m, const_cast<float_complex *>(reinterpret_cast<const float_complex *>(pred)), target);
+}
+
+/* ---- the independent fixed-size MESE code (mese/MESE_4_10.h) used by the reference's tests ---- */
+void ref_fixed_prepare_lagrange(int n, const float *trig, float *out)
+{
+    if (n == 4)
+        prepareReflectanceSpectrumLagrange4(out, trig);
+    else
+        prepareReflectanceSpectrumLagrange10(out, trig);
+}
+float ref_fixed_evaluate_lagrange(int n, float phase, const float *lagrange)
+{
+    return n == 4 ? evaluateReflectanceSpectrumLagrange4(phase, lagrange)
+                  : evaluateReflectanceSpectrumLagrange10(phase, lagrange);
+}
+void ref_fixed_trig_to_exp(int n, const float *trig, float *exp_out)
+{
+    if (n == 4)
+        trigonometricToExponentialMoments4(reinterpret_cast<float_complex *>(exp_out), trig);
+    else
+        trigonometricToExponentialMoments10(reinterpret_cast<float_complex *>(exp_out), trig);
+}
+void ref_fixed_levinson(int n, const float *col, float *sol)
+{
+    if (n == 4)
+        levinsonsAlgorithm4(reinterpret_cast<float_complex *>(sol), const_cast<float_complex *>(reinterpret_cast<const float_complex *>(col)));
+    else
+        levinsonsAlgorithm10(reinterpret_cast<float_complex *>(sol), const_cast<float_complex *>(reinterpret_cast<const float_complex *>(col)));
+}
+
+/* ---- helpers and overload probes ---- */
+void ref_euler_exp(float x, float *out)
+{
+    auto e = euler_exp(x);
+    out[0] = e.x;
+    out[1] = e.y;
+}
+float ref_exp_overload(float x)
+{
+    using namespace cut;
+    return exp(-x);
+}
+float ref_grid_sample(const float *vol, int nx, int ny, int nz, const float *dmin, const float *dmax, const float *p)
+{
+    RegularGrid grid(Vec3i(nx, ny, nz), to_range(dmin, dmax), std::vector<float>(vol, vol + size_t(nx) * ny * nz),
+                     RegularGrid::DataType::F32);
+    return grid.sample(Vec3f(p[0], p[1], p[2]));
+}
+int ref_eye_ray(const mraygb_camera *c, int x, int y, int w, int h, const float *dmin, const float *dmax,
+                float *out /* origin[3], dir[3], t_near, t_far */)
+{
+    auto cam = to_camera(c);
+    Vec2f ndc(x / static_cast<float>(w) * 2.f - 1.f, y / static_cast<float>(h) * 2.f - 1.f);
+    auto ray = cut::get_eye_ray(cam, ndc);
+    float tn, tf;
+    int hit = cut::intersect_AABB(ray, Vec3f(dmin[0], dmin[1], dmin[2]), Vec3f(dmax[0], dmax[1], dmax[2]), tn, tf);
+    out[0] = ray.origin.x;
+    out[1] = ray.origin.y;
+    out[2] = ray.origin.z;
+    out[3] = ray.dir.x;
+    out[4] = ray.dir.y;
+    out[5] = ray.dir.z;
+    out[6] = tn;
+    out[7] = tf;
+    return hit;
+}
+/* read_from_disk's table (transfer_function.cpp:46-97) from 256 RGBA floats; writes row 0 and returns 1 when
+ * every row equals row 0. */
+int ref_preintegrate(const float *tf1d, float step, float *row_out)
+{
+    array<Vec4f, TransferFunction::RESOLUTION> t;
+    for (int i = 0; i < 256; ++i)
+        t[i] = Vec4f(tf1d[4 * i], tf1d[4 * i + 1], tf1d[4 * i + 2], tf1d[4 * i + 3]);
+    auto tf = std::make_unique<TransferFunction>(preintegrate(t, step));
+    for (int x = 0; x < 256; ++x)
+    {
+        auto v = tf->data[x];
+        row_out[4 * x] = v.x;
+        row_out[4 * x + 1] = v.y;
+        row_out[4 * x + 2] = v.z;
+        row_out[4 * x + 3] = v.w;
+    }
+    int same = 1;
+    for (int y = 1; y < 256 && same; ++y)
+        for (int x = 0; x < 256; ++x)
+        {
+            Vec4f a = tf->data[y * 256 + x];
+            Vec4f b = tf->data[x];
+            if (a.x != b.x || a.y != b.y || a.z != b.z || a.w != b.w)
+            {
+                same = 0;
+                break;
+            }
+        }
+    return same;
+}
+float ref_tf_sample(const float *row, float fs, float bs, float *out)
+{
+    auto tf = std::make_unique<TransferFunction>(make_tf(row));
+    auto v = tf->sample(fs, bs);
+    out[0] = v.x;
+    out[1] = v.y;
+    out[2] = v.z;
+    out[3] = v.w;
+    return v.w;
+}
+
+} // extern "C"
