@@ -1,0 +1,452 @@
+"""Benchmark of the moment-image hot path: generate (moments + compaction) -> MESE preparation -> reconstruct.
+
+Default workload (the precision form): a 512^3 float32 mixing-layer grid (64 seeded Fourier modes, 5 % seeded
+noise), a 1024 x 1024 perspective view, 0.5-voxel steps, 64 trigonometric moments, Kahan-compensated FP32 moment
+sums and FP64 MESE preparation.  A step is one full pass over the image with the volume resident in HBM:
+    generate_grid_kernel -> scan / compaction -> prepare_kernel (FP64) -> reconstruct_kernel
+and the metric is million rays (pixels) per second of that pass.
+
+The JSON line also carries:
+  e2e           the same pass through the drop-in host API (mraygb_generate / mraygb_reconstruct): the volume is
+                uploaded from pinned host memory, the moment image comes back to the host and goes back up, the
+                RGBA comes back -- every copy inside the timed region;
+  plain_fp32    the same pass in the reference's plain FP32 arithmetic;
+  roofline      the dominant kernel (generate) against the measured HBM copy bandwidth (compulsory bytes), with
+                its FP32 issue rate beside it (the binding roof of this method);
+  cpu_baseline  the reference's CPU method (the oracle's FP32 restatement, OpenMP on all host cores) timed on a
+                row-strided sample of the same workload.
+
+--impl reference runs only the CPU reference method on bounded samples of the workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "Mrays/s moment gen+MESE recon (fwd, fwd+adjoint) vs plain FP32 at ≤1e-4 err"
+UNIT = "Mrays/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--size", type=int, default=512, help="volume edge (voxels)")
+    ap.add_argument("--image", type=int, default=1024, help="image edge (pixels)")
+    ap.add_argument("--moments", type=int, default=64)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU-baseline sample time")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload(args):
+    from mray_gb300 import workloads as W
+
+    return W.mixing_layer_workload(n=args.size, width=args.image, height=args.image, num_moments=args.moments,
+                                   modes=64, seed=21,
+                                   name=f"mixing_layer{args.size}^3_{args.image}x{args.image}_m{args.moments}_persp")
+
+
+def samples_per_ray(wl) -> np.ndarray:
+    """Samples of each ray (first, regular steps while t + step < t_far, last at t_far), counted from the per-ray
+    box intersection with the reference's float formulas."""
+    W, H = wl.width, wl.height
+    cam = wl.camera
+    x = np.arange(W, dtype=np.float32)[None, :]
+    y = np.arange(H, dtype=np.float32)[:, None]
+    nx = (x / np.float32(W)) * np.float32(2) - np.float32(1)
+    ny = (y / np.float32(H)) * np.float32(2) - np.float32(1)
+    nx, ny = np.broadcast_arrays(nx, ny)
+    m = np.array([[cam.transform[i][j] for j in range(4)] for i in range(4)], dtype=np.float32)
+    if cam.orthographic:
+        o = [np.float32(cam.position[i]) + nx * np.float32(cam.right[i]) + ny * np.float32(cam.up[i])
+             for i in range(3)]
+        d = [np.full_like(nx, np.float32(cam.dir[i])) for i in range(3)]
+    else:
+        xs = nx * np.float32(cam.aspect) * np.float32(cam.scale)
+        ys = ny * np.float32(cam.scale)
+        v = [m[i, 0] * xs + m[i, 1] * ys + m[i, 2] * np.float32(-1) for i in range(3)]
+        inv = np.float32(1) / np.sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2])
+        o = [np.full_like(nx, np.float32(cam.position[i])) for i in range(3)]
+        d = [v[i] * inv for i in range(3)]
+    with np.errstate(divide="ignore", invalid="ignore"):
+        tmin, tmax = [], []
+        for i in range(3):
+            inv = np.float32(1) / d[i]
+            tb = inv * (np.float32(wl.domain_min[i]) - o[i])
+            tt = inv * (np.float32(wl.domain_max[i]) - o[i])
+            tmin.append(np.minimum(tt, tb))
+            tmax.append(np.maximum(tt, tb))
+        tn = np.maximum(np.maximum(tmin[0], tmin[1]), tmin[2])
+        tf = np.minimum(np.minimum(tmax[0], tmax[1]), tmax[2])
+    tn = np.maximum(tn, np.float32(cam.znear))
+    hit = (tf > tn) & (tf > 0)
+    s = np.where(hit, np.ceil((tf - tn) / np.float32(wl.gen.step_size)) + 1, 0)
+    return s.astype(np.int64)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.dev}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------------------------------------------------
+# CPU reference method (the oracle's FP32 restatement of the reference's CPU path)
+# ------------------------------------------------------------------------------------------------------------
+
+def cpu_reference_sample(wl, row_step: int, row_offset: int = 0, nthreads: int = 0):
+    """generate (per-pixel moments + counts) + prepare + reconstruct on rows y = row_offset (mod row_step), with
+    the reference's CPU arithmetic.  Returns (rays, seconds)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    W, H, m = wl.width, wl.height, wl.num_moments
+    rows = (row_offset, H, row_step)
+    tf = O.preintegrate(wl.tf1d, wl.tf_step)
+    t0 = time.perf_counter()
+    mo, b, c = O.generate_moments(wl.camera, wl.gen, wl.volume, wl.domain_min, wl.domain_max, W, H, m, "f32",
+                                  nthreads=nthreads, rows=rows)
+    idx, data = O.compact(c, mo)
+    pm = O.prepare_moments(W, H, m, idx, data, bias=wl.rec.bias, precision="f32", nthreads=nthreads, rows=rows)
+    O.reconstruct(wl.camera, wl.rec, W, H, m, wl.domain_min, wl.domain_max, idx, pm, b, tf, "f32",
+                  nthreads=nthreads, rows=rows)
+    dt = time.perf_counter() - t0
+    rays = len(range(row_offset, H, row_step)) * W
+    return rays, dt
+
+
+def cpu_baseline(wl, target_s: float):
+    ncores = os.cpu_count() or 1
+    # calibrate on a sparse sample, then size the sample to the target time
+    probe_step = max(1, wl.height // 8)
+    rays, dt = cpu_reference_sample(wl, probe_step, 1)
+    rate = rays / max(dt, 1e-9)
+    want_rays = rate * target_s
+    step = int(max(1, min(wl.height, round(wl.width * wl.height / max(want_rays, 1.0)))))
+    rays, dt = cpu_reference_sample(wl, step, 0)
+    return {"value": rays / dt / 1e6, "unit": UNIT, "cores": ncores, "kind": "port",
+            "sample": f"rows y = 0 mod {step} of the {wl.width}x{wl.height} image ({rays} rays, {dt:.1f} s): "
+                      f"per-pixel generate + prepare + reconstruct in the reference's FP32 arithmetic "
+                      f"(oracle/mray_oracle.c, OpenMP {ncores} threads)"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    wl = workload(args)
+    ncores = os.cpu_count() or 1
+    # each step: a bounded row sample (every 128th row at the default size), rows rotating between steps
+    step_rows = max(1, wl.height // 8)
+    for i in range(args.warmup):
+        cpu_reference_sample(wl, step_rows, i % step_rows)
+    times, rays_total = [], 0
+    for i in range(args.steps):
+        rays, dt = cpu_reference_sample(wl, step_rows, (args.warmup + i) % step_rows)
+        times.append(dt)
+        rays_total += rays
+    total = sum(times)
+    value = rays_total / total / 1e6
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": wl.name, "volume": f"{args.size}^3 float32 mixing layer", "image":
+                       f"{wl.width}x{wl.height}", "num_moments": wl.num_moments, "step": "0.5 voxel",
+                       "sample_per_step": f"every {step_rows}th row ({wl.width * len(range(0, wl.height, step_rows))} rays)"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": ncores, "kind": "port",
+                             "sample": f"every {step_rows}th row per step, rows rotating; the reference's CPU "
+                                       f"method in its FP32 arithmetic (oracle/mray_oracle.c), OpenMP {ncores} threads"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------------------------------------------------
+# GPU path
+# ------------------------------------------------------------------------------------------------------------
+
+def read_profile_traffic():
+    """DRAM bytes per launch of generate_grid_kernel at the default workload, from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "generate_grid_kernel_mixing512_1024sq_m64.md")
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.strip().startswith("traffic_bytes_per_launch:"):
+                    return float(line.split(":", 1)[1].strip().split()[0])
+    except OSError:
+        pass
+    return None
+
+
+def run_ours(args):
+    import torch
+
+    import mray_gb300 as M
+
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+
+    wl = workload(args)
+    W, H, m = wl.width, wl.height, wl.num_moments
+    P = W * H
+    ctx = M.Context(local, precision=M.PRECISION_COMPENSATED_FP64_MESE)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    vol = torch.from_numpy(wl.volume).cuda()
+    ctx.upload_grid(vol, wl.domain_min, wl.domain_max)
+    tf = M.preintegrate(wl.tf1d, wl.tf_step)
+    ctx.upload_tf(tf.table)
+    torch.cuda.synchronize()
+
+    d_mo = torch.empty(P * m, dtype=torch.float32, device="cuda")
+    d_b = torch.empty(2 * P, dtype=torch.int16, device="cuda")
+    d_c = torch.empty(P, dtype=torch.int32, device="cuda")
+    d_idx = torch.empty(P + 1, dtype=torch.int32, device="cuda")
+    d_cm = torch.empty(P * m, dtype=torch.float32, device="cuda")
+    d_pm = torch.empty(P * m, dtype=torch.float32, device="cuda")
+    d_rgba = torch.empty(P * 4, dtype=torch.float32, device="cuda")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # 256 MiB > 129 MB L2
+
+    def step(ev=None):
+        if ev is not None:
+            ev[0].record(stream)
+        ctx.stage_generate_moments(wl.camera, wl.gen, W, H, m, d_mo, d_b, d_c)
+        if ev is not None:
+            ev[1].record(stream)
+        ctx.stage_compact(W, H, m, d_c, d_mo, d_idx, d_cm)
+        ctx.stage_prepare_moments(W, H, m, d_idx, d_cm, d_pm, bias=wl.rec.bias)
+        ctx.stage_reconstruct(wl.camera, wl.rec, W, H, m, wl.domain_min, wl.domain_max, d_idx, d_pm, d_b, d_rgba)
+        if ev is not None:
+            ev[2].record(stream)
+
+    def timed_loop(precision):
+        ctx.precision = precision
+        for _ in range(args.warmup):
+            step()
+        ctx.synchronize()
+        evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        launches0 = ctx.kernel_launches
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(float(i))  # evict the previous step's lines from L2 (outside the timed events)
+            step(evs[i])
+        ctx.synchronize()
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        launches = ctx.kernel_launches - launches0
+        step_ms = [e[0].elapsed_time(e[2]) for e in evs]
+        gen_ms = [e[0].elapsed_time(e[1]) for e in evs]
+        return sum(step_ms), statistics.mean(gen_ms), launches, wall
+
+    # plain FP32 form first (reported beside the headline), then the precision form under the clock sampler
+    plain_ms, _, _, _ = timed_loop(M.PRECISION_FP32)
+    sampler = ClockSampler(local)
+    sampler.start()
+    total_ms, gen_ms, launches, wall = timed_loop(M.PRECISION_COMPENSATED_FP64_MESE)
+    clocks = sampler.stop()
+
+    t_max = total_ms
+    plain_max = plain_ms
+    if dist:
+        t = torch.tensor([total_ms, plain_ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max, plain_max = float(t[0]), float(t[1])
+    value = world * P * args.steps / (t_max * 1e-3) / 1e6
+    plain_value = world * P * args.steps / (plain_max * 1e-3) / 1e6
+
+    # roofline of the dominant kernel (generate): compulsory bytes and method FLOPs per launch
+    spr = samples_per_ray(wl)
+    total_samples = int(spr.sum())
+    vol_bytes = wl.volume.size * 4
+    gen_bytes = vol_bytes + P * (m * 4 + 4 + 4)
+    gen_flops = total_samples * (4 * (m - 1) + 24)
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    hbm_peak = peaks.get("hbm_gbs")
+    peak_src = "measured"
+    if hbm_peak is None:
+        hbm_peak, peak_src = 6800.0, "fallback"
+    achieved = gen_bytes / (gen_ms * 1e-3) / 1e9
+    fp32_peak = 152 * 128 * 2 * (clocks.get("sm_max_mhz") or 2070.0) * 1e6 / 1e12
+    fp32_achieved = gen_flops / (gen_ms * 1e-3) / 1e12
+    traffic = read_profile_traffic()
+    roofline = {"bound": "hbm", "kernel": "generate_grid_kernel<16,true>", "achieved": achieved, "peak": hbm_peak,
+                "unit": "GB/s", "frac": achieved / hbm_peak, "peak_source": peak_src, "traffic": traffic,
+                "algorithmic_bytes_per_launch": gen_bytes, "kernel_ms": gen_ms,
+                "fp32": {"achieved_tflops": fp32_achieved, "peak_tflops": fp32_peak,
+                         "frac": fp32_achieved / fp32_peak, "flops_per_launch": gen_flops,
+                         "samples_per_launch": total_samples,
+                         "note": "method FLOPs 4(m-1)+24 per sample (FMA = 2) against the nominal FP32 issue rate "
+                                 "152 SMs x 128 lanes x 2 at the max SM clock; the binding roof of this method"}}
+
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(args, ctx, wl, dist)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(wl, args.cpu_seconds)
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+                "config": {"workload": wl.name, "volume": f"{args.size}^3 float32 mixing layer (64 modes, 5% noise)",
+                           "image": f"{W}x{H} perspective", "num_moments": m, "step": "0.5 voxel",
+                           "precision": "Kahan-compensated FP32 moment sums, FP64 MESE preparation",
+                           "l2": "256 MiB buffer written between timed steps (volume 512 MiB > L2)",
+                           "parallelism": "replicas" if world > 1 else "single GPU"},
+                "plain_fp32": {"value": plain_value, "unit": UNIT, "ms_per_step": plain_max / args.steps},
+                "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
+                "wall_s_timed": wall}
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def run_e2e(args, ctx, wl, dist):
+    """The drop-in host API with pinned host buffers; every copy is inside the timed region."""
+    import torch
+
+    import mray_gb300 as M
+
+    W, H, m = wl.width, wl.height, wl.num_moments
+    P = W * H
+    vol_h = torch.from_numpy(wl.volume).pin_memory()
+    vol_np = vol_h.numpy()
+    mi = M.MomentImageHost(W, H, m, True, True)
+    mi.data = torch.empty(P * m, dtype=torch.float32).pin_memory().numpy()
+    mi.index = torch.empty(P + 1, dtype=torch.int32).pin_memory().numpy().view(np.uint32)
+    mi.bounds = torch.empty(2 * P, dtype=torch.int16).pin_memory().numpy().view(np.uint16).reshape(P, 2)
+    img = M.ColorImageHost(W, H)
+    img.rgba_float = torch.empty(P * 4, dtype=torch.float32).pin_memory().numpy().reshape(H, W, 4)
+    img.rgba = torch.empty(P * 4, dtype=torch.uint8).pin_memory().numpy().reshape(H, W, 4)
+    grid = M.RegularGrid(vol_np, wl.domain_min, wl.domain_max)
+    tf = M.preintegrate(wl.tf1d, wl.tf_step)
+    data_full = mi.data
+
+    def one():
+        mi.data = data_full
+        M.generate(wl.camera, grid, mi, wl.gen, context=ctx)
+        M.reconstruct(wl.camera, mi, tf, img, wl.rec, context=ctx)
+
+    for _ in range(max(1, args.warmup)):
+        one()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        one()
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([dt], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dt = float(t[0])
+    world = dist.get_world_size() if dist else 1
+    moments_bytes = mi.data.size * 4
+    h2d = wl.volume.size * 4 + 256 * 16 + moments_bytes + (P + 1) * 4 + 4 * P
+    d2h = moments_bytes + (P + 1) * 4 + 4 * P + P * 16 + P * 4 + 4
+    return {"value": world * P * args.steps / dt / 1e6, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+            "d2h_bytes_per_step": int(d2h),
+            "path": "mraygb_upload_grid + mraygb_generate + mraygb_upload_tf + mraygb_reconstruct on pinned host "
+                    "buffers (the drop-in seam of generate_device / reconstruct_device)"}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,154 @@
+/*
+ * mraygb — GB300-native (sm_103a) moment-image generation, prediction coding / quantization and
+ * bounded-MESE reconstruction: the data-parallel hot path of TobiasRp/mray behind a C ABI.
+ *
+ * Two layers:
+ *
+ *  1. The drop-in host API (mraygb_generate / mraygb_reconstruct) takes and returns HOST buffers, with the
+ *     shapes of the reference's CUDA seam:
+ *        void generate_device(cut::Camera, const RegularGrid &, MomentImageHost &, const GenerationParameters &);
+ *        void generate_device(cut::Camera, const Particles &, MomentImageHost &, const GenerationParameters &);
+ *        void reconstruct_device(cut::Camera, const MomentImageHost &, const TransferFunction &,
+ *                                ColorImageHost &, const ReconstructionParameters &);
+ *     (src/moment_raymarcher.cuh:48-54, dispatched from src/moment_raymarcher.cpp:168-183 and 329-337).
+ *     The volume and transfer function stay resident in the context between calls.
+ *
+ *  2. The stage API (mraygb_stage_*) runs one step of the path on DEVICE pointers, ordered on the context's
+ *     stream, with no host synchronisation unless a size has to come back to the host.
+ *
+ * Every entry point returns an mraygb_status; on failure mraygb_last_error() describes it.  Nothing aborts
+ * the process (the reference terminates on CUDA errors, src/cut/cuda_common.cpp:32-53).  A context may be
+ * used by one host thread at a time; independent contexts are independent.
+ *
+ * No CUDA or torch types appear in these signatures: streams are passed as void* (a cudaStream_t).
+ */
+#ifndef MRAYGB_H
+#define MRAYGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "mraygb_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct mraygb_context mraygb_context;
+
+typedef enum mraygb_status
+{
+    MRAYGB_OK = 0,
+    MRAYGB_INVALID_ARGUMENT = 1,
+    MRAYGB_OUT_OF_MEMORY = 2,
+    MRAYGB_CUDA_ERROR = 3,
+    MRAYGB_DEVICE_TIMEOUT = 4,
+    MRAYGB_NUMERICAL = 5,
+    MRAYGB_NOT_SUPPORTED = 6,
+    MRAYGB_NO_VOLUME = 7
+} mraygb_status;
+
+/* Arithmetic forms of the path. */
+typedef enum mraygb_precision
+{
+    /* the reference's method in FP32 (moment sums in plain FP32, FP32 Levinson / MESE preparation) */
+    MRAYGB_PRECISION_FP32 = 0,
+    /* FP32 ray marching with compensated (Kahan) moment sums; MESE preparation (Levinson recursion,
+     * Toeplitz / Herglotz correlations) in FP64 */
+    MRAYGB_PRECISION_COMPENSATED_FP64_MESE = 1
+} mraygb_precision;
+
+/* Largest moment count (the reference's file format stores counts in 8 bits: src/main.cpp:288-293). */
+#define MRAYGB_MAX_MOMENTS 255
+
+/* ---- context -------------------------------------------------------------------------------------------- */
+
+/* Creates a context on CUDA device `device` with its own non-blocking stream. */
+int mraygb_create(int device, mraygb_context **out);
+void mraygb_destroy(mraygb_context *ctx);
+/* The last error message of this context ("" when none). */
+const char *mraygb_last_error(const mraygb_context *ctx);
+/* Orders all later work of this context on `stream` (a cudaStream_t; NULL restores the context's own). */
+int mraygb_set_stream(mraygb_context *ctx, void *stream);
+void *mraygb_get_stream(const mraygb_context *ctx);
+int mraygb_synchronize(mraygb_context *ctx);
+/* Selects the arithmetic form (mraygb_precision) for later generate / prepare calls. */
+int mraygb_set_precision(mraygb_context *ctx, int precision);
+/* Number of this library's kernels launched by the context so far. */
+uint64_t mraygb_kernel_launches(const mraygb_context *ctx);
+
+/* ---- resident inputs ------------------------------------------------------------------------------------ */
+
+/* A regular grid (RegularGrid, src/volume.h:31-123): float32, x fastest, z slowest, on the box [dmin, dmax].
+ * `data` is a host pointer, or a device pointer when data_on_device != 0 (then it is copied, not adopted).
+ * Replaces the per-call upload of RegularGridDevice (src/volume_device.cuh:52-97). */
+int mraygb_upload_grid(mraygb_context *ctx, const float *data, int nx, int ny, int nz, const float dmin[3],
+                       const float dmax[3], int data_on_device);
+
+/* The transfer-function table that reconstruction samples: 256 RGBA float entries of one row of
+ * TransferFunction::data (src/transfer_function.h:30-60).  read_from_disk / preintegrate build tables whose
+ * 256 rows are all equal (src/transfer_function.cpp:46-97), so one row is the whole table. */
+int mraygb_upload_tf(mraygb_context *ctx, const float *table_rgba256);
+
+/* ---- drop-in host API ----------------------------------------------------------------------------------- */
+
+/* generate_device(cam, RegularGrid, MomentImageHost, GenerationParameters) over the uploaded grid.
+ *   h_data         : capacity for W*H*m floats; receives the (compact, prediction-coded) moment data
+ *   h_index        : W*H+1 u32 when gp->compact_image, else may be NULL      (MomentImageHost::index)
+ *   h_bounds       : 2*W*H u16 (lower, upper) when gp->transform_to_bounds   (MomentImageHost::bounds)
+ *   h_coding_params: 2*(m-1) u16 when prediction coded with the default warp (MomentImageHost::coding_params)
+ *   h_data_size    : receives the number of floats written to h_data
+ * The moment image's remaining flags follow from gp: is_compact = compact_image, prediction_code =
+ * prediction_coding, coding_warp = coding_warp, domain = the grid's box. */
+int mraygb_generate(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_generation_params *gp, int width,
+                    int height, int num_moments, float *h_data, uint32_t *h_index, uint16_t *h_bounds,
+                    uint16_t *h_coding_params, uint64_t *h_data_size);
+
+/* reconstruct_device(cam, MomentImageHost, TransferFunction, ColorImageHost, ReconstructionParameters) with
+ * the uploaded transfer function.  The moment image is given by its members (h_index NULL = not compact,
+ * h_bounds NULL = no bounds, h_coding_params NULL unless prediction coded with the default warp).
+ *   h_rgba  : W*H*4 floats (the colour before the u8 store), or NULL
+ *   h_rgba8 : W*H*4 bytes as ColorImageHost stores them (clamp + truncate, src/color_image.h:41-47), or NULL */
+int mraygb_reconstruct(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_reconstruction_params *rp,
+                       int width, int height, int num_moments, const float domain_min[3], const float domain_max[3],
+                       const uint32_t *h_index, const float *h_data, uint64_t data_size, const uint16_t *h_bounds,
+                       int prediction_code, int coding_warp, const uint16_t *h_coding_params, float *h_rgba,
+                       uint8_t *h_rgba8);
+
+/* ---- stage API: device pointers, ordered on the context stream ------------------------------------------ */
+
+/* Per-ray moments over the uploaded grid (generate_ray, src/raymarch_generate.h:69-148, driven as
+ * generate_moments_kernel, src/moment_raymarcher.cu:163-185).
+ *   d_moments: W*H*m floats (non-compact layout; missed rays get zeros)
+ *   d_bounds : 2*W*H u16, written when gp->transform_to_bounds (may be NULL otherwise)
+ *   d_counts : W*H u32 moment counts for compaction (compute_num_moments, src/moment_compaction.h:147-174),
+ *              written when gp->compact_image (may be NULL otherwise). */
+int mraygb_stage_generate_moments(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_generation_params *gp,
+                                  int width, int height, int num_moments, float *d_moments, uint16_t *d_bounds,
+                                  uint32_t *d_counts);
+
+/* MomentImageDevice::compact (src/moment_image_device.cu:83-110): exclusive scan of the counts into
+ * d_index[W*H+1] and copy of the moments into the compact buffer (capacity floats).  *h_total receives the
+ * compact size (one device->host read of 4 bytes). */
+int mraygb_stage_compact(mraygb_context *ctx, int width, int height, int num_moments, const uint32_t *d_counts,
+                         const float *d_moments, uint32_t *d_index, float *d_compact, uint64_t capacity,
+                         uint64_t *h_total);
+
+/* Lagrange multipliers per pixel (prepare_moments_device, src/moment_image_device.cu:306-335): the moment data
+ * in the compact layout (d_index) or, with d_index NULL, the W*H*m layout; output in the same layout. */
+int mraygb_stage_prepare_moments(mraygb_context *ctx, int width, int height, int num_moments, const uint32_t *d_index,
+                                 const float *d_data, int prediction_code, int coding_warp,
+                                 const uint16_t *d_coding_params, float bias, float *d_pmoments);
+
+/* MESE re-march per pixel (reconstruct_moments_kernel, src/moment_raymarcher.cu:339-384) with the uploaded
+ * transfer function; d_rgba: W*H*4 floats; d_rgba8: W*H*4 bytes or NULL. */
+int mraygb_stage_reconstruct(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_reconstruction_params *rp,
+                             int width, int height, int num_moments, const float domain_min[3],
+                             const float domain_max[3], const uint32_t *d_index, const float *d_pmoments,
+                             const uint16_t *d_bounds, float *d_rgba, uint8_t *d_rgba8);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MRAYGB_H */

@@ -1,0 +1,19 @@
+"""mray_gb300: the moment-image hot path of TobiasRp/mray (moment generation, compaction, prediction coding and
+quantization, bounded-MESE reconstruction) as hand-written sm_103a CUDA behind a C ABI (include/mraygb.h).
+
+The Python layer mirrors the reference's raymarcher API (generate / reconstruct and the moment-image, colour-image,
+grid and transfer-function containers) and calls the C ABI through ctypes.
+"""
+from .types import (CODING_WARP_DEFAULT_TRANSFORMED, CODING_WARP_NONE, Camera, GenerationParameters,
+                    ReconstructionParameters)
+from .raymarcher import (MAX_MOMENTS, PRECISION_COMPENSATED_FP64_MESE, PRECISION_FP32, ColorImageHost, Context,
+                         MomentImageHost, RegularGrid, TransferFunction, default_context, generate, preintegrate,
+                         reconstruct)
+from ._lib import MrayError
+
+__all__ = [
+    "Camera", "GenerationParameters", "ReconstructionParameters", "CODING_WARP_DEFAULT_TRANSFORMED",
+    "CODING_WARP_NONE", "ColorImageHost", "Context", "MomentImageHost", "RegularGrid", "TransferFunction",
+    "default_context", "generate", "preintegrate", "reconstruct", "MrayError", "PRECISION_FP32",
+    "PRECISION_COMPENSATED_FP64_MESE", "MAX_MOMENTS",
+]

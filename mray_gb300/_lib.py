@@ -1,0 +1,88 @@
+"""Loads ``libmraygb.so`` (the CUDA library behind ``include/mraygb.h``) and declares its C ABI for ctypes.
+
+There is no fallback: if the library cannot be built or loaded, every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+from .types import Camera, GenerationParameters, ReconstructionParameters
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libmraygb.so")
+
+STATUS = {0: "OK", 1: "INVALID_ARGUMENT", 2: "OUT_OF_MEMORY", 3: "CUDA_ERROR", 4: "DEVICE_TIMEOUT", 5: "NUMERICAL",
+          6: "NOT_SUPPORTED", 7: "NO_VOLUME"}
+
+# every symbol include/mraygb.h declares
+EXPORTS = [
+    "mraygb_create", "mraygb_destroy", "mraygb_last_error", "mraygb_set_stream", "mraygb_get_stream",
+    "mraygb_synchronize", "mraygb_set_precision", "mraygb_kernel_launches", "mraygb_upload_grid", "mraygb_upload_tf",
+    "mraygb_generate", "mraygb_reconstruct", "mraygb_stage_generate_moments", "mraygb_stage_compact",
+    "mraygb_stage_prepare_moments", "mraygb_stage_reconstruct",
+]
+
+_lock = threading.Lock()
+_lib = None
+
+
+class MrayError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS.get(status, status)}: {message}")
+        self.status = status
+
+
+def _declare(L):
+    P = C.POINTER
+    vp = C.c_void_p
+    i = C.c_int
+    L.mraygb_create.argtypes = [i, P(vp)]
+    L.mraygb_destroy.argtypes = [vp]
+    L.mraygb_destroy.restype = None
+    L.mraygb_last_error.argtypes = [vp]
+    L.mraygb_last_error.restype = C.c_char_p
+    L.mraygb_set_stream.argtypes = [vp, vp]
+    L.mraygb_get_stream.argtypes = [vp]
+    L.mraygb_get_stream.restype = vp
+    L.mraygb_synchronize.argtypes = [vp]
+    L.mraygb_set_precision.argtypes = [vp, i]
+    L.mraygb_kernel_launches.argtypes = [vp]
+    L.mraygb_kernel_launches.restype = C.c_uint64
+    L.mraygb_upload_grid.argtypes = [vp, vp, i, i, i, C.c_float * 3, C.c_float * 3, i]
+    L.mraygb_upload_tf.argtypes = [vp, vp]
+    L.mraygb_generate.argtypes = [vp, P(Camera), P(GenerationParameters), i, i, i, vp, vp, vp, vp,
+                                  P(C.c_uint64)]
+    L.mraygb_reconstruct.argtypes = [vp, P(Camera), P(ReconstructionParameters), i, i, i, C.c_float * 3,
+                                     C.c_float * 3, vp, vp, C.c_uint64, vp, i, i, vp, vp, vp]
+    L.mraygb_stage_generate_moments.argtypes = [vp, P(Camera), P(GenerationParameters), i, i, i, vp, vp, vp]
+    L.mraygb_stage_compact.argtypes = [vp, i, i, i, vp, vp, vp, vp, C.c_uint64, P(C.c_uint64)]
+    L.mraygb_stage_prepare_moments.argtypes = [vp, i, i, i, vp, vp, i, i, vp, C.c_float, vp]
+    L.mraygb_stage_reconstruct.argtypes = [vp, P(Camera), P(ReconstructionParameters), i, i, i, C.c_float * 3,
+                                           C.c_float * 3, vp, vp, vp, vp, vp]
+    special = ("mraygb_destroy", "mraygb_last_error", "mraygb_get_stream", "mraygb_kernel_launches")
+    for name in EXPORTS:
+        if name not in special:
+            getattr(L, name).restype = C.c_int
+
+
+def load(build_if_missing: bool = True):
+    """The loaded library; builds it in-tree first when it is missing (nvcc required)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                if not build_if_missing:
+                    raise OSError(f"{LIB_PATH} is missing; run mray_gb300.build.build()")
+                from . import build as _build
+                _build.build()
+            _lib = C.CDLL(LIB_PATH)
+            _declare(_lib)
+        return _lib
+
+
+def check(ctx_handle, status: int) -> None:
+    if status != 0:
+        msg = load().mraygb_last_error(ctx_handle)
+        raise MrayError(status, msg.decode() if msg else "")

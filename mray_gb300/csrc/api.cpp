@@ -1,0 +1,593 @@
+// The C ABI (include/mraygb.h): contexts, resident inputs, the stage API and the drop-in host API.
+//
+// Host code only: argument checks, device buffers owned by the context, launches in stream order and the
+// copies of the drop-in calls.  Every failure is reported through the return code and mraygb_last_error;
+// nothing here aborts.
+
+#include "../../include/mraygb.h"
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include <cuda_runtime.h>
+
+#include "device_common.cuh"
+#include "internal.h"
+
+using namespace mraygb;
+
+namespace
+{
+
+struct DeviceBuffer
+{
+    void *ptr = nullptr;
+    size_t bytes = 0;
+
+    cudaError_t reserve(size_t n)
+    {
+        if (n <= bytes)
+            return cudaSuccess;
+        if (ptr)
+            cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+        cudaError_t e = cudaMalloc(&ptr, n);
+        if (e == cudaSuccess)
+            bytes = n;
+        return e;
+    }
+    void release()
+    {
+        if (ptr)
+            cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+    }
+    template <typename T> T *as() const { return static_cast<T *>(ptr); }
+};
+
+} // namespace
+
+struct mraygb_context
+{
+    int device = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    int precision = MRAYGB_PRECISION_FP32;
+    std::string error;
+    uint64_t launches = 0;
+
+    // resident inputs
+    DeviceBuffer grid;
+    int nx = 0, ny = 0, nz = 0;
+    float dmin[3] = {0, 0, 0}, dmax[3] = {0, 0, 0};
+    bool has_grid = false;
+    DeviceBuffer tf;
+    bool has_tf = false;
+
+    // work buffers of the drop-in calls and of the scan
+    DeviceBuffer moments, counts, index, compact, bounds, coding_params, pmoments, rgba, rgba8, scan_scratch;
+    DeviceBuffer error_flag;
+};
+
+namespace
+{
+
+int fail(mraygb_context *ctx, int code, const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (ctx)
+        ctx->error = buf;
+    return code;
+}
+
+int cuda_fail(mraygb_context *ctx, cudaError_t e, const char *what)
+{
+    cudaGetLastError(); // clear a sticky launch error where possible
+    return fail(ctx, e == cudaErrorMemoryAllocation ? MRAYGB_OUT_OF_MEMORY : MRAYGB_CUDA_ERROR, "%s: %s (%s)", what,
+                cudaGetErrorString(e), cudaGetErrorName(e));
+}
+
+#define CK(expr, what)                                                                                              \
+    do                                                                                                              \
+    {                                                                                                               \
+        cudaError_t e_ = (expr);                                                                                    \
+        if (e_ != cudaSuccess)                                                                                      \
+            return cuda_fail(ctx, e_, what);                                                                        \
+    } while (0)
+
+#define CHECK_CTX()                                                                                                 \
+    do                                                                                                              \
+    {                                                                                                               \
+        if (!ctx)                                                                                                   \
+            return MRAYGB_INVALID_ARGUMENT;                                                                         \
+        ctx->error.clear();                                                                                         \
+        cudaError_t e_ = cudaSetDevice(ctx->device);                                                                \
+        if (e_ != cudaSuccess)                                                                                      \
+            return cuda_fail(ctx, e_, "cudaSetDevice");                                                             \
+    } while (0)
+
+int check_image(mraygb_context *ctx, int width, int height, int m)
+{
+    if (width <= 0 || height <= 0 || width > 65535 || height > 65535)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "image size %dx%d outside 1..65535", width, height);
+    if (m < 1 || m > MRAYGB_MAX_MOMENTS)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "num_moments %d outside 1..%d", m, MRAYGB_MAX_MOMENTS);
+    if ((uint64_t)width * (uint64_t)height * (uint64_t)m >= (1ull << 32))
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "W*H*m = %llu exceeds the u32 moment index",
+                    (unsigned long long)width * height * m);
+    return MRAYGB_OK;
+}
+
+GridView grid_view(const mraygb_context *ctx)
+{
+    GridView g;
+    g.data = ctx->grid.as<float>();
+    g.nx = ctx->nx;
+    g.ny = ctx->ny;
+    g.nz = ctx->nz;
+    for (int i = 0; i < 3; ++i)
+    {
+        g.dmin[i] = ctx->dmin[i];
+        g.dmax[i] = ctx->dmax[i];
+        g.ext[i] = ctx->dmax[i] - ctx->dmin[i];
+    }
+    return g;
+}
+
+int check_device_error_flag(mraygb_context *ctx)
+{
+    int flag = 0;
+    CK(cudaMemcpyAsync(&flag, ctx->error_flag.ptr, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream),
+       "reading the device error flag");
+    CK(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+    if (flag)
+    {
+        CK(cudaMemsetAsync(ctx->error_flag.ptr, 0, sizeof(int), ctx->stream), "clearing the device error flag");
+        return fail(ctx, MRAYGB_NUMERICAL,
+                    "a ray exceeded its step bound: the step size is too small to advance t in float");
+    }
+    return MRAYGB_OK;
+}
+
+int validate_gen(mraygb_context *ctx, const mraygb_generation_params *gp)
+{
+    if (!gp)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "generation parameters are NULL");
+    if (!(gp->step_size > 0.f))
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "step_size must be > 0 (got %g)", (double)gp->step_size);
+    if (gp->prediction_coding && !gp->compact_image)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "prediction_coding requires compact_image");
+    if (gp->coding_warp != MRAYGB_CODING_WARP_DEFAULT_TRANSFORMED && gp->coding_warp != MRAYGB_CODING_WARP_NONE)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "unknown coding_warp %d", gp->coding_warp);
+    return MRAYGB_OK;
+}
+
+int run_generate_moments(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_generation_params *gp,
+                         int width, int height, int m, float *d_moments, uint16_t *d_bounds, uint32_t *d_counts)
+{
+    const DeviceCamera dc = to_device_camera(*cam);
+    CK(launch_generate_grid(grid_view(ctx), dc, *gp, width, height, m,
+                            ctx->precision == MRAYGB_PRECISION_COMPENSATED_FP64_MESE, d_moments, d_bounds, d_counts,
+                            ctx->error_flag.as<int>(), ctx->stream),
+       "generate kernel launch");
+    ctx->launches += 1;
+    if (gp->compact_image && d_counts && gp->error_threshold != 0.f)
+    {
+        CK(launch_count_moments(width * height, m, gp->error_threshold, d_moments, d_counts, ctx->stream),
+           "moment count kernel launch");
+        ctx->launches += 1;
+    }
+    return MRAYGB_OK;
+}
+
+int run_compact(mraygb_context *ctx, int width, int height, int m, const uint32_t *d_counts, const float *d_moments,
+                uint32_t *d_index, float *d_compact, uint64_t capacity, uint64_t *h_total)
+{
+    const size_t P = (size_t)width * (size_t)height;
+    const size_t words = scan_scratch_words(P);
+    CK(ctx->scan_scratch.reserve((words + 1) * sizeof(uint32_t)), "scan scratch allocation");
+    int launches = 0;
+    CK(launch_exclusive_scan(d_counts, d_index, P, ctx->scan_scratch.as<uint32_t>(), ctx->stream, &launches),
+       "scan launch");
+    ctx->launches += (uint64_t)launches;
+    uint32_t total = 0;
+    CK(cudaMemcpyAsync(&total, d_index + P, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream),
+       "reading the compact size");
+    CK(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+    if ((uint64_t)total > capacity)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "compact buffer holds %llu floats, %u needed",
+                    (unsigned long long)capacity, total);
+    CK(launch_compact_copy(width * height, m, d_counts, d_index, d_moments, d_compact, ctx->stream),
+       "compaction copy launch");
+    ctx->launches += 1;
+    if (h_total)
+        *h_total = total;
+    return MRAYGB_OK;
+}
+
+int run_prepare(mraygb_context *ctx, int width, int height, int m, const uint32_t *d_index, const float *d_data,
+                int prediction_code, int coding_warp, const uint16_t *d_coding_params, float bias, float *d_out)
+{
+    CK(launch_prepare(width * height, m, d_index, d_data, prediction_code, coding_warp, d_coding_params, bias,
+                      ctx->precision == MRAYGB_PRECISION_COMPENSATED_FP64_MESE, d_out, ctx->stream),
+       "prepare kernel launch");
+    ctx->launches += 1;
+    return MRAYGB_OK;
+}
+
+int run_reconstruct(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_reconstruction_params *rp, int width,
+                    int height, int m, const float dmin[3], const float dmax[3], const uint32_t *d_index,
+                    const float *d_pm, const uint16_t *d_bounds, float *d_rgba, uint8_t *d_rgba8)
+{
+    const DeviceCamera dc = to_device_camera(*cam);
+    ReconArgs a;
+    a.cam = &dc;
+    a.width = width;
+    a.height = height;
+    a.m = m;
+    for (int i = 0; i < 3; ++i)
+    {
+        a.dmin[i] = dmin[i];
+        a.dmax[i] = dmax[i];
+    }
+    a.index = d_index;
+    a.pmoments = d_pm;
+    a.bounds = d_bounds;
+    a.tf = ctx->tf.as<float4>();
+    a.step = rp->step_size;
+    a.emission = rp->medium_emission;
+    a.ert = rp->early_ray_termination;
+    a.rgba = d_rgba;
+    a.rgba8 = d_rgba8;
+    CK(launch_reconstruct(a, ctx->error_flag.as<int>(), ctx->stream), "reconstruct kernel launch");
+    ctx->launches += 1;
+    return MRAYGB_OK;
+}
+
+int validate_rec(mraygb_context *ctx, const mraygb_reconstruction_params *rp)
+{
+    if (!rp)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "reconstruction parameters are NULL");
+    if (!(rp->step_size > 0.f))
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "step_size must be > 0 (got %g)", (double)rp->step_size);
+    if (rp->use_truncated_fourier)
+        return fail(ctx, MRAYGB_NOT_SUPPORTED, "truncated Fourier reconstruction is not part of this path");
+    if (rp->ss_enable)
+        return fail(ctx, MRAYGB_NOT_SUPPORTED, "single scattering is not part of this path");
+    if (!ctx->has_tf)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "no transfer function uploaded");
+    return MRAYGB_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+int mraygb_create(int device, mraygb_context **out)
+{
+    if (!out)
+        return MRAYGB_INVALID_ARGUMENT;
+    *out = nullptr;
+    mraygb_context *ctx = new (std::nothrow) mraygb_context();
+    if (!ctx)
+        return MRAYGB_OUT_OF_MEMORY;
+    ctx->device = device;
+    int rc = MRAYGB_OK;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess)
+        e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess)
+        e = mese_init_constants();
+    if (e == cudaSuccess)
+        e = ctx->error_flag.reserve(sizeof(int));
+    if (e == cudaSuccess)
+        e = cudaMemset(ctx->error_flag.ptr, 0, sizeof(int));
+    if (e != cudaSuccess)
+    {
+        rc = e == cudaErrorMemoryAllocation ? MRAYGB_OUT_OF_MEMORY : MRAYGB_CUDA_ERROR;
+        mraygb_destroy(ctx);
+        return rc;
+    }
+    ctx->stream = ctx->own_stream;
+    *out = ctx;
+    return MRAYGB_OK;
+}
+
+void mraygb_destroy(mraygb_context *ctx)
+{
+    if (!ctx)
+        return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream)
+        cudaStreamSynchronize(ctx->stream);
+    DeviceBuffer *bufs[] = {&ctx->grid,    &ctx->tf,       &ctx->moments,       &ctx->counts,
+                            &ctx->index,   &ctx->compact,  &ctx->bounds,        &ctx->coding_params,
+                            &ctx->pmoments, &ctx->rgba,    &ctx->rgba8,         &ctx->scan_scratch,
+                            &ctx->error_flag};
+    for (DeviceBuffer *b : bufs)
+        b->release();
+    if (ctx->own_stream)
+        cudaStreamDestroy(ctx->own_stream);
+    delete ctx;
+}
+
+const char *mraygb_last_error(const mraygb_context *ctx) { return ctx ? ctx->error.c_str() : "null context"; }
+
+int mraygb_set_stream(mraygb_context *ctx, void *stream)
+{
+    CHECK_CTX();
+    ctx->stream = stream ? static_cast<cudaStream_t>(stream) : ctx->own_stream;
+    return MRAYGB_OK;
+}
+
+void *mraygb_get_stream(const mraygb_context *ctx) { return ctx ? static_cast<void *>(ctx->stream) : nullptr; }
+
+int mraygb_synchronize(mraygb_context *ctx)
+{
+    CHECK_CTX();
+    CK(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+    return check_device_error_flag(ctx);
+}
+
+int mraygb_set_precision(mraygb_context *ctx, int precision)
+{
+    CHECK_CTX();
+    if (precision != MRAYGB_PRECISION_FP32 && precision != MRAYGB_PRECISION_COMPENSATED_FP64_MESE)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "unknown precision form %d", precision);
+    ctx->precision = precision;
+    return MRAYGB_OK;
+}
+
+uint64_t mraygb_kernel_launches(const mraygb_context *ctx) { return ctx ? ctx->launches : 0; }
+
+int mraygb_upload_grid(mraygb_context *ctx, const float *data, int nx, int ny, int nz, const float dmin[3],
+                       const float dmax[3], int data_on_device)
+{
+    CHECK_CTX();
+    if (!data || !dmin || !dmax || nx <= 0 || ny <= 0 || nz <= 0)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "invalid grid (%p, %d x %d x %d)", (const void *)data, nx, ny, nz);
+    if ((uint64_t)nx * (uint64_t)ny >= (1ull << 31))
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "grid slices of %d x %d exceed the reference's int indexing", nx, ny);
+    for (int i = 0; i < 3; ++i)
+        if (!(dmax[i] > dmin[i]))
+            return fail(ctx, MRAYGB_INVALID_ARGUMENT, "empty domain along axis %d", i);
+    const size_t bytes = (size_t)nx * ny * nz * sizeof(float);
+    CK(ctx->grid.reserve(bytes), "grid allocation");
+    CK(cudaMemcpyAsync(ctx->grid.ptr, data, bytes, data_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                       ctx->stream),
+       "grid upload");
+    ctx->nx = nx;
+    ctx->ny = ny;
+    ctx->nz = nz;
+    for (int i = 0; i < 3; ++i)
+    {
+        ctx->dmin[i] = dmin[i];
+        ctx->dmax[i] = dmax[i];
+    }
+    ctx->has_grid = true;
+    if (!data_on_device)
+        CK(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+    return MRAYGB_OK;
+}
+
+int mraygb_upload_tf(mraygb_context *ctx, const float *table)
+{
+    CHECK_CTX();
+    if (!table)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "transfer function table is NULL");
+    CK(ctx->tf.reserve(256 * 4 * sizeof(float)), "transfer function allocation");
+    CK(cudaMemcpyAsync(ctx->tf.ptr, table, 256 * 4 * sizeof(float), cudaMemcpyHostToDevice, ctx->stream),
+       "transfer function upload");
+    CK(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+    ctx->has_tf = true;
+    return MRAYGB_OK;
+}
+
+// ---- stage API ------------------------------------------------------------------------------------------------
+
+int mraygb_stage_generate_moments(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_generation_params *gp,
+                                  int width, int height, int m, float *d_moments, uint16_t *d_bounds,
+                                  uint32_t *d_counts)
+{
+    CHECK_CTX();
+    int rc = check_image(ctx, width, height, m);
+    if (rc)
+        return rc;
+    if ((rc = validate_gen(ctx, gp)))
+        return rc;
+    if (!cam || !d_moments)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "camera or moment buffer is NULL");
+    if (!ctx->has_grid)
+        return fail(ctx, MRAYGB_NO_VOLUME, "no volume uploaded");
+    if (gp->compact_image && !d_counts)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "compact_image needs a count buffer");
+    if (gp->transform_to_bounds && !d_bounds)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "transform_to_bounds needs a bounds buffer");
+    return run_generate_moments(ctx, cam, gp, width, height, m, d_moments, d_bounds, d_counts);
+}
+
+int mraygb_stage_compact(mraygb_context *ctx, int width, int height, int m, const uint32_t *d_counts,
+                         const float *d_moments, uint32_t *d_index, float *d_compact, uint64_t capacity,
+                         uint64_t *h_total)
+{
+    CHECK_CTX();
+    int rc = check_image(ctx, width, height, m);
+    if (rc)
+        return rc;
+    if (!d_counts || !d_moments || !d_index || !d_compact)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "NULL buffer");
+    return run_compact(ctx, width, height, m, d_counts, d_moments, d_index, d_compact, capacity, h_total);
+}
+
+int mraygb_stage_prepare_moments(mraygb_context *ctx, int width, int height, int m, const uint32_t *d_index,
+                                 const float *d_data, int prediction_code, int coding_warp,
+                                 const uint16_t *d_coding_params, float bias, float *d_pmoments)
+{
+    CHECK_CTX();
+    int rc = check_image(ctx, width, height, m);
+    if (rc)
+        return rc;
+    if (!d_data || !d_pmoments)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "NULL buffer");
+    if (prediction_code && coding_warp == MRAYGB_CODING_WARP_DEFAULT_TRANSFORMED && !d_coding_params)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "prediction-coded moments need their coding parameters");
+    return run_prepare(ctx, width, height, m, d_index, d_data, prediction_code, coding_warp, d_coding_params, bias,
+                       d_pmoments);
+}
+
+int mraygb_stage_reconstruct(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_reconstruction_params *rp,
+                             int width, int height, int m, const float domain_min[3], const float domain_max[3],
+                             const uint32_t *d_index, const float *d_pmoments, const uint16_t *d_bounds, float *d_rgba,
+                             uint8_t *d_rgba8)
+{
+    CHECK_CTX();
+    int rc = check_image(ctx, width, height, m);
+    if (rc)
+        return rc;
+    if ((rc = validate_rec(ctx, rp)))
+        return rc;
+    if (!cam || !d_pmoments || !domain_min || !domain_max || (!d_rgba && !d_rgba8))
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "NULL argument");
+    return run_reconstruct(ctx, cam, rp, width, height, m, domain_min, domain_max, d_index, d_pmoments, d_bounds,
+                           d_rgba, d_rgba8);
+}
+
+// ---- drop-in host API -------------------------------------------------------------------------------------------
+
+int mraygb_generate(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_generation_params *gp, int width,
+                    int height, int m, float *h_data, uint32_t *h_index, uint16_t *h_bounds, uint16_t *h_coding_params,
+                    uint64_t *h_data_size)
+{
+    CHECK_CTX();
+    int rc = check_image(ctx, width, height, m);
+    if (rc)
+        return rc;
+    if ((rc = validate_gen(ctx, gp)))
+        return rc;
+    if (!cam || !h_data || !h_data_size)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "camera, data or size pointer is NULL");
+    if (gp->compact_image && !h_index)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "compact_image needs an index buffer");
+    if (gp->transform_to_bounds && !h_bounds)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "transform_to_bounds needs a bounds buffer");
+    if (!ctx->has_grid)
+        return fail(ctx, MRAYGB_NO_VOLUME, "no volume uploaded");
+    if (gp->prediction_coding)
+        return fail(ctx, MRAYGB_NOT_SUPPORTED, "prediction coding is not available in this build");
+
+    const size_t P = (size_t)width * (size_t)height;
+    const size_t N = P * (size_t)m;
+    CK(ctx->moments.reserve(N * sizeof(float)), "moment buffer allocation");
+    CK(ctx->counts.reserve(P * sizeof(uint32_t)), "count buffer allocation");
+    CK(ctx->bounds.reserve(2 * P * sizeof(uint16_t)), "bounds buffer allocation");
+    rc = run_generate_moments(ctx, cam, gp, width, height, m, ctx->moments.as<float>(), ctx->bounds.as<uint16_t>(),
+                              ctx->counts.as<uint32_t>());
+    if (rc)
+        return rc;
+    const float *d_out = ctx->moments.as<float>();
+    uint64_t size = N;
+    if (gp->compact_image)
+    {
+        CK(ctx->index.reserve((P + 1) * sizeof(uint32_t)), "index buffer allocation");
+        CK(ctx->compact.reserve(N * sizeof(float)), "compact buffer allocation");
+        rc = run_compact(ctx, width, height, m, ctx->counts.as<uint32_t>(), ctx->moments.as<float>(),
+                         ctx->index.as<uint32_t>(), ctx->compact.as<float>(), N, &size);
+        if (rc)
+            return rc;
+        d_out = ctx->compact.as<float>();
+        CK(cudaMemcpyAsync(h_index, ctx->index.ptr, (P + 1) * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream),
+           "index download");
+    }
+    if (size)
+        CK(cudaMemcpyAsync(h_data, d_out, size * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream),
+           "moment download");
+    if (gp->transform_to_bounds)
+        CK(cudaMemcpyAsync(h_bounds, ctx->bounds.ptr, 2 * P * sizeof(uint16_t), cudaMemcpyDeviceToHost, ctx->stream),
+           "bounds download");
+    (void)h_coding_params;
+    CK(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+    *h_data_size = size;
+    return check_device_error_flag(ctx);
+}
+
+int mraygb_reconstruct(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_reconstruction_params *rp,
+                       int width, int height, int m, const float domain_min[3], const float domain_max[3],
+                       const uint32_t *h_index, const float *h_data, uint64_t data_size, const uint16_t *h_bounds,
+                       int prediction_code, int coding_warp, const uint16_t *h_coding_params, float *h_rgba,
+                       uint8_t *h_rgba8)
+{
+    CHECK_CTX();
+    int rc = check_image(ctx, width, height, m);
+    if (rc)
+        return rc;
+    if ((rc = validate_rec(ctx, rp)))
+        return rc;
+    if (!cam || !h_data || !domain_min || !domain_max || (!h_rgba && !h_rgba8))
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "NULL argument");
+    const size_t P = (size_t)width * (size_t)height;
+    if (!h_index && data_size < P * (size_t)m)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "a non-compact image needs W*H*m floats");
+    if (prediction_code && coding_warp == MRAYGB_CODING_WARP_DEFAULT_TRANSFORMED && !h_coding_params)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "prediction-coded moments need their coding parameters");
+
+    const size_t nd = data_size ? data_size : 1;
+    CK(ctx->compact.reserve(nd * sizeof(float)), "moment buffer allocation");
+    CK(ctx->pmoments.reserve(nd * sizeof(float)), "multiplier buffer allocation");
+    CK(ctx->rgba.reserve(P * 4 * sizeof(float)), "colour buffer allocation");
+    if (h_rgba8)
+        CK(ctx->rgba8.reserve(P * 4), "u8 colour buffer allocation");
+    if (data_size)
+        CK(cudaMemcpyAsync(ctx->compact.ptr, h_data, data_size * sizeof(float), cudaMemcpyHostToDevice, ctx->stream),
+           "moment upload");
+    const uint32_t *d_index = nullptr;
+    if (h_index)
+    {
+        CK(ctx->index.reserve((P + 1) * sizeof(uint32_t)), "index buffer allocation");
+        CK(cudaMemcpyAsync(ctx->index.ptr, h_index, (P + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->stream),
+           "index upload");
+        d_index = ctx->index.as<uint32_t>();
+    }
+    const uint16_t *d_bounds = nullptr;
+    if (h_bounds)
+    {
+        CK(ctx->bounds.reserve(2 * P * sizeof(uint16_t)), "bounds buffer allocation");
+        CK(cudaMemcpyAsync(ctx->bounds.ptr, h_bounds, 2 * P * sizeof(uint16_t), cudaMemcpyHostToDevice, ctx->stream),
+           "bounds upload");
+        d_bounds = ctx->bounds.as<uint16_t>();
+    }
+    const uint16_t *d_cp = nullptr;
+    if (prediction_code && coding_warp == MRAYGB_CODING_WARP_DEFAULT_TRANSFORMED)
+    {
+        CK(ctx->coding_params.reserve(2 * (size_t)m * sizeof(uint16_t)), "coding parameter allocation");
+        CK(cudaMemcpyAsync(ctx->coding_params.ptr, h_coding_params, 2 * (size_t)(m - 1) * sizeof(uint16_t),
+                           cudaMemcpyHostToDevice, ctx->stream),
+           "coding parameter upload");
+        d_cp = ctx->coding_params.as<uint16_t>();
+    }
+    rc = run_prepare(ctx, width, height, m, d_index, ctx->compact.as<float>(), prediction_code, coding_warp, d_cp,
+                     rp->bias, ctx->pmoments.as<float>());
+    if (rc)
+        return rc;
+    rc = run_reconstruct(ctx, cam, rp, width, height, m, domain_min, domain_max, d_index, ctx->pmoments.as<float>(),
+                         d_bounds, ctx->rgba.as<float>(), h_rgba8 ? ctx->rgba8.as<uint8_t>() : nullptr);
+    if (rc)
+        return rc;
+    if (h_rgba)
+        CK(cudaMemcpyAsync(h_rgba, ctx->rgba.ptr, P * 4 * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream),
+           "colour download");
+    if (h_rgba8)
+        CK(cudaMemcpyAsync(h_rgba8, ctx->rgba8.ptr, P * 4, cudaMemcpyDeviceToHost, ctx->stream), "u8 colour download");
+    CK(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+    return check_device_error_flag(ctx);
+}
+
+} // extern "C"

@@ -1,0 +1,426 @@
+// Moment generation over a regular grid: one ray per 4-lane quad, moments split across the quad's lanes.
+//
+// Method (src/raymarch_generate.h:35-148).  A ray is marched from t_near in steps of `step` while
+// t + step < t_far (t accumulated in float exactly as the reference does), with one last sample at t_far.
+// Between consecutive samples the density is linear in the phase p in [-pi, 0], and the reference adds the
+// closed-form integral of that linear piece times e^{-ijp} to moment j (update_moments).  Over a segment
+// [p_m - h, p_m + h] with end values f0, f1 that integral is, exactly,
+//
+//     (f0 + f1) * alpha_j(h) * cos(j p_m)  -  (f1 - f0) * beta_j(h) * sin(j p_m)
+//     alpha_j(h) = sin(j h) / j,   beta_j(h) = (sin(j h) - j h cos(j h)) / (j^2 h)   (alpha_0 = h, beta_0 = 0)
+//
+// All regular segments share h = phase_step / 2, so a ray needs only the two sums
+//     C_j = sum_k (f_{k-1} + f_k) Re(z_k^j),   D_j = sum_k (f_k - f_{k-1}) Im(z_k^j),   z_k = e^{-i p_m,k}
+// and m_j = alpha_j C_j + beta_j D_j + (last segment, computed directly).  This is the reference's integral
+// regrouped; it avoids the reference's difference of two O(S/j^2) terms per step and needs one sincos per
+// segment instead of 2(m-1).
+//
+// Layout: a warp holds 8 rays (quads).  Per round the 4 lanes of a quad each march one sample (the four
+// consecutive t values are computed by every lane with the reference's sequential float adds), exchange
+// (f_{k-1}+f_k, f_k-f_{k-1}, z_k) with shuffles, and each lane accumulates the moments j = q + 4i it owns:
+// z_k^q z_k^{4i} by complex rotation, so no moment is more than 16 rotations from a fresh sincos.
+//
+// Two arithmetic forms: plain FP32 sums, or per-round partial sums added with Kahan compensation
+// (MRAYGB_PRECISION_COMPENSATED_FP64_MESE).
+
+#include "device_common.cuh"
+#include "internal.h"
+
+namespace mraygb
+{
+
+namespace
+{
+
+constexpr unsigned kFull = 0xffffffffu;
+
+struct GenArgs
+{
+    GridView grid;
+    DeviceCamera cam;
+    int width, height, m;
+    float step;
+    float data_min, data_max;
+    float bound_eps;
+    int transform_to_bounds;
+    int compact_image;
+    int error_threshold_zero;
+    float *moments;
+    uint16_t *bounds;
+    uint32_t *counts;
+    int *error_flag;
+};
+
+// alpha_j(h) = sin(jh)/j and beta_j(h) = (sin(jh) - jh cos(jh)) / (j^2 h); beta by its series for small jh
+__device__ __forceinline__ void seg_coeffs(int j, float h, float &alpha, float &beta)
+{
+    if (j == 0)
+    {
+        alpha = h;
+        beta = 0.f;
+        return;
+    }
+    const float x = (float)j * h;
+    float s, c;
+    sincosf(x, &s, &c);
+    alpha = s / (float)j;
+    float num;
+    if (fabsf(x) < 0.5f)
+    {
+        // sin x - x cos x = x^3/3 - x^5/30 + x^7/840 - x^9/45360 + x^11/3991680 - ...
+        const float x2 = x * x;
+        float poly = 1.f / 3991680.f;
+        poly = fmaf(poly, -x2, 1.f / 45360.f);
+        poly = fmaf(poly, -x2, 1.f / 840.f);
+        poly = fmaf(poly, -x2, 1.f / 30.f);
+        poly = fmaf(poly, -x2, 1.f / 3.f);
+        num = poly * x2 * x;
+    }
+    else
+    {
+        num = s - x * c;
+    }
+    beta = num / ((float)j * x);
+}
+
+template <int NJ, bool KAHAN>
+__global__ void __launch_bounds__(128) generate_grid_kernel(const GenArgs a)
+{
+    const int lane = threadIdx.x & 31;
+    const int q = lane & 3;
+    const int qbase = lane & ~3;
+    const int px = blockIdx.x * 8 + (lane >> 2);
+    const int py = blockIdx.y * 4 + (threadIdx.x >> 5);
+    const bool in_image = (px < a.width) && (py < a.height);
+    const size_t pix = in_image ? (size_t)py * (size_t)a.width + (size_t)px : 0;
+
+    float o[3], d[3];
+    float t_near = 0.f, t_far = 0.f;
+    bool hit = false;
+    if (in_image)
+    {
+        float nx, ny;
+        pixel_ndc(px, py, a.width, a.height, nx, ny);
+        eye_ray(a.cam, nx, ny, o, d);
+        const float bmin[3] = {a.grid.dmin[0], a.grid.dmin[1], a.grid.dmin[2]};
+        const float bmax[3] = {a.grid.dmax[0], a.grid.dmax[1], a.grid.dmax[2]};
+        hit = intersect_aabb(o, d, bmin, bmax, t_near, t_far);
+        t_near = rmax(t_near, a.cam.znear);
+        hit = hit && (t_far > 0.f);
+    }
+
+    float C[NJ], Dc[NJ], Ck[NJ], Dk[NJ];
+#pragma unroll
+    for (int i = 0; i < NJ; ++i)
+    {
+        C[i] = 0.f;
+        Dc[i] = 0.f;
+        Ck[i] = 0.f;
+        Dk[i] = 0.f;
+    }
+
+    float blo = 1.f, bhi = 0.f;
+    float pti = 0.f, pss = 0.f;
+    float f_tail = 0.f;
+    float p_tail = -kPiF;
+    float t = t_near;
+    const float step = a.step;
+    if (hit)
+    {
+        pti = (float)(3.141592653589793 / (double)__fsub_rn(t_far, t_near));
+        pss = (float)(3.141592653589793 * (double)__fdiv_rn(step, __fsub_rn(t_far, t_near)));
+        const float f0 = map_density(grid_sample(a.grid, __fadd_rn(o[0], __fmul_rn(t, d[0])),
+                                                 __fadd_rn(o[1], __fmul_rn(t, d[1])),
+                                                 __fadd_rn(o[2], __fmul_rn(t, d[2]))),
+                                     a.data_min, a.data_max);
+        blo = rmin(blo, f0);
+        bhi = rmax(bhi, f0);
+        f_tail = f0;
+    }
+    const float half_pss = 0.5f * pss;
+    // A ray ends by itself after about (t_far - t_near) / step samples; the cap only guards a step too small to
+    // advance t in float (the reference would loop forever there).
+    int cap = 0;
+    if (hit)
+    {
+        const float est = __fsub_rn(t_far, t_near) / step;
+        cap = (est < 1.6e9f ? (int)(1.25f * est) : 2000000000) + 64;
+    }
+    int marched = 0;
+
+    bool active = hit;
+    while (__any_sync(kFull, active))
+    {
+        // the next four t values, each taken only while t + step < t_far (raymarch_generate.h:90-95)
+        float tt = t, my_t = 0.f;
+        int nv = 0;
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+        {
+            const float tn = __fadd_rn(tt, step);
+            if (active && nv == i && tn < t_far)
+            {
+                nv = i + 1;
+                tt = tn;
+                if (q == i)
+                    my_t = tn;
+            }
+        }
+        const bool my_valid = q < nv;
+        float f_my = 0.f, p_my = 0.f;
+        if (my_valid)
+        {
+            p_my = sub_pi(__fmul_rn(__fsub_rn(my_t, t_near), pti));
+            f_my = map_density(grid_sample(a.grid, __fadd_rn(o[0], __fmul_rn(my_t, d[0])),
+                                           __fadd_rn(o[1], __fmul_rn(my_t, d[1])),
+                                           __fadd_rn(o[2], __fmul_rn(my_t, d[2]))),
+                               a.data_min, a.data_max);
+            blo = rmin(blo, f_my);
+            bhi = rmax(bhi, f_my);
+        }
+        float f_left = __shfl_up_sync(kFull, f_my, 1);
+        if (q == 0)
+            f_left = f_tail;
+        float S = 0.f, D = 0.f;
+        cf z = {1.f, 0.f};
+        if (my_valid)
+        {
+            S = f_left + f_my;
+            D = f_my - f_left;
+            float sn, cs;
+            sincosf(p_my - half_pss, &sn, &cs);
+            z = {cs, -sn};
+        }
+
+        float Ss[4], Ds[4];
+        cf w[4], v[4];
+#pragma unroll
+        for (int s = 0; s < 4; ++s)
+        {
+            Ss[s] = __shfl_sync(kFull, S, qbase + s);
+            Ds[s] = __shfl_sync(kFull, D, qbase + s);
+            cf zs;
+            zs.x = __shfl_sync(kFull, z.x, qbase + s);
+            zs.y = __shfl_sync(kFull, z.y, qbase + s);
+            const cf z2 = csq(zs);
+            const cf z3 = cmul(z2, zs);
+            v[s] = csq(z2);
+            cf u = {1.f, 0.f};
+            u = (q == 1) ? zs : u;
+            u = (q == 2) ? z2 : u;
+            u = (q == 3) ? z3 : u;
+            w[s] = u;
+        }
+
+#pragma unroll
+        for (int i = 0; i < NJ; ++i)
+        {
+            if (KAHAN)
+            {
+                float pc = Ss[0] * w[0].x;
+                float pd = Ds[0] * w[0].y;
+#pragma unroll
+                for (int s = 1; s < 4; ++s)
+                {
+                    pc = fmaf(Ss[s], w[s].x, pc);
+                    pd = fmaf(Ds[s], w[s].y, pd);
+                }
+                kahan_add(C[i], Ck[i], pc);
+                kahan_add(Dc[i], Dk[i], pd);
+            }
+            else
+            {
+#pragma unroll
+                for (int s = 0; s < 4; ++s)
+                {
+                    C[i] = fmaf(Ss[s], w[s].x, C[i]);
+                    Dc[i] = fmaf(Ds[s], w[s].y, Dc[i]);
+                }
+            }
+            if (i + 1 < NJ)
+            {
+#pragma unroll
+                for (int s = 0; s < 4; ++s)
+                    w[s] = cmul(w[s], v[s]);
+            }
+        }
+
+        // the last valid sample of this round becomes the left end of the next segment
+        const int src = qbase + (nv > 0 ? nv - 1 : 0);
+        const float f_last = __shfl_sync(kFull, f_my, src);
+        const float p_last = __shfl_sync(kFull, p_my, src);
+        if (nv > 0)
+        {
+            f_tail = f_last;
+            p_tail = p_last;
+            t = tt;
+        }
+        if (nv < 4)
+            active = false;
+        marched += nv;
+        if (active && marched > cap)
+        {
+            active = false;
+            if (q == 0)
+                atomicExch(a.error_flag, 1);
+        }
+    }
+
+    // last sample exactly at t_far (raymarch_generate.h:107-113)
+    float f_far = 0.f;
+    if (hit)
+    {
+        f_far = map_density(grid_sample(a.grid, __fadd_rn(o[0], __fmul_rn(t_far, d[0])),
+                                        __fadd_rn(o[1], __fmul_rn(t_far, d[1])),
+                                        __fadd_rn(o[2], __fmul_rn(t_far, d[2]))),
+                            a.data_min, a.data_max);
+        blo = rmin(blo, f_far);
+        bhi = rmax(bhi, f_far);
+    }
+    // bounds over the quad (every lane of the warp takes part in the shuffles)
+    blo = rmin(blo, __shfl_xor_sync(kFull, blo, 1));
+    bhi = rmax(bhi, __shfl_xor_sync(kFull, bhi, 1));
+    blo = rmin(blo, __shfl_xor_sync(kFull, blo, 2));
+    bhi = rmax(bhi, __shfl_xor_sync(kFull, bhi, 2));
+
+    if (!in_image)
+        return;
+
+    float *out = a.moments + pix * (size_t)a.m;
+    if (!hit)
+    {
+        // missed ray: zero moments, bound (0, 0), no moments kept by compaction
+        for (int j = q; j < a.m; j += 4)
+            out[j] = 0.f;
+        if (q == 0)
+        {
+            if (a.bounds && a.transform_to_bounds)
+            {
+                a.bounds[2 * pix] = 0;
+                a.bounds[2 * pix + 1] = 0;
+            }
+            if (a.counts && a.compact_image)
+                a.counts[pix] = 0;
+        }
+        return;
+    }
+
+    const float sL = f_tail + f_far;
+    const float dL = f_far - f_tail;
+    const float hL = -0.5f * p_tail;
+    float snL, csL;
+    sincosf(0.5f * p_tail, &snL, &csL);
+    const cf zL = {csL, -snL};
+    const cf zL2 = csq(zL);
+    const cf vL = csq(zL2);
+    cf wL = {1.f, 0.f};
+    wL = (q == 1) ? zL : wL;
+    wL = (q == 2) ? zL2 : wL;
+    wL = (q == 3) ? cmul(zL2, zL) : wL;
+
+    float lo = blo, hi = bhi;
+    double inv = 1.0;
+    if (a.transform_to_bounds)
+    {
+        lo = rmax(__fsub_rn(blo, a.bound_eps), 0.f);
+        hi = rmin(__fadd_rn(bhi, a.bound_eps), 1.f);
+        inv = 1.0 / (double)__fsub_rn(hi, lo);
+    }
+
+    const float h = half_pss;
+    float m0 = 0.f;
+#pragma unroll
+    for (int i = 0; i < NJ; ++i)
+    {
+        const int j = q + 4 * i;
+        if (j < a.m)
+        {
+            float al, be, alL, beL;
+            seg_coeffs(j, h, al, be);
+            seg_coeffs(j, hL, alL, beL);
+            const float trig = al * C[i] + be * Dc[i] + (alL * sL * wL.x + beL * dL * wL.y);
+            const float raw = __fmul_rn(trig, kMInvPi);
+            float val;
+            if (a.transform_to_bounds)
+                val = (j == 0) ? (float)((double)__fsub_rn(raw, lo) * inv) : (float)((double)raw * inv);
+            else
+                val = raw;
+            out[j] = val;
+            if (j == 0)
+                m0 = val;
+        }
+        wL = cmul(wL, vL);
+    }
+
+    if (q == 0)
+    {
+        const uint16_t lo16 = (uint16_t)__fmul_rn(lo, 65535.f);
+        const uint16_t hi16 = (uint16_t)__fmul_rn(hi, 65535.f);
+        if (a.bounds && a.transform_to_bounds)
+        {
+            a.bounds[2 * pix] = lo16;
+            a.bounds[2 * pix + 1] = hi16;
+        }
+        if (a.counts && a.compact_image)
+        {
+            // compute_num_moments (moment_compaction.h:147-174): an empty ray keeps no moments; with a zero
+            // error threshold every other ray keeps all m (otherwise count_moments_kernel refines this).
+            const bool is_zero = a.transform_to_bounds ? (lo16 == hi16) : (m0 == 0.f);
+            a.counts[pix] = is_zero ? 0u : (uint32_t)a.m;
+        }
+    }
+}
+
+template <int NJ>
+void launch_nj(const GenArgs &a, bool kahan, cudaStream_t stream)
+{
+    dim3 block(128);
+    dim3 grid((a.width + 7) / 8, (a.height + 3) / 4);
+    if (kahan)
+        generate_grid_kernel<NJ, true><<<grid, block, 0, stream>>>(a);
+    else
+        generate_grid_kernel<NJ, false><<<grid, block, 0, stream>>>(a);
+}
+
+} // namespace
+
+cudaError_t launch_generate_grid(const GridView &grid, const DeviceCamera &cam, const mraygb_generation_params &gp,
+                                 int width, int height, int m, bool kahan, float *moments, uint16_t *bounds,
+                                 uint32_t *counts, int *error_flag, cudaStream_t stream)
+{
+    GenArgs a;
+    a.grid = grid;
+    a.cam = cam;
+    a.width = width;
+    a.height = height;
+    a.m = m;
+    a.step = gp.step_size;
+    a.data_min = gp.data_min;
+    a.data_max = gp.data_max;
+    a.bound_eps = gp.transform_bound_eps;
+    a.transform_to_bounds = gp.transform_to_bounds ? 1 : 0;
+    a.compact_image = gp.compact_image ? 1 : 0;
+    a.error_threshold_zero = gp.error_threshold == 0.f ? 1 : 0;
+    a.moments = moments;
+    a.bounds = bounds;
+    a.counts = counts;
+    a.error_flag = error_flag;
+    const int nj = (m + 3) / 4;
+    if (nj <= 1)
+        launch_nj<1>(a, kahan, stream);
+    else if (nj <= 2)
+        launch_nj<2>(a, kahan, stream);
+    else if (nj <= 4)
+        launch_nj<4>(a, kahan, stream);
+    else if (nj <= 8)
+        launch_nj<8>(a, kahan, stream);
+    else if (nj <= 16)
+        launch_nj<16>(a, kahan, stream);
+    else if (nj <= 32)
+        launch_nj<32>(a, kahan, stream);
+    else
+        launch_nj<64>(a, kahan, stream);
+    return cudaGetLastError();
+}
+
+} // namespace mraygb

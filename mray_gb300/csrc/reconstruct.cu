@@ -1,0 +1,253 @@
+// Bounded-MESE re-march: one thread per pixel (reconstruct_ray with MESEReconstruction and no single
+// scattering, src/raymarch_reconstruct.h:127-200 and src/reconstruction_techniques.h:72-96; driven per pixel
+// as reconstruct_host / reconstruct_moments_kernel, src/moment_raymarcher.cpp:283-327, .cu:339-384).
+//
+// Per sample the density is rho(p) = lo + (hi - lo) (fast_atan(S(p)) / pi + 1/2) with the Lagrange series
+// S(p) = l_0 + 2 sum_{l>=1} l_l cos(l p) (evaluateMESELagrange, src/mese/MESE_dynamic.h:242-250).  The series is
+// summed by Clenshaw's recurrence on cos(p) - two operations per term, with the multipliers held in
+// registers - instead of the reference's complex power recurrence (five per term).
+//
+// The transfer-function row lives in shared memory and is sampled exactly as TransferFunction::sample does on
+// a table whose rows are all equal (src/transfer_function.h:44-59): the column comes from floor(256 fs), the
+// blend weight from frac(256 bs).
+
+#include "device_common.cuh"
+#include "internal.h"
+
+namespace mraygb
+{
+
+namespace
+{
+
+struct ReconDev
+{
+    DeviceCamera cam;
+    int width, height, m;
+    float dmin[3], dmax[3];
+    const uint32_t *index;
+    const float *pmoments;
+    const uint16_t *bounds;
+    const float4 *tf;
+    float step, emission, ert;
+    float *rgba;
+    uint8_t *rgba8;
+    int *error_flag;
+};
+
+// fast_atan (src/mese/complex_algebra.h:133-152)
+__device__ __forceinline__ float fast_atan(float tan)
+{
+    const bool negative = tan < 0.0f;
+    const float abs_tan = negative ? -tan : tan;
+    const bool greater_one = abs_tan > 1.0f;
+    float x = greater_one ? abs_tan : 1.0f;
+    x = 1.0f / x;
+    float y = greater_one ? 1.0f : abs_tan;
+    x = x * y;
+    y = x * x;
+    float z = y * 0.020835f - 0.085133f;
+    z = y * z + 0.180141f;
+    z = y * z - 0.330299f;
+    y = y * z + 0.999866f;
+    z = y * x;
+    z = z * -2.0f + 1.570796f;
+    z = greater_one ? z : 0.0f;
+    x = x * y + z;
+    return negative ? -x : x;
+}
+
+__device__ __forceinline__ float4 tf_sample(const float4 *T, float fs, float bs)
+{
+    const float ipx = fs * 256.f, ipy = bs * 256.f;
+    const float flx = floorf(ipx);
+    const float ax = ipx - flx, ay = ipy - floorf(ipy);
+    const int xl = (int)flx;
+    const int x0 = min(max(xl, 0), 255);
+    const int x1 = min(max(xl + 1, 0), 255);
+    const float4 a = T[x0], b = T[x1];
+    const float wll = (1.f - ax) * (1.f - ay), wlr = ax * (1.f - ay), wrl = (1.f - ax) * ay, wrr = ax * ay;
+    float4 r;
+    r.x = wll * a.x + wlr * a.x + wrl * b.x + wrr * b.x;
+    r.y = wll * a.y + wlr * a.y + wrl * b.y + wrr * b.y;
+    r.z = wll * a.z + wlr * a.z + wrl * b.z + wrr * b.z;
+    r.w = wll * a.w + wlr * a.w + wrl * b.w + wrr * b.w;
+    return r;
+}
+
+template <int MAXM>
+__device__ __forceinline__ float mese_density(const float (&lam2)[MAXM], float lam0, float p, float lo, float span)
+{
+    const float pc = rclamp(p, -kPiF, 0.0f);
+    const float c = cosf(pc);
+    const float c2 = c + c;
+    float b1 = 0.f, b2 = 0.f;
+#pragma unroll
+    for (int l = MAXM - 1; l >= 1; --l)
+    {
+        const float b0 = fmaf(c2, b1, lam2[l] - b2);
+        b2 = b1;
+        b1 = b0;
+    }
+    const float s = fmaf(c, b1, lam0 - b2);
+    return (fast_atan(s) * 0.318309886f + 0.5f) * span + lo;
+}
+
+template <int MAXM>
+__global__ void __launch_bounds__(128) reconstruct_kernel(const ReconDev a)
+{
+    __shared__ float4 s_tf[256];
+    for (int i = threadIdx.x + threadIdx.y * blockDim.x; i < 256; i += blockDim.x * blockDim.y)
+        s_tf[i] = a.tf[i];
+    __syncthreads();
+
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= a.width || y >= a.height)
+        return;
+    const size_t pix = (size_t)y * (size_t)a.width + (size_t)x;
+    size_t idx;
+    int n;
+    if (a.index)
+    {
+        idx = a.index[pix];
+        n = (int)(a.index[pix + 1] - a.index[pix]);
+    }
+    else
+    {
+        idx = pix * (size_t)a.m;
+        n = a.m;
+    }
+
+    float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (n == 0)
+    {
+        // reconstruct_zero_ray (src/raymarch_reconstruct.h:127-131)
+        const float4 z = tf_sample(s_tf, 0.f, 0.f);
+        out = make_float4(z.x, z.y, z.z, 0.f);
+    }
+    else
+    {
+        if (n > MAXM)
+            n = MAXM;
+        float lam2[MAXM];
+        const float lam0 = a.pmoments[idx];
+#pragma unroll
+        for (int l = 0; l < MAXM; ++l)
+            lam2[l] = (l < n && l > 0) ? 2.f * a.pmoments[idx + l] : 0.f;
+        float lo = 0.f, hi = 1.f;
+        if (a.bounds)
+        {
+            lo = a.bounds[2 * pix] / 65535.f;
+            hi = a.bounds[2 * pix + 1] / 65535.f;
+        }
+        const float span = hi - lo;
+
+        float nx, ny, o[3], d[3];
+        pixel_ndc(x, y, a.width, a.height, nx, ny);
+        eye_ray(a.cam, nx, ny, o, d);
+        float t_near, t_far;
+        const bool hit = intersect_aabb(o, d, a.dmin, a.dmax, t_near, t_far);
+        t_near = rmax(t_near, a.cam.znear);
+        if (hit && t_far > 0.f)
+        {
+            const float range = __fsub_rn(t_far, t_near);
+            float t = t_near;
+            float p = (float)((double)__fdiv_rn(__fsub_rn(t, t_near), range) * 3.141592653589793 -
+                              3.141592653589793);
+            const float phase_step = (float)(3.141592653589793 * (double)__fdiv_rn(a.step, range));
+            // the march ends by itself after about range / step samples; the cap only guards a step that is too
+            // small to advance t in float
+            const float est = range / a.step;
+            const int cap = (est < 1.6e9f ? (int)(1.25f * est) : 2000000000) + 64;
+            float L0 = 0.f, L1 = 0.f, L2 = 0.f, alpha = 0.f, T = 1.f, tau = 0.f;
+            float fs = mese_density<MAXM>(lam2, lam0, p, lo, span);
+            int it = 0;
+            while (t <= t_far)
+            {
+                if (++it > cap)
+                {
+                    atomicExch(a.error_flag, 1);
+                    break;
+                }
+                t = __fadd_rn(t, a.step);
+                p = __fadd_rn(p, phase_step);
+                const float bs = mese_density<MAXM>(lam2, lam0, p, lo, span);
+                const float4 s = tf_sample(s_tf, fs, bs);
+                L0 += (a.emission * s.x) * T;
+                L1 += (a.emission * s.y) * T;
+                L2 += (a.emission * s.z) * T;
+                tau += s.w;
+                T = expf(-tau);
+                alpha = 1.f - T;
+                fs = bs;
+                if (alpha >= a.ert)
+                {
+                    alpha = 1.f;
+                    break;
+                }
+            }
+            out = make_float4(L0, L1, L2, alpha);
+        }
+    }
+    if (a.rgba)
+        reinterpret_cast<float4 *>(a.rgba)[pix] = out;
+    if (a.rgba8)
+    {
+        // ColorImageHost::rgba8_t (src/color_image.h:41-47) after clamp to [0, 1]
+        uchar4 c;
+        c.x = (unsigned char)(rclamp(out.x, 0.f, 1.f) * 255.f);
+        c.y = (unsigned char)(rclamp(out.y, 0.f, 1.f) * 255.f);
+        c.z = (unsigned char)(rclamp(out.z, 0.f, 1.f) * 255.f);
+        c.w = (unsigned char)(rclamp(out.w, 0.f, 1.f) * 255.f);
+        reinterpret_cast<uchar4 *>(a.rgba8)[pix] = c;
+    }
+}
+
+template <int MAXM> void launch_m(const ReconDev &a, cudaStream_t stream)
+{
+    dim3 block(16, 8);
+    dim3 grid((a.width + 15) / 16, (a.height + 7) / 8);
+    reconstruct_kernel<MAXM><<<grid, block, 0, stream>>>(a);
+}
+
+} // namespace
+
+cudaError_t launch_reconstruct(const ReconArgs &r, int *error_flag, cudaStream_t stream)
+{
+    ReconDev a;
+    a.cam = *r.cam;
+    a.width = r.width;
+    a.height = r.height;
+    a.m = r.m;
+    for (int i = 0; i < 3; ++i)
+    {
+        a.dmin[i] = r.dmin[i];
+        a.dmax[i] = r.dmax[i];
+    }
+    a.index = r.index;
+    a.pmoments = r.pmoments;
+    a.bounds = r.bounds;
+    a.tf = r.tf;
+    a.step = r.step;
+    a.emission = r.emission;
+    a.ert = r.ert;
+    a.rgba = r.rgba;
+    a.rgba8 = r.rgba8;
+    a.error_flag = error_flag;
+    if (r.m <= 8)
+        launch_m<8>(a, stream);
+    else if (r.m <= 16)
+        launch_m<16>(a, stream);
+    else if (r.m <= 32)
+        launch_m<32>(a, stream);
+    else if (r.m <= 64)
+        launch_m<64>(a, stream);
+    else if (r.m <= 128)
+        launch_m<128>(a, stream);
+    else
+        launch_m<256>(a, stream);
+    return cudaGetLastError();
+}
+
+} // namespace mraygb

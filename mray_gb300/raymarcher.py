@@ -1,0 +1,313 @@
+"""Host-side mirror of the reference's moment raymarcher interface, running on the CUDA library.
+
+The names, argument meaning and error behaviour follow the reference (TobiasRp/mray):
+
+* :class:`MomentImageHost`   -- src/moment_image.h:33-147 (index / bounds / coding params / data)
+* :class:`ColorImageHost`    -- src/color_image.h:30-71 (u8 RGBA, plus the float colour before the u8 store)
+* :class:`RegularGrid`       -- src/volume.h:31-123
+* :class:`TransferFunction`  -- src/transfer_function.h:30-60, built by :func:`preintegrate`
+  (src/transfer_function.cpp:46-97)
+* :func:`generate`           -- generate(cam, volume, mi, params), src/moment_raymarcher.h:48-49
+* :func:`reconstruct`        -- reconstruct(cam, mi, tf, img, params), src/moment_raymarcher.h:61-64
+
+All compute runs in ``libmraygb.so``; there is no CPU path.  :class:`Context` exposes the C ABI's stage calls on
+device pointers (ints or CUDA tensors).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional
+
+import numpy as np
+
+from . import _lib
+from .types import Camera, GenerationParameters, ReconstructionParameters
+
+PRECISION_FP32 = 0
+PRECISION_COMPENSATED_FP64_MESE = 1
+MAX_MOMENTS = 255
+
+
+def _dptr(x) -> Optional[int]:
+    """A device address from None, an int or a CUDA tensor."""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    if hasattr(x, "data_ptr"):
+        if not x.is_cuda:
+            raise ValueError("expected a CUDA tensor")
+        if not x.is_contiguous():
+            raise ValueError("expected a contiguous tensor")
+        return x.data_ptr()
+    raise TypeError(f"cannot take a device pointer of {type(x)}")
+
+
+def _hptr(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _f3(v):
+    return (C.c_float * 3)(*[float(x) for x in v])
+
+
+class RegularGrid:
+    """RegularGrid: float32 data indexed [z, y, x] on the box [domain_min, domain_max]."""
+
+    def __init__(self, data: np.ndarray, domain_min=(0.0, 0.0, 0.0), domain_max=(1.0, 1.0, 1.0)):
+        self.data = data
+        self.domain_min = tuple(float(v) for v in domain_min)
+        self.domain_max = tuple(float(v) for v in domain_max)
+
+    @property
+    def size(self):
+        nz, ny, nx = self.data.shape
+        return (nx, ny, nz)
+
+
+class TransferFunction:
+    """TransferFunction: ``table`` is one row (256 x RGBA float) of the 256 x 256 table, all rows being equal."""
+
+    RESOLUTION = 256
+
+    def __init__(self, table: np.ndarray):
+        t = np.ascontiguousarray(table, dtype=np.float32)
+        if t.shape != (256, 4):
+            raise ValueError("transfer function table must be 256 x 4")
+        self.table = t
+
+
+def preintegrate(tf1d: np.ndarray, step_size: float) -> TransferFunction:
+    """preintegrate (transfer_function.cpp:46-97): entry x = (rgb_x * a_x s, a_x s), s = step_size (float
+    arithmetic, as the reference's)."""
+    t = np.ascontiguousarray(tf1d, dtype=np.float32)
+    w = t[:, 3] * np.float32(step_size)
+    out = np.empty_like(t)
+    out[:, 0] = t[:, 0] * w
+    out[:, 1] = t[:, 1] * w
+    out[:, 2] = t[:, 2] * w
+    out[:, 3] = w
+    return TransferFunction(out)
+
+
+class MomentImageHost:
+    """MomentImageHost (moment_image.h:33-147)."""
+
+    def __init__(self, width: int, height: int, num_moments: int, create_index: bool = True,
+                 create_bounds: bool = False):
+        self.width = int(width)
+        self.height = int(height)
+        self.num_moments = int(num_moments)
+        self.is_compact = False
+        self.prediction_code = False
+        self.coding_warp = 0
+        self.domain_min = (0.0, 0.0, 0.0)
+        self.domain_max = (1.0, 1.0, 1.0)
+        self.index = np.zeros(self.width * self.height + 1, dtype=np.uint32) if create_index else None
+        self.bounds = np.zeros((self.width * self.height, 2), dtype=np.uint16) if create_bounds else None
+        self.coding_params: Optional[np.ndarray] = None
+        self.data = np.zeros(self.width * self.height * self.num_moments, dtype=np.float32)
+
+    def has_bounds(self) -> bool:
+        return self.bounds is not None
+
+    def get_idx(self, x: int, y: int) -> int:
+        if self.is_compact:
+            return int(self.index[y * self.width + x])
+        return (y * self.width + x) * self.num_moments
+
+    def get_num_moments(self, x: int, y: int) -> int:
+        if self.is_compact:
+            p = y * self.width + x
+            return int(self.index[p + 1] - self.index[p])
+        return self.num_moments
+
+    def get_bounds(self, x: int, y: int):
+        if self.bounds is None:
+            return (0.0, 1.0)
+        b = self.bounds[y * self.width + x]
+        return (np.float32(b[0]) / np.float32(65535.0), np.float32(b[1]) / np.float32(65535.0))
+
+
+class ColorImageHost:
+    """ColorImageHost: u8 RGBA as the reference stores it, plus ``rgba_float`` (the colour before the store)."""
+
+    def __init__(self, width: int, height: int):
+        self.width = int(width)
+        self.height = int(height)
+        self.rgba = np.zeros((self.height, self.width, 4), dtype=np.uint8)
+        self.rgba_float = np.zeros((self.height, self.width, 4), dtype=np.float32)
+
+
+class Context:
+    """One mraygb_context: a device, a stream, the resident volume and transfer function."""
+
+    def __init__(self, device: int = 0, precision: int = PRECISION_FP32):
+        self._L = _lib.load()
+        h = C.c_void_p()
+        st = self._L.mraygb_create(int(device), C.byref(h))
+        if st != 0:
+            raise _lib.MrayError(st, f"cannot create a context on device {device}")
+        self._h = h
+        self.device = device
+        self._grid_key = None
+        self._tf_key = None
+        self.precision = precision
+
+    # ---- lifetime ----
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.mraygb_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, st):
+        _lib.check(self._h, st)
+
+    # ---- settings ----
+    @property
+    def precision(self) -> int:
+        return self._precision
+
+    @precision.setter
+    def precision(self, value: int):
+        self._check(self._L.mraygb_set_precision(self._h, int(value)))
+        self._precision = int(value)
+
+    def set_stream(self, stream) -> None:
+        """Orders later work on ``stream`` (a cudaStream_t as int, a torch.cuda.Stream, or None)."""
+        if stream is not None and hasattr(stream, "cuda_stream"):
+            stream = stream.cuda_stream
+        self._check(self._L.mraygb_set_stream(self._h, stream))
+
+    def synchronize(self) -> None:
+        self._check(self._L.mraygb_synchronize(self._h))
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(self._L.mraygb_kernel_launches(self._h))
+
+    # ---- resident inputs ----
+    def upload_grid(self, volume, domain_min, domain_max) -> None:
+        """Uploads a [z, y, x] float32 volume (numpy array or CUDA tensor)."""
+        if hasattr(volume, "data_ptr"):
+            nz, ny, nx = volume.shape
+            self._check(self._L.mraygb_upload_grid(self._h, _dptr(volume), nx, ny, nz, _f3(domain_min),
+                                                   _f3(domain_max), 1))
+        else:
+            v = np.ascontiguousarray(volume, dtype=np.float32)
+            nz, ny, nx = v.shape
+            self._check(self._L.mraygb_upload_grid(self._h, _hptr(v), nx, ny, nz, _f3(domain_min), _f3(domain_max),
+                                                   0))
+        self._grid_key = None
+
+    def upload_tf(self, table) -> None:
+        t = np.ascontiguousarray(table, dtype=np.float32)
+        if t.shape != (256, 4):
+            raise ValueError("transfer function table must be 256 x 4")
+        self._check(self._L.mraygb_upload_tf(self._h, _hptr(t)))
+        self._tf_key = None
+
+    # ---- drop-in host calls ----
+    def generate(self, cam: Camera, gp: GenerationParameters, width: int, height: int, num_moments: int,
+                 out: Optional[MomentImageHost] = None) -> MomentImageHost:
+        mi = out or MomentImageHost(width, height, num_moments, bool(gp.compact_image),
+                                    bool(gp.transform_to_bounds))
+        cap = width * height * num_moments
+        if mi.data.size < cap:
+            mi.data = np.zeros(cap, dtype=np.float32)
+        if gp.compact_image and mi.index is None:
+            mi.index = np.zeros(width * height + 1, dtype=np.uint32)
+        if gp.transform_to_bounds and mi.bounds is None:
+            mi.bounds = np.zeros((width * height, 2), dtype=np.uint16)
+        cp = np.zeros(max(2 * (num_moments - 1), 1), dtype=np.uint16)
+        size = C.c_uint64()
+        self._check(self._L.mraygb_generate(self._h, C.byref(cam), C.byref(gp), width, height, num_moments,
+                                            _hptr(mi.data), _hptr(mi.index) if gp.compact_image else None,
+                                            _hptr(mi.bounds) if gp.transform_to_bounds else None, _hptr(cp),
+                                            C.byref(size)))
+        mi.data = mi.data[:size.value]
+        mi.is_compact = bool(gp.compact_image)
+        mi.prediction_code = bool(gp.prediction_coding)
+        mi.coding_warp = int(gp.coding_warp)
+        mi.coding_params = cp[:2 * (num_moments - 1)] if (gp.prediction_coding and gp.coding_warp == 0) else None
+        return mi
+
+    def reconstruct(self, cam: Camera, rp: ReconstructionParameters, mi: MomentImageHost,
+                    img: Optional[ColorImageHost] = None) -> ColorImageHost:
+        img = img or ColorImageHost(mi.width, mi.height)
+        data = np.ascontiguousarray(mi.data, dtype=np.float32)
+        index = np.ascontiguousarray(mi.index, dtype=np.uint32) if mi.is_compact else None
+        bounds = np.ascontiguousarray(mi.bounds, dtype=np.uint16) if mi.bounds is not None else None
+        cp = np.ascontiguousarray(mi.coding_params, dtype=np.uint16) if mi.coding_params is not None else None
+        self._check(self._L.mraygb_reconstruct(self._h, C.byref(cam), C.byref(rp), mi.width, mi.height,
+                                               mi.num_moments, _f3(mi.domain_min), _f3(mi.domain_max), _hptr(index),
+                                               _hptr(data), data.size, _hptr(bounds), int(mi.prediction_code),
+                                               int(mi.coding_warp), _hptr(cp), _hptr(img.rgba_float),
+                                               _hptr(img.rgba)))
+        return img
+
+    # ---- stage calls on device pointers ----
+    def stage_generate_moments(self, cam, gp, width, height, num_moments, moments, bounds=None, counts=None):
+        self._check(self._L.mraygb_stage_generate_moments(self._h, C.byref(cam), C.byref(gp), width, height,
+                                                          num_moments, _dptr(moments), _dptr(bounds),
+                                                          _dptr(counts)))
+
+    def stage_compact(self, width, height, num_moments, counts, moments, index, compact, capacity=None) -> int:
+        total = C.c_uint64()
+        if capacity is None:
+            capacity = compact.numel() if hasattr(compact, "numel") else width * height * num_moments
+        self._check(self._L.mraygb_stage_compact(self._h, width, height, num_moments, _dptr(counts), _dptr(moments),
+                                                 _dptr(index), _dptr(compact), int(capacity), C.byref(total)))
+        return int(total.value)
+
+    def stage_prepare_moments(self, width, height, num_moments, index, data, pmoments, prediction_code=False,
+                              coding_warp=0, coding_params=None, bias=1e-6):
+        self._check(self._L.mraygb_stage_prepare_moments(self._h, width, height, num_moments, _dptr(index),
+                                                         _dptr(data), int(prediction_code), int(coding_warp),
+                                                         _dptr(coding_params), float(bias), _dptr(pmoments)))
+
+    def stage_reconstruct(self, cam, rp, width, height, num_moments, domain_min, domain_max, index, pmoments,
+                          bounds, rgba, rgba8=None):
+        self._check(self._L.mraygb_stage_reconstruct(self._h, C.byref(cam), C.byref(rp), width, height,
+                                                     num_moments, _f3(domain_min), _f3(domain_max), _dptr(index),
+                                                     _dptr(pmoments), _dptr(bounds), _dptr(rgba), _dptr(rgba8)))
+
+
+_default: dict = {}
+
+
+def default_context(device: int = 0) -> Context:
+    ctx = _default.get(device)
+    if ctx is None:
+        ctx = _default[device] = Context(device)
+    return ctx
+
+
+def generate(cam: Camera, volume: RegularGrid, mi: MomentImageHost, params: GenerationParameters,
+             context: Optional[Context] = None) -> None:
+    """generate(cam, volume, mi, params) (moment_raymarcher.h:48-49): fills ``mi`` in place."""
+    ctx = context or default_context()
+    ctx.upload_grid(volume.data, volume.domain_min, volume.domain_max)
+    out = ctx.generate(cam, params, mi.width, mi.height, mi.num_moments, out=mi)
+    mi.domain_min, mi.domain_max = volume.domain_min, volume.domain_max
+    assert out is mi
+
+
+def reconstruct(cam: Camera, mi: MomentImageHost, tf: TransferFunction, img: ColorImageHost,
+                params: ReconstructionParameters, context: Optional[Context] = None) -> None:
+    """reconstruct(cam, mi, tf, img, params) (moment_raymarcher.h:61-64): fills ``img`` in place."""
+    ctx = context or default_context()
+    ctx.upload_tf(tf.table)
+    ctx.reconstruct(cam, params, mi, img)
