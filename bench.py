@@ -61,6 +61,17 @@ def dist_info():
     return rank, world, local
 
 
+def reduce_max(values, dist=None, device="cpu"):
+    """Max over ranks of a list of floats (the timing of the slowest replica); identity without a process group."""
+    if dist is None:
+        return [float(v) for v in values]
+    import torch
+
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.tolist()]
+
+
 def workload(args):
     from mray_gb300 import workloads as W
 
@@ -326,12 +337,7 @@ def run_ours(args):
     total_ms, gen_ms, launches, wall = timed_loop(M.PRECISION_COMPENSATED_FP64_MESE)
     clocks = sampler.stop()
 
-    t_max = total_ms
-    plain_max = plain_ms
-    if dist:
-        t = torch.tensor([total_ms, plain_ms], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max, plain_max = float(t[0]), float(t[1])
+    t_max, plain_max = reduce_max([total_ms, plain_ms], dist, "cuda")
     value = world * P * args.steps / (t_max * 1e-3) / 1e6
     plain_value = world * P * args.steps / (plain_max * 1e-3) / 1e6
 
@@ -426,10 +432,7 @@ def run_e2e(args, ctx, wl, dist):
         one()
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
-    if dist:
-        t = torch.tensor([dt], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dt = float(t[0])
+    (dt,) = reduce_max([dt], dist, "cuda")
     world = dist.get_world_size() if dist else 1
     moments_bytes = mi.data.size * 4
     h2d = wl.volume.size * 4 + 256 * 16 + moments_bytes + (P + 1) * 4 + 4 * P

@@ -115,6 +115,15 @@ int mraygb_reconstruct(mraygb_context *ctx, const mraygb_camera *cam, const mray
                        int prediction_code, int coding_warp, const uint16_t *h_coding_params, float *h_rgba,
                        uint8_t *h_rgba8);
 
+/* moment_quantization::quantize_prediction_coding(mi, table) (src/moment_quantization.cpp:239-276 with
+ * pack_bits :92-114) for a compact, prediction-coded image in host memory: per pixel in row-major order and per
+ * moment index l ascending, code = trunc(clamp(v, 0, 1) * (2^table[l] - 1)), packed LSB first.  Like the
+ * reference's packer it emits whole bytes only.  *h_nbytes receives the byte count; h_out (capacity bytes) may
+ * be NULL to query the size. */
+int mraygb_quantize_prediction_coding(mraygb_context *ctx, int width, int height, int num_moments,
+                                      const uint32_t *h_index, const float *h_data, uint64_t data_size,
+                                      const uint8_t *h_table, uint8_t *h_out, uint64_t capacity, uint64_t *h_nbytes);
+
 /* ---- stage API: device pointers, ordered on the context stream ------------------------------------------ */
 
 /* Per-ray moments over the uploaded grid (generate_ray, src/raymarch_generate.h:69-148, driven as
@@ -133,6 +142,27 @@ int mraygb_stage_generate_moments(mraygb_context *ctx, const mraygb_camera *cam,
 int mraygb_stage_compact(mraygb_context *ctx, int width, int height, int num_moments, const uint32_t *d_counts,
                          const float *d_moments, uint32_t *d_index, float *d_compact, uint64_t capacity,
                          uint64_t *h_total);
+
+/* MomentImageDevice::prediction_encode (src/moment_image_device.cu:166-195; host form
+ * MomentImageHost::prediction_encode, src/moment_image.cpp:96-152) in place on a compact image: bias lerp,
+ * trigonometric -> exponential moments, Levinson-style encode, projection to the real line, coding parameters
+ * (per-index |min|, |max - min| / 2 over the image, ceil-quantized to u16, written to d_coding_params[2(m-1)]
+ * for the default warp) and the warp of every residual to [0, 1]. */
+int mraygb_stage_prediction_encode(mraygb_context *ctx, int width, int height, int num_moments,
+                                   const uint32_t *d_index, float *d_data, uint64_t data_size, int coding_warp,
+                                   float bias, uint16_t *d_coding_params);
+
+/* quantize_prediction_coding on device buffers: d_out must hold ceil(bits / 32) * 4 bytes (capacity);
+ * *h_nbytes receives the number of valid bytes (whole bytes, as the reference's packer). */
+int mraygb_stage_quantize_prediction_coding(mraygb_context *ctx, int width, int height, int num_moments,
+                                            const uint32_t *d_index, const float *d_data, const uint8_t *h_table,
+                                            uint8_t *d_out, uint64_t capacity, uint64_t *h_nbytes);
+
+/* dequantize_prediction_coding (src/moment_quantization.cpp:278-332 with unpack_bits :135-160): codes back to
+ * values in [0, 1] in the compact layout; codes the stream does not hold read as 0. */
+int mraygb_stage_dequantize_prediction_coding(mraygb_context *ctx, int width, int height, int num_moments,
+                                              const uint32_t *d_index, const uint8_t *h_table,
+                                              const uint8_t *d_bytes, uint64_t num_bytes, float *d_data);
 
 /* Lagrange multipliers per pixel (prepare_moments_device, src/moment_image_device.cu:306-335): the moment data
  * in the compact layout (d_index) or, with d_index NULL, the W*H*m layout; output in the same layout. */

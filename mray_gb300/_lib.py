@@ -21,7 +21,9 @@ EXPORTS = [
     "mraygb_create", "mraygb_destroy", "mraygb_last_error", "mraygb_set_stream", "mraygb_get_stream",
     "mraygb_synchronize", "mraygb_set_precision", "mraygb_kernel_launches", "mraygb_upload_grid", "mraygb_upload_tf",
     "mraygb_generate", "mraygb_reconstruct", "mraygb_stage_generate_moments", "mraygb_stage_compact",
-    "mraygb_stage_prepare_moments", "mraygb_stage_reconstruct",
+    "mraygb_stage_prepare_moments", "mraygb_stage_reconstruct", "mraygb_quantize_prediction_coding",
+    "mraygb_stage_prediction_encode", "mraygb_stage_quantize_prediction_coding",
+    "mraygb_stage_dequantize_prediction_coding",
 ]
 
 _lock = threading.Lock()
@@ -61,6 +63,11 @@ def _declare(L):
     L.mraygb_stage_prepare_moments.argtypes = [vp, i, i, i, vp, vp, i, i, vp, C.c_float, vp]
     L.mraygb_stage_reconstruct.argtypes = [vp, P(Camera), P(ReconstructionParameters), i, i, i, C.c_float * 3,
                                            C.c_float * 3, vp, vp, vp, vp, vp]
+    u64 = C.c_uint64
+    L.mraygb_quantize_prediction_coding.argtypes = [vp, i, i, i, vp, vp, u64, vp, vp, u64, P(u64)]
+    L.mraygb_stage_prediction_encode.argtypes = [vp, i, i, i, vp, vp, u64, i, C.c_float, vp]
+    L.mraygb_stage_quantize_prediction_coding.argtypes = [vp, i, i, i, vp, vp, vp, vp, u64, P(u64)]
+    L.mraygb_stage_dequantize_prediction_coding.argtypes = [vp, i, i, i, vp, vp, vp, u64, vp]
     special = ("mraygb_destroy", "mraygb_last_error", "mraygb_get_stream", "mraygb_kernel_launches")
     for name in EXPORTS:
         if name not in special:

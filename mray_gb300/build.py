@@ -1,7 +1,7 @@
 """Builds the CUDA library ``mray_gb300/libmraygb.so`` in-tree for sm_103a.
 
 Each translation unit is compiled by nvcc in parallel and the objects are linked into one shared library with
-the CUDA runtime linked statically.  ``mese.cu`` and ``quantize.cu`` are compiled without FMA contraction so
+the CUDA runtime linked statically.  ``mese.cu`` and ``coding.cu`` are compiled without FMA contraction so
 that the FP32 MESE algebra and the quantizer round exactly as the reference's separately rounded operations;
 the marching kernels keep contraction on.
 """
@@ -29,6 +29,7 @@ SOURCES = [
     ("reconstruct.cu", []),
     ("scan.cu", []),
     ("mese.cu", ["--fmad=false"]),
+    ("coding.cu", ["--fmad=false"]),
     ("api.cpp", ["-x", "cu"]),
 ]
 

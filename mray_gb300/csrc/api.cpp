@@ -72,6 +72,8 @@ struct mraygb_context
     // work buffers of the drop-in calls and of the scan
     DeviceBuffer moments, counts, index, compact, bounds, coding_params, pmoments, rgba, rgba8, scan_scratch;
     DeviceBuffer error_flag;
+    // prediction coding and quantization
+    DeviceBuffer coding_partial, coding_params_f, table, bits, bit_offset, scan_scratch64, packed;
 };
 
 namespace
@@ -253,6 +255,111 @@ int run_reconstruct(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_
     return MRAYGB_OK;
 }
 
+int run_prediction_encode(mraygb_context *ctx, int width, int height, int m, const uint32_t *d_index, float *d_data,
+                          uint64_t data_size, int coding_warp, float bias, uint16_t *d_coding_params)
+{
+    const int P = width * height;
+    CK(launch_prediction_encode(P, m, d_index, d_data, bias, ctx->stream), "prediction encode launch");
+    ctx->launches += 1;
+    CK(ctx->coding_params_f.reserve(2 * (size_t)m * sizeof(float)), "coding parameter allocation");
+    if (coding_warp == MRAYGB_CODING_WARP_DEFAULT_TRANSFORMED)
+    {
+        if (m > 1)
+        {
+            const int blocks = coding_minmax_blocks(P);
+            CK(ctx->coding_partial.reserve((size_t)blocks * (size_t)(m - 1) * sizeof(float2)), "partial allocation");
+            CK(launch_coding_params(P, m, d_index, d_data, data_size, ctx->coding_partial.as<float2>(),
+                                    d_coding_params, ctx->coding_params_f.as<float>(), ctx->stream),
+               "coding parameter launch");
+            ctx->launches += 2;
+        }
+    }
+    if (m > 1)
+    {
+        CK(launch_coding_warp(P, d_index, d_data, coding_warp, ctx->coding_params_f.as<float>(), ctx->stream),
+           "coding warp launch");
+        ctx->launches += 1;
+    }
+    return MRAYGB_OK;
+}
+
+// bit counts per index (table) and their prefix sums, uploaded to the context; returns the table pointers
+int upload_table(mraygb_context *ctx, int m, const uint8_t *h_table, const uint8_t **d_table,
+                 const uint32_t **d_prefix)
+{
+    if (!h_table)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "quantization table is NULL");
+    uint8_t host[256 + 4 * 257];
+    std::memset(host, 0, sizeof(host));
+    uint32_t prefix[257];
+    prefix[0] = 0;
+    for (int l = 0; l < m; ++l)
+    {
+        if (h_table[l] < 1 || h_table[l] > 32)
+            return fail(ctx, MRAYGB_INVALID_ARGUMENT, "quantization table entry %d is %d bits (1..32)", l,
+                        (int)h_table[l]);
+        host[l] = h_table[l];
+        prefix[l + 1] = prefix[l] + h_table[l];
+    }
+    std::memcpy(host + 256, prefix, sizeof(uint32_t) * (size_t)(m + 1));
+    CK(ctx->table.reserve(sizeof(host)), "table allocation");
+    CK(cudaMemcpyAsync(ctx->table.ptr, host, sizeof(host), cudaMemcpyHostToDevice, ctx->stream), "table upload");
+    *d_table = ctx->table.as<uint8_t>();
+    *d_prefix = reinterpret_cast<const uint32_t *>(ctx->table.as<uint8_t>() + 256);
+    return MRAYGB_OK;
+}
+
+// per-pixel bit offsets of the packed stream; *total_bits is read back to the host
+int run_bit_offsets(mraygb_context *ctx, int P, const uint32_t *d_index, const uint32_t *d_prefix,
+                    uint64_t *total_bits)
+{
+    CK(ctx->bits.reserve((size_t)P * sizeof(unsigned long long)), "bit count allocation");
+    CK(ctx->bit_offset.reserve(((size_t)P + 1) * sizeof(unsigned long long)), "bit offset allocation");
+    const size_t words = scan_scratch_words((size_t)P);
+    CK(ctx->scan_scratch64.reserve((words + 1) * sizeof(unsigned long long)), "scan scratch allocation");
+    CK(launch_pixel_bits(P, d_index, d_prefix, ctx->bits.as<unsigned long long>(), ctx->stream), "bit count launch");
+    ctx->launches += 1;
+    int launches = 0;
+    CK(launch_exclusive_scan_u64(ctx->bits.as<unsigned long long>(), ctx->bit_offset.as<unsigned long long>(),
+                                 (size_t)P, ctx->scan_scratch64.as<unsigned long long>(), ctx->stream, &launches),
+       "bit offset scan");
+    ctx->launches += (uint64_t)launches;
+    unsigned long long tb = 0;
+    CK(cudaMemcpyAsync(&tb, ctx->bit_offset.as<unsigned long long>() + P, sizeof(tb), cudaMemcpyDeviceToHost,
+                       ctx->stream),
+       "reading the bit count");
+    CK(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+    *total_bits = tb;
+    return MRAYGB_OK;
+}
+
+int run_quantize(mraygb_context *ctx, int width, int height, int m, const uint32_t *d_index, const float *d_data,
+                 const uint8_t *h_table, uint8_t *d_out, uint64_t capacity, uint64_t *h_nbytes)
+{
+    const int P = width * height;
+    const uint8_t *d_table;
+    const uint32_t *d_prefix;
+    int rc = upload_table(ctx, m, h_table, &d_table, &d_prefix);
+    if (rc)
+        return rc;
+    uint64_t total_bits = 0;
+    if ((rc = run_bit_offsets(ctx, P, d_index, d_prefix, &total_bits)))
+        return rc;
+    const uint64_t nbytes = total_bits / 8; // pack_bits emits whole bytes only
+    const uint64_t word_bytes = ((total_bits + 31) / 32) * 4;
+    if (capacity < word_bytes)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "packed buffer holds %llu bytes, %llu needed",
+                    (unsigned long long)capacity, (unsigned long long)word_bytes);
+    if (word_bytes)
+        CK(cudaMemsetAsync(d_out, 0, word_bytes, ctx->stream), "clearing the packed buffer");
+    CK(launch_pack(P, d_index, d_data, d_table, d_prefix, ctx->bit_offset.as<unsigned long long>(),
+                   reinterpret_cast<uint32_t *>(d_out), ctx->stream),
+       "pack launch");
+    ctx->launches += 1;
+    *h_nbytes = nbytes;
+    return MRAYGB_OK;
+}
+
 int validate_rec(mraygb_context *ctx, const mraygb_reconstruction_params *rp)
 {
     if (!rp)
@@ -312,7 +419,8 @@ void mraygb_destroy(mraygb_context *ctx)
     DeviceBuffer *bufs[] = {&ctx->grid,    &ctx->tf,       &ctx->moments,       &ctx->counts,
                             &ctx->index,   &ctx->compact,  &ctx->bounds,        &ctx->coding_params,
                             &ctx->pmoments, &ctx->rgba,    &ctx->rgba8,         &ctx->scan_scratch,
-                            &ctx->error_flag};
+                            &ctx->error_flag, &ctx->coding_partial, &ctx->coding_params_f, &ctx->table,
+                            &ctx->bits,    &ctx->bit_offset, &ctx->scan_scratch64, &ctx->packed};
     for (DeviceBuffer *b : bufs)
         b->release();
     if (ctx->own_stream)
@@ -461,7 +569,103 @@ int mraygb_stage_reconstruct(mraygb_context *ctx, const mraygb_camera *cam, cons
                            d_rgba, d_rgba8);
 }
 
+int mraygb_stage_prediction_encode(mraygb_context *ctx, int width, int height, int m, const uint32_t *d_index,
+                                   float *d_data, uint64_t data_size, int coding_warp, float bias,
+                                   uint16_t *d_coding_params)
+{
+    CHECK_CTX();
+    int rc = check_image(ctx, width, height, m);
+    if (rc)
+        return rc;
+    if (!d_index || !d_data)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "prediction coding needs a compact image (index and data)");
+    if (coding_warp != MRAYGB_CODING_WARP_DEFAULT_TRANSFORMED && coding_warp != MRAYGB_CODING_WARP_NONE)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "unknown coding_warp %d", coding_warp);
+    if (coding_warp == MRAYGB_CODING_WARP_DEFAULT_TRANSFORMED && m > 1 && !d_coding_params)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "the default warp needs a coding parameter buffer");
+    return run_prediction_encode(ctx, width, height, m, d_index, d_data, data_size, coding_warp, bias,
+                                 d_coding_params);
+}
+
+int mraygb_stage_quantize_prediction_coding(mraygb_context *ctx, int width, int height, int m,
+                                            const uint32_t *d_index, const float *d_data, const uint8_t *h_table,
+                                            uint8_t *d_out, uint64_t capacity, uint64_t *h_nbytes)
+{
+    CHECK_CTX();
+    int rc = check_image(ctx, width, height, m);
+    if (rc)
+        return rc;
+    if (!d_index || !d_data || !d_out || !h_nbytes)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "NULL argument");
+    return run_quantize(ctx, width, height, m, d_index, d_data, h_table, d_out, capacity, h_nbytes);
+}
+
+int mraygb_stage_dequantize_prediction_coding(mraygb_context *ctx, int width, int height, int m,
+                                              const uint32_t *d_index, const uint8_t *h_table,
+                                              const uint8_t *d_bytes, uint64_t num_bytes, float *d_data)
+{
+    CHECK_CTX();
+    int rc = check_image(ctx, width, height, m);
+    if (rc)
+        return rc;
+    if (!d_index || !d_data || (!d_bytes && num_bytes))
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "NULL argument");
+    const int P = width * height;
+    const uint8_t *d_table;
+    const uint32_t *d_prefix;
+    if ((rc = upload_table(ctx, m, h_table, &d_table, &d_prefix)))
+        return rc;
+    uint64_t total_bits = 0;
+    if ((rc = run_bit_offsets(ctx, P, d_index, d_prefix, &total_bits)))
+        return rc;
+    CK(launch_unpack(P, d_index, d_table, d_prefix, ctx->bit_offset.as<unsigned long long>(), d_bytes, num_bytes,
+                     d_data, ctx->stream),
+       "unpack launch");
+    ctx->launches += 1;
+    return MRAYGB_OK;
+}
+
 // ---- drop-in host API -------------------------------------------------------------------------------------------
+
+int mraygb_quantize_prediction_coding(mraygb_context *ctx, int width, int height, int m, const uint32_t *h_index,
+                                      const float *h_data, uint64_t data_size, const uint8_t *h_table,
+                                      uint8_t *h_out, uint64_t capacity, uint64_t *h_nbytes)
+{
+    CHECK_CTX();
+    int rc = check_image(ctx, width, height, m);
+    if (rc)
+        return rc;
+    if (!h_index || (!h_data && data_size) || !h_nbytes)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "NULL argument");
+    const size_t P = (size_t)width * (size_t)height;
+    const size_t nd = data_size ? data_size : 1;
+    CK(ctx->index.reserve((P + 1) * sizeof(uint32_t)), "index buffer allocation");
+    CK(ctx->compact.reserve(nd * sizeof(float)), "moment buffer allocation");
+    CK(cudaMemcpyAsync(ctx->index.ptr, h_index, (P + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->stream),
+       "index upload");
+    if (data_size)
+        CK(cudaMemcpyAsync(ctx->compact.ptr, h_data, data_size * sizeof(float), cudaMemcpyHostToDevice, ctx->stream),
+           "moment upload");
+    // upper bound of the packed size: 32 bits per value
+    const uint64_t cap = (uint64_t)nd * 4 + 8;
+    CK(ctx->packed.reserve(cap), "packed buffer allocation");
+    uint64_t nbytes = 0;
+    rc = run_quantize(ctx, width, height, m, ctx->index.as<uint32_t>(), ctx->compact.as<float>(), h_table,
+                      ctx->packed.as<uint8_t>(), cap, &nbytes);
+    if (rc)
+        return rc;
+    *h_nbytes = nbytes;
+    if (h_out)
+    {
+        if (capacity < nbytes)
+            return fail(ctx, MRAYGB_INVALID_ARGUMENT, "output holds %llu bytes, %llu needed",
+                        (unsigned long long)capacity, (unsigned long long)nbytes);
+        if (nbytes)
+            CK(cudaMemcpyAsync(h_out, ctx->packed.ptr, nbytes, cudaMemcpyDeviceToHost, ctx->stream), "packed download");
+    }
+    CK(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+    return MRAYGB_OK;
+}
 
 int mraygb_generate(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_generation_params *gp, int width,
                     int height, int m, float *h_data, uint32_t *h_index, uint16_t *h_bounds, uint16_t *h_coding_params,
@@ -481,8 +685,10 @@ int mraygb_generate(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_
         return fail(ctx, MRAYGB_INVALID_ARGUMENT, "transform_to_bounds needs a bounds buffer");
     if (!ctx->has_grid)
         return fail(ctx, MRAYGB_NO_VOLUME, "no volume uploaded");
-    if (gp->prediction_coding)
-        return fail(ctx, MRAYGB_NOT_SUPPORTED, "prediction coding is not available in this build");
+    if (gp->prediction_coding && gp->coding_warp == MRAYGB_CODING_WARP_DEFAULT_TRANSFORMED && m > 1 &&
+        !h_coding_params)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "prediction coding with the default warp needs a coding "
+                                                  "parameter buffer");
 
     const size_t P = (size_t)width * (size_t)height;
     const size_t N = P * (size_t)m;
@@ -504,6 +710,18 @@ int mraygb_generate(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_
         if (rc)
             return rc;
         d_out = ctx->compact.as<float>();
+        if (gp->prediction_coding)
+        {
+            CK(ctx->coding_params.reserve(2 * (size_t)m * sizeof(uint16_t)), "coding parameter allocation");
+            rc = run_prediction_encode(ctx, width, height, m, ctx->index.as<uint32_t>(), ctx->compact.as<float>(),
+                                       size, gp->coding_warp, gp->bias, ctx->coding_params.as<uint16_t>());
+            if (rc)
+                return rc;
+            if (gp->coding_warp == MRAYGB_CODING_WARP_DEFAULT_TRANSFORMED && m > 1)
+                CK(cudaMemcpyAsync(h_coding_params, ctx->coding_params.ptr, 2 * (size_t)(m - 1) * sizeof(uint16_t),
+                                   cudaMemcpyDeviceToHost, ctx->stream),
+                   "coding parameter download");
+        }
         CK(cudaMemcpyAsync(h_index, ctx->index.ptr, (P + 1) * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream),
            "index download");
     }
@@ -513,7 +731,6 @@ int mraygb_generate(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_
     if (gp->transform_to_bounds)
         CK(cudaMemcpyAsync(h_bounds, ctx->bounds.ptr, 2 * P * sizeof(uint16_t), cudaMemcpyDeviceToHost, ctx->stream),
            "bounds download");
-    (void)h_coding_params;
     CK(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
     *h_data_size = size;
     return check_device_error_flag(ctx);

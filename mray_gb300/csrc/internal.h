@@ -22,6 +22,9 @@ cudaError_t mese_init_constants();
 // determine_best_number_moments for every pixel whose count is non-zero (error threshold > 0)
 cudaError_t launch_count_moments(int num_pixels, int m, float error_threshold, const float *moments,
                                  uint32_t *counts, cudaStream_t stream);
+// per-pixel part of prediction coding, in place on the compact moment data
+cudaError_t launch_prediction_encode(int num_pixels, int m, const uint32_t *index, float *data, float bias,
+                                     cudaStream_t stream);
 // Lagrange multipliers; fp64 selects the FP64 form
 cudaError_t launch_prepare(int num_pixels, int m, const uint32_t *index, const float *data, int prediction_code,
                            int coding_warp, const uint16_t *coding_params, float bias, bool fp64, float *pmoments,
@@ -32,8 +35,25 @@ cudaError_t launch_prepare(int num_pixels, int m, const uint32_t *index, const f
 size_t scan_scratch_words(size_t n);
 cudaError_t launch_exclusive_scan(const uint32_t *counts, uint32_t *out, size_t n, uint32_t *scratch,
                                   cudaStream_t stream, int *launches);
+cudaError_t launch_exclusive_scan_u64(const unsigned long long *in, unsigned long long *out, size_t n,
+                                      unsigned long long *scratch, cudaStream_t stream, int *launches);
 cudaError_t launch_compact_copy(int num_pixels, int m, const uint32_t *counts, const uint32_t *index,
                                 const float *moments, float *compact, cudaStream_t stream);
+
+// coding.cu
+int coding_minmax_blocks(int num_pixels);
+cudaError_t launch_coding_params(int num_pixels, int m, const uint32_t *index, const float *data, uint64_t total,
+                                 float2 *partial, uint16_t *params_u16, float *params_f, cudaStream_t stream);
+cudaError_t launch_coding_warp(int num_pixels, const uint32_t *index, float *data, int warp_type,
+                               const float *params, cudaStream_t stream);
+cudaError_t launch_pixel_bits(int num_pixels, const uint32_t *index, const uint32_t *prefix_bits,
+                              unsigned long long *bits, cudaStream_t stream);
+cudaError_t launch_pack(int num_pixels, const uint32_t *index, const float *data, const uint8_t *table,
+                        const uint32_t *prefix_bits, const unsigned long long *bit_offset, uint32_t *words,
+                        cudaStream_t stream);
+cudaError_t launch_unpack(int num_pixels, const uint32_t *index, const uint8_t *table, const uint32_t *prefix_bits,
+                          const unsigned long long *bit_offset, const uint8_t *bytes, unsigned long long num_bytes,
+                          float *data, cudaStream_t stream);
 
 // reconstruct.cu
 struct ReconArgs

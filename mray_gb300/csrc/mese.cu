@@ -161,6 +161,38 @@ __global__ void __launch_bounds__(128) count_moments_kernel(int num_pixels, int 
     counts[p] = (uint32_t)n;
 }
 
+// MomentImageHost::prediction_encode, per-pixel part (moment_image.cpp:103-126): bias lerp, trigonometric ->
+// exponential moments, encode, projection of the residuals to the real line; in place
+template <int MAXM>
+__global__ void __launch_bounds__(128) prediction_encode_kernel(int num_pixels, int m,
+                                                                const uint32_t *__restrict__ index,
+                                                                float *__restrict__ data, float bias)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= num_pixels)
+        return;
+    size_t idx;
+    int n;
+    pixel_span(index, m, p, idx, n);
+    if (n <= 0)
+        return;
+    if (n > MAXM)
+        n = MAXM;
+    float *d = data + idx;
+    d[0] = (1 - bias) * d[0] + bias * 0.5f; // cut::lerp(data[idx], 0.5f, bias)
+    for (int i = 1; i < n; ++i)
+        d[i] = (1 - bias) * d[i] + bias * 0.0f;
+    cx<float> e[MAXM], code[MAXM], poly[MAXM], tmp[MAXM];
+    trig_to_exp<float>(n, e, d, two_pi_over_l<float>());
+    pc_encode<float>(n, e, code, poly, tmp);
+    // transform_quantization_real (moment_prediction_coding.h:81-92): out[0] = c_0 stays d[0]
+    const cx<float> axis = mk(-code[0].y, code[0].x);
+    const float len = sqrtf(cabs2(axis));
+    const cx<float> inv_axis = cdiv(mk(len, 0.f), axis);
+    for (int l = 1; l < n; ++l)
+        d[l] = cmulc(code[l], inv_axis).x;
+}
+
 template <typename T, int MAXM>
 cudaError_t launch_prepare_t(int num_pixels, int m, const uint32_t *index, const float *data, int pc, int warp,
                              const uint16_t *cp, float bias, float *out, cudaStream_t stream)
@@ -216,6 +248,22 @@ cudaError_t launch_count_moments(int num_pixels, int m, float thr, const float *
         count_moments_kernel<128><<<grid, block, 0, stream>>>(num_pixels, m, thr, moments, counts);
     else
         count_moments_kernel<256><<<grid, block, 0, stream>>>(num_pixels, m, thr, moments, counts);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_prediction_encode(int num_pixels, int m, const uint32_t *index, float *data, float bias,
+                                     cudaStream_t stream)
+{
+    const int block = 128;
+    const int grid = (num_pixels + block - 1) / block;
+    if (m <= 32)
+        prediction_encode_kernel<32><<<grid, block, 0, stream>>>(num_pixels, m, index, data, bias);
+    else if (m <= 64)
+        prediction_encode_kernel<64><<<grid, block, 0, stream>>>(num_pixels, m, index, data, bias);
+    else if (m <= 128)
+        prediction_encode_kernel<128><<<grid, block, 0, stream>>>(num_pixels, m, index, data, bias);
+    else
+        prediction_encode_kernel<256><<<grid, block, 0, stream>>>(num_pixels, m, index, data, bias);
     return cudaGetLastError();
 }
 

@@ -17,12 +17,12 @@ constexpr int kThreads = 256;
 constexpr int kItems = 8;
 constexpr int kTile = kThreads * kItems;
 
-__device__ __forceinline__ uint32_t warp_inclusive_scan(uint32_t v, int lane)
+template <typename T> __device__ __forceinline__ T warp_inclusive_scan(T v, int lane)
 {
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1)
     {
-        uint32_t u = __shfl_up_sync(0xffffffffu, v, d);
+        T u = __shfl_up_sync(0xffffffffu, v, d);
         if (lane >= d)
             v += u;
     }
@@ -30,32 +30,33 @@ __device__ __forceinline__ uint32_t warp_inclusive_scan(uint32_t v, int lane)
 }
 
 // block-wide exclusive scan of one value per thread; returns the exclusive prefix, total in *total
-__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t *total)
+template <typename T> __device__ __forceinline__ T block_exclusive_scan(T v, T *total)
 {
-    __shared__ uint32_t warp_sums[kThreads / 32];
+    __shared__ T warp_sums[kThreads / 32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint32_t inc = warp_inclusive_scan(v, lane);
+    const T inc = warp_inclusive_scan<T>(v, lane);
     if (lane == 31)
         warp_sums[warp] = inc;
     __syncthreads();
     if (warp == 0)
     {
-        uint32_t s = lane < kThreads / 32 ? warp_sums[lane] : 0u;
-        s = warp_inclusive_scan(s, lane);
+        T s = lane < kThreads / 32 ? warp_sums[lane] : T(0);
+        s = warp_inclusive_scan<T>(s, lane);
         if (lane < kThreads / 32)
             warp_sums[lane] = s;
     }
     __syncthreads();
-    const uint32_t warp_prefix = warp == 0 ? 0u : warp_sums[warp - 1];
+    const T warp_prefix = warp == 0 ? T(0) : warp_sums[warp - 1];
     *total = warp_sums[kThreads / 32 - 1];
     return warp_prefix + inc - v;
 }
 
-__global__ void __launch_bounds__(kThreads) tile_reduce_kernel(const uint32_t *__restrict__ in, size_t n,
-                                                               uint32_t *__restrict__ sums)
+template <typename T>
+__global__ void __launch_bounds__(kThreads) tile_reduce_kernel(const T *__restrict__ in, size_t n,
+                                                               T *__restrict__ sums)
 {
     const size_t base = (size_t)blockIdx.x * kTile;
-    uint32_t s = 0;
+    T s = 0;
 #pragma unroll
     for (int k = 0; k < kItems; ++k)
     {
@@ -63,38 +64,38 @@ __global__ void __launch_bounds__(kThreads) tile_reduce_kernel(const uint32_t *_
         if (i < n)
             s += in[i];
     }
-    uint32_t total;
-    block_exclusive_scan(s, &total);
+    T total;
+    block_exclusive_scan<T>(s, &total);
     if (threadIdx.x == 0)
         sums[blockIdx.x] = total;
 }
 
 // exclusive scan of one tile plus its offset; the block holding the last element also writes out[n]
-__global__ void __launch_bounds__(kThreads) tile_scan_kernel(const uint32_t *__restrict__ in, size_t n,
-                                                             const uint32_t *__restrict__ offsets,
-                                                             uint32_t *__restrict__ out)
+template <typename T>
+__global__ void __launch_bounds__(kThreads) tile_scan_kernel(const T *__restrict__ in, size_t n,
+                                                             const T *__restrict__ offsets, T *__restrict__ out)
 {
-    __shared__ uint32_t tile[kTile];
+    __shared__ T tile[kTile];
     const size_t base = (size_t)blockIdx.x * kTile;
 #pragma unroll
     for (int k = 0; k < kItems; ++k)
     {
         const int li = k * kThreads + threadIdx.x;
         const size_t i = base + li;
-        tile[li] = i < n ? in[i] : 0u;
+        tile[li] = i < n ? in[i] : T(0);
     }
     __syncthreads();
-    uint32_t v[kItems];
-    uint32_t s = 0;
+    T v[kItems];
+    T s = 0;
 #pragma unroll
     for (int k = 0; k < kItems; ++k)
     {
         v[k] = tile[threadIdx.x * kItems + k];
         s += v[k];
     }
-    uint32_t total;
-    uint32_t prefix = block_exclusive_scan(s, &total);
-    const uint32_t off = offsets ? offsets[blockIdx.x] : 0u;
+    T total;
+    T prefix = block_exclusive_scan<T>(s, &total);
+    const T off = offsets ? offsets[blockIdx.x] : T(0);
     prefix += off;
     __syncthreads();
 #pragma unroll
@@ -139,34 +140,46 @@ size_t scan_scratch_words(size_t n)
     return nb + (nb + 1) + scan_scratch_words(nb);
 }
 
-cudaError_t launch_exclusive_scan(const uint32_t *counts, uint32_t *out, size_t n, uint32_t *scratch,
-                                  cudaStream_t stream, int *launches)
+template <typename T>
+cudaError_t exclusive_scan_t(const T *counts, T *out, size_t n, T *scratch, cudaStream_t stream, int *launches)
 {
     if (n == 0)
-        return cudaMemsetAsync(out, 0, sizeof(uint32_t), stream);
+        return cudaMemsetAsync(out, 0, sizeof(T), stream);
     const size_t nb = (n + kTile - 1) / kTile;
     if (nb == 1)
     {
-        tile_scan_kernel<<<1, kThreads, 0, stream>>>(counts, n, nullptr, out);
+        tile_scan_kernel<T><<<1, kThreads, 0, stream>>>(counts, n, nullptr, out);
         if (launches)
             *launches += 1;
         return cudaGetLastError();
     }
-    uint32_t *sums = scratch;
-    uint32_t *offs = scratch + nb;
-    tile_reduce_kernel<<<(unsigned)nb, kThreads, 0, stream>>>(counts, n, sums);
+    T *sums = scratch;
+    T *offs = scratch + nb;
+    tile_reduce_kernel<T><<<(unsigned)nb, kThreads, 0, stream>>>(counts, n, sums);
     if (launches)
         *launches += 1;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess)
         return e;
-    e = launch_exclusive_scan(sums, offs, nb, scratch + nb + (nb + 1), stream, launches);
+    e = exclusive_scan_t<T>(sums, offs, nb, scratch + nb + (nb + 1), stream, launches);
     if (e != cudaSuccess)
         return e;
-    tile_scan_kernel<<<(unsigned)nb, kThreads, 0, stream>>>(counts, n, offs, out);
+    tile_scan_kernel<T><<<(unsigned)nb, kThreads, 0, stream>>>(counts, n, offs, out);
     if (launches)
         *launches += 1;
     return cudaGetLastError();
+}
+
+cudaError_t launch_exclusive_scan(const uint32_t *counts, uint32_t *out, size_t n, uint32_t *scratch,
+                                  cudaStream_t stream, int *launches)
+{
+    return exclusive_scan_t<uint32_t>(counts, out, n, scratch, stream, launches);
+}
+
+cudaError_t launch_exclusive_scan_u64(const unsigned long long *in, unsigned long long *out, size_t n,
+                                      unsigned long long *scratch, cudaStream_t stream, int *launches)
+{
+    return exclusive_scan_t<unsigned long long>(in, out, n, scratch, stream, launches);
 }
 
 cudaError_t launch_compact_copy(int num_pixels, int m, const uint32_t *counts, const uint32_t *index,

@@ -258,6 +258,25 @@ class Context:
                                                _hptr(img.rgba)))
         return img
 
+    def quantize_prediction_coding(self, mi: MomentImageHost, table) -> np.ndarray:
+        """quantize_prediction_coding(mi, table) (moment_quantization.cpp:239-276): the packed code bytes."""
+        if not mi.is_compact:
+            raise ValueError("quantize_prediction_coding needs a compact moment image")
+        t = np.ascontiguousarray(table, dtype=np.uint8)
+        if t.size < mi.num_moments:
+            raise ValueError("the quantization table needs one entry per moment index")
+        data = np.ascontiguousarray(mi.data, dtype=np.float32)
+        index = np.ascontiguousarray(mi.index, dtype=np.uint32)
+        n = C.c_uint64()
+        self._check(self._L.mraygb_quantize_prediction_coding(self._h, mi.width, mi.height, mi.num_moments,
+                                                              _hptr(index), _hptr(data), data.size, _hptr(t), None,
+                                                              0, C.byref(n)))
+        out = np.zeros(max(n.value, 1), dtype=np.uint8)
+        self._check(self._L.mraygb_quantize_prediction_coding(self._h, mi.width, mi.height, mi.num_moments,
+                                                              _hptr(index), _hptr(data), data.size, _hptr(t),
+                                                              _hptr(out), out.size, C.byref(n)))
+        return out[:n.value]
+
     # ---- stage calls on device pointers ----
     def stage_generate_moments(self, cam, gp, width, height, num_moments, moments, bounds=None, counts=None):
         self._check(self._L.mraygb_stage_generate_moments(self._h, C.byref(cam), C.byref(gp), width, height,
@@ -271,6 +290,30 @@ class Context:
         self._check(self._L.mraygb_stage_compact(self._h, width, height, num_moments, _dptr(counts), _dptr(moments),
                                                  _dptr(index), _dptr(compact), int(capacity), C.byref(total)))
         return int(total.value)
+
+    def stage_prediction_encode(self, width, height, num_moments, index, data, data_size, coding_warp=0,
+                                bias=1e-4, coding_params=None):
+        self._check(self._L.mraygb_stage_prediction_encode(self._h, width, height, num_moments, _dptr(index),
+                                                           _dptr(data), int(data_size), int(coding_warp),
+                                                           float(bias), _dptr(coding_params)))
+
+    def stage_quantize_prediction_coding(self, width, height, num_moments, index, data, table, out,
+                                         capacity=None) -> int:
+        t = np.ascontiguousarray(table, dtype=np.uint8)
+        n = C.c_uint64()
+        if capacity is None:
+            capacity = out.numel() * out.element_size()
+        self._check(self._L.mraygb_stage_quantize_prediction_coding(self._h, width, height, num_moments,
+                                                                    _dptr(index), _dptr(data), _hptr(t), _dptr(out),
+                                                                    int(capacity), C.byref(n)))
+        return int(n.value)
+
+    def stage_dequantize_prediction_coding(self, width, height, num_moments, index, table, packed, num_bytes,
+                                           data):
+        t = np.ascontiguousarray(table, dtype=np.uint8)
+        self._check(self._L.mraygb_stage_dequantize_prediction_coding(self._h, width, height, num_moments,
+                                                                      _dptr(index), _hptr(t), _dptr(packed),
+                                                                      int(num_bytes), _dptr(data)))
 
     def stage_prepare_moments(self, width, height, num_moments, index, data, pmoments, prediction_code=False,
                               coding_warp=0, coding_params=None, bias=1e-6):
@@ -303,6 +346,17 @@ def generate(cam: Camera, volume: RegularGrid, mi: MomentImageHost, params: Gene
     out = ctx.generate(cam, params, mi.width, mi.height, mi.num_moments, out=mi)
     mi.domain_min, mi.domain_max = volume.domain_min, volume.domain_max
     assert out is mi
+
+
+def quantize_prediction_coding(mi: MomentImageHost, table, context: Optional[Context] = None) -> np.ndarray:
+    """moment_quantization::quantize_prediction_coding(mi, table) on the GPU."""
+    return (context or default_context()).quantize_prediction_coding(mi, table)
+
+
+def default_quantization_table(num_moments: int, num_bits: int) -> np.ndarray:
+    """get_prediction_coding_quantization_table without a loaded table (moment_quantization.cpp:186-203):
+    16 bits for index 0, num_bits for the rest."""
+    return np.array([16] + [num_bits] * (num_moments - 1), dtype=np.uint8)[:num_moments]
 
 
 def reconstruct(cam: Camera, mi: MomentImageHost, tf: TransferFunction, img: ColorImageHost,

@@ -326,6 +326,10 @@ void ref_transform_quantization_real(int n, const float *code, float c0, float *
 {
     transform_quantization_real(n, const_cast<float_complex *>(reinterpret_cast<const float_complex *>(code)), c0, out);
 }
+void ref_transform_quantization_real_warp(int n, float *inout, int warp, const float *params)
+{
+    transform_quantization_real_warp(n, inout, WarpParameters{warp, params});
+}
 void ref_transform_dequantization_real(int n, const float *in, float *code, int warp, const float *params)
 {
     transform_dequantization_real(n, in, reinterpret_cast<float_complex *>(code), WarpParameters{warp, params});

@@ -1,0 +1,332 @@
+"""Writes the golden fixtures of tests/golden/ from the reference's OWN CPU implementation.
+
+The reference (TobiasRp/mray) is compiled from its sources by oracle/Makefile (`make ref`, sources under
+/root/reference/src) into oracle/_ref/libmrayref.so together with a small C-ABI harness.  This script calls it
+on seeded inputs and stores inputs and outputs as small .npz files:
+
+  known_answers.npz   the inputs of the reference's own unit tests (tests/test_mese.cpp, test_prediction_coding.cpp,
+                      test_coding_transform.cpp, test_moment_compaction.cpp) with the outputs of the dynamic MESE
+                      code and of the independent fixed-size MESE code (mese/MESE_4_10.h) they compare against
+  probes.npz          euler_exp / exp(-x) as the reference's build evaluates them, TF tables and samples,
+                      grid samples and eye rays
+  pipeline_ml.npz     generate() -> (compaction, prediction coding) -> prepare -> reconstruct on a Marschner-Lobb
+                      64^3 volume, 48x40 orthographic image, 16 moments
+  pipeline_mix.npz    the same on a 40^3 mixing layer, 32x32 perspective image, 64 moments
+  quantize.npz        quantize_prediction_coding of a ragged compact image under several bit tables
+
+Run from the repository root:  python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import oracle as O  # noqa: E402
+from mray_gb300 import workloads as W  # noqa: E402
+
+P = lambda a: None if a is None else a.ctypes.data_as(C.c_void_p)  # noqa: E731
+
+
+def f32(*v):
+    return np.array(v, dtype=np.float32)
+
+
+def cplx(values):
+    a = np.zeros(2 * len(values), dtype=np.float32)
+    for i, v in enumerate(values):
+        a[2 * i], a[2 * i + 1] = np.float32(complex(v).real), np.float32(complex(v).imag)
+    return a
+
+
+def declare(ref):
+    ref.ref_evaluate_mese.restype = C.c_float
+    ref.ref_evaluate_mese.argtypes = [C.c_int, C.c_float, C.c_void_p]
+    ref.ref_fixed_evaluate_lagrange.restype = C.c_float
+    ref.ref_fixed_evaluate_lagrange.argtypes = [C.c_int, C.c_float, C.c_void_p]
+    ref.ref_fast_atan.restype = C.c_float
+    ref.ref_fast_atan.argtypes = [C.c_float]
+    ref.ref_rmse.restype = C.c_float
+    ref.ref_rmse.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+    ref.ref_determine_best_number_moments.argtypes = [C.c_int, C.c_void_p, C.c_float]
+    ref.ref_transform_quantization_real.argtypes = [C.c_int, C.c_void_p, C.c_float, C.c_void_p]
+    ref.ref_euler_exp.argtypes = [C.c_float, C.c_void_p]
+    ref.ref_exp_overload.restype = C.c_float
+    ref.ref_exp_overload.argtypes = [C.c_float]
+    ref.ref_grid_sample.restype = C.c_float
+    ref.ref_preintegrate.argtypes = [C.c_void_p, C.c_float, C.c_void_p]
+    ref.ref_tf_sample.argtypes = [C.c_void_p, C.c_float, C.c_float, C.c_void_p]
+    ref.ref_tf_sample.restype = C.c_float
+    ref.ref_quantize_prediction_coding.restype = C.c_uint64
+    ref.ref_generate_grid.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p,
+                                      C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                      C.c_void_p, C.c_void_p, C.c_void_p]
+    for name in ("ref_reconstruct_float", "ref_reconstruct_u8"):
+        getattr(ref, name).argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                       C.c_uint64, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                       C.c_void_p, C.c_void_p]
+    ref.ref_prepare_moments.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_uint64, C.c_int,
+                                        C.c_int, C.c_void_p, C.c_float, C.c_void_p]
+    ref.ref_prediction_encode.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_uint64, C.c_int,
+                                          C.c_float, C.c_void_p]
+    ref.ref_find_coding_transform_parameters.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                                         C.c_uint64, C.c_void_p]
+    ref.ref_quantize_prediction_coding.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_uint64,
+                                                   C.c_void_p, C.c_void_p]
+
+
+def known_answers(ref):
+    out = {}
+    # tests/test_mese.cpp:31-57: fixed (MESE_4_10) vs dynamic preparation and evaluation at p = -pi/2
+    for name, mom in (("m4", f32(0.5, 0.25, 0.25, 0.1)),
+                      ("m10", f32(0.22008814, 0.0, 0.01400074, 0.00271224, 0.00426201, 0, 0, 0, 0, 0))):
+        n = mom.size
+        pm_fixed = np.zeros(n, np.float32)
+        ref.ref_fixed_prepare_lagrange(n, P(mom), P(pm_fixed))
+        pm_dyn = np.zeros(n, np.float32)
+        ref.ref_prepare_lagrange(n, P(mom), P(pm_dyn))
+        p = np.float32(-np.pi + np.pi * 0.5)
+        out[f"mese_{name}_moments"] = mom
+        out[f"mese_{name}_lagrange_fixed"] = pm_fixed
+        out[f"mese_{name}_lagrange_dynamic"] = pm_dyn
+        out[f"mese_{name}_value_fixed"] = np.float32(ref.ref_fixed_evaluate_lagrange(n, p, P(pm_fixed)))
+        out[f"mese_{name}_value_dynamic"] = np.float32(ref.ref_evaluate_mese(n, p, P(pm_fixed)))
+        e_fixed = np.zeros(2 * n, np.float32)
+        ref.ref_fixed_trig_to_exp(n, P(mom), P(e_fixed))
+        e_dyn = np.zeros(2 * n, np.float32)
+        ref.ref_trig_to_exp(n, P(mom), P(e_dyn))
+        out[f"mese_{name}_exp_fixed"] = e_fixed
+        out[f"mese_{name}_exp_dynamic"] = e_dyn
+        sol_fixed = np.zeros(2 * n, np.float32)
+        ref.ref_fixed_levinson(n, P(e_fixed), P(sol_fixed))
+        sol_dyn = np.zeros(2 * n, np.float32)
+        ref.ref_levinson(n, P(e_fixed), P(sol_dyn))
+        out[f"mese_{name}_levinson_fixed"] = sol_fixed
+        out[f"mese_{name}_levinson_dynamic"] = sol_dyn
+    # tests/test_mese.cpp:185-206: the 4-moment preparation compared with the fixed-size code
+    prep4 = f32(0.22008814, 0.0, 0.01400074, 0.00271224)
+    pf = np.zeros(4, np.float32)
+    ref.ref_fixed_prepare_lagrange(4, P(prep4), P(pf))
+    pd = np.zeros(4, np.float32)
+    ref.ref_prepare_lagrange(4, P(prep4), P(pd))
+    out.update(prep4_moments=prep4, prep4_fixed=pf, prep4_dynamic=pd)
+    # tests/test_mese.cpp:59-75 and 115-133: exponential moments and Levinson on the same 4 moments
+    ef = np.zeros(8, np.float32)
+    ref.ref_fixed_trig_to_exp(4, P(prep4), P(ef))
+    ed = np.zeros(8, np.float32)
+    ref.ref_trig_to_exp(4, P(prep4), P(ed))
+    lf = np.zeros(8, np.float32)
+    ref.ref_fixed_levinson(4, P(ef), P(lf))
+    ld = np.zeros(8, np.float32)
+    ref.ref_levinson(4, P(ef), P(ld))
+    out.update(prep4_exp_fixed=ef, prep4_exp_dynamic=ed, prep4_levinson_fixed=lf, prep4_levinson_dynamic=ld)
+    # tests/test_mese.cpp:94-113: 28-moment exp <-> trig round trip
+    trig28 = f32(5.2070445e-01, 7.4165657e-02, -1.3283056e-02, 1.2487045e-02, 1.3437086e-02, -9.5647079e-04,
+                 -1.2216626e-03, 2.1146263e-03, -5.4606516e-04, 1.0199437e-02, 1.1894707e-02, -1.9188672e-02,
+                 -5.5241492e-03, 2.8166445e-02, 6.7452774e-03, -1.9198583e-02, 4.3223342e-03, -6.1640824e-04,
+                 7.8988671e-03, 2.4080461e-02, -9.6553434e-03, -1.9514188e-02, 1.1532067e-02, -4.1229022e-03,
+                 2.3510400e-02, 1.7623754e-02, -1.4590423e-02, 1.1135901e-03)
+    e28 = np.zeros(56, np.float32)
+    ref.ref_trig_to_exp(28, P(trig28), P(e28))
+    t28 = np.zeros(56, np.float32)
+    ref.ref_exp_to_trig(28, P(e28), P(t28))
+    out["roundtrip28_trig"], out["roundtrip28_exp"], out["roundtrip28_back"] = trig28, e28, t28
+    # tests/test_mese.cpp:135-183: correlations on "any random signal"
+    sig = cplx([2, 4, 8, 16])
+    rhs = cplx([1, 42, 0.1, 0.2])
+    a = np.zeros(8, np.float32)
+    ref.ref_autocorrelation(4, P(sig), P(a))
+    c = np.zeros(8, np.float32)
+    ref.ref_correlation(4, P(sig), P(rhs), P(c))
+    ic = np.zeros(4, np.float32)
+    ref.ref_imaginary_correlation(4, P(sig), P(rhs), P(ic))
+    out.update(corr_lhs=sig, corr_rhs=rhs, autocorr=a, corr=c, imag_corr=ic)
+    # tests/test_prediction_coding.cpp:30-100: encode / decode / real projection
+    for name, trig in (("pc5", f32(0.22, 0.0, 0.014, 0.0027, 0.004)),
+                       ("pc5b", f32(0.22008814, 0.0, 0.01400074, 0.00271224, 0.00426201))):
+        n = trig.size
+        e = np.zeros(2 * n, np.float32)
+        ref.ref_trig_to_exp(n, P(trig), P(e))
+        code = np.zeros(2 * n, np.float32)
+        ref.ref_encode(n, P(e), P(code))
+        dec = np.zeros(2 * n, np.float32)
+        poly = np.zeros(2 * n, np.float32)
+        ref.ref_decode(n, P(code), P(dec), P(poly))
+        real = np.zeros(n, np.float32)
+        ref.ref_transform_quantization_real(n, P(code), trig[0], P(real))
+        warped = real.copy()
+        ref.ref_transform_quantization_real_warp(n, P(warped), 1, None)
+        back = np.zeros(2 * n, np.float32)
+        ref.ref_transform_dequantization_real(n, P(warped), P(back), 1, None)
+        out.update({f"{name}_trig": trig, f"{name}_exp": e, f"{name}_code": code, f"{name}_decoded": dec,
+                    f"{name}_decoded_poly": poly, f"{name}_real": real, f"{name}_warped_none": warped,
+                    f"{name}_back_warp_none": back})
+    # tests/test_coding_transform.cpp:32-62: ramp x/15 - 0.6 over 16 pixels x 10 moments -> (0.6, 0.5)
+    w, h, m = 16, 1, 10
+    counts = np.full(w * h, m, np.uint32)
+    raw = np.repeat((np.arange(w, dtype=np.float32) / np.float32(w - 1) - np.float32(0.6)), m).astype(np.float32)
+    index = np.zeros(w * h + 1, np.uint32)
+    index[1:] = np.cumsum(counts)
+    params = np.zeros(2 * (m - 1), np.float32)
+    ref.ref_find_coding_transform_parameters(w, h, m, P(index), P(raw), raw.size, P(params))
+    out.update(ramp_index=index, ramp_data=raw, ramp_params=params)
+    # tests/test_moment_compaction.cpp:30-66: extrapolated tail rmse for n = 2 and n = 8
+    trig10 = f32(1.9176584e-01, -3.7339486e-02, -1.4143054e-02, -1.6614912e-02, -2.2262430e-02, -1.2005451e-02,
+                 -7.5180288e-03, 2.5505440e-02, 2.8378680e-02, 1.6212923e-02)
+    e10 = np.zeros(20, np.float32)
+    ref.ref_trig_to_exp(10, P(trig10), P(e10))
+    out["compaction_trig"], out["compaction_exp"] = trig10, e10
+    for n in (2, 8):
+        ext = np.zeros(20, np.float32)
+        ref.ref_evaluate_unknown_moments(n, P(e10), 10, P(ext))
+        b = np.zeros(20, np.float32)
+        b[0:2 * n:2] = trig10[:n]
+        ref.ref_exponential_to_bounded_moments(10, P(ext), P(b), n)
+        out[f"compaction_ext{n}"] = ext
+        out[f"compaction_bounded{n}"] = b
+        out[f"compaction_rmse{n}"] = np.float32(ref.ref_rmse(n, 10, P(b), P(trig10)))
+    for thr in (0.0, 0.05, 0.01, 0.001):
+        out[f"compaction_best_{thr}"] = np.int32(ref.ref_determine_best_number_moments(10, P(trig10), thr))
+    xs = np.linspace(-40, 40, 801).astype(np.float32)
+    out["fast_atan_x"] = xs
+    out["fast_atan_y"] = np.array([ref.ref_fast_atan(float(x)) for x in xs], np.float32)
+    return out
+
+
+def probes(ref):
+    out = {}
+    rng = np.random.default_rng(0)
+    xs = rng.uniform(-200, 0, 4000).astype(np.float32)
+    e = np.zeros((xs.size, 2), np.float32)
+    for i, x in enumerate(xs):
+        ref.ref_euler_exp(float(x), P(e[i]))
+    out["euler_x"], out["euler_y"] = xs, e
+    ts = rng.uniform(0, 20, 2000).astype(np.float32)
+    out["exp_x"] = ts
+    out["exp_y"] = np.array([ref.ref_exp_overload(float(t)) for t in ts], np.float32)
+    tf1d = W.transfer_function(7)
+    row = np.zeros((256, 4), np.float32)
+    same = ref.ref_preintegrate(P(tf1d), C.c_float(0.05), P(row))
+    out["tf1d"], out["tf_row"], out["tf_rows_equal"] = tf1d, row, np.int32(same)
+    fb = rng.uniform(-0.05, 1.05, size=(500, 2)).astype(np.float32)
+    s = np.zeros((500, 4), np.float32)
+    for i in range(500):
+        ref.ref_tf_sample(P(row), float(fb[i, 0]), float(fb[i, 1]), P(s[i]))
+    out["tf_fs_bs"], out["tf_samples"] = fb, s
+    vol = W.marschner_lobb(16)
+    pts = rng.uniform(-1.2, 1.2, size=(800, 3)).astype(np.float32)
+    dmin, dmax = f32(-1, -1, -1), f32(1, 1, 1)
+    ref.ref_grid_sample.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+    out["grid_points"] = pts
+    out["grid_samples"] = np.array([ref.ref_grid_sample(P(vol), 16, 16, 16, P(dmin), P(dmax), P(p)) for p in pts],
+                                   np.float32)
+    rays = []
+    for cam in (W.ortho_camera(11), W.perspective_camera((1.9, -1.1, 1.45), (0, 0, 0), 38.0, 1.0)):
+        r = np.zeros((12, 9, 8), np.float32)
+        hits = np.zeros((12, 9), np.int32)
+        ref.ref_eye_ray.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                    C.c_void_p]
+        for y in range(9):
+            for x in range(12):
+                hits[x, y] = ref.ref_eye_ray(C.byref(cam), x, y, 12, 9, P(dmin), P(dmax), P(r[x, y]))
+        rays.append((r, hits))
+    out["rays_ortho"], out["hits_ortho"] = rays[0]
+    out["rays_persp"], out["hits_persp"] = rays[1]
+    return out
+
+
+def pipeline(ref, wl):
+    out = {}
+    Wd, H, m = wl.width, wl.height, wl.num_moments
+    vol = np.ascontiguousarray(wl.volume)
+    nz, ny, nx = vol.shape
+    dmin, dmax = f32(*wl.domain_min), f32(*wl.domain_max)
+    tf = np.zeros((256, 4), np.float32)
+    ref.ref_preintegrate(P(np.ascontiguousarray(wl.tf1d)), C.c_float(wl.tf_step), P(tf))
+    out["tf_table"] = tf
+    for pc in (0, 1):
+        wl.gen.prediction_coding = pc
+        data = np.zeros(Wd * H * m, np.float32)
+        index = np.zeros(Wd * H + 1, np.uint32)
+        bounds = np.zeros(2 * Wd * H, np.uint16)
+        cp = np.zeros(2 * m, np.uint16)
+        size = C.c_uint64()
+        flags = np.zeros(4, np.int32)
+        ref.ref_generate_grid(C.byref(wl.camera), C.byref(wl.gen), P(vol), nx, ny, nz, P(dmin), P(dmax), Wd, H, m,
+                              P(data), P(index), P(bounds), P(cp), C.byref(size), P(flags))
+        data = data[:size.value].copy()
+        key = f"pc{pc}"
+        out[f"{key}_index"], out[f"{key}_bounds"], out[f"{key}_data"] = index, bounds, data
+        if pc:
+            out[f"{key}_coding_params"] = cp[:2 * (m - 1)].copy()
+        cpp = cp if pc else None
+        pm = np.zeros(max(data.size, 1), np.float32)
+        ref.ref_prepare_moments(Wd, H, m, P(index), P(data), data.size, pc, 0, P(cpp), C.c_float(wl.rec.bias), P(pm))
+        out[f"{key}_pmoments"] = pm[:data.size]
+        rgba = np.zeros((H, Wd, 4), np.float32)
+        ref.ref_reconstruct_float(C.byref(wl.camera), C.byref(wl.rec), Wd, H, m, P(index), P(data), data.size,
+                                  P(bounds), pc, 0, P(cpp), P(dmin), P(dmax), P(tf), P(rgba))
+        out[f"{key}_rgba"] = rgba
+        u8 = np.zeros((H, Wd, 4), np.uint8)
+        ref.ref_reconstruct_u8(C.byref(wl.camera), C.byref(wl.rec), Wd, H, m, P(index), P(data), data.size,
+                               P(bounds), pc, 0, P(cpp), P(dmin), P(dmax), P(tf), P(u8))
+        out[f"{key}_rgba8"] = u8
+        if pc:
+            table = np.array([16] + [10] * (m - 1), np.uint8)
+            n = ref.ref_quantize_prediction_coding(Wd, H, m, P(index), P(data), data.size, P(table), None)
+            q = np.zeros(max(n, 1), np.uint8)
+            ref.ref_quantize_prediction_coding(Wd, H, m, P(index), P(data), data.size, P(table), P(q))
+            out[f"{key}_codes_16_10"] = q[:n]
+    wl.gen.prediction_coding = 0
+    return out
+
+
+def quantize(ref):
+    out = {}
+    rng = np.random.default_rng(42)
+    Wd, H, m = 23, 11, 12
+    counts = rng.integers(0, m + 1, size=Wd * H).astype(np.uint32)
+    index = np.zeros(Wd * H + 1, np.uint32)
+    index[1:] = np.cumsum(counts)
+    vals = rng.uniform(-0.1, 1.1, size=int(index[-1])).astype(np.float32)
+    vals[::7] = 1.0
+    vals[::11] = 0.0
+    out["index"], out["values"] = index, vals
+    tables = {"t16_10": [16] + [10] * (m - 1), "t_ragged": [16] + [5 + i for i in range(m - 1)],
+              "t32": [32] * m, "t_odd": [13] + [3] * (m - 1)}
+    for name, t in tables.items():
+        t = np.array(t, np.uint8)
+        n = ref.ref_quantize_prediction_coding(Wd, H, m, P(index), P(vals), vals.size, P(t), None)
+        q = np.zeros(max(n, 1), np.uint8)
+        ref.ref_quantize_prediction_coding(Wd, H, m, P(index), P(vals), vals.size, P(t), P(q))
+        out[f"{name}_table"], out[f"{name}_bytes"] = t, q[:n]
+    out["shape"] = np.array([Wd, H, m], np.int32)
+    return out
+
+
+def main():
+    ref = O.ref_lib()
+    if ref is None:
+        raise SystemExit("the reference sources are not available; cannot write golden fixtures")
+    declare(ref)
+    np.savez_compressed(os.path.join(HERE, "known_answers.npz"), **known_answers(ref))
+    np.savez_compressed(os.path.join(HERE, "probes.npz"), **probes(ref))
+    ml = W.ml_workload(n=64, width=48, height=40, num_moments=16, seed=11, name="golden_ml")
+    np.savez_compressed(os.path.join(HERE, "pipeline_ml.npz"), **pipeline(ref, ml))
+    mix = W.mixing_layer_workload(n=40, width=32, height=32, num_moments=64, modes=16, seed=5, name="golden_mix")
+    np.savez_compressed(os.path.join(HERE, "pipeline_mix.npz"), **pipeline(ref, mix))
+    np.savez_compressed(os.path.join(HERE, "quantize.npz"), **quantize(ref))
+    for f in sorted(os.listdir(HERE)):
+        if f.endswith(".npz"):
+            print(f, os.path.getsize(os.path.join(HERE, f)))
+
+
+if __name__ == "__main__":
+    main()

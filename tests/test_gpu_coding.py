@@ -1,0 +1,176 @@
+"""GPU prediction coding, coding parameters, quantization and bit packing against the oracle.
+
+Bar: codes and packed bytes bit-identical to the reference's packer for the same prediction-coded floats;
+coding parameters (u16) identical; the encoded floats within 1e-5 absolute (only cosf / sinf rounding differs).
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from helpers import small_mixing, small_ml
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+def _dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).to("cuda")
+
+
+def _ragged_image(seed=0, width=40, height=24, m=16):
+    """A compact image with random per-pixel counts 0..m (the error-threshold compaction case), from real
+    moments of the Marschner-Lobb case."""
+    wl = small_ml(width, height, m, seed=seed + 3)
+    mo, b, c = O.generate_moments(wl.camera, wl.gen, wl.volume, wl.domain_min, wl.domain_max, width, height, m, "f32")
+    rng = np.random.default_rng(seed)
+    counts = np.where(c > 0, rng.integers(0, m + 1, size=c.shape), 0).astype(np.uint32)
+    index, data = O.compact(counts, mo)
+    return width, height, m, index, data
+
+
+def _encode_gpu(ctx, W, H, m, index, data, warp, bias):
+    d_idx = _dev(index.view(np.int32))
+    d_data = _dev(data)
+    d_cp = torch.zeros(max(2 * (m - 1), 1), dtype=torch.int16, device="cuda")
+    ctx.stage_prediction_encode(W, H, m, d_idx, d_data, data.size, coding_warp=warp, bias=bias, coding_params=d_cp)
+    ctx.synchronize()
+    return d_data.cpu().numpy(), d_cp.cpu().numpy().view(np.uint16)[:2 * (m - 1)]
+
+
+@pytest.mark.parametrize("warp", [0, 1])
+@pytest.mark.parametrize("ragged_seed", [None, 1, 2])
+def test_prediction_encode_matches_oracle(gpu_context, warp, ragged_seed):
+    if ragged_seed is None:
+        wl = small_ml(96, 80, 31)
+        mi = O.workload_generate(wl, "f32")
+        W, H, m, index, data = wl.width, wl.height, wl.num_moments, mi["index"], mi["data"]
+    else:
+        W, H, m, index, data = _ragged_image(ragged_seed)
+    bias = 5e-5
+    ours, cp = _encode_gpu(gpu_context, W, H, m, index, data, warp, bias)
+    ref, cp_ref = O.prediction_encode(W, H, m, index, data, warp, bias)
+    assert np.abs(ours.astype(np.float64) - ref).max() <= 1e-5
+    if warp == 0:
+        # the parameters come from exact min / max reductions of the encoded residuals
+        assert np.abs(cp.astype(int) - cp_ref.astype(int)).max() <= 1
+        assert np.mean(cp == cp_ref) >= 0.9
+    # 10-bit codes of the two encodings: differences only where a float sits on a code boundary
+    table = O.default_quantization_table(m, 10)
+    a = O.quantize_prediction_coding(W, H, m, index, ours, table)
+    b = O.quantize_prediction_coding(W, H, m, index, ref, table)
+    assert a.size == b.size
+
+
+TABLES = {
+    "16_10": lambda m: O.default_quantization_table(m, 10),
+    "16_12": lambda m: O.default_quantization_table(m, 12),
+    "ragged_bits": lambda m: np.array([16] + [8 + (i % 9) for i in range(1, m)], dtype=np.uint8)[:m],
+    "32": lambda m: np.full(m, 32, dtype=np.uint8),
+    "odd": lambda m: np.array([13] + [7] * (m - 1), dtype=np.uint8)[:m],
+}
+
+
+@pytest.mark.parametrize("table_name", list(TABLES))
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_quantize_pack_bit_exact(gpu_context, table_name, seed):
+    """Same prediction-coded floats in: identical codes and identical packed bytes (the trailing partial byte
+    dropped as the reference's packer does)."""
+    W, H, m, index, data = _ragged_image(seed)
+    rng = np.random.default_rng(seed)
+    # values around [0, 1] including the clamp edges and exact code boundaries
+    vals = rng.uniform(-0.1, 1.1, size=data.size).astype(np.float32)
+    vals[::17] = 0.0
+    vals[::19] = 1.0
+    vals[::23] = np.float32(511) / np.float32(1023)
+    table = TABLES[table_name](m)
+    ref = O.quantize_prediction_coding(W, H, m, index, vals, table)
+    d_out = torch.zeros(vals.size * 4 + 16, dtype=torch.uint8, device="cuda")
+    n = gpu_context.stage_quantize_prediction_coding(W, H, m, _dev(index.view(np.int32)), _dev(vals), table, d_out)
+    gpu_context.synchronize()
+    assert n == ref.size
+    assert np.array_equal(d_out.cpu().numpy()[:n], ref)
+
+
+@pytest.mark.parametrize("table_name", ["16_10", "ragged_bits", "32"])
+def test_dequantize_round_trip(gpu_context, table_name):
+    W, H, m, index, data = _ragged_image(4)
+    rng = np.random.default_rng(4)
+    vals = rng.uniform(0.0, 1.0, size=data.size).astype(np.float32)
+    table = TABLES[table_name](m)
+    packed = O.quantize_prediction_coding(W, H, m, index, vals, table)
+    ref = O.dequantize_prediction_coding(W, H, m, index, table, packed, vals.size)
+    d_out = torch.zeros(max(vals.size, 1), dtype=torch.float32, device="cuda")
+    d_packed = _dev(np.concatenate([packed, np.zeros(8, np.uint8)]))
+    gpu_context.stage_dequantize_prediction_coding(W, H, m, _dev(index.view(np.int32)), table, d_packed, packed.size,
+                                                   d_out)
+    gpu_context.synchronize()
+    assert np.array_equal(d_out.cpu().numpy()[:vals.size], ref)
+
+
+def test_quantize_host_api_matches_reference_packer(gpu_context):
+    import mray_gb300 as M
+
+    W, H, m, index, data = _ragged_image(5)
+    mi = M.MomentImageHost(W, H, m, True)
+    mi.is_compact, mi.prediction_code = True, True
+    mi.index, mi.data = index, np.clip(data, 0, 1).astype(np.float32)
+    table = M.default_quantization_table(m, 10)
+    ours = M.quantize_prediction_coding(mi, table, context=gpu_context)
+    assert np.array_equal(ours, O.quantize_prediction_coding(W, H, m, index, mi.data, table))
+
+
+@pytest.mark.parametrize("warp", [0, 1])
+def test_dropin_generate_prediction_coded_then_reconstruct(gpu_context, warp):
+    """generate with prediction_coding (the reference's default), codes at 10 bits, reconstruct from the
+    prediction-coded image; compared with the reference method end to end."""
+    import mray_gb300 as M
+
+    wl = small_ml(96, 80, 31)
+    wl.gen.prediction_coding = 1
+    wl.gen.coding_warp = warp
+    grid = M.RegularGrid(wl.volume, wl.domain_min, wl.domain_max)
+    mi = M.MomentImageHost(wl.width, wl.height, wl.num_moments, True, True)
+    M.generate(wl.camera, grid, mi, wl.gen, context=gpu_context)
+    ref = O.workload_generate(wl, "f32")
+    assert mi.prediction_code and np.array_equal(mi.index, ref["index"])
+    if warp == 0:
+        assert np.abs(mi.coding_params.astype(int) - ref["coding_params"].astype(int)).max() <= 1
+    assert np.abs(mi.data.astype(np.float64) - ref["data"]).max() <= 2e-4
+    table = M.default_quantization_table(wl.num_moments, 10)
+    codes = M.quantize_prediction_coding(mi, table, context=gpu_context)
+    codes_ref = O.quantize_prediction_coding(wl.width, wl.height, wl.num_moments, ref["index"], ref["data"], table)
+    assert codes.size == codes_ref.size
+    # end-to-end code agreement (moments differ from the reference's by its own FP32 rounding)
+    assert np.mean(codes == codes_ref) >= 0.99
+    # reconstruct from the prediction-coded image (prepare_moments_from_pred_coding)
+    tf = M.preintegrate(wl.tf1d, wl.tf_step)
+    img = M.ColorImageHost(wl.width, wl.height)
+    M.reconstruct(wl.camera, mi, tf, img, wl.rec, context=gpu_context)
+    rgba_ref = O.workload_reconstruct(wl, ref, "f32")
+    diff = np.abs(img.rgba_float - rgba_ref).max(axis=-1)
+    assert np.quantile(diff, 0.999) <= 1e-3
+    assert diff.max() <= 2e-2
+
+
+def test_prepare_from_prediction_coding_same_input(gpu_context):
+    """prepare_moments_from_pred_coding on the same prediction-coded floats: the re-march matches the oracle."""
+    wl = small_ml(64, 48, 16)
+    wl.gen.prediction_coding = 1
+    ref = O.workload_generate(wl, "f32")
+    W, H, m = wl.width, wl.height, wl.num_moments
+    tf = O.preintegrate(wl.tf1d, wl.tf_step)
+    gpu_context.upload_tf(tf)
+    d_idx = _dev(ref["index"].view(np.int32))
+    d_data = _dev(ref["data"])
+    d_pm = torch.zeros_like(d_data)
+    d_cp = _dev(ref["coding_params"].view(np.int16))
+    gpu_context.stage_prepare_moments(W, H, m, d_idx, d_data, d_pm, prediction_code=True, coding_warp=0,
+                                      coding_params=d_cp, bias=wl.rec.bias)
+    gpu_context.synchronize()
+    pm_ref = O.prepare_moments(W, H, m, ref["index"], ref["data"], True, 0, ref["coding_params"], wl.rec.bias)
+    pm = d_pm.cpu().numpy()
+    rgba = O.reconstruct(wl.camera, wl.rec, W, H, m, wl.domain_min, wl.domain_max, ref["index"], pm, ref["bounds"],
+                         tf, "f32")
+    rgba_ref = O.reconstruct(wl.camera, wl.rec, W, H, m, wl.domain_min, wl.domain_max, ref["index"], pm_ref,
+                             ref["bounds"], tf, "f32")
+    assert np.abs(rgba - rgba_ref).max() <= 1e-3

@@ -66,8 +66,17 @@ def test_generate_moments_match_oracle(gpu_context, case, transform):
     assert np.array_equal(c, ref_c)
     hit = ref_c > 0
     assert hit.sum() > 0
-    err = moment_rel_err(mo, ref_m, ref_m[..., 0])[hit]
-    assert err.max() <= MOMENT_TOL, f"max rel err {err.max():.3e}"
+    # Against the reference's FP32 moments: within 1e-4 relative, widened per pixel by the reference's own
+    # FP32 rounding error (its distance to the FP64 evaluation of the same method).  On long noisy rays that
+    # error alone exceeds 1e-4 (the reference differences two O(S/j^2) terms per step); these kernels stay
+    # within 1e-4 of the FP64 result there.
+    ref64, _, _ = O.generate_moments(wl.camera, wl.gen, wl.volume, wl.domain_min, wl.domain_max, wl.width,
+                                     wl.height, wl.num_moments, "f64")
+    own = moment_rel_err(ref_m, ref64, ref64[..., 0])
+    err = moment_rel_err(mo, ref_m, ref_m[..., 0])
+    assert np.all(err[hit] <= MOMENT_TOL + own[hit]), f"max excess {(err - own)[hit].max():.3e}"
+    err64 = moment_rel_err(mo, ref64, ref64[..., 0])[hit]
+    assert err64.max() <= MOMENT_TOL, f"max rel err vs f64 {err64.max():.3e}"
     # missed rays carry zero moments
     assert np.all(mo[~hit] == 0.0)
 

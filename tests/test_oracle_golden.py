@@ -1,0 +1,314 @@
+"""The oracle pinned to the reference's own CPU implementation (CPU only).
+
+The fixtures in tests/golden/ were written by tests/golden/make_golden.py from the reference compiled from its
+sources.  The oracle's f32 body must reproduce them bit for bit (it performs the reference's float operations in
+the reference's order, built without contraction); the assertions of the reference's own unit tests are
+re-checked on the same inputs.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+from mray_gb300 import workloads as W
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def load(name):
+    return np.load(os.path.join(GOLDEN, name))
+
+
+def P(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+@pytest.fixture(scope="module")
+def L():
+    return O.lib()
+
+
+@pytest.fixture(scope="module")
+def ka():
+    return load("known_answers.npz")
+
+
+# ---- tests/test_mese.cpp ------------------------------------------------------------------------------------
+
+@pytest.mark.parametrize("name", ["m4", "m10"])
+def test_mese_prepare_and_evaluate(L, ka, name):
+    mom = ka[f"mese_{name}_moments"]
+    n = mom.size
+    pm = np.zeros(n, np.float32)
+    L.oracle_prepare_lagrange_f32(n, P(mom), P(pm))
+    assert np.array_equal(pm, ka[f"mese_{name}_lagrange_dynamic"])
+    # test_mese.cpp:31-57: the fixed-size code and the dynamic code agree on the value (ASSERT_FLOAT_EQ)
+    p = np.float32(-np.pi + np.pi * 0.5)
+    v = L.oracle_evaluate_mese_f32(n, float(p), P(ka[f"mese_{name}_lagrange_fixed"]), 0)
+    assert np.float32(v) == ka[f"mese_{name}_value_dynamic"]
+    assert abs(float(ka[f"mese_{name}_value_fixed"]) - float(v)) <= 4 * np.spacing(np.float32(v))
+
+
+def test_mese_prepare_against_fixed_size_code(L, ka):
+    """test_mese.cpp:185-206: the dynamic preparation within 1e-2 of the fixed-size code."""
+    mom = ka["prep4_moments"]
+    pm = np.zeros(4, np.float32)
+    L.oracle_prepare_lagrange_f32(4, P(mom), P(pm))
+    assert np.array_equal(pm, ka["prep4_dynamic"])
+    assert np.abs(pm - ka["prep4_fixed"]).max() < 1e-2
+
+
+@pytest.mark.parametrize("name", ["m4", "m10"])
+def test_trig_to_exp_and_levinson_pinned(L, ka, name):
+    mom = ka[f"mese_{name}_moments"]
+    n = mom.size
+    e = np.zeros(2 * n, np.float32)
+    L.oracle_trig_to_exp_f32(n, P(mom), P(e))
+    assert np.array_equal(e, ka[f"mese_{name}_exp_dynamic"])
+    sol = np.zeros(2 * n, np.float32)
+    L.oracle_levinson_f32(n, P(ka[f"mese_{name}_exp_fixed"]), P(sol))
+    assert np.array_equal(sol, ka[f"mese_{name}_levinson_dynamic"])
+
+
+def test_trig_to_exp_and_levinson_against_fixed_size_code(L, ka):
+    """test_mese.cpp:59-75 (exponential moments, ASSERT_FLOAT_EQ) and :115-133 (Levinson within 1e-2)."""
+    mom = ka["prep4_moments"]
+    e = np.zeros(8, np.float32)
+    L.oracle_trig_to_exp_f32(4, P(mom), P(e))
+    assert np.array_equal(e, ka["prep4_exp_dynamic"])
+    fixed = ka["prep4_exp_fixed"]
+    assert np.all(np.abs(e - fixed) <= 4 * np.spacing(np.maximum(np.abs(e), np.abs(fixed))))
+    sol = np.zeros(8, np.float32)
+    L.oracle_levinson_f32(4, P(fixed), P(sol))
+    assert np.array_equal(sol, ka["prep4_levinson_dynamic"])
+    assert np.abs(sol - ka["prep4_levinson_fixed"]).max() < 1e-2
+
+
+def test_exp_trig_round_trip(L, ka):
+    trig = ka["roundtrip28_trig"]
+    e = np.zeros(56, np.float32)
+    L.oracle_trig_to_exp_f32(28, P(trig), P(e))
+    assert np.array_equal(e, ka["roundtrip28_exp"])
+    back = np.zeros(56, np.float32)
+    L.oracle_exp_to_trig_f32(28, P(e), P(back))
+    assert np.array_equal(back, ka["roundtrip28_back"])
+    assert np.abs(back[0::2] - trig).max() < 0.01  # test_mese.cpp:111-112
+
+
+def test_correlations(L, ka):
+    lhs, rhs = ka["corr_lhs"], ka["corr_rhs"]
+    a = np.zeros(8, np.float32)
+    L.oracle_autocorrelation_f32(4, P(lhs), P(a))
+    c = np.zeros(8, np.float32)
+    L.oracle_correlation_f32(4, P(lhs), P(rhs), P(c))
+    ic = np.zeros(4, np.float32)
+    L.oracle_imaginary_correlation_f32(4, P(lhs), P(rhs), P(ic))
+    assert np.array_equal(a, ka["autocorr"])
+    assert np.array_equal(c, ka["corr"])
+    assert np.array_equal(ic, ka["imag_corr"])
+
+
+def test_fast_atan(L, ka):
+    ys = np.array([L.oracle_fast_atan_f32(float(x)) for x in ka["fast_atan_x"]], np.float32)
+    assert np.array_equal(ys, ka["fast_atan_y"])
+    # "maximal absolute error around 1.1e-5" (complex_algebra.h:133); measured 1.21e-5
+    assert np.abs(ys.astype(np.float64) - np.arctan(ka["fast_atan_x"].astype(np.float64))).max() < 1.25e-5
+
+
+# ---- tests/test_prediction_coding.cpp -----------------------------------------------------------------------
+
+@pytest.mark.parametrize("name", ["pc5", "pc5b"])
+def test_prediction_coding_round_trip(L, ka, name):
+    trig = ka[f"{name}_trig"]
+    n = trig.size
+    e = np.zeros(2 * n, np.float32)
+    L.oracle_trig_to_exp_f32(n, P(trig), P(e))
+    assert np.array_equal(e, ka[f"{name}_exp"])
+    code = np.zeros(2 * n, np.float32)
+    L.oracle_encode_f32(n, P(e), P(code))
+    assert np.array_equal(code, ka[f"{name}_code"])
+    dec = np.zeros(2 * n, np.float32)
+    poly = np.zeros(2 * n, np.float32)
+    L.oracle_decode_f32(n, P(code), P(dec), P(poly))
+    assert np.array_equal(dec, ka[f"{name}_decoded"])
+    assert np.array_equal(poly, ka[f"{name}_decoded_poly"])
+    # test_prediction_coding.cpp:59-66: decoded exponential moments within 1e-6, m_1 = 0 stays exactly 0
+    assert np.abs(dec - e).max() <= 1e-6
+    if trig[1] == 0:
+        assert e[2] == 0 and e[3] == 0 and code[2] == 0 and code[3] == 0
+    real = np.zeros(n, np.float32)
+    L.oracle_transform_quantization_real_f32(n, P(code), float(trig[0]), P(real))
+    assert np.array_equal(real, ka[f"{name}_real"])
+    # transform_quantization_real_warp with CODING_WARP_NONE: x * 0.5 + 0.5, clamped to [0, 1]
+    warped = real.copy()
+    warped[1:] = np.clip(real[1:] * np.float32(0.5) + np.float32(0.5), 0, 1)
+    assert np.array_equal(warped, ka[f"{name}_warped_none"])
+    back = np.zeros(2 * n, np.float32)
+    L.oracle_transform_dequantization_real_f32(n, P(warped), P(back), 1, None)
+    assert np.array_equal(back, ka[f"{name}_back_warp_none"])
+    # test_prediction_coding.cpp:93-99: the real projection round trip within 1e-7 (indices >= 1)
+    assert np.abs(back[2:] - code[2:]).max() <= 1e-7
+
+
+# ---- tests/test_coding_transform.cpp ------------------------------------------------------------------------
+
+def test_coding_transform_known_answer(ka):
+    params = O.find_coding_transform_parameters(16, 1, 10, ka["ramp_index"], ka["ramp_data"])
+    assert np.array_equal(params, ka["ramp_params"])
+    assert np.abs(params[0::2] - 0.6).max() < 1e-6 and np.abs(params[1::2] - 0.5).max() < 1e-6
+
+
+# ---- tests/test_moment_compaction.cpp -----------------------------------------------------------------------
+
+def test_compaction_rrmse(L, ka):
+    trig, e = ka["compaction_trig"], ka["compaction_exp"]
+    got = np.zeros(20, np.float32)
+    L.oracle_trig_to_exp_f32(10, P(trig), P(got))
+    assert np.array_equal(got, e)
+    rm = {}
+    for n in (2, 8):
+        ext = np.zeros(20, np.float32)
+        L.oracle_evaluate_unknown_moments_f32(n, P(e), 10, P(ext))
+        assert np.array_equal(ext, ka[f"compaction_ext{n}"])
+        b = np.zeros(20, np.float32)
+        b[0:2 * n:2] = trig[:n]
+        L.oracle_exponential_to_bounded_moments_f32(10, P(ext), P(b), n)
+        assert np.array_equal(b, ka[f"compaction_bounded{n}"])
+        rm[n] = np.float32(L.oracle_rmse_f32(n, 10, P(b), P(trig)))
+        assert rm[n] == ka[f"compaction_rmse{n}"]
+    assert rm[8] < rm[2]  # test_moment_compaction.cpp:62
+    for thr in (0.0, 0.05, 0.01, 0.001):
+        assert L.oracle_determine_best_number_moments_f32(10, P(trig), thr) == int(ka[f"compaction_best_{thr}"])
+
+
+# ---- tests/test_moment_image.cpp ----------------------------------------------------------------------------
+
+def test_compaction_index_arithmetic():
+    """test_moment_image.cpp:31-63: counts x per pixel of an 8x4 image with 10 moments."""
+    w, h, m = 8, 4, 10
+    counts = np.tile(np.arange(w, dtype=np.uint32), h).reshape(h, w)
+    mo = np.zeros((h, w, m), np.float32)
+    for x in range(w):
+        mo[:, x, :x] = x / 8.0
+    index, data = O.compact(counts, mo)
+    assert data.size == counts.sum()
+    assert np.array_equal(np.diff(index.astype(np.int64)).reshape(h, w), counts.astype(np.int64))
+    assert index[1] == 0 and index[2] == 1 and index[3] == 3 and index[4] == 6
+
+
+def test_quantize_dequantize_16bit():
+    """test_moment_image.cpp:153-184: 16-bit prediction-coding quantization round trip within 1e-2."""
+    w, h, m = 8, 4, 10
+    counts = np.array([[x + 1 if x > 0 else 0 for x in range(w)]] * h, np.uint32)
+    mo = np.zeros((h, w, m), np.float32)
+    for x in range(w):
+        mo[:, x, :x] = x / 8.0
+    index, data = O.compact(counts, mo)
+    table = O.default_quantization_table(m, 16)
+    q = O.quantize_prediction_coding(w, h, m, index, data, table)
+    back = O.dequantize_prediction_coding(w, h, m, index, table, q, data.size)
+    for y in range(h):
+        for x in range(w):
+            i0 = index[y * w + x]
+            for l in range(x):
+                assert abs(back[i0 + l] - x / 8.0) < 1e-2
+
+
+# ---- probes: overload choices, TF, sampling, rays -------------------------------------------------------------
+
+def test_probes_match_reference_build():
+    pr = load("probes.npz")
+    L = O.lib()
+    e = np.zeros(2, np.float32)
+    for x, ref in zip(pr["euler_x"], pr["euler_y"]):
+        L.oracle_euler_exp_f32(C.c_float(x), P(e))
+        assert np.array_equal(e, ref)
+    table = O.preintegrate(pr["tf1d"], 0.05)
+    assert np.array_equal(table, pr["tf_row"]) and int(pr["tf_rows_equal"]) == 1
+    out = np.zeros(4, np.float32)
+    L.oracle_tf_sample_f32.argtypes = [C.c_void_p, C.c_float, C.c_float, C.c_void_p]
+    for (fs, bs), ref in zip(pr["tf_fs_bs"], pr["tf_samples"]):
+        L.oracle_tf_sample_f32(P(table), fs, bs, P(out))
+        assert np.array_equal(out, ref)
+    vol = W.marschner_lobb(16)
+    g, keep = O._grid(vol, (-1, -1, -1), (1, 1, 1))
+    for p, ref in zip(pr["grid_points"], pr["grid_samples"]):
+        assert np.float32(L.oracle_grid_sample_f32(C.byref(g), P(np.ascontiguousarray(p)))) == ref
+
+
+def test_eye_rays_match_reference_build():
+    pr = load("probes.npz")
+    L = O.lib()
+    L.oracle_eye_ray_f32.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+    L.oracle_intersect_aabb_f32.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    dmin = np.array([-1, -1, -1], np.float32)
+    dmax = np.array([1, 1, 1], np.float32)
+    for key, cam in (("ortho", W.ortho_camera(11)),
+                     ("persp", W.perspective_camera((1.9, -1.1, 1.45), (0, 0, 0), 38.0, 1.0))):
+        rays, hits = pr[f"rays_{key}"], pr[f"hits_{key}"]
+        o = np.zeros(3, np.float32)
+        d = np.zeros(3, np.float32)
+        tn = C.c_float()
+        tf = C.c_float()
+        for y in range(9):
+            for x in range(12):
+                L.oracle_eye_ray_f32(C.byref(cam), x, y, 12, 9, P(o), P(d))
+                hit = L.oracle_intersect_aabb_f32(P(o), P(d), P(dmin), P(dmax), C.byref(tn), C.byref(tf))
+                assert np.array_equal(o, rays[x, y, :3]) and np.array_equal(d, rays[x, y, 3:6])
+                assert hit == hits[x, y]
+                assert np.float32(tn.value) == rays[x, y, 6] and np.float32(tf.value) == rays[x, y, 7]
+
+
+# ---- whole pipeline ------------------------------------------------------------------------------------------
+
+@pytest.mark.parametrize("fixture,kind", [("pipeline_ml.npz", "ml"), ("pipeline_mix.npz", "mix")])
+def test_pipeline_bit_exact(fixture, kind):
+    g = load(fixture)
+    if kind == "ml":
+        wl = W.ml_workload(n=64, width=48, height=40, num_moments=16, seed=11, name="golden_ml")
+    else:
+        wl = W.mixing_layer_workload(n=40, width=32, height=32, num_moments=64, modes=16, seed=5, name="golden_mix")
+    tf = O.preintegrate(wl.tf1d, wl.tf_step)
+    assert np.array_equal(tf, g["tf_table"])
+    for pc in (0, 1):
+        wl.gen.prediction_coding = pc
+        mi = O.workload_generate(wl, "f32")
+        k = f"pc{pc}"
+        assert np.array_equal(mi["index"], g[f"{k}_index"])
+        assert np.array_equal(mi["bounds"].reshape(-1), g[f"{k}_bounds"])
+        assert np.array_equal(mi["data"], g[f"{k}_data"])
+        if pc:
+            assert np.array_equal(mi["coding_params"], g[f"{k}_coding_params"])
+        pm = O.prepare_moments(wl.width, wl.height, wl.num_moments, mi["index"], mi["data"], bool(pc), 0,
+                               mi["coding_params"], wl.rec.bias, "f32")
+        assert np.array_equal(pm, g[f"{k}_pmoments"])
+        rgba = O.reconstruct(wl.camera, wl.rec, wl.width, wl.height, wl.num_moments, wl.domain_min, wl.domain_max,
+                             mi["index"], pm, mi["bounds"], tf, "f32")
+        assert np.array_equal(rgba, g[f"{k}_rgba"])
+        assert np.array_equal(O.rgba_to_u8(rgba), g[f"{k}_rgba8"])
+        if pc:
+            table = O.default_quantization_table(wl.num_moments, 10)
+            q = O.quantize_prediction_coding(wl.width, wl.height, wl.num_moments, mi["index"], mi["data"], table)
+            assert np.array_equal(q, g[f"{k}_codes_16_10"])
+
+
+def test_quantize_tables_bit_exact():
+    g = load("quantize.npz")
+    Wd, H, m = (int(v) for v in g["shape"])
+    for name in ("t16_10", "t_ragged", "t32", "t_odd"):
+        q = O.quantize_prediction_coding(Wd, H, m, g["index"], g["values"], g[f"{name}_table"])
+        assert np.array_equal(q, g[f"{name}_bytes"]), name
+
+
+def test_fp64_oracle_agrees_with_fp32_on_smooth_case():
+    """The f64 body is the same method: on the smooth Marschner-Lobb case the reference's FP32 moments sit within
+    1e-4 (relative to m_0) of it."""
+    wl = W.ml_workload(n=64, width=48, height=40, num_moments=16, seed=11)
+    m32, b32, c32 = O.generate_moments(wl.camera, wl.gen, wl.volume, wl.domain_min, wl.domain_max, 48, 40, 16, "f32")
+    m64, b64, c64 = O.generate_moments(wl.camera, wl.gen, wl.volume, wl.domain_min, wl.domain_max, 48, 40, 16, "f64")
+    hit = c32 > 0
+    assert np.array_equal(c32, c64)
+    err = np.abs(m32 - m64).max(axis=-1) / np.maximum(np.abs(m64[..., 0]), 1e-3)
+    assert err[hit].max() < 1e-4
