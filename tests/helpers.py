@@ -21,3 +21,19 @@ def small_mixing(width=64, height=64, m=64, n=96, seed=21):
     from mray_gb300 import workloads as W
 
     return W.mixing_layer_workload(n=n, width=width, height=height, num_moments=m, seed=seed)
+
+
+def rgba_agreement(ours: np.ndarray, ref32: np.ndarray, ref64: np.ndarray, tol: float = 1e-3) -> np.ndarray:
+    """Per pixel: True where the colour matches the reference's FP32 result within ``tol`` (max over channels), or,
+    where the reference's own FP32 result is further than ``tol`` from the FP64 evaluation of the same method, where
+    ours is at least as close to that FP64 value as the reference's is."""
+    d_ref = np.abs(ours.astype(np.float64) - ref32).max(axis=-1)
+    d_64 = np.abs(ours.astype(np.float64) - ref64).max(axis=-1)
+    own = np.abs(ref32.astype(np.float64) - ref64).max(axis=-1)
+    return (d_ref <= tol) | (d_64 <= np.maximum(tol, own))
+
+
+def moments_bounds_agree(b32: np.ndarray, b64: np.ndarray) -> np.ndarray:
+    """Pixels whose u16 density bounds agree between the FP32 and FP64 evaluations (the bounds are truncated to
+    u16, so a last-bit difference of the sampled extremes can move them one step)."""
+    return np.all(b32 == b64, axis=-1)

@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 import oracle as O
-from helpers import moment_rel_err, small_mixing, small_ml
+from helpers import moment_rel_err, moments_bounds_agree, rgba_agreement, small_mixing, small_ml
 
 torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
@@ -70,12 +70,13 @@ def test_generate_moments_match_oracle(gpu_context, case, transform):
     # FP32 rounding error (its distance to the FP64 evaluation of the same method).  On long noisy rays that
     # error alone exceeds 1e-4 (the reference differences two O(S/j^2) terms per step); these kernels stay
     # within 1e-4 of the FP64 result there.
-    ref64, _, _ = O.generate_moments(wl.camera, wl.gen, wl.volume, wl.domain_min, wl.domain_max, wl.width,
-                                     wl.height, wl.num_moments, "f64")
+    ref64, b64, _ = O.generate_moments(wl.camera, wl.gen, wl.volume, wl.domain_min, wl.domain_max, wl.width,
+                                       wl.height, wl.num_moments, "f64")
     own = moment_rel_err(ref_m, ref64, ref64[..., 0])
     err = moment_rel_err(mo, ref_m, ref_m[..., 0])
     assert np.all(err[hit] <= MOMENT_TOL + own[hit]), f"max excess {(err - own)[hit].max():.3e}"
-    err64 = moment_rel_err(mo, ref64, ref64[..., 0])[hit]
+    same = hit & (moments_bounds_agree(ref_b, b64) if transform else hit)
+    err64 = moment_rel_err(mo, ref64, ref64[..., 0])[same]
     assert err64.max() <= MOMENT_TOL, f"max rel err vs f64 {err64.max():.3e}"
     # missed rays carry zero moments
     assert np.all(mo[~hit] == 0.0)
@@ -87,10 +88,10 @@ def test_generate_moments_vs_fp64_oracle(gpu_context, case):
     import mray_gb300 as M
 
     wl = _case(case)
-    mo, _, c = _gpu_moments(gpu_context, wl, precision=M.PRECISION_COMPENSATED_FP64_MESE)
-    ref_m, _, ref_c = O.generate_moments(wl.camera, wl.gen, wl.volume, wl.domain_min, wl.domain_max, wl.width,
-                                         wl.height, wl.num_moments, "f64")
-    hit = (ref_c > 0) & (c > 0)
+    mo, b, c = _gpu_moments(gpu_context, wl, precision=M.PRECISION_COMPENSATED_FP64_MESE)
+    ref_m, ref_b, ref_c = O.generate_moments(wl.camera, wl.gen, wl.volume, wl.domain_min, wl.domain_max, wl.width,
+                                             wl.height, wl.num_moments, "f64")
+    hit = (ref_c > 0) & (c > 0) & moments_bounds_agree(b, ref_b)
     err = moment_rel_err(mo, ref_m, ref_m[..., 0])[hit]
     assert err.max() <= MOMENT_TOL, f"max rel err vs f64 {err.max():.3e}"
 
@@ -142,7 +143,7 @@ def _oracle_image(wl):
 
 @pytest.mark.parametrize("case", [CASES[0], CASES[1], CASES[3], CASES[4]], ids=lambda c: f"{c['kind']}-m{c['m']}")
 def test_prepare_and_reconstruct_from_same_moments(gpu_context, case):
-    """Same compact moment image in: GPU Lagrange multipliers + re-march against the oracle's."""
+    """Same compact moment image in: GPU Lagrange multipliers and re-march against the oracle's."""
     wl = _case(case)
     mi, tf = _oracle_image(wl)
     W, H, m = wl.width, wl.height, wl.num_moments
@@ -154,24 +155,44 @@ def test_prepare_and_reconstruct_from_same_moments(gpu_context, case):
     pm_ref = O.prepare_moments(W, H, m, mi["index"], mi["data"], bias=wl.rec.bias, precision="f32")
     d_b = _dev(mi["bounds"].reshape(-1).view(np.int16))
     d_rgba = torch.zeros(W * H * 4, dtype=torch.float32, device="cuda")
-    # re-march from the oracle's multipliers isolates the march
+
+    def oracle_march(pm, precision):
+        return O.reconstruct(wl.camera, wl.rec, W, H, m, wl.domain_min, wl.domain_max, mi["index"],
+                             pm.astype(np.float32 if precision == "f32" else np.float64), mi["bounds"], tf, precision)
+
+    # 1. the march alone, from the oracle's multipliers
     gpu_context.stage_reconstruct(wl.camera, wl.rec, W, H, m, wl.domain_min, wl.domain_max, d_idx, _dev(pm_ref), d_b,
                                   d_rgba)
     gpu_context.synchronize()
-    rgba_ref = O.reconstruct(wl.camera, wl.rec, W, H, m, wl.domain_min, wl.domain_max, mi["index"], pm_ref,
-                             mi["bounds"], tf, "f32")
     rgba = d_rgba.cpu().numpy().reshape(H, W, 4)
-    assert np.abs(rgba - rgba_ref).max() <= RGBA_TOL
-    # the multipliers: reference arithmetic, so only cosf/sinf rounding differs
-    pm = d_pm.cpu().numpy()
+    ok = rgba_agreement(rgba, oracle_march(pm_ref, "f32"), oracle_march(pm_ref, "f64"), RGBA_TOL)
+    assert ok.all(), f"{(~ok).sum()} pixels neither within 1e-3 of the reference nor closer to FP64"
+    # 2. the multipliers: the reference's arithmetic, so only cosf / sinf rounding differs
     gpu_context.stage_reconstruct(wl.camera, wl.rec, W, H, m, wl.domain_min, wl.domain_max, d_idx, d_pm, d_b, d_rgba)
     gpu_context.synchronize()
     rgba2 = d_rgba.cpu().numpy().reshape(H, W, 4)
-    rgba_ref2 = O.reconstruct(wl.camera, wl.rec, W, H, m, wl.domain_min, wl.domain_max, mi["index"], pm.astype(np.float32),
-                              mi["bounds"], tf, "f32")
-    assert np.abs(rgba2 - rgba_ref2).max() <= RGBA_TOL
+    pm = d_pm.cpu().numpy()
+    ok2 = rgba_agreement(rgba2, oracle_march(pm, "f32"), oracle_march(pm, "f64"), RGBA_TOL)
+    assert ok2.all()
     if m <= 31:
-        assert np.abs(rgba2 - rgba_ref).max() <= RGBA_TOL
+        # well-conditioned moment counts: the whole prepare + march within 1e-3 of the reference
+        assert np.abs(rgba2 - oracle_march(pm_ref, "f32")).max() <= RGBA_TOL
+
+
+def _full_oracle(wl):
+    """The reference's FP32 pipeline and the FP64 evaluation of the same method (same sample positions)."""
+    ref = O.workload_generate(wl, "f32")
+    rgba32 = O.workload_reconstruct(wl, ref, "f32")
+    m64, b64, c64 = O.generate_moments(wl.camera, wl.gen, wl.volume, wl.domain_min, wl.domain_max, wl.width,
+                                       wl.height, wl.num_moments, "f64")
+    idx64, _ = O.compact(c64, m64.astype(np.float32))
+    data64 = m64.reshape(-1, wl.num_moments)[c64.reshape(-1) > 0].reshape(-1)
+    pm64 = O.prepare_moments(wl.width, wl.height, wl.num_moments, idx64, data64.astype(np.float32), bias=wl.rec.bias,
+                             precision="f64")
+    tf = O.preintegrate(wl.tf1d, wl.tf_step)
+    rgba64 = O.reconstruct(wl.camera, wl.rec, wl.width, wl.height, wl.num_moments, wl.domain_min, wl.domain_max,
+                           idx64, pm64, b64, tf, "f64")
+    return ref, rgba32, rgba64
 
 
 def test_dropin_generate_reconstruct_ml(gpu_context):
@@ -182,7 +203,7 @@ def test_dropin_generate_reconstruct_ml(gpu_context):
     grid = M.RegularGrid(wl.volume, wl.domain_min, wl.domain_max)
     mi = M.MomentImageHost(wl.width, wl.height, wl.num_moments, True, True)
     M.generate(wl.camera, grid, mi, wl.gen, context=gpu_context)
-    ref = O.workload_generate(wl, "f32")
+    ref, rgba32, rgba64 = _full_oracle(wl)
     assert mi.is_compact and np.array_equal(mi.index, ref["index"])
     assert np.array_equal(mi.bounds.reshape(-1), ref["bounds"].reshape(-1))
     counts = np.diff(ref["index"].astype(np.int64)).reshape(wl.height, wl.width)
@@ -190,8 +211,7 @@ def test_dropin_generate_reconstruct_ml(gpu_context):
     theirs = np.zeros_like(ours)
     for arr, src in ((ours, mi.data), (theirs, ref["data"])):
         flat = arr.reshape(-1, wl.num_moments)
-        sel = counts.reshape(-1) > 0
-        flat[sel] = src.reshape(-1, wl.num_moments)
+        flat[counts.reshape(-1) > 0] = src.reshape(-1, wl.num_moments)
     err = moment_rel_err(ours, theirs, theirs[..., 0])[counts > 0]
     assert err.max() <= MOMENT_TOL
 
@@ -199,14 +219,10 @@ def test_dropin_generate_reconstruct_ml(gpu_context):
     assert np.array_equal(tf.table, O.preintegrate(wl.tf1d, wl.tf_step))
     img = M.ColorImageHost(wl.width, wl.height)
     M.reconstruct(wl.camera, mi, tf, img, wl.rec, context=gpu_context)
-    rgba_ref = O.workload_reconstruct(wl, ref, "f32")
-    diff = np.abs(img.rgba_float - rgba_ref)
-    # the moments differ from the reference's by the reference's own FP32 rounding (<= 1e-4 relative); MESE
-    # amplifies that in a few pixels, so the end-to-end colour is held to 1e-3 on 99.9 % of the pixels
-    assert np.quantile(diff.max(axis=-1), 0.999) <= RGBA_TOL
-    assert diff.max() <= 2e-2
-    u8_ref = O.rgba_to_u8(rgba_ref)
-    assert np.mean(np.abs(img.rgba.astype(int) - u8_ref.astype(int)) <= 1) >= 0.999
+    ok = rgba_agreement(img.rgba_float, rgba32, rgba64, RGBA_TOL)
+    assert ok.all(), f"{(~ok).sum()} pixels"
+    # the stored u8 colour: within one step of the reference's on 99.9 % of the channels
+    assert np.mean(np.abs(img.rgba.astype(int) - O.rgba_to_u8(rgba32).astype(int)) <= 1) >= 0.999
 
 
 def test_dropin_rejects_bad_arguments(gpu_context):
