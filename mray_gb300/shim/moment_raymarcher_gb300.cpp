@@ -1,0 +1,171 @@
+// Reference-side shim: the reference's CUDA seam (generate_device / reconstruct_device, declared in
+// src/moment_raymarcher.cuh:48-54) implemented over the mraygb C ABI.  A maintainer of the reference builds
+// this file in place of src/moment_raymarcher.cu's generate/reconstruct launchers and links libmraygb.so;
+// main.cpp, the CLI and eval/mray_cli.py stay unchanged.  It only converts containers and maps a failure
+// status to the reference's behaviour (a message and std::terminate, as CHECK_CUDA does).
+//
+// Compiled against the reference's headers only (tests/test_shim_compiles.py checks that it compiles).
+
+#include "moment_raymarcher.cuh"
+
+#include <cstdio>
+#include <exception>
+#include <mutex>
+
+#include "mraygb.h"
+
+namespace
+{
+
+mraygb_context *context()
+{
+    static mraygb_context *ctx = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        if (mraygb_create(0, &ctx) != MRAYGB_OK)
+        {
+            std::fprintf(stderr, "mraygb: cannot create a context on device 0\n");
+            std::terminate();
+        }
+    });
+    return ctx;
+}
+
+void check(int status)
+{
+    if (status != MRAYGB_OK)
+    {
+        std::fprintf(stderr, "mraygb error %d: %s\n", status, mraygb_last_error(context()));
+        std::terminate();
+    }
+}
+
+mraygb_camera to_c(const cut::Camera &c)
+{
+    mraygb_camera o{};
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j)
+            o.transform[i][j] = c.transform[i][j];
+    const Vec3f *v[4] = {&c.position, &c.right, &c.up, &c.dir};
+    float *d[4] = {o.position, o.right, o.up, o.dir};
+    for (int k = 0; k < 4; ++k)
+    {
+        d[k][0] = v[k]->x;
+        d[k][1] = v[k]->y;
+        d[k][2] = v[k]->z;
+    }
+    o.scale = c.scale;
+    o.aspect = c.aspect;
+    o.znear = c.znear;
+    o.orthographic = c.orthographic ? 1 : 0;
+    return o;
+}
+
+mraygb_generation_params to_c(const GenerationParameters &p)
+{
+    mraygb_generation_params o{};
+    o.step_size = p.step_size;
+    o.step_size_write_samples = p.step_size_write_samples;
+    o.data_min = p.data_min;
+    o.data_max = p.data_max;
+    o.error_threshold = p.error_threshold;
+    o.bias = p.bias;
+    o.compact_image = p.compact_image;
+    o.prediction_coding = p.prediction_coding;
+    o.compress = p.compress;
+    o.entropy_coding = p.entropy_coding;
+    o.quantization_bits = p.quantization_bits;
+    o.coding_warp = p.coding_warp;
+    o.quantization_curve_sampling = p.quantization_curve_sampling;
+    o.transform_to_bounds = p.transform_to_bounds;
+    o.transform_bound_eps = p.transform_bound_eps;
+    return o;
+}
+
+mraygb_reconstruction_params to_c(const ReconstructionParameters &p)
+{
+    mraygb_reconstruction_params o{};
+    o.bias = p.bias;
+    o.medium_emission = p.medium_emission;
+    o.medium_scattering = p.medium_scattering;
+    o.early_ray_termination = p.early_ray_termination;
+    o.data_min = p.data_min;
+    o.data_max = p.data_max;
+    o.step_size = p.step_size;
+    o.step_size_write_samples = p.step_size_write_samples;
+    o.use_truncated_fourier = p.use_truncated_fourier;
+    o.ss_enable = p.ss.enable;
+    return o;
+}
+
+} // namespace
+
+void generate_device(cut::Camera cam, const RegularGrid &volume, MomentImageHost &img,
+                     const GenerationParameters &params)
+{
+    if (volume.type != RegularGrid::DataType::F32)
+    {
+        std::fprintf(stderr, "mraygb: only float grids are supported\n");
+        std::terminate();
+    }
+    const float dmin[3] = {volume.domain.min.x, volume.domain.min.y, volume.domain.min.z};
+    const float dmax[3] = {volume.domain.max.x, volume.domain.max.y, volume.domain.max.z};
+    check(mraygb_upload_grid(context(), volume.data.data(), volume.size.x, volume.size.y, volume.size.z, dmin, dmax,
+                             0));
+    const auto c = to_c(cam);
+    const auto g = to_c(params);
+    img.domain = volume.domain;
+    img.data.resize(size_t(img.width) * img.height * img.num_moments);
+    if (params.compact_image)
+        img.index.resize(size_t(img.width) * img.height + 1);
+    if (params.transform_to_bounds)
+        img.bounds.resize(size_t(img.width) * img.height);
+    std::vector<uint16_t> bounds(params.transform_to_bounds ? 2 * size_t(img.width) * img.height : 0);
+    std::vector<uint16_t> cp(img.num_moments > 1 ? 2 * size_t(img.num_moments - 1) : 1);
+    uint64_t size = 0;
+    check(mraygb_generate(context(), &c, &g, img.width, img.height, img.num_moments, img.data.data(),
+                          params.compact_image ? img.index.data() : nullptr,
+                          params.transform_to_bounds ? bounds.data() : nullptr, cp.data(), &size));
+    img.data.resize(size);
+    for (size_t i = 0; i < img.bounds.size() && !bounds.empty(); ++i)
+    {
+        img.bounds[i].lower = bounds[2 * i];
+        img.bounds[i].upper = bounds[2 * i + 1];
+    }
+    img.is_compact = params.compact_image;
+    img.prediction_code = params.prediction_coding;
+    img.coding_warp = static_cast<CodingWarpType>(params.coding_warp);
+    img.coding_params.clear();
+    if (params.prediction_coding && params.coding_warp == CODING_WARP_DEFAULT_TRANSFORMED)
+        for (int i = 0; i + 1 < img.num_moments; ++i)
+            img.coding_params.push_back(CodingParamType{cp[2 * i], cp[2 * i + 1]});
+}
+
+void reconstruct_device(cut::Camera cam, const MomentImageHost &mi, const TransferFunction &tf, ColorImageHost &cimg,
+                        const ReconstructionParameters &params)
+{
+    // preintegrate() / read_from_disk() tables have 256 equal rows; the first row is the whole table
+    check(mraygb_upload_tf(context(), reinterpret_cast<const float *>(tf.data.data())));
+    const auto c = to_c(cam);
+    const auto r = to_c(params);
+    const float dmin[3] = {mi.domain.min.x, mi.domain.min.y, mi.domain.min.z};
+    const float dmax[3] = {mi.domain.max.x, mi.domain.max.y, mi.domain.max.z};
+    std::vector<uint16_t> bounds;
+    for (const auto &b : mi.bounds)
+    {
+        bounds.push_back(b.lower);
+        bounds.push_back(b.upper);
+    }
+    std::vector<uint16_t> cp;
+    for (const auto &p : mi.coding_params)
+    {
+        cp.push_back(p.param1);
+        cp.push_back(p.param2);
+    }
+    static_assert(sizeof(ColorImageHost::rgba8_t) == 4, "rgba8_t is four bytes");
+    check(mraygb_reconstruct(context(), &c, &r, mi.width, mi.height, mi.num_moments, dmin, dmax,
+                             mi.is_compact ? mi.index.data() : nullptr, mi.data.data(), mi.data.size(),
+                             bounds.empty() ? nullptr : bounds.data(), mi.prediction_code, mi.coding_warp,
+                             cp.empty() ? nullptr : cp.data(), nullptr,
+                             reinterpret_cast<uint8_t *>(cimg.rgba.data())));
+}

@@ -1,0 +1,22 @@
+"""The reference-side shim (mray_gb300/shim/moment_raymarcher_gb300.cpp) compiles against the reference's own
+headers: the drop-in seam type-checks.  Runs only where the reference sources are present."""
+import os
+import shutil
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+REF = "/root/reference/src"
+
+
+@pytest.mark.skipif(not os.path.isdir(REF), reason="reference sources not present")
+def test_shim_compiles_against_reference_headers(tmp_path):
+    cuda_inc = "/usr/local/cuda/include"
+    if not shutil.which("g++") or not os.path.isdir(cuda_inc):
+        pytest.skip("g++ or CUDA headers missing")
+    cmd = ["g++", "-std=c++14", "-fsyntax-only", "-DCUDA_SUPPORT", "-include", "algorithm", "-include", "cstring",
+           "-include", "numeric", "-I", REF, "-I", os.path.join(ROOT, "include"), "-I", cuda_inc, "-w",
+           os.path.join(ROOT, "mray_gb300", "shim", "moment_raymarcher_gb300.cpp")]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
