@@ -164,6 +164,21 @@ int mraygb_stage_dequantize_prediction_coding(mraygb_context *ctx, int width, in
                                               const uint32_t *d_index, const uint8_t *h_table,
                                               const uint8_t *d_bytes, uint64_t num_bytes, float *d_data);
 
+/* Compaction that allocates nothing, for callers that must not call cudaMalloc / cudaFree while they work:
+ * renderers and services that reserve all device memory up front in their own pool or arena (where an
+ * allocation can stall every stream on the device, exceed the pool's budget or fragment memory the pool
+ * manages).  It has no counterpart in the reference.  Same result as mraygb_stage_compact, but without a
+ * context: it runs on the current device and on `stream` (a cudaStream_t, NULL for the default stream), and
+ * the scan's block sums live in a fixed device array of 16448 words (64 KiB) that each GPU loading the library
+ * holds until the process exits.  Limit: W * H <= 16,777,216 pixels (4096 x 4096); larger images return
+ * MRAYGB_INVALID_ARGUMENT.  The first call on a device looks up the array's device address (set-up), so make
+ * that first call before any stream capture.  All calls share the array: calls that overlap on the GPU race on
+ * it and must be ordered by the caller.  Failures are reported by the return code only (there is no context to
+ * hold a message). */
+int mraygb_stage_compact_noalloc(void *stream, int width, int height, int num_moments, const uint32_t *d_counts,
+                                 const float *d_moments, uint32_t *d_index, float *d_compact, uint64_t capacity,
+                                 uint64_t *h_total);
+
 /* Lagrange multipliers per pixel (prepare_moments_device, src/moment_image_device.cu:306-335): the moment data
  * in the compact layout (d_index) or, with d_index NULL, the W*H*m layout; output in the same layout. */
 int mraygb_stage_prepare_moments(mraygb_context *ctx, int width, int height, int num_moments, const uint32_t *d_index,

@@ -23,7 +23,7 @@ EXPORTS = [
     "mraygb_generate", "mraygb_reconstruct", "mraygb_stage_generate_moments", "mraygb_stage_compact",
     "mraygb_stage_prepare_moments", "mraygb_stage_reconstruct", "mraygb_quantize_prediction_coding",
     "mraygb_stage_prediction_encode", "mraygb_stage_quantize_prediction_coding",
-    "mraygb_stage_dequantize_prediction_coding",
+    "mraygb_stage_dequantize_prediction_coding", "mraygb_stage_compact_noalloc",
 ]
 
 _lock = threading.Lock()
@@ -68,6 +68,7 @@ def _declare(L):
     L.mraygb_stage_prediction_encode.argtypes = [vp, i, i, i, vp, vp, u64, i, C.c_float, vp]
     L.mraygb_stage_quantize_prediction_coding.argtypes = [vp, i, i, i, vp, vp, vp, vp, u64, P(u64)]
     L.mraygb_stage_dequantize_prediction_coding.argtypes = [vp, i, i, i, vp, vp, vp, u64, vp]
+    L.mraygb_stage_compact_noalloc.argtypes = [vp, i, i, i, vp, vp, vp, vp, u64, P(u64)]
     special = ("mraygb_destroy", "mraygb_last_error", "mraygb_get_stream", "mraygb_kernel_launches")
     for name in EXPORTS:
         if name not in special:

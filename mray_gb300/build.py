@@ -28,6 +28,7 @@ SOURCES = [
     ("generate.cu", []),
     ("reconstruct.cu", []),
     ("scan.cu", []),
+    ("compact_noalloc.cu", []),
     ("mese.cu", ["--fmad=false"]),
     ("coding.cu", ["--fmad=false"]),
     ("api.cpp", ["-x", "cu"]),
