@@ -6,7 +6,8 @@
 //   prepare_moments_from_pred_coding  src/moment_preparation.h:32-53
 //   determine_best_number_moments     src/moment_compaction.h:113-142 (with :35-111)
 //
-// One thread per pixel; the O(m^2) recursions work on per-thread arrays of m complex values.
+// One thread per pixel; the O(m^2) recursions work on per-thread arrays of m complex values held in
+// thread-strided shared memory (element k of thread t at k * BLOCK + t: conflict-free, no local-memory spills).
 
 #include "internal.h"
 #include "mese_device.cuh"
@@ -38,19 +39,29 @@ __device__ __forceinline__ void pixel_span(const uint32_t *index, int m, int p, 
     }
 }
 
-template <typename T, int MAXM>
-__global__ void __launch_bounds__(128) prepare_kernel(int num_pixels, int m, const uint32_t *__restrict__ index,
-                                                      const float *__restrict__ data, int prediction_code,
-                                                      int coding_warp, const uint16_t *__restrict__ coding_params,
-                                                      float bias, float *__restrict__ out)
+// Shared-memory budget of one block: NC complex and NR real arrays of MAXM elements per thread.
+template <typename T, int MAXM, int NC, int NR> constexpr int smem_per_thread()
 {
+    return MAXM * (NC * (int)sizeof(cx<T>) + NR * (int)sizeof(T));
+}
+
+// Lagrange multipliers (prepare_moments_from_std_coding / prepare_moments_from_pred_coding).  Arrays live in
+// thread-strided shared memory: code (prediction-coded input only), e (exponential moments), poly (Levinson
+// solution) and the real accumulators of the correlation.
+template <typename T, int MAXM, int BLOCK>
+__global__ void __launch_bounds__(BLOCK) prepare_kernel(int num_pixels, int m, const uint32_t *__restrict__ index,
+                                                        const float *__restrict__ data, int prediction_code,
+                                                        int coding_warp, const uint16_t *__restrict__ coding_params,
+                                                        float bias, float *__restrict__ out)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
     __shared__ float s_params[2 * MAXM];
     if (prediction_code && coding_warp == 0 && coding_params)
         for (int i = threadIdx.x; i < 2 * (m - 1); i += blockDim.x)
             s_params[i] = coding_params[i] / 65535.f; // CodingParamType::get_param1/2 (coding_params.h:52-54)
     __syncthreads();
 
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    const int p = blockIdx.x * BLOCK + threadIdx.x;
     if (p >= num_pixels)
         return;
     size_t idx;
@@ -61,53 +72,57 @@ __global__ void __launch_bounds__(128) prepare_kernel(int num_pixels, int m, con
     if (n > MAXM)
         n = MAXM;
 
-    cx<T> a0[MAXM], a1[MAXM], a2[MAXM];
+    cx<T> *base = reinterpret_cast<cx<T> *>(smem);
+    const Strided<cx<T>, BLOCK> e{base + threadIdx.x};
+    const Strided<cx<T>, BLOCK> poly{base + MAXM * BLOCK + threadIdx.x};
+    const Strided<cx<T>, BLOCK> code{base + 2 * MAXM * BLOCK + threadIdx.x};
+    const Strided<T, BLOCK> acc{reinterpret_cast<T *>(base + 3 * MAXM * BLOCK) + threadIdx.x};
     if (prediction_code)
     {
-        cx<T> code[MAXM];
         pc_dequant_real<T>(n, data + idx, code, coding_warp, s_params);
-        pc_decode<T>(n, code, a0, a1, a2);          // a0 = exp moments, a1 = evaluation polynomial
-        lagrange_from_poly<T, float>(n, a1, a0, a2, out + idx);
+        pc_decode<T>(n, code, e, poly);
     }
     else
     {
-        T mom[MAXM];
+        // cut::lerp(m, target, bias) = (1 - bias) m + bias target (cuda_math.h:72-75), into the accumulators
         const T b = T(bias);
-        mom[0] = (T(1) - b) * T(data[idx]) + b * T(0.5f); // cut::lerp (cuda_math.h:72-75)
+        acc[0] = (T(1) - b) * T(data[idx]) + b * T(0.5f);
         for (int i = 1; i < n; ++i)
-            mom[i] = (T(1) - b) * T(data[idx + i]) + b * T(0.0f);
-        trig_to_exp<T>(n, a0, mom, two_pi_over_l<T>());
-        levinson<T>(n, a1, a0, a2);
-        lagrange_from_poly<T, float>(n, a1, a0, a2, out + idx);
+            acc[i] = (T(1) - b) * T(data[idx + i]) + b * T(0.0f);
+        trig_to_exp<T>(n, e, acc, two_pi_over_l<T>());
+        levinson<T>(n, poly, e);
     }
+    lagrange_from_poly<T>(n, poly, e, acc);
+    const T norm = T(1) / (MeseConst<T>::pi * ((cx<T>)poly[0]).x);
+    for (int i = 0; i < n; ++i)
+        out[idx + i] = float(norm * T(acc[i]));
 }
 
 // ---- error-threshold compaction (float, the reference's arithmetic) ---------------------------------------
 
-template <int MAXM>
-__device__ void eval_unknown(int num, const cx<float> *e, int max_moments, cx<float> *new_e, cx<float> *lev)
+template <typename A> __device__ void eval_unknown(int num, const A &e, int max_moments, const A &new_e, const A &lev)
 {
     const int mm = max_moments - 1;
     const int n = num - 1;
-    levinson<float>(num, lev, e, new_e);
+    levinson<float>(num, lev, e);
     for (int i = 0; i < n + 1; ++i)
-        lev[i] = cscale(MeseConst<float>::two_pi, lev[i]);
+        lev[i] = cscale(MeseConst<float>::two_pi, (cx<float>)lev[i]);
     for (int l = 0; l < n + 1; ++l)
-        new_e[l] = e[l];
-    const cx<float> inv_lev0 = cdiv(mk<float>(-1.f, 0.f), lev[0]);
+        new_e[l] = (cx<float>)e[l];
+    const cx<float> inv_lev0 = cdiv(mk<float>(-1.f, 0.f), (cx<float>)lev[0]);
     for (int k = 0; k < mm - n; ++k)
     {
-        cx<float> acc = mk<float>(0, 0);
+        cx<float> a = mk<float>(0, 0);
         for (int j = 1; j < n + 1; ++j)
-            acc = cadd(acc, cmulc(new_e[j + k], lev[n + 1 - j]));
-        new_e[n + k + 1] = cmulc(acc, inv_lev0);
+            a = cadd(a, cmulc((cx<float>)new_e[j + k], (cx<float>)lev[n + 1 - j]));
+        new_e[n + k + 1] = cmulc(a, inv_lev0);
     }
 }
 
 // exponential_to_bounded_moments: the reference multiplies by exp_moments[l] inside the sum (kept as is)
-__device__ void exp_to_bounded(int num, const cx<float> *e, cx<float> *b, int n)
+template <typename A> __device__ void exp_to_bounded(int num, const A &e, const A &b, int n)
 {
-    const cx<float> gamma_0 = cdivr(e[0], 2.f);
+    const cx<float> gamma_0 = cdivr((cx<float>)e[0], 2.f);
     // float_complex(0, 2) * M_PI * gamma_0: M_PI converts to float_complex((float)M_PI)
     const cx<float> i2pi = cmulc(mk<float>(0.f, 2.f), mk<float>(MeseConst<float>::pi_l, 0.f));
     for (int l = n; l < num; ++l)
@@ -116,37 +131,42 @@ __device__ void exp_to_bounded(int num, const cx<float> *e, cx<float> *b, int n)
         for (int j = 0; j < l; ++j)
         {
             const cx<float> dq = cdiv(mk<float>((float)(l - j), 0.f), cscale((float)l, gamma_0));
-            b[l] = cadd(b[l], cmulc(cmulc(dq, e[l]), b[l - j]));
+            b[l] = cadd((cx<float>)b[l], cmulc(cmulc(dq, (cx<float>)e[l]), (cx<float>)b[l - j]));
         }
-        b[l] = csub(cdiv(e[l], cmulc(i2pi, gamma_0)), b[l]);
+        b[l] = csub(cdiv((cx<float>)e[l], cmulc(i2pi, gamma_0)), (cx<float>)b[l]);
     }
 }
 
-template <int MAXM>
-__global__ void __launch_bounds__(128) count_moments_kernel(int num_pixels, int m, float thr,
-                                                            const float *__restrict__ moments,
-                                                            uint32_t *__restrict__ counts)
+// determine_best_number_moments for the pixels whose count is non-zero
+template <int MAXM, int BLOCK>
+__global__ void __launch_bounds__(BLOCK) count_moments_kernel(int num_pixels, int m, float thr,
+                                                              const float *__restrict__ moments,
+                                                              uint32_t *__restrict__ counts)
 {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int p = blockIdx.x * BLOCK + threadIdx.x;
     if (p >= num_pixels || counts[p] == 0)
         return;
     const float *mo = moments + (size_t)p * (size_t)m;
-    cx<float> te[MAXM], text[MAXM], tlev[MAXM];
+    cx<float> *base = reinterpret_cast<cx<float> *>(smem);
+    const Strided<cx<float>, BLOCK> te{base + threadIdx.x};
+    const Strided<cx<float>, BLOCK> text{base + MAXM * BLOCK + threadIdx.x};
+    const Strided<cx<float>, BLOCK> tlev{base + 2 * MAXM * BLOCK + threadIdx.x};
     const float norm = 1.0f / mo[0];
     trig_to_exp<float>(m, te, mo, two_pi_over_l<float>());
     int n = m / 2;
     int s = m / 4;
     while (s > 0)
     {
-        eval_unknown<MAXM>(n, te, m, text, tlev);
-        cx<float> *ext = tlev;
+        eval_unknown(n, te, m, text, tlev);
+        const Strided<cx<float>, BLOCK> &ext = tlev;
         for (int l = 0; l < n; ++l)
             ext[l] = mk<float>(mo[l], 0.f);
         exp_to_bounded(m, text, ext, n);
         float sum = 0.f;
         for (int k = n; k < m; ++k)
         {
-            const float diff = ext[k].x - mo[k];
+            const float diff = ((cx<float>)ext[k]).x - mo[k];
             sum += diff * diff;
         }
         const float rrmse = sqrtf(sum) * norm;
@@ -163,12 +183,15 @@ __global__ void __launch_bounds__(128) count_moments_kernel(int num_pixels, int 
 
 // MomentImageHost::prediction_encode, per-pixel part (moment_image.cpp:103-126): bias lerp, trigonometric ->
 // exponential moments, encode, projection of the residuals to the real line; in place
-template <int MAXM>
-__global__ void __launch_bounds__(128) prediction_encode_kernel(int num_pixels, int m,
-                                                                const uint32_t *__restrict__ index,
-                                                                float *__restrict__ data, float bias)
+// MomentImageHost::prediction_encode, per-pixel part (moment_image.cpp:103-126): bias lerp, trigonometric ->
+// exponential moments, encode, projection of the residuals to the real line; in place
+template <int MAXM, int BLOCK>
+__global__ void __launch_bounds__(BLOCK) prediction_encode_kernel(int num_pixels, int m,
+                                                                  const uint32_t *__restrict__ index,
+                                                                  float *__restrict__ data, float bias)
 {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int p = blockIdx.x * BLOCK + threadIdx.x;
     if (p >= num_pixels)
         return;
     size_t idx;
@@ -182,24 +205,47 @@ __global__ void __launch_bounds__(128) prediction_encode_kernel(int num_pixels, 
     d[0] = (1 - bias) * d[0] + bias * 0.5f; // cut::lerp(data[idx], 0.5f, bias)
     for (int i = 1; i < n; ++i)
         d[i] = (1 - bias) * d[i] + bias * 0.0f;
-    cx<float> e[MAXM], code[MAXM], poly[MAXM], tmp[MAXM];
+    cx<float> *base = reinterpret_cast<cx<float> *>(smem);
+    const Strided<cx<float>, BLOCK> e{base + threadIdx.x};
+    const Strided<cx<float>, BLOCK> code{base + MAXM * BLOCK + threadIdx.x};
+    const Strided<cx<float>, BLOCK> poly{base + 2 * MAXM * BLOCK + threadIdx.x};
     trig_to_exp<float>(n, e, d, two_pi_over_l<float>());
-    pc_encode<float>(n, e, code, poly, tmp);
+    pc_encode<float>(n, e, code, poly);
     // transform_quantization_real (moment_prediction_coding.h:81-92): out[0] = c_0 stays d[0]
-    const cx<float> axis = mk(-code[0].y, code[0].x);
+    const cx<float> c0 = code[0];
+    const cx<float> axis = mk(-c0.y, c0.x);
     const float len = sqrtf(cabs2(axis));
     const cx<float> inv_axis = cdiv(mk(len, 0.f), axis);
     for (int l = 1; l < n; ++l)
-        d[l] = cmulc(code[l], inv_axis).x;
+        d[l] = cmulc((cx<float>)code[l], inv_axis).x;
+}
+
+// threads per block for a per-thread shared-memory need: the largest of 128, 64, 32, 16, 8 threads whose arrays
+// fit in 120 KiB (large moment counts in FP64 get sub-warp blocks rather than local-memory arrays)
+template <int PER_THREAD> constexpr int block_for()
+{
+    constexpr int budget = 120 * 1024;
+    return budget / PER_THREAD >= 128 ? 128
+         : budget / PER_THREAD >= 64  ? 64
+         : budget / PER_THREAD >= 32  ? 32
+         : budget / PER_THREAD >= 16  ? 16
+                                      : 8;
 }
 
 template <typename T, int MAXM>
 cudaError_t launch_prepare_t(int num_pixels, int m, const uint32_t *index, const float *data, int pc, int warp,
                              const uint16_t *cp, float bias, float *out, cudaStream_t stream)
 {
-    const int block = 128;
+    constexpr int per = smem_per_thread<T, MAXM, 3, 1>();
+    constexpr int block = block_for<per>();
+    constexpr int bytes = per * block;
+    cudaError_t e = cudaFuncSetAttribute(prepare_kernel<T, MAXM, block>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e != cudaSuccess)
+        return e;
     const int grid = (num_pixels + block - 1) / block;
-    prepare_kernel<T, MAXM><<<grid, block, 0, stream>>>(num_pixels, m, index, data, pc, warp, cp, bias, out);
+    prepare_kernel<T, MAXM, block><<<grid, block, bytes, stream>>>(num_pixels, m, index, data, pc, warp, cp, bias,
+                                                                    out);
     return cudaGetLastError();
 }
 
@@ -214,6 +260,37 @@ cudaError_t launch_prepare_m(int num_pixels, int m, const uint32_t *index, const
     if (m <= 128)
         return launch_prepare_t<T, 128>(num_pixels, m, index, data, pc, warp, cp, bias, out, stream);
     return launch_prepare_t<T, 256>(num_pixels, m, index, data, pc, warp, cp, bias, out, stream);
+}
+
+template <int MAXM>
+cudaError_t launch_count_t(int num_pixels, int m, float thr, const float *moments, uint32_t *counts,
+                           cudaStream_t stream)
+{
+    constexpr int per = smem_per_thread<float, MAXM, 3, 0>();
+    constexpr int block = block_for<per>();
+    constexpr int bytes = per * block;
+    cudaError_t e = cudaFuncSetAttribute(count_moments_kernel<MAXM, block>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e != cudaSuccess)
+        return e;
+    count_moments_kernel<MAXM, block><<<(num_pixels + block - 1) / block, block, bytes, stream>>>(num_pixels, m, thr,
+                                                                                              moments, counts);
+    return cudaGetLastError();
+}
+
+template <int MAXM>
+cudaError_t launch_encode_t(int num_pixels, int m, const uint32_t *index, float *data, float bias, cudaStream_t stream)
+{
+    constexpr int per = smem_per_thread<float, MAXM, 3, 0>();
+    constexpr int block = block_for<per>();
+    constexpr int bytes = per * block;
+    cudaError_t e = cudaFuncSetAttribute(prediction_encode_kernel<MAXM, block>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e != cudaSuccess)
+        return e;
+    prediction_encode_kernel<MAXM, block><<<(num_pixels + block - 1) / block, block, bytes, stream>>>(
+        num_pixels, m, index, data, bias);
+    return cudaGetLastError();
 }
 
 } // namespace
@@ -238,33 +315,25 @@ cudaError_t mese_init_constants()
 cudaError_t launch_count_moments(int num_pixels, int m, float thr, const float *moments, uint32_t *counts,
                                  cudaStream_t stream)
 {
-    const int block = 128;
-    const int grid = (num_pixels + block - 1) / block;
     if (m <= 32)
-        count_moments_kernel<32><<<grid, block, 0, stream>>>(num_pixels, m, thr, moments, counts);
-    else if (m <= 64)
-        count_moments_kernel<64><<<grid, block, 0, stream>>>(num_pixels, m, thr, moments, counts);
-    else if (m <= 128)
-        count_moments_kernel<128><<<grid, block, 0, stream>>>(num_pixels, m, thr, moments, counts);
-    else
-        count_moments_kernel<256><<<grid, block, 0, stream>>>(num_pixels, m, thr, moments, counts);
-    return cudaGetLastError();
+        return launch_count_t<32>(num_pixels, m, thr, moments, counts, stream);
+    if (m <= 64)
+        return launch_count_t<64>(num_pixels, m, thr, moments, counts, stream);
+    if (m <= 128)
+        return launch_count_t<128>(num_pixels, m, thr, moments, counts, stream);
+    return launch_count_t<256>(num_pixels, m, thr, moments, counts, stream);
 }
 
 cudaError_t launch_prediction_encode(int num_pixels, int m, const uint32_t *index, float *data, float bias,
                                      cudaStream_t stream)
 {
-    const int block = 128;
-    const int grid = (num_pixels + block - 1) / block;
     if (m <= 32)
-        prediction_encode_kernel<32><<<grid, block, 0, stream>>>(num_pixels, m, index, data, bias);
-    else if (m <= 64)
-        prediction_encode_kernel<64><<<grid, block, 0, stream>>>(num_pixels, m, index, data, bias);
-    else if (m <= 128)
-        prediction_encode_kernel<128><<<grid, block, 0, stream>>>(num_pixels, m, index, data, bias);
-    else
-        prediction_encode_kernel<256><<<grid, block, 0, stream>>>(num_pixels, m, index, data, bias);
-    return cudaGetLastError();
+        return launch_encode_t<32>(num_pixels, m, index, data, bias, stream);
+    if (m <= 64)
+        return launch_encode_t<64>(num_pixels, m, index, data, bias, stream);
+    if (m <= 128)
+        return launch_encode_t<128>(num_pixels, m, index, data, bias, stream);
+    return launch_encode_t<256>(num_pixels, m, index, data, bias, stream);
 }
 
 cudaError_t launch_prepare(int num_pixels, int m, const uint32_t *index, const float *data, int prediction_code,

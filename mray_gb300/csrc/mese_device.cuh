@@ -1,9 +1,12 @@
-// Per-pixel bounded-MESE algebra on the device, generic over float / double.
+// Per-pixel bounded-MESE algebra on the device, generic over float / double and over the array type.
 //
 // The float instantiation performs the reference's operations in the reference's order (these kernels are
 // compiled without FMA contraction), so its results differ from the reference's CPU build only where CUDA's
 // cosf / sinf round differently from the C library's.  The double instantiation is the same method in FP64
 // with exact constants (the precision form).
+//
+// Arrays are accessed through an index operator only: the kernels pass thread-strided views of shared memory
+// (element k of thread t at k * BLOCK + t, so a warp reading element k touches 32 consecutive words).
 //
 //   trigonometricToExponentialMoments  src/mese/MESE_dynamic.h:35-54
 //   levinsonsAlgorithm                 src/mese/MESE_dynamic.h:100-135
@@ -25,6 +28,13 @@ namespace mraygb
 template <typename T> struct cx
 {
     T x, y;
+};
+
+// element k of a thread's array in thread-strided shared memory
+template <typename E, int STRIDE> struct Strided
+{
+    E *p;
+    __device__ __forceinline__ E &operator[](int k) const { return p[k * STRIDE]; }
 };
 
 template <typename T> struct MeseConst;
@@ -83,8 +93,8 @@ template <typename T> __device__ __forceinline__ T tclamp(T v, T lo, T hi) { ret
 
 // trigonometricToExponentialMoments (float* trig overload)
 // two_pi_over_l[l] = float_complex(0, 2.0f * M_PI / float(l)).y: the reference's double quotient rounded to T
-template <typename T, typename TrigArr>
-__device__ void trig_to_exp(int n, cx<T> *e, const TrigArr &trig, const T *two_pi_over_l)
+template <typename T, typename A, typename TrigArr>
+__device__ void trig_to_exp(int n, const A &e, const TrigArr &trig, const T *two_pi_over_l)
 {
     using K = MeseConst<T>;
     T phase = K::pi * T(trig[0]) - K::half_pi;
@@ -95,22 +105,45 @@ __device__ void trig_to_exp(int n, cx<T> *e, const TrigArr &trig, const T *two_p
     {
         cx<T> acc = mk<T>(0, 0);
         for (int j = 0; j < l; ++j)
-            acc = cadd(acc, cmulr(cscale(T(l - j), e[j]), T(trig[l - j])));
+            acc = cadd(acc, cmulr(cscale(T(l - j), (cx<T>)e[j]), T(trig[l - j])));
         e[l] = cmulc(acc, mk<T>(0, two_pi_over_l[l]));
     }
-    e[0] = cscale(T(2), e[0]);
+    e[0] = cscale(T(2), (cx<T>)e[0]);
 }
 
-template <typename T> __device__ void levinson(int n, cx<T> *sol, const cx<T> *col, cx<T> *tmp)
+// One Levinson-style update of the solution / evaluation polynomial in place: with the old values o,
+//   new[0] = f o[0].x,  new[k] = f (o[k] - conj(o[j-k]) u) (0 < k < j),  new[j] = f (-o[0].x u).
+// The reference copies the flipped solution to a temporary first; updating the pairs (k, j-k) together needs
+// no copy and performs the same operations on the same values.
+template <typename T, typename A> __device__ __forceinline__ void levinson_update(int j, const A &sol, cx<T> u, T f)
 {
-    sol[0] = mk<T>(T(1) / col[0].x, 0);
+    const T s0 = ((cx<T>)sol[0]).x;
+    int k = 1, kk = j - 1;
+    for (; k < kk; ++k, --kk)
+    {
+        const cx<T> a = sol[k], b = sol[kk];
+        sol[k] = cscale(f, csub(a, cmulc(cconj(b), u)));
+        sol[kk] = cscale(f, csub(b, cmulc(cconj(a), u)));
+    }
+    if (k == kk)
+    {
+        const cx<T> a = sol[k];
+        sol[k] = cscale(f, csub(a, cmulc(cconj(a), u)));
+    }
+    sol[j] = cscale(f, cscale(-s0, u));
+    sol[0] = mk<T>(f * s0, 0);
+}
+
+template <typename T, typename A, typename C> __device__ void levinson(int n, const A &sol, const C &col)
+{
+    sol[0] = mk<T>(T(1) / ((cx<T>)col[0]).x, 0);
     bool invalid = false;
     for (int j = 1; j < n; ++j)
     {
         cx<T> u = mk<T>(0, 0);
         if (!invalid)
             for (int k = 0; k < j; ++k)
-                u = cadd(u, cmulc(sol[k], col[j - k]));
+                u = cadd(u, cmulc((cx<T>)sol[k], (cx<T>)col[j - k]));
         T a2 = cabs2(u);
         if (a2 >= T(1))
         {
@@ -118,66 +151,48 @@ template <typename T> __device__ void levinson(int n, cx<T> *sol, const cx<T> *c
             a2 = 0;
             invalid = true;
         }
-        const T factor = T(1) / (T(1) - a2);
-        for (int k = 1; k < j; ++k)
-            tmp[k] = cconj(sol[j - k]);
-        tmp[j] = mk<T>(sol[0].x, 0);
-        sol[0] = mk<T>(factor * sol[0].x, 0);
-        for (int k = 1; k < j; ++k)
-            sol[k] = cscale(factor, csub(sol[k], cmulc(tmp[k], u)));
-        sol[j] = cscale(factor, cscale(-tmp[j].x, u));
+        levinson_update<T>(j, sol, u, T(1) / (T(1) - a2));
     }
 }
 
-template <typename T> __device__ void autocorr(int n, cx<T> *out, const cx<T> *s)
-{
-    for (int k = 0; k < n; ++k)
-    {
-        cx<T> acc = mk<T>(0, 0);
-        for (int j = 0; j < n - k; ++j)
-            acc = cadd(acc, cmulc(s[j], cconj(s[j + k])));
-        out[k] = acc;
-    }
-}
-
-// computeImaginaryCorrelation, written straight to an output of type O
-template <typename T, typename O> __device__ void imag_corr_scaled(int n, O *out, const cx<T> *lhs, const cx<T> *rhs,
-                                                                   T norm)
-{
-    for (int k = 0; k < n; ++k)
-    {
-        T acc = 0;
-        for (int j = 0; j < n - k; ++j)
-            acc += lhs[k + j].x * rhs[j].y + lhs[k + j].y * rhs[j].x;
-        out[k] = O(norm * acc);
-    }
-}
-
-// the shared tail of prepareMESELagrange / prepare_moments_from_pred_coding: poly (Levinson solution) and
-// exp (exponential moments) in, Lagrange multipliers out
-template <typename T, typename O>
-__device__ void lagrange_from_poly(int n, cx<T> *poly, cx<T> *e, cx<T> *tmp, O *out)
+// the tail of prepareMESELagrange / prepare_moments_from_pred_coding: poly (the Levinson solution, scaled by
+// 2 pi here) and e (the exponential moments, e[0] halved here) in, Lagrange multipliers out.  The autocorrelation
+// of poly (computeAutocorrelation) is formed one lag q at a time and scattered straight into the imaginary
+// correlation with e (computeImaginaryCorrelation): out[k] accumulates its terms in the order of q = k + j,
+// the reference's order, so no autocorrelation array is needed.
+template <typename T, typename A, typename O>
+__device__ void lagrange_from_poly(int n, const A &poly, const A &e, const O &acc)
 {
     using K = MeseConst<T>;
     for (int i = 0; i < n; ++i)
-        poly[i] = cscale(K::two_pi, poly[i]);
-    autocorr(n, tmp, poly);
-    e[0] = cscale(T(0.5), e[0]);
-    const T norm = T(1) / (K::pi * poly[0].x);
-    imag_corr_scaled(n, out, tmp, e, norm);
+        poly[i] = cscale(K::two_pi, (cx<T>)poly[i]);
+    e[0] = cscale(T(0.5), (cx<T>)e[0]);
+    for (int k = 0; k < n; ++k)
+        acc[k] = T(0);
+    for (int q = 0; q < n; ++q)
+    {
+        cx<T> a = mk<T>(0, 0);
+        for (int j = 0; j < n - q; ++j)
+            a = cadd(a, cmulc((cx<T>)poly[j], cconj((cx<T>)poly[j + q])));
+        for (int k = 0; k <= q; ++k)
+        {
+            const cx<T> ej = e[q - k];
+            acc[k] = T(acc[k]) + (a.x * ej.y + a.y * ej.x);
+        }
+    }
 }
 
 // encode (moment_prediction_coding.h:123-158)
-template <typename T> __device__ void pc_encode(int n, const cx<T> *e, cx<T> *code, cx<T> *poly, cx<T> *tmp)
+template <typename T, typename A> __device__ void pc_encode(int n, const A &e, const A &code, const A &poly)
 {
-    code[0] = e[0];
-    poly[0] = mk<T>(T(1) / e[0].x, 0);
+    code[0] = (cx<T>)e[0];
+    poly[0] = mk<T>(T(1) / ((cx<T>)e[0]).x, 0);
     bool invalid = false;
     for (int l = 1; l < n; ++l)
     {
         cx<T> u = mk<T>(0, 0);
         for (int k = 0; k < l; ++k)
-            u = cadd(u, cmulc(poly[k], e[l - k]));
+            u = cadd(u, cmulc((cx<T>)poly[k], (cx<T>)e[l - k]));
         code[l] = u;
         T a2 = cabs2(u);
         if (invalid || a2 >= T(1))
@@ -186,23 +201,16 @@ template <typename T> __device__ void pc_encode(int n, const cx<T> *e, cx<T> *co
             a2 = 0;
             invalid = true;
         }
-        const T factor = T(1) / (T(1) - a2);
-        for (int k = 1; k < l; ++k)
-            tmp[k] = cconj(poly[l - k]);
-        tmp[l] = mk<T>(poly[0].x, 0);
-        poly[0] = mk<T>(factor * poly[0].x, 0);
-        for (int k = 1; k < l; ++k)
-            poly[k] = cscale(factor, csub(poly[k], cmulc(tmp[k], u)));
-        poly[l] = cscale(factor, cscale(-tmp[l].x, u));
+        levinson_update<T>(l, poly, u, T(1) / (T(1) - a2));
     }
 }
 
 // decode (moment_prediction_coding.h:163-208)
-template <typename T> __device__ void pc_decode(int n, const cx<T> *code, cx<T> *e, cx<T> *poly, cx<T> *tmp)
+template <typename T, typename A> __device__ void pc_decode(int n, const A &code, const A &e, const A &poly)
 {
     using K = MeseConst<T>;
-    e[0] = code[0];
-    poly[0] = mk<T>(T(1) / e[0].x, 0);
+    e[0] = (cx<T>)code[0];
+    poly[0] = mk<T>(T(1) / ((cx<T>)e[0]).x, 0);
     bool invalid = false;
     for (int l = 1; l < n; ++l)
     {
@@ -216,29 +224,13 @@ template <typename T> __device__ void pc_decode(int n, const cx<T> *code, cx<T> 
         }
         cx<T> gamma = mk<T>(0, 0);
         for (int k = 1; k < l; ++k)
-            gamma = cadd(gamma, cmulc(poly[k], e[l - k]));
-        e[l] = cmulc(cdiv(mk<T>(1, 0), poly[0]), csub(u, gamma));
-        const T factor = T(1) / (T(1) - a2);
-        for (int k = 1; k < l; ++k)
-            tmp[k] = cconj(poly[l - k]);
-        tmp[l] = mk<T>(poly[0].x, 0);
-        poly[0] = mk<T>(factor * poly[0].x, 0);
-        for (int k = 1; k < l; ++k)
-            poly[k] = cscale(factor, csub(poly[k], cmulc(tmp[k], u)));
-        poly[l] = cscale(factor, cscale(-tmp[l].x, u));
+            gamma = cadd(gamma, cmulc((cx<T>)poly[k], (cx<T>)e[l - k]));
+        e[l] = cmulc(cdiv(mk<T>(1, 0), (cx<T>)poly[0]), csub(u, gamma));
+        levinson_update<T>(l, poly, u, T(1) / (T(1) - a2));
     }
 }
 
-// prediction_coding_warp / prediction_coding_inv_warp; params are the dequantized u16 coding parameters
-__device__ __forceinline__ float pc_warp(int l, float x, int warp, const float *p)
-{
-    float w;
-    if (warp == 0)
-        w = (x + p[(l - 1) * 2]) / (p[(l - 1) * 2 + 1] * 2.f);
-    else
-        w = x * 0.5f + 0.5f;
-    return tclamp(w, 0.f, 1.f);
-}
+// prediction_coding_inv_warp; params are the dequantized u16 coding parameters
 template <typename T> __device__ __forceinline__ T pc_inv_warp(int l, T x, int warp, const float *p)
 {
     if (warp == 0)
@@ -247,16 +239,17 @@ template <typename T> __device__ __forceinline__ T pc_inv_warp(int l, T x, int w
 }
 
 // transform_dequantization_real
-template <typename T>
-__device__ void pc_dequant_real(int n, const float *in, cx<T> *out, int warp, const float *params)
+template <typename T, typename A>
+__device__ void pc_dequant_real(int n, const float *in, const A &out, int warp, const float *params)
 {
     using K = MeseConst<T>;
     const T c0 = T(in[0]);
     const T phase = K::pi * c0 - K::half_pi;
     T s, c;
     dsincos(phase, &s, &c);
-    out[0] = cscale(T(2) * K::inv_4pi, mk(c, s));
-    const cx<T> axis = mk(-out[0].y, out[0].x);
+    const cx<T> o0 = cscale(T(2) * K::inv_4pi, mk(c, s));
+    out[0] = o0;
+    const cx<T> axis = mk(-o0.y, o0.x);
     const T len = dsqrt(cabs2(axis));
     const cx<T> factor = cdivr(axis, len);
     for (int l = 1; l < n; ++l)
