@@ -25,6 +25,11 @@ cudaError_t launch_count_moments(int num_pixels, int m, float error_threshold, c
 // per-pixel part of prediction coding, in place on the compact moment data
 cudaError_t launch_prediction_encode(int num_pixels, int m, const uint32_t *index, float *data, float bias,
                                      cudaStream_t stream);
+// mese_f64.cu: the FP64 preparation
+cudaError_t mese_f64_init_constants();
+cudaError_t launch_prepare_f64(int num_pixels, int m, const uint32_t *index, const float *data, int prediction_code,
+                               int coding_warp, const uint16_t *coding_params, float bias, float *pmoments,
+                               cudaStream_t stream);
 // Lagrange multipliers; fp64 selects the FP64 form
 cudaError_t launch_prepare(int num_pixels, int m, const uint32_t *index, const float *data, int prediction_code,
                            int coding_warp, const uint16_t *coding_params, float bias, bool fp64, float *pmoments,

@@ -9,94 +9,13 @@
 // One thread per pixel; the O(m^2) recursions work on per-thread arrays of m complex values held in
 // thread-strided shared memory (element k of thread t at k * BLOCK + t: conflict-free, no local-memory spills).
 
-#include "internal.h"
-#include "mese_device.cuh"
+#include "mese_kernels.cuh"
 
 namespace mraygb
 {
 
 namespace
 {
-
-__constant__ float c_two_pi_over_l_f[256];
-__constant__ double c_two_pi_over_l_d[256];
-
-template <typename T> __device__ __forceinline__ const T *two_pi_over_l();
-template <> __device__ __forceinline__ const float *two_pi_over_l<float>() { return c_two_pi_over_l_f; }
-template <> __device__ __forceinline__ const double *two_pi_over_l<double>() { return c_two_pi_over_l_d; }
-
-__device__ __forceinline__ void pixel_span(const uint32_t *index, int m, int p, size_t &idx, int &n)
-{
-    if (index)
-    {
-        idx = index[p];
-        n = (int)(index[p + 1] - index[p]);
-    }
-    else
-    {
-        idx = (size_t)p * (size_t)m;
-        n = m;
-    }
-}
-
-// Shared-memory budget of one block: NC complex and NR real arrays of MAXM elements per thread.
-template <typename T, int MAXM, int NC, int NR> constexpr int smem_per_thread()
-{
-    return MAXM * (NC * (int)sizeof(cx<T>) + NR * (int)sizeof(T));
-}
-
-// Lagrange multipliers (prepare_moments_from_std_coding / prepare_moments_from_pred_coding).  Arrays live in
-// thread-strided shared memory: code (prediction-coded input only), e (exponential moments), poly (Levinson
-// solution) and the real accumulators of the correlation.
-template <typename T, int MAXM, int BLOCK>
-__global__ void __launch_bounds__(BLOCK) prepare_kernel(int num_pixels, int m, const uint32_t *__restrict__ index,
-                                                        const float *__restrict__ data, int prediction_code,
-                                                        int coding_warp, const uint16_t *__restrict__ coding_params,
-                                                        float bias, float *__restrict__ out)
-{
-    extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ float s_params[2 * MAXM];
-    if (prediction_code && coding_warp == 0 && coding_params)
-        for (int i = threadIdx.x; i < 2 * (m - 1); i += blockDim.x)
-            s_params[i] = coding_params[i] / 65535.f; // CodingParamType::get_param1/2 (coding_params.h:52-54)
-    __syncthreads();
-
-    const int p = blockIdx.x * BLOCK + threadIdx.x;
-    if (p >= num_pixels)
-        return;
-    size_t idx;
-    int n;
-    pixel_span(index, m, p, idx, n);
-    if (n <= 0)
-        return;
-    if (n > MAXM)
-        n = MAXM;
-
-    cx<T> *base = reinterpret_cast<cx<T> *>(smem);
-    const Strided<cx<T>, BLOCK> e{base + threadIdx.x};
-    const Strided<cx<T>, BLOCK> poly{base + MAXM * BLOCK + threadIdx.x};
-    const Strided<cx<T>, BLOCK> code{base + 2 * MAXM * BLOCK + threadIdx.x};
-    const Strided<T, BLOCK> acc{reinterpret_cast<T *>(base + 3 * MAXM * BLOCK) + threadIdx.x};
-    if (prediction_code)
-    {
-        pc_dequant_real<T>(n, data + idx, code, coding_warp, s_params);
-        pc_decode<T>(n, code, e, poly);
-    }
-    else
-    {
-        // cut::lerp(m, target, bias) = (1 - bias) m + bias target (cuda_math.h:72-75), into the accumulators
-        const T b = T(bias);
-        acc[0] = (T(1) - b) * T(data[idx]) + b * T(0.5f);
-        for (int i = 1; i < n; ++i)
-            acc[i] = (T(1) - b) * T(data[idx + i]) + b * T(0.0f);
-        trig_to_exp<T>(n, e, acc, two_pi_over_l<T>());
-        levinson<T>(n, poly, e);
-    }
-    lagrange_from_poly<T>(n, poly, e, acc);
-    const T norm = T(1) / (MeseConst<T>::pi * ((cx<T>)poly[0]).x);
-    for (int i = 0; i < n; ++i)
-        out[idx + i] = float(norm * T(acc[i]));
-}
 
 // ---- error-threshold compaction (float, the reference's arithmetic) ---------------------------------------
 
@@ -220,48 +139,6 @@ __global__ void __launch_bounds__(BLOCK) prediction_encode_kernel(int num_pixels
         d[l] = cmulc((cx<float>)code[l], inv_axis).x;
 }
 
-// threads per block for a per-thread shared-memory need: the largest of 128, 64, 32, 16, 8 threads whose arrays
-// fit in 120 KiB (large moment counts in FP64 get sub-warp blocks rather than local-memory arrays)
-template <int PER_THREAD> constexpr int block_for()
-{
-    constexpr int budget = 120 * 1024;
-    return budget / PER_THREAD >= 128 ? 128
-         : budget / PER_THREAD >= 64  ? 64
-         : budget / PER_THREAD >= 32  ? 32
-         : budget / PER_THREAD >= 16  ? 16
-                                      : 8;
-}
-
-template <typename T, int MAXM>
-cudaError_t launch_prepare_t(int num_pixels, int m, const uint32_t *index, const float *data, int pc, int warp,
-                             const uint16_t *cp, float bias, float *out, cudaStream_t stream)
-{
-    constexpr int per = smem_per_thread<T, MAXM, 3, 1>();
-    constexpr int block = block_for<per>();
-    constexpr int bytes = per * block;
-    cudaError_t e = cudaFuncSetAttribute(prepare_kernel<T, MAXM, block>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    if (e != cudaSuccess)
-        return e;
-    const int grid = (num_pixels + block - 1) / block;
-    prepare_kernel<T, MAXM, block><<<grid, block, bytes, stream>>>(num_pixels, m, index, data, pc, warp, cp, bias,
-                                                                    out);
-    return cudaGetLastError();
-}
-
-template <typename T>
-cudaError_t launch_prepare_m(int num_pixels, int m, const uint32_t *index, const float *data, int pc, int warp,
-                             const uint16_t *cp, float bias, float *out, cudaStream_t stream)
-{
-    if (m <= 32)
-        return launch_prepare_t<T, 32>(num_pixels, m, index, data, pc, warp, cp, bias, out, stream);
-    if (m <= 64)
-        return launch_prepare_t<T, 64>(num_pixels, m, index, data, pc, warp, cp, bias, out, stream);
-    if (m <= 128)
-        return launch_prepare_t<T, 128>(num_pixels, m, index, data, pc, warp, cp, bias, out, stream);
-    return launch_prepare_t<T, 256>(num_pixels, m, index, data, pc, warp, cp, bias, out, stream);
-}
-
 template <int MAXM>
 cudaError_t launch_count_t(int num_pixels, int m, float thr, const float *moments, uint32_t *counts,
                            cudaStream_t stream)
@@ -297,19 +174,10 @@ cudaError_t launch_encode_t(int num_pixels, int m, const uint32_t *index, float 
 
 cudaError_t mese_init_constants()
 {
-    float f[256];
-    double d[256];
-    f[0] = 0.f;
-    d[0] = 0.0;
-    for (int l = 1; l < 256; ++l)
-    {
-        f[l] = (float)(2.0f * 3.141592653589793 / (double)(float)l); // 2.0f * M_PI / static_cast<float>(l)
-        d[l] = 2.0 * 3.141592653589793 / (double)l;
-    }
-    cudaError_t e = cudaMemcpyToSymbol(c_two_pi_over_l_f, f, sizeof(f));
+    cudaError_t e = init_tables();
     if (e != cudaSuccess)
         return e;
-    return cudaMemcpyToSymbol(c_two_pi_over_l_d, d, sizeof(d));
+    return mese_f64_init_constants();
 }
 
 cudaError_t launch_count_moments(int num_pixels, int m, float thr, const float *moments, uint32_t *counts,
@@ -341,8 +209,8 @@ cudaError_t launch_prepare(int num_pixels, int m, const uint32_t *index, const f
                            cudaStream_t stream)
 {
     if (fp64)
-        return launch_prepare_m<double>(num_pixels, m, index, data, prediction_code, coding_warp, coding_params, bias,
-                                        pmoments, stream);
+        return launch_prepare_f64(num_pixels, m, index, data, prediction_code, coding_warp, coding_params, bias,
+                                  pmoments, stream);
     return launch_prepare_m<float>(num_pixels, m, index, data, prediction_code, coding_warp, coding_params, bias,
                                    pmoments, stream);
 }
