@@ -172,3 +172,62 @@ def mixing_layer_workload(n: int = 512, width: int = 1024, height: int = 1024, n
     name = name or f"mixing_layer{n}_{width}x{height}_m{num_moments}_persp"
     return Workload(name, mixing_layer(n, modes=modes, seed=seed), (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), width,
                     height, num_moments, cam, gen, rec, transfer_function(seed + 1), tf_step=0.05 * (512.0 / n))
+
+
+def sph_particles(n: int, seed: int = 31, clusters: int = 200, cluster_frac: float = 0.3):
+    """Particles in the unit cube: (1 - cluster_frac) uniform and cluster_frac in seeded Gaussian clusters
+    (sigma 0.01..0.05), clipped to the cube; values ~ LogNormal(0, 0.5).  Returns x, y, z, v (float32)."""
+    rng = np.random.default_rng(seed)
+    n_cl = int(n * cluster_frac)
+    n_un = n - n_cl
+    pts = np.empty((n, 3), dtype=np.float32)
+    pts[:n_un] = rng.random((n_un, 3), dtype=np.float32)
+    centres = rng.random((clusters, 3))
+    sigmas = rng.uniform(0.01, 0.05, size=clusters)
+    which = rng.integers(0, clusters, size=n_cl)
+    pts[n_un:] = np.clip(centres[which] + sigmas[which, None] * rng.standard_normal((n_cl, 3)), 0.0, 1.0)
+    v = rng.lognormal(0.0, 0.5, size=n).astype(np.float32)
+    return pts[:, 0].copy(), pts[:, 1].copy(), pts[:, 2].copy(), v
+
+
+@dataclasses.dataclass
+class ParticleWorkload:
+    """A particle configuration: particles, one global smoothing length, view, image, moments, parameters."""
+
+    name: str
+    x: np.ndarray
+    y: np.ndarray
+    z: np.ndarray
+    v: np.ndarray
+    h: float
+    domain_min: tuple
+    domain_max: tuple
+    width: int
+    height: int
+    num_moments: int
+    camera: Camera
+    gen: GenerationParameters
+    rec: ReconstructionParameters
+    tf1d: np.ndarray
+    tf_step: float
+
+
+def sph_workload(n: int = 20000, h: float = 1.0 / 32, width: int = 64, height: int = 64, num_moments: int = 16,
+                 seed: int = 31, name: str | None = None) -> ParticleWorkload:
+    """SPH particles with one global smoothing length (the reference's grid: cell size = h); the ray box is the
+    particles' bounding box (the loader's domain); step h / 2; data_min / data_max at the 1st / 99th
+    percentiles of a seeded sample of the values."""
+    x, y, z, v = sph_particles(n, seed)
+    dmin = (float(x.min()), float(y.min()), float(z.min()))
+    dmax = (float(x.max()), float(y.max()), float(z.max()))
+    rng = np.random.default_rng(seed + 7)
+    sample = v[rng.integers(0, n, size=min(n, 100000))]
+    lo, hi = float(np.percentile(sample, 1)), float(np.percentile(sample, 99))
+    step = h / 2
+    gen = GenerationParameters(step_size=step, error_threshold=0.0, bias=5e-5, compact_image=1, prediction_coding=0,
+                               transform_to_bounds=1, transform_bound_eps=0.005, data_min=lo, data_max=hi)
+    rec = ReconstructionParameters(step_size=step, bias=5e-5, medium_emission=1.0, early_ray_termination=0.99)
+    cam = perspective_camera(eye=(1.9, -1.1, 1.45), target=(0.5, 0.5, 0.5), fov_deg=38.0, aspect=width / height)
+    name = name or f"sph{n}_h{h:g}_{width}x{height}_m{num_moments}"
+    return ParticleWorkload(name, x, y, z, v, h, dmin, dmax, width, height, num_moments, cam, gen, rec,
+                            transfer_function(seed + 1), tf_step=0.05)

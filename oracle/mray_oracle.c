@@ -30,6 +30,18 @@ void oracle_euler_exp_f32(float x, float out[2])
 }
 #define ORACLE_EXP_F32(v) ((float)exp((double)(v)))
 
+/* UniformGridDevice::getIndexFromCell (particle_grid.cuh:64-83): 4x4x4 tiles (4x4x1 for a flat grid) */
+uint32_t oracle_particles_cell_index(const oracle_particles *p, int cx, int cy, int cz)
+{
+    const int tx = 4, ty = 4, tz = p->tz;
+    int width_tiles = (p->sx + tx - 1) / tx;
+    int height_tiles = (p->sy + ty - 1) / ty;
+    int tile_x = cx / tx, tile_y = cy / ty, tile_z = cz / tz;
+    int in_x = cx % tx, in_y = cy % ty, in_z = cz % tz;
+    return (uint32_t)((tile_z * height_tiles * width_tiles + tile_y * width_tiles + tile_x) * (tx * ty * tz) +
+                      in_z * tx * ty + in_y * tx + in_x);
+}
+
 /* f32: the reference's arithmetic */
 #define R float
 #define SFX f32
@@ -47,6 +59,110 @@ void oracle_euler_exp_f32(float x, float out[2])
 #undef R
 #undef SFX
 #undef ORACLE_F32
+
+/* -------------------------------------------------------------------------------------------------------------
+ * SPH particle grid (Particles::create_grid, volume.cpp:55-81; createGridFromDomain, particle_grid.cuh:392-403,
+ * particle_grid.cpp:37-56; UniformGrid, particle_grid.cuh:284-306)
+ * ----------------------------------------------------------------------------------------------------------- */
+
+static uint32_t next_multiple(uint32_t x, int multiple) { return ((x - 1) / (uint32_t)multiple + 1) * (uint32_t)multiple; }
+
+typedef struct
+{
+    uint32_t cell;
+    uint64_t index;
+} cell_key;
+
+static int cmp_cell_key(const void *a, const void *b)
+{
+    const cell_key *x = (const cell_key *)a, *y = (const cell_key *)b;
+    if (x->cell != y->cell)
+        return x->cell < y->cell ? -1 : 1;
+    return x->index < y->index ? -1 : (x->index > y->index ? 1 : 0);
+}
+
+oracle_particles *oracle_particles_create(const float *x, const float *y, const float *z, const float *v, uint64_t n,
+                                          float h, const float dmin[3], const float dmax[3])
+{
+    if (n == 0)
+        return NULL;
+    oracle_particles *P = (oracle_particles *)calloc(1, sizeof(oracle_particles));
+    float mn[3] = {x[0], y[0], z[0]}, mx[3] = {x[0], y[0], z[0]};
+    for (uint64_t i = 1; i < n; ++i)
+    {
+        const float q[3] = {x[i], y[i], z[i]};
+        for (int k = 0; k < 3; ++k)
+        {
+            mn[k] = q[k] < mn[k] ? q[k] : mn[k]; /* std::min(min, x) */
+            mx[k] = mx[k] < q[k] ? q[k] : mx[k]; /* std::max(max, x) */
+        }
+    }
+    uint32_t g[3];
+    for (int k = 0; k < 3; ++k)
+        g[k] = (uint32_t)((mx[k] - mn[k]) / h + 1.0f);
+    P->sx = (int)next_multiple(g[0], 4);
+    P->sy = (int)next_multiple(g[1], 4);
+    P->sz = g[2] > 1 ? (int)next_multiple(g[2], 4) : (int)g[2];
+    P->tz = P->sz == 1 ? 1 : 4;
+    for (int k = 0; k < 3; ++k)
+    {
+        P->gmin[k] = mn[k];
+        P->dmin[k] = dmin[k];
+        P->dmax[k] = dmax[k];
+    }
+    P->inv_cell = (float)(1.0 / (double)h);
+    P->r2 = h * h;
+    P->h = h;
+    P->inv_h = 1.f / h;
+    P->total = (uint32_t)P->sx * (uint32_t)P->sy * (uint32_t)P->sz;
+    P->n = n;
+    cell_key *keys = (cell_key *)malloc(sizeof(cell_key) * n);
+    for (uint64_t i = 0; i < n; ++i)
+    {
+        int c[3];
+        const float q[3] = {x[i], y[i], z[i]};
+        const int sz[3] = {P->sx, P->sy, P->sz};
+        for (int k = 0; k < 3; ++k)
+        {
+            c[k] = (int)((q[k] - P->gmin[k]) * P->inv_cell);
+            /* the reference indexes out of its grid here when rounding lands on the padded edge; clamp */
+            c[k] = c[k] < 0 ? 0 : (c[k] > sz[k] - 1 ? sz[k] - 1 : c[k]);
+        }
+        keys[i].cell = oracle_particles_cell_index(P, c[0], c[1], c[2]);
+        keys[i].index = i;
+    }
+    qsort(keys, n, sizeof(cell_key), cmp_cell_key);
+    P->x = (float *)malloc(sizeof(float) * n);
+    P->y = (float *)malloc(sizeof(float) * n);
+    P->z = (float *)malloc(sizeof(float) * n);
+    P->v = (float *)malloc(sizeof(float) * n);
+    P->cell_start = (uint32_t *)calloc((size_t)P->total + 1, sizeof(uint32_t));
+    for (uint64_t i = 0; i < n; ++i)
+    {
+        const uint64_t j = keys[i].index;
+        P->x[i] = x[j];
+        P->y[i] = y[j];
+        P->z[i] = z[j];
+        P->v[i] = v[j];
+        P->cell_start[keys[i].cell + 1] += 1;
+    }
+    for (uint32_t c = 0; c < P->total; ++c)
+        P->cell_start[c + 1] += P->cell_start[c];
+    free(keys);
+    return P;
+}
+
+void oracle_particles_destroy(oracle_particles *P)
+{
+    if (!P)
+        return;
+    free(P->x);
+    free(P->y);
+    free(P->z);
+    free(P->v);
+    free(P->cell_start);
+    free(P);
+}
 
 /* -------------------------------------------------------------------------------------------------------------
  * Float-only container steps and integer / byte work

@@ -37,6 +37,29 @@ typedef struct oracle_grid
     float dmin[3], dmax[3];
 } oracle_grid;
 
+/* SPH particles (src/volume.h:125-157) with the reference's uniform grid (src/particle_grid.cuh:64-403): cell
+ * size = smoothing length, origin = the particles' minimum, 4x4x4-tiled cell order.  Built by
+ * oracle_particles_create, which sorts the particles by cell (stable: original order inside a cell) and keeps the
+ * first particle of every cell as a CSR start array. */
+typedef struct oracle_particles
+{
+    float *x, *y, *z, *v; /* sorted by cell */
+    uint64_t n;
+    float h, inv_h;
+    float dmin[3], dmax[3]; /* the ray box (the loader's domain) */
+    float gmin[3];
+    float inv_cell, r2;
+    int sx, sy, sz, tz;
+    uint32_t total;
+    uint32_t *cell_start; /* total + 1 */
+} oracle_particles;
+
+oracle_particles *oracle_particles_create(const float *x, const float *y, const float *z, const float *v, uint64_t n,
+                                          float h, const float dmin[3], const float dmax[3]);
+void oracle_particles_destroy(oracle_particles *p);
+/* cell order of the grid (UniformGridDevice::getIndexFromCell, particle_grid.cuh:64-83) */
+uint32_t oracle_particles_cell_index(const oracle_particles *p, int cx, int cy, int cz);
+
 /* Options that select between reference-faithful and exact evaluation. */
 typedef struct oracle_options
 {
@@ -49,6 +72,11 @@ typedef struct oracle_options
 
 #define ORACLE_DECL(R, SFX)                                                                                         \
     /* per-ray generation over an image (moment_raymarcher.cpp:121-166, raymarch_generate.h:69-148)         */      \
+    void oracle_generate_moments_particles_##SFX(const mraygb_camera *cam, const mraygb_generation_params *gp,     \
+                                                 const oracle_particles *parts, int width, int height,              \
+                                                 int num_moments, R *moments, uint16_t *bounds, uint32_t *counts,   \
+                                                 const oracle_options *opt);                                         \
+    R oracle_particles_sample_##SFX(const oracle_particles *parts, const R p[3]);                                   \
     void oracle_generate_moments_##SFX(const mraygb_camera *cam, const mraygb_generation_params *gp,               \
                                        const oracle_grid *grid, int width, int height, int num_moments,              \
                                        R *moments, uint16_t *bounds, uint32_t *counts, const oracle_options *opt);   \

@@ -71,6 +71,26 @@ def ref_lib():
         return _ref
 
 
+class ParticleSet:
+    """oracle_particles: the reference's uniform particle grid built by the oracle (owns its C memory)."""
+
+    def __init__(self, x, y, z, v, h, dmin, dmax):
+        L = lib()
+        self._keep = [np.ascontiguousarray(a, dtype=np.float32) for a in (x, y, z, v)]
+        self.n = self._keep[0].size
+        self.h = float(h)
+        self.dmin, self.dmax = tuple(dmin), tuple(dmax)
+        self.handle = L.oracle_particles_create(*[_ptr(a) for a in self._keep], self.n, self.h,
+                                                (C.c_float * 3)(*dmin), (C.c_float * 3)(*dmax))
+        if not self.handle:
+            raise ValueError("no particles")
+
+    def __del__(self):
+        if getattr(self, "handle", None):
+            lib().oracle_particles_destroy(self.handle)
+            self.handle = None
+
+
 def _declare(L):
     from mray_gb300.types import Camera, GenerationParameters, ReconstructionParameters
 
@@ -100,6 +120,17 @@ def _declare(L):
         getattr(L, f"oracle_grid_sample_{sfx}").argtypes = [P(Grid), C.c_void_p]
         getattr(L, f"oracle_grid_sample_{sfx}").restype = R
         getattr(L, f"oracle_tf_sample_{sfx}").argtypes = [C.c_void_p, R, R, C.c_void_p]
+    L.oracle_particles_create.restype = C.c_void_p
+    L.oracle_particles_create.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_float,
+                                          C.c_float * 3, C.c_float * 3]
+    L.oracle_particles_destroy.argtypes = [C.c_void_p]
+    for sfx, R in (("f32", C.c_float), ("f64", C.c_double)):
+        f = getattr(L, f"oracle_generate_moments_particles_{sfx}")
+        f.argtypes = [P(Camera), P(GenerationParameters), C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p,
+                      C.c_void_p, C.c_void_p, P(Options)]
+        f.restype = None
+        getattr(L, f"oracle_particles_sample_{sfx}").argtypes = [C.c_void_p, C.c_void_p]
+        getattr(L, f"oracle_particles_sample_{sfx}").restype = R
     L.oracle_compact.restype = C.c_uint64
     L.oracle_compact.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     L.oracle_prediction_encode.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_uint64, C.c_int,
@@ -166,6 +197,30 @@ def generate_moments(cam, gp, volume, dmin, dmax, width, height, m, precision="f
                                                        _ptr(moments), _ptr(bounds), _ptr(counts), C.byref(o))
     del keep
     return moments, bounds, counts
+
+
+def generate_moments_particles(cam, gp, parts: ParticleSet, width, height, m, precision="f32", nthreads=0,
+                               rows=None):
+    """generate_host's per-pixel loop over SPH particles: (moments[H,W,m], bounds[H,W,2] u16, counts[H,W] u32)."""
+    L = lib()
+    dt = _dt(precision)
+    moments = np.zeros((height, width, m), dtype=dt)
+    bounds = np.zeros((height, width, 2), dtype=np.uint16)
+    counts = np.zeros((height, width), dtype=np.uint32)
+    o = options(nthreads, rows)
+    getattr(L, f"oracle_generate_moments_particles_{precision}")(C.byref(cam), C.byref(gp), parts.handle, width,
+                                                                 height, m, _ptr(moments), _ptr(bounds),
+                                                                 _ptr(counts), C.byref(o))
+    return moments, bounds, counts
+
+
+def particles_sample(parts: ParticleSet, points, precision="f32"):
+    """Particles::sample at each point (N x 3)."""
+    L = lib()
+    dt = _dt(precision)
+    pts = np.ascontiguousarray(points, dtype=dt)
+    f = getattr(L, f"oracle_particles_sample_{precision}")
+    return np.array([f(parts.handle, _ptr(pts[i])) for i in range(pts.shape[0])], dtype=dt)
 
 
 def compact(counts, moments):

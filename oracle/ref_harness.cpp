@@ -167,6 +167,42 @@ int ref_generate_grid(const mraygb_camera *c, const mraygb_generation_params *g,
     return 0;
 }
 
+/* Particles::sample (volume.cpp:83-94) at npts points, with the grid Particles builds (volume.cpp:55-81). */
+int ref_particles_sample(const float *x, const float *y, const float *z, const float *v, uint64_t n, float h,
+                         const float *dmin, const float *dmax, const float *pts, uint64_t npts, float *out)
+{
+    Particles parts(to_range(dmin, dmax), std::vector<float>(x, x + n), std::vector<float>(y, y + n),
+                    std::vector<float>(z, z + n), std::vector<float>(v, v + n), h);
+    for (uint64_t i = 0; i < npts; ++i)
+        out[i] = parts.sample(Vec3f(pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]));
+    return 0;
+}
+
+/* generate() over Particles -> generate_host (moment_raymarcher.cpp:121-175). */
+int ref_generate_particles(const mraygb_camera *c, const mraygb_generation_params *g, const float *x, const float *y,
+                           const float *z, const float *v, uint64_t n, float h, const float *dmin, const float *dmax,
+                           int w, int hgt, int m, float *out_data, uint32_t *out_index, uint16_t *out_bounds,
+                           uint64_t *out_size)
+{
+    auto gp = to_gen(g);
+    Particles parts(to_range(dmin, dmax), std::vector<float>(x, x + n), std::vector<float>(y, y + n),
+                    std::vector<float>(z, z + n), std::vector<float>(v, v + n), h);
+    MomentImageHost mi(w, hgt, m, gp.compact_image, gp.transform_to_bounds);
+    mi.domain = parts.domain;
+    generate(to_camera(c), parts, mi, gp);
+    std::memcpy(out_data, mi.data.data(), sizeof(float) * mi.data.size());
+    *out_size = mi.data.size();
+    if (out_index && !mi.index.empty())
+        std::memcpy(out_index, mi.index.data(), sizeof(uint32_t) * mi.index.size());
+    if (out_bounds && mi.has_bounds())
+        for (size_t i = 0; i < mi.bounds.size(); ++i)
+        {
+            out_bounds[2 * i] = mi.bounds[i].lower;
+            out_bounds[2 * i + 1] = mi.bounds[i].upper;
+        }
+    return 0;
+}
+
 /* reconstruct() -> reconstruct_host (moment_raymarcher.cpp:283-337): u8 RGBA as the reference stores it. */
 int ref_reconstruct_u8(const mraygb_camera *c, const mraygb_reconstruction_params *r, int w, int h, int m,
                        const uint32_t *index, const float *data, uint64_t data_size, const uint16_t *bounds,
