@@ -85,6 +85,16 @@ uint64_t mraygb_kernel_launches(const mraygb_context *ctx);
 int mraygb_upload_grid(mraygb_context *ctx, const float *data, int nx, int ny, int nz, const float dmin[3],
                        const float dmax[3], int data_on_device);
 
+/* SPH particles (Particles, src/volume.h:125-157) with one smoothing length h, marched inside the box
+ * [dmin, dmax] (Particles::domain).  x, y, z, v are n floats each: host pointers, or device pointers when
+ * data_on_device != 0 (copied, not adopted).  The library builds the reference's uniform particle grid on the
+ * device (Particles::create_grid, src/volume.cpp:55-81: cell size h, origin at the particles' minimum, 4x4x4
+ * tiled cells), with the particles of a cell kept in their input order; it replaces the per-call upload of
+ * ParticlesDevice (src/volume_device.cuh:135-186).  The particles replace a grid uploaded before, and the other
+ * way round: generation samples the volume uploaded last.  1 <= n <= 2^31. */
+int mraygb_upload_particles(mraygb_context *ctx, const float *x, const float *y, const float *z, const float *v,
+                            uint64_t n, float h, const float dmin[3], const float dmax[3], int data_on_device);
+
 /* The transfer-function table that reconstruction samples: 256 RGBA float entries of one row of
  * TransferFunction::data (src/transfer_function.h:30-60).  read_from_disk / preintegrate build tables whose
  * 256 rows are all equal (src/transfer_function.cpp:46-97), so one row is the whole table. */
@@ -92,7 +102,8 @@ int mraygb_upload_tf(mraygb_context *ctx, const float *table_rgba256);
 
 /* ---- drop-in host API ----------------------------------------------------------------------------------- */
 
-/* generate_device(cam, RegularGrid, MomentImageHost, GenerationParameters) over the uploaded grid.
+/* generate_device(cam, RegularGrid or Particles, MomentImageHost, GenerationParameters) over the volume
+ * uploaded last.
  *   h_data         : capacity for W*H*m floats; receives the (compact, prediction-coded) moment data
  *   h_index        : W*H+1 u32 when gp->compact_image, else may be NULL      (MomentImageHost::index)
  *   h_bounds       : 2*W*H u16 (lower, upper) when gp->transform_to_bounds   (MomentImageHost::bounds)

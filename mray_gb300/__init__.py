@@ -7,13 +7,13 @@ grid and transfer-function containers) and calls the C ABI through ctypes.
 from .types import (CODING_WARP_DEFAULT_TRANSFORMED, CODING_WARP_NONE, Camera, GenerationParameters,
                     ReconstructionParameters)
 from .raymarcher import (MAX_MOMENTS, PRECISION_COMPENSATED_FP64_MESE, PRECISION_FP32, ColorImageHost, Context,
-                         MomentImageHost, RegularGrid, TransferFunction, default_context, default_quantization_table,
+                         MomentImageHost, Particles, RegularGrid, TransferFunction, default_context, default_quantization_table,
                          generate, preintegrate, quantize_prediction_coding, reconstruct)
 from ._lib import MrayError
 
 __all__ = [
     "Camera", "GenerationParameters", "ReconstructionParameters", "CODING_WARP_DEFAULT_TRANSFORMED",
-    "CODING_WARP_NONE", "ColorImageHost", "Context", "MomentImageHost", "RegularGrid", "TransferFunction",
+    "CODING_WARP_NONE", "ColorImageHost", "Context", "MomentImageHost", "Particles", "RegularGrid", "TransferFunction",
     "default_context", "default_quantization_table", "quantize_prediction_coding", "generate", "preintegrate", "reconstruct", "MrayError", "PRECISION_FP32",
     "PRECISION_COMPENSATED_FP64_MESE", "MAX_MOMENTS",
 ]

@@ -29,6 +29,7 @@ SOURCES = [
     ("reconstruct.cu", []),
     ("scan.cu", []),
     ("compact_noalloc.cu", []),
+    ("particles.cu", []),
     ("mese.cu", ["--fmad=false"]),
     ("mese_f64.cu", []),
     ("coding.cu", ["--fmad=false"]),

@@ -6,6 +6,8 @@
 
 #include "../../include/mraygb.h"
 
+#include <algorithm>
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -61,11 +63,19 @@ struct mraygb_context
     std::string error;
     uint64_t launches = 0;
 
-    // resident inputs
+    // resident inputs: the volume uploaded last (a grid or particles) and the transfer function
+    enum Volume
+    {
+        NONE,
+        GRID,
+        PARTICLES
+    } volume = NONE;
     DeviceBuffer grid;
     int nx = 0, ny = 0, nz = 0;
     float dmin[3] = {0, 0, 0}, dmax[3] = {0, 0, 0};
-    bool has_grid = false;
+    DeviceBuffer particle_pts, particle_cells;
+    ParticleGridParams particle_grid{};
+    uint64_t num_particles = 0;
     DeviceBuffer tf;
     bool has_tf = false;
 
@@ -145,6 +155,20 @@ GridView grid_view(const mraygb_context *ctx)
     return g;
 }
 
+ParticleView particle_view(const mraygb_context *ctx)
+{
+    ParticleView v;
+    v.g = ctx->particle_grid;
+    v.pts = ctx->particle_pts.as<float4>();
+    v.cell_start = ctx->particle_cells.as<uint32_t>();
+    for (int i = 0; i < 3; ++i)
+    {
+        v.dmin[i] = ctx->dmin[i];
+        v.dmax[i] = ctx->dmax[i];
+    }
+    return v;
+}
+
 int check_device_error_flag(mraygb_context *ctx)
 {
     int flag = 0;
@@ -174,13 +198,19 @@ int validate_gen(mraygb_context *ctx, const mraygb_generation_params *gp)
 }
 
 int run_generate_moments(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_generation_params *gp,
-                         int width, int height, int m, float *d_moments, uint16_t *d_bounds, uint32_t *d_counts)
+                         int width, int height, int m, float *d_moments, uint16_t *d_bounds, uint32_t *d_counts,
+                         float4 *d_bounds4 = nullptr)
 {
     const DeviceCamera dc = to_device_camera(*cam);
-    CK(launch_generate_grid(grid_view(ctx), dc, *gp, width, height, m,
-                            ctx->precision == MRAYGB_PRECISION_COMPENSATED_FP64_MESE, d_moments, d_bounds, d_counts,
-                            ctx->error_flag.as<int>(), ctx->stream),
-       "generate kernel launch");
+    const bool kahan = ctx->precision == MRAYGB_PRECISION_COMPENSATED_FP64_MESE;
+    if (ctx->volume == mraygb_context::PARTICLES)
+        CK(launch_generate_particles(particle_view(ctx), dc, *gp, width, height, m, kahan, d_moments, d_bounds,
+                                     d_counts, d_bounds4, ctx->error_flag.as<int>(), ctx->stream),
+           "generate kernel launch");
+    else
+        CK(launch_generate_grid(grid_view(ctx), dc, *gp, width, height, m, kahan, d_moments, d_bounds, d_counts,
+                                d_bounds4, ctx->error_flag.as<int>(), ctx->stream),
+           "generate kernel launch");
     ctx->launches += 1;
     if (gp->compact_image && d_counts && gp->error_threshold != 0.f)
     {
@@ -416,7 +446,8 @@ void mraygb_destroy(mraygb_context *ctx)
     cudaSetDevice(ctx->device);
     if (ctx->stream)
         cudaStreamSynchronize(ctx->stream);
-    DeviceBuffer *bufs[] = {&ctx->grid,    &ctx->tf,       &ctx->moments,       &ctx->counts,
+    DeviceBuffer *bufs[] = {&ctx->grid,    &ctx->particle_pts, &ctx->particle_cells,
+                            &ctx->tf,       &ctx->moments,       &ctx->counts,
                             &ctx->index,   &ctx->compact,  &ctx->bounds,        &ctx->coding_params,
                             &ctx->pmoments, &ctx->rgba,    &ctx->rgba8,         &ctx->scan_scratch,
                             &ctx->error_flag, &ctx->coding_partial, &ctx->coding_params_f, &ctx->table,
@@ -481,9 +512,123 @@ int mraygb_upload_grid(mraygb_context *ctx, const float *data, int nx, int ny, i
         ctx->dmin[i] = dmin[i];
         ctx->dmax[i] = dmax[i];
     }
-    ctx->has_grid = true;
+    ctx->volume = mraygb_context::GRID;
+    ctx->particle_pts.release();
+    ctx->particle_cells.release();
     if (!data_on_device)
         CK(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+    return MRAYGB_OK;
+}
+
+int mraygb_upload_particles(mraygb_context *ctx, const float *x, const float *y, const float *z, const float *v,
+                            uint64_t n, float h, const float dmin[3], const float dmax[3], int data_on_device)
+{
+    CHECK_CTX();
+    if (!x || !y || !z || !v || !dmin || !dmax)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "NULL particle array or domain");
+    if (n == 0 || n > (1ull << 31))
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "particle count %llu outside 1..2^31", (unsigned long long)n);
+    if (!(h > 0.f) || !std::isfinite(h))
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "smoothing length must be finite and > 0 (got %g)", (double)h);
+    for (int i = 0; i < 3; ++i)
+        if (!(dmax[i] > dmin[i]))
+            return fail(ctx, MRAYGB_INVALID_ARGUMENT, "empty domain along axis %d", i);
+
+    // the buffers of a previous volume may be overwritten from here on; on failure no volume is resident
+    ctx->volume = mraygb_context::NONE;
+
+    // temporaries of the build, released at the end
+    DeviceBuffer stage, keys, keys_alt, vals, vals_alt, counts, hist, hist_scan, minmax;
+    struct Release
+    {
+        DeviceBuffer *b[9];
+        ~Release()
+        {
+            for (DeviceBuffer *p : b)
+                p->release();
+        }
+    } release{{&stage, &keys, &keys_alt, &vals, &vals_alt, &counts, &hist, &hist_scan, &minmax}};
+
+    const float *dx = x, *dy = y, *dz = z, *dv = v;
+    if (!data_on_device)
+    {
+        CK(stage.reserve(4 * n * sizeof(float)), "particle staging allocation");
+        float *s = stage.as<float>();
+        const float *src[4] = {x, y, z, v};
+        for (int k = 0; k < 4; ++k)
+            CK(cudaMemcpyAsync(s + k * n, src[k], n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream),
+               "particle upload");
+        dx = s;
+        dy = s + n;
+        dz = s + 2 * n;
+        dv = s + 3 * n;
+    }
+
+    // 1. bounding box of the particles -> grid parameters (createGridFromDomain)
+    const size_t mm_floats = particle_minmax_scratch_floats(n);
+    CK(minmax.reserve((mm_floats + 6) * sizeof(float)), "particle scratch allocation");
+    float *box_d = minmax.as<float>() + mm_floats;
+    CK(launch_particle_minmax(dx, dy, dz, n, minmax.as<float>(), box_d, ctx->stream), "particle bounds kernel");
+    float box[6];
+    CK(cudaMemcpyAsync(box, box_d, sizeof(box), cudaMemcpyDeviceToHost, ctx->stream), "reading particle bounds");
+    CK(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+    ctx->launches += 2;
+    uint64_t cells = 1;
+    for (int k = 0; k < 3; ++k)
+    {
+        const float c = (box[3 + k] - box[k]) / h + 1.0f;
+        if (!std::isfinite(c) || c >= 16777216.f)
+            return fail(ctx, MRAYGB_INVALID_ARGUMENT, "particle extent / h = %g cells along axis %d", (double)c, k);
+        cells *= (uint64_t)c + 4;
+    }
+    if (cells > (1ull << 30))
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "the particle grid needs about %llu cells (limit 2^30): h too small",
+                    (unsigned long long)cells);
+    const ParticleGridParams g = particle_grid_params(box, box + 3, h);
+    const uint32_t total = g.total;
+
+    // 2. cell of every particle, per-cell counts, CSR starts
+    CK(keys.reserve(n * sizeof(uint32_t)), "particle key allocation");
+    CK(counts.reserve((size_t)total * sizeof(uint32_t)), "particle cell count allocation");
+    CK(ctx->particle_cells.reserve(((size_t)total + 1) * sizeof(uint32_t)), "particle cell allocation");
+    CK(cudaMemsetAsync(counts.ptr, 0, (size_t)total * sizeof(uint32_t), ctx->stream), "clearing cell counts");
+    CK(launch_particle_cells(dx, dy, dz, n, g, keys.as<uint32_t>(), counts.as<uint32_t>(), ctx->stream),
+       "particle cell kernel");
+    const size_t hw = particle_radix_hist_words((uint32_t)n);
+    const size_t words = std::max(scan_scratch_words(total), scan_scratch_words(hw)) + 1;
+    CK(ctx->scan_scratch.reserve(words * sizeof(uint32_t)), "scan scratch allocation");
+    int launches = 1;
+    CK(launch_exclusive_scan(counts.as<uint32_t>(), ctx->particle_cells.as<uint32_t>(), total,
+                             ctx->scan_scratch.as<uint32_t>(), ctx->stream, &launches),
+       "cell scan");
+
+    // 3. stable sort by cell, 4. gather into (x, y, z, v) records
+    CK(keys_alt.reserve(n * sizeof(uint32_t)), "particle key allocation");
+    CK(vals.reserve(n * sizeof(uint32_t)), "particle index allocation");
+    CK(vals_alt.reserve(n * sizeof(uint32_t)), "particle index allocation");
+    CK(hist.reserve(hw * sizeof(uint32_t)), "radix histogram allocation");
+    CK(hist_scan.reserve((hw + 1) * sizeof(uint32_t)), "radix histogram allocation");
+    uint32_t *order = nullptr;
+    CK(launch_particle_sort((uint32_t)n, total, keys.as<uint32_t>(), keys_alt.as<uint32_t>(), vals.as<uint32_t>(),
+                            vals_alt.as<uint32_t>(), hist.as<uint32_t>(), hist_scan.as<uint32_t>(),
+                            ctx->scan_scratch.as<uint32_t>(), &order, ctx->stream, &launches),
+       "particle sort");
+    CK(ctx->particle_pts.reserve(n * sizeof(float4)), "particle allocation");
+    CK(launch_particle_gather(n, order, dx, dy, dz, dv, ctx->particle_pts.as<float4>(), ctx->stream),
+       "particle gather kernel");
+    launches += 1;
+    CK(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+    ctx->launches += (uint64_t)launches;
+
+    ctx->particle_grid = g;
+    ctx->num_particles = n;
+    for (int i = 0; i < 3; ++i)
+    {
+        ctx->dmin[i] = dmin[i];
+        ctx->dmax[i] = dmax[i];
+    }
+    ctx->volume = mraygb_context::PARTICLES;
+    ctx->grid.release();
     return MRAYGB_OK;
 }
 
@@ -514,7 +659,7 @@ int mraygb_stage_generate_moments(mraygb_context *ctx, const mraygb_camera *cam,
         return rc;
     if (!cam || !d_moments)
         return fail(ctx, MRAYGB_INVALID_ARGUMENT, "camera or moment buffer is NULL");
-    if (!ctx->has_grid)
+    if (ctx->volume == mraygb_context::NONE)
         return fail(ctx, MRAYGB_NO_VOLUME, "no volume uploaded");
     if (gp->compact_image && !d_counts)
         return fail(ctx, MRAYGB_INVALID_ARGUMENT, "compact_image needs a count buffer");
@@ -683,7 +828,7 @@ int mraygb_generate(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_
         return fail(ctx, MRAYGB_INVALID_ARGUMENT, "compact_image needs an index buffer");
     if (gp->transform_to_bounds && !h_bounds)
         return fail(ctx, MRAYGB_INVALID_ARGUMENT, "transform_to_bounds needs a bounds buffer");
-    if (!ctx->has_grid)
+    if (ctx->volume == mraygb_context::NONE)
         return fail(ctx, MRAYGB_NO_VOLUME, "no volume uploaded");
     if (gp->prediction_coding && gp->coding_warp == MRAYGB_CODING_WARP_DEFAULT_TRANSFORMED && m > 1 &&
         !h_coding_params)

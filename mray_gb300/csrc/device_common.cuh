@@ -170,6 +170,119 @@ __device__ __forceinline__ float grid_sample(const GridView &g, float px, float 
     return s;
 }
 
+// ---- SPH particles ----------------------------------------------------------------------------------------
+// The reference's uniform grid (src/particle_grid.cuh:284-306, createGridFromDomain :392-403): cell size = the
+// smoothing length h, origin at the particles' minimum, sx and sy padded to multiples of 4 (sz too unless the
+// grid is flat), cells in 4x4x4 tiles (4x4x1 when flat).
+struct ParticleGridParams
+{
+    float gmin[3];
+    float inv_cell; // (float)(1.0 / h)
+    float r2;       // h * h
+    float inv_h;    // 1.f / h
+    int sx, sy, sz, tz;
+    uint32_t total;
+};
+
+struct ParticleView
+{
+    ParticleGridParams g;
+    const float4 *pts;          // (x, y, z, value) sorted by cell, input order inside a cell
+    const uint32_t *cell_start; // CSR: the particles of cell c are [cell_start[c], cell_start[c + 1])
+    float dmin[3], dmax[3];     // the ray box (Particles::domain)
+};
+
+// getIndexFromCell (src/particle_grid.cuh:64-83)
+__host__ __device__ __forceinline__ uint32_t particle_cell_index(const ParticleGridParams &g, int cx, int cy, int cz)
+{
+    const int width_tiles = (g.sx + 3) / 4, height_tiles = (g.sy + 3) / 4;
+    const int tile = (cz / g.tz) * height_tiles * width_tiles + (cy / 4) * width_tiles + cx / 4;
+    return (uint32_t)(tile * (16 * g.tz) + (cz % g.tz) * 16 + (cy % 4) * 4 + cx % 4);
+}
+
+// the cell of a particle during the grid build (getCellIndex, clamped: the reference indexes past its grid when
+// rounding lands a particle on the padded edge)
+__device__ __forceinline__ uint32_t particle_cell(const ParticleGridParams &g, float x, float y, float z)
+{
+    const float p[3] = {x, y, z};
+    const int s[3] = {g.sx, g.sy, g.sz};
+    int c[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+    {
+        c[k] = (int)__fmul_rn(__fsub_rn(p[k], g.gmin[k]), g.inv_cell);
+        c[k] = c[k] < 0 ? 0 : (c[k] > s[k] - 1 ? s[k] - 1 : c[k]);
+    }
+    return particle_cell_index(g, c[0], c[1], c[2]);
+}
+
+// cubicSpline (src/cut/kernels.h:55-64)
+__device__ __forceinline__ float cubic_spline(float x)
+{
+    constexpr float sigma = 0.5641895835477563f;
+    if (x < 1.f)
+        return __fmul_rn(sigma, __fsub_rn(1.f, __fmul_rn(__fmul_rn(__fmul_rn(1.5f, x), x),
+                                                        __fsub_rn(1.f, __fmul_rn(x, 0.5f)))));
+    if (x < 2.f)
+    {
+        const float u = __fsub_rn(2.f, x);
+        return __fmul_rn(__fmul_rn(__fmul_rn(sigma / 4.f, u), u), u);
+    }
+    return 0.f;
+}
+
+// Particles::sample (src/volume.cpp:83-94): the 27 cells around p in z, y, x order (forEachNeighbor,
+// src/particle_grid.cuh:156-211), weights W(|p - x_i| / h) for |p - x_i|^2 < h^2, normalised by their sum
+// (InterpolateParticlesOp, src/particle_interpolate.h:35-58).  Cells come from the CSR array instead of the
+// reference's EMPTY_CELL scan; the particles visited and their order are the same.
+__device__ __forceinline__ float particle_sample(const ParticleView &v, float px, float py, float pz)
+{
+    const float p[3] = {px, py, pz};
+    const int s[3] = {v.g.sx, v.g.sy, v.g.sz};
+    int lo[3], hi[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+    {
+        int c = (int)__fmul_rn(__fsub_rn(p[k], v.g.gmin[k]), v.g.inv_cell);
+        c = c < -2 ? -2 : (c > s[k] + 1 ? s[k] + 1 : c); // no effect on the loop ranges below
+        lo[k] = c - 1 > 0 ? c - 1 : 0;
+        hi[k] = c + 2 < s[k] ? c + 2 : s[k];
+    }
+    float value = 0.f, wsum = 0.f;
+    for (int z = lo[2]; z < hi[2]; ++z)
+        for (int y = lo[1]; y < hi[1]; ++y)
+            for (int x = lo[0]; x < hi[0]; ++x)
+            {
+                const uint32_t cell = particle_cell_index(v.g, x, y, z);
+                const uint32_t b = __ldg(v.cell_start + cell), e = __ldg(v.cell_start + cell + 1);
+                for (uint32_t i = b; i < e; ++i)
+                {
+                    const float4 q = __ldg(v.pts + i);
+                    const float dx = __fsub_rn(px, q.x), dy = __fsub_rn(py, q.y), dz = __fsub_rn(pz, q.z);
+                    const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+                    if (d2 < v.g.r2)
+                    {
+                        const float w = cubic_spline(__fmul_rn(__fsqrt_rn(d2), v.g.inv_h));
+                        wsum = __fadd_rn(wsum, w);
+                        value = __fadd_rn(value, __fmul_rn(w, q.w));
+                    }
+                }
+            }
+    if (wsum != 0.f)
+        value = __fdiv_rn(value, wsum);
+    return value;
+}
+
+// the two volumes behind one generate kernel: the ray box and one sample
+__device__ __forceinline__ float volume_sample(const GridView &g, float x, float y, float z)
+{
+    return grid_sample(g, x, y, z);
+}
+__device__ __forceinline__ float volume_sample(const ParticleView &v, float x, float y, float z)
+{
+    return particle_sample(v, x, y, z);
+}
+
 __device__ __forceinline__ float map_density(float s, float dmin, float dmax)
 {
     return rclamp(__fdiv_rn(__fsub_rn(s, dmin), __fsub_rn(dmax, dmin)), 0.f, 1.f);
@@ -192,6 +305,38 @@ struct cf
 };
 __device__ __forceinline__ cf cmul(cf a, cf b) { return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x}; }
 __device__ __forceinline__ cf csq(cf a) { return {a.x * a.x - a.y * a.y, 2.f * a.x * a.y}; }
+
+// alpha_j(h) = sin(jh)/j and beta_j(h) = (sin(jh) - jh cos(jh)) / (j^2 h); beta by its series for small jh
+__device__ __forceinline__ void seg_coeffs(int j, float h, float &alpha, float &beta)
+{
+    if (j == 0)
+    {
+        alpha = h;
+        beta = 0.f;
+        return;
+    }
+    const float x = (float)j * h;
+    float s, c;
+    sincosf(x, &s, &c);
+    alpha = s / (float)j;
+    float num;
+    if (fabsf(x) < 0.5f)
+    {
+        // sin x - x cos x = x^3/3 - x^5/30 + x^7/840 - x^9/45360 + x^11/3991680 - ...
+        const float x2 = x * x;
+        float poly = 1.f / 3991680.f;
+        poly = fmaf(poly, -x2, 1.f / 45360.f);
+        poly = fmaf(poly, -x2, 1.f / 840.f);
+        poly = fmaf(poly, -x2, 1.f / 30.f);
+        poly = fmaf(poly, -x2, 1.f / 3.f);
+        num = poly * x2 * x;
+    }
+    else
+    {
+        num = s - x * c;
+    }
+    beta = num / ((float)j * x);
+}
 
 // Kahan-compensated accumulation of `v` into (sum, comp)
 __device__ __forceinline__ void kahan_add(float &sum, float &comp, float v)

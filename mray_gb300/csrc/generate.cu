@@ -1,4 +1,6 @@
-// Moment generation over a regular grid: one ray per 4-lane quad, moments split across the quad's lanes.
+// Moment generation over a regular grid or SPH particles: one ray per 4-lane quad, moments split across the
+// quad's lanes.  The two volumes share the kernel body (generate_quads); they differ only in the sample
+// (corner-aligned trilinear grid sample, or the SPH sum over the 27 neighbour cells) and the ray box.
 //
 // Method (src/raymarch_generate.h:35-148).  A ray is marched from t_near in steps of `step` while
 // t + step < t_far (t accumulated in float exactly as the reference does), with one last sample at t_far.
@@ -34,9 +36,9 @@ namespace
 
 constexpr unsigned kFull = 0xffffffffu;
 
-struct GenArgs
+template <class V> struct GenArgs
 {
-    GridView grid;
+    V vol; // GridView or ParticleView
     DeviceCamera cam;
     int width, height, m;
     float step;
@@ -48,43 +50,11 @@ struct GenArgs
     float *moments;
     uint16_t *bounds;
     uint32_t *counts;
+    float4 *bounds4; // the differentiation form: (lo, hi, min, max) of the samples, unquantized, or NULL
     int *error_flag;
 };
 
-// alpha_j(h) = sin(jh)/j and beta_j(h) = (sin(jh) - jh cos(jh)) / (j^2 h); beta by its series for small jh
-__device__ __forceinline__ void seg_coeffs(int j, float h, float &alpha, float &beta)
-{
-    if (j == 0)
-    {
-        alpha = h;
-        beta = 0.f;
-        return;
-    }
-    const float x = (float)j * h;
-    float s, c;
-    sincosf(x, &s, &c);
-    alpha = s / (float)j;
-    float num;
-    if (fabsf(x) < 0.5f)
-    {
-        // sin x - x cos x = x^3/3 - x^5/30 + x^7/840 - x^9/45360 + x^11/3991680 - ...
-        const float x2 = x * x;
-        float poly = 1.f / 3991680.f;
-        poly = fmaf(poly, -x2, 1.f / 45360.f);
-        poly = fmaf(poly, -x2, 1.f / 840.f);
-        poly = fmaf(poly, -x2, 1.f / 30.f);
-        poly = fmaf(poly, -x2, 1.f / 3.f);
-        num = poly * x2 * x;
-    }
-    else
-    {
-        num = s - x * c;
-    }
-    beta = num / ((float)j * x);
-}
-
-template <int NJ, bool KAHAN>
-__global__ void __launch_bounds__(128) generate_grid_kernel(const GenArgs a)
+template <class V, int NJ, bool KAHAN> __device__ __forceinline__ void generate_quads(const GenArgs<V> &a)
 {
     const int lane = threadIdx.x & 31;
     const int q = lane & 3;
@@ -102,8 +72,8 @@ __global__ void __launch_bounds__(128) generate_grid_kernel(const GenArgs a)
         float nx, ny;
         pixel_ndc(px, py, a.width, a.height, nx, ny);
         eye_ray(a.cam, nx, ny, o, d);
-        const float bmin[3] = {a.grid.dmin[0], a.grid.dmin[1], a.grid.dmin[2]};
-        const float bmax[3] = {a.grid.dmax[0], a.grid.dmax[1], a.grid.dmax[2]};
+        const float bmin[3] = {a.vol.dmin[0], a.vol.dmin[1], a.vol.dmin[2]};
+        const float bmax[3] = {a.vol.dmax[0], a.vol.dmax[1], a.vol.dmax[2]};
         hit = intersect_aabb(o, d, bmin, bmax, t_near, t_far);
         t_near = rmax(t_near, a.cam.znear);
         hit = hit && (t_far > 0.f);
@@ -129,7 +99,7 @@ __global__ void __launch_bounds__(128) generate_grid_kernel(const GenArgs a)
     {
         pti = (float)(3.141592653589793 / (double)__fsub_rn(t_far, t_near));
         pss = (float)(3.141592653589793 * (double)__fdiv_rn(step, __fsub_rn(t_far, t_near)));
-        const float f0 = map_density(grid_sample(a.grid, __fadd_rn(o[0], __fmul_rn(t, d[0])),
+        const float f0 = map_density(volume_sample(a.vol, __fadd_rn(o[0], __fmul_rn(t, d[0])),
                                                  __fadd_rn(o[1], __fmul_rn(t, d[1])),
                                                  __fadd_rn(o[2], __fmul_rn(t, d[2]))),
                                      a.data_min, a.data_max);
@@ -171,7 +141,7 @@ __global__ void __launch_bounds__(128) generate_grid_kernel(const GenArgs a)
         if (my_valid)
         {
             p_my = sub_pi(__fmul_rn(__fsub_rn(my_t, t_near), pti));
-            f_my = map_density(grid_sample(a.grid, __fadd_rn(o[0], __fmul_rn(my_t, d[0])),
+            f_my = map_density(volume_sample(a.vol, __fadd_rn(o[0], __fmul_rn(my_t, d[0])),
                                            __fadd_rn(o[1], __fmul_rn(my_t, d[1])),
                                            __fadd_rn(o[2], __fmul_rn(my_t, d[2]))),
                                a.data_min, a.data_max);
@@ -270,7 +240,7 @@ __global__ void __launch_bounds__(128) generate_grid_kernel(const GenArgs a)
     float f_far = 0.f;
     if (hit)
     {
-        f_far = map_density(grid_sample(a.grid, __fadd_rn(o[0], __fmul_rn(t_far, d[0])),
+        f_far = map_density(volume_sample(a.vol, __fadd_rn(o[0], __fmul_rn(t_far, d[0])),
                                         __fadd_rn(o[1], __fmul_rn(t_far, d[1])),
                                         __fadd_rn(o[2], __fmul_rn(t_far, d[2]))),
                             a.data_min, a.data_max);
@@ -301,6 +271,8 @@ __global__ void __launch_bounds__(128) generate_grid_kernel(const GenArgs a)
             }
             if (a.counts && a.compact_image)
                 a.counts[pix] = 0;
+            if (a.bounds4)
+                a.bounds4[pix] = make_float4(0.f, 0.f, 0.f, 0.f);
         }
         return;
     }
@@ -354,6 +326,8 @@ __global__ void __launch_bounds__(128) generate_grid_kernel(const GenArgs a)
 
     if (q == 0)
     {
+        if (a.bounds4)
+            a.bounds4[pix] = make_float4(lo, hi, blo, bhi);
         const uint16_t lo16 = (uint16_t)__fmul_rn(lo, 65535.f);
         const uint16_t hi16 = (uint16_t)__fmul_rn(hi, 65535.f);
         if (a.bounds && a.transform_to_bounds)
@@ -371,25 +345,42 @@ __global__ void __launch_bounds__(128) generate_grid_kernel(const GenArgs a)
     }
 }
 
-template <int NJ>
-void launch_nj(const GenArgs &a, bool kahan, cudaStream_t stream)
+template <int NJ, bool KAHAN> __global__ void __launch_bounds__(128) generate_grid_kernel(const GenArgs<GridView> a)
 {
-    dim3 block(128);
-    dim3 grid((a.width + 7) / 8, (a.height + 3) / 4);
-    if (kahan)
-        generate_grid_kernel<NJ, true><<<grid, block, 0, stream>>>(a);
-    else
-        generate_grid_kernel<NJ, false><<<grid, block, 0, stream>>>(a);
+    generate_quads<GridView, NJ, KAHAN>(a);
 }
 
-} // namespace
-
-cudaError_t launch_generate_grid(const GridView &grid, const DeviceCamera &cam, const mraygb_generation_params &gp,
-                                 int width, int height, int m, bool kahan, float *moments, uint16_t *bounds,
-                                 uint32_t *counts, int *error_flag, cudaStream_t stream)
+template <int NJ, bool KAHAN>
+__global__ void __launch_bounds__(128) generate_particles_kernel(const GenArgs<ParticleView> a)
 {
-    GenArgs a;
-    a.grid = grid;
+    generate_quads<ParticleView, NJ, KAHAN>(a);
+}
+
+template <int NJ, bool KAHAN> void launch_kernel(const GenArgs<GridView> &a, dim3 grid, cudaStream_t stream)
+{
+    generate_grid_kernel<NJ, KAHAN><<<grid, 128, 0, stream>>>(a);
+}
+template <int NJ, bool KAHAN> void launch_kernel(const GenArgs<ParticleView> &a, dim3 grid, cudaStream_t stream)
+{
+    generate_particles_kernel<NJ, KAHAN><<<grid, 128, 0, stream>>>(a);
+}
+
+template <int NJ, class V> void launch_nj(const GenArgs<V> &a, bool kahan, cudaStream_t stream)
+{
+    const dim3 grid((a.width + 7) / 8, (a.height + 3) / 4);
+    if (kahan)
+        launch_kernel<NJ, true>(a, grid, stream);
+    else
+        launch_kernel<NJ, false>(a, grid, stream);
+}
+
+template <class V>
+cudaError_t launch_generate(const V &vol, const DeviceCamera &cam, const mraygb_generation_params &gp, int width,
+                            int height, int m, bool kahan, float *moments, uint16_t *bounds, uint32_t *counts,
+                            float4 *bounds4, int *error_flag, cudaStream_t stream)
+{
+    GenArgs<V> a;
+    a.vol = vol;
     a.cam = cam;
     a.width = width;
     a.height = height;
@@ -404,6 +395,7 @@ cudaError_t launch_generate_grid(const GridView &grid, const DeviceCamera &cam, 
     a.moments = moments;
     a.bounds = bounds;
     a.counts = counts;
+    a.bounds4 = bounds4;
     a.error_flag = error_flag;
     const int nj = (m + 3) / 4;
     if (nj <= 1)
@@ -421,6 +413,25 @@ cudaError_t launch_generate_grid(const GridView &grid, const DeviceCamera &cam, 
     else
         launch_nj<64>(a, kahan, stream);
     return cudaGetLastError();
+}
+
+} // namespace
+
+cudaError_t launch_generate_grid(const GridView &grid, const DeviceCamera &cam, const mraygb_generation_params &gp,
+                                 int width, int height, int m, bool kahan, float *moments, uint16_t *bounds,
+                                 uint32_t *counts, float4 *bounds4, int *error_flag, cudaStream_t stream)
+{
+    return launch_generate(grid, cam, gp, width, height, m, kahan, moments, bounds, counts, bounds4, error_flag,
+                           stream);
+}
+
+cudaError_t launch_generate_particles(const ParticleView &parts, const DeviceCamera &cam,
+                                      const mraygb_generation_params &gp, int width, int height, int m, bool kahan,
+                                      float *moments, uint16_t *bounds, uint32_t *counts, float4 *bounds4,
+                                      int *error_flag, cudaStream_t stream)
+{
+    return launch_generate(parts, cam, gp, width, height, m, kahan, moments, bounds, counts, bounds4, error_flag,
+                           stream);
 }
 
 } // namespace mraygb

@@ -10,12 +10,40 @@ namespace mraygb
 {
 
 struct GridView;
+struct ParticleView;
+struct ParticleGridParams;
 struct DeviceCamera;
 
 // generate.cu
 cudaError_t launch_generate_grid(const GridView &grid, const DeviceCamera &cam, const mraygb_generation_params &gp,
                                  int width, int height, int m, bool kahan, float *moments, uint16_t *bounds,
-                                 uint32_t *counts, int *error_flag, cudaStream_t stream);
+                                 uint32_t *counts, float4 *bounds4, int *error_flag, cudaStream_t stream);
+
+cudaError_t launch_generate_particles(const ParticleView &parts, const DeviceCamera &cam,
+                                      const mraygb_generation_params &gp, int width, int height, int m, bool kahan,
+                                      float *moments, uint16_t *bounds, uint32_t *counts, float4 *bounds4,
+                                      int *error_flag, cudaStream_t stream);
+
+// particles.cu: the particle grid build
+ParticleGridParams particle_grid_params(const float mn[3], const float mx[3], float h);
+size_t particle_minmax_scratch_floats(uint64_t n);
+// min (out6[0..2]) and max (out6[3..5]) of the positions
+cudaError_t launch_particle_minmax(const float *x, const float *y, const float *z, uint64_t n, float *scratch,
+                                   float *out6, cudaStream_t stream);
+// cell of every particle and per-cell counts (counts zeroed by the caller)
+cudaError_t launch_particle_cells(const float *x, const float *y, const float *z, uint64_t n,
+                                  const ParticleGridParams &g, uint32_t *cell_of, uint32_t *counts,
+                                  cudaStream_t stream);
+// stable LSD radix sort of n cell keys (< total) with the particle index as payload; keys and keys_alt are
+// overwritten, *sorted_vals points at vals or vals_alt.  hist holds particle_radix_hist_words(n) words, hist_scan
+// one more, scan_scratch scan_scratch_words(particle_radix_hist_words(n)).
+size_t particle_radix_hist_words(uint32_t n);
+cudaError_t launch_particle_sort(uint32_t n, uint32_t total, uint32_t *keys, uint32_t *keys_alt, uint32_t *vals,
+                                 uint32_t *vals_alt, uint32_t *hist, uint32_t *hist_scan, uint32_t *scan_scratch,
+                                 uint32_t **sorted_vals, cudaStream_t stream, int *launches);
+// pts[i] = (x, y, z, v)[order[i]]
+cudaError_t launch_particle_gather(uint64_t n, const uint32_t *order, const float *x, const float *y, const float *z,
+                                   const float *v, float4 *pts, cudaStream_t stream);
 
 // mese.cu
 cudaError_t mese_init_constants();
@@ -73,6 +101,10 @@ struct ReconArgs
     float step, emission, ert;
     float *rgba;
     uint8_t *rgba8;
+    // the differentiation form: per-pixel (lo, hi, ., .) float bounds instead of the u16 ones, and the transfer
+    // function sampled linearly in the front density (texture convention)
+    const float4 *bounds4 = nullptr;
+    int tf_linear = 0;
 };
 cudaError_t launch_reconstruct(const ReconArgs &a, int *error_flag, cudaStream_t stream);
 

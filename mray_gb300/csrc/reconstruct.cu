@@ -36,6 +36,7 @@ struct ReconDev
     float step, emission, ert;
     float *rgba;
     uint8_t *rgba8;
+    const float4 *bounds4;
     int *error_flag;
 };
 
@@ -79,6 +80,30 @@ __device__ __forceinline__ float4 tf_sample(const float4 *T, float fs, float bs)
     return r;
 }
 
+// The differentiation form's transfer function: the row sampled linearly in the front density with the texture
+// convention of TransferFunctionDevice::sample (src/transfer_function_device.cuh:30-65: linear filter, normalised
+// coordinates, clamp; the rows being equal, the back density drops out).  Weight of entry x1 in *w, entries in
+// *x0 / *x1 (equal where clamped).
+__device__ __forceinline__ float4 tf_sample_linear(const float4 *T, float fs, int *x0o = nullptr, int *x1o = nullptr,
+                                                   float *wo = nullptr)
+{
+    const float u = fs * 256.f - 0.5f;
+    const float fl = floorf(u);
+    const float w = u - fl;
+    const int xl = (int)fl;
+    const int x0 = min(max(xl, 0), 255);
+    const int x1 = min(max(xl + 1, 0), 255);
+    const float4 a = T[x0], b = T[x1];
+    if (x0o)
+    {
+        *x0o = x0;
+        *x1o = x1;
+        *wo = w;
+    }
+    return make_float4((1.f - w) * a.x + w * b.x, (1.f - w) * a.y + w * b.y, (1.f - w) * a.z + w * b.z,
+                       (1.f - w) * a.w + w * b.w);
+}
+
 // S(theta) = sum_{k=0}^{n-1} a_k cos(k theta), a_0 = l_0, a_k = 2 l_k, by Reinsch's recurrence:
 //   cos(theta) > 0 : lam = -4 sin^2(theta/2),  u <- u + d,  d <- a_k + lam u + d
 //   cos(theta) <= 0: lam =  4 cos^2(theta/2),  u <- d - u,  d <- a_k + lam u - d
@@ -105,7 +130,7 @@ __device__ __forceinline__ float mese_density(const float (&lam2)[MAXM], float l
     return (fast_atan(s) * 0.318309886f + 0.5f) * span + lo;
 }
 
-template <int MAXM>
+template <int MAXM, bool LINEAR>
 __global__ void __launch_bounds__(128) reconstruct_kernel(const ReconDev a)
 {
     __shared__ float4 s_tf[256];
@@ -135,7 +160,7 @@ __global__ void __launch_bounds__(128) reconstruct_kernel(const ReconDev a)
     if (n == 0)
     {
         // reconstruct_zero_ray (src/raymarch_reconstruct.h:127-131)
-        const float4 z = tf_sample(s_tf, 0.f, 0.f);
+        const float4 z = LINEAR ? tf_sample_linear(s_tf, 0.f) : tf_sample(s_tf, 0.f, 0.f);
         out = make_float4(z.x, z.y, z.z, 0.f);
     }
     else
@@ -148,7 +173,13 @@ __global__ void __launch_bounds__(128) reconstruct_kernel(const ReconDev a)
         for (int l = 0; l < MAXM; ++l)
             lam2[l] = (l < n && l > 0) ? 2.f * a.pmoments[idx + l] : 0.f;
         float lo = 0.f, hi = 1.f;
-        if (a.bounds)
+        if (a.bounds4)
+        {
+            const float4 b4 = a.bounds4[pix];
+            lo = b4.x;
+            hi = b4.y;
+        }
+        else if (a.bounds)
         {
             lo = a.bounds[2 * pix] / 65535.f;
             hi = a.bounds[2 * pix + 1] / 65535.f;
@@ -185,7 +216,7 @@ __global__ void __launch_bounds__(128) reconstruct_kernel(const ReconDev a)
                 t = __fadd_rn(t, a.step);
                 p = __fadd_rn(p, phase_step);
                 const float bs = mese_density<MAXM>(lam2, lam0, p, lo, span);
-                const float4 s = tf_sample(s_tf, fs, bs);
+                const float4 s = LINEAR ? tf_sample_linear(s_tf, fs) : tf_sample(s_tf, fs, bs);
                 L0 += (a.emission * s.x) * T;
                 L1 += (a.emission * s.y) * T;
                 L2 += (a.emission * s.z) * T;
@@ -216,11 +247,14 @@ __global__ void __launch_bounds__(128) reconstruct_kernel(const ReconDev a)
     }
 }
 
-template <int MAXM> void launch_m(const ReconDev &a, cudaStream_t stream)
+template <int MAXM> void launch_m(const ReconDev &a, bool linear, cudaStream_t stream)
 {
     dim3 block(16, 8);
     dim3 grid((a.width + 15) / 16, (a.height + 7) / 8);
-    reconstruct_kernel<MAXM><<<grid, block, 0, stream>>>(a);
+    if (linear)
+        reconstruct_kernel<MAXM, true><<<grid, block, 0, stream>>>(a);
+    else
+        reconstruct_kernel<MAXM, false><<<grid, block, 0, stream>>>(a);
 }
 
 } // namespace
@@ -246,19 +280,21 @@ cudaError_t launch_reconstruct(const ReconArgs &r, int *error_flag, cudaStream_t
     a.ert = r.ert;
     a.rgba = r.rgba;
     a.rgba8 = r.rgba8;
+    a.bounds4 = r.bounds4;
     a.error_flag = error_flag;
+    const bool lin = r.tf_linear != 0;
     if (r.m <= 8)
-        launch_m<8>(a, stream);
+        launch_m<8>(a, lin, stream);
     else if (r.m <= 16)
-        launch_m<16>(a, stream);
+        launch_m<16>(a, lin, stream);
     else if (r.m <= 32)
-        launch_m<32>(a, stream);
+        launch_m<32>(a, lin, stream);
     else if (r.m <= 64)
-        launch_m<64>(a, stream);
+        launch_m<64>(a, lin, stream);
     else if (r.m <= 128)
-        launch_m<128>(a, stream);
+        launch_m<128>(a, lin, stream);
     else
-        launch_m<256>(a, stream);
+        launch_m<256>(a, lin, stream);
     return cudaGetLastError();
 }
 

@@ -65,6 +65,24 @@ class RegularGrid:
         return (nx, ny, nz)
 
 
+class Particles:
+    """Particles (volume.h:125-157): SPH particles x, y, z with scalar values, one smoothing length, marched inside
+    the box [domain_min, domain_max]."""
+
+    def __init__(self, domain_min, domain_max, x, y, z, values, smoothing_length: float):
+        self.domain_min = tuple(float(v) for v in domain_min)
+        self.domain_max = tuple(float(v) for v in domain_max)
+        self.x, self.y, self.z, self.values = x, y, z, values
+        self.smoothing_length = float(smoothing_length)
+
+    def size(self) -> int:
+        return len(self.x)
+
+    def get_step_size(self) -> float:
+        """Particles::get_step_size: half the smoothing length."""
+        return float(np.float32(self.smoothing_length) * np.float32(0.5))
+
+
 class TransferFunction:
     """TransferFunction: ``table`` is one row (256 x RGBA float) of the 256 x 256 table, all rows being equal."""
 
@@ -212,6 +230,21 @@ class Context:
                                                    0))
         self._grid_key = None
 
+    def upload_particles(self, x, y, z, v, smoothing_length: float, domain_min, domain_max) -> None:
+        """Uploads SPH particles (four float32 arrays: numpy arrays or CUDA tensors) and builds their cell grid on
+        the device; they replace an uploaded grid."""
+        if hasattr(x, "data_ptr"):
+            n = x.numel()
+            ptrs = [_dptr(a) for a in (x, y, z, v)]
+            on_device = 1
+        else:
+            arrs = [np.ascontiguousarray(a, dtype=np.float32) for a in (x, y, z, v)]
+            n = arrs[0].size
+            ptrs = [_hptr(a) for a in arrs]
+            on_device = 0
+        self._check(self._L.mraygb_upload_particles(self._h, *ptrs, n, float(smoothing_length), _f3(domain_min),
+                                                    _f3(domain_max), on_device))
+
     def upload_tf(self, table) -> None:
         t = np.ascontiguousarray(table, dtype=np.float32)
         if t.shape != (256, 4):
@@ -338,11 +371,16 @@ def default_context(device: int = 0) -> Context:
     return ctx
 
 
-def generate(cam: Camera, volume: RegularGrid, mi: MomentImageHost, params: GenerationParameters,
+def generate(cam: Camera, volume, mi: MomentImageHost, params: GenerationParameters,
              context: Optional[Context] = None) -> None:
-    """generate(cam, volume, mi, params) (moment_raymarcher.h:48-49): fills ``mi`` in place."""
+    """generate(cam, volume, mi, params) for a RegularGrid or Particles (moment_raymarcher.h:48-49): fills ``mi``
+    in place."""
     ctx = context or default_context()
-    ctx.upload_grid(volume.data, volume.domain_min, volume.domain_max)
+    if isinstance(volume, Particles):
+        ctx.upload_particles(volume.x, volume.y, volume.z, volume.values, volume.smoothing_length,
+                             volume.domain_min, volume.domain_max)
+    else:
+        ctx.upload_grid(volume.data, volume.domain_min, volume.domain_max)
     out = ctx.generate(cam, params, mi.width, mi.height, mi.num_moments, out=mi)
     mi.domain_min, mi.domain_max = volume.domain_min, volume.domain_max
     assert out is mi

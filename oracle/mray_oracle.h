@@ -68,6 +68,14 @@ typedef struct oracle_options
     int row_begin;    /* first image row processed                        */
     int row_end;      /* one past the last row (<=0: image height)        */
     int row_step;     /* process every row_step-th row (<=0: 1)           */
+    /* The differentiation form (a variant of the method whose loss is piecewise smooth in its inputs):
+     *   tf_linear  : reconstruct samples the transfer function row linearly in the front density with the
+     *                texture convention of the reference's GPU path (u = 256 fs - 1/2, clamp to the edge);
+     *   bounds_out : generate writes the per-pixel density bounds (lo, hi) unquantized, 2*W*H of R;
+     *   bounds_in  : reconstruct reads (lo, hi) from here (2*W*H of R) instead of the u16 bounds. */
+    int tf_linear;
+    void *bounds_out;
+    const void *bounds_in;
 } oracle_options;
 
 #define ORACLE_DECL(R, SFX)                                                                                         \
@@ -89,7 +97,7 @@ typedef struct oracle_options
     void oracle_reconstruct_##SFX(const mraygb_camera *cam, const mraygb_reconstruction_params *rp,                \
                                   int width, int height, int num_moments, const float domain_min[3],                 \
                                   const float domain_max[3], const uint32_t *index, const R *pmoments,               \
-                                  const uint16_t *bounds, const float *tf_table, R *rgba,                             \
+                                  const uint16_t *bounds, const R *tf_table, R *rgba,                                 \
                                   const oracle_options *opt);                                                        \
     /* MESE primitives (mese/MESE_dynamic.h)                                                                  */    \
     void oracle_trig_to_exp_##SFX(int n, const R *trig, R *exp_out /* 2n */);                                     \
@@ -117,7 +125,8 @@ typedef struct oracle_options
                               R dir[3]);                                                                           \
     int oracle_intersect_aabb_##SFX(const R origin[3], const R dir[3], const float bmin[3], const float bmax[3],  \
                                     R *t_near, R *t_far);                                                          \
-    void oracle_tf_sample_##SFX(const float *tf_table, R fs, R bs, R out[4]);
+    void oracle_tf_sample_##SFX(const R *tf_table, R fs, R bs, R out[4]);                                           \
+    void oracle_tf_sample_linear_##SFX(const R *tf_table, R fs, R out[4]);
 
 ORACLE_DECL(float, f32)
 ORACLE_DECL(double, f64)

@@ -27,7 +27,8 @@ fp = np.ctypeslib.ndpointer
 
 class Options(C.Structure):
     _fields_ = [("exact_atan", C.c_int), ("nthreads", C.c_int), ("row_begin", C.c_int), ("row_end", C.c_int),
-                ("row_step", C.c_int)]
+                ("row_step", C.c_int), ("tf_linear", C.c_int), ("bounds_out", C.c_void_p),
+                ("bounds_in", C.c_void_p)]
 
 
 class Grid(C.Structure):
@@ -120,6 +121,7 @@ def _declare(L):
         getattr(L, f"oracle_grid_sample_{sfx}").argtypes = [P(Grid), C.c_void_p]
         getattr(L, f"oracle_grid_sample_{sfx}").restype = R
         getattr(L, f"oracle_tf_sample_{sfx}").argtypes = [C.c_void_p, R, R, C.c_void_p]
+        getattr(L, f"oracle_tf_sample_linear_{sfx}").argtypes = [C.c_void_p, R, C.c_void_p]
     L.oracle_particles_create.restype = C.c_void_p
     L.oracle_particles_create.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_float,
                                           C.c_float * 3, C.c_float * 3]
@@ -184,8 +186,10 @@ def _dt(precision):
 # pipeline stages
 # --------------------------------------------------------------------------------------------------------------
 
-def generate_moments(cam, gp, volume, dmin, dmax, width, height, m, precision="f32", nthreads=0, rows=None):
-    """generate_host's per-pixel loop: returns (moments[H,W,m], bounds[H,W,2] u16, counts[H,W] u32)."""
+def generate_moments(cam, gp, volume, dmin, dmax, width, height, m, precision="f32", nthreads=0, rows=None,
+                     float_bounds=False):
+    """generate_host's per-pixel loop: returns (moments[H,W,m], bounds[H,W,2] u16, counts[H,W] u32), and with
+    float_bounds the unquantized bounds[H,W,2] in the working precision as a fourth value."""
     L = lib()
     dt = _dt(precision)
     g, keep = _grid(volume, dmin, dmax)
@@ -193,9 +197,13 @@ def generate_moments(cam, gp, volume, dmin, dmax, width, height, m, precision="f
     bounds = np.zeros((height, width, 2), dtype=np.uint16)
     counts = np.zeros((height, width), dtype=np.uint32)
     o = options(nthreads, rows)
+    bf = np.zeros((height, width, 2), dtype=dt) if float_bounds else None
+    o.bounds_out = bf.ctypes.data if float_bounds else None
     getattr(L, f"oracle_generate_moments_{precision}")(C.byref(cam), C.byref(gp), C.byref(g), width, height, m,
                                                        _ptr(moments), _ptr(bounds), _ptr(counts), C.byref(o))
     del keep
+    if float_bounds:
+        return moments, bounds, counts, bf
     return moments, bounds, counts
 
 
@@ -297,16 +305,20 @@ def prepare_moments(width, height, m, index, data, prediction_code=False, coding
 
 
 def reconstruct(cam, rp, width, height, m, dmin, dmax, index, pmoments, bounds, tf_table, precision="f32",
-                nthreads=0, rows=None, exact_atan=False):
-    """reconstruct_host with float RGBA: returns rgba[H,W,4]."""
+                nthreads=0, rows=None, exact_atan=False, tf_linear=False, float_bounds=None):
+    """reconstruct_host with float RGBA: returns rgba[H,W,4].  tf_linear / float_bounds select the
+    differentiation form (linear transfer-function row in the front density; unquantized bounds[H,W,2])."""
     L = lib()
     dt = _dt(precision)
     pm = np.ascontiguousarray(pmoments, dtype=dt)
     idx = None if index is None else np.ascontiguousarray(index, dtype=np.uint32)
     b = None if bounds is None else np.ascontiguousarray(bounds, dtype=np.uint16)
-    t = np.ascontiguousarray(tf_table, dtype=np.float32)
+    t = np.ascontiguousarray(tf_table, dtype=dt)
     out = np.zeros((height, width, 4), dtype=dt)
     o = options(nthreads, rows, exact_atan)
+    o.tf_linear = int(tf_linear)
+    bf = None if float_bounds is None else np.ascontiguousarray(float_bounds, dtype=dt)
+    o.bounds_in = None if bf is None else bf.ctypes.data
     getattr(L, f"oracle_reconstruct_{precision}")(C.byref(cam), C.byref(rp), width, height, m,
                                                   (C.c_float * 3)(*dmin), (C.c_float * 3)(*dmax), _ptr(idx),
                                                   _ptr(pm), _ptr(b), _ptr(t), _ptr(out), C.byref(o))

@@ -13,6 +13,9 @@ on seeded inputs and stores inputs and outputs as small .npz files:
                       64^3 volume, 48x40 orthographic image, 16 moments
   pipeline_mix.npz    the same on a 40^3 mixing layer, 32x32 perspective image, 64 moments
   quantize.npz        quantize_prediction_coding of a ragged compact image under several bit tables
+  particles.npz       Particles::sample and generate() over SPH particles: a jittered lattice with one particle
+                      per grid cell (so the reference's unstable sort by cell cannot change the summation order)
+                      and a clustered set
 
 Run from the repository root:  python tests/golden/make_golden.py
 """
@@ -47,6 +50,10 @@ def cplx(values):
 
 
 def declare(ref):
+    u64, f, vp = C.c_uint64, C.c_float, C.c_void_p
+    ref.ref_particles_sample.argtypes = [vp, vp, vp, vp, u64, f, vp, vp, vp, u64, vp]
+    ref.ref_generate_particles.argtypes = [vp, vp, vp, vp, vp, vp, u64, f, vp, vp, C.c_int, C.c_int, C.c_int, vp, vp,
+                                           vp, vp]
     ref.ref_evaluate_mese.restype = C.c_float
     ref.ref_evaluate_mese.argtypes = [C.c_int, C.c_float, C.c_void_p]
     ref.ref_fixed_evaluate_lagrange.restype = C.c_float
@@ -288,6 +295,61 @@ def pipeline(ref, wl):
     return out
 
 
+def _particle_case(ref, prefix, x, y, z, v, h, dmin, dmax, cam, gen, Wd, H, m, rng):
+    out = {}
+    n = x.size
+    out[f"{prefix}_xyzv"] = np.stack([x, y, z, v])
+    out[f"{prefix}_h"] = np.float32(h)
+    out[f"{prefix}_domain"] = np.stack([dmin, dmax])
+    lo, hi = dmin - np.float32(0.05), dmax + np.float32(0.05)
+    pts = (lo + (hi - lo) * rng.random((400, 3))).astype(np.float32)
+    pts[:50] = np.stack([x[:50], y[:50], z[:50]], axis=1)  # exactly on particles (zero distance)
+    samples = np.zeros(pts.shape[0], np.float32)
+    ref.ref_particles_sample(P(x), P(y), P(z), P(v), n, C.c_float(h), P(dmin), P(dmax), P(pts), pts.shape[0],
+                             P(samples))
+    out[f"{prefix}_points"], out[f"{prefix}_samples"] = pts, samples
+    data = np.zeros(Wd * H * m, np.float32)
+    index = np.zeros(Wd * H + 1, np.uint32)
+    bounds = np.zeros(2 * Wd * H, np.uint16)
+    size = C.c_uint64()
+    ref.ref_generate_particles(C.byref(cam), C.byref(gen), P(x), P(y), P(z), P(v), n, C.c_float(h), P(dmin),
+                               P(dmax), Wd, H, m, P(data), P(index), P(bounds), C.byref(size))
+    out[f"{prefix}_camera"] = np.frombuffer(bytes(cam), np.uint8).copy()
+    out[f"{prefix}_gen"] = np.frombuffer(bytes(gen), np.uint8).copy()
+    out[f"{prefix}_shape"] = np.array([Wd, H, m], np.int32)
+    out[f"{prefix}_data"], out[f"{prefix}_index"], out[f"{prefix}_bounds"] = data[:size.value].copy(), index, bounds
+    return out
+
+
+def particles(ref):
+    out = {}
+    rng = np.random.default_rng(77)
+    # one particle per cell: positions (i + 0.25 + 0.5 u) h, so (p - min) / h stays inside [i, i + 0.5)
+    side, h = 10, np.float32(0.1)
+    ii = np.stack(np.meshgrid(np.arange(side), np.arange(side), np.arange(side), indexing="ij"), -1).reshape(-1, 3)
+    pos = ((ii + 0.25 + 0.5 * rng.random(ii.shape)) * float(h)).astype(np.float32)
+    pos[0] = np.float32(0.25) * h  # cell (0, 0, 0): the grid origin is exactly 0.25 h on every axis
+    perm = rng.permutation(pos.shape[0])
+    pos = pos[perm]
+    x, y, z = (np.ascontiguousarray(pos[:, k]) for k in range(3))
+    v = rng.lognormal(0.0, 0.5, size=x.size).astype(np.float32)
+    gmin = np.array([x.min(), y.min(), z.min()], np.float32)
+    inv = np.float32(1.0 / float(h))
+    cells = ((pos - gmin).astype(np.float32) * inv).astype(np.int32)
+    assert len({tuple(c) for c in cells}) == x.size, "lattice cells collide"
+    wl = W.sph_workload(n=64, h=float(h), width=24, height=20, num_moments=8, seed=3)
+    dmin, dmax = f32(0, 0, 0), f32(1, 1, 1)
+    gen = wl.gen
+    gen.step_size = float(h) / 2
+    gen.data_min, gen.data_max = 0.3, 3.0
+    out.update(_particle_case(ref, "lattice", x, y, z, v, float(h), dmin, dmax, wl.camera, gen, 24, 20, 8, rng))
+    # clustered: 70 % uniform, 30 % in Gaussian clusters; ties inside a cell (summation order unpinned)
+    wl = W.sph_workload(n=3000, h=1.0 / 16, width=24, height=20, num_moments=8, seed=9)
+    out.update(_particle_case(ref, "cluster", wl.x, wl.y, wl.z, wl.v, wl.h, f32(*wl.domain_min), f32(*wl.domain_max),
+                              wl.camera, wl.gen, 24, 20, 8, rng))
+    return out
+
+
 def quantize(ref):
     out = {}
     rng = np.random.default_rng(42)
@@ -323,6 +385,7 @@ def main():
     mix = W.mixing_layer_workload(n=40, width=32, height=32, num_moments=64, modes=16, seed=5, name="golden_mix")
     np.savez_compressed(os.path.join(HERE, "pipeline_mix.npz"), **pipeline(ref, mix))
     np.savez_compressed(os.path.join(HERE, "quantize.npz"), **quantize(ref))
+    np.savez_compressed(os.path.join(HERE, "particles.npz"), **particles(ref))
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

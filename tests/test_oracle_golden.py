@@ -312,3 +312,48 @@ def test_fp64_oracle_agrees_with_fp32_on_smooth_case():
     assert np.array_equal(c32, c64)
     err = np.abs(m32 - m64).max(axis=-1) / np.maximum(np.abs(m64[..., 0]), 1e-3)
     assert err[hit].max() < 1e-4
+
+
+def _particle_fixture(g, prefix):
+    from mray_gb300.types import Camera, GenerationParameters
+
+    x, y, z, v = (np.ascontiguousarray(a) for a in g[f"{prefix}_xyzv"])
+    dmin, dmax = g[f"{prefix}_domain"]
+    parts = O.ParticleSet(x, y, z, v, float(g[f"{prefix}_h"]), tuple(dmin), tuple(dmax))
+    cam = Camera.from_buffer_copy(g[f"{prefix}_camera"].tobytes())
+    gen = GenerationParameters.from_buffer_copy(g[f"{prefix}_gen"].tobytes())
+    return parts, cam, gen
+
+
+def _particle_generate(parts, cam, gen, shape):
+    Wd, H, m = (int(s) for s in shape)
+    moments, bounds, counts = O.generate_moments_particles(cam, gen, parts, Wd, H, m, "f32")
+    index, data = O.compact(counts, moments)
+    return index, data, bounds.reshape(-1)
+
+
+def test_particles_lattice_bit_exact():
+    """One particle per grid cell: the reference's sort order is unique, so sample and moments are bit-exact."""
+    g = load("particles.npz")
+    parts, cam, gen = _particle_fixture(g, "lattice")
+    s = O.particles_sample(parts, g["lattice_points"], "f32")
+    assert np.array_equal(s, g["lattice_samples"])
+    index, data, bounds = _particle_generate(parts, cam, gen, g["lattice_shape"])
+    assert np.array_equal(index, g["lattice_index"])
+    assert np.array_equal(bounds, g["lattice_bounds"])
+    assert np.array_equal(data, g["lattice_data"])
+
+
+def test_particles_clustered_within_summation_order():
+    """Several particles per cell: the reference's std::sort leaves their order (and so the float summation
+    order) unspecified; the oracle uses the input order.  Samples agree to a few ulp, the u16 bounds and the
+    compaction exactly where the samples' bounds do."""
+    g = load("particles.npz")
+    parts, cam, gen = _particle_fixture(g, "cluster")
+    s = O.particles_sample(parts, g["cluster_points"], "f32")
+    ref = g["cluster_samples"]
+    assert np.max(np.abs(s - ref) / np.maximum(np.abs(ref), 1e-30)) < 2e-6
+    index, data, bounds = _particle_generate(parts, cam, gen, g["cluster_shape"])
+    assert np.array_equal(index, g["cluster_index"])
+    assert np.max(np.abs(bounds.astype(np.int64) - g["cluster_bounds"].astype(np.int64))) <= 1
+    assert np.allclose(data, g["cluster_data"], rtol=0, atol=2e-5)
