@@ -68,7 +68,8 @@ int mraygb_create(int device, mraygb_context **out);
 void mraygb_destroy(mraygb_context *ctx);
 /* The last error message of this context ("" when none). */
 const char *mraygb_last_error(const mraygb_context *ctx);
-/* Orders all later work of this context on `stream` (a cudaStream_t; NULL restores the context's own). */
+/* Orders all later work of this context on `stream` (a cudaStream_t; NULL restores the context's own; the legacy
+ * default stream is cudaStreamLegacy, since NULL does not select it). */
 int mraygb_set_stream(mraygb_context *ctx, void *stream);
 void *mraygb_get_stream(const mraygb_context *ctx);
 int mraygb_synchronize(mraygb_context *ctx);
@@ -202,6 +203,30 @@ int mraygb_stage_reconstruct(mraygb_context *ctx, const mraygb_camera *cam, cons
                              int width, int height, int num_moments, const float domain_min[3],
                              const float domain_max[3], const uint32_t *d_index, const float *d_pmoments,
                              const uint16_t *d_bounds, float *d_rgba, uint8_t *d_rgba8);
+
+/* ---- differentiation form -------------------------------------------------------------------------------
+ * No counterpart in the reference.  The moment-image method with three changes that make an image-space loss
+ * piecewise smooth in the volume and the transfer function: no compaction (every pixel keeps m moments), the
+ * re-march reads the unquantized per-pixel density bounds, and the transfer-function row is sampled linearly in
+ * the front density with the texture convention of the reference's GPU path (TransferFunctionDevice::sample,
+ * src/transfer_function_device.cuh:30-65).  All buffers are device pointers on the context's stream. */
+
+/* Forward over the volume uploaded last: generate (gp->compact_image = 0, prediction_coding = 0,
+ * transform_to_bounds = 1; m <= 64), Lagrange multipliers in the context's precision form, re-march with the
+ * transfer-function row d_tf (256 RGBA floats).  Writes d_moments (W*H*m), d_bounds4 (W*H*4: lo, hi and the
+ * samples' min, max), d_pmoments (W*H*m) and d_rgba (W*H*4), which the backward reads.  16-byte aligned float4
+ * buffers. */
+int mraygb_diff_forward(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_generation_params *gp,
+                        const mraygb_reconstruction_params *rp, int width, int height, int m, const float *d_tf,
+                        float *d_moments, float *d_bounds4, float *d_pmoments, float *d_rgba);
+
+/* Adjoint of mraygb_diff_forward for the loss gradient d_grad_rgba (W*H*4): adds d loss / d transfer-function row
+ * to d_grad_tf (256*4) and, when d_grad_volume is not NULL (regular grids only), d loss / d voxel density to
+ * d_grad_volume (nx*ny*nz).  The forward's buffers must be unchanged. */
+int mraygb_diff_backward(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_generation_params *gp,
+                         const mraygb_reconstruction_params *rp, int width, int height, int m, const float *d_tf,
+                         const float *d_moments, const float *d_bounds4, const float *d_pmoments, const float *d_rgba,
+                         const float *d_grad_rgba, float *d_grad_tf, float *d_grad_volume);
 
 #ifdef __cplusplus
 }

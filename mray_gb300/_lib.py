@@ -24,7 +24,8 @@ EXPORTS = [
     "mraygb_generate", "mraygb_reconstruct", "mraygb_stage_generate_moments", "mraygb_stage_compact",
     "mraygb_stage_prepare_moments", "mraygb_stage_reconstruct", "mraygb_quantize_prediction_coding",
     "mraygb_stage_prediction_encode", "mraygb_stage_quantize_prediction_coding",
-    "mraygb_stage_dequantize_prediction_coding", "mraygb_stage_compact_noalloc",
+    "mraygb_stage_dequantize_prediction_coding", "mraygb_stage_compact_noalloc", "mraygb_diff_forward",
+    "mraygb_diff_backward",
 ]
 
 _lock = threading.Lock()
@@ -71,6 +72,9 @@ def _declare(L):
     L.mraygb_stage_quantize_prediction_coding.argtypes = [vp, i, i, i, vp, vp, vp, vp, u64, P(u64)]
     L.mraygb_stage_dequantize_prediction_coding.argtypes = [vp, i, i, i, vp, vp, vp, u64, vp]
     L.mraygb_stage_compact_noalloc.argtypes = [vp, i, i, i, vp, vp, vp, vp, u64, P(u64)]
+    G, RP = P(GenerationParameters), P(ReconstructionParameters)
+    L.mraygb_diff_forward.argtypes = [vp, P(Camera), G, RP, i, i, i, vp, vp, vp, vp, vp]
+    L.mraygb_diff_backward.argtypes = [vp, P(Camera), G, RP, i, i, i, vp, vp, vp, vp, vp, vp, vp, vp]
     special = ("mraygb_destroy", "mraygb_last_error", "mraygb_get_stream", "mraygb_kernel_launches")
     for name in EXPORTS:
         if name not in special:

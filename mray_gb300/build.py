@@ -30,6 +30,7 @@ SOURCES = [
     ("scan.cu", []),
     ("compact_noalloc.cu", []),
     ("particles.cu", []),
+    ("adjoint.cu", []),
     ("mese.cu", ["--fmad=false"]),
     ("mese_f64.cu", []),
     ("coding.cu", ["--fmad=false"]),

@@ -84,6 +84,8 @@ struct mraygb_context
     DeviceBuffer error_flag;
     // prediction coding and quantization
     DeviceBuffer coding_partial, coding_params_f, table, bits, bit_offset, scan_scratch64, packed;
+    // adjoint work buffers of the differentiation form
+    DeviceBuffer adj_lambda, adj_bounds;
 };
 
 namespace
@@ -258,7 +260,8 @@ int run_prepare(mraygb_context *ctx, int width, int height, int m, const uint32_
 
 int run_reconstruct(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_reconstruction_params *rp, int width,
                     int height, int m, const float dmin[3], const float dmax[3], const uint32_t *d_index,
-                    const float *d_pm, const uint16_t *d_bounds, float *d_rgba, uint8_t *d_rgba8)
+                    const float *d_pm, const uint16_t *d_bounds, float *d_rgba, uint8_t *d_rgba8,
+                    const float4 *d_bounds4 = nullptr, const float4 *d_tf = nullptr, int diff_form = 0)
 {
     const DeviceCamera dc = to_device_camera(*cam);
     ReconArgs a;
@@ -274,7 +277,9 @@ int run_reconstruct(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_
     a.index = d_index;
     a.pmoments = d_pm;
     a.bounds = d_bounds;
-    a.tf = ctx->tf.as<float4>();
+    a.tf = d_tf ? d_tf : ctx->tf.as<float4>();
+    a.bounds4 = d_bounds4;
+    a.diff_form = diff_form;
     a.step = rp->step_size;
     a.emission = rp->medium_emission;
     a.ert = rp->early_ray_termination;
@@ -451,7 +456,8 @@ void mraygb_destroy(mraygb_context *ctx)
                             &ctx->index,   &ctx->compact,  &ctx->bounds,        &ctx->coding_params,
                             &ctx->pmoments, &ctx->rgba,    &ctx->rgba8,         &ctx->scan_scratch,
                             &ctx->error_flag, &ctx->coding_partial, &ctx->coding_params_f, &ctx->table,
-                            &ctx->bits,    &ctx->bit_offset, &ctx->scan_scratch64, &ctx->packed};
+                            &ctx->bits,    &ctx->bit_offset, &ctx->scan_scratch64, &ctx->packed,
+                            &ctx->adj_lambda, &ctx->adj_bounds};
     for (DeviceBuffer *b : bufs)
         b->release();
     if (ctx->own_stream)
@@ -953,3 +959,118 @@ int mraygb_reconstruct(mraygb_context *ctx, const mraygb_camera *cam, const mray
 }
 
 } // extern "C"
+
+// ---- differentiation form ------------------------------------------------------------------------------------
+
+namespace
+{
+
+int validate_diff(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_generation_params *gp,
+                  const mraygb_reconstruction_params *rp, int width, int height, int m)
+{
+    int rc = check_image(ctx, width, height, m);
+    if (rc)
+        return rc;
+    if ((rc = validate_gen(ctx, gp)))
+        return rc;
+    if (!cam || !rp)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "camera or reconstruction parameters are NULL");
+    if (gp->compact_image || gp->prediction_coding || !gp->transform_to_bounds)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT,
+                    "the differentiation form needs compact_image = 0, prediction_coding = 0, transform_to_bounds = 1");
+    if (m > 64)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "the differentiation form supports up to 64 moments (got %d)", m);
+    if (!(rp->step_size > 0.f))
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "reconstruction step_size must be > 0");
+    if (ctx->volume == mraygb_context::NONE)
+        return fail(ctx, MRAYGB_NO_VOLUME, "no volume uploaded");
+    return MRAYGB_OK;
+}
+
+} // namespace
+
+int mraygb_diff_forward(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_generation_params *gp,
+                        const mraygb_reconstruction_params *rp, int width, int height, int m, const float *d_tf,
+                        float *d_moments, float *d_bounds4, float *d_pmoments, float *d_rgba)
+{
+    CHECK_CTX();
+    int rc = validate_diff(ctx, cam, gp, rp, width, height, m);
+    if (rc)
+        return rc;
+    if (!d_tf || !d_moments || !d_bounds4 || !d_pmoments || !d_rgba)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "NULL device buffer");
+    if ((reinterpret_cast<uintptr_t>(d_bounds4) | reinterpret_cast<uintptr_t>(d_rgba) |
+         reinterpret_cast<uintptr_t>(d_tf)) & 15u)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "d_tf, d_bounds4 and d_rgba must be 16-byte aligned");
+    const size_t P = (size_t)width * (size_t)height;
+    CK(ctx->bounds.reserve(2 * P * sizeof(uint16_t)), "bounds buffer allocation");
+    rc = run_generate_moments(ctx, cam, gp, width, height, m, d_moments, ctx->bounds.as<uint16_t>(), nullptr,
+                              reinterpret_cast<float4 *>(d_bounds4));
+    if (rc)
+        return rc;
+    rc = run_prepare(ctx, width, height, m, nullptr, d_moments, 0, MRAYGB_CODING_WARP_NONE, nullptr, rp->bias,
+                     d_pmoments);
+    if (rc)
+        return rc;
+    return run_reconstruct(ctx, cam, rp, width, height, m, ctx->dmin, ctx->dmax, nullptr, d_pmoments, nullptr, d_rgba,
+                           nullptr, reinterpret_cast<const float4 *>(d_bounds4),
+                           reinterpret_cast<const float4 *>(d_tf), 1);
+}
+
+int mraygb_diff_backward(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_generation_params *gp,
+                         const mraygb_reconstruction_params *rp, int width, int height, int m, const float *d_tf,
+                         const float *d_moments, const float *d_bounds4, const float *d_pmoments, const float *d_rgba,
+                         const float *d_grad_rgba, float *d_grad_tf, float *d_grad_volume)
+{
+    CHECK_CTX();
+    int rc = validate_diff(ctx, cam, gp, rp, width, height, m);
+    if (rc)
+        return rc;
+    if (!d_tf || !d_moments || !d_bounds4 || !d_pmoments || !d_rgba || !d_grad_rgba || !d_grad_tf)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "NULL device buffer");
+    if ((reinterpret_cast<uintptr_t>(d_bounds4) | reinterpret_cast<uintptr_t>(d_rgba) |
+         reinterpret_cast<uintptr_t>(d_tf) | reinterpret_cast<uintptr_t>(d_grad_rgba) |
+         reinterpret_cast<uintptr_t>(d_grad_tf)) & 15u)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "float4 buffers must be 16-byte aligned");
+    if (d_grad_volume && ctx->volume != mraygb_context::GRID)
+        return fail(ctx, MRAYGB_NOT_SUPPORTED, "density gradients need a regular grid (particles: transfer function "
+                                               "gradient only)");
+    const size_t P = (size_t)width * (size_t)height;
+    CK(ctx->adj_lambda.reserve(P * (size_t)m * sizeof(float)), "adjoint buffer allocation");
+    CK(ctx->adj_bounds.reserve(P * sizeof(float2)), "adjoint buffer allocation");
+    const DeviceCamera dc = to_device_camera(*cam);
+    ReconAdjArgs a;
+    a.cam = &dc;
+    a.width = width;
+    a.height = height;
+    a.m = m;
+    for (int i = 0; i < 3; ++i)
+    {
+        a.dmin[i] = ctx->dmin[i];
+        a.dmax[i] = ctx->dmax[i];
+    }
+    a.pmoments = d_pmoments;
+    a.bounds4 = reinterpret_cast<const float4 *>(d_bounds4);
+    a.tf = reinterpret_cast<const float4 *>(d_tf);
+    a.step = rp->step_size;
+    a.emission = rp->medium_emission;
+    a.ert = rp->early_ray_termination;
+    a.rgba = reinterpret_cast<const float4 *>(d_rgba);
+    a.grad_rgba = reinterpret_cast<const float4 *>(d_grad_rgba);
+    a.grad_lambda = ctx->adj_lambda.as<float>();
+    a.grad_bounds = ctx->adj_bounds.as<float2>();
+    a.grad_tf = reinterpret_cast<float4 *>(d_grad_tf);
+    CK(launch_reconstruct_adjoint(a, ctx->error_flag.as<int>(), ctx->stream), "re-march adjoint launch");
+    ctx->launches += 1;
+    if (!d_grad_volume)
+        return MRAYGB_OK;
+    CK(launch_prepare_adjoint((int)P, m, d_moments, rp->bias, ctx->adj_lambda.as<float>(), ctx->adj_lambda.as<float>(),
+                              ctx->stream),
+       "preparation adjoint launch");
+    CK(launch_generate_adjoint(grid_view(ctx), d_grad_volume, dc, *gp, width, height, m, d_moments,
+                               reinterpret_cast<const float4 *>(d_bounds4), ctx->adj_lambda.as<float>(),
+                               ctx->adj_bounds.as<float2>(), ctx->error_flag.as<int>(), ctx->stream),
+       "generation adjoint launch");
+    ctx->launches += 2;
+    return MRAYGB_OK;
+}

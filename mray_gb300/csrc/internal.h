@@ -101,11 +101,36 @@ struct ReconArgs
     float step, emission, ert;
     float *rgba;
     uint8_t *rgba8;
-    // the differentiation form: per-pixel (lo, hi, ., .) float bounds instead of the u16 ones, and the transfer
-    // function sampled linearly in the front density (texture convention)
+    // per-pixel (lo, hi, ., .) float bounds instead of the u16 ones
     const float4 *bounds4 = nullptr;
-    int tf_linear = 0;
+    // the differentiation form's density and transfer function (exact atan, cubic B-spline row)
+    int diff_form = 0;
 };
 cudaError_t launch_reconstruct(const ReconArgs &a, int *error_flag, cudaStream_t stream);
+
+// adjoint.cu: the differentiation form's adjoints (non-compact images, float bounds, linear transfer function)
+struct ReconAdjArgs
+{
+    const DeviceCamera *cam;
+    int width, height, m;
+    float dmin[3], dmax[3];
+    const float *pmoments;
+    const float4 *bounds4;
+    const float4 *tf;
+    float step, emission, ert;
+    const float4 *rgba, *grad_rgba;
+    float *grad_lambda;
+    float2 *grad_bounds;
+    float4 *grad_tf;
+};
+cudaError_t launch_reconstruct_adjoint(const ReconAdjArgs &a, int *error_flag, cudaStream_t stream);
+// d loss / d moments from d loss / d Lagrange multipliers (grad_moments may alias grad_lambda)
+cudaError_t launch_prepare_adjoint(int num_pixels, int m, const float *moments, float bias, const float *grad_lambda,
+                                   float *grad_moments, cudaStream_t stream);
+// d loss / d voxel density, accumulated into grad_volume
+cudaError_t launch_generate_adjoint(const GridView &grid, float *grad_volume, const DeviceCamera &cam,
+                                    const mraygb_generation_params &gp, int width, int height, int m,
+                                    const float *moments, const float4 *bounds4, const float *grad_moments,
+                                    const float2 *grad_bounds, int *error_flag, cudaStream_t stream);
 
 } // namespace mraygb

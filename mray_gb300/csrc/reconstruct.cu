@@ -17,6 +17,7 @@
 
 #include "device_common.cuh"
 #include "internal.h"
+#include "reconstruct_common.cuh"
 
 namespace mraygb
 {
@@ -40,97 +41,8 @@ struct ReconDev
     int *error_flag;
 };
 
-// fast_atan (src/mese/complex_algebra.h:133-152)
-__device__ __forceinline__ float fast_atan(float tan)
-{
-    const bool negative = tan < 0.0f;
-    const float abs_tan = negative ? -tan : tan;
-    const bool greater_one = abs_tan > 1.0f;
-    float x = greater_one ? abs_tan : 1.0f;
-    x = 1.0f / x;
-    float y = greater_one ? 1.0f : abs_tan;
-    x = x * y;
-    y = x * x;
-    float z = y * 0.020835f - 0.085133f;
-    z = y * z + 0.180141f;
-    z = y * z - 0.330299f;
-    y = y * z + 0.999866f;
-    z = y * x;
-    z = z * -2.0f + 1.570796f;
-    z = greater_one ? z : 0.0f;
-    x = x * y + z;
-    return negative ? -x : x;
-}
-
-__device__ __forceinline__ float4 tf_sample(const float4 *T, float fs, float bs)
-{
-    const float ipx = fs * 256.f, ipy = bs * 256.f;
-    const float flx = floorf(ipx);
-    const float ax = ipx - flx, ay = ipy - floorf(ipy);
-    const int xl = (int)flx;
-    const int x0 = min(max(xl, 0), 255);
-    const int x1 = min(max(xl + 1, 0), 255);
-    const float4 a = T[x0], b = T[x1];
-    const float wll = (1.f - ax) * (1.f - ay), wlr = ax * (1.f - ay), wrl = (1.f - ax) * ay, wrr = ax * ay;
-    float4 r;
-    r.x = wll * a.x + wlr * a.x + wrl * b.x + wrr * b.x;
-    r.y = wll * a.y + wlr * a.y + wrl * b.y + wrr * b.y;
-    r.z = wll * a.z + wlr * a.z + wrl * b.z + wrr * b.z;
-    r.w = wll * a.w + wlr * a.w + wrl * b.w + wrr * b.w;
-    return r;
-}
-
-// The differentiation form's transfer function: the row sampled linearly in the front density with the texture
-// convention of TransferFunctionDevice::sample (src/transfer_function_device.cuh:30-65: linear filter, normalised
-// coordinates, clamp; the rows being equal, the back density drops out).  Weight of entry x1 in *w, entries in
-// *x0 / *x1 (equal where clamped).
-__device__ __forceinline__ float4 tf_sample_linear(const float4 *T, float fs, int *x0o = nullptr, int *x1o = nullptr,
-                                                   float *wo = nullptr)
-{
-    const float u = fs * 256.f - 0.5f;
-    const float fl = floorf(u);
-    const float w = u - fl;
-    const int xl = (int)fl;
-    const int x0 = min(max(xl, 0), 255);
-    const int x1 = min(max(xl + 1, 0), 255);
-    const float4 a = T[x0], b = T[x1];
-    if (x0o)
-    {
-        *x0o = x0;
-        *x1o = x1;
-        *wo = w;
-    }
-    return make_float4((1.f - w) * a.x + w * b.x, (1.f - w) * a.y + w * b.y, (1.f - w) * a.z + w * b.z,
-                       (1.f - w) * a.w + w * b.w);
-}
-
-// S(theta) = sum_{k=0}^{n-1} a_k cos(k theta), a_0 = l_0, a_k = 2 l_k, by Reinsch's recurrence:
-//   cos(theta) > 0 : lam = -4 sin^2(theta/2),  u <- u + d,  d <- a_k + lam u + d
-//   cos(theta) <= 0: lam =  4 cos^2(theta/2),  u <- d - u,  d <- a_k + lam u - d
-//   S = d - (lam / 2) u
-template <int MAXM>
-__device__ __forceinline__ float mese_density(const float (&lam2)[MAXM], float lam0, float p, float lo, float span)
-{
-    const float pc = rclamp(p, -kPiF, 0.0f);
-    float sh, ch;
-    sincosf(0.5f * pc, &sh, &ch);
-    const bool pos = fabsf(pc) < 1.5707963267948966f; // cos(pc) > 0
-    const float sg = pos ? 1.f : -1.f;
-    const float lam = pos ? -4.f * sh * sh : 4.f * ch * ch;
-    float u = 0.f, d = 0.f;
-#pragma unroll
-    for (int l = MAXM - 1; l >= 1; --l)
-    {
-        u = fmaf(sg, u, d);
-        d = fmaf(lam, u, fmaf(sg, d, lam2[l]));
-    }
-    u = fmaf(sg, u, d);
-    d = fmaf(lam, u, fmaf(sg, d, lam0));
-    const float s = fmaf(-0.5f * lam, u, d);
-    return (fast_atan(s) * 0.318309886f + 0.5f) * span + lo;
-}
-
-template <int MAXM, bool LINEAR>
+// DIFF: the differentiation form (float bounds read by the caller's choice, exact atan, B-spline transfer function)
+template <int MAXM, bool DIFF>
 __global__ void __launch_bounds__(128) reconstruct_kernel(const ReconDev a)
 {
     __shared__ float4 s_tf[256];
@@ -160,7 +72,7 @@ __global__ void __launch_bounds__(128) reconstruct_kernel(const ReconDev a)
     if (n == 0)
     {
         // reconstruct_zero_ray (src/raymarch_reconstruct.h:127-131)
-        const float4 z = LINEAR ? tf_sample_linear(s_tf, 0.f) : tf_sample(s_tf, 0.f, 0.f);
+        const float4 z = DIFF ? tf_sample_bspline(s_tf, bspline_tap(0.f)) : tf_sample(s_tf, 0.f, 0.f);
         out = make_float4(z.x, z.y, z.z, 0.f);
     }
     else
@@ -204,7 +116,8 @@ __global__ void __launch_bounds__(128) reconstruct_kernel(const ReconDev a)
             const float est = range / a.step;
             const int cap = (est < 1.6e9f ? (int)(1.25f * est) : 2000000000) + 64;
             float L0 = 0.f, L1 = 0.f, L2 = 0.f, alpha = 0.f, T = 1.f, tau = 0.f;
-            float fs = mese_density<MAXM>(lam2, lam0, p, lo, span);
+            float fs = DIFF ? mese_density_exact<MAXM>(lam2, lam0, p, lo, span)
+                            : mese_density<MAXM>(lam2, lam0, p, lo, span);
             int it = 0;
             while (t <= t_far)
             {
@@ -215,8 +128,9 @@ __global__ void __launch_bounds__(128) reconstruct_kernel(const ReconDev a)
                 }
                 t = __fadd_rn(t, a.step);
                 p = __fadd_rn(p, phase_step);
-                const float bs = mese_density<MAXM>(lam2, lam0, p, lo, span);
-                const float4 s = LINEAR ? tf_sample_linear(s_tf, fs) : tf_sample(s_tf, fs, bs);
+                const float bs = DIFF ? mese_density_exact<MAXM>(lam2, lam0, p, lo, span)
+                                      : mese_density<MAXM>(lam2, lam0, p, lo, span);
+                const float4 s = DIFF ? tf_sample_bspline(s_tf, bspline_tap(fs)) : tf_sample(s_tf, fs, bs);
                 L0 += (a.emission * s.x) * T;
                 L1 += (a.emission * s.y) * T;
                 L2 += (a.emission * s.z) * T;
@@ -247,11 +161,11 @@ __global__ void __launch_bounds__(128) reconstruct_kernel(const ReconDev a)
     }
 }
 
-template <int MAXM> void launch_m(const ReconDev &a, bool linear, cudaStream_t stream)
+template <int MAXM> void launch_m(const ReconDev &a, bool diff, cudaStream_t stream)
 {
     dim3 block(16, 8);
     dim3 grid((a.width + 15) / 16, (a.height + 7) / 8);
-    if (linear)
+    if (diff)
         reconstruct_kernel<MAXM, true><<<grid, block, 0, stream>>>(a);
     else
         reconstruct_kernel<MAXM, false><<<grid, block, 0, stream>>>(a);
@@ -282,7 +196,7 @@ cudaError_t launch_reconstruct(const ReconArgs &r, int *error_flag, cudaStream_t
     a.rgba8 = r.rgba8;
     a.bounds4 = r.bounds4;
     a.error_flag = error_flag;
-    const bool lin = r.tf_linear != 0;
+    const bool lin = r.diff_form != 0;
     if (r.m <= 8)
         launch_m<8>(a, lin, stream);
     else if (r.m <= 16)

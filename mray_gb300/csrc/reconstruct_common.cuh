@@ -1,0 +1,173 @@
+// Device functions shared by the MESE re-march (reconstruct.cu) and its adjoint (adjoint.cu): fast_atan, the
+// transfer-function samples and the MESE density by Reinsch's modified Clenshaw recurrence.
+#pragma once
+
+#include "device_common.cuh"
+
+namespace mraygb
+{
+
+// fast_atan (src/mese/complex_algebra.h:133-152)
+__device__ __forceinline__ float fast_atan(float tan)
+{
+    const bool negative = tan < 0.0f;
+    const float abs_tan = negative ? -tan : tan;
+    const bool greater_one = abs_tan > 1.0f;
+    float x = greater_one ? abs_tan : 1.0f;
+    x = 1.0f / x;
+    float y = greater_one ? 1.0f : abs_tan;
+    x = x * y;
+    y = x * x;
+    float z = y * 0.020835f - 0.085133f;
+    z = y * z + 0.180141f;
+    z = y * z - 0.330299f;
+    y = y * z + 0.999866f;
+    z = y * x;
+    z = z * -2.0f + 1.570796f;
+    z = greater_one ? z : 0.0f;
+    x = x * y + z;
+    return negative ? -x : x;
+}
+
+__device__ __forceinline__ float4 tf_sample(const float4 *T, float fs, float bs)
+{
+    const float ipx = fs * 256.f, ipy = bs * 256.f;
+    const float flx = floorf(ipx);
+    const float ax = ipx - flx, ay = ipy - floorf(ipy);
+    const int xl = (int)flx;
+    const int x0 = min(max(xl, 0), 255);
+    const int x1 = min(max(xl + 1, 0), 255);
+    const float4 a = T[x0], b = T[x1];
+    const float wll = (1.f - ax) * (1.f - ay), wlr = ax * (1.f - ay), wrl = (1.f - ax) * ay, wrr = ax * ay;
+    float4 r;
+    r.x = wll * a.x + wlr * a.x + wrl * b.x + wrr * b.x;
+    r.y = wll * a.y + wlr * a.y + wrl * b.y + wrr * b.y;
+    r.z = wll * a.z + wlr * a.z + wrl * b.z + wrr * b.z;
+    r.w = wll * a.w + wlr * a.w + wrl * b.w + wrr * b.w;
+    return r;
+}
+
+// The differentiation form's transfer function: the row as a uniform cubic B-spline in the front density (C2, so an
+// image-space loss stays smooth where a density crosses a table entry; the rows being equal, the back density
+// drops out).  Knots at the texel centres of the reference's GPU texture (TransferFunctionDevice::sample,
+// src/transfer_function_device.cuh:30-65: u = 256 fs - 1/2), entries clamped at the ends.  Base entry i - 1 and
+// the four weights in *base / w when asked for.
+struct BSplineTap
+{
+    int i; // entries i - 1 .. i + 2 (clamped)
+    float t;
+    float w[4];
+};
+
+__device__ __forceinline__ BSplineTap bspline_tap(float fs)
+{
+    BSplineTap k;
+    const float u = fs * 256.f - 0.5f;
+    const float fl = floorf(u);
+    k.t = u - fl;
+    k.i = (int)fl;
+    const float t = k.t, s = 1.f - t, t2 = t * t, t3 = t2 * t;
+    k.w[0] = s * s * s * (1.f / 6.f);
+    k.w[1] = (3.f * t3 - 6.f * t2 + 4.f) * (1.f / 6.f);
+    k.w[2] = (-3.f * t3 + 3.f * t2 + 3.f * t + 1.f) * (1.f / 6.f);
+    k.w[3] = t3 * (1.f / 6.f);
+    return k;
+}
+
+__device__ __forceinline__ int bspline_entry(const BSplineTap &k, int j) { return min(max(k.i - 1 + j, 0), 255); }
+
+__device__ __forceinline__ float4 tf_sample_bspline(const float4 *T, const BSplineTap &k)
+{
+    float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+    {
+        const float4 e = T[bspline_entry(k, j)];
+        r.x = fmaf(k.w[j], e.x, r.x);
+        r.y = fmaf(k.w[j], e.y, r.y);
+        r.z = fmaf(k.w[j], e.z, r.z);
+        r.w = fmaf(k.w[j], e.w, r.w);
+    }
+    return r;
+}
+
+// d tf_sample_bspline / d fs (256 d / d u)
+__device__ __forceinline__ float4 tf_bspline_derivative(const float4 *T, const BSplineTap &k)
+{
+    const float t = k.t, s = 1.f - t;
+    const float d[4] = {-0.5f * s * s, 0.5f * (3.f * t * t - 4.f * t), 0.5f * (-3.f * t * t + 2.f * t + 1.f),
+                        0.5f * t * t};
+    float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+    {
+        const float4 e = T[bspline_entry(k, j)];
+        r.x = fmaf(d[j], e.x, r.x);
+        r.y = fmaf(d[j], e.y, r.y);
+        r.z = fmaf(d[j], e.z, r.z);
+        r.w = fmaf(d[j], e.w, r.w);
+    }
+    return make_float4(256.f * r.x, 256.f * r.y, 256.f * r.z, 256.f * r.w);
+}
+
+// S(theta) = sum_{k=0}^{n-1} a_k cos(k theta), a_0 = l_0, a_k = 2 l_k, by Reinsch's recurrence:
+//   cos(theta) > 0 : lam = -4 sin^2(theta/2),  u <- u + d,  d <- a_k + lam u + d
+//   cos(theta) <= 0: lam =  4 cos^2(theta/2),  u <- d - u,  d <- a_k + lam u - d
+//   S = d - (lam / 2) u
+template <int MAXM> __device__ __forceinline__ float mese_series(const float (&lam2)[MAXM], float lam0, float pc)
+{
+    float sh, ch;
+    sincosf(0.5f * pc, &sh, &ch);
+    const bool pos = fabsf(pc) < 1.5707963267948966f; // cos(pc) > 0
+    const float sg = pos ? 1.f : -1.f;
+    const float lam = pos ? -4.f * sh * sh : 4.f * ch * ch;
+    float u = 0.f, d = 0.f;
+#pragma unroll
+    for (int l = MAXM - 1; l >= 1; --l)
+    {
+        u = fmaf(sg, u, d);
+        d = fmaf(lam, u, fmaf(sg, d, lam2[l]));
+    }
+    u = fmaf(sg, u, d);
+    d = fmaf(lam, u, fmaf(sg, d, lam0));
+    return fmaf(-0.5f * lam, u, d);
+}
+
+// the bounded density at phase p: lo + span (atan(S) / pi + 1/2) (MESEReconstruction::reconstruct,
+// src/reconstruction_techniques.h:72-96), p clamped to [-pi, 0]
+template <int MAXM>
+__device__ __forceinline__ float mese_density(const float (&lam2)[MAXM], float lam0, float p, float lo, float span)
+{
+    const float pc = rclamp(p, -kPiF, 0.0f);
+    const float s = mese_series<MAXM>(lam2, lam0, pc);
+    return (fast_atan(s) * 0.318309886f + 0.5f) * span + lo;
+}
+
+// the differentiation form's density: exact atan (fast_atan jumps by 2.4e-5 at |t| = 1)
+template <int MAXM>
+__device__ __forceinline__ float mese_density_exact(const float (&lam2)[MAXM], float lam0, float p, float lo,
+                                                    float span)
+{
+    const float pc = rclamp(p, -kPiF, 0.0f);
+    const float s = mese_series<MAXM>(lam2, lam0, pc);
+    return (atanf(s) * 0.318309886f + 0.5f) * span + lo;
+}
+
+// d fast_atan / dt: fast_atan is t P(t^2) for |t| <= 1 and pi/2 - P(1/t^2) / |t| (odd) beyond, with P the
+// polynomial above; the derivative is Q(y) = P(y) + 2 y P'(y) at y = t^2, or Q(1/t^2) / t^2.
+__device__ __forceinline__ float fast_atan_derivative(float t)
+{
+    const float a = fabsf(t);
+    const bool greater_one = a > 1.0f;
+    const float r = greater_one ? 1.0f / a : a;
+    const float y = r * r;
+    // P(y) = (((0.020835 y - 0.085133) y + 0.180141) y - 0.330299) y + 0.999866
+    // Q(y) = P + 2 y P' = ((9 * 0.020835 y - 7 * 0.085133) y + 5 * 0.180141) y - 3 * 0.330299) y + 0.999866
+    float q = fmaf(9.0f * 0.020835f, y, -7.0f * 0.085133f);
+    q = fmaf(q, y, 5.0f * 0.180141f);
+    q = fmaf(q, y, -3.0f * 0.330299f);
+    q = fmaf(q, y, 0.999866f);
+    return greater_one ? q * y : q;
+}
+
+} // namespace mraygb

@@ -204,9 +204,12 @@ class Context:
         self._precision = int(value)
 
     def set_stream(self, stream) -> None:
-        """Orders later work on ``stream`` (a cudaStream_t as int, a torch.cuda.Stream, or None)."""
+        """Orders later work on ``stream``: a torch.cuda.Stream (torch's default stream included), a cudaStream_t as
+        an int, or None for the context's own stream."""
         if stream is not None and hasattr(stream, "cuda_stream"):
-            stream = stream.cuda_stream
+            # torch's default stream has the handle 0, which the C ABI reads as "the context's own stream": pass
+            # cudaStreamLegacy (1) for it instead
+            stream = stream.cuda_stream or 1
         self._check(self._L.mraygb_set_stream(self._h, stream))
 
     def synchronize(self) -> None:
@@ -359,6 +362,19 @@ class Context:
         self._check(self._L.mraygb_stage_reconstruct(self._h, C.byref(cam), C.byref(rp), width, height,
                                                      num_moments, _f3(domain_min), _f3(domain_max), _dptr(index),
                                                      _dptr(pmoments), _dptr(bounds), _dptr(rgba), _dptr(rgba8)))
+
+    # ---- differentiation form (device buffers: CUDA tensors or addresses) ----
+    def diff_forward(self, cam, gp, rp, width, height, num_moments, tf, moments, bounds4, pmoments, rgba) -> None:
+        self._check(self._L.mraygb_diff_forward(self._h, C.byref(cam), C.byref(gp), C.byref(rp), width, height,
+                                                num_moments, _dptr(tf), _dptr(moments), _dptr(bounds4),
+                                                _dptr(pmoments), _dptr(rgba)))
+
+    def diff_backward(self, cam, gp, rp, width, height, num_moments, tf, moments, bounds4, pmoments, rgba, grad_rgba,
+                      grad_tf, grad_volume=None) -> None:
+        self._check(self._L.mraygb_diff_backward(self._h, C.byref(cam), C.byref(gp), C.byref(rp), width, height,
+                                                 num_moments, _dptr(tf), _dptr(moments), _dptr(bounds4),
+                                                 _dptr(pmoments), _dptr(rgba), _dptr(grad_rgba), _dptr(grad_tf),
+                                                 _dptr(grad_volume)))
 
 
 _default: dict = {}

@@ -174,6 +174,27 @@ def mixing_layer_workload(n: int = 512, width: int = 1024, height: int = 1024, n
                     height, num_moments, cam, gen, rec, transfer_function(seed + 1), tf_step=0.05 * (512.0 / n))
 
 
+def diff_workload(n: int = 256, width: int = 512, height: int = 512, num_moments: int = 31, seed: int = 11,
+                  noise: float = 0.05, name: str | None = None):
+    """The differentiation form on a Marschner-Lobb n^3 volume with an orthographic seeded view: no compaction,
+    early ray termination off (ert = 1: a march stops only where the transmittance is exactly 0), the preintegration
+    step scaled with the sample count (0.05 * 64 / n).  Returns (workload, target_tf1d): the target transfer
+    function carries seeded N(0, noise) perturbations on its 256 extinction (alpha) and 256 emission entries (one
+    value per entry scaling the entry's rgb), clipped at 0.  The density range is [-0.1, 1.1], so that neither
+    the density mapping nor the bounds transform clamps (both would put kinks into the loss)."""
+    wl = ml_workload(n=n, width=width, height=height, num_moments=num_moments, seed=seed,
+                     name=name or f"diff_ml{n}_{width}x{height}_m{num_moments}")
+    wl.gen.compact_image = 0
+    wl.gen.data_min, wl.gen.data_max = -0.1, 1.1
+    wl.rec.early_ray_termination = 1.0
+    wl.tf_step = 0.05 * 64.0 / n
+    rng = np.random.default_rng(seed + 101)
+    target = wl.tf1d.astype(np.float64).copy()
+    target[:, 3] += rng.normal(0.0, noise, size=256)
+    target[:, :3] *= (1.0 + rng.normal(0.0, noise, size=256))[:, None]
+    return wl, np.clip(target, 0.0, None).astype(np.float32)
+
+
 def sph_particles(n: int, seed: int = 31, clusters: int = 200, cluster_frac: float = 0.3):
     """Particles in the unit cube: (1 - cluster_frac) uniform and cluster_frac in seeded Gaussian clusters
     (sigma 0.01..0.05), clipped to the cube; values ~ LogNormal(0, 0.5).  Returns x, y, z, v (float32)."""

@@ -68,12 +68,13 @@ typedef struct oracle_options
     int row_begin;    /* first image row processed                        */
     int row_end;      /* one past the last row (<=0: image height)        */
     int row_step;     /* process every row_step-th row (<=0: 1)           */
-    /* The differentiation form (a variant of the method whose loss is piecewise smooth in its inputs):
-     *   tf_linear  : reconstruct samples the transfer function row linearly in the front density with the
-     *                texture convention of the reference's GPU path (u = 256 fs - 1/2, clamp to the edge);
+    /* The differentiation form (a variant of the method whose loss is smooth almost everywhere in its inputs;
+     * combine with exact_atan = 1):
+     *   tf_bspline : reconstruct samples the transfer function row as a uniform cubic B-spline in the front
+     *                density, knots at the texel centres of the reference's GPU texture (u = 256 fs - 1/2);
      *   bounds_out : generate writes the per-pixel density bounds (lo, hi) unquantized, 2*W*H of R;
      *   bounds_in  : reconstruct reads (lo, hi) from here (2*W*H of R) instead of the u16 bounds. */
-    int tf_linear;
+    int tf_bspline;
     void *bounds_out;
     const void *bounds_in;
 } oracle_options;
@@ -88,9 +89,9 @@ typedef struct oracle_options
     void oracle_generate_moments_##SFX(const mraygb_camera *cam, const mraygb_generation_params *gp,               \
                                        const oracle_grid *grid, int width, int height, int num_moments,              \
                                        R *moments, uint16_t *bounds, uint32_t *counts, const oracle_options *opt);   \
-    /* Lagrange multipliers per pixel (moment_image.cpp:154-183)                                              */    \
+    /* Lagrange multipliers per pixel (moment_image.cpp:154-183); data in the working precision              */    \
     void oracle_prepare_moments_##SFX(int width, int height, int num_moments, const uint32_t *index,               \
-                                      const float *data, int prediction_code, int coding_warp,                       \
+                                      const R *data, int prediction_code, int coding_warp,                           \
                                       const uint16_t *coding_params, float bias, R *pmoments,                        \
                                       const oracle_options *opt);                                                    \
     /* MESE re-march per pixel, float RGBA before the u8 store (moment_raymarcher.cpp:283-327)               */      \
@@ -126,7 +127,7 @@ typedef struct oracle_options
     int oracle_intersect_aabb_##SFX(const R origin[3], const R dir[3], const float bmin[3], const float bmax[3],  \
                                     R *t_near, R *t_far);                                                          \
     void oracle_tf_sample_##SFX(const R *tf_table, R fs, R bs, R out[4]);                                           \
-    void oracle_tf_sample_linear_##SFX(const R *tf_table, R fs, R out[4]);
+    void oracle_tf_sample_bspline_##SFX(const R *tf_table, R fs, R out[4]);
 
 ORACLE_DECL(float, f32)
 ORACLE_DECL(double, f64)

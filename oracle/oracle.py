@@ -27,7 +27,7 @@ fp = np.ctypeslib.ndpointer
 
 class Options(C.Structure):
     _fields_ = [("exact_atan", C.c_int), ("nthreads", C.c_int), ("row_begin", C.c_int), ("row_end", C.c_int),
-                ("row_step", C.c_int), ("tf_linear", C.c_int), ("bounds_out", C.c_void_p),
+                ("row_step", C.c_int), ("tf_bspline", C.c_int), ("bounds_out", C.c_void_p),
                 ("bounds_in", C.c_void_p)]
 
 
@@ -121,7 +121,7 @@ def _declare(L):
         getattr(L, f"oracle_grid_sample_{sfx}").argtypes = [P(Grid), C.c_void_p]
         getattr(L, f"oracle_grid_sample_{sfx}").restype = R
         getattr(L, f"oracle_tf_sample_{sfx}").argtypes = [C.c_void_p, R, R, C.c_void_p]
-        getattr(L, f"oracle_tf_sample_linear_{sfx}").argtypes = [C.c_void_p, R, C.c_void_p]
+        getattr(L, f"oracle_tf_sample_bspline_{sfx}").argtypes = [C.c_void_p, R, C.c_void_p]
     L.oracle_particles_create.restype = C.c_void_p
     L.oracle_particles_create.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_float,
                                           C.c_float * 3, C.c_float * 3]
@@ -294,7 +294,7 @@ def prepare_moments(width, height, m, index, data, prediction_code=False, coding
                     bias=1e-6, precision="f32", nthreads=0, rows=None):
     """MomentImageHost::prepare_moments for every pixel; returns the Lagrange multipliers in the data layout."""
     L = lib()
-    d = np.ascontiguousarray(data, dtype=np.float32)
+    d = np.ascontiguousarray(data, dtype=_dt(precision))
     out = np.zeros(max(d.size, 1), dtype=_dt(precision))
     cp = None if coding_params is None else np.ascontiguousarray(coding_params, dtype=np.uint16)
     idx = None if index is None else np.ascontiguousarray(index, dtype=np.uint32)
@@ -305,9 +305,10 @@ def prepare_moments(width, height, m, index, data, prediction_code=False, coding
 
 
 def reconstruct(cam, rp, width, height, m, dmin, dmax, index, pmoments, bounds, tf_table, precision="f32",
-                nthreads=0, rows=None, exact_atan=False, tf_linear=False, float_bounds=None):
-    """reconstruct_host with float RGBA: returns rgba[H,W,4].  tf_linear / float_bounds select the
-    differentiation form (linear transfer-function row in the front density; unquantized bounds[H,W,2])."""
+                nthreads=0, rows=None, exact_atan=False, tf_bspline=False, float_bounds=None):
+    """reconstruct_host with float RGBA: returns rgba[H,W,4].  tf_bspline / float_bounds select the
+    differentiation form (transfer-function row as a cubic B-spline in the front density; unquantized
+    bounds[H,W,2])."""
     L = lib()
     dt = _dt(precision)
     pm = np.ascontiguousarray(pmoments, dtype=dt)
@@ -316,7 +317,7 @@ def reconstruct(cam, rp, width, height, m, dmin, dmax, index, pmoments, bounds, 
     t = np.ascontiguousarray(tf_table, dtype=dt)
     out = np.zeros((height, width, 4), dtype=dt)
     o = options(nthreads, rows, exact_atan)
-    o.tf_linear = int(tf_linear)
+    o.tf_bspline = int(tf_bspline)
     bf = None if float_bounds is None else np.ascontiguousarray(float_bounds, dtype=dt)
     o.bounds_in = None if bf is None else bf.ctypes.data
     getattr(L, f"oracle_reconstruct_{precision}")(C.byref(cam), C.byref(rp), width, height, m,
@@ -372,3 +373,24 @@ def workload_reconstruct(wl, mi, precision="f32", nthreads=0, exact_atan=False):
                          mi["coding_warp"], mi["coding_params"], wl.rec.bias, precision, nthreads)
     return reconstruct(wl.camera, wl.rec, wl.width, wl.height, wl.num_moments, wl.domain_min, wl.domain_max,
                        mi["index"], pm, mi["bounds"], tf, precision, nthreads, exact_atan=exact_atan)
+
+
+def preintegrate_r(tf1d, step_size, precision="f64"):
+    """The preintegrated row (rgb a s, a s) in the working precision (float: the reference's own arithmetic)."""
+    if precision == "f32":
+        return preintegrate(tf1d, step_size)
+    t = np.asarray(tf1d, dtype=np.float64)
+    w = t[:, 3] * float(step_size)
+    return np.concatenate([t[:, :3] * w[:, None], w[:, None]], axis=1)
+
+
+def diff_forward(cam, gp, rp, volume, dmin, dmax, width, height, m, tf_table, precision="f64", nthreads=0,
+                 exact_atan=True):
+    """The differentiation form's forward on the CPU: generate without compaction, unquantized bounds,
+    Lagrange multipliers, re-march with exact atan and the transfer-function row as a cubic B-spline in the
+    front density.  Returns rgba[H,W,4] in the working precision."""
+    moments, _, _, bf = generate_moments(cam, gp, volume, dmin, dmax, width, height, m, precision, nthreads,
+                                         float_bounds=True)
+    pm = prepare_moments(width, height, m, None, moments.reshape(-1), False, 1, None, rp.bias, precision, nthreads)
+    return reconstruct(cam, rp, width, height, m, dmin, dmax, None, pm, None, tf_table, precision, nthreads,
+                       exact_atan=exact_atan, tf_bspline=True, float_bounds=bf)

@@ -17,6 +17,10 @@ def pytest_configure(config):
 def gpu_context():
     import mray_gb300 as M
 
+    import torch
+
     ctx = M.Context(0)
+    # torch's current (default) stream: the tests' tensor fills and copies are ordered with the library's kernels
+    ctx.set_stream(torch.cuda.current_stream())
     yield ctx
     ctx.close()

@@ -1,0 +1,234 @@
+"""The differentiation form on the GPU: its forward against the oracle, and the hand-written adjoint (re-march,
+Lagrange-multiplier preparation, generation) against finite differences.
+
+The differentiated method: no compaction, unquantized density bounds, exact arctangent, transfer-function row as
+a cubic B-spline in the front density.  Two checks of the gradients:
+  * the FP64 reference gradient: central differences (eps = 2^-10, exact in float storage) of the FP64 oracle of
+    the same method, under a fixed linear image loss (the gradient is then the Jacobian alone, not the forward's
+    residual), relative error <= 1e-3 per parameter on parameters whose gradient is not negligible;
+  * under the configuration's L2 loss (target rendered with a perturbed transfer function) on 32 seeded parameters
+    (16 transfer-function entries, 16 voxels): against central differences (eps about 1e-3) of the FP64 oracle,
+    and against central differences (eps = 1e-3) of the FP32 GPU forward itself on the strong parameters.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+def _workload(n=40, width=40, height=36, m=16, seed=11):
+    from mray_gb300 import workloads as W
+
+    return W.diff_workload(n=n, width=width, height=height, num_moments=m, seed=seed)
+
+
+class GpuRender:
+    """The GPU forward / backward of one workload on fixed device buffers."""
+
+    def __init__(self, ctx, wl):
+        self.ctx, self.wl = ctx, wl
+        W, H, m = wl.width, wl.height, wl.num_moments
+        self.moments = torch.empty(W * H * m, device="cuda")
+        self.bounds4 = torch.empty(W * H * 4, device="cuda")
+        self.pm = torch.empty(W * H * m, device="cuda")
+        self.rgba = torch.empty((H, W, 4), device="cuda")
+
+    def forward(self, volume, table):
+        wl = self.wl
+        self.vol = torch.from_numpy(np.ascontiguousarray(volume, dtype=np.float32)).cuda()
+        self.tab = torch.from_numpy(np.ascontiguousarray(table, dtype=np.float32)).cuda()
+        self.ctx.upload_grid(self.vol, wl.domain_min, wl.domain_max)
+        self.ctx.diff_forward(wl.camera, wl.gen, wl.rec, wl.width, wl.height, wl.num_moments, self.tab, self.moments,
+                              self.bounds4, self.pm, self.rgba)
+        self.ctx.synchronize()
+        return self.rgba.cpu().numpy().astype(np.float64)
+
+    def backward(self, grad_rgba, volume_grad=True):
+        wl = self.wl
+        g = torch.from_numpy(np.ascontiguousarray(grad_rgba, dtype=np.float32)).cuda()
+        gtf = torch.zeros((256, 4), device="cuda")
+        gvol = torch.zeros_like(self.vol) if volume_grad else None
+        self.ctx.diff_backward(wl.camera, wl.gen, wl.rec, wl.width, wl.height, wl.num_moments, self.tab, self.moments,
+                               self.bounds4, self.pm, self.rgba, g, gtf, gvol)
+        self.ctx.synchronize()
+        return gtf.cpu().numpy().astype(np.float64), (gvol.cpu().numpy().astype(np.float64) if volume_grad else None)
+
+
+def _oracle_rgba(wl, volume, table):
+    return O.diff_forward(wl.camera, wl.gen, wl.rec, volume, wl.domain_min, wl.domain_max, wl.width, wl.height,
+                          wl.num_moments, table, "f64")
+
+
+@pytest.mark.parametrize("m", [8, 16, 31])
+def test_diff_forward_matches_oracle(gpu_context, m):
+    wl, _ = _workload(m=m)
+    table = O.preintegrate(wl.tf1d, wl.tf_step)
+    rgba = GpuRender(gpu_context, wl).forward(wl.volume, table)
+    ref32 = O.diff_forward(wl.camera, wl.gen, wl.rec, wl.volume, wl.domain_min, wl.domain_max, wl.width, wl.height,
+                           m, table, "f32")
+    ref64 = _oracle_rgba(wl, wl.volume, table)
+    assert np.abs(rgba - ref32).max() <= 1e-3
+    assert np.abs(rgba - ref64).max() <= 1e-3
+    assert rgba[..., 3].max() > 0.1  # the view sees the volume
+
+
+def _fd64(wl, volume, table, weights, params, eps=2.0 ** -10):
+    """Central differences of the FP64 oracle under the linear loss sum(weights * rgba)."""
+    out = []
+    for kind, idx in params:
+        vals = []
+        for sgn in (1.0, -1.0):
+            v, t = volume, table
+            if kind == "vox":
+                v = volume.copy()
+                v[idx] += np.float32(sgn * eps)
+            else:
+                t = table.astype(np.float64).copy()
+                t[idx] += sgn * eps
+            vals.append(float((weights * _oracle_rgba(wl, v, t)).sum()))
+        out.append((vals[0] - vals[1]) / (2 * eps))
+    return np.array(out)
+
+
+def _pick(rng, grad_vol, grad_tf, n_tf, n_vox):
+    """Seeded parameters whose gradient is not negligible (above 1 % of the largest of its kind)."""
+    tf_ok = np.argwhere(np.abs(grad_tf) > 1e-2 * np.abs(grad_tf).max())
+    vox_ok = np.argwhere(np.abs(grad_vol) > 1e-2 * np.abs(grad_vol).max())
+    params = [("tf", tuple(tf_ok[i])) for i in rng.choice(len(tf_ok), n_tf, replace=False)]
+    params += [("vox", tuple(vox_ok[i])) for i in rng.choice(len(vox_ok), n_vox, replace=False)]
+    return params
+
+
+@pytest.mark.parametrize("m", [16, 31])
+def test_adjoint_against_fp64_reference_gradient(gpu_context, m):
+    wl, _ = _workload(m=m)
+    table = O.preintegrate(wl.tf1d, wl.tf_step)
+    rng = np.random.default_rng(5)
+    weights = rng.standard_normal((wl.height, wl.width, 4))
+    R = GpuRender(gpu_context, wl)
+    R.forward(wl.volume, table)
+    gtf, gvol = R.backward(weights)
+    params = _pick(rng, gvol, gtf, 8, 8)
+    ad = np.array([gtf[idx] if kind == "tf" else gvol[idx] for kind, idx in params])
+    fd = _fd64(wl, wl.volume, table, weights, params)
+    rel = np.abs(ad - fd) / np.abs(fd)
+    assert rel.max() <= 1e-3, f"max rel err {rel.max():.3e} at {params[int(rel.argmax())]}: ad {ad} fd {fd}"
+
+
+def _l2_setup(ctx):
+    wl, target_tf = _workload(n=48, width=48, height=40, m=31)
+    table = O.preintegrate(wl.tf1d, wl.tf_step).astype(np.float64)
+    R = GpuRender(ctx, wl)
+    target = R.forward(wl.volume, O.preintegrate(target_tf, wl.tf_step))
+    return wl, table, R, target
+
+
+def _perturbed(wl, table, kind, idx, delta):
+    v, t = wl.volume, table
+    if kind == "vox":
+        v = wl.volume.copy()
+        v[idx] += np.float32(delta)
+    else:
+        t = table.copy()
+        t[idx] += delta
+    return v, t
+
+
+def test_l2_adjoint_against_fp64_central_differences(gpu_context):
+    """The L2 loss of the configuration (target rendered with the perturbed transfer function): the GPU adjoint,
+    fed the FP64 forward's residual, against central differences (eps = 2^-10, about 1e-3) of the FP64 oracle on
+    32 seeded parameters (16 transfer-function entries, 16 voxels)."""
+    wl, table, R, target = _l2_setup(gpu_context)
+    rgba64 = _oracle_rgba(wl, wl.volume, table)
+    R.forward(wl.volume, table)
+    gtf, gvol = R.backward(2.0 * (rgba64 - target))
+    params = _pick(np.random.default_rng(17), gvol, gtf, 16, 16)
+    eps = 2.0 ** -10
+    fd = []
+    for kind, idx in params:
+        lp = ((_oracle_rgba(wl, *_perturbed(wl, table, kind, idx, eps)) - target) ** 2).sum()
+        lm = ((_oracle_rgba(wl, *_perturbed(wl, table, kind, idx, -eps)) - target) ** 2).sum()
+        fd.append((lp - lm) / (2 * eps))
+    fd = np.array(fd)
+    ad = np.array([gtf[idx] if kind == "tf" else gvol[idx] for kind, idx in params])
+    rel = np.abs(ad - fd) / np.abs(fd)
+    assert rel.max() <= 1e-3, f"max rel err {rel.max():.3e} at {params[int(rel.argmax())]}"
+
+
+def test_l2_adjoint_against_gpu_central_differences(gpu_context):
+    """Central differences (eps = 1e-3) of the FP32 GPU forward itself on the seeded parameters whose gradient is
+    at least a tenth of the largest of its kind; below that the FP32 rounding of the forward (about 1e-7 of each
+    colour, divided by 2 eps) is no longer small against the difference quotient."""
+    wl, table, R, target = _l2_setup(gpu_context)
+    rgba = R.forward(wl.volume, table)
+    gtf, gvol = R.backward(2.0 * (rgba - target))
+    rng = np.random.default_rng(23)
+    tf_ok = np.argwhere(np.abs(gtf) > 0.1 * np.abs(gtf).max())
+    vox_ok = np.argwhere(np.abs(gvol) > 0.1 * np.abs(gvol).max())
+    params = [("tf", tuple(tf_ok[i])) for i in rng.choice(len(tf_ok), min(16, len(tf_ok)), replace=False)]
+    params += [("vox", tuple(vox_ok[i])) for i in rng.choice(len(vox_ok), min(16, len(vox_ok)), replace=False)]
+    eps = 1e-3
+    fd = []
+    for kind, idx in params:
+        lp = ((R.forward(*_perturbed(wl, table, kind, idx, eps)) - target) ** 2).sum()
+        lm = ((R.forward(*_perturbed(wl, table, kind, idx, -eps)) - target) ** 2).sum()
+        fd.append((lp - lm) / (2 * eps))
+    fd = np.array(fd)
+    ad = np.array([gtf[idx] if kind == "tf" else gvol[idx] for kind, idx in params])
+    rel = np.abs(ad - fd) / np.abs(fd)
+    assert rel.max() <= 1e-3, f"max rel err {rel.max():.3e} at {params[int(rel.argmax())]}"
+
+
+def test_autograd_function_and_tf1d_chain(gpu_context):
+    """torch.autograd.Function: the same gradients as the direct calls, and through preintegrate_table to the 1D
+    extinction / emission entries."""
+    from mray_gb300.autograd import RenderSpec, preintegrate_table, render
+
+    wl, target_tf = _workload(m=16)
+    spec = RenderSpec(wl.camera, wl.gen, wl.rec, wl.width, wl.height, wl.num_moments, wl.domain_min, wl.domain_max,
+                      gpu_context)
+    vol = torch.from_numpy(wl.volume).cuda().requires_grad_(True)
+    tf1d = torch.from_numpy(wl.tf1d.astype(np.float32)).cuda().requires_grad_(True)
+    with torch.no_grad():
+        target = render(vol, preintegrate_table(torch.from_numpy(target_tf).cuda(), wl.tf_step), spec)
+    rgba = render(vol, preintegrate_table(tf1d, wl.tf_step), spec)
+    loss = ((rgba - target) ** 2).sum()
+    loss.backward()
+    R = GpuRender(gpu_context, wl)
+    table = O.preintegrate(wl.tf1d, wl.tf_step)
+    r = R.forward(wl.volume, table)
+    gtf, gvol = R.backward(2.0 * (r - target.cpu().numpy()))
+    assert np.allclose(vol.grad.cpu().numpy(), gvol, rtol=1e-4, atol=1e-6 * np.abs(gvol).max())
+    # chain to the 1D table: d table / d tf1d by hand
+    s = wl.tf_step
+    t1 = wl.tf1d.astype(np.float64)
+    expect = np.zeros_like(t1)
+    expect[:, :3] = gtf[:, :3] * (t1[:, 3:4] * s)
+    expect[:, 3] = (gtf[:, :3] * t1[:, :3]).sum(axis=1) * s + gtf[:, 3] * s
+    assert np.allclose(tf1d.grad.cpu().numpy(), expect, rtol=1e-3, atol=1e-5 * np.abs(expect).max())
+
+
+def test_diff_form_argument_errors(gpu_context):
+    import mray_gb300 as M
+
+    wl, _ = _workload(m=8)
+    R = GpuRender(gpu_context, wl)
+    R.forward(wl.volume, O.preintegrate(wl.tf1d, wl.tf_step))
+    wl.gen.compact_image = 1
+    with pytest.raises(M.MrayError, match="INVALID_ARGUMENT"):
+        R.forward(wl.volume, O.preintegrate(wl.tf1d, wl.tf_step))
+    wl.gen.compact_image = 0
+    # particles: transfer-function gradient only
+    from mray_gb300 import workloads as Wk
+
+    p = Wk.sph_workload(n=2000, h=1.0 / 16, width=wl.width, height=wl.height, num_moments=8)
+    gpu_context.upload_particles(p.x, p.y, p.z, p.v, p.h, p.domain_min, p.domain_max)
+    gtf = torch.zeros((256, 4), device="cuda")
+    gvol = torch.zeros(8, device="cuda")
+    g = torch.zeros_like(R.rgba)
+    with pytest.raises(M.MrayError, match="NOT_SUPPORTED"):
+        gpu_context.diff_backward(wl.camera, wl.gen, wl.rec, wl.width, wl.height, 8, R.tab, R.moments, R.bounds4,
+                                  R.pm, R.rgba, g, gtf, gvol)
