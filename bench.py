@@ -2,8 +2,9 @@
 
 Default workload (the precision form): a 512^3 float32 mixing-layer grid (64 seeded Fourier modes, 5 % seeded
 noise), a 1024 x 1024 perspective view, 0.5-voxel steps, 64 trigonometric moments, Kahan-compensated FP32 moment
-sums and FP64 MESE preparation.  A step is one full pass over the image with the volume resident in HBM:
-    generate_grid_kernel -> scan / compaction -> prepare_kernel (FP64) -> reconstruct_kernel
+sums and the MESE preparation's FP64 steps in float-float arithmetic.  A step is one full pass over the image
+with the volume resident in HBM:
+    generate_grid_kernel -> scan / compaction -> prepare_ff_kernel -> reconstruct_kernel
 and the metric is million rays (pixels) per second of that pass.
 
 The JSON line also carries:
@@ -51,6 +52,9 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU-baseline sample time")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the differentiation-form, SPH and FP64-error sections")
+    ap.add_argument("--sph-particles", type=int, default=16_000_000)
     return ap.parse_args()
 
 
@@ -220,8 +224,9 @@ def run_reference(args):
         return
     wl = workload(args)
     ncores = os.cpu_count() or 1
-    # each step: a bounded row sample (every 128th row at the default size), rows rotating between steps
-    step_rows = max(1, wl.height // 8)
+    # each step: a bounded row sample (every 16th row at the default size: 64 rows, enough for every host core),
+    # rows rotating between steps
+    step_rows = max(1, wl.height // 64)
     for i in range(args.warmup):
         cpu_reference_sample(wl, step_rows, i % step_rows)
     times, rays_total = [], 0
@@ -330,16 +335,19 @@ def run_ours(args):
         gen_ms = [e[0].elapsed_time(e[1]) for e in evs]
         return sum(step_ms), statistics.mean(gen_ms), launches, wall
 
-    # plain FP32 form first (reported beside the headline), then the precision form under the clock sampler
+    # the plain FP32 form and the FP64 precision form first (reported beside the headline), then the headline
+    # precision form (float-float MESE preparation) under the clock sampler
     plain_ms, _, _, _ = timed_loop(M.PRECISION_FP32)
+    fp64_ms, _, _, _ = timed_loop(M.PRECISION_COMPENSATED_FP64_MESE)
     sampler = ClockSampler(local)
     sampler.start()
-    total_ms, gen_ms, launches, wall = timed_loop(M.PRECISION_COMPENSATED_FP64_MESE)
+    total_ms, gen_ms, launches, wall = timed_loop(M.PRECISION_COMPENSATED_FF_MESE)
     clocks = sampler.stop()
 
-    t_max, plain_max = reduce_max([total_ms, plain_ms], dist, "cuda")
+    t_max, plain_max, fp64_max = reduce_max([total_ms, plain_ms, fp64_ms], dist, "cuda")
     value = world * P * args.steps / (t_max * 1e-3) / 1e6
     plain_value = world * P * args.steps / (plain_max * 1e-3) / 1e6
+    fp64_value = world * P * args.steps / (fp64_max * 1e-3) / 1e6
 
     # roofline of the dominant kernel (generate): compulsory bytes and method FLOPs per launch
     spr = samples_per_ray(wl)
@@ -378,18 +386,28 @@ def run_ours(args):
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(wl, args.cpu_seconds)
 
+    extras = {}
+    if rank == 0 and not args.no_extras:
+        extras["differentiation_form"] = run_diff(args, local)
+        extras["sph"] = run_sph(args, local)
+        extras["errors_vs_fp64"] = precision_errors(args, local)
+
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
                 "config": {"workload": wl.name, "volume": f"{args.size}^3 float32 mixing layer (64 modes, 5% noise)",
                            "image": f"{W}x{H} perspective", "num_moments": m, "step": "0.5 voxel",
-                           "precision": "Kahan-compensated FP32 moment sums, FP64 MESE preparation",
+                           "precision": "Kahan-compensated FP32 moment sums; MESE preparation with its FP64 steps "
+                                        "(exponential moments, Levinson) in float-float arithmetic, FP32 tail",
                            "l2": "256 MiB buffer written between timed steps (volume 512 MiB > L2)",
                            "parallelism": "replicas" if world > 1 else "single GPU"},
                 "plain_fp32": {"value": plain_value, "unit": UNIT, "ms_per_step": plain_max / args.steps},
+                "precision_form_fp64": {"value": fp64_value, "unit": UNIT, "ms_per_step": fp64_max / args.steps,
+                                        "note": "the same pass with the MESE preparation in native FP64"},
+                "precision_over_plain": value / plain_value,
                 "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
-                "wall_s_timed": wall}
+                "wall_s_timed": wall, **extras}
         print(json.dumps(line), flush=True)
     ctx.close()
     if dist:
@@ -441,6 +459,241 @@ def run_e2e(args, ctx, wl, dist):
             "d2h_bytes_per_step": int(d2h),
             "path": "mraygb_upload_grid + mraygb_generate + mraygb_upload_tf + mraygb_reconstruct on pinned host "
                     "buffers (the drop-in seam of generate_device / reconstruct_device)"}
+
+
+# ------------------------------------------------------------------------------------------------------------
+# further sections of the JSON line: the differentiation form, SPH particles, errors against the FP64 oracle
+# ------------------------------------------------------------------------------------------------------------
+
+def _events(n):
+    import torch
+
+    return [[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in range(n)]
+
+
+def run_diff(args, local):
+    """The differentiation form on its configuration (256^3 Marschner-Lobb, 512^2 orthographic, 31 moments, L2 loss
+    against a target rendered with the perturbed transfer function): forward, and forward + adjoint to the
+    transfer-function row and all voxel densities."""
+    import torch
+
+    import mray_gb300 as M
+    from mray_gb300 import workloads as W
+
+    wl, target_tf = W.diff_workload(n=256, width=512, height=512, num_moments=31)
+    Wd, H, m = wl.width, wl.height, wl.num_moments
+    P = Wd * H
+    ctx = M.Context(local)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    vol = torch.from_numpy(wl.volume).cuda()
+    ctx.upload_grid(vol, wl.domain_min, wl.domain_max)
+    tab = torch.from_numpy(M.preintegrate(wl.tf1d, wl.tf_step).table).cuda()
+    ttab = torch.from_numpy(M.preintegrate(target_tf, wl.tf_step).table).cuda()
+    mo = torch.empty(P * m, device="cuda")
+    b4 = torch.empty(P * 4, device="cuda")
+    pm = torch.empty(P * m, device="cuda")
+    rgba = torch.empty((H, Wd, 4), device="cuda")
+    target = torch.empty((H, Wd, 4), device="cuda")
+    gtab = torch.zeros((256, 4), device="cuda")
+    gvol = torch.zeros_like(vol)
+    torch.cuda.synchronize()
+    ctx.diff_forward(wl.camera, wl.gen, wl.rec, Wd, H, m, ttab, mo, b4, pm, target)
+
+    def fwd():
+        ctx.diff_forward(wl.camera, wl.gen, wl.rec, Wd, H, m, tab, mo, b4, pm, rgba)
+
+    def fwd_bwd():
+        fwd()
+        with torch.cuda.stream(stream):
+            g = 2.0 * (rgba - target)
+            gtab.zero_()
+            gvol.zero_()
+        ctx.diff_backward(wl.camera, wl.gen, wl.rec, Wd, H, m, tab, mo, b4, pm, rgba, g, gtab, gvol)
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        ctx.synchronize()
+        ev = _events(args.steps)
+        l0 = ctx.kernel_launches
+        for e in ev:
+            e[0].record(stream)
+            fn()
+            e[1].record(stream)
+        ctx.synchronize()
+        return statistics.mean(e[0].elapsed_time(e[1]) for e in ev), (ctx.kernel_launches - l0) // args.steps
+
+    f_ms, f_l = timed(fwd)
+    fb_ms, fb_l = timed(fwd_bwd)
+    loss = float(((rgba - target) ** 2).sum())
+    ctx.close()
+    return {"workload": f"{wl.name}_ortho (256^3 Marschner-Lobb, 512x512, m=31, no compaction, ert 1)",
+            "fwd": {"value": P / (f_ms * 1e-3) / 1e6, "unit": UNIT, "ms": f_ms, "gpu_launches_per_step": f_l},
+            "fwd_adjoint": {"value": P / (fb_ms * 1e-3) / 1e6, "unit": UNIT, "ms": fb_ms,
+                            "gpu_launches_per_step": fb_l,
+                            "gradients": "transfer-function row (256 x RGBA) and all 256^3 voxel densities"},
+            "fwd_adjoint_over_fwd": fb_ms / f_ms, "loss": loss,
+            "note": "forward = generate (no compaction) + FP32 Lagrange multipliers + re-march (exact atan, "
+                    "B-spline transfer function); adjoint = re-march adjoint + preparation adjoint + generation "
+                    "adjoint; the L2 residual and the gradient zeroing (torch) are inside the timed region"}
+
+
+def run_sph(args, local):
+    """SPH particles (16M: 70 % uniform, 30 % in 200 Gaussian clusters, LogNormal values, one smoothing length
+    h = 1/256 so that the grid has 256^3 cells), 1024^2 perspective view, 64 moments: the device grid build, the
+    forward pass in both arithmetic forms, and the differentiation form with its transfer-function adjoint."""
+    import torch
+
+    import mray_gb300 as M
+    from mray_gb300 import workloads as W
+
+    n = args.sph_particles
+    h = 1.0 / 256
+    x, y, z, v = W.sph_particles(n, seed=31)
+    wl = W.sph_workload(n=64, h=h, width=args.image, height=args.image, num_moments=args.moments, seed=31)
+    rng = np.random.default_rng(38)
+    smp = v[rng.integers(0, n, size=100000)]
+    wl.gen.data_min, wl.gen.data_max = float(np.percentile(smp, 1)), float(np.percentile(smp, 99))
+    dmin = (float(x.min()), float(y.min()), float(z.min()))
+    dmax = (float(x.max()), float(y.max()), float(z.max()))
+    Wd, H, m = wl.width, wl.height, wl.num_moments
+    P = Wd * H
+    ctx = M.Context(local)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    xs = [torch.from_numpy(a).cuda() for a in (x, y, z, v)]
+    torch.cuda.synchronize()
+    up = []
+    for _ in range(3):
+        e = _events(1)[0]
+        e[0].record(stream)
+        ctx.upload_particles(*xs, h, dmin, dmax)
+        e[1].record(stream)
+        ctx.synchronize()
+        up.append(e[0].elapsed_time(e[1]))
+    tf = M.preintegrate(wl.tf1d, wl.tf_step)
+    ctx.upload_tf(tf.table)
+    d_mo = torch.empty(P * m, device="cuda")
+    d_b = torch.empty(2 * P, dtype=torch.int16, device="cuda")
+    d_c = torch.empty(P, dtype=torch.int32, device="cuda")
+    d_idx = torch.empty(P + 1, dtype=torch.int32, device="cuda")
+    d_cm = torch.empty(P * m, device="cuda")
+    d_pm = torch.empty(P * m, device="cuda")
+    d_rgba = torch.empty(P * 4, device="cuda")
+
+    def fwd():
+        ctx.stage_generate_moments(wl.camera, wl.gen, Wd, H, m, d_mo, d_b, d_c)
+        ctx.stage_compact(Wd, H, m, d_c, d_mo, d_idx, d_cm)
+        ctx.stage_prepare_moments(Wd, H, m, d_idx, d_cm, d_pm, bias=wl.rec.bias)
+        ctx.stage_reconstruct(wl.camera, wl.rec, Wd, H, m, dmin, dmax, d_idx, d_pm, d_b, d_rgba)
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        ctx.synchronize()
+        ev = _events(args.steps)
+        for e in ev:
+            e[0].record(stream)
+            fn()
+            e[1].record(stream)
+        ctx.synchronize()
+        return statistics.mean(e[0].elapsed_time(e[1]) for e in ev)
+
+    out = {"workload": f"sph{n}_h1/256_{Wd}x{H}_m{m}_persp",
+           "particles": f"{n} particles, 70 % uniform + 30 % in 200 Gaussian clusters (sigma 0.01-0.05), "
+                        "values LogNormal(0, 0.5), one smoothing length h = 1/256 (256^3 cells), cubic spline",
+           "grid_build_ms": min(up)}
+    for name, prec in (("fwd_fp32", M.PRECISION_FP32), ("fwd_precision_form", M.PRECISION_COMPENSATED_FF_MESE)):
+        ctx.precision = prec
+        ms = timed(fwd)
+        out[name] = {"value": P / (ms * 1e-3) / 1e6, "unit": UNIT, "ms": ms}
+    ctx.precision = M.PRECISION_FP32
+    # differentiation form: forward + transfer-function adjoint
+    wl.gen.compact_image = 0
+    b4 = torch.empty(P * 4, device="cuda")
+    rgba = torch.empty((H, Wd, 4), device="cuda")
+    tab = torch.from_numpy(tf.table).cuda()
+    gtab = torch.zeros((256, 4), device="cuda")
+
+    def fwd_bwd():
+        ctx.diff_forward(wl.camera, wl.gen, wl.rec, Wd, H, m, tab, d_mo, b4, d_pm, rgba)
+        with torch.cuda.stream(stream):
+            g = 2.0 * rgba
+            gtab.zero_()
+        ctx.diff_backward(wl.camera, wl.gen, wl.rec, Wd, H, m, tab, d_mo, b4, d_pm, rgba, g, gtab, None)
+
+    ms = timed(fwd_bwd)
+    out["diff_fwd_tf_adjoint"] = {"value": P / (ms * 1e-3) / 1e6, "unit": UNIT, "ms": ms}
+    ctx.close()
+    return out
+
+
+def precision_errors(args, local):
+    """Max and RMS errors of the moments, the transmittance and the RGBA of both arithmetic forms against the FP64
+    oracle of the same method, on every 8th row of a 128 x 128 image of the default workload (its volume and
+    view); pixels whose u16 density bounds differ from the FP64 ones are left out (the bounds are truncated, so
+    a last-bit difference of a sampled extreme can move them one step)."""
+    import torch
+
+    import mray_gb300 as M
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    a = argparse.Namespace(**vars(args))
+    a.image = 128
+    wl = workload(a)
+    Wd, H, m = wl.width, wl.height, wl.num_moments
+    P = Wd * H
+    rows = (0, H, 8)
+    mo64, b64, c64 = O.generate_moments(wl.camera, wl.gen, wl.volume, wl.domain_min, wl.domain_max, Wd, H, m, "f64",
+                                        rows=rows)
+    idx64, _ = O.compact(c64, mo64.astype(np.float32))
+    cnt = c64.reshape(-1)
+    data64 = np.concatenate([mo64.reshape(-1, m)[p, :cnt[p]] for p in range(P)]) if cnt.sum() else np.zeros(0)
+    pm64 = O.prepare_moments(Wd, H, m, idx64, data64, False, 1, None, wl.rec.bias, "f64", rows=rows)
+    tf = O.preintegrate(wl.tf1d, wl.tf_step)
+    rgba64 = O.reconstruct(wl.camera, wl.rec, Wd, H, m, wl.domain_min, wl.domain_max, idx64, pm64, b64, tf, "f64",
+                           rows=rows)
+    ctx = M.Context(local)
+    ctx.set_stream(torch.cuda.current_stream())
+    ctx.upload_grid(torch.from_numpy(wl.volume).cuda(), wl.domain_min, wl.domain_max)
+    ctx.upload_tf(tf)
+    sel = np.zeros((H, Wd), bool)
+    sel[0:H:8] = True
+    out = {"sample": f"rows y = 0 mod 8 of a {Wd}x{H} image of the default volume and view; FP64 oracle of the "
+                     "same method (oracle/mray_oracle.c, double, exact constants)",
+           "moment_error": "max_j |m_j - m_j(FP64)| / max(|m_0(FP64)|, 1e-3) per pixel",
+           "rgba_error": "max over channels |c - c(FP64)| per pixel"}
+    for name, prec in (("fp32", M.PRECISION_FP32), ("precision_form_fp64", M.PRECISION_COMPENSATED_FP64_MESE),
+                       ("precision_form", M.PRECISION_COMPENSATED_FF_MESE)):
+        ctx.precision = prec
+        d_mo = torch.zeros(P * m, device="cuda")
+        d_b = torch.zeros(2 * P, dtype=torch.int16, device="cuda")
+        d_c = torch.zeros(P, dtype=torch.int32, device="cuda")
+        d_idx = torch.zeros(P + 1, dtype=torch.int32, device="cuda")
+        d_cm = torch.zeros(P * m, device="cuda")
+        d_pm = torch.zeros(P * m, device="cuda")
+        d_rgba = torch.zeros(P * 4, device="cuda")
+        ctx.stage_generate_moments(wl.camera, wl.gen, Wd, H, m, d_mo, d_b, d_c)
+        ctx.stage_compact(Wd, H, m, d_c, d_mo, d_idx, d_cm)
+        ctx.stage_prepare_moments(Wd, H, m, d_idx, d_cm, d_pm, bias=wl.rec.bias)
+        ctx.stage_reconstruct(wl.camera, wl.rec, Wd, H, m, wl.domain_min, wl.domain_max, d_idx, d_pm, d_b, d_rgba)
+        ctx.synchronize()
+        mo = d_mo.cpu().numpy().reshape(H, Wd, m).astype(np.float64)
+        b = d_b.cpu().numpy().view(np.uint16).reshape(H, Wd, 2)
+        rgba = d_rgba.cpu().numpy().reshape(H, Wd, 4).astype(np.float64)
+        ok = sel & (c64 > 0) & np.all(b == b64, axis=-1)
+        me = (np.abs(mo - mo64).max(axis=-1) / np.maximum(np.abs(mo64[..., 0]), 1e-3))[ok]
+        te = np.abs(rgba[..., 3] - rgba64[..., 3])[ok]
+        re = np.abs(rgba - rgba64).max(axis=-1)[ok]
+        out[name] = {"pixels": int(ok.sum()),
+                     "moments": {"max": float(me.max()), "rms": float(np.sqrt((me ** 2).mean()))},
+                     "transmittance": {"max": float(te.max()), "rms": float(np.sqrt((te ** 2).mean()))},
+                     "rgba": {"max": float(re.max()), "rms": float(np.sqrt((re ** 2).mean())),
+                              "frac_above_1e-4": float((re > 1e-4).mean()), "frac_above_1e-3": float((re > 1e-3).mean())}}
+    ctx.close()
+    return out
 
 
 def main():

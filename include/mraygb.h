@@ -55,7 +55,11 @@ typedef enum mraygb_precision
     MRAYGB_PRECISION_FP32 = 0,
     /* FP32 ray marching with compensated (Kahan) moment sums; MESE preparation (Levinson recursion,
      * Toeplitz / Herglotz correlations) in FP64 */
-    MRAYGB_PRECISION_COMPENSATED_FP64_MESE = 1
+    MRAYGB_PRECISION_COMPENSATED_FP64_MESE = 1,
+    /* as COMPENSATED_FP64_MESE with the FP64 steps of the preparation (exponential moments, Levinson's
+     * recursion) in float-float arithmetic (about 48 significant bits) and its correlation tail in FP32 on the
+     * rounded results; prediction-coded moments take the FP64 preparation.  No counterpart in the reference. */
+    MRAYGB_PRECISION_COMPENSATED_FF_MESE = 2
 } mraygb_precision;
 
 /* Largest moment count (the reference's file format stores counts in 8 bits: src/main.cpp:288-293). */

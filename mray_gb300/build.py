@@ -33,6 +33,7 @@ SOURCES = [
     ("adjoint.cu", []),
     ("mese.cu", ["--fmad=false"]),
     ("mese_f64.cu", []),
+    ("mese_ff.cu", []),
     ("coding.cu", ["--fmad=false"]),
     ("api.cpp", ["-x", "cu"]),
 ]

@@ -204,7 +204,7 @@ int run_generate_moments(mraygb_context *ctx, const mraygb_camera *cam, const mr
                          float4 *d_bounds4 = nullptr)
 {
     const DeviceCamera dc = to_device_camera(*cam);
-    const bool kahan = ctx->precision == MRAYGB_PRECISION_COMPENSATED_FP64_MESE;
+    const bool kahan = ctx->precision != MRAYGB_PRECISION_FP32;
     if (ctx->volume == mraygb_context::PARTICLES)
         CK(launch_generate_particles(particle_view(ctx), dc, *gp, width, height, m, kahan, d_moments, d_bounds,
                                      d_counts, d_bounds4, ctx->error_flag.as<int>(), ctx->stream),
@@ -251,9 +251,12 @@ int run_compact(mraygb_context *ctx, int width, int height, int m, const uint32_
 int run_prepare(mraygb_context *ctx, int width, int height, int m, const uint32_t *d_index, const float *d_data,
                 int prediction_code, int coding_warp, const uint16_t *d_coding_params, float bias, float *d_out)
 {
-    CK(launch_prepare(width * height, m, d_index, d_data, prediction_code, coding_warp, d_coding_params, bias,
-                      ctx->precision == MRAYGB_PRECISION_COMPENSATED_FP64_MESE, d_out, ctx->stream),
-       "prepare kernel launch");
+    if (ctx->precision == MRAYGB_PRECISION_COMPENSATED_FF_MESE && !prediction_code)
+        CK(launch_prepare_ff(width * height, m, d_index, d_data, bias, d_out, ctx->stream), "prepare kernel launch");
+    else
+        CK(launch_prepare(width * height, m, d_index, d_data, prediction_code, coding_warp, d_coding_params, bias,
+                          ctx->precision != MRAYGB_PRECISION_FP32, d_out, ctx->stream),
+           "prepare kernel launch");
     ctx->launches += 1;
     return MRAYGB_OK;
 }
@@ -486,7 +489,8 @@ int mraygb_synchronize(mraygb_context *ctx)
 int mraygb_set_precision(mraygb_context *ctx, int precision)
 {
     CHECK_CTX();
-    if (precision != MRAYGB_PRECISION_FP32 && precision != MRAYGB_PRECISION_COMPENSATED_FP64_MESE)
+    if (precision != MRAYGB_PRECISION_FP32 && precision != MRAYGB_PRECISION_COMPENSATED_FP64_MESE &&
+        precision != MRAYGB_PRECISION_COMPENSATED_FF_MESE)
         return fail(ctx, MRAYGB_INVALID_ARGUMENT, "unknown precision form %d", precision);
     ctx->precision = precision;
     return MRAYGB_OK;

@@ -177,6 +177,8 @@ cudaError_t mese_init_constants()
     cudaError_t e = init_tables();
     if (e != cudaSuccess)
         return e;
+    if ((e = mese_ff_init_constants()) != cudaSuccess)
+        return e;
     return mese_f64_init_constants();
 }
 

@@ -25,6 +25,7 @@ from .types import Camera, GenerationParameters, ReconstructionParameters
 
 PRECISION_FP32 = 0
 PRECISION_COMPENSATED_FP64_MESE = 1
+PRECISION_COMPENSATED_FF_MESE = 2
 MAX_MOMENTS = 255
 
 

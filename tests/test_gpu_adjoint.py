@@ -76,21 +76,13 @@ def test_diff_forward_matches_oracle(gpu_context, m):
 
 
 def _fd64(wl, volume, table, weights, params, eps=2.0 ** -10):
-    """Central differences of the FP64 oracle under the linear loss sum(weights * rgba)."""
-    out = []
-    for kind, idx in params:
-        vals = []
-        for sgn in (1.0, -1.0):
-            v, t = volume, table
-            if kind == "vox":
-                v = volume.copy()
-                v[idx] += np.float32(sgn * eps)
-            else:
-                t = table.astype(np.float64).copy()
-                t[idx] += sgn * eps
-            vals.append(float((weights * _oracle_rgba(wl, v, t)).sum()))
-        out.append((vals[0] - vals[1]) / (2 * eps))
-    return np.array(out)
+    """Central differences of the FP64 oracle under the linear loss sum(weights * rgba), Richardson-combined."""
+    t64 = table.astype(np.float64)
+
+    def loss(v, t):
+        return float((weights * _oracle_rgba(wl, v, t)).sum())
+
+    return np.array([_richardson(loss, wl, t64, kind, idx, eps) for kind, idx in params])
 
 
 def _pick(rng, grad_vol, grad_tf, n_tf, n_vox):
@@ -137,31 +129,40 @@ def _perturbed(wl, table, kind, idx, delta):
     return v, t
 
 
+def _richardson(loss, wl, table, kind, idx, eps):
+    """Central differences at eps and 2 eps combined as (4 D(eps) - D(2 eps)) / 3, which removes their eps^2
+    truncation term: voxels near where rays enter the volume change the image strongly enough that D(1e-3) alone
+    is off by a few 1e-3."""
+    def d(e):
+        return (loss(*_perturbed(wl, table, kind, idx, e)) - loss(*_perturbed(wl, table, kind, idx, -e))) / (2 * e)
+    return (4.0 * d(eps) - d(2 * eps)) / 3.0
+
+
 def test_l2_adjoint_against_fp64_central_differences(gpu_context):
     """The L2 loss of the configuration (target rendered with the perturbed transfer function): the GPU adjoint,
-    fed the FP64 forward's residual, against central differences (eps = 2^-10, about 1e-3) of the FP64 oracle on
-    32 seeded parameters (16 transfer-function entries, 16 voxels)."""
+    fed the FP64 forward's residual, against central differences (eps = 2^-10, about 1e-3, Richardson-combined
+    with 2 eps) of the FP64 oracle on 32 seeded parameters (16 transfer-function entries, 16 voxels)."""
     wl, table, R, target = _l2_setup(gpu_context)
     rgba64 = _oracle_rgba(wl, wl.volume, table)
     R.forward(wl.volume, table)
     gtf, gvol = R.backward(2.0 * (rgba64 - target))
     params = _pick(np.random.default_rng(17), gvol, gtf, 16, 16)
-    eps = 2.0 ** -10
-    fd = []
-    for kind, idx in params:
-        lp = ((_oracle_rgba(wl, *_perturbed(wl, table, kind, idx, eps)) - target) ** 2).sum()
-        lm = ((_oracle_rgba(wl, *_perturbed(wl, table, kind, idx, -eps)) - target) ** 2).sum()
-        fd.append((lp - lm) / (2 * eps))
-    fd = np.array(fd)
+
+    def loss(v, t):
+        return ((_oracle_rgba(wl, v, t) - target) ** 2).sum()
+
+    fd = np.array([_richardson(loss, wl, table, kind, idx, 2.0 ** -10) for kind, idx in params])
     ad = np.array([gtf[idx] if kind == "tf" else gvol[idx] for kind, idx in params])
     rel = np.abs(ad - fd) / np.abs(fd)
     assert rel.max() <= 1e-3, f"max rel err {rel.max():.3e} at {params[int(rel.argmax())]}"
 
 
 def test_l2_adjoint_against_gpu_central_differences(gpu_context):
-    """Central differences (eps = 1e-3) of the FP32 GPU forward itself on the seeded parameters whose gradient is
-    at least a tenth of the largest of its kind; below that the FP32 rounding of the forward (about 1e-7 of each
-    colour, divided by 2 eps) is no longer small against the difference quotient."""
+    """Central differences (eps = 1e-3, Richardson-combined with 2 eps) of the FP32 GPU forward itself on the
+    seeded parameters whose gradient is at least a tenth of the largest of its kind.  Tolerance 1e-2: the FP32
+    forward's own rounding moves L(p + eps) - L(p - eps) by a few 1e-3 of itself for a single voxel (measured with
+    the oracle's FP32 and FP64 forms of the same method), so the 1e-3 bound is checked against the FP64 oracle's
+    differences above and this test checks that the kernels' FP32 forward and adjoint agree with each other."""
     wl, table, R, target = _l2_setup(gpu_context)
     rgba = R.forward(wl.volume, table)
     gtf, gvol = R.backward(2.0 * (rgba - target))
@@ -170,16 +171,14 @@ def test_l2_adjoint_against_gpu_central_differences(gpu_context):
     vox_ok = np.argwhere(np.abs(gvol) > 0.1 * np.abs(gvol).max())
     params = [("tf", tuple(tf_ok[i])) for i in rng.choice(len(tf_ok), min(16, len(tf_ok)), replace=False)]
     params += [("vox", tuple(vox_ok[i])) for i in rng.choice(len(vox_ok), min(16, len(vox_ok)), replace=False)]
-    eps = 1e-3
-    fd = []
-    for kind, idx in params:
-        lp = ((R.forward(*_perturbed(wl, table, kind, idx, eps)) - target) ** 2).sum()
-        lm = ((R.forward(*_perturbed(wl, table, kind, idx, -eps)) - target) ** 2).sum()
-        fd.append((lp - lm) / (2 * eps))
-    fd = np.array(fd)
+
+    def loss(v, t):
+        return ((R.forward(v, t) - target) ** 2).sum()
+
+    fd = np.array([_richardson(loss, wl, table, kind, idx, 1e-3) for kind, idx in params])
     ad = np.array([gtf[idx] if kind == "tf" else gvol[idx] for kind, idx in params])
     rel = np.abs(ad - fd) / np.abs(fd)
-    assert rel.max() <= 1e-3, f"max rel err {rel.max():.3e} at {params[int(rel.argmax())]}"
+    assert rel.max() <= 1e-2, f"max rel err {rel.max():.3e} at {params[int(rel.argmax())]}"
 
 
 def test_autograd_function_and_tf1d_chain(gpu_context):
