@@ -91,7 +91,7 @@ struct TfGradCache
     }
 };
 
-template <int MAXM> __global__ void __launch_bounds__(128) reconstruct_adjoint_kernel(const ReconAdjDev a)
+template <int MAXM> __global__ void __launch_bounds__(128, 3) reconstruct_adjoint_kernel(const ReconAdjDev a)
 {
     __shared__ float4 s_tf[256];
     __shared__ float4 s_g[256];
@@ -143,8 +143,10 @@ template <int MAXM> __global__ void __launch_bounds__(128) reconstruct_adjoint_k
             // alpha == 1 marks a terminated march (then alpha no longer depends on the samples)
             const float galpha_T = out.w == 1.f ? 0.f : g.w * (1.f - out.w);
             float L0 = 0.f, L1 = 0.f, L2 = 0.f, T = 1.f, tau = 0.f;
-            float pc_f = rclamp(p, -kPiF, 0.0f);
-            float S_f = mese_series<MAXM>(lam2, lam0, pc_f);
+            // each step takes its front sample at phase p: cos(l p) for l < m by complex rotation, once for the series
+            // value S and once more for d S / d lambda_l = 2 cos(l p) (the forward sums the same series by Reinsch's
+            // recurrence; the two agree to a few ulp of the multipliers' sum)
+            float pc = rclamp(p, -kPiF, 0.0f);
             int it = 0;
             while (t <= t_far)
             {
@@ -153,14 +155,22 @@ template <int MAXM> __global__ void __launch_bounds__(128) reconstruct_adjoint_k
                     atomicExch(a.error_flag, 1);
                     break;
                 }
-                t = __fadd_rn(t, a.step);
-                p = __fadd_rn(p, phase_step);
-                const float pc_b = rclamp(p, -kPiF, 0.0f);
-                const float S_b = mese_series<MAXM>(lam2, lam0, pc_b);
-                const float r = atanf(S_f) * 0.318309886f + 0.5f;
+                float cs, sn;
+                sincosf(pc, &sn, &cs);
+                float S = lam0, zr = cs, zi = sn;
+#pragma unroll
+                for (int l = 1; l < MAXM; ++l)
+                {
+                    S = fmaf(lam2[l], zr, S);
+                    const float nr = zr * cs - zi * sn;
+                    zi = fmaf(zr, sn, zi * cs);
+                    zr = nr;
+                }
+                const float r = atanf(S) * 0.318309886f + 0.5f;
                 const float fs = r * span + lo;
                 const BSplineTap k = bspline_tap(fs);
-                const float4 s = tf_sample_bspline(s_tf, k);
+                float4 s, dt;
+                tf_bspline_value_derivative(s_tf, k, s, dt);
                 // d loss / d sample: emission terms see T before this step, extinction the radiance behind it
                 float4 gs;
                 gs.x = g.x * a.emission * T;
@@ -176,29 +186,25 @@ template <int MAXM> __global__ void __launch_bounds__(128) reconstruct_adjoint_k
                 // transfer-function entries
                 cache.add(s_g, k, gs);
                 // front density -> series value -> multipliers and bounds
-                {
-                    const float4 dt = tf_bspline_derivative(s_tf, k);
-                    const float gfs = dt.x * gs.x + dt.y * gs.y + dt.z * gs.z + dt.w * gs.w;
-                    glo = fmaf(gfs, 1.f - r, glo);
-                    ghi = fmaf(gfs, r, ghi);
-                    const float gS = gfs * span * 0.318309886f / fmaf(S_f, S_f, 1.f);
-                    glam[0] += gS;
-                    // d S / d lambda_l = 2 cos(l pc) by complex rotation
-                    float cs, sn;
-                    sincosf(pc_f, &sn, &cs);
-                    float zr = cs, zi = sn;
-                    const float g2 = 2.f * gS;
+                const float gfs = dt.x * gs.x + dt.y * gs.y + dt.z * gs.z + dt.w * gs.w;
+                glo = fmaf(gfs, 1.f - r, glo);
+                ghi = fmaf(gfs, r, ghi);
+                const float gS = gfs * span * 0.318309886f / fmaf(S, S, 1.f);
+                glam[0] += gS;
+                const float g2 = 2.f * gS;
+                zr = cs;
+                zi = sn;
 #pragma unroll
-                    for (int l = 1; l < MAXM; ++l)
-                    {
-                        glam[l] = fmaf(g2, zr, glam[l]);
-                        const float nr = zr * cs - zi * sn;
-                        zi = fmaf(zr, sn, zi * cs);
-                        zr = nr;
-                    }
+                for (int l = 1; l < MAXM; ++l)
+                {
+                    glam[l] = fmaf(g2, zr, glam[l]);
+                    const float nr = zr * cs - zi * sn;
+                    zi = fmaf(zr, sn, zi * cs);
+                    zr = nr;
                 }
-                pc_f = pc_b;
-                S_f = S_b;
+                t = __fadd_rn(t, a.step);
+                p = __fadd_rn(p, phase_step);
+                pc = rclamp(p, -kPiF, 0.0f);
                 if (alpha >= a.ert)
                     break;
             }

@@ -9,6 +9,8 @@
 // Levinson solution and exponential moments adds about 1e-7.  So the values of the first two steps are float pairs
 // (hi + lo, about 48 significant bits) and the tail is FP32.
 //
+// Layout: a pixel per group of 8 lanes, its arrays in shared memory (see prepare_ff_kernel).
+//
 // Arithmetic: error-free transformations (two-sum, two-product by FMA) written with explicit round-to-nearest
 // intrinsics, so no contraction can change them.  Sums of products use the compensated dot-product scheme of
 // Ogita, Rump and Oishi ("Accurate sum and dot product", SIAM J. Sci. Comput. 26(6), 2005): the running sum in
@@ -128,71 +130,120 @@ __device__ __forceinline__ void pixel_span_ff(const uint32_t *index, int m, int 
     }
 }
 
-// Lagrange multipliers of one pixel (prepare_moments_from_std_coding, src/moment_preparation.h:55-64)
+// ---- one pixel per group of 8 lanes ----------------------------------------------------------------------
+// The arrays of a pixel (x, E, sol as float pairs) live in shared memory; the 8 lanes of its group split every
+// sum (lane r takes the indices = r mod 8, each with its own compensated accumulator) and combine the partial
+// sums with three butterfly shuffles, and split the Levinson update by index pairs.  Per pixel 10 floats per
+// moment of shared memory.
+
+constexpr int kGroup = 8;
+constexpr int kPixPerBlock = 16; // 128 threads
+
+// (s, c) compensated partial sums of the group combined: two-sum of the running sums, compensations added
+__device__ __forceinline__ void group_reduce(Dot &d)
+{
+#pragma unroll
+    for (int o = 1; o < kGroup; o <<= 1)
+    {
+        const float s2 = __shfl_xor_sync(0xffffffffu, d.s, o);
+        const float c2 = __shfl_xor_sync(0xffffffffu, d.c, o);
+        const ff t = two_sum(d.s, s2);
+        d.s = t.hi;
+        d.c = __fadd_rn(__fadd_rn(d.c, c2), t.lo);
+    }
+}
+
+template <int MAXM> struct FfLayout
+{
+    static constexpr int floats_per_pixel = MAXM * 10; // E, sol (4 floats per moment), x (2)
+};
+
 template <int MAXM>
 __global__ void __launch_bounds__(128) prepare_ff_kernel(int num_pixels, int m, const uint32_t *__restrict__ index,
                                                          const float *__restrict__ data, float bias,
                                                          float *__restrict__ out)
 {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= num_pixels)
+    extern __shared__ __align__(16) float smem_ff[];
+    const int lane = threadIdx.x & 31;
+    const int r = lane & (kGroup - 1);
+    const int slot = threadIdx.x / kGroup;
+    const int p = blockIdx.x * kPixPerBlock + slot;
+    float *base = smem_ff + (size_t)slot * FfLayout<MAXM>::floats_per_pixel;
+    cff *E = reinterpret_cast<cff *>(base);
+    cff *sol = E + MAXM;
+    ff *x = reinterpret_cast<ff *>(sol + MAXM);
+
+    size_t idx = 0;
+    int n = 0;
+    if (p < num_pixels)
+    {
+        pixel_span_ff(index, m, p, idx, n);
+        n = n < MAXM ? n : MAXM;
+    }
+    // every group of the warp runs the same number of steps (the shuffles span the warp)
+    const int nw = __reduce_max_sync(0xffffffffu, n);
+    if (nw == 0)
         return;
-    size_t idx;
-    int n;
-    pixel_span_ff(index, m, p, idx, n);
-    if (n <= 0)
-        return;
-    if (n > MAXM)
-        n = MAXM;
     const float *in = data + idx;
 
-    // cut::lerp(m, target, bias) in pairs: (1 - b) m_i (+ b / 2 for i = 0)
-    ff x[MAXM];
+    // cut::lerp(m, target, bias) in pairs
     const ff omb = two_sum(1.f, -bias);
-    for (int i = 0; i < n; ++i)
-        x[i] = ff_mul_f(omb, in[i]);
-    x[0] = ff_add(x[0], {__fmul_rn(bias, 0.5f), 0.f});
-
-    // exponential moments: E_0 = e^{i (pi x_0 - pi / 2)} / (4 pi) (in FP64: one sincos per pixel),
-    // E_l = (2 pi i / l) sum_{j<l} (l - j) x_{l-j} E_j, E_0 doubled at the end
-    cff E[MAXM];
+    for (int i = r; i < nw; i += kGroup)
     {
-        const double phi = 3.141592653589793 * ((double)x[0].hi + (double)x[0].lo) - 1.5707963267948966;
+        ff v = ff_mul_f(omb, i < n ? in[i] : 0.f);
+        if (i == 0)
+            v = ff_add(v, {__fmul_rn(bias, 0.5f), 0.f});
+        x[i] = v;
+    }
+    if (r == 0)
+    {
+        const ff x0 = n > 0 ? x[0] : ff{0.f, 0.f};
+        const double phi = 3.141592653589793 * ((double)x0.hi + (double)x0.lo) - 1.5707963267948966;
         double sp, cp;
         sincos(phi, &sp, &cp);
         E[0].re = ff_from_double(0.07957747154594767 * cp);
         E[0].im = ff_from_double(0.07957747154594767 * sp);
     }
-    for (int l = 1; l < n; ++l)
+    __syncwarp();
+
+    // exponential moments: E_l = (2 pi i / l) sum_{j<l} (l - j) x_{l-j} E_j
+    for (int l = 1; l < nw; ++l)
     {
         Dot ar, ai;
-        for (int j = 0; j < l; ++j)
+        for (int j = r; j < l; j += kGroup)
         {
-            const ff s = ff_mul_f(x[l - j], (float)(l - j));
-            ar.add(s, E[j].re);
-            ai.add(s, E[j].im);
+            const ff sc = ff_mul_f(x[l - j], (float)(l - j));
+            const cff e = E[j];
+            ar.add(sc, e.re);
+            ai.add(sc, e.im);
         }
-        const float2 w2 = c_two_pi_over_l_ff[l];
-        const ff w = {w2.x, w2.y};
-        // (i w)(re + i im) = (-w im, w re)
-        E[l].re = ff_neg(ff_mul(w, ai.result()));
-        E[l].im = ff_mul(w, ar.result());
+        group_reduce(ar);
+        group_reduce(ai);
+        if (r == 0)
+        {
+            const float2 w2 = c_two_pi_over_l_ff[l];
+            const ff w = {w2.x, w2.y};
+            E[l].re = ff_neg(ff_mul(w, ai.result()));
+            E[l].im = ff_mul(w, ar.result());
+        }
+        __syncwarp();
     }
-    E[0].re = {2.f * E[0].re.hi, 2.f * E[0].re.lo};
-    E[0].im = {2.f * E[0].im.hi, 2.f * E[0].im.lo};
+    if (r == 0)
+    {
+        E[0].re = {2.f * E[0].re.hi, 2.f * E[0].re.lo};
+        E[0].im = {2.f * E[0].im.hi, 2.f * E[0].im.lo};
+        sol[0].re = ff_div({1.f, 0.f}, E[0].re);
+        sol[0].im = {0.f, 0.f};
+    }
+    __syncwarp();
 
     // Levinson's recursion with the invalid latch
-    cff sol[MAXM];
-    sol[0].re = ff_div({1.f, 0.f}, E[0].re);
-    sol[0].im = {0.f, 0.f};
     bool invalid = false;
-    for (int j = 1; j < n; ++j)
+    for (int j = 1; j < nw; ++j)
     {
-        cff u = {{0.f, 0.f}, {0.f, 0.f}};
+        Dot ur, ui;
         if (!invalid)
-        {
-            Dot ur, ui;
-            for (int k = 0; k < j; ++k)
+            for (int k = r; k < j; k += kGroup)
             {
                 const cff a = sol[k], b = E[j - k];
                 ur.add(a.re, b.re);
@@ -200,9 +251,9 @@ __global__ void __launch_bounds__(128) prepare_ff_kernel(int num_pixels, int m, 
                 ui.add(a.re, b.im);
                 ui.add(a.im, b.re);
             }
-            u.re = ur.result();
-            u.im = ui.result();
-        }
+        group_reduce(ur);
+        group_reduce(ui);
+        cff u = {ur.result(), ui.result()};
         Dot a2d;
         a2d.add(u.re, u.re);
         a2d.add(u.im, u.im);
@@ -214,13 +265,12 @@ __global__ void __launch_bounds__(128) prepare_ff_kernel(int num_pixels, int m, 
             invalid = true;
         }
         const ff f = ff_div({1.f, 0.f}, ff_add({1.f, 0.f}, ff_neg(a2)));
-        // new_k = f (o_k - conj(o_{j-k}) u), pairs (k, j - k) in place
         const ff s0 = sol[0].re;
-        int k = 1, kk = j - 1;
-        for (; k <= kk; ++k, --kk)
+        // new_k = f (o_k - conj(o_{j-k}) u) for the pairs (k, j - k), 1 <= k <= j / 2
+        for (int k = 1 + r; k <= j - k; k += kGroup)
         {
+            const int kk = j - k;
             const cff a = sol[k], b = sol[kk];
-            // conj(b) u = (b.re u.re + b.im u.im, b.re u.im - b.im u.re)
             Dot vr, vi;
             vr.init(a.re);
             vr.sub(b.re, u.re);
@@ -228,8 +278,7 @@ __global__ void __launch_bounds__(128) prepare_ff_kernel(int num_pixels, int m, 
             vi.init(a.im);
             vi.sub(b.re, u.im);
             vi.add(b.im, u.re);
-            sol[k].re = ff_mul(f, vr.result());
-            sol[k].im = ff_mul(f, vi.result());
+            cff na = {ff_mul(f, vr.result()), ff_mul(f, vi.result())};
             if (k != kk)
             {
                 Dot wr, wi;
@@ -239,52 +288,69 @@ __global__ void __launch_bounds__(128) prepare_ff_kernel(int num_pixels, int m, 
                 wi.init(b.im);
                 wi.sub(a.re, u.im);
                 wi.add(a.im, u.re);
-                sol[kk].re = ff_mul(f, wr.result());
-                sol[kk].im = ff_mul(f, wi.result());
+                sol[kk] = {ff_mul(f, wr.result()), ff_mul(f, wi.result())};
             }
+            sol[k] = na;
         }
-        sol[j].re = ff_neg(ff_mul(ff_mul(f, s0), u.re));
-        sol[j].im = ff_neg(ff_mul(ff_mul(f, s0), u.im));
-        sol[0].re = ff_mul(f, s0);
+        if (r == 0)
+        {
+            const ff fs0 = ff_mul(f, s0);
+            sol[j] = {ff_neg(ff_mul(fs0, u.re)), ff_neg(ff_mul(fs0, u.im))};
+            sol[0] = {fs0, {0.f, 0.f}};
+        }
+        __syncwarp();
     }
 
-    // the tail in FP32 on the rounded values: P = 2 pi sol, E_0 halved, autocorrelation scattered into the
-    // imaginary correlation (lagrange_from_poly)
-    cx<float> P[MAXM], Ef[MAXM];
-    float acc[MAXM];
-    for (int i = 0; i < n; ++i)
-    {
-        P[i] = {6.28318531f * ff_round(sol[i].re), 6.28318531f * ff_round(sol[i].im)};
-        Ef[i] = {ff_round(E[i].re), ff_round(E[i].im)};
-        acc[i] = 0.f;
-    }
-    Ef[0] = {0.5f * Ef[0].x, 0.5f * Ef[0].y};
-    for (int q = 0; q < n; ++q)
+    // the tail in FP32 on the rounded values (lagrange_from_poly): P = 2 pi sol and the exponential moments with
+    // E_0 halved, as float complex in the space of x; then the autocorrelation a_q and the correlation
+    cx<float> *Pf = reinterpret_cast<cx<float> *>(x);
+    for (int i = r; i < nw; i += kGroup)
+        Pf[i] = {6.28318531f * ff_round(sol[i].re), 6.28318531f * ff_round(sol[i].im)};
+    __syncwarp();
+    // a_q into sol's space (as float complex), E rounded into E's second half-space is not needed: read E directly
+    cx<float> *A = reinterpret_cast<cx<float> *>(sol);
+    for (int q = r; q < nw; q += kGroup)
     {
         float ar = 0.f, ai = 0.f;
-        for (int j = 0; j < n - q; ++j)
+        for (int j = 0; j < nw - q; ++j)
         {
-            // P_j conj(P_{j+q})
-            ar = fmaf(P[j].x, P[j + q].x, fmaf(P[j].y, P[j + q].y, ar));
-            ai = fmaf(P[j].y, P[j + q].x, fmaf(-P[j].x, P[j + q].y, ai));
+            const cx<float> a = Pf[j], b = Pf[j + q];
+            ar = fmaf(a.x, b.x, fmaf(a.y, b.y, ar));
+            ai = fmaf(a.y, b.x, fmaf(-a.x, b.y, ai));
         }
-        for (int k = 0; k <= q; ++k)
-        {
-            const cx<float> e = Ef[q - k];
-            acc[k] = fmaf(ar, e.y, fmaf(ai, e.x, acc[k]));
-        }
+        A[q] = {ar, ai};
     }
-    const float norm = 1.f / (3.14159265f * P[0].x);
-    float *o = out + idx;
-    for (int i = 0; i < n; ++i)
-        o[i] = norm * acc[i];
+    __syncwarp();
+    const float norm = 1.f / (3.14159265f * Pf[0].x);
+    for (int k = r; k < nw; k += kGroup)
+    {
+        float acc = 0.f;
+        for (int q = k; q < nw; ++q)
+        {
+            const cff e = E[q - k];
+            float ex = ff_round(e.re), ey = ff_round(e.im);
+            if (q == k)
+            {
+                ex *= 0.5f;
+                ey *= 0.5f;
+            }
+            acc = fmaf(A[q].x, ey, fmaf(A[q].y, ex, acc));
+        }
+        if (k < n)
+            out[idx + k] = norm * acc;
+    }
 }
 
 template <int MAXM>
 cudaError_t launch_ff_m(int num_pixels, int m, const uint32_t *index, const float *data, float bias, float *out,
                         cudaStream_t stream)
 {
-    prepare_ff_kernel<MAXM><<<(num_pixels + 127) / 128, 128, 0, stream>>>(num_pixels, m, index, data, bias, out);
+    const int bytes = kPixPerBlock * FfLayout<MAXM>::floats_per_pixel * (int)sizeof(float);
+    cudaError_t e = cudaFuncSetAttribute(prepare_ff_kernel<MAXM>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e != cudaSuccess)
+        return e;
+    prepare_ff_kernel<MAXM><<<(num_pixels + kPixPerBlock - 1) / kPixPerBlock, kPixPerBlock * kGroup, bytes, stream>>>(
+        num_pixels, m, index, data, bias, out);
     return cudaGetLastError();
 }
 
