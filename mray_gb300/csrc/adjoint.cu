@@ -91,17 +91,22 @@ struct TfGradCache
     }
 };
 
+// The transfer-function gradient of a block is accumulated in kTfCopies copies of the 256-entry table in shared
+// memory, lane l adding to copy l mod kTfCopies: neighbouring rays sample similar densities at the same step, and
+// shared-memory atomics on one address from many lanes of a warp serialize.
+constexpr int kTfCopies = 16;
+
 template <int MAXM> __global__ void __launch_bounds__(128, 3) reconstruct_adjoint_kernel(const ReconAdjDev a)
 {
     __shared__ float4 s_tf[256];
-    __shared__ float4 s_g[256];
+    extern __shared__ float4 s_gall[]; // kTfCopies * 256 (dynamic: above the 48 KiB of static shared memory)
     const int tid = threadIdx.x + threadIdx.y * blockDim.x;
     for (int i = tid; i < 256; i += blockDim.x * blockDim.y)
-    {
         s_tf[i] = a.tf[i];
-        s_g[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-    }
+    for (int i = tid; i < kTfCopies * 256; i += blockDim.x * blockDim.y)
+        s_gall[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     __syncthreads();
+    float4 *s_g = s_gall + (tid % kTfCopies) * 256;
 
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
@@ -143,9 +148,8 @@ template <int MAXM> __global__ void __launch_bounds__(128, 3) reconstruct_adjoin
             // alpha == 1 marks a terminated march (then alpha no longer depends on the samples)
             const float galpha_T = out.w == 1.f ? 0.f : g.w * (1.f - out.w);
             float L0 = 0.f, L1 = 0.f, L2 = 0.f, T = 1.f, tau = 0.f;
-            // each step takes its front sample at phase p: cos(l p) for l < m by complex rotation, once for the series
-            // value S and once more for d S / d lambda_l = 2 cos(l p) (the forward sums the same series by Reinsch's
-            // recurrence; the two agree to a few ulp of the multipliers' sum)
+            // each step takes its front sample at phase p: the series value S by the forward's own recurrence
+            // (mese_series), and d S / d lambda_l = 2 cos(l p) from the modified three-term recurrence below
             float pc = rclamp(p, -kPiF, 0.0f);
             int it = 0;
             while (t <= t_far)
@@ -155,17 +159,7 @@ template <int MAXM> __global__ void __launch_bounds__(128, 3) reconstruct_adjoin
                     atomicExch(a.error_flag, 1);
                     break;
                 }
-                float cs, sn;
-                sincosf(pc, &sn, &cs);
-                float S = lam0, zr = cs, zi = sn;
-#pragma unroll
-                for (int l = 1; l < MAXM; ++l)
-                {
-                    S = fmaf(lam2[l], zr, S);
-                    const float nr = zr * cs - zi * sn;
-                    zi = fmaf(zr, sn, zi * cs);
-                    zr = nr;
-                }
+                const float S = mese_series<MAXM>(lam2, lam0, pc);
                 const float r = atanf(S) * 0.318309886f + 0.5f;
                 const float fs = r * span + lo;
                 const BSplineTap k = bspline_tap(fs);
@@ -191,16 +185,27 @@ template <int MAXM> __global__ void __launch_bounds__(128, 3) reconstruct_adjoin
                 ghi = fmaf(gfs, r, ghi);
                 const float gS = gfs * span * 0.318309886f / fmaf(S, S, 1.f);
                 glam[0] += gS;
-                const float g2 = 2.f * gS;
-                zr = cs;
-                zi = sn;
-#pragma unroll
-                for (int l = 1; l < MAXM; ++l)
+                // cos(l pc) for l >= 1 by Reinsch's modification of the three-term recurrence (stable where pc
+                // nears 0 or -pi, the two ends of every ray): with d = -4 sin^2(pc / 2) while cos pc > 0,
+                //   e_{l+1} = e_l + d c_l,  c_{l+1} = c_l + e_{l+1}      (e_l = c_l - c_{l-1}),
+                // and with d = 4 cos^2(pc / 2) otherwise,
+                //   e_{l+1} = d c_l - e_l,  c_{l+1} = e_{l+1} - c_l      (e_l = c_l + c_{l-1})
                 {
-                    glam[l] = fmaf(g2, zr, glam[l]);
-                    const float nr = zr * cs - zi * sn;
-                    zi = fmaf(zr, sn, zi * cs);
-                    zr = nr;
+                    float sh, ch;
+                    sincosf(0.5f * pc, &sh, &ch);
+                    const bool pos = fabsf(pc) < 1.5707963267948966f;
+                    const float sg = pos ? 1.f : -1.f;
+                    const float d = pos ? -4.f * sh * sh : 4.f * ch * ch;
+                    float e = 0.5f * d;
+                    float c = e + sg; // cos pc: 1 + d/2, or d/2 - 1
+                    const float g2 = 2.f * gS;
+#pragma unroll
+                    for (int l = 1; l < MAXM; ++l)
+                    {
+                        glam[l] = fmaf(g2, c, glam[l]);
+                        e = fmaf(d, c, sg * e);
+                        c = fmaf(sg, c, e);
+                    }
                 }
                 t = __fadd_rn(t, a.step);
                 p = __fadd_rn(p, phase_step);
@@ -219,7 +224,16 @@ template <int MAXM> __global__ void __launch_bounds__(128, 3) reconstruct_adjoin
     __syncthreads();
     for (int i = tid; i < 256; i += blockDim.x * blockDim.y)
     {
-        const float4 v = s_g[i];
+        float4 v = s_gall[i];
+#pragma unroll
+        for (int c = 1; c < kTfCopies; ++c)
+        {
+            const float4 w = s_gall[c * 256 + i];
+            v.x += w.x;
+            v.y += w.y;
+            v.z += w.z;
+            v.w += w.w;
+        }
         if (v.x != 0.f)
             atomicAdd(&a.grad_tf[i].x, v.x);
         if (v.y != 0.f)
@@ -522,10 +536,8 @@ __device__ __forceinline__ void scatter_sample(const GridView &g, float *grad, f
     {
         const int dx = c & 1, dy = (c >> 1) & 1, dz = c >> 2;
         const float w = (dx ? a[0] : 1.f - a[0]) * (dy ? a[1] : 1.f - a[1]) * (dz ? a[2] : 1.f - a[2]);
-        int x = il[0] + dx, y = il[1] + dy, z = il[2] + dz;
-        x = x < 0 ? 0 : (x > g.nx - 1 ? g.nx - 1 : x);
-        y = y < 0 ? 0 : (y > g.ny - 1 ? g.ny - 1 : y);
-        z = z < 0 ? 0 : (z > g.nz - 1 ? g.nz - 1 : z);
+        const int x = min(max(il[0] + dx, 0), g.nx - 1), y = min(max(il[1] + dy, 0), g.ny - 1),
+                  z = min(max(il[2] + dz, 0), g.nz - 1);
         if (w != 0.f)
             atomicAdd(grad + ((size_t)z * (size_t)(g.ny * g.nx) + (size_t)(y * g.nx) + (size_t)x), w * gs);
     }
@@ -846,11 +858,17 @@ template <int NJ> __global__ void __launch_bounds__(128) generate_adjoint_kernel
     }
 }
 
-template <int MAXM> void launch_recon_adj(const ReconAdjDev &a, cudaStream_t stream)
+template <int MAXM> cudaError_t launch_recon_adj(const ReconAdjDev &a, cudaStream_t stream)
 {
+    const int bytes = kTfCopies * 256 * (int)sizeof(float4);
+    cudaError_t e =
+        cudaFuncSetAttribute(reconstruct_adjoint_kernel<MAXM>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e != cudaSuccess)
+        return e;
     dim3 block(16, 8);
     dim3 grid((a.width + 15) / 16, (a.height + 7) / 8);
-    reconstruct_adjoint_kernel<MAXM><<<grid, block, 0, stream>>>(a);
+    reconstruct_adjoint_kernel<MAXM><<<grid, block, bytes, stream>>>(a);
+    return cudaGetLastError();
 }
 
 template <int MAXM>
@@ -892,14 +910,12 @@ cudaError_t launch_reconstruct_adjoint(const ReconAdjArgs &r, int *error_flag, c
     a.grad_tf = r.grad_tf;
     a.error_flag = error_flag;
     if (r.m <= 8)
-        launch_recon_adj<8>(a, stream);
-    else if (r.m <= 16)
-        launch_recon_adj<16>(a, stream);
-    else if (r.m <= 32)
-        launch_recon_adj<32>(a, stream);
-    else
-        launch_recon_adj<64>(a, stream);
-    return cudaGetLastError();
+        return launch_recon_adj<8>(a, stream);
+    if (r.m <= 16)
+        return launch_recon_adj<16>(a, stream);
+    if (r.m <= 32)
+        return launch_recon_adj<32>(a, stream);
+    return launch_recon_adj<64>(a, stream);
 }
 
 cudaError_t launch_prepare_adjoint(int num_pixels, int m, const float *moments, float bias, const float *grad_lambda,

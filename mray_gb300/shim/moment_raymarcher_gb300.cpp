@@ -100,21 +100,16 @@ mraygb_reconstruction_params to_c(const ReconstructionParameters &p)
 
 } // namespace
 
-void generate_device(cut::Camera cam, const RegularGrid &volume, MomentImageHost &img,
-                     const GenerationParameters &params)
+namespace
 {
-    if (volume.type != RegularGrid::DataType::F32)
-    {
-        std::fprintf(stderr, "mraygb: only float grids are supported\n");
-        std::terminate();
-    }
-    const float dmin[3] = {volume.domain.min.x, volume.domain.min.y, volume.domain.min.z};
-    const float dmax[3] = {volume.domain.max.x, volume.domain.max.y, volume.domain.max.z};
-    check(mraygb_upload_grid(context(), volume.data.data(), volume.size.x, volume.size.y, volume.size.z, dmin, dmax,
-                             0));
+
+// the moment image of the volume uploaded last, written into the reference's container
+void generate_uploaded(const cut::Camera &cam, const Range<Vec3f> &domain, MomentImageHost &img,
+                       const GenerationParameters &params)
+{
     const auto c = to_c(cam);
     const auto g = to_c(params);
-    img.domain = volume.domain;
+    img.domain = domain;
     img.data.resize(size_t(img.width) * img.height * img.num_moments);
     if (params.compact_image)
         img.index.resize(size_t(img.width) * img.height + 1);
@@ -139,6 +134,33 @@ void generate_device(cut::Camera cam, const RegularGrid &volume, MomentImageHost
     if (params.prediction_coding && params.coding_warp == CODING_WARP_DEFAULT_TRANSFORMED)
         for (int i = 0; i + 1 < img.num_moments; ++i)
             img.coding_params.push_back(CodingParamType{cp[2 * i], cp[2 * i + 1]});
+}
+
+} // namespace
+
+void generate_device(cut::Camera cam, const RegularGrid &volume, MomentImageHost &img,
+                     const GenerationParameters &params)
+{
+    if (volume.type != RegularGrid::DataType::F32)
+    {
+        std::fprintf(stderr, "mraygb: only float grids are supported\n");
+        std::terminate();
+    }
+    const float dmin[3] = {volume.domain.min.x, volume.domain.min.y, volume.domain.min.z};
+    const float dmax[3] = {volume.domain.max.x, volume.domain.max.y, volume.domain.max.z};
+    check(mraygb_upload_grid(context(), volume.data.data(), volume.size.x, volume.size.y, volume.size.z, dmin, dmax,
+                             0));
+    generate_uploaded(cam, volume.domain, img, params);
+}
+
+void generate_device(cut::Camera cam, const Particles &volume, MomentImageHost &img,
+                     const GenerationParameters &params)
+{
+    const float dmin[3] = {volume.domain.min.x, volume.domain.min.y, volume.domain.min.z};
+    const float dmax[3] = {volume.domain.max.x, volume.domain.max.y, volume.domain.max.z};
+    check(mraygb_upload_particles(context(), volume.x.data(), volume.y.data(), volume.z.data(),
+                                  volume.values.data(), volume.size(), volume.smoothing_length, dmin, dmax, 0));
+    generate_uploaded(cam, volume.domain, img, params);
 }
 
 void reconstruct_device(cut::Camera cam, const MomentImageHost &mi, const TransferFunction &tf, ColorImageHost &cimg,
