@@ -107,6 +107,8 @@ struct Dot
     }
     __device__ __forceinline__ void sub(ff a, ff b) { add(ff_neg(a), b); }
     __device__ __forceinline__ ff result() const { return two_sum(s, c); }
+    // where the compensation is far below the sum (or both are tiny): the pair normalised in three operations
+    __device__ __forceinline__ ff fast_result() const { return fast_two_sum(s, c); }
 };
 
 struct cff
@@ -130,20 +132,25 @@ __device__ __forceinline__ void pixel_span_ff(const uint32_t *index, int m, int 
     }
 }
 
-// ---- one pixel per group of 8 lanes ----------------------------------------------------------------------
-// The arrays of a pixel (x, E, sol as float pairs) live in shared memory; the 8 lanes of its group split every
-// sum (lane r takes the indices = r mod 8, each with its own compensated accumulator) and combine the partial
-// sums with three butterfly shuffles, and split the Levinson update by index pairs.  Per pixel 10 floats per
-// moment of shared memory.
+// ---- one pixel per group of G lanes -----------------------------------------------------------------------
+// The arrays of a pixel (x, E, sol as float pairs) live in shared memory; the G lanes of its group split every
+// sum (lane r takes the indices = r mod G, each with its own compensated accumulator) and combine the partial
+// sums with butterfly shuffles, and split the Levinson update by index pairs.  Per pixel 10 floats per moment of
+// shared memory.
 
-constexpr int kGroup = 8;
-constexpr int kPixPerBlock = 16; // 128 threads
+// G = 8 lanes per pixel (measured at 64 moments: 3.36 ms per 512^2 launch; 4 lanes, with one shuffle level less
+// per sum but half the warps per SM for the same shared memory, 4.60 ms)
+template <int MAXM> struct FfGroup
+{
+    static constexpr int G = 8;
+    static constexpr int pixels = MAXM <= 128 ? 16 : 8;
+};
 
 // (s, c) compensated partial sums of the group combined: two-sum of the running sums, compensations added
-__device__ __forceinline__ void group_reduce(Dot &d)
+template <int G> __device__ __forceinline__ void group_reduce(Dot &d)
 {
 #pragma unroll
-    for (int o = 1; o < kGroup; o <<= 1)
+    for (int o = 1; o < G; o <<= 1)
     {
         const float s2 = __shfl_xor_sync(0xffffffffu, d.s, o);
         const float c2 = __shfl_xor_sync(0xffffffffu, d.c, o);
@@ -165,9 +172,10 @@ __global__ void __launch_bounds__(128) prepare_ff_kernel(int num_pixels, int m, 
 {
     extern __shared__ __align__(16) float smem_ff[];
     const int lane = threadIdx.x & 31;
+    constexpr int kGroup = FfGroup<MAXM>::G;
     const int r = lane & (kGroup - 1);
     const int slot = threadIdx.x / kGroup;
-    const int p = blockIdx.x * kPixPerBlock + slot;
+    const int p = blockIdx.x * FfGroup<MAXM>::pixels + slot;
     float *base = smem_ff + (size_t)slot * FfLayout<MAXM>::floats_per_pixel;
     cff *E = reinterpret_cast<cff *>(base);
     cff *sol = E + MAXM;
@@ -186,18 +194,13 @@ __global__ void __launch_bounds__(128) prepare_ff_kernel(int num_pixels, int m, 
         return;
     const float *in = data + idx;
 
-    // cut::lerp(m, target, bias) in pairs
+    // cut::lerp(m, target, bias) in pairs; x holds y_i = i x_i, the factors of the recurrence below
     const ff omb = two_sum(1.f, -bias);
     for (int i = r; i < nw; i += kGroup)
-    {
-        ff v = ff_mul_f(omb, i < n ? in[i] : 0.f);
-        if (i == 0)
-            v = ff_add(v, {__fmul_rn(bias, 0.5f), 0.f});
-        x[i] = v;
-    }
+        x[i] = ff_mul_f(ff_mul_f(omb, i < n ? in[i] : 0.f), (float)i);
     if (r == 0)
     {
-        const ff x0 = n > 0 ? x[0] : ff{0.f, 0.f};
+        const ff x0 = ff_add(ff_mul_f(omb, n > 0 ? in[0] : 0.f), {__fmul_rn(bias, 0.5f), 0.f});
         const double phi = 3.141592653589793 * ((double)x0.hi + (double)x0.lo) - 1.5707963267948966;
         double sp, cp;
         sincos(phi, &sp, &cp);
@@ -206,19 +209,19 @@ __global__ void __launch_bounds__(128) prepare_ff_kernel(int num_pixels, int m, 
     }
     __syncwarp();
 
-    // exponential moments: E_l = (2 pi i / l) sum_{j<l} (l - j) x_{l-j} E_j
+    // exponential moments: E_l = (2 pi i / l) sum_{j<l} y_{l-j} E_j
     for (int l = 1; l < nw; ++l)
     {
         Dot ar, ai;
         for (int j = r; j < l; j += kGroup)
         {
-            const ff sc = ff_mul_f(x[l - j], (float)(l - j));
+            const ff sc = x[l - j];
             const cff e = E[j];
             ar.add(sc, e.re);
             ai.add(sc, e.im);
         }
-        group_reduce(ar);
-        group_reduce(ai);
+        group_reduce<kGroup>(ar);
+        group_reduce<kGroup>(ai);
         if (r == 0)
         {
             const float2 w2 = c_two_pi_over_l_ff[l];
@@ -237,8 +240,11 @@ __global__ void __launch_bounds__(128) prepare_ff_kernel(int num_pixels, int m, 
     }
     __syncwarp();
 
-    // Levinson's recursion with the invalid latch
+    // Levinson's recursion with the invalid latch, on the solution divided by F = prod_j f_j: with
+    // sol = F shat the update new_k = f (o_k - conj(o_{j-k}) u) becomes shat_k - conj(shat_{j-k}) u, and
+    // shat_0 stays 1 / E_0 (only F changes), u = F sum_k shat_k E_{j-k}
     bool invalid = false;
+    ff F = {1.f, 0.f};
     for (int j = 1; j < nw; ++j)
     {
         Dot ur, ui;
@@ -251,9 +257,9 @@ __global__ void __launch_bounds__(128) prepare_ff_kernel(int num_pixels, int m, 
                 ui.add(a.re, b.im);
                 ui.add(a.im, b.re);
             }
-        group_reduce(ur);
-        group_reduce(ui);
-        cff u = {ur.result(), ui.result()};
+        group_reduce<kGroup>(ur);
+        group_reduce<kGroup>(ui);
+        cff u = {ff_mul(F, ur.result()), ff_mul(F, ui.result())};
         Dot a2d;
         a2d.add(u.re, u.re);
         a2d.add(u.im, u.im);
@@ -265,8 +271,7 @@ __global__ void __launch_bounds__(128) prepare_ff_kernel(int num_pixels, int m, 
             invalid = true;
         }
         const ff f = ff_div({1.f, 0.f}, ff_add({1.f, 0.f}, ff_neg(a2)));
-        const ff s0 = sol[0].re;
-        // new_k = f (o_k - conj(o_{j-k}) u) for the pairs (k, j - k), 1 <= k <= j / 2
+        // pairs (k, j - k), 1 <= k <= j / 2: shat_k - conj(shat_{j-k}) u and shat_{j-k} - conj(shat_k) u
         for (int k = 1 + r; k <= j - k; k += kGroup)
         {
             const int kk = j - k;
@@ -278,7 +283,7 @@ __global__ void __launch_bounds__(128) prepare_ff_kernel(int num_pixels, int m, 
             vi.init(a.im);
             vi.sub(b.re, u.im);
             vi.add(b.im, u.re);
-            cff na = {ff_mul(f, vr.result()), ff_mul(f, vi.result())};
+            const cff na = {vr.fast_result(), vi.fast_result()};
             if (k != kk)
             {
                 Dot wr, wi;
@@ -288,18 +293,22 @@ __global__ void __launch_bounds__(128) prepare_ff_kernel(int num_pixels, int m, 
                 wi.init(b.im);
                 wi.sub(a.re, u.im);
                 wi.add(a.im, u.re);
-                sol[kk] = {ff_mul(f, wr.result()), ff_mul(f, wi.result())};
+                sol[kk] = {wr.fast_result(), wi.fast_result()};
             }
             sol[k] = na;
         }
         if (r == 0)
         {
-            const ff fs0 = ff_mul(f, s0);
-            sol[j] = {ff_neg(ff_mul(fs0, u.re)), ff_neg(ff_mul(fs0, u.im))};
-            sol[0] = {fs0, {0.f, 0.f}};
+            const ff s0 = sol[0].re;
+            sol[j] = {ff_neg(ff_mul(s0, u.re)), ff_neg(ff_mul(s0, u.im))};
         }
+        F = ff_mul(F, f);
         __syncwarp();
     }
+    // sol = F shat
+    for (int i = r; i < nw; i += kGroup)
+        sol[i] = {ff_mul(F, sol[i].re), ff_mul(F, sol[i].im)};
+    __syncwarp();
 
     // the tail in FP32 on the rounded values (lagrange_from_poly): P = 2 pi sol and the exponential moments with
     // E_0 halved, as float complex in the space of x; then the autocorrelation a_q and the correlation
@@ -345,11 +354,12 @@ template <int MAXM>
 cudaError_t launch_ff_m(int num_pixels, int m, const uint32_t *index, const float *data, float bias, float *out,
                         cudaStream_t stream)
 {
-    const int bytes = kPixPerBlock * FfLayout<MAXM>::floats_per_pixel * (int)sizeof(float);
+    constexpr int ppb = FfGroup<MAXM>::pixels;
+    const int bytes = ppb * FfLayout<MAXM>::floats_per_pixel * (int)sizeof(float);
     cudaError_t e = cudaFuncSetAttribute(prepare_ff_kernel<MAXM>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (e != cudaSuccess)
         return e;
-    prepare_ff_kernel<MAXM><<<(num_pixels + kPixPerBlock - 1) / kPixPerBlock, kPixPerBlock * kGroup, bytes, stream>>>(
+    prepare_ff_kernel<MAXM><<<(num_pixels + ppb - 1) / ppb, ppb * FfGroup<MAXM>::G, bytes, stream>>>(
         num_pixels, m, index, data, bias, out);
     return cudaGetLastError();
 }
