@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the differentiation-form, SPH and FP64-error sections")
     ap.add_argument("--sph-particles", type=int, default=16_000_000)
+    ap.add_argument("--section", default="all", choices=["all", "diff", "sph", "large"],
+                    help="diff / sph: run only that section and print its JSON (for profiling)")
     return ap.parse_args()
 
 
@@ -390,6 +392,7 @@ def run_ours(args):
     if rank == 0 and not args.no_extras:
         extras["differentiation_form"] = run_diff(args, local)
         extras["sph"] = run_sph(args, local)
+        extras["large"] = run_large(args, local)
         extras["errors_vs_fp64"] = precision_errors(args, local)
 
     if rank == 0:
@@ -629,6 +632,96 @@ def run_sph(args, local):
     return out
 
 
+def run_large(args, local):
+    """The large configuration (both forms): a 1024^3 float32 mixing layer (256 modes, built on the device), a
+    2048^2 perspective view, 64 moments, prediction coding with the default warp and 10-bit codes (table [16, 10 x
+    63]).  A step: generate -> compaction -> prediction encode + coding parameters -> quantize and pack the codes
+    -> unpack and dequantize -> Lagrange multipliers from the prediction-coded moments -> reconstruct; in the plain
+    FP32 form and in the float-float precision form.  Then the differentiation form (no compaction) with its
+    transfer-function adjoint."""
+    import torch
+
+    import mray_gb300 as M
+    from mray_gb300 import workloads as W
+
+    n, Wd, H, m = 1024, 2048, 2048, 64
+    P = Wd * H
+    gen, rec, cam, tf1d, tf_step = W.mixing_layer_setup(n, Wd, H, prediction_coding=True)
+    dmin, dmax = (0.0, 0.0, 0.0), (1.0, 1.0, 1.0)
+    ctx = M.Context(local)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    vol = W.mixing_layer_device(n, modes=256, seed=21)
+    torch.cuda.synchronize()
+    ctx.upload_grid(vol, dmin, dmax)
+    del vol
+    tf = M.preintegrate(tf1d, tf_step)
+    ctx.upload_tf(tf.table)
+    table = M.default_quantization_table(m, 10)
+    d_mo = torch.empty(P * m, device="cuda")
+    d_b = torch.empty(2 * P, dtype=torch.int16, device="cuda")
+    d_c = torch.empty(P, dtype=torch.int32, device="cuda")
+    d_idx = torch.empty(P + 1, dtype=torch.int32, device="cuda")
+    d_cm = torch.empty(P * m, device="cuda")
+    d_cp = torch.empty(2 * m, dtype=torch.int16, device="cuda")
+    d_codes = torch.empty(P * (16 + 10 * (m - 1)) // 8 + 64, dtype=torch.uint8, device="cuda")
+    d_pm = torch.empty(P * m, device="cuda")
+    d_rgba = torch.empty(P * 4, device="cuda")
+    sizes = {}
+
+    def fwd():
+        ctx.stage_generate_moments(cam, gen, Wd, H, m, d_mo, d_b, d_c)
+        total = ctx.stage_compact(Wd, H, m, d_c, d_mo, d_idx, d_cm)
+        ctx.stage_prediction_encode(Wd, H, m, d_idx, d_cm, total, 0, gen.bias, d_cp)
+        nbytes = ctx.stage_quantize_prediction_coding(Wd, H, m, d_idx, d_cm, table, d_codes)
+        ctx.stage_dequantize_prediction_coding(Wd, H, m, d_idx, table, d_codes, nbytes, d_cm)
+        ctx.stage_prepare_moments(Wd, H, m, d_idx, d_cm, d_pm, prediction_code=1, coding_warp=0, coding_params=d_cp,
+                                  bias=rec.bias)
+        ctx.stage_reconstruct(cam, rec, Wd, H, m, dmin, dmax, d_idx, d_pm, d_b, d_rgba)
+        sizes["moments"], sizes["code_bytes"] = total, nbytes
+
+    def timed(fn, steps):
+        for _ in range(args.warmup):
+            fn()
+        ctx.synchronize()
+        ev = _events(steps)
+        for e in ev:
+            e[0].record(stream)
+            fn()
+            e[1].record(stream)
+        ctx.synchronize()
+        return statistics.mean(e[0].elapsed_time(e[1]) for e in ev)
+
+    steps = max(1, min(args.steps, 3))
+    out = {"workload": f"mixing_layer{n}^3_{Wd}x{H}_m{m}_persp_prediction_coded_10bit",
+           "volume": "1024^3 float32 mixing layer, 256 modes, 5 % noise (built on the device with torch)"}
+    for name, prec in (("fwd_fp32", M.PRECISION_FP32), ("fwd_precision_form", M.PRECISION_COMPENSATED_FF_MESE)):
+        ctx.precision = prec
+        ms = timed(fwd, steps)
+        out[name] = {"value": P / (ms * 1e-3) / 1e6, "unit": UNIT, "ms": ms}
+    out["compact_moments"], out["code_bytes"] = int(sizes["moments"]), int(sizes["code_bytes"])
+    ctx.precision = M.PRECISION_FP32
+    del d_cm, d_codes
+    # the differentiation form with the transfer-function adjoint
+    gen.compact_image, gen.prediction_coding = 0, 0
+    b4 = torch.empty(P * 4, device="cuda")
+    rgba = torch.empty((H, Wd, 4), device="cuda")
+    tab = torch.from_numpy(tf.table).cuda()
+    gtab = torch.zeros((256, 4), device="cuda")
+
+    def fwd_bwd():
+        ctx.diff_forward(cam, gen, rec, Wd, H, m, tab, d_mo, b4, d_pm, rgba)
+        with torch.cuda.stream(stream):
+            g = 2.0 * rgba
+            gtab.zero_()
+        ctx.diff_backward(cam, gen, rec, Wd, H, m, tab, d_mo, b4, d_pm, rgba, g, gtab, None)
+
+    ms = timed(fwd_bwd, steps)
+    out["diff_fwd_tf_adjoint"] = {"value": P / (ms * 1e-3) / 1e6, "unit": UNIT, "ms": ms}
+    ctx.close()
+    return out
+
+
 def precision_errors(args, local):
     """Max and RMS errors of the moments, the transmittance and the RGBA of both arithmetic forms against the FP64
     oracle of the same method, on every 8th row of a 128 x 128 image of the default workload (its volume and
@@ -700,6 +793,13 @@ def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.section != "all":
+        import torch
+
+        _, _, local = dist_info()
+        torch.cuda.set_device(local)
+        fn = {"diff": run_diff, "sph": run_sph, "large": run_large}[args.section]
+        print(json.dumps({args.section: fn(args, local)}), flush=True)
     else:
         run_ours(args)
 

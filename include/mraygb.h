@@ -58,7 +58,8 @@ typedef enum mraygb_precision
     MRAYGB_PRECISION_COMPENSATED_FP64_MESE = 1,
     /* as COMPENSATED_FP64_MESE with the FP64 steps of the preparation (exponential moments, Levinson's
      * recursion) in float-float arithmetic (about 48 significant bits) and its correlation tail in FP32 on the
-     * rounded results; prediction-coded moments take the FP64 preparation.  No counterpart in the reference. */
+     * rounded results (prediction-coded moments: the decode recursion in float-float).  No counterpart in the
+     * reference. */
     MRAYGB_PRECISION_COMPENSATED_FF_MESE = 2
 } mraygb_precision;
 

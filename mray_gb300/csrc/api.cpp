@@ -251,8 +251,10 @@ int run_compact(mraygb_context *ctx, int width, int height, int m, const uint32_
 int run_prepare(mraygb_context *ctx, int width, int height, int m, const uint32_t *d_index, const float *d_data,
                 int prediction_code, int coding_warp, const uint16_t *d_coding_params, float bias, float *d_out)
 {
-    if (ctx->precision == MRAYGB_PRECISION_COMPENSATED_FF_MESE && !prediction_code)
-        CK(launch_prepare_ff(width * height, m, d_index, d_data, bias, d_out, ctx->stream), "prepare kernel launch");
+    if (ctx->precision == MRAYGB_PRECISION_COMPENSATED_FF_MESE)
+        CK(launch_prepare_ff(width * height, m, d_index, d_data, prediction_code, coding_warp, d_coding_params, bias,
+                             d_out, ctx->stream),
+           "prepare kernel launch");
     else
         CK(launch_prepare(width * height, m, d_index, d_data, prediction_code, coding_warp, d_coding_params, bias,
                           ctx->precision != MRAYGB_PRECISION_FP32, d_out, ctx->stream),

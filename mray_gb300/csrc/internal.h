@@ -58,10 +58,11 @@ cudaError_t mese_f64_init_constants();
 cudaError_t launch_prepare_f64(int num_pixels, int m, const uint32_t *index, const float *data, int prediction_code,
                                int coding_warp, const uint16_t *coding_params, float bias, float *pmoments,
                                cudaStream_t stream);
-// mese_ff.cu: the float-float preparation (standard coding)
+// mese_ff.cu: the float-float preparation
 cudaError_t mese_ff_init_constants();
-cudaError_t launch_prepare_ff(int num_pixels, int m, const uint32_t *index, const float *data, float bias,
-                              float *pmoments, cudaStream_t stream);
+cudaError_t launch_prepare_ff(int num_pixels, int m, const uint32_t *index, const float *data, int prediction_code,
+                              int coding_warp, const uint16_t *coding_params, float bias, float *pmoments,
+                              cudaStream_t stream);
 // Lagrange multipliers; fp64 selects the FP64 form
 cudaError_t launch_prepare(int num_pixels, int m, const uint32_t *index, const float *data, int prediction_code,
                            int coding_warp, const uint16_t *coding_params, float bias, bool fp64, float *pmoments,

@@ -165,12 +165,53 @@ template <int MAXM> struct FfLayout
     static constexpr int floats_per_pixel = MAXM * 10; // E, sol (4 floats per moment), x (2)
 };
 
-template <int MAXM>
+// the pair update of Levinson's recursion on the solution divided by prod_j f_j (see the kernel): for the pairs
+// (k, j - k), 1 <= k <= j / 2, shat_k - conj(shat_{j-k}) u and shat_{j-k} - conj(shat_k) u, split over the group
+template <int G> __device__ __forceinline__ void scaled_levinson_update(cff *sol, int j, int r, const cff &u)
+{
+    for (int k = 1 + r; k <= j - k; k += G)
+    {
+        const int kk = j - k;
+        const cff a = sol[k], b = sol[kk];
+        Dot vr, vi;
+        vr.init(a.re);
+        vr.sub(b.re, u.re);
+        vr.sub(b.im, u.im);
+        vi.init(a.im);
+        vi.sub(b.re, u.im);
+        vi.add(b.im, u.re);
+        const cff na = {vr.fast_result(), vi.fast_result()};
+        if (k != kk)
+        {
+            Dot wr, wi;
+            wr.init(b.re);
+            wr.sub(a.re, u.re);
+            wr.sub(a.im, u.im);
+            wi.init(b.im);
+            wi.sub(a.re, u.im);
+            wi.add(a.im, u.re);
+            sol[kk] = {wr.fast_result(), wi.fast_result()};
+        }
+        sol[k] = na;
+    }
+}
+
+// PC: prediction-coded input (prepare_moments_from_pred_coding, src/moment_preparation.h:32-53): the codes are
+// turned into reflection coefficients (transform_dequantization_real, src/moment_prediction_coding.h:97-118) and
+// decoded (decode, :163-208) into the exponential moments and the evaluation polynomial; otherwise standard
+// coding (prepare_moments_from_std_coding, :55-64).
+template <int MAXM, bool PC>
 __global__ void __launch_bounds__(128) prepare_ff_kernel(int num_pixels, int m, const uint32_t *__restrict__ index,
-                                                         const float *__restrict__ data, float bias,
+                                                         const float *__restrict__ data, float bias, int coding_warp,
+                                                         const uint16_t *__restrict__ coding_params,
                                                          float *__restrict__ out)
 {
     extern __shared__ __align__(16) float smem_ff[];
+    __shared__ float s_params[PC ? 2 * MAXM : 1];
+    if (PC && coding_warp == 0 && coding_params)
+        for (int i = threadIdx.x; i < 2 * (m - 1); i += blockDim.x)
+            s_params[i] = coding_params[i] / 65535.f; // CodingParamType::get_param1/2 (coding_params.h:52-54)
+    __syncthreads();
     const int lane = threadIdx.x & 31;
     constexpr int kGroup = FfGroup<MAXM>::G;
     const int r = lane & (kGroup - 1);
@@ -194,116 +235,167 @@ __global__ void __launch_bounds__(128) prepare_ff_kernel(int num_pixels, int m, 
         return;
     const float *in = data + idx;
 
-    // cut::lerp(m, target, bias) in pairs; x holds y_i = i x_i, the factors of the recurrence below
-    const ff omb = two_sum(1.f, -bias);
-    for (int i = r; i < nw; i += kGroup)
-        x[i] = ff_mul_f(ff_mul_f(omb, i < n ? in[i] : 0.f), (float)i);
-    if (r == 0)
-    {
-        const ff x0 = ff_add(ff_mul_f(omb, n > 0 ? in[0] : 0.f), {__fmul_rn(bias, 0.5f), 0.f});
-        const double phi = 3.141592653589793 * ((double)x0.hi + (double)x0.lo) - 1.5707963267948966;
-        double sp, cp;
-        sincos(phi, &sp, &cp);
-        E[0].re = ff_from_double(0.07957747154594767 * cp);
-        E[0].im = ff_from_double(0.07957747154594767 * sp);
-    }
-    __syncwarp();
-
-    // exponential moments: E_l = (2 pi i / l) sum_{j<l} y_{l-j} E_j
-    for (int l = 1; l < nw; ++l)
-    {
-        Dot ar, ai;
-        for (int j = r; j < l; j += kGroup)
-        {
-            const ff sc = x[l - j];
-            const cff e = E[j];
-            ar.add(sc, e.re);
-            ai.add(sc, e.im);
-        }
-        group_reduce<kGroup>(ar);
-        group_reduce<kGroup>(ai);
-        if (r == 0)
-        {
-            const float2 w2 = c_two_pi_over_l_ff[l];
-            const ff w = {w2.x, w2.y};
-            E[l].re = ff_neg(ff_mul(w, ai.result()));
-            E[l].im = ff_mul(w, ar.result());
-        }
-        __syncwarp();
-    }
-    if (r == 0)
-    {
-        E[0].re = {2.f * E[0].re.hi, 2.f * E[0].re.lo};
-        E[0].im = {2.f * E[0].im.hi, 2.f * E[0].im.lo};
-        sol[0].re = ff_div({1.f, 0.f}, E[0].re);
-        sol[0].im = {0.f, 0.f};
-    }
-    __syncwarp();
-
-    // Levinson's recursion with the invalid latch, on the solution divided by F = prod_j f_j: with
-    // sol = F shat the update new_k = f (o_k - conj(o_{j-k}) u) becomes shat_k - conj(shat_{j-k}) u, and
-    // shat_0 stays 1 / E_0 (only F changes), u = F sum_k shat_k E_{j-k}
     bool invalid = false;
     ff F = {1.f, 0.f};
-    for (int j = 1; j < nw; ++j)
+    if (!PC)
     {
-        Dot ur, ui;
-        if (!invalid)
-            for (int k = r; k < j; k += kGroup)
-            {
-                const cff a = sol[k], b = E[j - k];
-                ur.add(a.re, b.re);
-                ur.sub(a.im, b.im);
-                ui.add(a.re, b.im);
-                ui.add(a.im, b.re);
-            }
-        group_reduce<kGroup>(ur);
-        group_reduce<kGroup>(ui);
-        cff u = {ff_mul(F, ur.result()), ff_mul(F, ui.result())};
-        Dot a2d;
-        a2d.add(u.re, u.re);
-        a2d.add(u.im, u.im);
-        ff a2 = a2d.result();
-        if (invalid || a2.hi >= 1.f)
+        // cut::lerp(m, target, bias) in pairs; x holds y_i = i x_i, the factors of the recurrence below
+        const ff omb = two_sum(1.f, -bias);
+        for (int i = r; i < nw; i += kGroup)
+            x[i] = ff_mul_f(ff_mul_f(omb, i < n ? in[i] : 0.f), (float)i);
+        if (r == 0)
         {
-            u = {{0.f, 0.f}, {0.f, 0.f}};
-            a2 = {0.f, 0.f};
-            invalid = true;
+            const ff x0 = ff_add(ff_mul_f(omb, n > 0 ? in[0] : 0.f), {__fmul_rn(bias, 0.5f), 0.f});
+            const double phi = 3.141592653589793 * ((double)x0.hi + (double)x0.lo) - 1.5707963267948966;
+            double sp, cp;
+            sincos(phi, &sp, &cp);
+            E[0].re = ff_from_double(0.07957747154594767 * cp);
+            E[0].im = ff_from_double(0.07957747154594767 * sp);
         }
-        const ff f = ff_div({1.f, 0.f}, ff_add({1.f, 0.f}, ff_neg(a2)));
-        // pairs (k, j - k), 1 <= k <= j / 2: shat_k - conj(shat_{j-k}) u and shat_{j-k} - conj(shat_k) u
-        for (int k = 1 + r; k <= j - k; k += kGroup)
+        __syncwarp();
+
+        // exponential moments: E_l = (2 pi i / l) sum_{j<l} y_{l-j} E_j
+        for (int l = 1; l < nw; ++l)
         {
-            const int kk = j - k;
-            const cff a = sol[k], b = sol[kk];
-            Dot vr, vi;
-            vr.init(a.re);
-            vr.sub(b.re, u.re);
-            vr.sub(b.im, u.im);
-            vi.init(a.im);
-            vi.sub(b.re, u.im);
-            vi.add(b.im, u.re);
-            const cff na = {vr.fast_result(), vi.fast_result()};
-            if (k != kk)
+            Dot ar, ai;
+            for (int j = r; j < l; j += kGroup)
             {
-                Dot wr, wi;
-                wr.init(b.re);
-                wr.sub(a.re, u.re);
-                wr.sub(a.im, u.im);
-                wi.init(b.im);
-                wi.sub(a.re, u.im);
-                wi.add(a.im, u.re);
-                sol[kk] = {wr.fast_result(), wi.fast_result()};
+                const ff sc = x[l - j];
+                const cff e = E[j];
+                ar.add(sc, e.re);
+                ai.add(sc, e.im);
             }
-            sol[k] = na;
+            group_reduce<kGroup>(ar);
+            group_reduce<kGroup>(ai);
+            if (r == 0)
+            {
+                const float2 w2 = c_two_pi_over_l_ff[l];
+                const ff w = {w2.x, w2.y};
+                E[l].re = ff_neg(ff_mul(w, ai.result()));
+                E[l].im = ff_mul(w, ar.result());
+            }
+            __syncwarp();
         }
         if (r == 0)
         {
-            const ff s0 = sol[0].re;
-            sol[j] = {ff_neg(ff_mul(s0, u.re)), ff_neg(ff_mul(s0, u.im))};
+            E[0].re = {2.f * E[0].re.hi, 2.f * E[0].re.lo};
+            E[0].im = {2.f * E[0].im.hi, 2.f * E[0].im.lo};
+            sol[0].re = ff_div({1.f, 0.f}, E[0].re);
+            sol[0].im = {0.f, 0.f};
         }
-        F = ff_mul(F, f);
         __syncwarp();
+
+        // Levinson's recursion with the invalid latch, on the solution divided by F = prod_j f_j: with
+        // sol = F shat the update new_k = f (o_k - conj(o_{j-k}) u) becomes shat_k - conj(shat_{j-k}) u, and
+        // shat_0 stays 1 / E_0 (only F changes), u = F sum_k shat_k E_{j-k}
+        for (int j = 1; j < nw; ++j)
+        {
+            Dot ur, ui;
+            if (!invalid)
+                for (int k = r; k < j; k += kGroup)
+                {
+                    const cff a = sol[k], b = E[j - k];
+                    ur.add(a.re, b.re);
+                    ur.sub(a.im, b.im);
+                    ui.add(a.re, b.im);
+                    ui.add(a.im, b.re);
+                }
+            group_reduce<kGroup>(ur);
+            group_reduce<kGroup>(ui);
+            cff u = {ff_mul(F, ur.result()), ff_mul(F, ui.result())};
+            Dot a2d;
+            a2d.add(u.re, u.re);
+            a2d.add(u.im, u.im);
+            ff a2 = a2d.result();
+            if (invalid || a2.hi >= 1.f)
+            {
+                u = {{0.f, 0.f}, {0.f, 0.f}};
+                a2 = {0.f, 0.f};
+                invalid = true;
+            }
+            scaled_levinson_update<kGroup>(sol, j, r, u);
+            if (r == 0)
+            {
+                const ff s0 = sol[0].re;
+                sol[j] = {ff_neg(ff_mul(s0, u.re)), ff_neg(ff_mul(s0, u.im))};
+            }
+            F = ff_div(F, ff_add({1.f, 0.f}, ff_neg(a2)));
+            __syncwarp();
+        }
+    }
+    else
+    {
+        // transform_dequantization_real: code_0 = 2 e^{i (pi c_0 - pi/2)} / (4 pi), code_l = w_l axis / |axis| with
+        // axis = i code_0 and w_l the inverse warp of the input; x holds w_l, the factor is formed per use
+        double cp, sp;
+        sincos(3.141592653589793 * (double)(n > 0 ? in[0] : 0.f) - 1.5707963267948966, &sp, &cp);
+        const ff fre = ff_from_double(-sp), fim = ff_from_double(cp); // axis / |axis| = i e^{i phi}
+        for (int i = 1 + r; i < nw; i += kGroup)
+        {
+            const float c = i < n ? in[i] : 0.f;
+            ff w;
+            if (coding_warp == 0)
+            {
+                // prediction_coding_inv_warp: c p1 2 - p0
+                const ff cp1 = ff_mul_f({c, 0.f}, s_params[(i - 1) * 2 + 1]);
+                w = ff_add({2.f * cp1.hi, 2.f * cp1.lo}, {-s_params[(i - 1) * 2], 0.f});
+            }
+            else
+            {
+                w = two_sum(2.f * c, -1.f);
+            }
+            x[i] = w;
+        }
+        if (r == 0)
+        {
+            E[0].re = ff_from_double(0.15915494309189535 * cp);
+            E[0].im = ff_from_double(0.15915494309189535 * sp);
+            sol[0].re = ff_div({1.f, 0.f}, E[0].re);
+            sol[0].im = {0.f, 0.f};
+        }
+        __syncwarp();
+        // decode: u_l = code_l (latched once |u|^2 >= 1 - 1e-6), E_l = (u_l - sum_{k=1}^{l-1} poly_k E_{l-k}) / poly_0,
+        // then the Levinson update with u_l; poly = F shat as above
+        const ff p0 = sol[0].re;
+        for (int l = 1; l < nw; ++l)
+        {
+            Dot gr, gi;
+            for (int k = 1 + r; k < l; k += kGroup)
+            {
+                const cff a = sol[k], b = E[l - k];
+                gr.add(a.re, b.re);
+                gr.sub(a.im, b.im);
+                gi.add(a.re, b.im);
+                gi.add(a.im, b.re);
+            }
+            group_reduce<kGroup>(gr);
+            group_reduce<kGroup>(gi);
+            const ff w = x[l];
+            cff u = {ff_mul(w, fre), ff_mul(w, fim)};
+            Dot a2d;
+            a2d.add(u.re, u.re);
+            a2d.add(u.im, u.im);
+            ff a2 = a2d.result();
+            if (invalid || a2.hi >= 1.f - 1e-6f)
+            {
+                u = {{0.f, 0.f}, {0.f, 0.f}};
+                a2 = {0.f, 0.f};
+                invalid = true;
+            }
+            if (r == 0)
+            {
+                // (u - F gamma_hat) / (F p0)
+                const ff fp0 = ff_mul(F, p0);
+                const ff er = ff_add(u.re, ff_neg(ff_mul(F, gr.result())));
+                const ff ei = ff_add(u.im, ff_neg(ff_mul(F, gi.result())));
+                E[l] = {ff_div(er, fp0), ff_div(ei, fp0)};
+            }
+            scaled_levinson_update<kGroup>(sol, l, r, u);
+            if (r == 0)
+                sol[l] = {ff_neg(ff_mul(p0, u.re)), ff_neg(ff_mul(p0, u.im))};
+            F = ff_div(F, ff_add({1.f, 0.f}, ff_neg(a2)));
+            __syncwarp();
+        }
     }
     // sol = F shat
     for (int i = r; i < nw; i += kGroup)
@@ -350,18 +442,28 @@ __global__ void __launch_bounds__(128) prepare_ff_kernel(int num_pixels, int m, 
     }
 }
 
-template <int MAXM>
-cudaError_t launch_ff_m(int num_pixels, int m, const uint32_t *index, const float *data, float bias, float *out,
-                        cudaStream_t stream)
+template <int MAXM, bool PC>
+cudaError_t launch_ff_pc(int num_pixels, int m, const uint32_t *index, const float *data, float bias, int warp,
+                         const uint16_t *cp, float *out, cudaStream_t stream)
 {
     constexpr int ppb = FfGroup<MAXM>::pixels;
     const int bytes = ppb * FfLayout<MAXM>::floats_per_pixel * (int)sizeof(float);
-    cudaError_t e = cudaFuncSetAttribute(prepare_ff_kernel<MAXM>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaError_t e =
+        cudaFuncSetAttribute(prepare_ff_kernel<MAXM, PC>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (e != cudaSuccess)
         return e;
-    prepare_ff_kernel<MAXM><<<(num_pixels + ppb - 1) / ppb, ppb * FfGroup<MAXM>::G, bytes, stream>>>(
-        num_pixels, m, index, data, bias, out);
+    prepare_ff_kernel<MAXM, PC><<<(num_pixels + ppb - 1) / ppb, ppb * FfGroup<MAXM>::G, bytes, stream>>>(
+        num_pixels, m, index, data, bias, warp, cp, out);
     return cudaGetLastError();
+}
+
+template <int MAXM>
+cudaError_t launch_ff_m(int num_pixels, int m, const uint32_t *index, const float *data, int pc, int warp,
+                        const uint16_t *cp, float bias, float *out, cudaStream_t stream)
+{
+    if (pc)
+        return launch_ff_pc<MAXM, true>(num_pixels, m, index, data, bias, warp, cp, out, stream);
+    return launch_ff_pc<MAXM, false>(num_pixels, m, index, data, bias, warp, cp, out, stream);
 }
 
 } // namespace
@@ -379,18 +481,20 @@ cudaError_t mese_ff_init_constants()
     return cudaMemcpyToSymbol(c_two_pi_over_l_ff, t, sizeof(t));
 }
 
-cudaError_t launch_prepare_ff(int num_pixels, int m, const uint32_t *index, const float *data, float bias,
-                              float *pmoments, cudaStream_t stream)
+cudaError_t launch_prepare_ff(int num_pixels, int m, const uint32_t *index, const float *data, int prediction_code,
+                              int coding_warp, const uint16_t *coding_params, float bias, float *pmoments,
+                              cudaStream_t stream)
 {
+    const int pc = prediction_code ? 1 : 0;
     if (m <= 16)
-        return launch_ff_m<16>(num_pixels, m, index, data, bias, pmoments, stream);
+        return launch_ff_m<16>(num_pixels, m, index, data, pc, coding_warp, coding_params, bias, pmoments, stream);
     if (m <= 32)
-        return launch_ff_m<32>(num_pixels, m, index, data, bias, pmoments, stream);
+        return launch_ff_m<32>(num_pixels, m, index, data, pc, coding_warp, coding_params, bias, pmoments, stream);
     if (m <= 64)
-        return launch_ff_m<64>(num_pixels, m, index, data, bias, pmoments, stream);
+        return launch_ff_m<64>(num_pixels, m, index, data, pc, coding_warp, coding_params, bias, pmoments, stream);
     if (m <= 128)
-        return launch_ff_m<128>(num_pixels, m, index, data, bias, pmoments, stream);
-    return launch_ff_m<256>(num_pixels, m, index, data, bias, pmoments, stream);
+        return launch_ff_m<128>(num_pixels, m, index, data, pc, coding_warp, coding_params, bias, pmoments, stream);
+    return launch_ff_m<256>(num_pixels, m, index, data, pc, coding_warp, coding_params, bias, pmoments, stream);
 }
 
 } // namespace mraygb

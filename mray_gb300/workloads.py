@@ -158,10 +158,41 @@ def ml_workload(n: int = 64, width: int = 512, height: int = 512, num_moments: i
                     ortho_camera(seed), gen, rec, transfer_function(seed + 1), tf_step=0.05)
 
 
-def mixing_layer_workload(n: int = 512, width: int = 1024, height: int = 1024, num_moments: int = 64,
-                          modes: int = 64, seed: int = 21, prediction_coding: bool = False,
-                          name: str | None = None) -> Workload:
-    """Mixing layer n^3 on [0,1]^3, perspective view, 0.5-voxel steps."""
+def mixing_layer_device(n: int, modes: int = 64, seed: int = 1, noise: float = 0.05, z0: float = 0.5,
+                        amplitude: float = 0.08, width: float = 0.02, device: str = "cuda"):
+    """The mixing-layer field of :func:`mixing_layer` built on the GPU with torch (for volumes too large to build
+    on the host quickly, e.g. 1024^3): the same modes and formula; the 5 % noise comes from torch's seeded
+    generator, so the values differ from the host version's while the distribution is the same."""
+    import torch
+
+    rng = np.random.default_rng(seed)
+    k = rng.uniform(1.0, 32.0, size=modes)
+    theta = rng.uniform(0.0, 2.0 * np.pi, size=modes)
+    phase = rng.uniform(0.0, 2.0 * np.pi, size=modes)
+    amp = k ** (-5.0 / 3.0)
+    amp *= amplitude / np.sqrt(np.sum(amp * amp) / 2.0)
+    c = torch.arange(n, dtype=torch.float64, device=device) / n
+    yy, xx = torch.meshgrid(c, c, indexing="ij")  # [y, x]
+    h = torch.zeros((n, n), dtype=torch.float64, device=device)
+    for i in range(modes):
+        kx, ky = float(k[i] * np.cos(theta[i])), float(k[i] * np.sin(theta[i]))
+        h += float(amp[i]) * torch.cos(2.0 * np.pi * (kx * xx + ky * yy) + float(phase[i]))
+    h32 = h.float()
+    zc = c.float()
+    out = torch.empty((n, n, n), dtype=torch.float32, device=device)
+    gen = torch.Generator(device=device)
+    gen.manual_seed(seed + 1000003)
+    for iz in range(n):
+        sl = out[iz]
+        torch.tanh((zc[iz] - z0 - h32) * (1.0 / width), out=sl)
+        sl.add_(1.0).mul_(0.5)
+        if noise > 0.0:
+            sl.add_(noise * torch.randn((n, n), generator=gen, device=device, dtype=torch.float32))
+    return out
+
+
+def mixing_layer_setup(n: int, width: int, height: int, prediction_coding: bool = False, seed: int = 21):
+    """The view and parameters of the mixing-layer workloads: (gen, rec, camera, tf1d, tf_step)."""
     step = 0.5 / n
     gen = GenerationParameters(step_size=step, error_threshold=0.0, bias=5e-5, compact_image=1,
                                prediction_coding=1 if prediction_coding else 0, transform_to_bounds=1,
@@ -169,9 +200,17 @@ def mixing_layer_workload(n: int = 512, width: int = 1024, height: int = 1024, n
                                coding_warp=0)
     rec = ReconstructionParameters(step_size=step, bias=5e-5, medium_emission=1.0, early_ray_termination=0.99)
     cam = perspective_camera(eye=(1.9, -1.1, 1.45), target=(0.5, 0.5, 0.5), fov_deg=38.0, aspect=width / height)
+    return gen, rec, cam, transfer_function(seed + 1), 0.05 * (512.0 / n)
+
+
+def mixing_layer_workload(n: int = 512, width: int = 1024, height: int = 1024, num_moments: int = 64,
+                          modes: int = 64, seed: int = 21, prediction_coding: bool = False,
+                          name: str | None = None) -> Workload:
+    """Mixing layer n^3 on [0,1]^3, perspective view, 0.5-voxel steps."""
+    gen, rec, cam, tf1d, tf_step = mixing_layer_setup(n, width, height, prediction_coding, seed)
     name = name or f"mixing_layer{n}_{width}x{height}_m{num_moments}_persp"
     return Workload(name, mixing_layer(n, modes=modes, seed=seed), (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), width,
-                    height, num_moments, cam, gen, rec, transfer_function(seed + 1), tf_step=0.05 * (512.0 / n))
+                    height, num_moments, cam, gen, rec, tf1d, tf_step=tf_step)
 
 
 def diff_workload(n: int = 256, width: int = 512, height: int = 512, num_moments: int = 31, seed: int = 11,

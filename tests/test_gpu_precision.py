@@ -29,30 +29,36 @@ CASES = [("ml", 31), ("mix", 64)]
 
 
 @pytest.mark.parametrize("form", ["fp64", "ff"])
+@pytest.mark.parametrize("pc", [0, 1], ids=["std", "prediction_coded"])
 @pytest.mark.parametrize("kind,m", CASES)
-def test_precision_prepare_matches_fp64_oracle(gpu_context, form, kind, m):
+def test_precision_prepare_matches_fp64_oracle(gpu_context, form, pc, kind, m):
     import mray_gb300 as M
 
     wl = small_ml(64, 56, m) if kind == "ml" else small_mixing(48, 40, m, 96)
+    wl.gen.prediction_coding = pc
     mi = O.workload_generate(wl, "f32")
     W, H = wl.width, wl.height
     d_idx = _dev(mi["index"].view(np.int32))
     d_data = _dev(mi["data"])
     d_pm = torch.zeros_like(d_data)
+    cp = mi["coding_params"]
+    d_cp = _dev(cp.view(np.int16)) if cp is not None else None
     gpu_context.precision = (M.PRECISION_COMPENSATED_FP64_MESE if form == "fp64"
                              else M.PRECISION_COMPENSATED_FF_MESE)
-    gpu_context.stage_prepare_moments(W, H, m, d_idx, d_data, d_pm, bias=wl.rec.bias)
+    gpu_context.stage_prepare_moments(W, H, m, d_idx, d_data, d_pm, prediction_code=pc, coding_warp=0,
+                                      coding_params=d_cp, bias=wl.rec.bias)
     gpu_context.synchronize()
     gpu_context.precision = M.PRECISION_FP32
     pm = d_pm.cpu().numpy().astype(np.float64)
-    pm64 = O.prepare_moments(W, H, m, mi["index"], mi["data"], bias=wl.rec.bias, precision="f64")
+    pm64 = O.prepare_moments(W, H, m, mi["index"], mi["data"], bool(pc), 0, cp, wl.rec.bias, "f64")
     err = _lambda_err(pm, pm64, mi["index"])
     # FP64: the same arithmetic up to contraction and the sincos of the first exponential moment; float-float:
     # 48-bit steps, then the FP32 tail (about 1e-7 of the largest multiplier) and the float result
     tol = 1e-6 if form == "fp64" else 2e-5
     assert np.quantile(err, 0.99) <= tol / 4 and err.max() <= tol, f"p99 {np.quantile(err, .99):.2e} max {err.max():.2e}"
     # the FP32 preparation, for scale: the precision forms are far closer to FP64
-    gpu_context.stage_prepare_moments(W, H, m, d_idx, d_data, d_pm, bias=wl.rec.bias)
+    gpu_context.stage_prepare_moments(W, H, m, d_idx, d_data, d_pm, prediction_code=pc, coding_warp=0,
+                                      coding_params=d_cp, bias=wl.rec.bias)
     gpu_context.synchronize()
     err32 = _lambda_err(d_pm.cpu().numpy().astype(np.float64), pm64, mi["index"])
     assert np.median(err) < np.median(err32)
