@@ -70,7 +70,9 @@ struct mraygb_context
         GRID,
         PARTICLES
     } volume = NONE;
-    DeviceBuffer grid;
+    // the grid as a 3D array behind a point-sampled texture (hardware clamp to edge, 3D-blocked layout)
+    cudaArray_t grid_array = nullptr;
+    cudaTextureObject_t grid_tex = 0;
     int nx = 0, ny = 0, nz = 0;
     float dmin[3] = {0, 0, 0}, dmax[3] = {0, 0, 0};
     DeviceBuffer particle_pts, particle_cells;
@@ -144,7 +146,7 @@ int check_image(mraygb_context *ctx, int width, int height, int m)
 GridView grid_view(const mraygb_context *ctx)
 {
     GridView g;
-    g.data = ctx->grid.as<float>();
+    g.tex = ctx->grid_tex;
     g.nx = ctx->nx;
     g.ny = ctx->ny;
     g.nz = ctx->nz;
@@ -169,6 +171,17 @@ ParticleView particle_view(const mraygb_context *ctx)
         v.dmax[i] = ctx->dmax[i];
     }
     return v;
+}
+
+void release_grid(mraygb_context *ctx)
+{
+    if (ctx->grid_tex)
+        cudaDestroyTextureObject(ctx->grid_tex);
+    if (ctx->grid_array)
+        cudaFreeArray(ctx->grid_array);
+    ctx->grid_tex = 0;
+    ctx->grid_array = nullptr;
+    ctx->nx = ctx->ny = ctx->nz = 0;
 }
 
 int check_device_error_flag(mraygb_context *ctx)
@@ -456,7 +469,8 @@ void mraygb_destroy(mraygb_context *ctx)
     cudaSetDevice(ctx->device);
     if (ctx->stream)
         cudaStreamSynchronize(ctx->stream);
-    DeviceBuffer *bufs[] = {&ctx->grid,    &ctx->particle_pts, &ctx->particle_cells,
+    release_grid(ctx);
+    DeviceBuffer *bufs[] = {&ctx->particle_pts, &ctx->particle_cells,
                             &ctx->tf,       &ctx->moments,       &ctx->counts,
                             &ctx->index,   &ctx->compact,  &ctx->bounds,        &ctx->coding_params,
                             &ctx->pmoments, &ctx->rgba,    &ctx->rgba8,         &ctx->scan_scratch,
@@ -511,11 +525,38 @@ int mraygb_upload_grid(mraygb_context *ctx, const float *data, int nx, int ny, i
     for (int i = 0; i < 3; ++i)
         if (!(dmax[i] > dmin[i]))
             return fail(ctx, MRAYGB_INVALID_ARGUMENT, "empty domain along axis %d", i);
-    const size_t bytes = (size_t)nx * ny * nz * sizeof(float);
-    CK(ctx->grid.reserve(bytes), "grid allocation");
-    CK(cudaMemcpyAsync(ctx->grid.ptr, data, bytes, data_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
-                       ctx->stream),
-       "grid upload");
+    int max3d[3] = {0, 0, 0};
+    cudaDeviceGetAttribute(&max3d[0], cudaDevAttrMaxTexture3DWidth, ctx->device);
+    cudaDeviceGetAttribute(&max3d[1], cudaDevAttrMaxTexture3DHeight, ctx->device);
+    cudaDeviceGetAttribute(&max3d[2], cudaDevAttrMaxTexture3DDepth, ctx->device);
+    if (nx > max3d[0] || ny > max3d[1] || nz > max3d[2])
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "grid %d x %d x %d exceeds the 3D texture limits %d x %d x %d", nx, ny,
+                    nz, max3d[0], max3d[1], max3d[2]);
+    // same dimensions: the array is reused
+    if (!(ctx->grid_array && ctx->nx == nx && ctx->ny == ny && ctx->nz == nz))
+    {
+        release_grid(ctx);
+        const cudaChannelFormatDesc desc = cudaCreateChannelDesc<float>();
+        CK(cudaMalloc3DArray(&ctx->grid_array, &desc, make_cudaExtent(nx, ny, nz)), "grid allocation");
+        cudaResourceDesc res;
+        std::memset(&res, 0, sizeof(res));
+        res.resType = cudaResourceTypeArray;
+        res.res.array.array = ctx->grid_array;
+        cudaTextureDesc td;
+        std::memset(&td, 0, sizeof(td));
+        td.addressMode[0] = td.addressMode[1] = td.addressMode[2] = cudaAddressModeClamp;
+        td.filterMode = cudaFilterModePoint;
+        td.readMode = cudaReadModeElementType;
+        td.normalizedCoords = 0;
+        CK(cudaCreateTextureObject(&ctx->grid_tex, &res, &td, nullptr), "grid texture");
+    }
+    cudaMemcpy3DParms cp;
+    std::memset(&cp, 0, sizeof(cp));
+    cp.srcPtr = make_cudaPitchedPtr(const_cast<float *>(data), (size_t)nx * sizeof(float), nx, ny);
+    cp.dstArray = ctx->grid_array;
+    cp.extent = make_cudaExtent(nx, ny, nz);
+    cp.kind = data_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    CK(cudaMemcpy3DAsync(&cp, ctx->stream), "grid upload");
     ctx->nx = nx;
     ctx->ny = ny;
     ctx->nz = nz;
@@ -640,7 +681,7 @@ int mraygb_upload_particles(mraygb_context *ctx, const float *x, const float *y,
         ctx->dmax[i] = dmax[i];
     }
     ctx->volume = mraygb_context::PARTICLES;
-    ctx->grid.release();
+    release_grid(ctx);
     return MRAYGB_OK;
 }
 

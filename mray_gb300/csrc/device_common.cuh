@@ -52,7 +52,7 @@ inline DeviceCamera to_device_camera(const mraygb_camera &c)
 
 struct GridView
 {
-    const float *data;
+    cudaTextureObject_t tex; // the voxels in a 3D array: point sampling, unnormalized coordinates, clamp to edge
     int nx, ny, nz;
     float dmin[3];
     float ext[3]; // dmax - dmin, rounded as the reference rounds it
@@ -124,12 +124,11 @@ __device__ __forceinline__ bool intersect_aabb(const float o[3], const float d[3
     return smallest_tmax > largest_tmin;
 }
 
-__device__ __forceinline__ float grid_get(const GridView &g, int x, int y, int z)
+// voxel (floor(x), floor(y), floor(z)) of the 3D texture, clamped to the grid (RegularGrid::get's clamp,
+// src/volume.h:89-95): the coordinates passed are integer + 1/2
+__device__ __forceinline__ float grid_get(const GridView &g, float x, float y, float z)
 {
-    x = x < 0 ? 0 : (x > g.nx - 1 ? g.nx - 1 : x);
-    y = y < 0 ? 0 : (y > g.ny - 1 ? g.ny - 1 : y);
-    z = z < 0 ? 0 : (z > g.nz - 1 ? g.nz - 1 : z);
-    return __ldg(g.data + ((size_t)z * (size_t)(g.ny * g.nx) + (size_t)(y * g.nx) + (size_t)x));
+    return tex3D<float>(g.tex, x, y, z);
 }
 
 // Corner-aligned trilinear sample with clamp-to-edge, summed in the reference's order.
@@ -137,26 +136,26 @@ __device__ __forceinline__ float grid_sample(const GridView &g, float px, float 
 {
     const float p[3] = {px, py, pz};
     const int sz[3] = {g.nx, g.ny, g.nz};
-    float a[3];
-    int il[3];
+    float a[3], fl[3];
 #pragma unroll
     for (int i = 0; i < 3; ++i)
     {
         float np = __fdiv_rn(__fsub_rn(p[i], g.dmin[i]), g.ext[i]);
         float ip = __fmul_rn(np, (float)sz[i]);
-        float fl = floorf(ip);
-        a[i] = __fsub_rn(ip, fl);
-        il[i] = (int)fl;
+        fl[i] = floorf(ip);
+        a[i] = __fsub_rn(ip, fl[i]);
     }
-    const int xl = il[0], yl = il[1], zl = il[2];
+    // texel centres of the lower and upper corners (the clamp is the texture's address mode)
+    const float xl = __fadd_rn(fl[0], 0.5f), yl = __fadd_rn(fl[1], 0.5f), zl = __fadd_rn(fl[2], 0.5f);
+    const float xr = __fadd_rn(fl[0], 1.5f), yr = __fadd_rn(fl[1], 1.5f), zr = __fadd_rn(fl[2], 1.5f);
     const float lll = grid_get(g, xl, yl, zl);
-    const float lrl = grid_get(g, xl, yl + 1, zl);
-    const float rrl = grid_get(g, xl + 1, yl + 1, zl);
-    const float rll = grid_get(g, xl + 1, yl, zl);
-    const float llr = grid_get(g, xl, yl, zl + 1);
-    const float lrr = grid_get(g, xl, yl + 1, zl + 1);
-    const float rrr = grid_get(g, xl + 1, yl + 1, zl + 1);
-    const float rlr = grid_get(g, xl + 1, yl, zl + 1);
+    const float lrl = grid_get(g, xl, yr, zl);
+    const float rrl = grid_get(g, xr, yr, zl);
+    const float rll = grid_get(g, xr, yl, zl);
+    const float llr = grid_get(g, xl, yl, zr);
+    const float lrr = grid_get(g, xl, yr, zr);
+    const float rrr = grid_get(g, xr, yr, zr);
+    const float rlr = grid_get(g, xr, yl, zr);
     const float ax = a[0], ay = a[1], az = a[2];
     const float bx = __fsub_rn(1.f, ax), by = __fsub_rn(1.f, ay), bz = __fsub_rn(1.f, az);
     float s = __fmul_rn(__fmul_rn(__fmul_rn(bx, by), bz), lll);
