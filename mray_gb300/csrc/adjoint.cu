@@ -94,9 +94,9 @@ struct TfGradCache
 // The transfer-function gradient of a block is accumulated in kTfCopies copies of the 256-entry table in shared
 // memory, lane l adding to copy l mod kTfCopies: neighbouring rays sample similar densities at the same step, and
 // shared-memory atomics on one address from many lanes of a warp serialize.
-constexpr int kTfCopies = 16;
+constexpr int kTfCopies = 8;
 
-template <int MAXM> __global__ void __launch_bounds__(128, 3) reconstruct_adjoint_kernel(const ReconAdjDev a)
+template <int MAXM> __global__ void __launch_bounds__(128, 4) reconstruct_adjoint_kernel(const ReconAdjDev a)
 {
     __shared__ float4 s_tf[256];
     extern __shared__ float4 s_gall[]; // kTfCopies * 256 (dynamic: above the 48 KiB of static shared memory)
@@ -265,114 +265,68 @@ __device__ __forceinline__ float abs2(C2 a) { return a.x * a.x + a.y * a.y; }
 // Complex adjoints are carried as d L / d re + i d L / d im.  For w = a b: a_bar += w_bar conj(b); for w = conj(c) u:
 // c_bar += conj(w_bar) u, u_bar += w_bar c.
 //
-// One pixel per group of 8 lanes with its arrays in shared memory (the thread-per-pixel form kept 2 KiB per thread
-// in local memory); every O(n^2) loop is split over the lanes by index (each step's sums combined by butterfly
-// shuffles), the recursions stay sequential in their step index.
-constexpr int kAdjGroup = 8;
-constexpr int kAdjPixels = 16; // 128 threads
-
-__device__ __forceinline__ float adj_group_sum(float v)
-{
-#pragma unroll
-    for (int o = 1; o < kAdjGroup; o <<= 1)
-        v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-
-// complex arrays E, sol, uu, A, gE, gP and real arrays x, gl, gx per pixel
-template <int MAXM> struct AdjLayout
-{
-    static constexpr int floats_per_pixel = MAXM * (6 * 2 + 3);
-};
-
+// One thread per pixel, the arrays (2 KiB at 32 moments) in local memory: measured faster (1.44 ms per 512^2 launch
+// at m = 31) than the same kernel with its arrays in shared memory, one lane per pixel (1.80 ms: fewer resident
+// threads) or one pixel per group of 8 lanes (1.93 ms: the per-step reductions and syncs of the sequential
+// recursions cost more than the split of their O(n) bodies saves).
 template <int MAXM>
-__global__ void __launch_bounds__(128) prepare_adjoint_kernel(int num_pixels, int m, const float *__restrict__ moments,
-                                                              float bias, const float *grad_lambda,
-                                                              float *grad_moments)
+__global__ void __launch_bounds__(64) prepare_adjoint_kernel(int num_pixels, int m, const float *__restrict__ moments,
+                                                             float bias, const float *grad_lambda,
+                                                             float *grad_moments)
 {
-    extern __shared__ __align__(16) float smem_adj[];
-    const int lane = threadIdx.x & 31;
-    const int r = lane & (kAdjGroup - 1);
-    const int slot = threadIdx.x / kAdjGroup;
-    const int pix = blockIdx.x * kAdjPixels + slot;
-    float *base = smem_adj + (size_t)slot * AdjLayout<MAXM>::floats_per_pixel;
-    C2 *E = reinterpret_cast<C2 *>(base);
-    C2 *sol = E + MAXM;
-    C2 *uu = sol + MAXM;
-    C2 *A = uu + MAXM;
-    C2 *gE = A + MAXM;
-    C2 *gP = gE + MAXM;
-    float *xm = reinterpret_cast<float *>(gP + MAXM);
-    float *gl = xm + MAXM;
-    float *gx = gl + MAXM;
-
-    const int n_own = pix < num_pixels ? (m < MAXM ? m : MAXM) : 0;
-    const size_t idx = (size_t)(pix < num_pixels ? pix : 0) * (size_t)m;
-    // a pixel whose multipliers get no gradient (a ray that misses the box) is skipped
-    bool any = false;
-    for (int k = r; k < n_own; k += kAdjGroup)
-        any |= grad_lambda[idx + k] != 0.f;
-    any = adj_group_sum(any ? 1.f : 0.f) > 0.f;
-    const int n = any ? n_own : 0;
-    if (!any)
-        for (int k = r; k < n_own; k += kAdjGroup)
-            grad_moments[idx + k] = 0.f;
-    const int nw = __reduce_max_sync(0xffffffffu, n);
-    if (nw == 0)
+    const int pix = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pix >= num_pixels)
         return;
+    const int n = m < MAXM ? m : MAXM;
+    const size_t idx = (size_t)pix * (size_t)m;
+    float gl[MAXM];
+    bool any = false;
+    for (int k = 0; k < n; ++k)
+    {
+        gl[k] = grad_lambda[idx + k];
+        any |= gl[k] != 0.f;
+    }
+    if (!any)
+    {
+        for (int k = 0; k < n; ++k)
+            grad_moments[idx + k] = 0.f;
+        return;
+    }
     constexpr float kPi = 3.14159265358979f;
     constexpr float kInv4Pi = 0.0795774715459477f;
-    constexpr float kTwoPi = 6.283185307179586f;
 
     // ---- forward, keeping what the reverse sweep needs ----
-    for (int i = r; i < nw; i += kAdjGroup)
-    {
-        const float v = i < n ? moments[idx + i] : 0.f;
-        xm[i] = (1.f - bias) * v + (i == 0 ? bias * 0.5f : 0.f);
-        gl[i] = i < n ? grad_lambda[idx + i] : 0.f;
-        gx[i] = 0.f;
-        gE[i] = c2(0.f, 0.f);
-        gP[i] = c2(0.f, 0.f);
-    }
-    __syncwarp();
-    const float phi = kPi * xm[0] - 0.5f * kPi;
-    float sphi, cphi;
-    sincosf(phi, &sphi, &cphi);
-    if (r == 0)
-        E[0] = c2(kInv4Pi * cphi, kInv4Pi * sphi);
-    __syncwarp();
-    // trigonometricToExponentialMoments (E[0] un-doubled inside the recurrence)
-    for (int l = 1; l < nw; ++l)
-    {
-        C2 acc = c2(0.f, 0.f);
-        for (int j = r; j < l; j += kAdjGroup)
-            acc = acc + (float(l - j) * xm[l - j]) * E[j];
-        acc = c2(adj_group_sum(acc.x), adj_group_sum(acc.y));
-        if (r == 0)
-        {
-            const float w = (float)(6.283185307179586 / (double)l);
-            E[l] = c2(-w * acc.y, w * acc.x);
-        }
-        __syncwarp();
-    }
-    if (r == 0)
-    {
-        E[0] = 2.f * E[0];
-        sol[0] = c2(1.f / E[0].x, 0.f);
-    }
-    __syncwarp();
-    // levinsonsAlgorithm with the invalid latch; the reflection coefficients in uu, the latched steps in bits
+    float xm[MAXM];
+    C2 E[MAXM], sol[MAXM], uu[MAXM];
     uint32_t latched[(MAXM + 31) / 32];
     for (int i = 0; i < (MAXM + 31) / 32; ++i)
         latched[i] = 0u;
+    xm[0] = (1.f - bias) * moments[idx] + bias * 0.5f;
+    for (int i = 1; i < n; ++i)
+        xm[i] = (1.f - bias) * moments[idx + i];
+    // trigonometricToExponentialMoments (E[0] un-doubled inside the recurrence)
+    const float phi = kPi * xm[0] - 0.5f * kPi;
+    float sphi, cphi;
+    sincosf(phi, &sphi, &cphi);
+    E[0] = c2(kInv4Pi * cphi, kInv4Pi * sphi);
+    for (int l = 1; l < n; ++l)
+    {
+        C2 acc = c2(0.f, 0.f);
+        for (int j = 0; j < l; ++j)
+            acc = acc + (float(l - j) * xm[l - j]) * E[j];
+        const float w = (float)(6.283185307179586 / (double)l);
+        E[l] = c2(-w * acc.y, w * acc.x);
+    }
+    E[0] = 2.f * E[0];
+    // levinsonsAlgorithm with the invalid latch
+    sol[0] = c2(1.f / E[0].x, 0.f);
     bool invalid = false;
-    for (int j = 1; j < nw; ++j)
+    for (int j = 1; j < n; ++j)
     {
         C2 u = c2(0.f, 0.f);
         if (!invalid)
-            for (int k = r; k < j; k += kAdjGroup)
+            for (int k = 0; k < j; ++k)
                 u = u + sol[k] * E[j - k];
-        u = c2(adj_group_sum(u.x), adj_group_sum(u.y));
         float a2 = abs2(u);
         if (invalid || a2 >= 1.f)
         {
@@ -381,168 +335,169 @@ __global__ void __launch_bounds__(128) prepare_adjoint_kernel(int num_pixels, in
             invalid = true;
             latched[j >> 5] |= 1u << (j & 31);
         }
+        uu[j] = u;
         const float f = 1.f / (1.f - a2);
         const float s0 = sol[0].x;
-        for (int k = 1 + r; k <= j - k; k += kAdjGroup)
+        int k = 1, kk = j - 1;
+        for (; k < kk; ++k, --kk)
         {
-            const int kk = j - k;
-            const C2 pa = sol[k], pb = sol[kk];
-            sol[k] = f * (pa - conj(pb) * u);
-            if (k != kk)
-                sol[kk] = f * (pb - conj(pa) * u);
+            const C2 p = sol[k], q = sol[kk];
+            sol[k] = f * (p - conj(q) * u);
+            sol[kk] = f * (q - conj(p) * u);
         }
-        if (r == 0)
+        if (k == kk)
         {
-            uu[j] = u;
-            sol[j] = f * ((-s0) * u);
-            sol[0] = c2(f * s0, 0.f);
+            const C2 p = sol[k];
+            sol[k] = f * (p - conj(p) * u);
         }
-        __syncwarp();
+        sol[j] = f * ((-s0) * u);
+        sol[0] = c2(f * s0, 0.f);
     }
-    // A_q = sum_j P_j conj(P_{j+q}) with P = 2 pi sol
-    for (int q = r; q < nw; q += kAdjGroup)
+    // P = 2 pi sol; Eh = E with Eh[0] = E[0] / 2; a_q = sum_j P_j conj(P_{j+q}); acc_k = sum_{q>=k} Im(a_q Eh_{q-k})
+    constexpr float kTwoPi = 6.283185307179586f;
+    C2 A[MAXM];
+    float accv[MAXM];
+    for (int q = 0; q < n; ++q)
     {
-        C2 a = c2(0.f, 0.f);
-        for (int j = 0; j + q < nw; ++j)
-            a = a + (kTwoPi * sol[j]) * conj(kTwoPi * sol[j + q]);
-        A[q] = a;
+        C2 s = c2(0.f, 0.f);
+        for (int j = 0; j + q < n; ++j)
+            s = s + (kTwoPi * sol[j]) * conj(kTwoPi * sol[j + q]);
+        A[q] = s;
     }
-    __syncwarp();
-    // acc_k = sum_{q>=k} Im(A_q Eh_{q-k}) (Eh = E with E_0 halved), and d loss / d norm = sum_k lambda_bar_k acc_k
-    float gnorm = 0.f;
-    for (int k = r; k < nw; k += kAdjGroup)
+    for (int k = 0; k < n; ++k)
     {
-        float a = 0.f;
-        for (int q = k; q < nw; ++q)
+        float s = 0.f;
+        for (int q = k; q < n; ++q)
         {
-            const C2 e = (q == k) ? 0.5f * E[0] : E[q - k];
-            a += A[q].x * e.y + A[q].y * e.x;
+            const C2 e = (q - k == 0) ? 0.5f * E[0] : E[q - k];
+            s += A[q].x * e.y + A[q].y * e.x;
         }
-        gnorm += gl[k] * a;
+        accv[k] = s;
     }
-    gnorm = adj_group_sum(gnorm);
     const float P0 = kTwoPi * sol[0].x;
     const float norm = 1.f / (kPi * P0);
 
     // ---- reverse ----
-    for (int k = r; k < nw; k += kAdjGroup)
-        gl[k] *= norm; // d / d acc_k
-    __syncwarp();
-    // Eh_bar_d = sum_k acc_bar_k (A_{k+d}.y, A_{k+d}.x)
-    for (int d = r; d < nw; d += kAdjGroup)
+    // lambda_k = norm acc_k
+    float gnorm = 0.f;
+    for (int k = 0; k < n; ++k)
     {
-        C2 g = c2(0.f, 0.f);
-        for (int k = 0; k + d < nw; ++k)
-            g = g + gl[k] * c2(A[k + d].y, A[k + d].x);
-        gE[d] = d == 0 ? 0.5f * g : g; // Eh_0 = E_0 / 2
+        gnorm += gl[k] * accv[k];
+        gl[k] *= norm; // now d / d acc_k
     }
-    // A_bar_q = sum_{k<=q} acc_bar_k (Eh_{q-k}.y, Eh_{q-k}.x), into A's space
-    __syncwarp();
-    for (int q = r; q < nw; q += kAdjGroup)
+    // acc_k = sum_{q>=k} Im(A_q Eh_{q-k}): A_bar_q += acc_bar_k (Eh.y, Eh.x); Eh_bar_{q-k} += acc_bar_k (A.y, A.x)
+    C2 gE[MAXM], gP[MAXM];
+    for (int i = 0; i < n; ++i)
     {
-        C2 g = c2(0.f, 0.f);
+        gE[i] = c2(0.f, 0.f);
+        gP[i] = c2(0.f, 0.f);
+    }
+    for (int q = 0; q < n; ++q)
+    {
+        C2 gA = c2(0.f, 0.f);
         for (int k = 0; k <= q; ++k)
         {
-            const C2 e = (q == k) ? 0.5f * E[0] : E[q - k];
-            g = g + gl[k] * c2(e.y, e.x);
+            const C2 e = (q - k == 0) ? 0.5f * E[0] : E[q - k];
+            gA = gA + gl[k] * c2(e.y, e.x);
+            gE[q - k] = gE[q - k] + gl[k] * c2(A[q].y, A[q].x);
         }
-        A[q] = g;
+        // A_q = sum_j P_j conj(P_{j+q})
+        for (int j = 0; j + q < n; ++j)
+        {
+            const C2 pj = kTwoPi * sol[j], pq = kTwoPi * sol[j + q];
+            gP[j] = gP[j] + gA * pq;
+            gP[j + q] = gP[j + q] + conj(gA) * pj;
+        }
     }
-    __syncwarp();
-    // P_bar_j = sum_q A_bar_q P_{j+q} + sum_{q<=j} conj(A_bar_q) P_{j-q}; sol_bar = 2 pi P_bar
-    for (int j = r; j < nw; j += kAdjGroup)
-    {
-        C2 g = c2(0.f, 0.f);
-        for (int q = 0; j + q < nw; ++q)
-            g = g + A[q] * (kTwoPi * sol[j + q]);
-        for (int q = 0; q <= j; ++q)
-            g = g + conj(A[q]) * (kTwoPi * sol[j - q]);
-        if (j == 0)
-            g.x += gnorm * (-norm / P0);
-        gP[j] = kTwoPi * g;
-    }
-    __syncwarp();
+    gP[0].x += gnorm * (-norm / P0);
+    gE[0] = 0.5f * gE[0]; // Eh[0] = E[0] / 2
+    // sol_bar = 2 pi P_bar (reuse gP)
+    for (int i = 0; i < n; ++i)
+        gP[i] = kTwoPi * gP[i];
 
     // Levinson backwards: sol holds the state after step j, gP its adjoint
-    for (int j = nw - 1; j >= 1; --j)
+    for (int j = n - 1; j >= 1; --j)
     {
         const C2 u = uu[j];
         const float a2 = abs2(u);
         const float f = 1.f / (1.f - a2);
+        // f_bar = sum_k Re(conj(s_bar_k) new_k) / f
         float gf = 0.f;
-        for (int k = r; k <= j; k += kAdjGroup)
+        for (int k = 0; k <= j; ++k)
             gf += gP[k].x * sol[k].x + gP[k].y * sol[k].y;
-        gf = adj_group_sum(gf) / f;
-        __syncwarp();
-        // old_k = new_k + u conj(new_{j-k}), pairs in place
-        for (int k = r; k <= j - k; k += kAdjGroup)
+        gf /= f;
+        // old_k = new_k + u conj(new_{j-k}), k = 0..j-1 (pairs in place)
         {
-            const int kk = j - k;
-            const C2 pa = sol[k], pb = sol[kk];
-            sol[k] = pa + u * conj(pb);
-            if (k != kk)
-                sol[kk] = pb + u * conj(pa);
-        }
-        __syncwarp();
-        if (r == 0)
+            int k = 0, kk = j;
+            for (; k < kk; ++k, --kk)
+            {
+                const C2 p = sol[k], q = sol[kk];
+                sol[k] = p + u * conj(q);
+                sol[kk] = q + u * conj(p);
+            }
+            if (k == kk)
+            {
+                const C2 p = sol[k];
+                sol[k] = p + u * conj(p);
+            }
             sol[j] = c2(0.f, 0.f);
-        // u_bar = -f sum_{k=1..j} s_bar_k old_{j-k}
-        C2 gu = c2(0.f, 0.f);
-        for (int k = 1 + r; k <= j; k += kAdjGroup)
-            gu = gu - (f * gP[k]) * sol[j - k];
-        gu = c2(adj_group_sum(gu.x), adj_group_sum(gu.y));
-        __syncwarp();
-        // old_bar_i = f s_bar_i - conj(f s_bar_{j-i}) u, pairs in place; old_j's adjoint dropped
-        for (int i = r; i <= j - i; i += kAdjGroup)
-        {
-            const int ii = j - i;
-            const C2 vi = f * gP[i], vii = f * gP[ii];
-            gP[i] = vi - conj(vii) * u;
-            if (i != ii)
-                gP[ii] = vii - conj(vi) * u;
         }
-        __syncwarp();
-        if (r == 0)
+        // v_bar = f s_bar; u_bar = -f sum_{k=1..j} s_bar_k old_{j-k}; old_bar_i = f s_bar_i - conj(f s_bar_{j-i}) u
+        C2 gu = c2(0.f, 0.f);
+        for (int k = 1; k <= j; ++k)
+            gu = gu - (f * gP[k]) * sol[j - k];
+        {
+            int i = 0, ii = j;
+            for (; i < ii; ++i, --ii)
+            {
+                const C2 vi = f * gP[i], vii = f * gP[ii];
+                gP[i] = vi - conj(vii) * u;
+                gP[ii] = vii - conj(vi) * u; // ii = j: old_j is the constant 0, its adjoint is dropped below
+            }
+            if (i == ii)
+            {
+                const C2 vi = f * gP[i];
+                gP[i] = vi - conj(vi) * u;
+            }
             gP[j] = c2(0.f, 0.f);
-        __syncwarp();
+        }
         if (!((latched[j >> 5] >> (j & 31)) & 1u))
         {
-            // f = 1 / (1 - |u|^2): d f / d u = 2 f^2 u; u = sum_{k<j} old_k E_{j-k}
+            // f = 1 / (1 - |u|^2): d f / d u = 2 f^2 u
             gu = gu + (2.f * gf * f * f) * u;
-            for (int k = r; k < j; k += kAdjGroup)
+            // u = sum_{k<j} old_k E_{j-k}
+            for (int k = 0; k < j; ++k)
             {
                 const C2 ok = sol[k];
                 gP[k] = gP[k] + gu * conj(E[j - k]);
                 gE[j - k] = gE[j - k] + gu * conj(ok);
             }
         }
-        __syncwarp();
     }
-    // sol_0 = 1 / E_0.x (real); then trigonometricToExponentialMoments backwards with E[0] = 2 e_0
-    if (r == 0)
-    {
-        gE[0].x += -gP[0].x / (E[0].x * E[0].x);
-        E[0] = 0.5f * E[0];
-        gE[0] = 2.f * gE[0];
-    }
-    __syncwarp();
-    for (int l = nw - 1; l >= 1; --l)
+    // sol_0 = 1 / E_0.x (real)
+    gE[0].x += -gP[0].x / (E[0].x * E[0].x);
+
+    // trigonometricToExponentialMoments backwards: E[0] = 2 e_0
+    float gx[MAXM];
+    for (int i = 0; i < n; ++i)
+        gx[i] = 0.f;
+    E[0] = 0.5f * E[0];
+    gE[0] = 2.f * gE[0];
+    for (int l = n - 1; l >= 1; --l)
     {
         const float w = (float)(6.283185307179586 / (double)l);
-        const C2 g = gE[l];
-        const C2 gacc = c2(g.y * w, -g.x * w); // E_l = (i w) acc
-        for (int j = r; j < l; j += kAdjGroup)
+        // E_l = (i w) acc: acc_bar = E_bar_l (-i w)
+        const C2 gacc = c2(gE[l].y * w, -gE[l].x * w);
+        for (int j = 0; j < l; ++j)
         {
             const float sc = float(l - j) * xm[l - j];
             gE[j] = gE[j] + sc * gacc;
             gx[l - j] += float(l - j) * (gacc.x * E[j].x + gacc.y * E[j].y);
         }
-        __syncwarp();
     }
-    if (r == 0)
-        gx[0] += kPi * kInv4Pi * (-gE[0].x * sphi + gE[0].y * cphi);
-    __syncwarp();
-    for (int i = r; i < n; i += kAdjGroup)
+    // e_0 = (cos phi, sin phi) / (4 pi), phi = pi x_0 - pi / 2
+    gx[0] += kPi * kInv4Pi * (-gE[0].x * sphi + gE[0].y * cphi);
+    for (int i = 0; i < n; ++i)
         grad_moments[idx + i] = (1.f - bias) * gx[i];
 }
 
@@ -564,32 +519,24 @@ struct GenAdjArgs
     int *error_flag;
 };
 
-// the trilinear sample's corners and weights (grid_sample), for the scatter of d loss / d sample
-__device__ __forceinline__ void scatter_sample(const GridView &g, float *grad, float px, float py, float pz,
-                                               float gs)
+// d loss / d sample scattered to the eight corners of the trilinear sample at q (the sample's own corners and
+// weights, with the clamp to the grid)
+__device__ __forceinline__ void scatter_sample(const GridView &g, float *grad, const GridPoint &q, float gs)
 {
-    const float p[3] = {px, py, pz};
-    const int sz[3] = {g.nx, g.ny, g.nz};
-    float a[3];
-    int il[3];
+    const int x0 = min(max((int)q.fl[0], 0), g.nx - 1), x1 = min(max((int)q.fl[0] + 1, 0), g.nx - 1);
+    const float wx[2] = {(1.f - q.a[0]) * gs, q.a[0] * gs};
 #pragma unroll
-    for (int i = 0; i < 3; ++i)
+    for (int c = 0; c < 4; ++c)
     {
-        const float np = __fdiv_rn(__fsub_rn(p[i], g.dmin[i]), g.ext[i]);
-        const float ip = __fmul_rn(np, (float)sz[i]);
-        const float fl = floorf(ip);
-        a[i] = __fsub_rn(ip, fl);
-        il[i] = (int)fl;
-    }
-#pragma unroll
-    for (int c = 0; c < 8; ++c)
-    {
-        const int dx = c & 1, dy = (c >> 1) & 1, dz = c >> 2;
-        const float w = (dx ? a[0] : 1.f - a[0]) * (dy ? a[1] : 1.f - a[1]) * (dz ? a[2] : 1.f - a[2]);
-        const int x = min(max(il[0] + dx, 0), g.nx - 1), y = min(max(il[1] + dy, 0), g.ny - 1),
-                  z = min(max(il[2] + dz, 0), g.nz - 1);
-        if (w != 0.f)
-            atomicAdd(grad + ((size_t)z * (size_t)(g.ny * g.nx) + (size_t)(y * g.nx) + (size_t)x), w * gs);
+        const int dy = c & 1, dz = c >> 1;
+        const float wyz = (dy ? q.a[1] : 1.f - q.a[1]) * (dz ? q.a[2] : 1.f - q.a[2]);
+        const int y = min(max((int)q.fl[1] + dy, 0), g.ny - 1), z = min(max((int)q.fl[2] + dz, 0), g.nz - 1);
+        float *row = grad + (size_t)(z * g.ny + y) * (size_t)g.nx;
+        const float w0 = wx[0] * wyz, w1 = wx[1] * wyz;
+        if (w0 != 0.f)
+            atomicAdd(row + x0, w0);
+        if (w1 != 0.f)
+            atomicAdd(row + x1, w1);
     }
 }
 
@@ -683,14 +630,15 @@ template <int NJ> __global__ void __launch_bounds__(128) generate_adjoint_kernel
 
     // the sample waiting for its left-end weight: lane 0 holds the first sample (at t_near)
     bool min_done = false, max_done = false;
-    float pend_t = t_near, pend_g = 0.f, pend_f = 0.f;
+    GridPoint pend_q = {};
+    float pend_g = 0.f, pend_f = 0.f;
     bool pend = false;
     float p_tail = -kPiF;
     if (hit)
     {
-        const float sx = __fadd_rn(o[0], __fmul_rn(t, d[0])), sy = __fadd_rn(o[1], __fmul_rn(t, d[1])),
-                    sz = __fadd_rn(o[2], __fmul_rn(t, d[2]));
-        const float s0 = grid_sample(a.grid, sx, sy, sz);
+        const GridPoint q0 = grid_point(a.grid, __fadd_rn(o[0], __fmul_rn(t, d[0])),
+                                        __fadd_rn(o[1], __fmul_rn(t, d[1])), __fadd_rn(o[2], __fmul_rn(t, d[2])));
+        const float s0 = grid_blend(a.grid, q0);
         const float f0 = map_density(s0, a.data_min, a.data_max);
         float g0 = 0.f;
         if (f0 == b4.z && !min_done)
@@ -706,6 +654,7 @@ template <int NJ> __global__ void __launch_bounds__(128) generate_adjoint_kernel
         pend = (q == 0);
         pend_g = g0;
         pend_f = s0;
+        pend_q = q0;
     }
     int cap = 0;
     if (hit)
@@ -733,12 +682,14 @@ template <int NJ> __global__ void __launch_bounds__(128) generate_adjoint_kernel
         }
         const bool my_valid = q < nv;
         float p_my = 0.f, s_my = 0.f, f_my = 0.f;
+        GridPoint q_my = {};
         cf z = {1.f, 0.f};
         if (my_valid)
         {
             p_my = sub_pi(__fmul_rn(__fsub_rn(my_t, t_near), pti));
-            s_my = grid_sample(a.grid, __fadd_rn(o[0], __fmul_rn(my_t, d[0])), __fadd_rn(o[1], __fmul_rn(my_t, d[1])),
-                               __fadd_rn(o[2], __fmul_rn(my_t, d[2])));
+            q_my = grid_point(a.grid, __fadd_rn(o[0], __fmul_rn(my_t, d[0])), __fadd_rn(o[1], __fmul_rn(my_t, d[1])),
+                              __fadd_rn(o[2], __fmul_rn(my_t, d[2])));
+            s_my = grid_blend(a.grid, q_my);
             f_my = map_density(s_my, a.data_min, a.data_max);
             float sn, cs;
             sincosf(p_my - h, &sn, &cs);
@@ -791,9 +742,7 @@ template <int NJ> __global__ void __launch_bounds__(128) generate_adjoint_kernel
             {
                 const float gsamp = (pend_g + As[0] + Bs[0]) * map_density_derivative(pend_f, a.data_min, a.data_max);
                 if (gsamp != 0.f)
-                    scatter_sample(a.grid, a.grad_volume, __fadd_rn(o[0], __fmul_rn(pend_t, d[0])),
-                                   __fadd_rn(o[1], __fmul_rn(pend_t, d[1])), __fadd_rn(o[2], __fmul_rn(pend_t, d[2])),
-                                   gsamp);
+                    scatter_sample(a.grid, a.grad_volume, pend_q, gsamp);
                 pend = false;
             }
             // the bound adjoints go to the first sample equal to the minimum / maximum
@@ -828,16 +777,14 @@ template <int NJ> __global__ void __launch_bounds__(128) generate_adjoint_kernel
                 {
                     const float gsamp = (gmy + a_next + b_next) * map_density_derivative(s_my, a.data_min, a.data_max);
                     if (gsamp != 0.f)
-                        scatter_sample(a.grid, a.grad_volume, __fadd_rn(o[0], __fmul_rn(my_t, d[0])),
-                                       __fadd_rn(o[1], __fmul_rn(my_t, d[1])), __fadd_rn(o[2], __fmul_rn(my_t, d[2])),
-                                       gsamp);
+                        scatter_sample(a.grid, a.grad_volume, q_my, gsamp);
                 }
                 else
                 {
                     pend = true;
                     pend_g = gmy;
                     pend_f = s_my;
-                    pend_t = my_t;
+                    pend_q = q_my;
                 }
             }
             p_tail = p_last;
@@ -888,14 +835,13 @@ template <int NJ> __global__ void __launch_bounds__(128) generate_adjoint_kernel
     {
         const float gsamp = (pend_g + AL + BL) * map_density_derivative(pend_f, a.data_min, a.data_max);
         if (gsamp != 0.f)
-            scatter_sample(a.grid, a.grad_volume, __fadd_rn(o[0], __fmul_rn(pend_t, d[0])),
-                           __fadd_rn(o[1], __fmul_rn(pend_t, d[1])), __fadd_rn(o[2], __fmul_rn(pend_t, d[2])), gsamp);
+            scatter_sample(a.grid, a.grad_volume, pend_q, gsamp);
     }
     if (q == 0)
     {
-        const float sx = __fadd_rn(o[0], __fmul_rn(t_far, d[0])), sy = __fadd_rn(o[1], __fmul_rn(t_far, d[1])),
-                    sz = __fadd_rn(o[2], __fmul_rn(t_far, d[2]));
-        const float s_far = grid_sample(a.grid, sx, sy, sz);
+        const GridPoint qf = grid_point(a.grid, __fadd_rn(o[0], __fmul_rn(t_far, d[0])),
+                                        __fadd_rn(o[1], __fmul_rn(t_far, d[1])), __fadd_rn(o[2], __fmul_rn(t_far, d[2])));
+        const float s_far = grid_blend(a.grid, qf);
         const float f_far = map_density(s_far, a.data_min, a.data_max);
         float g = AL - BL;
         if (!min_done && f_far == b4.z)
@@ -904,7 +850,7 @@ template <int NJ> __global__ void __launch_bounds__(128) generate_adjoint_kernel
             g += g_max;
         const float gsamp = g * map_density_derivative(s_far, a.data_min, a.data_max);
         if (gsamp != 0.f)
-            scatter_sample(a.grid, a.grad_volume, sx, sy, sz, gsamp);
+            scatter_sample(a.grid, a.grad_volume, qf, gsamp);
     }
 }
 
@@ -925,13 +871,7 @@ template <int MAXM>
 cudaError_t launch_prep_adj(int P, int m, const float *moments, float bias, const float *gl, float *gm,
                             cudaStream_t stream)
 {
-    const int bytes = kAdjPixels * AdjLayout<MAXM>::floats_per_pixel * (int)sizeof(float);
-    cudaError_t e = cudaFuncSetAttribute(prepare_adjoint_kernel<MAXM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         bytes);
-    if (e != cudaSuccess)
-        return e;
-    prepare_adjoint_kernel<MAXM><<<(P + kAdjPixels - 1) / kAdjPixels, kAdjPixels * kAdjGroup, bytes, stream>>>(
-        P, m, moments, bias, gl, gm);
+    prepare_adjoint_kernel<MAXM><<<(P + 63) / 64, 64, 0, stream>>>(P, m, moments, bias, gl, gm);
     return cudaGetLastError();
 }
 

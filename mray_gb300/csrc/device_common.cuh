@@ -131,23 +131,35 @@ __device__ __forceinline__ float grid_get(const GridView &g, float x, float y, f
     return tex3D<float>(g.tex, x, y, z);
 }
 
-// Corner-aligned trilinear sample with clamp-to-edge, summed in the reference's order.
-__device__ __forceinline__ float grid_sample(const GridView &g, float px, float py, float pz)
+// The position of a sample in voxel units: the lower corner floor(ip) and the fractions ip - floor(ip), in the
+// reference's float operations (RegularGrid::sample, src/volume.h:97-123).
+struct GridPoint
+{
+    float fl[3], a[3];
+};
+
+__device__ __forceinline__ GridPoint grid_point(const GridView &g, float px, float py, float pz)
 {
     const float p[3] = {px, py, pz};
     const int sz[3] = {g.nx, g.ny, g.nz};
-    float a[3], fl[3];
+    GridPoint q;
 #pragma unroll
     for (int i = 0; i < 3; ++i)
     {
         float np = __fdiv_rn(__fsub_rn(p[i], g.dmin[i]), g.ext[i]);
         float ip = __fmul_rn(np, (float)sz[i]);
-        fl[i] = floorf(ip);
-        a[i] = __fsub_rn(ip, fl[i]);
+        q.fl[i] = floorf(ip);
+        q.a[i] = __fsub_rn(ip, q.fl[i]);
     }
+    return q;
+}
+
+// Corner-aligned trilinear blend with clamp-to-edge, summed in the reference's order.
+__device__ __forceinline__ float grid_blend(const GridView &g, const GridPoint &q)
+{
     // texel centres of the lower and upper corners (the clamp is the texture's address mode)
-    const float xl = __fadd_rn(fl[0], 0.5f), yl = __fadd_rn(fl[1], 0.5f), zl = __fadd_rn(fl[2], 0.5f);
-    const float xr = __fadd_rn(fl[0], 1.5f), yr = __fadd_rn(fl[1], 1.5f), zr = __fadd_rn(fl[2], 1.5f);
+    const float xl = __fadd_rn(q.fl[0], 0.5f), yl = __fadd_rn(q.fl[1], 0.5f), zl = __fadd_rn(q.fl[2], 0.5f);
+    const float xr = __fadd_rn(q.fl[0], 1.5f), yr = __fadd_rn(q.fl[1], 1.5f), zr = __fadd_rn(q.fl[2], 1.5f);
     const float lll = grid_get(g, xl, yl, zl);
     const float lrl = grid_get(g, xl, yr, zl);
     const float rrl = grid_get(g, xr, yr, zl);
@@ -156,7 +168,7 @@ __device__ __forceinline__ float grid_sample(const GridView &g, float px, float 
     const float lrr = grid_get(g, xl, yr, zr);
     const float rrr = grid_get(g, xr, yr, zr);
     const float rlr = grid_get(g, xr, yl, zr);
-    const float ax = a[0], ay = a[1], az = a[2];
+    const float ax = q.a[0], ay = q.a[1], az = q.a[2];
     const float bx = __fsub_rn(1.f, ax), by = __fsub_rn(1.f, ay), bz = __fsub_rn(1.f, az);
     float s = __fmul_rn(__fmul_rn(__fmul_rn(bx, by), bz), lll);
     s = __fadd_rn(s, __fmul_rn(__fmul_rn(__fmul_rn(ax, by), bz), rll));
@@ -167,6 +179,11 @@ __device__ __forceinline__ float grid_sample(const GridView &g, float px, float 
     s = __fadd_rn(s, __fmul_rn(__fmul_rn(__fmul_rn(bx, ay), az), lrr));
     s = __fadd_rn(s, __fmul_rn(__fmul_rn(__fmul_rn(ax, ay), az), rrr));
     return s;
+}
+
+__device__ __forceinline__ float grid_sample(const GridView &g, float px, float py, float pz)
+{
+    return grid_blend(g, grid_point(g, px, py, pz));
 }
 
 // ---- SPH particles ----------------------------------------------------------------------------------------
