@@ -77,6 +77,8 @@ typedef struct oracle_options
     int tf_bspline;
     void *bounds_out;
     const void *bounds_in;
+    /* generate only: columns col_begin, col_begin + col_step, ... below col_end (col_end <= 0: the width) */
+    int col_begin, col_end, col_step;
 } oracle_options;
 
 #define ORACLE_DECL(R, SFX)                                                                                         \

@@ -28,7 +28,7 @@ fp = np.ctypeslib.ndpointer
 class Options(C.Structure):
     _fields_ = [("exact_atan", C.c_int), ("nthreads", C.c_int), ("row_begin", C.c_int), ("row_end", C.c_int),
                 ("row_step", C.c_int), ("tf_bspline", C.c_int), ("bounds_out", C.c_void_p),
-                ("bounds_in", C.c_void_p)]
+                ("bounds_in", C.c_void_p), ("col_begin", C.c_int), ("col_end", C.c_int), ("col_step", C.c_int)]
 
 
 class Grid(C.Structure):
@@ -187,7 +187,7 @@ def _dt(precision):
 # --------------------------------------------------------------------------------------------------------------
 
 def generate_moments(cam, gp, volume, dmin, dmax, width, height, m, precision="f32", nthreads=0, rows=None,
-                     float_bounds=False):
+                     float_bounds=False, cols=None):
     """generate_host's per-pixel loop: returns (moments[H,W,m], bounds[H,W,2] u16, counts[H,W] u32), and with
     float_bounds the unquantized bounds[H,W,2] in the working precision as a fourth value."""
     L = lib()
@@ -197,6 +197,8 @@ def generate_moments(cam, gp, volume, dmin, dmax, width, height, m, precision="f
     bounds = np.zeros((height, width, 2), dtype=np.uint16)
     counts = np.zeros((height, width), dtype=np.uint32)
     o = options(nthreads, rows)
+    if cols is not None:
+        o.col_begin, o.col_end, o.col_step = cols
     bf = np.zeros((height, width, 2), dtype=dt) if float_bounds else None
     o.bounds_out = bf.ctypes.data if float_bounds else None
     getattr(L, f"oracle_generate_moments_{precision}")(C.byref(cam), C.byref(gp), C.byref(g), width, height, m,
