@@ -141,6 +141,25 @@ int mraygb_quantize_prediction_coding(mraygb_context *ctx, int width, int height
                                       const uint32_t *h_index, const float *h_data, uint64_t data_size,
                                       const uint8_t *h_table, uint8_t *h_out, uint64_t capacity, uint64_t *h_nbytes);
 
+/* create_quantization_table (src/measure_coding_error.cpp:374-438) as main.cpp:318-327 runs it before the codes
+ * are written: on the sample_moment_image (src/moment_image_sample.h:33-62) of a compact, prediction-coded
+ * moment image.  With sampling > 0 the sample is s x s pixels, s = min(W, sampling) = min(H, sampling), pixel
+ * (x, y) of the sample being pixel (x * (W / s), y * (H / s)) of the image (the reference's
+ * quantization_curve_sampling, 64 by default); the reference indexes a w x h sample as h x w, so a non-square
+ * sample (min(W, sampling) != min(H, sampling)) returns MRAYGB_NOT_SUPPORTED.  With sampling <= 0 the whole
+ * image is the sample (create_quantization_table applied to the image as given).
+ *   h_table : num_moments bytes: [0] = 16, [1] = start_bits, then per index the fewest bits (>= 2, at most the
+ *             previous index's) whose mean rRMSE stays below that of index 1 at start_bits.  The reference
+ *             installs the table as its global quantization table (set_prediction_coding_quantization_table);
+ *             here the caller passes it to mraygb_(stage_)quantize_prediction_coding.
+ *   h_means : num_moments * 32 floats or NULL: the mean rRMSE of quantizing moment idx to b bits at
+ *             [idx * 32 + b], for every idx in [1, m) and b in [min(2, start_bits), start_bits]; NaN elsewhere.
+ * num_moments >= 2, start_bits in 1..31; the data must be prediction coded (residuals in [0, 1]). */
+int mraygb_create_quantization_table(mraygb_context *ctx, int width, int height, int num_moments,
+                                     const uint32_t *h_index, const float *h_data, uint64_t data_size,
+                                     int coding_warp, const uint16_t *h_coding_params, int start_bits, int sampling,
+                                     uint8_t *h_table, float *h_means);
+
 /* ---- stage API: device pointers, ordered on the context stream ------------------------------------------ */
 
 /* Per-ray moments over the uploaded grid (generate_ray, src/raymarch_generate.h:69-148, driven as
@@ -180,6 +199,13 @@ int mraygb_stage_quantize_prediction_coding(mraygb_context *ctx, int width, int 
 int mraygb_stage_dequantize_prediction_coding(mraygb_context *ctx, int width, int height, int num_moments,
                                               const uint32_t *d_index, const uint8_t *h_table,
                                               const uint8_t *d_bytes, uint64_t num_bytes, float *d_data);
+
+/* mraygb_create_quantization_table on device buffers (d_coding_params: 2(m-1) u16 for the default warp).  The
+ * table and the means are returned in host memory; the call waits for the stream. */
+int mraygb_stage_create_quantization_table(mraygb_context *ctx, int width, int height, int num_moments,
+                                           const uint32_t *d_index, const float *d_data, int coding_warp,
+                                           const uint16_t *d_coding_params, int start_bits, int sampling,
+                                           uint8_t *h_table, float *h_means);
 
 /* Compaction that allocates nothing, for callers that must not call cudaMalloc / cudaFree while they work:
  * renderers and services that reserve all device memory up front in their own pool or arena (where an

@@ -8,12 +8,13 @@ from .types import (CODING_WARP_DEFAULT_TRANSFORMED, CODING_WARP_NONE, Camera, G
                     ReconstructionParameters)
 from .raymarcher import (MAX_MOMENTS, PRECISION_COMPENSATED_FF_MESE, PRECISION_COMPENSATED_FP64_MESE, PRECISION_FP32, ColorImageHost, Context,
                          MomentImageHost, Particles, RegularGrid, TransferFunction, default_context, default_quantization_table,
-                         generate, preintegrate, quantize_prediction_coding, reconstruct)
+                         generate, preintegrate, quantize_prediction_coding, reconstruct,
+                         create_quantization_table)
 from ._lib import MrayError
 
 __all__ = [
     "Camera", "GenerationParameters", "ReconstructionParameters", "CODING_WARP_DEFAULT_TRANSFORMED",
     "CODING_WARP_NONE", "ColorImageHost", "Context", "MomentImageHost", "Particles", "RegularGrid", "TransferFunction",
-    "default_context", "default_quantization_table", "quantize_prediction_coding", "generate", "preintegrate", "reconstruct", "MrayError", "PRECISION_FP32",
+    "default_context", "default_quantization_table", "create_quantization_table", "quantize_prediction_coding", "generate", "preintegrate", "reconstruct", "MrayError", "PRECISION_FP32",
     "PRECISION_COMPENSATED_FP64_MESE", "PRECISION_COMPENSATED_FF_MESE", "MAX_MOMENTS",
 ]

@@ -25,7 +25,7 @@ EXPORTS = [
     "mraygb_stage_prepare_moments", "mraygb_stage_reconstruct", "mraygb_quantize_prediction_coding",
     "mraygb_stage_prediction_encode", "mraygb_stage_quantize_prediction_coding",
     "mraygb_stage_dequantize_prediction_coding", "mraygb_stage_compact_noalloc", "mraygb_diff_forward",
-    "mraygb_diff_backward",
+    "mraygb_diff_backward", "mraygb_create_quantization_table", "mraygb_stage_create_quantization_table",
 ]
 
 _lock = threading.Lock()
@@ -75,6 +75,8 @@ def _declare(L):
     G, RP = P(GenerationParameters), P(ReconstructionParameters)
     L.mraygb_diff_forward.argtypes = [vp, P(Camera), G, RP, i, i, i, vp, vp, vp, vp, vp]
     L.mraygb_diff_backward.argtypes = [vp, P(Camera), G, RP, i, i, i, vp, vp, vp, vp, vp, vp, vp, vp]
+    L.mraygb_create_quantization_table.argtypes = [vp, i, i, i, vp, vp, u64, i, vp, i, i, vp, vp]
+    L.mraygb_stage_create_quantization_table.argtypes = [vp, i, i, i, vp, vp, i, vp, i, i, vp, vp]
     special = ("mraygb_destroy", "mraygb_last_error", "mraygb_get_stream", "mraygb_kernel_launches")
     for name in EXPORTS:
         if name not in special:

@@ -35,6 +35,7 @@ SOURCES = [
     ("mese_f64.cu", []),
     ("mese_ff.cu", []),
     ("coding.cu", ["--fmad=false"]),
+    ("quant_curve.cu", ["--fmad=false"]),
     ("api.cpp", ["-x", "cu"]),
 ]
 

@@ -13,6 +13,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <vector>
 
 #include <cuda_runtime.h>
 
@@ -88,6 +89,8 @@ struct mraygb_context
     DeviceBuffer coding_partial, coding_params_f, table, bits, bit_offset, scan_scratch64, packed;
     // adjoint work buffers of the differentiation form
     DeviceBuffer adj_lambda, adj_bounds;
+    // the quantization curve: per-sample moments and errors, the means, the uploaded sample of the host call
+    DeviceBuffer qc_scratch, qc_means, qc_index, qc_data;
 };
 
 namespace
@@ -476,7 +479,8 @@ void mraygb_destroy(mraygb_context *ctx)
                             &ctx->pmoments, &ctx->rgba,    &ctx->rgba8,         &ctx->scan_scratch,
                             &ctx->error_flag, &ctx->coding_partial, &ctx->coding_params_f, &ctx->table,
                             &ctx->bits,    &ctx->bit_offset, &ctx->scan_scratch64, &ctx->packed,
-                            &ctx->adj_lambda, &ctx->adj_bounds};
+                            &ctx->adj_lambda, &ctx->adj_bounds, &ctx->qc_scratch, &ctx->qc_means,
+                            &ctx->qc_index, &ctx->qc_data};
     for (DeviceBuffer *b : bufs)
         b->release();
     if (ctx->own_stream)
@@ -823,7 +827,182 @@ int mraygb_stage_dequantize_prediction_coding(mraygb_context *ctx, int width, in
     return MRAYGB_OK;
 }
 
+// ---- quantization curve ---------------------------------------------------------------------------------------
+
+namespace
+{
+
+int check_quant_table_args(mraygb_context *ctx, int width, int height, int m, int coding_warp, int start_bits,
+                           uint8_t *h_table)
+{
+    int rc = check_image(ctx, width, height, m);
+    if (rc)
+        return rc;
+    if (m < 2)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "the quantization table needs num_moments >= 2 (got %d)", m);
+    if (start_bits < 1 || start_bits > 31)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "start_bits %d outside 1..31", start_bits);
+    if (coding_warp != MRAYGB_CODING_WARP_DEFAULT_TRANSFORMED && coding_warp != MRAYGB_CODING_WARP_NONE)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "unknown coding warp %d", coding_warp);
+    if (!h_table)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "NULL table");
+    return MRAYGB_OK;
+}
+
+// sample_moment_image's size as main.cpp:320-322 chooses it
+int sample_shape(mraygb_context *ctx, int width, int height, int sampling, int *sx, int *sy)
+{
+    if (sampling <= 0)
+    {
+        *sx = width;
+        *sy = height;
+        return MRAYGB_OK;
+    }
+    const int w = std::min(width, sampling), h = std::min(height, sampling);
+    if (w != h)
+        return fail(ctx, MRAYGB_NOT_SUPPORTED,
+                    "sample_moment_image of a %dx%d image at %d gives a %dx%d sample, which the reference indexes "
+                    "as %dx%d; only square samples are defined",
+                    width, height, sampling, w, h, h, w);
+    *sx = w;
+    *sy = h;
+    return MRAYGB_OK;
+}
+
+// the error means of every reachable (index, bits) pair on the device, then create_quantization_table's search
+// (measure_coding_error.cpp:400-435) over them
+int run_quant_table(mraygb_context *ctx, int width, int height, int m, const uint32_t *d_index, const float *d_data,
+                    int coding_warp, const uint16_t *d_coding_params, int sx, int sy, int start_bits,
+                    uint8_t *h_table, float *h_means)
+{
+    const int bmin = std::min(2, start_bits), nb = start_bits - bmin + 1;
+    const size_t P = (size_t)sx * (size_t)sy;
+    // the per-pixel errors of one pass stay within 1 GiB
+    const size_t row_bytes = (size_t)nb * P * sizeof(float);
+    const size_t rows = std::max<size_t>(1, std::min<size_t>((size_t)(m - 1), (size_t(1) << 30) / row_bytes));
+    CK(ctx->qc_scratch.reserve(quant_curve_scratch_bytes(sx, sy, m, nb, rows)), "quantization curve scratch");
+    CK(ctx->qc_means.reserve((size_t)(m - 1) * nb * sizeof(float)), "quantization curve means");
+    int launches = 0;
+    CK(launch_quant_curve(width, height, m, d_index, d_data, coding_warp,
+                          coding_warp == MRAYGB_CODING_WARP_DEFAULT_TRANSFORMED ? d_coding_params : nullptr, sx, sy,
+                          bmin, nb, rows, ctx->qc_scratch.ptr, ctx->qc_means.as<float>(), ctx->stream, &launches),
+       "quantization curve launch");
+    ctx->launches += launches;
+    std::vector<float> means((size_t)(m - 1) * nb);
+    CK(cudaMemcpyAsync(means.data(), ctx->qc_means.ptr, means.size() * sizeof(float), cudaMemcpyDeviceToHost,
+                       ctx->stream),
+       "means download");
+    CK(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+    auto mean = [&](int idx, int b) { return means[(size_t)(idx - 1) * nb + (b - bmin)]; };
+    h_table[0] = 16;
+    h_table[1] = (uint8_t)start_bits;
+    const int minimum_bits = 2;
+    const float threshold = mean(1, start_bits);
+    for (int idx = 2; idx < m; ++idx)
+    {
+        h_table[idx] = h_table[idx - 1];
+        for (int b = h_table[idx - 1]; b >= minimum_bits; --b)
+        {
+            if (mean(idx, b) >= threshold)
+                break;
+            h_table[idx] = (uint8_t)b;
+        }
+    }
+    if (h_means)
+    {
+        std::fill(h_means, h_means + (size_t)m * 32, NAN);
+        for (int idx = 1; idx < m; ++idx)
+            for (int b = bmin; b <= start_bits; ++b)
+                h_means[idx * 32 + b] = mean(idx, b);
+    }
+    return MRAYGB_OK;
+}
+
+} // namespace
+
+int mraygb_stage_create_quantization_table(mraygb_context *ctx, int width, int height, int m,
+                                           const uint32_t *d_index, const float *d_data, int coding_warp,
+                                           const uint16_t *d_coding_params, int start_bits, int sampling,
+                                           uint8_t *h_table, float *h_means)
+{
+    CHECK_CTX();
+    int rc = check_quant_table_args(ctx, width, height, m, coding_warp, start_bits, h_table);
+    if (rc)
+        return rc;
+    if (!d_index || !d_data)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "the quantization curve needs a compact image (index and data)");
+    if (coding_warp == MRAYGB_CODING_WARP_DEFAULT_TRANSFORMED && !d_coding_params)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "the default coding warp needs the coding parameters");
+    int sx, sy;
+    if ((rc = sample_shape(ctx, width, height, sampling, &sx, &sy)))
+        return rc;
+    return run_quant_table(ctx, width, height, m, d_index, d_data, coding_warp, d_coding_params, sx, sy, start_bits,
+                           h_table, h_means);
+}
+
 // ---- drop-in host API -------------------------------------------------------------------------------------------
+
+int mraygb_create_quantization_table(mraygb_context *ctx, int width, int height, int m, const uint32_t *h_index,
+                                     const float *h_data, uint64_t data_size, int coding_warp,
+                                     const uint16_t *h_coding_params, int start_bits, int sampling, uint8_t *h_table,
+                                     float *h_means)
+{
+    CHECK_CTX();
+    int rc = check_quant_table_args(ctx, width, height, m, coding_warp, start_bits, h_table);
+    if (rc)
+        return rc;
+    if (!h_index || (!h_data && data_size))
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "the quantization curve needs a compact image (index and data)");
+    if (coding_warp == MRAYGB_CODING_WARP_DEFAULT_TRANSFORMED && !h_coding_params)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "the default coding warp needs the coding parameters");
+    int sx, sy;
+    if ((rc = sample_shape(ctx, width, height, sampling, &sx, &sy)))
+        return rc;
+    // sample on the host (moment_image_sample.h:33-62 and MomentImageHost::compact) and move only the sample
+    const int fx = width / sx, fy = height / sy;
+    const size_t P = (size_t)sx * (size_t)sy;
+    std::vector<uint32_t> s_index(P + 1);
+    uint64_t total = 0;
+    for (int y = 0; y < sy; ++y)
+        for (int x = 0; x < sx; ++x)
+        {
+            const size_t src = (size_t)(y * fy) * (size_t)width + (size_t)(x * fx);
+            const uint32_t off = h_index[src], n = h_index[src + 1] - off;
+            if (h_index[src + 1] < off || n > (uint32_t)m || (uint64_t)off + n > data_size)
+                return fail(ctx, MRAYGB_INVALID_ARGUMENT, "pixel (%d, %d): moments [%u, %u) outside the %llu values",
+                            x * fx, y * fy, off, off + n, (unsigned long long)data_size);
+            s_index[(size_t)y * sx + x] = (uint32_t)total;
+            total += n;
+        }
+    s_index[P] = (uint32_t)total;
+    std::vector<float> s_data(total ? total : 1);
+    for (size_t s = 0; s < P; ++s)
+    {
+        const int x = (int)(s % sx), y = (int)(s / sx);
+        const size_t src = (size_t)(y * fy) * (size_t)width + (size_t)(x * fx);
+        std::memcpy(s_data.data() + s_index[s], h_data + h_index[src], (s_index[s + 1] - s_index[s]) * sizeof(float));
+    }
+    CK(ctx->qc_index.reserve((P + 1) * sizeof(uint32_t)), "sample index buffer");
+    CK(ctx->qc_data.reserve(s_data.size() * sizeof(float)), "sample data buffer");
+    CK(cudaMemcpyAsync(ctx->qc_index.ptr, s_index.data(), (P + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                       ctx->stream),
+       "sample index upload");
+    CK(cudaMemcpyAsync(ctx->qc_data.ptr, s_data.data(), s_data.size() * sizeof(float), cudaMemcpyHostToDevice,
+                       ctx->stream),
+       "sample data upload");
+    const uint16_t *d_cp = nullptr;
+    if (coding_warp == MRAYGB_CODING_WARP_DEFAULT_TRANSFORMED)
+    {
+        CK(ctx->coding_params.reserve(2 * (size_t)(m - 1) * sizeof(uint16_t)), "coding parameter buffer");
+        CK(cudaMemcpyAsync(ctx->coding_params.ptr, h_coding_params, 2 * (size_t)(m - 1) * sizeof(uint16_t),
+                           cudaMemcpyHostToDevice, ctx->stream),
+           "coding parameter upload");
+        d_cp = ctx->coding_params.as<uint16_t>();
+    }
+    return run_quant_table(ctx, sx, sy, m, ctx->qc_index.as<uint32_t>(), ctx->qc_data.as<float>(), coding_warp, d_cp,
+                           sx, sy, start_bits, h_table, h_means);
+}
+
 
 int mraygb_quantize_prediction_coding(mraygb_context *ctx, int width, int height, int m, const uint32_t *h_index,
                                       const float *h_data, uint64_t data_size, const uint8_t *h_table,

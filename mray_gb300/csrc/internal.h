@@ -68,6 +68,15 @@ cudaError_t launch_prepare(int num_pixels, int m, const uint32_t *index, const f
                            int coding_warp, const uint16_t *coding_params, float bias, bool fp64, float *pmoments,
                            cudaStream_t stream);
 
+// quant_curve.cu: the data-dependent quantization table's error means for every (index, bits) pair
+// scratch bytes for an sx x sy sample, bits bmin .. bmin + nb - 1, rows_per_pass moment indices per pass
+size_t quant_curve_scratch_bytes(int sx, int sy, int m, int nb, size_t rows_per_pass);
+// d_means[(idx - 1) * nb + (b - bmin)] for idx in [1, m): the mean rRMSE of quantizing moment idx to b bits
+cudaError_t launch_quant_curve(int width, int height, int m, const uint32_t *index, const float *data, int warp,
+                               const uint16_t *coding_params, int sx, int sy, int bmin, int nb,
+                               size_t rows_per_pass, void *scratch, float *d_means, cudaStream_t stream,
+                               int *launches);
+
 // scan.cu
 // exclusive scan of n u32 counts into out[0..n] (out[n] = total); scratch must hold scan_scratch_words(n)
 size_t scan_scratch_words(size_t n);

@@ -314,7 +314,41 @@ class Context:
                                                               _hptr(out), out.size, C.byref(n)))
         return out[:n.value]
 
+    def create_quantization_table(self, mi: MomentImageHost, start_bits: int, sampling: int = 0,
+                                  return_means: bool = False):
+        """create_quantization_table(img, start_bits) (measure_coding_error.cpp:374-438) on a compact
+        prediction-coded image; with ``sampling`` > 0 on its sample_moment_image (main.cpp:318-327).  Returns the
+        table (u8 per moment index) and, with ``return_means``, the mean rRMSE of every (index, bits) pair as an
+        (m, 32) array (NaN where not evaluated)."""
+        if not mi.is_compact or mi.index is None:
+            raise ValueError("create_quantization_table needs a compact moment image")
+        if not mi.prediction_code:
+            raise ValueError("create_quantization_table needs a prediction-coded moment image")
+        m = mi.num_moments
+        data = np.ascontiguousarray(mi.data, dtype=np.float32)
+        index = np.ascontiguousarray(mi.index, dtype=np.uint32)
+        cp = None if mi.coding_params is None else np.ascontiguousarray(mi.coding_params, dtype=np.uint16)
+        table = np.zeros(m, dtype=np.uint8)
+        means = np.zeros((m, 32), dtype=np.float32) if return_means else None
+        self._check(self._L.mraygb_create_quantization_table(self._h, mi.width, mi.height, m, _hptr(index),
+                                                             _hptr(data), data.size, int(mi.coding_warp), _hptr(cp),
+                                                             int(start_bits), int(sampling), _hptr(table),
+                                                             _hptr(means)))
+        return (table, means) if return_means else table
+
     # ---- stage calls on device pointers ----
+    def stage_create_quantization_table(self, width, height, num_moments, index, data, coding_warp, coding_params,
+                                        start_bits, sampling=64, return_means=False):
+        """mraygb_stage_create_quantization_table: the table (and the means) of a compact prediction-coded image
+        in device memory; see :meth:`create_quantization_table`."""
+        table = np.zeros(num_moments, dtype=np.uint8)
+        means = np.zeros((num_moments, 32), dtype=np.float32) if return_means else None
+        self._check(self._L.mraygb_stage_create_quantization_table(self._h, width, height, num_moments,
+                                                                   _dptr(index), _dptr(data), int(coding_warp),
+                                                                   _dptr(coding_params), int(start_bits),
+                                                                   int(sampling), _hptr(table), _hptr(means)))
+        return (table, means) if return_means else table
+
     def stage_generate_moments(self, cam, gp, width, height, num_moments, moments, bounds=None, counts=None):
         self._check(self._L.mraygb_stage_generate_moments(self._h, C.byref(cam), C.byref(gp), width, height,
                                                           num_moments, _dptr(moments), _dptr(bounds),
@@ -406,6 +440,15 @@ def generate(cam: Camera, volume, mi: MomentImageHost, params: GenerationParamet
 def quantize_prediction_coding(mi: MomentImageHost, table, context: Optional[Context] = None) -> np.ndarray:
     """moment_quantization::quantize_prediction_coding(mi, table) on the GPU."""
     return (context or default_context()).quantize_prediction_coding(mi, table)
+
+
+def create_quantization_table(img: MomentImageHost, start_bits: int, context: Optional[Context] = None,
+                              sampling: int = 0) -> np.ndarray:
+    """create_quantization_table(img, start_bits) (measure_coding_error.cpp:374-438): the data-dependent table
+    for a compact prediction-coded image.  The reference installs it as its global table; here it is returned for
+    :func:`quantize_prediction_coding`.  ``sampling`` > 0 first takes sample_moment_image(img, s, s) with
+    s = min(width, sampling) = min(height, sampling), as main.cpp:318-327 does with quantization_curve_sampling."""
+    return (context or default_context()).create_quantization_table(img, start_bits, sampling)
 
 
 def default_quantization_table(num_moments: int, num_bits: int) -> np.ndarray:

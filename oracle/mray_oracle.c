@@ -30,6 +30,12 @@ void oracle_euler_exp_f32(float x, float out[2])
 }
 #define ORACLE_EXP_F32(v) ((float)exp((double)(v)))
 
+/* cosf / sinf of transform_dequantization_real (moment_prediction_coding.h:103-104): the C library's (the
+ * reference's CPU build) by default; the correctly rounded values (the double functions rounded to float) when
+ * set, for checking a device implementation that rounds correctly operation by operation. */
+static int oracle_rounded_trig = 0;
+void oracle_set_rounded_trig(int on) { oracle_rounded_trig = on != 0; }
+
 /* UniformGridDevice::getIndexFromCell (particle_grid.cuh:64-83): 4x4x4 tiles (4x4x1 for a flat grid) */
 uint32_t oracle_particles_cell_index(const oracle_particles *p, int cx, int cy, int cz)
 {
@@ -323,6 +329,30 @@ float oracle_dequantize(uint32_t q, int num_bits, float vmin, float vmax)
     }
     float norm = (float)q / (float)((1 << num_bits) - 1);
     return norm * (vmax - vmin) + vmin;
+}
+
+/* sample_moment_image (moment_image_sample.h:33-62): the sample is a full image whose index holds the moment
+ * counts; compact() (moment_image.cpp:69-94) then turns the counts into offsets and packs the data. */
+uint64_t oracle_sample_moment_image(int width, int height, const uint32_t *index, const float *data, int s,
+                                    uint32_t *s_index, float *s_data)
+{
+    const int factor_x = width / s, factor_y = height / s;
+    uint32_t sum = 0;
+    for (int y = 0; y < s; ++y)
+    {
+        for (int x = 0; x < s; ++x)
+        {
+            size_t src = (size_t)(y * factor_y) * (size_t)width + (size_t)(x * factor_x);
+            uint32_t n = index[src + 1] - index[src];
+            s_index[y * s + x] = sum;
+            if (s_data)
+                for (uint32_t l = 0; l < n; ++l)
+                    s_data[(size_t)sum + l] = data[(size_t)index[src] + l];
+            sum += n;
+        }
+    }
+    s_index[(size_t)s * (size_t)s] = sum;
+    return sum;
 }
 
 void oracle_default_quantization_table(int m, int num_bits, uint8_t *table)

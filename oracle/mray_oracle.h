@@ -129,7 +129,14 @@ typedef struct oracle_options
     int oracle_intersect_aabb_##SFX(const R origin[3], const R dir[3], const float bmin[3], const float bmax[3],  \
                                     R *t_near, R *t_far);                                                          \
     void oracle_tf_sample_##SFX(const R *tf_table, R fs, R bs, R out[4]);                                           \
-    void oracle_tf_sample_bspline_##SFX(const R *tf_table, R fs, R out[4]);
+    void oracle_tf_sample_bspline_##SFX(const R *tf_table, R fs, R out[4]);                                         \
+    /* quantization curve (measure_coding_error.cpp:92-192, 357-438) on a compact prediction-coded image       */   \
+    R oracle_measure_idx_error_##SFX(int width, int height, int num_moments, const uint32_t *index, const R *data, \
+                                     int coding_warp, const uint16_t *coding_params, int idx, int b, R *errors,     \
+                                     uint32_t *size, int nthreads);                                                 \
+    int oracle_create_quantization_table_##SFX(int width, int height, int num_moments, const uint32_t *index,      \
+                                               const R *data, int coding_warp, const uint16_t *coding_params,       \
+                                               int start_bits, uint8_t *table, R *means, int nthreads);
 
 ORACLE_DECL(float, f32)
 ORACLE_DECL(double, f64)
@@ -166,6 +173,14 @@ uint64_t oracle_quantize_prediction_coding(int width, int height, int num_moment
 void oracle_dequantize_prediction_coding(int width, int height, int num_moments, const uint32_t *index,
                                          const uint8_t *table, const uint8_t *bytes, uint64_t num_bytes,
                                          float *data);
+/* Test switch: cosf / sinf of the f32 prediction-coding dequantization from the C library (0, the default, as the
+ * reference's CPU build) or correctly rounded (1). */
+void oracle_set_rounded_trig(int on);
+/* sample_moment_image (moment_image_sample.h:33-62) followed by MomentImageHost::compact (moment_image.cpp:69-94)
+ * for a compact image: pixel (x, y) of the s x s sample is pixel (x * (W / s), y * (H / s)) of the image.
+ * s_index[s*s+1]; s_data may be NULL to query the compact size, which is returned. */
+uint64_t oracle_sample_moment_image(int width, int height, const uint32_t *index, const float *data, int s,
+                                    uint32_t *s_index, float *s_data);
 /* get_prediction_coding_quantization_table default (moment_quantization.cpp:186-203). */
 void oracle_default_quantization_table(int num_moments, int num_bits, uint8_t *table);
 

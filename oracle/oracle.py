@@ -150,6 +150,20 @@ def _declare(L):
                                                       C.c_void_p, C.c_uint64, C.c_void_p]
     L.oracle_preintegrate.argtypes = [C.c_void_p, C.c_float, C.c_void_p]
     L.oracle_rgba_to_u8.argtypes = [C.c_uint64, C.c_void_p, C.c_void_p]
+    L.oracle_set_rounded_trig.argtypes = [C.c_int]
+    L.oracle_set_rounded_trig.restype = None
+    L.oracle_sample_moment_image.restype = C.c_uint64
+    L.oracle_sample_moment_image.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
+                                             C.c_void_p]
+    for sfx, R in (("f32", C.c_float), ("f64", C.c_double)):
+        f = getattr(L, f"oracle_measure_idx_error_{sfx}")
+        f.restype = R
+        f.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int,
+                      C.c_void_p, C.c_void_p, C.c_int]
+        f = getattr(L, f"oracle_create_quantization_table_{sfx}")
+        f.restype = C.c_int
+        f.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p,
+                      C.c_void_p, C.c_int]
 
 
 def _ptr(a):
@@ -290,6 +304,67 @@ def dequantize_prediction_coding(width, height, m, index, table, packed, size):
 
 def default_quantization_table(m, bits):
     return np.array([16] + [bits] * (m - 1), dtype=np.uint8)[:m]
+
+
+class rounded_trig:
+    """Within the block, the f32 prediction-coding dequantization takes correctly rounded cos / sin instead of the
+    C library's cosf / sinf (for comparing a device implementation operation by operation)."""
+
+    def __enter__(self):
+        lib().oracle_set_rounded_trig(1)
+        return self
+
+    def __exit__(self, *exc):
+        lib().oracle_set_rounded_trig(0)
+
+
+def sample_moment_image(width, height, index, data, s):
+    """sample_moment_image(img, s, s) + compact on a compact image: returns (index[s*s+1], data)."""
+    L = lib()
+    idx = np.ascontiguousarray(index, dtype=np.uint32)
+    d = np.ascontiguousarray(data, dtype=np.float32)
+    s_index = np.zeros(s * s + 1, dtype=np.uint32)
+    n = int(L.oracle_sample_moment_image(width, height, _ptr(idx), _ptr(d), s, _ptr(s_index), None))
+    s_data = np.zeros(max(n, 1), dtype=np.float32)
+    L.oracle_sample_moment_image(width, height, _ptr(idx), _ptr(d), s, _ptr(s_index), _ptr(s_data))
+    return s_index, s_data[:n]
+
+
+def _coding_params(cp, m):
+    return None if cp is None else np.ascontiguousarray(cp, dtype=np.uint16)[:2 * (m - 1)]
+
+
+def measure_idx_error(width, height, m, index, data, coding_warp, coding_params, idx, b, precision="f32",
+                      nthreads=0):
+    """measure_idx_error on a compact prediction-coded image: (mean rRMSE, per-pixel rRMSE of the non-empty
+    pixels in row-major order) for moment idx quantized to b bits (idx < 0: nothing quantized)."""
+    L = lib()
+    dt = _dt(precision)
+    idx_a = np.ascontiguousarray(index, dtype=np.uint32)
+    d = np.ascontiguousarray(data, dtype=dt)
+    cp = _coding_params(coding_params, m)
+    errors = np.zeros(max(int(np.count_nonzero(np.diff(idx_a.astype(np.int64)))), 1), dtype=dt)
+    size = C.c_uint32()
+    mean = getattr(L, f"oracle_measure_idx_error_{precision}")(width, height, m, _ptr(idx_a), _ptr(d), coding_warp,
+                                                               _ptr(cp), idx, b, _ptr(errors), C.byref(size),
+                                                               nthreads)
+    return float(mean), errors[:size.value]
+
+
+def create_quantization_table(width, height, m, index, data, coding_warp, coding_params, start_bits,
+                              precision="f32", nthreads=0):
+    """create_quantization_table on a compact prediction-coded image: returns (table[m] u8, means[m, 32] of the
+    evaluations the search made (NaN elsewhere), number of evaluations)."""
+    L = lib()
+    dt = _dt(precision)
+    table = np.zeros(m, dtype=np.uint8)
+    means = np.zeros((m, 32), dtype=dt)
+    cp = _coding_params(coding_params, m)
+    n = getattr(L, f"oracle_create_quantization_table_{precision}")(
+        width, height, m, _ptr(np.ascontiguousarray(index, dtype=np.uint32)),
+        _ptr(np.ascontiguousarray(data, dtype=dt)), coding_warp, _ptr(cp), start_bits, _ptr(table), _ptr(means),
+        nthreads)
+    return table, means, int(n)
 
 
 def prepare_moments(width, height, m, index, data, prediction_code=False, coding_warp=0, coding_params=None,

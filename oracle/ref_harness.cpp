@@ -15,6 +15,7 @@
 #include "raymarch_reconstruct.h"
 #include "moment_compaction.h"
 #include "moment_image.h"
+#include "moment_image_sample.h"
 #include "moment_quantization.h"
 #include "coding_transform.h"
 #include "moment_prediction_coding.h"
@@ -307,6 +308,67 @@ uint64_t ref_quantize_prediction_coding(int w, int h, int m, const uint32_t *ind
     if (out)
         std::memcpy(out, bytes.data(), bytes.size());
     return bytes.size();
+}
+
+/* sample_moment_image (moment_image_sample.h:33-62) of a compact image: s x s pixels.  s_index receives s*s+1
+ * offsets, s_data (may be nullptr) the compact data; returns the data size. */
+uint64_t ref_sample_moment_image(int w, int h, int m, const uint32_t *index, const float *data, uint64_t data_size,
+                                 int s, uint32_t *s_index, float *s_data)
+{
+    auto mi = make_mi(w, h, m, index, data, data_size, nullptr, 1, 0, nullptr, nullptr, nullptr);
+    auto simg = sample_moment_image(mi, s, s);
+    std::memcpy(s_index, simg.index.data(), sizeof(uint32_t) * simg.index.size());
+    if (s_data)
+        std::memcpy(s_data, simg.data.data(), sizeof(float) * simg.data.size());
+    return simg.data.size();
+}
+
+/* Per-pixel rRMSE of compute_coding_error (measure_coding_error.cpp:143-182) against compute_reference
+ * (:92-141) for the image whose moment idx is quantized to b bits (apply_quantization, :41-66; idx < 0: none),
+ * evaluated with the reference's MomentImageHost, transform_dequantization_real, decode and
+ * exponentialToTrigonometricMoments.  measure_coding_error.cpp itself includes the HDF5 headers and is not
+ * compiled here, so its two loops are spelled out below around those calls.  errors[i] belongs to the i-th
+ * non-empty pixel in row-major order; returns the number of non-empty pixels. */
+uint32_t ref_coding_errors(int w, int h, int m, const uint32_t *index, const float *data, uint64_t data_size,
+                           int warp, const uint16_t *coding_params, int idx, int b, float *errors)
+{
+    auto mi = make_mi(w, h, m, index, data, data_size, nullptr, 1, warp, coding_params, nullptr, nullptr);
+    const std::vector<float> params = mi.get_coding_params();
+    auto trig = [&](const float *in, int n, std::vector<float> &out) {
+        std::vector<float_complex> code(n), e(n), poly(n), tmp(n);
+        transform_dequantization_real(n, in, code.data(), WarpParameters{mi.coding_warp, params.data()});
+        decode(n, code.data(), e.data(), poly.data(), tmp.data());
+        exponentialToTrigonometricMoments(n, tmp.data(), e.data());
+        out.resize(n);
+        for (int l = 0; l < n; ++l)
+            out[l] = tmp[l].x;
+    };
+    uint32_t k = 0;
+    std::vector<float> ref, q, in;
+    for (int y = 0; y < h; ++y)
+        for (int x = 0; x < w; ++x)
+        {
+            int n = mi.get_num_moments(x, y);
+            if (n <= 0)
+                continue;
+            const float *src = &mi.data[mi.get_idx(x, y)];
+            trig(src, n, ref);
+            in.assign(src, src + n);
+            if (idx >= 0 && n > idx)
+            {
+                float p = std::pow(2.0f, float(b));
+                in[idx] = std::floor(in[idx] * p) / p;
+            }
+            trig(in.data(), n, q);
+            float sum = 0.0f;
+            for (int l = 0; l < n; ++l)
+            {
+                float diff = ref[l] - q[l];
+                sum += diff * diff;
+            }
+            errors[k++] = sqrtf(sum) / ref[0];
+        }
+    return k;
 }
 
 /* ---- MESE primitives (mese/MESE_dynamic.h) ---- */

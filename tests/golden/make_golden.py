@@ -16,6 +16,11 @@ on seeded inputs and stores inputs and outputs as small .npz files:
   particles.npz       Particles::sample and generate() over SPH particles: a jittered lattice with one particle
                       per grid cell (so the reference's unstable sort by cell cannot change the summation order)
                       and a clustered set
+  quant_curve.npz     prediction-coded images from generate() (one with error-threshold compaction), their
+                      sample_moment_image and the per-pixel rRMSE of compute_coding_error for several (index, bits)
+                      pairs (measure_coding_error.cpp needs HDF5, so the harness composes its loop from the
+                      reference's own sample_moment_image, transform_dequantization_real, decode and
+                      exponentialToTrigonometricMoments)
 
 Run from the repository root:  python tests/golden/make_golden.py
 """
@@ -54,6 +59,10 @@ def declare(ref):
     ref.ref_particles_sample.argtypes = [vp, vp, vp, vp, u64, f, vp, vp, vp, u64, vp]
     ref.ref_generate_particles.argtypes = [vp, vp, vp, vp, vp, vp, u64, f, vp, vp, C.c_int, C.c_int, C.c_int, vp, vp,
                                            vp, vp]
+    ref.ref_sample_moment_image.restype = u64
+    ref.ref_sample_moment_image.argtypes = [C.c_int, C.c_int, C.c_int, vp, vp, u64, C.c_int, vp, vp]
+    ref.ref_coding_errors.restype = C.c_uint32
+    ref.ref_coding_errors.argtypes = [C.c_int, C.c_int, C.c_int, vp, vp, u64, C.c_int, vp, C.c_int, C.c_int, vp]
     ref.ref_evaluate_mese.restype = C.c_float
     ref.ref_evaluate_mese.argtypes = [C.c_int, C.c_float, C.c_void_p]
     ref.ref_fixed_evaluate_lagrange.restype = C.c_float
@@ -373,6 +382,53 @@ def quantize(ref):
     return out
 
 
+QC_PAIRS = [(1, 10), (2, 10), (3, 9), (7, 6), (15, 4), (30, 3), (63, 2), (5, 16), (-1, 0)]
+
+
+def _qc_image(ref, wl):
+    Wd, H, m = wl.width, wl.height, wl.num_moments
+    vol = np.ascontiguousarray(wl.volume)
+    nz, ny, nx = vol.shape
+    dmin, dmax = f32(*wl.domain_min), f32(*wl.domain_max)
+    data = np.zeros(Wd * H * m, np.float32)
+    index = np.zeros(Wd * H + 1, np.uint32)
+    bounds = np.zeros(2 * Wd * H, np.uint16)
+    cp = np.zeros(2 * m, np.uint16)
+    size = C.c_uint64()
+    flags = np.zeros(4, np.int32)
+    ref.ref_generate_grid(C.byref(wl.camera), C.byref(wl.gen), P(vol), nx, ny, nz, P(dmin), P(dmax), Wd, H, m,
+                          P(data), P(index), P(bounds), P(cp), C.byref(size), P(flags))
+    return index, data[:size.value].copy(), cp[:2 * (m - 1)].copy()
+
+
+def quant_curve(ref):
+    """Prediction-coded images from the reference's generate, their sample_moment_image and the per-pixel rRMSE
+    of compute_coding_error for a set of (index, bits) pairs, from the reference's own building blocks."""
+    out = {}
+    mix = W.mixing_layer_workload(n=40, width=32, height=32, num_moments=64, modes=16, seed=5, name="golden_mix")
+    ml = W.ml_workload(n=64, width=48, height=48, num_moments=24, seed=11, name="golden_ml_thr")
+    ml.gen.error_threshold = 5e-2  # error-threshold compaction: ragged moment counts (2 .. 22)
+    for key, wl, s in (("mix", mix, 16), ("mlthr", ml, 24)):
+        wl.gen.prediction_coding = 1
+        Wd, H, m = wl.width, wl.height, wl.num_moments
+        index, data, cp = _qc_image(ref, wl)
+        out[f"{key}_shape"] = np.array([Wd, H, m, s], np.int32)
+        out[f"{key}_index"], out[f"{key}_data"], out[f"{key}_coding_params"] = index, data, cp
+        s_index = np.zeros(s * s + 1, np.uint32)
+        n = ref.ref_sample_moment_image(Wd, H, m, P(index), P(data), data.size, s, P(s_index), None)
+        s_data = np.zeros(max(n, 1), np.float32)
+        ref.ref_sample_moment_image(Wd, H, m, P(index), P(data), data.size, s, P(s_index), P(s_data))
+        out[f"{key}_s_index"], out[f"{key}_s_data"] = s_index, s_data[:n]
+        nonempty = int(np.count_nonzero(np.diff(s_index.astype(np.int64))))
+        for idx, b in QC_PAIRS:
+            if idx >= m:
+                continue
+            e = np.zeros(max(nonempty, 1), np.float32)
+            k = ref.ref_coding_errors(s, s, m, P(s_index), P(s_data), n, 0, P(cp), idx, b, P(e))
+            out[f"{key}_err_{idx}_{b}"] = e[:k]
+    return out
+
+
 def main():
     ref = O.ref_lib()
     if ref is None:
@@ -386,6 +442,7 @@ def main():
     np.savez_compressed(os.path.join(HERE, "pipeline_mix.npz"), **pipeline(ref, mix))
     np.savez_compressed(os.path.join(HERE, "quantize.npz"), **quantize(ref))
     np.savez_compressed(os.path.join(HERE, "particles.npz"), **particles(ref))
+    np.savez_compressed(os.path.join(HERE, "quant_curve.npz"), **quant_curve(ref))
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

@@ -5,7 +5,9 @@ moments, prediction coding, 10-bit codes): checks that do not need the oracle to
   and compaction counts there are exact, the moments within 1e-4 of the FP64 evaluation;
 * codes: the oracle's quantizer and bit packer applied to the GPU's prediction-coded floats of the whole image
   give the GPU's bytes, bit for bit, and unpacking them gives the same floats on both sides;
-* compaction: the index is the exclusive scan of the counts, every non-empty pixel keeps all 64 moments.
+* compaction: the index is the exclusive scan of the counts, every non-empty pixel keeps all 64 moments;
+* the data-dependent quantization table of the 64 x 64 sample (quantization_curve_sampling's default) equals the
+  oracle's.
 """
 import numpy as np
 import pytest
@@ -55,6 +57,7 @@ def large(gpu_context):
     ctx.stage_dequantize_prediction_coding(WIDTH, HEIGHT, m, d_idx, table, d_codes, nbytes, d_deq)
     ctx.synchronize()
     out = dict(gen=gen, cam=cam, vol=vol_host, dmin=dmin, dmax=dmax, table=table, total=total,
+               d_index=d_idx, d_coded=d_cm, d_coding_params=d_cp, coding_params=d_cp.cpu().numpy().view(np.uint16),
                moments=d_mo.cpu().numpy().reshape(HEIGHT, WIDTH, m),
                bounds=d_b.cpu().numpy().view(np.uint16).reshape(HEIGHT, WIDTH, 2),
                counts=d_c.cpu().numpy().view(np.uint32).reshape(HEIGHT, WIDTH),
@@ -98,3 +101,22 @@ def test_large_codes_bit_exact(large):
     assert np.array_equal(deq, g["dequantized"])
     again = O.quantize_prediction_coding(WIDTH, HEIGHT, M_MOM, g["index"], g["dequantized"], g["table"])
     assert np.array_equal(again, g["codes"])
+
+
+def test_large_quantization_table(large, gpu_context):
+    """create_quantization_table on the sample_moment_image(64, 64) of the full prediction-coded image."""
+    g = large
+    d_coded = g["d_coded"]
+    table, means = gpu_context.stage_create_quantization_table(WIDTH, HEIGHT, M_MOM, g["d_index"], d_coded, 0,
+                                                               g["d_coding_params"], 10, sampling=64,
+                                                               return_means=True)
+    s_index, s_data = O.sample_moment_image(WIDTH, HEIGHT, g["index"], g["coded"], 64)
+    with O.rounded_trig():  # the device's rounding of the first code: the same means, bit for bit
+        cr_table, cr_means, _ = O.create_quantization_table(64, 64, M_MOM, s_index, s_data, 0, g["coding_params"], 10)
+    seen = np.isfinite(cr_means)
+    assert np.array_equal(means[seen], cr_means[seen])
+    ref_table, ref_means, _ = O.create_quantization_table(64, 64, M_MOM, s_index, s_data, 0, g["coding_params"], 10)
+    seen = np.isfinite(ref_means)
+    rel = np.abs(means[seen].astype(np.float64) - ref_means[seen]) / np.abs(ref_means[seen])
+    assert rel.max() <= 1e-5, f"max rel diff of the means {rel.max():.2e}"  # 10 bits
+    assert table.tolist() == ref_table.tolist() == cr_table.tolist()

@@ -357,3 +357,62 @@ def test_particles_clustered_within_summation_order():
     assert np.array_equal(index, g["cluster_index"])
     assert np.max(np.abs(bounds.astype(np.int64) - g["cluster_bounds"].astype(np.int64))) <= 1
     assert np.allclose(data, g["cluster_data"], rtol=0, atol=2e-5)
+
+
+# ---- the data-dependent quantization curve (measure_coding_error.cpp) --------------------------------------------
+
+def _sequential_mean(values):
+    """get_mean (measure_coding_error.cpp:184-192): a float running sum divided by the count."""
+    acc = np.float32(0)
+    for v in values:
+        acc = np.float32(acc + v)
+    return np.float32(acc / np.float32(len(values)))
+
+
+@pytest.mark.parametrize("key", ["mix", "mlthr"])
+def test_quant_curve_sample_and_errors_bit_exact(key):
+    g = load("quant_curve.npz")
+    Wd, H, m, s = (int(v) for v in g[f"{key}_shape"])
+    s_index, s_data = O.sample_moment_image(Wd, H, g[f"{key}_index"], g[f"{key}_data"], s)
+    assert np.array_equal(s_index, g[f"{key}_s_index"])
+    assert np.array_equal(s_data, g[f"{key}_s_data"])
+    counts = np.diff(s_index.astype(np.int64))
+    if key == "mlthr":  # error-threshold compaction leaves ragged moment counts
+        assert len(set(counts[counts > 0].tolist())) > 3
+    checked = 0
+    for name in g.files:
+        if not name.startswith(f"{key}_err_"):
+            continue
+        idx, b = (int(v) for v in name.split("_")[-2:])
+        mean, errors = O.measure_idx_error(s, s, m, s_index, s_data, 0, g[f"{key}_coding_params"], idx, b)
+        assert np.array_equal(errors, g[name]), name
+        assert np.float32(mean) == _sequential_mean(g[name]), name
+        checked += 1
+    assert checked >= 7
+
+
+def test_quant_curve_search_rule():
+    """The table is create_quantization_table's search (measure_coding_error.cpp:400-435) over the means the oracle
+    evaluated: [16, start_bits, ...]; each later index starts at the previous index's bits and steps down to 2 bits
+    while the mean rRMSE stays below the threshold (the mean of index 1 at start_bits)."""
+    g = load("quant_curve.npz")
+    Wd, H, m, s = (int(v) for v in g["mix_shape"])
+    for start_bits in (10, 6):
+        table, means, evals = O.create_quantization_table(s, s, m, g["mix_s_index"], g["mix_s_data"], 0,
+                                                          g["mix_coding_params"], start_bits)
+        assert table[0] == 16 and table[1] == start_bits
+        thr = means[1, start_bits]
+        assert np.isfinite(thr) and thr > 0
+        expect, visited = [16, start_bits], 1
+        for idx in range(2, m):
+            t = expect[-1]
+            for b in range(expect[-1], 1, -1):
+                visited += 1
+                assert np.isfinite(means[idx, b]), (idx, b)
+                if means[idx, b] >= thr:
+                    break
+                t = b
+            expect.append(t)
+        assert table.tolist() == expect
+        assert evals == visited == np.count_nonzero(np.isfinite(means))
+        assert 2 <= table[-1] < start_bits  # the curve does go down on this image
