@@ -701,6 +701,8 @@ def run_large(args, local):
         out[name] = {"value": P / (ms * 1e-3) / 1e6, "unit": UNIT, "ms": ms}
     out["compact_moments"], out["code_bytes"] = int(sizes["moments"]), int(sizes["code_bytes"])
     ctx.precision = M.PRECISION_FP32
+    out["quantization_table"] = quantization_table_timing(args, ctx, cam, gen, Wd, H, m, d_mo, d_b, d_c, d_idx,
+                                                          d_cm, d_cp, steps)
     del d_cm, d_codes
     # the differentiation form with the transfer-function adjoint
     gen.compact_image, gen.prediction_coding = 0, 0
@@ -720,6 +722,49 @@ def run_large(args, local):
     out["diff_fwd_tf_adjoint"] = {"value": P / (ms * 1e-3) / 1e6, "unit": UNIT, "ms": ms}
     ctx.close()
     return out
+
+
+def quantization_table_timing(args, ctx, cam, gen, Wd, H, m, d_mo, d_b, d_c, d_idx, d_cm, d_cp, steps):
+    """The data-dependent quantization table of the generate flow (create_quantization_table on the 64 x 64
+    sample_moment_image, main.cpp:318-327) for the prediction-coded image: the stage call's wall time (launches,
+    the read-back of the means and the search), and the oracle's sequential search on the same sample on the
+    host cores (the reference's CPU path; its OpenMP loops over the sample's pixels)."""
+    import torch
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    ctx.stage_generate_moments(cam, gen, Wd, H, m, d_mo, d_b, d_c)
+    total = ctx.stage_compact(Wd, H, m, d_c, d_mo, d_idx, d_cm)
+    ctx.stage_prediction_encode(Wd, H, m, d_idx, d_cm, total, 0, gen.bias, d_cp)
+    ctx.synchronize()
+    launches0 = ctx.kernel_launches
+    times = []
+    for i in range(args.warmup + steps):
+        t0 = time.perf_counter()
+        table = ctx.stage_create_quantization_table(Wd, H, m, d_idx, d_cm, 0, d_cp, 10, sampling=64)
+        if i >= args.warmup:
+            times.append((time.perf_counter() - t0) * 1e3)
+    launches = (ctx.kernel_launches - launches0) // (args.warmup + steps)
+    # the sample on the host for the oracle: offsets of the sampled pixels, their moments gathered on the device
+    s = 64
+    index = d_idx.cpu().numpy().view(np.uint32)
+    src = (np.arange(s)[:, None] * (H // s) * Wd + np.arange(s)[None, :] * (Wd // s)).reshape(-1)
+    off, cnt = index[src].astype(np.int64), (index[src + 1] - index[src]).astype(np.int64)
+    s_index = np.zeros(s * s + 1, np.uint32)
+    s_index[1:] = np.cumsum(cnt)
+    gather = np.concatenate([np.arange(o, o + c) for o, c in zip(off, cnt)]) if cnt.sum() else np.zeros(0, np.int64)
+    s_data = d_cm[torch.from_numpy(gather).cuda()].cpu().numpy() if gather.size else np.zeros(0, np.float32)
+    cp = d_cp.cpu().numpy().view(np.uint16)[:2 * (m - 1)]
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    ref_table, _, evals = O.create_quantization_table(s, s, m, s_index, s_data, 0, cp, 10, nthreads=threads)
+    cpu_ms = (time.perf_counter() - t0) * 1e3
+    return {"sample": f"{s}x{s} of {Wd}x{H}", "start_bits": 10, "ms": statistics.mean(times),
+            "gpu_launches": int(launches), "table_bits_per_pixel": int(table.astype(np.int64).sum()),
+            "table_equals_oracle": bool(table.tolist() == ref_table.tolist()),
+            "cpu_oracle": {"ms": cpu_ms, "threads": threads, "evaluations": evals,
+                           "kind": "port (sequential search of measure_coding_error.cpp:374-438)"}}
 
 
 def precision_errors(args, local):

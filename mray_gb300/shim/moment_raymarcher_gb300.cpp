@@ -7,6 +7,7 @@
 // Compiled against the reference's headers only (tests/test_shim_compiles.py checks that it compiles).
 
 #include "moment_raymarcher.cuh"
+#include "moment_quantization.h"
 
 #include <cstdio>
 #include <exception>
@@ -190,4 +191,23 @@ void reconstruct_device(cut::Camera cam, const MomentImageHost &mi, const Transf
                              bounds.empty() ? nullptr : bounds.data(), mi.prediction_code, mi.coding_warp,
                              cp.empty() ? nullptr : cp.data(), nullptr,
                              reinterpret_cast<uint8_t *>(cimg.rgba.data())));
+}
+
+// create_quantization_table (src/measure_coding_error.cpp:374-438) over the C ABI: the same table for the same
+// (already sampled) image, installed as the reference's global prediction-coding table.  measure_coding_error.cpp
+// also holds the offline curve study that main.cpp:770 calls, so this is a second name: main.cpp:322 calls it in
+// place of create_quantization_table.
+void create_quantization_table_gb300(const MomentImageHost &img, int start_bits)
+{
+    std::vector<uint16_t> cp;
+    for (const auto &p : img.coding_params)
+    {
+        cp.push_back(p.param1);
+        cp.push_back(p.param2);
+    }
+    std::vector<Byte> table(img.num_moments);
+    check(mraygb_create_quantization_table(context(), img.width, img.height, img.num_moments, img.index.data(),
+                                           img.data.data(), img.data.size(), img.coding_warp,
+                                           cp.empty() ? nullptr : cp.data(), start_bits, 0, table.data(), nullptr));
+    moment_quantization::set_prediction_coding_quantization_table(table);
 }
