@@ -7,6 +7,8 @@
  *   mraygb_camera                 <- cut::Camera            (src/cut/camera.h:39-55)
  *   mraygb_generation_params      <- GenerationParameters   (src/parameters.h:49-70)
  *   mraygb_reconstruction_params  <- ReconstructionParameters (src/parameters.h:231-247)
+ *   mraygb_error_params           <- ErrorReconstructionParameters (src/parameters.h:124-137)
+ *   mraygb_uncertainty_params     <- UncertaintyReconstructionParameters (src/parameters.h:319-325)
  *
  * C++ `bool` members are stored as uint8_t (same size and alignment under the
  * Itanium and AAPCS64 ABIs).  No CUDA or torch types appear here.
@@ -74,6 +76,37 @@ typedef struct mraygb_reconstruction_params
     uint8_t ss_enable;             /* 0 (must be 0) */
     uint8_t pad0[2];
 } mraygb_reconstruction_params;
+
+/* Error measures of the per-pixel error bound (src/common.h:152-157). */
+enum
+{
+    MRAYGB_ERROR_MAX = 0,
+    MRAYGB_ERROR_RMSE = 1,
+    MRAYGB_ERROR_PERCENTILE = 2
+};
+
+/* ErrorReconstructionParameters (src/parameters.h:124-137), same defaults. */
+typedef struct mraygb_error_params
+{
+    int32_t error_type;       /* 2 = MRAYGB_ERROR_PERCENTILE */
+    int32_t error_percentile; /* 90 */
+    float bias;               /* 1e-6 */
+    float data_min;           /* 0.0 */
+    float data_max;           /* 1.0 */
+    float step_size;          /* 0.01 */
+    uint8_t compress;         /* 0 (file format; not on this path) */
+    uint8_t entropy_coding;   /* 0 (file format; not on this path) */
+    uint8_t quantization_bits; /* 32 (file format; not on this path) */
+    uint8_t pad0[1];
+} mraygb_error_params;
+
+/* UncertaintyReconstructionParameters (src/parameters.h:319-325), same defaults. */
+typedef struct mraygb_uncertainty_params
+{
+    mraygb_reconstruction_params rec;
+    float bound_interpolation; /* 0.5 */
+    int32_t error_type;        /* 1 = MRAYGB_ERROR_RMSE */
+} mraygb_uncertainty_params;
 
 /* Coding warps (src/coding_params.h:35-42). */
 enum

@@ -16,6 +16,10 @@ import numpy as np
 
 CODING_WARP_DEFAULT_TRANSFORMED = 0
 CODING_WARP_NONE = 1
+# error measures of the per-pixel error bound (common.h:152-157)
+MAX_ERROR = 0
+RMSE = 1
+ERROR_PERCENTILE = 2
 
 
 class Camera(C.Structure):
@@ -148,6 +152,60 @@ class ReconstructionParameters(C.Structure):
         self.step_size_write_samples = 1.5
         self.use_truncated_fourier = 0
         self.ss_enable = 0
+        for k, v in kw.items():
+            if not hasattr(self, k):
+                raise AttributeError(k)
+            setattr(self, k, v)
+
+
+class ErrorReconstructionParameters(C.Structure):
+    """``ErrorReconstructionParameters`` (parameters.h:124-137) with the reference's defaults; the file-format
+    fields (compress, entropy_coding, quantization_bits) are carried but not used on this path."""
+
+    _fields_ = [
+        ("error_type", C.c_int32),
+        ("error_percentile", C.c_int32),
+        ("bias", C.c_float),
+        ("data_min", C.c_float),
+        ("data_max", C.c_float),
+        ("step_size", C.c_float),
+        ("compress", C.c_uint8),
+        ("entropy_coding", C.c_uint8),
+        ("quantization_bits", C.c_uint8),
+        ("pad0", C.c_uint8 * 1),
+    ]
+
+    def __init__(self, **kw):
+        super().__init__()
+        self.error_type = ERROR_PERCENTILE
+        self.error_percentile = 90
+        self.bias = 1e-6
+        self.data_min = 0.0
+        self.data_max = 1.0
+        self.step_size = 0.01
+        self.compress = 0
+        self.entropy_coding = 0
+        self.quantization_bits = 32
+        for k, v in kw.items():
+            if not hasattr(self, k):
+                raise AttributeError(k)
+            setattr(self, k, v)
+
+
+class UncertaintyReconstructionParameters(C.Structure):
+    """``UncertaintyReconstructionParameters`` (parameters.h:319-325) with the reference's defaults."""
+
+    _fields_ = [
+        ("rec", ReconstructionParameters),
+        ("bound_interpolation", C.c_float),
+        ("error_type", C.c_int32),
+    ]
+
+    def __init__(self, **kw):
+        super().__init__()
+        self.rec = ReconstructionParameters()
+        self.bound_interpolation = 0.5
+        self.error_type = RMSE
         for k, v in kw.items():
             if not hasattr(self, k):
                 raise AttributeError(k)

@@ -136,7 +136,22 @@ typedef struct oracle_options
                                      uint32_t *size, int nthreads);                                                 \
     int oracle_create_quantization_table_##SFX(int width, int height, int num_moments, const uint32_t *index,      \
                                                const R *data, int coding_warp, const uint16_t *coding_params,       \
-                                               int start_bits, uint8_t *table, R *means, int nthreads);
+                                               int start_bits, uint8_t *table, R *means, int nthreads);     \
+    /* error bounds and uncertainty rendering (moment_raymarcher.cpp:516-706)                                */    \
+    void oracle_reconstruct_error_##SFX(const mraygb_camera *cam, const mraygb_error_params *ep,                  \
+                                        const oracle_grid *grid, const oracle_particles *parts, int width,         \
+                                        int height, int num_moments, const uint32_t *index, const R *data,          \
+                                        int prediction_code, int coding_warp, const uint16_t *coding_params,        \
+                                        const uint16_t *bounds, R *errors, uint16_t *error_bounds,                  \
+                                        const oracle_options *opt);                                                  \
+    void oracle_uncertainty_tf_##SFX(const R *tf1d, float step_size, int error_type, R *table);                  \
+    void oracle_reconstruct_uncertainty_##SFX(const mraygb_camera *cam, const mraygb_uncertainty_params *up,      \
+                                              int mode, int width, int height, int num_moments,                    \
+                                              const float domain_min[3], const float domain_max[3],                \
+                                              const uint32_t *index, const R *data, int prediction_code,           \
+                                              int coding_warp, const uint16_t *coding_params,                      \
+                                              const uint16_t *bounds, const uint16_t *error_bounds, const R *T,    \
+                                              R *rgba, const oracle_options *opt);
 
 ORACLE_DECL(float, f32)
 ORACLE_DECL(double, f64)

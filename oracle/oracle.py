@@ -150,6 +150,14 @@ def _declare(L):
                                                       C.c_void_p, C.c_uint64, C.c_void_p]
     L.oracle_preintegrate.argtypes = [C.c_void_p, C.c_float, C.c_void_p]
     L.oracle_rgba_to_u8.argtypes = [C.c_uint64, C.c_void_p, C.c_void_p]
+    for sfx in ("f32", "f64"):
+        getattr(L, f"oracle_reconstruct_error_{sfx}").argtypes = [
+            C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
+            C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        getattr(L, f"oracle_uncertainty_tf_{sfx}").argtypes = [C.c_void_p, C.c_float, C.c_int, C.c_void_p]
+        getattr(L, f"oracle_reconstruct_uncertainty_{sfx}").argtypes = [
+            C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float * 3, C.c_float * 3, C.c_void_p,
+            C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     L.oracle_set_rounded_trig.argtypes = [C.c_int]
     L.oracle_set_rounded_trig.restype = None
     L.oracle_sample_moment_image.restype = C.c_uint64
@@ -400,6 +408,62 @@ def reconstruct(cam, rp, width, height, m, dmin, dmax, index, pmoments, bounds, 
     getattr(L, f"oracle_reconstruct_{precision}")(C.byref(cam), C.byref(rp), width, height, m,
                                                   (C.c_float * 3)(*dmin), (C.c_float * 3)(*dmax), _ptr(idx),
                                                   _ptr(pm), _ptr(b), _ptr(t), _ptr(out), C.byref(o))
+    return out
+
+
+def reconstruct_error(cam, ep, volume, dmin, dmax, width, height, m, index, data, prediction_code=False,
+                      coding_warp=0, coding_params=None, bounds=None, precision="f32", nthreads=0, rows=None,
+                      particles=None):
+    """reconstruct_error_host: per pixel the error measure of the MESE reconstruction against the volume (a grid,
+    or ``particles`` when given).  Returns (errors[H,W] in the working precision, error bounds[H,W] u16)."""
+    L = lib()
+    dt = _dt(precision)
+    g, keep = (_grid(volume, dmin, dmax) if particles is None else (None, None))
+    idx = None if index is None else np.ascontiguousarray(index, dtype=np.uint32)
+    d = np.ascontiguousarray(data, dtype=dt)
+    cp = None if coding_params is None else np.ascontiguousarray(coding_params, dtype=np.uint16)
+    b = None if bounds is None else np.ascontiguousarray(bounds, dtype=np.uint16)
+    errors = np.zeros((height, width), dtype=dt)
+    eb = np.zeros((height, width), dtype=np.uint16)
+    o = options(nthreads, rows)
+    getattr(L, f"oracle_reconstruct_error_{precision}")(
+        C.byref(cam), C.byref(ep), C.byref(g) if g is not None else None,
+        particles.handle if particles is not None else None, width, height, m, _ptr(idx), _ptr(d),
+        int(prediction_code), int(coding_warp), _ptr(cp), _ptr(b), _ptr(errors), _ptr(eb), C.byref(o))
+    del keep
+    return errors, eb
+
+
+def uncertainty_tf(tf1d, step_size, error_type, precision="f32"):
+    """read_from_disk_uncertainty's table for a float 1D table: box filter (MAX_ERROR, ERROR_PERCENTILE) or
+    Gaussian filter (RMSE); returns [256 (y), 256 (x), 4]."""
+    L = lib()
+    dt = _dt(precision)
+    src = np.ascontiguousarray(tf1d, dtype=dt)
+    out = np.zeros((256, 256, 4), dtype=dt)
+    getattr(L, f"oracle_uncertainty_tf_{precision}")(_ptr(src), step_size, int(error_type), _ptr(out))
+    return out
+
+
+def reconstruct_uncertainty(cam, up, mode, width, height, m, dmin, dmax, index, data, error_bounds,
+                            prediction_code=False, coding_warp=0, coding_params=None, bounds=None, table=None,
+                            precision="f32", nthreads=0, rows=None):
+    """reconstruct_uncertainty_interpolation (mode 0, ``table`` = the preintegrated row) or _convolution (mode 1,
+    ``table`` = the 256 x 256 uncertainty table): float RGBA[H,W,4]."""
+    L = lib()
+    dt = _dt(precision)
+    idx = None if index is None else np.ascontiguousarray(index, dtype=np.uint32)
+    d = np.ascontiguousarray(data, dtype=dt)
+    cp = None if coding_params is None else np.ascontiguousarray(coding_params, dtype=np.uint16)
+    b = None if bounds is None else np.ascontiguousarray(bounds, dtype=np.uint16)
+    eb = np.ascontiguousarray(error_bounds, dtype=np.uint16)
+    t = np.ascontiguousarray(table, dtype=dt)
+    out = np.zeros((height, width, 4), dtype=dt)
+    o = options(nthreads, rows)
+    getattr(L, f"oracle_reconstruct_uncertainty_{precision}")(
+        C.byref(cam), C.byref(up), int(mode), width, height, m, (C.c_float * 3)(*dmin), (C.c_float * 3)(*dmax),
+        _ptr(idx), _ptr(d), int(prediction_code), int(coding_warp), _ptr(cp), _ptr(b), _ptr(eb), _ptr(t), _ptr(out),
+        C.byref(o))
     return out
 
 

@@ -119,6 +119,35 @@ MomentImageHost make_mi(int w, int h, int m, const uint32_t *index, const float 
     return mi;
 }
 
+ErrorReconstructionParameters to_err(const mraygb_error_params *e)
+{
+    ErrorReconstructionParameters p;
+    p.error_type = e->error_type;
+    p.error_percentile = e->error_percentile;
+    p.bias = e->bias;
+    p.data_min = e->data_min;
+    p.data_max = e->data_max;
+    p.step_size = e->step_size;
+    return p;
+}
+
+UncertaintyReconstructionParameters to_unc(const mraygb_uncertainty_params *u)
+{
+    UncertaintyReconstructionParameters p;
+    p.rec = to_rec(&u->rec);
+    p.bound_interpolation = u->bound_interpolation;
+    p.error_type = u->error_type;
+    return p;
+}
+
+TransferFunction make_tf2d(const float *table)
+{
+    TransferFunction tf;
+    for (int i = 0; i < TransferFunction::RESOLUTION * TransferFunction::RESOLUTION; ++i)
+        tf.data[i] = Vec4f(table[4 * i], table[4 * i + 1], table[4 * i + 2], table[4 * i + 3]);
+    return tf;
+}
+
 TransferFunction make_tf(const float *row)
 {
     TransferFunction tf;
@@ -129,6 +158,10 @@ TransferFunction make_tf(const float *row)
     return tf;
 }
 } // namespace
+
+// transfer_function.cpp defines the two filters of read_from_disk_uncertainty without declaring them in a header
+TransferFunction box_filter(array<Vec4f, TransferFunction::RESOLUTION> tf1d, float step_size);
+TransferFunction gaussian_filter(array<Vec4f, TransferFunction::RESOLUTION> tf1d, float step_size);
 
 extern "C" {
 
@@ -369,6 +402,117 @@ uint32_t ref_coding_errors(int w, int h, int m, const uint32_t *index, const flo
             errors[k++] = sqrtf(sum) / ref[0];
         }
     return k;
+}
+
+/* reconstruct_error (moment_raymarcher.cpp:552-560, host form :516-539) over a float grid: the u16 error bounds. */
+int ref_reconstruct_error(const mraygb_camera *c, const mraygb_error_params *e, const float *vol, int nx, int ny,
+                          int nz, const float *dmin, const float *dmax, int w, int h, int m, const uint32_t *index,
+                          const float *data, uint64_t data_size, const uint16_t *bounds, int prediction_code,
+                          int coding_warp, const uint16_t *coding_params, uint16_t *out)
+{
+    auto mi = make_mi(w, h, m, index, data, data_size, bounds, prediction_code, coding_warp, coding_params, dmin,
+                      dmax);
+    mi.add_error_bounds();
+    RegularGrid grid(Vec3i(nx, ny, nz), to_range(dmin, dmax), std::vector<float>(vol, vol + size_t(nx) * ny * nz),
+                     RegularGrid::DataType::F32);
+    reconstruct_error(to_camera(c), grid, mi, to_err(e));
+    std::memcpy(out, mi.error_bounds.data(), sizeof(uint16_t) * mi.error_bounds.size());
+    return 0;
+}
+
+/* read_from_disk_uncertainty's filters (transfer_function.cpp:151-248) on a float 1D table: 256 x 256 RGBA. */
+int ref_uncertainty_tf(const float *tf1d, float step_size, int error_type, float *out)
+{
+    array<Vec4f, TransferFunction::RESOLUTION> t;
+    for (int i = 0; i < TransferFunction::RESOLUTION; ++i)
+        t[i] = Vec4f(tf1d[4 * i], tf1d[4 * i + 1], tf1d[4 * i + 2], tf1d[4 * i + 3]);
+    auto tf = (error_type == RMSE) ? gaussian_filter(t, step_size) : box_filter(t, step_size);
+    for (size_t i = 0; i < tf.data.size(); ++i)
+    {
+        out[4 * i] = tf.data[i].x;
+        out[4 * i + 1] = tf.data[i].y;
+        out[4 * i + 2] = tf.data[i].z;
+        out[4 * i + 3] = tf.data[i].w;
+    }
+    return 0;
+}
+
+/* reconstruct_uncertainty_interpolation (mode 0, on a preintegrated row) / reconstruct_uncertainty_convolution
+ * (mode 1, on a 256 x 256 table) (moment_raymarcher.cpp:562-717): u8 RGBA as the reference stores it. */
+int ref_reconstruct_uncertainty_u8(const mraygb_camera *c, const mraygb_uncertainty_params *u, int mode, int w,
+                                   int h, int m, const uint32_t *index, const float *data, uint64_t data_size,
+                                   const uint16_t *bounds, const uint16_t *error_bounds, int prediction_code,
+                                   int coding_warp, const uint16_t *coding_params, const float *dmin,
+                                   const float *dmax, const float *table, uint8_t *out)
+{
+    auto mi = make_mi(w, h, m, index, data, data_size, bounds, prediction_code, coding_warp, coding_params, dmin,
+                      dmax);
+    mi.add_error_bounds();
+    std::memcpy(mi.error_bounds.data(), error_bounds, sizeof(uint16_t) * size_t(w) * h);
+    auto tf = mode == 0 ? make_tf(table) : make_tf2d(table);
+    ColorImageHost img(w, h);
+    if (mode == 0)
+        reconstruct_uncertainty_interpolation(to_camera(c), mi, tf, img, to_unc(u));
+    else
+        reconstruct_uncertainty_convolution(to_camera(c), mi, tf, img, to_unc(u));
+    std::memcpy(out, img.rgba.data(), 4 * size_t(w) * h);
+    return 0;
+}
+
+/* The per-pixel bodies of the two uncertainty renderers (MESE branches, moment_raymarcher.cpp:581-604, 660-688)
+ * keeping the float colour. */
+int ref_reconstruct_uncertainty_float(const mraygb_camera *c, const mraygb_uncertainty_params *u, int mode, int w,
+                                      int h, int m, const uint32_t *index, const float *data, uint64_t data_size,
+                                      const uint16_t *bounds, const uint16_t *error_bounds, int prediction_code,
+                                      int coding_warp, const uint16_t *coding_params, const float *dmin,
+                                      const float *dmax, const float *table, float *out)
+{
+    auto mi = make_mi(w, h, m, index, data, data_size, bounds, prediction_code, coding_warp, coding_params, dmin,
+                      dmax);
+    mi.add_error_bounds();
+    std::memcpy(mi.error_bounds.data(), error_bounds, sizeof(uint16_t) * size_t(w) * h);
+    auto tf = mode == 0 ? make_tf(table) : make_tf2d(table);
+    auto cam = to_camera(c);
+    auto params = to_unc(u);
+    NoSingleScattering ss;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int y = 0; y < h; ++y)
+        for (int x = 0; x < w; ++x)
+        {
+            Vec2f ndc(x / static_cast<float>(w) * 2.f - 1.f, y / static_cast<float>(h) * 2.f - 1.f);
+            Vec4f color;
+            if (mi.get_num_moments(x, y) == 0)
+                color = reconstruct_zero_ray(tf);
+            else
+            {
+                auto pm = mi.prepare_moments(x, y, params.rec.bias);
+                MESEReconstructionDefault mese(pm.size(), pm.data(), mi.get_bounds(x, y));
+                auto ray = cut::get_eye_ray(cam, ndc);
+                if (mode == 0)
+                {
+                    ErrorBoundMESEReconstruction<MESEReconstructionDefault> bound_rec(mese, mi.get_error_bound(x, y));
+                    ErrorBoundInterpolator<ErrorBoundMESEReconstruction<MESEReconstructionDefault>> interp(
+                        bound_rec, params.bound_interpolation);
+                    color = reconstruct_ray(ray, mi.domain, cam.znear, interp, tf, ss, params.rec);
+                }
+                else if (params.error_type == MAX_ERROR)
+                {
+                    ErrorBoundMESEReconstruction<MESEReconstructionDefault> bound_rec(mese, mi.get_error_bound(x, y));
+                    color = reconstruct_ray_uncertainty_tf(ray, mi.domain, cam.znear, bound_rec, tf, ss, params.rec);
+                }
+                else
+                {
+                    MeanStdDevMESEReconstruction<MESEReconstructionDefault> bound_rec(mese, mi.get_error_bound(x, y));
+                    color = reconstruct_ray_uncertainty_tf(ray, mi.domain, cam.znear, bound_rec, tf, ss, params.rec);
+                }
+            }
+            float *o = out + 4 * (size_t(y) * w + x);
+            o[0] = color.x;
+            o[1] = color.y;
+            o[2] = color.z;
+            o[3] = color.w;
+        }
+    return 0;
 }
 
 /* ---- MESE primitives (mese/MESE_dynamic.h) ---- */

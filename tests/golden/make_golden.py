@@ -21,6 +21,9 @@ on seeded inputs and stores inputs and outputs as small .npz files:
                       pairs (measure_coding_error.cpp needs HDF5, so the harness composes its loop from the
                       reference's own sample_moment_image, transform_dequantization_real, decode and
                       exponentialToTrigonometricMoments)
+  uncertainty.npz     error bounds of reconstruct_error (max, RMSE, P^2 percentile at 90 and 50), rows of the two
+                      uncertainty tables of read_from_disk_uncertainty and the float colours of the interpolation
+                      and convolution renderers on the Marschner-Lobb pipeline image
 
 Run from the repository root:  python tests/golden/make_golden.py
 """
@@ -59,6 +62,11 @@ def declare(ref):
     ref.ref_particles_sample.argtypes = [vp, vp, vp, vp, u64, f, vp, vp, vp, u64, vp]
     ref.ref_generate_particles.argtypes = [vp, vp, vp, vp, vp, vp, u64, f, vp, vp, C.c_int, C.c_int, C.c_int, vp, vp,
                                            vp, vp]
+    i = C.c_int
+    ref.ref_reconstruct_error.argtypes = [vp, vp, vp, i, i, i, vp, vp, i, i, i, vp, vp, u64, vp, i, i, vp, vp]
+    ref.ref_uncertainty_tf.argtypes = [vp, f, i, vp]
+    ref.ref_reconstruct_uncertainty_float.argtypes = [vp, vp, i, i, i, i, vp, vp, u64, vp, vp, i, i, vp, vp, vp, vp,
+                                                      vp]
     ref.ref_sample_moment_image.restype = u64
     ref.ref_sample_moment_image.argtypes = [C.c_int, C.c_int, C.c_int, vp, vp, u64, C.c_int, vp, vp]
     ref.ref_coding_errors.restype = C.c_uint32
@@ -429,6 +437,64 @@ def quant_curve(ref):
     return out
 
 
+def uncertainty(ref):
+    """Error bounds (reconstruct_error, three measures and two percentiles), the two uncertainty tables of
+    read_from_disk_uncertainty (every 17th row) and the two uncertainty renderers, from the reference's own code on
+    the Marschner-Lobb pipeline image (standard and prediction coding)."""
+    from mray_gb300.types import ErrorReconstructionParameters, UncertaintyReconstructionParameters
+
+    out = {}
+    wl = W.ml_workload(n=64, width=48, height=40, num_moments=16, seed=11, name="golden_ml")
+    Wd, H, m = wl.width, wl.height, wl.num_moments
+    vol = np.ascontiguousarray(wl.volume)
+    nz, ny, nx = vol.shape
+    dmin, dmax = f32(*wl.domain_min), f32(*wl.domain_max)
+    tf1d = np.ascontiguousarray(wl.tf1d, np.float32)
+    for et in (0, 1):
+        t = np.zeros((256, 256, 4), np.float32)
+        ref.ref_uncertainty_tf(P(tf1d), C.c_float(wl.tf_step), et, P(t))
+        out[f"table{et}_rows"] = t[::17].copy()
+    row = np.zeros((256, 4), np.float32)
+    ref.ref_preintegrate(P(tf1d), C.c_float(wl.tf_step), P(row))
+    for pc in (0, 1):
+        wl.gen.prediction_coding = pc
+        index, data, cp = _qc_image(ref, wl)
+        bounds = np.zeros(2 * Wd * H, np.uint16)
+        d2 = np.zeros(Wd * H * m, np.float32)
+        i2 = np.zeros(Wd * H + 1, np.uint32)
+        cp2 = np.zeros(2 * m, np.uint16)
+        size = C.c_uint64()
+        flags = np.zeros(4, np.int32)
+        ref.ref_generate_grid(C.byref(wl.camera), C.byref(wl.gen), P(vol), nx, ny, nz, P(dmin), P(dmax), Wd, H, m,
+                              P(d2), P(i2), P(bounds), P(cp2), C.byref(size), P(flags))
+        cpp = cp if pc else None
+        for et, pct in ((0, 90), (1, 90), (2, 90), (2, 50)):
+            ep = ErrorReconstructionParameters(error_type=et, error_percentile=pct, step_size=wl.rec.step_size,
+                                               bias=wl.rec.bias)
+            eb = np.zeros(Wd * H, np.uint16)
+            ref.ref_reconstruct_error(C.byref(wl.camera), C.byref(ep), P(vol), nx, ny, nz, P(dmin), P(dmax), Wd, H,
+                                      m, P(index), P(data), data.size, P(bounds), pc, 0, P(cpp), P(eb))
+            out[f"pc{pc}_eb{et}_{pct}"] = eb
+        for mode, et in ((0, 1), (1, 0), (1, 1), (1, 2)):
+            up = UncertaintyReconstructionParameters(rec=wl.rec, error_type=et, bound_interpolation=0.3)
+            if mode == 0:
+                table = row
+            else:
+                table = np.zeros((256, 256, 4), np.float32)
+                ref.ref_uncertainty_tf(P(tf1d), C.c_float(wl.tf_step), 1 if et == 1 else 0, P(table))
+            eb = out[f"pc{pc}_eb{et}_90"]
+            rgba = np.zeros((H, Wd, 4), np.float32)
+            ref.ref_reconstruct_uncertainty_float(C.byref(wl.camera), C.byref(up), mode, Wd, H, m, P(index), P(data),
+                                                  data.size, P(bounds), P(eb), pc, 0, P(cpp), P(dmin), P(dmax),
+                                                  P(np.ascontiguousarray(table)), P(rgba))
+            out[f"pc{pc}_unc{mode}_{et}"] = rgba
+        out[f"pc{pc}_index"], out[f"pc{pc}_data"], out[f"pc{pc}_bounds"] = index, data, bounds
+        if pc:
+            out["pc1_coding_params"] = cp
+    wl.gen.prediction_coding = 0
+    return out
+
+
 def main():
     ref = O.ref_lib()
     if ref is None:
@@ -443,6 +509,7 @@ def main():
     np.savez_compressed(os.path.join(HERE, "quantize.npz"), **quantize(ref))
     np.savez_compressed(os.path.join(HERE, "particles.npz"), **particles(ref))
     np.savez_compressed(os.path.join(HERE, "quant_curve.npz"), **quant_curve(ref))
+    np.savez_compressed(os.path.join(HERE, "uncertainty.npz"), **uncertainty(ref))
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

@@ -36,12 +36,15 @@ def test_library_exports_every_declared_symbol():
 
 def test_struct_layouts_match_the_c_header(tmp_path):
     """sizeof / offsetof of the POD mirrors as gcc lays out include/mraygb_types.h, against the ctypes mirrors."""
-    from mray_gb300.types import Camera, GenerationParameters, ReconstructionParameters
+    from mray_gb300.types import (Camera, ErrorReconstructionParameters, GenerationParameters,
+                                  ReconstructionParameters, UncertaintyReconstructionParameters)
 
     src = tmp_path / "layout.c"
-    fields = {"mraygb_camera": [f[0] for f in Camera._fields_],
-              "mraygb_generation_params": [f[0] for f in GenerationParameters._fields_],
-              "mraygb_reconstruction_params": [f[0] for f in ReconstructionParameters._fields_]}
+    classes = {"mraygb_camera": Camera, "mraygb_generation_params": GenerationParameters,
+               "mraygb_reconstruction_params": ReconstructionParameters,
+               "mraygb_error_params": ErrorReconstructionParameters,
+               "mraygb_uncertainty_params": UncertaintyReconstructionParameters}
+    fields = {st: [f[0] for f in cls._fields_] for st, cls in classes.items()}
     lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{ROOT}/include/mraygb_types.h"', 'int main(){']
     for st, fl in fields.items():
         lines.append(f'printf("{st} %zu\\n", sizeof({st}));')
@@ -53,8 +56,7 @@ def test_struct_layouts_match_the_c_header(tmp_path):
     subprocess.run(["gcc", "-o", str(exe), str(src)], check=True)
     out = dict(line.rsplit(" ", 1) for line in subprocess.run([str(exe)], capture_output=True, text=True,
                                                               check=True).stdout.splitlines())
-    for st, cls in (("mraygb_camera", Camera), ("mraygb_generation_params", GenerationParameters),
-                    ("mraygb_reconstruction_params", ReconstructionParameters)):
+    for st, cls in classes.items():
         assert int(out[st]) == C.sizeof(cls)
         for f in fields[st]:
             assert int(out[f"{st}.{f}"]) == getattr(cls, f).offset, f

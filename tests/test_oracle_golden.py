@@ -416,3 +416,36 @@ def test_quant_curve_search_rule():
         assert table.tolist() == expect
         assert evals == visited == np.count_nonzero(np.isfinite(means))
         assert 2 <= table[-1] < start_bits  # the curve does go down on this image
+
+
+# ---- error bounds and uncertainty rendering (moment_raymarcher.cpp:516-717) ---------------------------------------
+
+def test_error_bounds_and_uncertainty_bit_exact():
+    from mray_gb300.types import ErrorReconstructionParameters, UncertaintyReconstructionParameters
+
+    g = load("uncertainty.npz")
+    wl = W.ml_workload(n=64, width=48, height=40, num_moments=16, seed=11, name="golden_ml")
+    Wd, H, m = wl.width, wl.height, wl.num_moments
+    tables = {et: O.uncertainty_tf(wl.tf1d, wl.tf_step, et) for et in (0, 1)}
+    for et in (0, 1):
+        assert np.array_equal(tables[et][::17], g[f"table{et}_rows"]), et
+    row = O.preintegrate(wl.tf1d, wl.tf_step)
+    for pc in (0, 1):
+        idx, data, b = g[f"pc{pc}_index"], g[f"pc{pc}_data"], g[f"pc{pc}_bounds"]
+        cp = g["pc1_coding_params"] if pc else None
+        for et, pct in ((0, 90), (1, 90), (2, 90), (2, 50)):
+            ep = ErrorReconstructionParameters(error_type=et, error_percentile=pct, step_size=wl.rec.step_size,
+                                               bias=wl.rec.bias)
+            _, eb = O.reconstruct_error(wl.camera, ep, wl.volume, wl.domain_min, wl.domain_max, Wd, H, m, idx, data,
+                                        pc, 0, cp, b)
+            assert np.array_equal(eb.reshape(-1), g[f"pc{pc}_eb{et}_{pct}"]), (pc, et, pct)
+            assert eb.max() > 0
+        for mode, et in ((0, 1), (1, 0), (1, 1), (1, 2)):
+            up = UncertaintyReconstructionParameters(rec=wl.rec, error_type=et, bound_interpolation=0.3)
+            table = row if mode == 0 else tables[1 if et == 1 else 0]
+            rgba = O.reconstruct_uncertainty(wl.camera, up, mode, Wd, H, m, wl.domain_min, wl.domain_max, idx, data,
+                                             g[f"pc{pc}_eb{et}_90"], pc, 0, cp, b, table)
+            assert np.array_equal(rgba, g[f"pc{pc}_unc{mode}_{et}"]), (pc, mode, et)
+    # the P^2 estimate moves with the percentile and stays below the maximum on average
+    pct50, pct90 = g["pc0_eb2_50"].astype(float), g["pc0_eb2_90"].astype(float)
+    assert pct50.mean() < pct90.mean() <= g["pc0_eb0_90"].astype(float).mean()
