@@ -160,6 +160,41 @@ int mraygb_create_quantization_table(mraygb_context *ctx, int width, int height,
                                      int coding_warp, const uint16_t *h_coding_params, int start_bits, int sampling,
                                      uint8_t *h_table, float *h_means);
 
+/* reconstruct_error (src/moment_raymarcher.cpp:541-560; host form :516-539, GPU :693-752) over the volume uploaded
+ * last: per pixel the Lagrange multipliers of its moments (prepare_moments with ep->bias), then along the eye ray
+ * at t = t_near, t_near + step, ... <= t_far (src/raymarch_reconstruct.h:322-378) the bounded-MESE density at
+ * phase(t) against the volume's mapped density at t, reduced by ep->error_type: the maximum, the RMSE or the P^2
+ * estimate of the ep->error_percentile-th percentile (src/error_measures.h:30-229) of the absolute differences.
+ *   h_error_bounds : W*H u16 as MomentImageHost::set_error_bound stores them (e * 65535 truncated,
+ *                    src/moment_image.h:102-106)
+ *   h_errors       : W*H floats before the u16 store, or NULL
+ * Pixels without moments get 0 (the reference evaluates an empty multiplier array there). */
+int mraygb_reconstruct_error(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_error_params *ep, int width,
+                             int height, int num_moments, const uint32_t *h_index, const float *h_data,
+                             uint64_t data_size, const uint16_t *h_bounds, int prediction_code, int coding_warp,
+                             const uint16_t *h_coding_params, uint16_t *h_error_bounds, float *h_errors);
+
+/* read_from_disk_uncertainty (src/transfer_function.cpp:233-248) on a float 1D table (read_tf's output: 256 RGBA):
+ * box_filter (:151-186) for MRAYGB_ERROR_MAX and MRAYGB_ERROR_PERCENTILE, gaussian_filter (:188-231) for
+ * MRAYGB_ERROR_RMSE, built on the device as a 256 x 256 RGBA table ([y][x]) that stays resident for the convolution
+ * renderer.  h_table (256 * 256 * 4 floats) receives it when non-NULL. */
+int mraygb_upload_uncertainty_tf(mraygb_context *ctx, const float *tf1d_rgba256, float step_size, int error_type,
+                                 float *h_table);
+
+/* reconstruct_uncertainty_interpolation (mode 0) and reconstruct_uncertainty_convolution (mode 1)
+ * (src/moment_raymarcher.cpp:562-717, GPU :755-950) with the error bounds of mraygb_reconstruct_error.  Mode 0
+ * marches the density lerp(clamp(rho - e), clamp(rho + e), bound_interpolation) (ErrorBoundInterpolator,
+ * src/reconstruction_techniques.h:99-155) with the transfer function of mraygb_upload_tf; mode 1 looks up the pair
+ * (clamp(rho - e), clamp(rho + e)) for MRAYGB_ERROR_MAX, (rho, e) otherwise, in the table of
+ * mraygb_upload_uncertainty_tf (reconstruct_ray_uncertainty_tf, src/raymarch_reconstruct.h:203-259).  Image
+ * arguments and outputs as mraygb_reconstruct. */
+int mraygb_reconstruct_uncertainty(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_uncertainty_params *up,
+                                   int mode, int width, int height, int num_moments, const float domain_min[3],
+                                   const float domain_max[3], const uint32_t *h_index, const float *h_data,
+                                   uint64_t data_size, const uint16_t *h_bounds, const uint16_t *h_error_bounds,
+                                   int prediction_code, int coding_warp, const uint16_t *h_coding_params,
+                                   float *h_rgba, uint8_t *h_rgba8);
+
 /* ---- stage API: device pointers, ordered on the context stream ------------------------------------------ */
 
 /* Per-ray moments over the uploaded grid (generate_ray, src/raymarch_generate.h:69-148, driven as
@@ -206,6 +241,19 @@ int mraygb_stage_create_quantization_table(mraygb_context *ctx, int width, int h
                                            const uint32_t *d_index, const float *d_data, int coding_warp,
                                            const uint16_t *d_coding_params, int start_bits, int sampling,
                                            uint8_t *h_table, float *h_means);
+
+/* mraygb_reconstruct_error on the Lagrange multipliers of mraygb_stage_prepare_moments (d_errors may be NULL). */
+int mraygb_stage_reconstruct_error(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_error_params *ep,
+                                   int width, int height, int num_moments, const uint32_t *d_index,
+                                   const float *d_pmoments, const uint16_t *d_bounds, uint16_t *d_error_bounds,
+                                   float *d_errors);
+
+/* mraygb_reconstruct_uncertainty on the Lagrange multipliers of mraygb_stage_prepare_moments: d_rgba W*H*4 floats. */
+int mraygb_stage_reconstruct_uncertainty(mraygb_context *ctx, const mraygb_camera *cam,
+                                         const mraygb_uncertainty_params *up, int mode, int width, int height,
+                                         int num_moments, const float domain_min[3], const float domain_max[3],
+                                         const uint32_t *d_index, const float *d_pmoments, const uint16_t *d_bounds,
+                                         const uint16_t *d_error_bounds, float *d_rgba);
 
 /* Compaction that allocates nothing, for callers that must not call cudaMalloc / cudaFree while they work:
  * renderers and services that reserve all device memory up front in their own pool or arena (where an

@@ -4,12 +4,14 @@ quantization, bounded-MESE reconstruction) as hand-written sm_103a CUDA behind a
 The Python layer mirrors the reference's raymarcher API (generate / reconstruct and the moment-image, colour-image,
 grid and transfer-function containers) and calls the C ABI through ctypes.
 """
-from .types import (CODING_WARP_DEFAULT_TRANSFORMED, CODING_WARP_NONE, Camera, GenerationParameters,
-                    ReconstructionParameters)
+from .types import (CODING_WARP_DEFAULT_TRANSFORMED, CODING_WARP_NONE, ERROR_PERCENTILE, MAX_ERROR, RMSE, Camera,
+                    ErrorReconstructionParameters, GenerationParameters, ReconstructionParameters,
+                    UncertaintyReconstructionParameters)
 from .raymarcher import (MAX_MOMENTS, PRECISION_COMPENSATED_FF_MESE, PRECISION_COMPENSATED_FP64_MESE, PRECISION_FP32, ColorImageHost, Context,
                          MomentImageHost, Particles, RegularGrid, TransferFunction, default_context, default_quantization_table,
                          generate, preintegrate, quantize_prediction_coding, reconstruct,
-                         create_quantization_table)
+                         create_quantization_table, UncertaintyTransferFunction, read_from_disk_uncertainty,
+                         reconstruct_error, reconstruct_uncertainty_interpolation, reconstruct_uncertainty_convolution)
 from ._lib import MrayError
 
 __all__ = [
@@ -17,4 +19,7 @@ __all__ = [
     "CODING_WARP_NONE", "ColorImageHost", "Context", "MomentImageHost", "Particles", "RegularGrid", "TransferFunction",
     "default_context", "default_quantization_table", "create_quantization_table", "quantize_prediction_coding", "generate", "preintegrate", "reconstruct", "MrayError", "PRECISION_FP32",
     "PRECISION_COMPENSATED_FP64_MESE", "PRECISION_COMPENSATED_FF_MESE", "MAX_MOMENTS",
+    "ErrorReconstructionParameters", "UncertaintyReconstructionParameters", "MAX_ERROR", "RMSE", "ERROR_PERCENTILE",
+    "UncertaintyTransferFunction", "read_from_disk_uncertainty", "reconstruct_error",
+    "reconstruct_uncertainty_interpolation", "reconstruct_uncertainty_convolution",
 ]

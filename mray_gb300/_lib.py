@@ -8,7 +8,8 @@ import ctypes as C
 import os
 import threading
 
-from .types import Camera, GenerationParameters, ReconstructionParameters
+from .types import (Camera, ErrorReconstructionParameters, GenerationParameters, ReconstructionParameters,
+                    UncertaintyReconstructionParameters)
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libmraygb.so")
@@ -26,6 +27,8 @@ EXPORTS = [
     "mraygb_stage_prediction_encode", "mraygb_stage_quantize_prediction_coding",
     "mraygb_stage_dequantize_prediction_coding", "mraygb_stage_compact_noalloc", "mraygb_diff_forward",
     "mraygb_diff_backward", "mraygb_create_quantization_table", "mraygb_stage_create_quantization_table",
+    "mraygb_reconstruct_error", "mraygb_stage_reconstruct_error", "mraygb_upload_uncertainty_tf",
+    "mraygb_reconstruct_uncertainty", "mraygb_stage_reconstruct_uncertainty",
 ]
 
 _lock = threading.Lock()
@@ -77,6 +80,14 @@ def _declare(L):
     L.mraygb_diff_backward.argtypes = [vp, P(Camera), G, RP, i, i, i, vp, vp, vp, vp, vp, vp, vp, vp]
     L.mraygb_create_quantization_table.argtypes = [vp, i, i, i, vp, vp, u64, i, vp, i, i, vp, vp]
     L.mraygb_stage_create_quantization_table.argtypes = [vp, i, i, i, vp, vp, i, vp, i, i, vp, vp]
+    EP, UP = P(ErrorReconstructionParameters), P(UncertaintyReconstructionParameters)
+    f3 = C.c_float * 3
+    L.mraygb_reconstruct_error.argtypes = [vp, P(Camera), EP, i, i, i, vp, vp, u64, vp, i, i, vp, vp, vp]
+    L.mraygb_stage_reconstruct_error.argtypes = [vp, P(Camera), EP, i, i, i, vp, vp, vp, vp, vp]
+    L.mraygb_upload_uncertainty_tf.argtypes = [vp, vp, C.c_float, i, vp]
+    L.mraygb_reconstruct_uncertainty.argtypes = [vp, P(Camera), UP, i, i, i, i, f3, f3, vp, vp, u64, vp, vp, i, i, vp,
+                                                 vp, vp]
+    L.mraygb_stage_reconstruct_uncertainty.argtypes = [vp, P(Camera), UP, i, i, i, i, f3, f3, vp, vp, vp, vp, vp]
     special = ("mraygb_destroy", "mraygb_last_error", "mraygb_get_stream", "mraygb_kernel_launches")
     for name in EXPORTS:
         if name not in special:

@@ -36,6 +36,7 @@ SOURCES = [
     ("mese_ff.cu", []),
     ("coding.cu", ["--fmad=false"]),
     ("quant_curve.cu", ["--fmad=false"]),
+    ("uncertainty.cu", ["--fmad=false"]),
     ("api.cpp", ["-x", "cu"]),
 ]
 

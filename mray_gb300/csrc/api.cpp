@@ -91,6 +91,10 @@ struct mraygb_context
     DeviceBuffer adj_lambda, adj_bounds;
     // the quantization curve: per-sample moments and errors, the means, the uploaded sample of the host call
     DeviceBuffer qc_scratch, qc_means, qc_index, qc_data;
+    // error bounds and uncertainty rendering: the bounds and errors of the host calls, the 256 x 256 uncertainty
+    // table (resident) and the 1D table it is built from
+    DeviceBuffer error_bounds, errors, unc_table, unc_tf1d;
+    bool has_unc_table = false;
 };
 
 namespace
@@ -416,6 +420,154 @@ int run_quantize(mraygb_context *ctx, int width, int height, int m, const uint32
     return MRAYGB_OK;
 }
 
+// the moment image of a drop-in call on the device: data into ctx->compact, index / bounds / coding parameters when
+// given; pointers to the device copies (null where the image has none)
+int upload_moment_image(mraygb_context *ctx, int width, int height, int m, const uint32_t *h_index,
+                        const float *h_data, uint64_t data_size, const uint16_t *h_bounds, int prediction_code,
+                        int coding_warp, const uint16_t *h_coding_params, const uint32_t **d_index,
+                        const uint16_t **d_bounds, const uint16_t **d_cp)
+{
+    const size_t P = (size_t)width * (size_t)height;
+    if (!h_data)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "NULL moment data");
+    if (!h_index && data_size < P * (size_t)m)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "a non-compact image needs W*H*m floats");
+    if (prediction_code && coding_warp == MRAYGB_CODING_WARP_DEFAULT_TRANSFORMED && !h_coding_params)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "prediction-coded moments need their coding parameters");
+    const size_t nd = data_size ? data_size : 1;
+    CK(ctx->compact.reserve(nd * sizeof(float)), "moment buffer allocation");
+    CK(ctx->pmoments.reserve(nd * sizeof(float)), "multiplier buffer allocation");
+    if (data_size)
+        CK(cudaMemcpyAsync(ctx->compact.ptr, h_data, data_size * sizeof(float), cudaMemcpyHostToDevice, ctx->stream),
+           "moment upload");
+    *d_index = nullptr;
+    if (h_index)
+    {
+        CK(ctx->index.reserve((P + 1) * sizeof(uint32_t)), "index buffer allocation");
+        CK(cudaMemcpyAsync(ctx->index.ptr, h_index, (P + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->stream),
+           "index upload");
+        *d_index = ctx->index.as<uint32_t>();
+    }
+    *d_bounds = nullptr;
+    if (h_bounds)
+    {
+        CK(ctx->bounds.reserve(2 * P * sizeof(uint16_t)), "bounds buffer allocation");
+        CK(cudaMemcpyAsync(ctx->bounds.ptr, h_bounds, 2 * P * sizeof(uint16_t), cudaMemcpyHostToDevice, ctx->stream),
+           "bounds upload");
+        *d_bounds = ctx->bounds.as<uint16_t>();
+    }
+    *d_cp = nullptr;
+    if (prediction_code && coding_warp == MRAYGB_CODING_WARP_DEFAULT_TRANSFORMED)
+    {
+        CK(ctx->coding_params.reserve(2 * (size_t)m * sizeof(uint16_t)), "coding parameter allocation");
+        CK(cudaMemcpyAsync(ctx->coding_params.ptr, h_coding_params, 2 * (size_t)(m - 1) * sizeof(uint16_t),
+                           cudaMemcpyHostToDevice, ctx->stream),
+           "coding parameter upload");
+        *d_cp = ctx->coding_params.as<uint16_t>();
+    }
+    return MRAYGB_OK;
+}
+
+int validate_error_params(mraygb_context *ctx, const mraygb_error_params *ep)
+{
+    if (!ep)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "error parameters are NULL");
+    if (!(ep->step_size > 0.f))
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "step_size must be > 0 (got %g)", (double)ep->step_size);
+    if (ep->error_type < MRAYGB_ERROR_MAX || ep->error_type > MRAYGB_ERROR_PERCENTILE)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "unknown error type %d", ep->error_type);
+    if (ep->error_type == MRAYGB_ERROR_PERCENTILE && (ep->error_percentile < 1 || ep->error_percentile > 99))
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "error_percentile %d outside 1..99", ep->error_percentile);
+    if (ctx->volume == mraygb_context::NONE)
+        return fail(ctx, MRAYGB_NO_VOLUME, "no volume uploaded");
+    return MRAYGB_OK;
+}
+
+// the error measure per pixel over the resident volume
+int run_error_bounds(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_error_params *ep, int width,
+                     int height, int m, const uint32_t *d_index, const float *d_pm, const uint16_t *d_bounds,
+                     uint16_t *d_error_bounds, float *d_errors)
+{
+    const DeviceCamera dc = to_device_camera(*cam);
+    ErrorArgs a;
+    a.cam = &dc;
+    a.width = width;
+    a.height = height;
+    a.m = m;
+    a.index = d_index;
+    a.pmoments = d_pm;
+    a.bounds = d_bounds;
+    a.step = ep->step_size;
+    a.data_min = ep->data_min;
+    a.data_max = ep->data_max;
+    a.percentile = ep->error_percentile;
+    a.error_bounds = d_error_bounds;
+    a.errors = d_errors;
+    if (ctx->volume == mraygb_context::PARTICLES)
+        CK(launch_error_bounds_particles(particle_view(ctx), a, ep->error_type, ctx->error_flag.as<int>(), ctx->stream),
+           "error bound launch");
+    else
+        CK(launch_error_bounds_grid(grid_view(ctx), a, ep->error_type, ctx->error_flag.as<int>(), ctx->stream),
+           "error bound launch");
+    ctx->launches += 1;
+    return MRAYGB_OK;
+}
+
+int validate_uncertainty(mraygb_context *ctx, const mraygb_uncertainty_params *up, int mode)
+{
+    if (!up)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "uncertainty parameters are NULL");
+    const mraygb_reconstruction_params *rp = &up->rec;
+    if (!(rp->step_size > 0.f))
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "step_size must be > 0 (got %g)", (double)rp->step_size);
+    if (rp->use_truncated_fourier)
+        return fail(ctx, MRAYGB_NOT_SUPPORTED, "truncated Fourier reconstruction is not part of this path");
+    if (rp->ss_enable)
+        return fail(ctx, MRAYGB_NOT_SUPPORTED, "single scattering is not part of this path");
+    if (mode != 0 && mode != 1)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "mode %d: 0 = interpolation, 1 = convolution", mode);
+    if (mode == 0 && !ctx->has_tf)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "no transfer function uploaded");
+    if (mode == 1 && !ctx->has_unc_table)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "no uncertainty transfer function uploaded");
+    return MRAYGB_OK;
+}
+
+int run_uncertainty(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_uncertainty_params *up, int mode,
+                    int width, int height, int m, const float dmin[3], const float dmax[3], const uint32_t *d_index,
+                    const float *d_pm, const uint16_t *d_bounds, const uint16_t *d_error_bounds, float *d_rgba,
+                    uint8_t *d_rgba8)
+{
+    const DeviceCamera dc = to_device_camera(*cam);
+    UncertaintyArgs a;
+    a.cam = &dc;
+    a.width = width;
+    a.height = height;
+    a.m = m;
+    for (int i = 0; i < 3; ++i)
+    {
+        a.dmin[i] = dmin[i];
+        a.dmax[i] = dmax[i];
+    }
+    a.index = d_index;
+    a.pmoments = d_pm;
+    a.bounds = d_bounds;
+    a.error_bounds = d_error_bounds;
+    a.tf = ctx->tf.as<float4>();
+    a.table = ctx->unc_table.as<float4>();
+    a.step = up->rec.step_size;
+    a.emission = up->rec.medium_emission;
+    a.ert = up->rec.early_ray_termination;
+    a.interp = up->bound_interpolation;
+    a.mode = mode;
+    a.error_type = up->error_type;
+    a.rgba = d_rgba;
+    a.rgba8 = d_rgba8;
+    CK(launch_uncertainty(a, ctx->error_flag.as<int>(), ctx->stream), "uncertainty launch");
+    ctx->launches += 1;
+    return MRAYGB_OK;
+}
+
 int validate_rec(mraygb_context *ctx, const mraygb_reconstruction_params *rp)
 {
     if (!rp)
@@ -480,7 +632,8 @@ void mraygb_destroy(mraygb_context *ctx)
                             &ctx->error_flag, &ctx->coding_partial, &ctx->coding_params_f, &ctx->table,
                             &ctx->bits,    &ctx->bit_offset, &ctx->scan_scratch64, &ctx->packed,
                             &ctx->adj_lambda, &ctx->adj_bounds, &ctx->qc_scratch, &ctx->qc_means,
-                            &ctx->qc_index, &ctx->qc_data};
+                            &ctx->qc_index, &ctx->qc_data, &ctx->error_bounds, &ctx->errors, &ctx->unc_table,
+                            &ctx->unc_tf1d};
     for (DeviceBuffer *b : bufs)
         b->release();
     if (ctx->own_stream)
@@ -1173,6 +1326,152 @@ int mraygb_reconstruct(mraygb_context *ctx, const mraygb_camera *cam, const mray
         return rc;
     rc = run_reconstruct(ctx, cam, rp, width, height, m, domain_min, domain_max, d_index, ctx->pmoments.as<float>(),
                          d_bounds, ctx->rgba.as<float>(), h_rgba8 ? ctx->rgba8.as<uint8_t>() : nullptr);
+    if (rc)
+        return rc;
+    if (h_rgba)
+        CK(cudaMemcpyAsync(h_rgba, ctx->rgba.ptr, P * 4 * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream),
+           "colour download");
+    if (h_rgba8)
+        CK(cudaMemcpyAsync(h_rgba8, ctx->rgba8.ptr, P * 4, cudaMemcpyDeviceToHost, ctx->stream), "u8 colour download");
+    CK(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+    return check_device_error_flag(ctx);
+}
+
+// ---- error bounds and uncertainty rendering ----------------------------------------------------------------------
+
+int mraygb_stage_reconstruct_error(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_error_params *ep,
+                                   int width, int height, int m, const uint32_t *d_index, const float *d_pmoments,
+                                   const uint16_t *d_bounds, uint16_t *d_error_bounds, float *d_errors)
+{
+    CHECK_CTX();
+    int rc = check_image(ctx, width, height, m);
+    if (rc)
+        return rc;
+    if ((rc = validate_error_params(ctx, ep)))
+        return rc;
+    if (!cam || !d_pmoments || !d_error_bounds)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "NULL argument");
+    return run_error_bounds(ctx, cam, ep, width, height, m, d_index, d_pmoments, d_bounds, d_error_bounds, d_errors);
+}
+
+int mraygb_reconstruct_error(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_error_params *ep, int width,
+                             int height, int m, const uint32_t *h_index, const float *h_data, uint64_t data_size,
+                             const uint16_t *h_bounds, int prediction_code, int coding_warp,
+                             const uint16_t *h_coding_params, uint16_t *h_error_bounds, float *h_errors)
+{
+    CHECK_CTX();
+    int rc = check_image(ctx, width, height, m);
+    if (rc)
+        return rc;
+    if ((rc = validate_error_params(ctx, ep)))
+        return rc;
+    if (!cam || !h_error_bounds)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "NULL argument");
+    const size_t P = (size_t)width * (size_t)height;
+    const uint32_t *d_index;
+    const uint16_t *d_bounds, *d_cp;
+    if ((rc = upload_moment_image(ctx, width, height, m, h_index, h_data, data_size, h_bounds, prediction_code,
+                                  coding_warp, h_coding_params, &d_index, &d_bounds, &d_cp)))
+        return rc;
+    CK(ctx->error_bounds.reserve(P * sizeof(uint16_t)), "error bound buffer allocation");
+    if (h_errors)
+        CK(ctx->errors.reserve(P * sizeof(float)), "error buffer allocation");
+    rc = run_prepare(ctx, width, height, m, d_index, ctx->compact.as<float>(), prediction_code, coding_warp, d_cp,
+                     ep->bias, ctx->pmoments.as<float>());
+    if (rc)
+        return rc;
+    rc = run_error_bounds(ctx, cam, ep, width, height, m, d_index, ctx->pmoments.as<float>(), d_bounds,
+                          ctx->error_bounds.as<uint16_t>(), h_errors ? ctx->errors.as<float>() : nullptr);
+    if (rc)
+        return rc;
+    CK(cudaMemcpyAsync(h_error_bounds, ctx->error_bounds.ptr, P * sizeof(uint16_t), cudaMemcpyDeviceToHost,
+                       ctx->stream),
+       "error bound download");
+    if (h_errors)
+        CK(cudaMemcpyAsync(h_errors, ctx->errors.ptr, P * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream),
+           "error download");
+    CK(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+    return check_device_error_flag(ctx);
+}
+
+int mraygb_upload_uncertainty_tf(mraygb_context *ctx, const float *tf1d_rgba256, float step_size, int error_type,
+                                 float *h_table)
+{
+    CHECK_CTX();
+    if (!tf1d_rgba256)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "NULL transfer function");
+    if (error_type < MRAYGB_ERROR_MAX || error_type > MRAYGB_ERROR_PERCENTILE)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "unknown error type %d", error_type);
+    CK(ctx->unc_tf1d.reserve(256 * sizeof(float4)), "transfer function allocation");
+    CK(ctx->unc_table.reserve(256 * 256 * sizeof(float4)), "uncertainty table allocation");
+    CK(cudaMemcpyAsync(ctx->unc_tf1d.ptr, tf1d_rgba256, 256 * sizeof(float4), cudaMemcpyHostToDevice, ctx->stream),
+       "transfer function upload");
+    CK(launch_uncertainty_tf(ctx->unc_tf1d.as<float4>(), step_size, error_type, ctx->unc_table.as<float4>(),
+                             ctx->stream),
+       "uncertainty table launch");
+    ctx->launches += 1;
+    if (h_table)
+        CK(cudaMemcpyAsync(h_table, ctx->unc_table.ptr, 256 * 256 * sizeof(float4), cudaMemcpyDeviceToHost,
+                           ctx->stream),
+           "uncertainty table download");
+    CK(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+    ctx->has_unc_table = true;
+    return MRAYGB_OK;
+}
+
+int mraygb_stage_reconstruct_uncertainty(mraygb_context *ctx, const mraygb_camera *cam,
+                                         const mraygb_uncertainty_params *up, int mode, int width, int height, int m,
+                                         const float domain_min[3], const float domain_max[3],
+                                         const uint32_t *d_index, const float *d_pmoments, const uint16_t *d_bounds,
+                                         const uint16_t *d_error_bounds, float *d_rgba)
+{
+    CHECK_CTX();
+    int rc = check_image(ctx, width, height, m);
+    if (rc)
+        return rc;
+    if ((rc = validate_uncertainty(ctx, up, mode)))
+        return rc;
+    if (!cam || !domain_min || !domain_max || !d_pmoments || !d_error_bounds || !d_rgba)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "NULL argument");
+    return run_uncertainty(ctx, cam, up, mode, width, height, m, domain_min, domain_max, d_index, d_pmoments,
+                           d_bounds, d_error_bounds, d_rgba, nullptr);
+}
+
+int mraygb_reconstruct_uncertainty(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_uncertainty_params *up,
+                                   int mode, int width, int height, int m, const float domain_min[3],
+                                   const float domain_max[3], const uint32_t *h_index, const float *h_data,
+                                   uint64_t data_size, const uint16_t *h_bounds, const uint16_t *h_error_bounds,
+                                   int prediction_code, int coding_warp, const uint16_t *h_coding_params,
+                                   float *h_rgba, uint8_t *h_rgba8)
+{
+    CHECK_CTX();
+    int rc = check_image(ctx, width, height, m);
+    if (rc)
+        return rc;
+    if ((rc = validate_uncertainty(ctx, up, mode)))
+        return rc;
+    if (!cam || !domain_min || !domain_max || !h_error_bounds || (!h_rgba && !h_rgba8))
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "NULL argument");
+    const size_t P = (size_t)width * (size_t)height;
+    const uint32_t *d_index;
+    const uint16_t *d_bounds, *d_cp;
+    if ((rc = upload_moment_image(ctx, width, height, m, h_index, h_data, data_size, h_bounds, prediction_code,
+                                  coding_warp, h_coding_params, &d_index, &d_bounds, &d_cp)))
+        return rc;
+    CK(ctx->error_bounds.reserve(P * sizeof(uint16_t)), "error bound buffer allocation");
+    CK(cudaMemcpyAsync(ctx->error_bounds.ptr, h_error_bounds, P * sizeof(uint16_t), cudaMemcpyHostToDevice,
+                       ctx->stream),
+       "error bound upload");
+    CK(ctx->rgba.reserve(P * 4 * sizeof(float)), "colour buffer allocation");
+    if (h_rgba8)
+        CK(ctx->rgba8.reserve(P * 4), "u8 colour buffer allocation");
+    rc = run_prepare(ctx, width, height, m, d_index, ctx->compact.as<float>(), prediction_code, coding_warp, d_cp,
+                     up->rec.bias, ctx->pmoments.as<float>());
+    if (rc)
+        return rc;
+    rc = run_uncertainty(ctx, cam, up, mode, width, height, m, domain_min, domain_max, d_index,
+                         ctx->pmoments.as<float>(), d_bounds, ctx->error_bounds.as<uint16_t>(),
+                         ctx->rgba.as<float>(), h_rgba8 ? ctx->rgba8.as<uint8_t>() : nullptr);
     if (rc)
         return rc;
     if (h_rgba)

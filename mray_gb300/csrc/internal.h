@@ -68,6 +68,43 @@ cudaError_t launch_prepare(int num_pixels, int m, const uint32_t *index, const f
                            int coding_warp, const uint16_t *coding_params, float bias, bool fp64, float *pmoments,
                            cudaStream_t stream);
 
+// uncertainty.cu: error bounds, the uncertainty table, uncertainty rendering
+struct ErrorArgs
+{
+    const DeviceCamera *cam;
+    int width, height, m;
+    const uint32_t *index;  // compact index or null
+    const float *pmoments;  // Lagrange multipliers in the data layout
+    const uint16_t *bounds; // 2*W*H u16 or null
+    float step, data_min, data_max;
+    int percentile;
+    uint16_t *error_bounds; // W*H u16
+    float *errors;          // W*H floats or null
+};
+cudaError_t launch_error_bounds_grid(const GridView &grid, const ErrorArgs &a, int error_type, int *error_flag,
+                                     cudaStream_t stream);
+cudaError_t launch_error_bounds_particles(const ParticleView &parts, const ErrorArgs &a, int error_type,
+                                          int *error_flag, cudaStream_t stream);
+// 256 x 256 RGBA, [y][x]
+cudaError_t launch_uncertainty_tf(const float4 *tf1d, float step, int error_type, float4 *table, cudaStream_t stream);
+struct UncertaintyArgs
+{
+    const DeviceCamera *cam;
+    int width, height, m;
+    float dmin[3], dmax[3];
+    const uint32_t *index;
+    const float *pmoments;
+    const uint16_t *bounds;
+    const uint16_t *error_bounds;
+    const float4 *tf;    // mode 0: preintegrated row
+    const float4 *table; // mode 1: uncertainty table
+    float step, emission, ert, interp;
+    int mode, error_type;
+    float *rgba;
+    uint8_t *rgba8;
+};
+cudaError_t launch_uncertainty(const UncertaintyArgs &a, int *error_flag, cudaStream_t stream);
+
 // quant_curve.cu: the data-dependent quantization table's error means for every (index, bits) pair
 // scratch bytes for an sx x sy sample, bits bmin .. bmin + nb - 1, rows_per_pass moment indices per pass
 size_t quant_curve_scratch_bytes(int sx, int sy, int m, int nb, size_t rows_per_pass);

@@ -21,7 +21,8 @@ from typing import Optional
 import numpy as np
 
 from . import _lib
-from .types import Camera, GenerationParameters, ReconstructionParameters
+from .types import (Camera, ErrorReconstructionParameters, GenerationParameters, ReconstructionParameters,
+                    UncertaintyReconstructionParameters)
 
 PRECISION_FP32 = 0
 PRECISION_COMPENSATED_FP64_MESE = 1
@@ -96,6 +97,23 @@ class TransferFunction:
         self.table = t
 
 
+class UncertaintyTransferFunction:
+    """read_from_disk_uncertainty's table (transfer_function.cpp:233-248): the 1D table (read_tf's output, 256 x RGBA
+    float), the step size and the error type that selects the box or the Gaussian filter.  The 256 x 256 table is
+    built on the device (``Context.upload_uncertainty_tf``)."""
+
+    def __init__(self, tf1d: np.ndarray, step_size: float, error_type: int):
+        t = np.ascontiguousarray(tf1d, dtype=np.float32)
+        if t.shape != (256, 4):
+            raise ValueError("transfer function table must be 256 x 4")
+        self.tf1d, self.step_size, self.error_type = t, float(step_size), int(error_type)
+
+
+def read_from_disk_uncertainty(tf1d: np.ndarray, step_size: float, error_type: int) -> UncertaintyTransferFunction:
+    """read_from_disk_uncertainty(filepath, step_size, error_type) on the table the file holds."""
+    return UncertaintyTransferFunction(tf1d, step_size, error_type)
+
+
 def preintegrate(tf1d: np.ndarray, step_size: float) -> TransferFunction:
     """preintegrate (transfer_function.cpp:46-97): entry x = (rgb_x * a_x s, a_x s), s = step_size (float
     arithmetic, as the reference's)."""
@@ -125,7 +143,18 @@ class MomentImageHost:
         self.index = np.zeros(self.width * self.height + 1, dtype=np.uint32) if create_index else None
         self.bounds = np.zeros((self.width * self.height, 2), dtype=np.uint16) if create_bounds else None
         self.coding_params: Optional[np.ndarray] = None
+        self.error_bounds: Optional[np.ndarray] = None
         self.data = np.zeros(self.width * self.height * self.num_moments, dtype=np.float32)
+
+    def add_error_bounds(self) -> None:
+        """add_error_bounds (moment_image.h:100): one u16 error bound per pixel."""
+        self.error_bounds = np.zeros(self.width * self.height, dtype=np.uint16)
+
+    def has_error_bounds(self) -> bool:
+        return self.error_bounds is not None
+
+    def get_error_bound(self, x: int, y: int) -> float:
+        return float(np.float32(self.error_bounds[y * self.width + x]) / np.float32(65535.0))
 
     def has_bounds(self) -> bool:
         return self.bounds is not None
@@ -295,6 +324,55 @@ class Context:
                                                _hptr(img.rgba)))
         return img
 
+    def _image_arrays(self, mi: MomentImageHost):
+        data = np.ascontiguousarray(mi.data, dtype=np.float32)
+        index = np.ascontiguousarray(mi.index, dtype=np.uint32) if mi.is_compact else None
+        bounds = np.ascontiguousarray(mi.bounds, dtype=np.uint16) if mi.bounds is not None else None
+        cp = np.ascontiguousarray(mi.coding_params, dtype=np.uint16) if mi.coding_params is not None else None
+        return data, index, bounds, cp
+
+    def reconstruct_error(self, cam: Camera, ep: ErrorReconstructionParameters, mi: MomentImageHost,
+                          return_errors: bool = False):
+        """reconstruct_error(cam, volume, mi, params) over the volume uploaded last (moment_raymarcher.cpp:541-560):
+        fills mi.error_bounds (u16 per pixel) and, with ``return_errors``, returns the float errors [H, W]."""
+        if mi.error_bounds is None:
+            mi.add_error_bounds()
+        data, index, bounds, cp = self._image_arrays(mi)
+        eb = np.zeros(mi.width * mi.height, dtype=np.uint16)
+        errors = np.zeros((mi.height, mi.width), dtype=np.float32) if return_errors else None
+        self._check(self._L.mraygb_reconstruct_error(self._h, C.byref(cam), C.byref(ep), mi.width, mi.height,
+                                                     mi.num_moments, _hptr(index), _hptr(data), data.size,
+                                                     _hptr(bounds), int(mi.prediction_code), int(mi.coding_warp),
+                                                     _hptr(cp), _hptr(eb), _hptr(errors)))
+        mi.error_bounds = eb
+        return errors
+
+    def upload_uncertainty_tf(self, utf: UncertaintyTransferFunction, return_table: bool = False):
+        """The uncertainty table of ``utf`` built on the device and kept resident; with ``return_table`` also
+        returned as [256 (y), 256 (x), 4]."""
+        table = np.zeros((256, 256, 4), dtype=np.float32) if return_table else None
+        self._check(self._L.mraygb_upload_uncertainty_tf(self._h, _hptr(utf.tf1d), utf.step_size, utf.error_type,
+                                                         _hptr(table)))
+        return table
+
+    def reconstruct_uncertainty(self, cam: Camera, up: UncertaintyReconstructionParameters, mode: int,
+                                mi: MomentImageHost, img: Optional[ColorImageHost] = None) -> ColorImageHost:
+        """mode 0: reconstruct_uncertainty_interpolation with the transfer function of ``upload_tf``; mode 1:
+        reconstruct_uncertainty_convolution with the table of ``upload_uncertainty_tf``
+        (moment_raymarcher.cpp:562-717)."""
+        if mi.error_bounds is None:
+            raise ValueError("the moment image has no error bounds (reconstruct_error first)")
+        img = img or ColorImageHost(mi.width, mi.height)
+        data, index, bounds, cp = self._image_arrays(mi)
+        eb = np.ascontiguousarray(mi.error_bounds, dtype=np.uint16)
+        self._check(self._L.mraygb_reconstruct_uncertainty(self._h, C.byref(cam), C.byref(up), int(mode), mi.width,
+                                                           mi.height, mi.num_moments, _f3(mi.domain_min),
+                                                           _f3(mi.domain_max), _hptr(index), _hptr(data), data.size,
+                                                           _hptr(bounds), _hptr(eb), int(mi.prediction_code),
+                                                           int(mi.coding_warp), _hptr(cp), _hptr(img.rgba_float),
+                                                           _hptr(img.rgba)))
+        return img
+
     def quantize_prediction_coding(self, mi: MomentImageHost, table) -> np.ndarray:
         """quantize_prediction_coding(mi, table) (moment_quantization.cpp:239-276): the packed code bytes."""
         if not mi.is_compact:
@@ -337,6 +415,19 @@ class Context:
         return (table, means) if return_means else table
 
     # ---- stage calls on device pointers ----
+    def stage_reconstruct_error(self, cam, ep, width, height, num_moments, index, pmoments, bounds, error_bounds,
+                                errors=None):
+        self._check(self._L.mraygb_stage_reconstruct_error(self._h, C.byref(cam), C.byref(ep), width, height,
+                                                           num_moments, _dptr(index), _dptr(pmoments), _dptr(bounds),
+                                                           _dptr(error_bounds), _dptr(errors)))
+
+    def stage_reconstruct_uncertainty(self, cam, up, mode, width, height, num_moments, domain_min, domain_max, index,
+                                      pmoments, bounds, error_bounds, rgba):
+        self._check(self._L.mraygb_stage_reconstruct_uncertainty(self._h, C.byref(cam), C.byref(up), int(mode),
+                                                                 width, height, num_moments, _f3(domain_min),
+                                                                 _f3(domain_max), _dptr(index), _dptr(pmoments),
+                                                                 _dptr(bounds), _dptr(error_bounds), _dptr(rgba)))
+
     def stage_create_quantization_table(self, width, height, num_moments, index, data, coding_warp, coding_params,
                                         start_bits, sampling=64, return_means=False):
         """mraygb_stage_create_quantization_table: the table (and the means) of a compact prediction-coded image
@@ -463,3 +554,39 @@ def reconstruct(cam: Camera, mi: MomentImageHost, tf: TransferFunction, img: Col
     ctx = context or default_context()
     ctx.upload_tf(tf.table)
     ctx.reconstruct(cam, params, mi, img)
+
+
+def _upload_volume(ctx: Context, volume) -> None:
+    if isinstance(volume, Particles):
+        ctx.upload_particles(volume.x, volume.y, volume.z, volume.values, volume.smoothing_length,
+                             volume.domain_min, volume.domain_max)
+    else:
+        ctx.upload_grid(volume.data, volume.domain_min, volume.domain_max)
+
+
+def reconstruct_error(cam: Camera, volume, mi: MomentImageHost, params: ErrorReconstructionParameters,
+                      context: Optional[Context] = None) -> None:
+    """reconstruct_error(cam, volume, mi, params) for a RegularGrid or Particles (moment_raymarcher.h:73-76): fills
+    mi.error_bounds in place."""
+    ctx = context or default_context()
+    _upload_volume(ctx, volume)
+    ctx.reconstruct_error(cam, params, mi)
+
+
+def reconstruct_uncertainty_interpolation(cam: Camera, mi: MomentImageHost, tf: TransferFunction,
+                                          img: ColorImageHost, params: UncertaintyReconstructionParameters,
+                                          context: Optional[Context] = None) -> None:
+    """reconstruct_uncertainty_interpolation(cam, mi, tf, img, params) (moment_raymarcher.h:78-79)."""
+    ctx = context or default_context()
+    ctx.upload_tf(tf.table)
+    ctx.reconstruct_uncertainty(cam, params, 0, mi, img)
+
+
+def reconstruct_uncertainty_convolution(cam: Camera, mi: MomentImageHost, tf: UncertaintyTransferFunction,
+                                        img: ColorImageHost, params: UncertaintyReconstructionParameters,
+                                        context: Optional[Context] = None) -> None:
+    """reconstruct_uncertainty_convolution(cam, mi, tf, img, params) (moment_raymarcher.h:84-85) with the table of
+    read_from_disk_uncertainty."""
+    ctx = context or default_context()
+    ctx.upload_uncertainty_tf(tf)
+    ctx.reconstruct_uncertainty(cam, params, 1, mi, img)
