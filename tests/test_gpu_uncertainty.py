@@ -1,0 +1,196 @@
+"""Error bounds (reconstruct_error) and uncertainty rendering (interpolation and convolution) against the oracle,
+through the C ABI.
+
+* Uncertainty tables: the box filter is the reference's float arithmetic, bit for bit; the Gaussian filter rounds
+  exp of a float argument correctly where the C library's expf may differ by an ulp (1e-6 relative).
+* Error bounds: the device's MESE density is the re-march's (Reinsch's series) where the reference sums a power
+  recurrence, so the densities differ by FP32 rounding.  The maximum and the RMSE are continuous in them; the
+  P^2 estimate is not (a marker moves or not by a comparison), so it is held to a looser per-pixel bar with the
+  error against the FP64 oracle of the same method beside it.
+* Uncertainty colours: per pixel within 1e-3 of the reference's FP32 colour, or at least as close to the FP64
+  evaluation of the same method, on 99.8 % of the pixels (the bar of the plain re-march).
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from helpers import rgba_agreement, small_ml
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+RGBA_TOL = 1e-3
+
+
+def _dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def _host_image(M, wl, ref):
+    mi = M.MomentImageHost(wl.width, wl.height, wl.num_moments, True, True)
+    mi.index, mi.data, mi.is_compact = ref["index"].copy(), ref["data"].copy(), True
+    mi.bounds = ref["bounds"].reshape(-1, 2).copy()
+    mi.prediction_code = bool(ref["prediction_code"])
+    mi.coding_warp = 0
+    mi.coding_params = None if ref["coding_params"] is None else ref["coding_params"].copy()
+    mi.domain_min, mi.domain_max = wl.domain_min, wl.domain_max
+    return mi
+
+
+def _oracle_errors(wl, ref, ep, precision):
+    return O.reconstruct_error(wl.camera, ep, wl.volume, wl.domain_min, wl.domain_max, wl.width, wl.height,
+                               wl.num_moments, ref["index"], ref["data"], ref["prediction_code"], 0,
+                               ref["coding_params"], ref["bounds"], precision)
+
+
+@pytest.mark.parametrize("pc", [0, 1], ids=["std", "prediction_coded"])
+@pytest.mark.parametrize("et,pct", [(0, 90), (1, 90), (2, 90), (2, 50)], ids=["max", "rmse", "p90", "p50"])
+def test_error_bounds_match_oracle(gpu_context, pc, et, pct):
+    import mray_gb300 as M
+
+    wl = small_ml(96, 80, 31)
+    wl.gen.prediction_coding = pc
+    ref = O.workload_generate(wl, "f32")
+    ep = M.ErrorReconstructionParameters(error_type=et, error_percentile=pct, step_size=wl.rec.step_size,
+                                         bias=wl.rec.bias)
+    gpu_context.upload_grid(wl.volume, wl.domain_min, wl.domain_max)
+    mi = _host_image(M, wl, ref)
+    errors = gpu_context.reconstruct_error(wl.camera, ep, mi, return_errors=True)
+    e32, eb32 = _oracle_errors(wl, ref, ep, "f32")
+    e64, _ = _oracle_errors(wl, ref, ep, "f64")
+    hit = e32 > 0
+    assert hit.mean() > 0.3
+    # the stored codes are the float errors truncated to u16
+    assert np.array_equal(mi.error_bounds.reshape(wl.height, wl.width),
+                          (errors.astype(np.float32) * np.float32(65535)).astype(np.uint16))
+    d = np.abs(errors.astype(np.float64) - e32)
+    own = np.abs(e32.astype(np.float64) - e64)
+    if et in (0, 1):
+        # continuous measures: within 1e-5 (in density units) of the reference's, or of FP64 as close as it is
+        ok = (d <= 1e-5) | (np.abs(errors - e64) <= np.maximum(1e-5, own))
+        assert ok.mean() >= 0.998, f"{(~ok).sum()} pixels, max diff {d.max():.2e}"
+        assert np.abs(mi.error_bounds.astype(int) - eb32.reshape(-1).astype(int)).max() <= 2
+    else:
+        ok = (d <= 1e-3) | (np.abs(errors - e64) <= np.maximum(1e-3, own))
+        assert ok.mean() >= 0.99, f"{(~ok).sum()} pixels, max diff {d.max():.2e}"
+        assert np.median(d[hit]) <= 1e-5
+
+
+def test_error_bounds_stage_call_and_particles(gpu_context):
+    """The stage call on device multipliers equals the host call; the SPH volume gives the oracle's errors."""
+    import mray_gb300 as M
+    from mray_gb300 import workloads as Wl
+
+    wl = small_ml(64, 48, 16)
+    ref = O.workload_generate(wl, "f32")
+    ep = M.ErrorReconstructionParameters(error_type=M.MAX_ERROR, step_size=wl.rec.step_size, bias=wl.rec.bias)
+    gpu_context.upload_grid(wl.volume, wl.domain_min, wl.domain_max)
+    mi = _host_image(M, wl, ref)
+    gpu_context.reconstruct_error(wl.camera, ep, mi)
+    W, H, m = wl.width, wl.height, wl.num_moments
+    d_idx, d_data = _dev(ref["index"].view(np.int32)), _dev(ref["data"])
+    d_pm = torch.zeros_like(d_data)
+    gpu_context.stage_prepare_moments(W, H, m, d_idx, d_data, d_pm, bias=wl.rec.bias)
+    d_eb = torch.zeros(W * H, dtype=torch.int16, device="cuda")
+    d_b = _dev(ref["bounds"].reshape(-1).view(np.int16))
+    gpu_context.stage_reconstruct_error(wl.camera, ep, W, H, m, d_idx, d_pm, d_b, d_eb)
+    gpu_context.synchronize()
+    assert np.array_equal(d_eb.cpu().numpy().view(np.uint16), mi.error_bounds)
+
+    # SPH particles: a clustered set with the reference's cubic spline and one smoothing length
+    swl = Wl.sph_workload(n=200_000, h=1.0 / 64, width=48, height=40, num_moments=16, seed=5)
+    parts = O.ParticleSet(swl.x, swl.y, swl.z, swl.v, swl.h, swl.domain_min, swl.domain_max)
+    gpu_context.upload_particles(swl.x, swl.y, swl.z, swl.v, swl.h, swl.domain_min, swl.domain_max)
+    moments, bounds, counts = O.generate_moments_particles(swl.camera, swl.gen, parts, 48, 40, 16)
+    idx, data = O.compact(counts, moments.astype(np.float32))
+    sep = M.ErrorReconstructionParameters(error_type=M.RMSE, step_size=swl.rec.step_size, bias=swl.rec.bias,
+                                          data_min=swl.gen.data_min, data_max=swl.gen.data_max)
+    smi = M.MomentImageHost(48, 40, 16, True, True)
+    smi.index, smi.data, smi.is_compact, smi.bounds = idx, data, True, bounds.reshape(-1, 2)
+    errs = gpu_context.reconstruct_error(swl.camera, sep, smi, return_errors=True)
+    e32, _ = O.reconstruct_error(swl.camera, sep, None, swl.domain_min, swl.domain_max, 48, 40, 16, idx, data,
+                                 False, 0, None, bounds, "f32", particles=parts)
+    assert (e32 > 0).mean() > 0.3
+    assert np.abs(errs - e32).max() <= 1e-4
+
+
+@pytest.mark.parametrize("et", [0, 1, 2])
+def test_uncertainty_tables(gpu_context, et):
+    import mray_gb300 as M
+
+    wl = small_ml(32, 32, 8)
+    utf = M.read_from_disk_uncertainty(wl.tf1d, wl.tf_step, et)
+    table = gpu_context.upload_uncertainty_tf(utf, return_table=True)
+    ref = O.uncertainty_tf(wl.tf1d, wl.tf_step, et)
+    if et == M.RMSE:
+        assert np.allclose(table, ref, rtol=1e-6, atol=1e-12)
+    else:
+        assert np.array_equal(table, ref)
+
+
+@pytest.mark.parametrize("pc", [0, 1], ids=["std", "prediction_coded"])
+@pytest.mark.parametrize("mode,et", [(0, 1), (1, 0), (1, 1), (1, 2)],
+                         ids=["interp", "conv-max", "conv-rmse", "conv-p90"])
+def test_uncertainty_rendering_matches_oracle(gpu_context, pc, mode, et):
+    import mray_gb300 as M
+
+    wl = small_ml(96, 80, 31)
+    wl.gen.prediction_coding = pc
+    ref = O.workload_generate(wl, "f32")
+    ep = M.ErrorReconstructionParameters(error_type=et, step_size=wl.rec.step_size, bias=wl.rec.bias)
+    _, eb = _oracle_errors(wl, ref, ep, "f32")
+    mi = _host_image(M, wl, ref)
+    mi.error_bounds = eb.reshape(-1).copy()
+    up = M.UncertaintyReconstructionParameters(rec=wl.rec, error_type=et, bound_interpolation=0.3)
+    if mode == 0:
+        table = O.preintegrate(wl.tf1d, wl.tf_step)
+        gpu_context.upload_tf(table)
+    else:
+        table = O.uncertainty_tf(wl.tf1d, wl.tf_step, 1 if et == 1 else 0)
+        gpu_context.upload_uncertainty_tf(M.read_from_disk_uncertainty(wl.tf1d, wl.tf_step, et))
+    img = gpu_context.reconstruct_uncertainty(wl.camera, up, mode, mi)
+
+    def oracle(precision):
+        return O.reconstruct_uncertainty(wl.camera, up, mode, wl.width, wl.height, wl.num_moments, wl.domain_min,
+                                         wl.domain_max, ref["index"], ref["data"], eb, pc, 0, ref["coding_params"],
+                                         ref["bounds"], table, precision)
+
+    rgba32, rgba64 = oracle("f32"), oracle("f64")
+    assert rgba32[..., 3].mean() > 0.05
+    ok = rgba_agreement(img.rgba_float, rgba32, rgba64, RGBA_TOL)
+    assert ok.mean() >= 0.998, f"{(~ok).sum()} pixels"
+    assert np.mean(np.abs(img.rgba.astype(int) - O.rgba_to_u8(rgba32).astype(int)) <= 1) >= 0.999
+
+
+def test_uncertainty_errors(gpu_context):
+    import mray_gb300 as M
+
+    wl = small_ml(32, 24, 8)
+    ref = O.workload_generate(wl, "f32")
+    mi = _host_image(M, wl, ref)
+    fresh = M.Context(0)
+    try:
+        ep = M.ErrorReconstructionParameters(step_size=wl.rec.step_size)
+        with pytest.raises(M.MrayError) as e:  # no volume
+            fresh.reconstruct_error(wl.camera, ep, mi)
+        assert e.value.status == 7
+        fresh.upload_grid(wl.volume, wl.domain_min, wl.domain_max)
+        for bad in (dict(error_type=3), dict(error_percentile=0), dict(error_percentile=100), dict(step_size=0.0)):
+            with pytest.raises(M.MrayError) as e:
+                fresh.reconstruct_error(wl.camera, M.ErrorReconstructionParameters(**{"step_size": 0.01, **bad}), mi)
+            assert e.value.status == 1, bad
+        fresh.reconstruct_error(wl.camera, ep, mi)
+        up = M.UncertaintyReconstructionParameters(rec=wl.rec)
+        with pytest.raises(M.MrayError) as e:  # no uncertainty table yet
+            fresh.reconstruct_uncertainty(wl.camera, up, 1, mi)
+        assert e.value.status == 1
+        with pytest.raises(M.MrayError) as e:
+            fresh.reconstruct_uncertainty(wl.camera, up, 2, mi)
+        assert e.value.status == 1
+        up.rec.use_truncated_fourier = 1
+        fresh.upload_tf(O.preintegrate(wl.tf1d, wl.tf_step))
+        with pytest.raises(M.MrayError) as e:
+            fresh.reconstruct_uncertainty(wl.camera, up, 0, mi)
+        assert e.value.status == 6
+    finally:
+        fresh.close()
