@@ -55,7 +55,7 @@ def parse():
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the differentiation-form, SPH and FP64-error sections")
     ap.add_argument("--sph-particles", type=int, default=16_000_000)
-    ap.add_argument("--section", default="all", choices=["all", "diff", "sph", "large"],
+    ap.add_argument("--section", default="all", choices=["all", "diff", "sph", "large", "uncertainty"],
                     help="diff / sph: run only that section and print its JSON (for profiling)")
     return ap.parse_args()
 
@@ -393,6 +393,7 @@ def run_ours(args):
         extras["differentiation_form"] = run_diff(args, local)
         extras["sph"] = run_sph(args, local)
         extras["large"] = run_large(args, local)
+        extras["uncertainty"] = run_uncertainty(args, local)
         extras["errors_vs_fp64"] = precision_errors(args, local)
 
     if rank == 0:
@@ -767,6 +768,85 @@ def quantization_table_timing(args, ctx, cam, gen, Wd, H, m, d_mo, d_b, d_c, d_i
                            "kind": "port (sequential search of measure_coding_error.cpp:374-438)"}}
 
 
+def run_uncertainty(args, local):
+    """Error bounds and uncertainty rendering on the default workload (512^3 mixing layer, 1024^2, m = 64): the
+    moment image is generated, compacted and prepared once; then per launch the error-bound kernel for each measure
+    (reconstruct_error at the re-march step), the uncertainty table build and the two renderers.  The oracle's
+    RMSE error bounds on every 8th row, on the host cores, beside them."""
+    import torch
+
+    import mray_gb300 as M
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    wl = workload(args)
+    Wd, H, m = wl.width, wl.height, wl.num_moments
+    P = Wd * H
+    ctx = M.Context(local)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    ctx.upload_grid(torch.from_numpy(wl.volume).cuda(), wl.domain_min, wl.domain_max)
+    mo = torch.empty(P * m, device="cuda")
+    b = torch.empty(2 * P, dtype=torch.int16, device="cuda")
+    c = torch.empty(P, dtype=torch.int32, device="cuda")
+    idx = torch.empty(P + 1, dtype=torch.int32, device="cuda")
+    cm = torch.empty(P * m, device="cuda")
+    pm = torch.empty(P * m, device="cuda")
+    eb = torch.empty(P, dtype=torch.int16, device="cuda")
+    rgba = torch.empty(P * 4, device="cuda")
+    ctx.stage_generate_moments(wl.camera, wl.gen, Wd, H, m, mo, b, c)
+    ctx.stage_compact(Wd, H, m, c, mo, idx, cm)
+    ctx.stage_prepare_moments(Wd, H, m, idx, cm, pm, bias=wl.rec.bias)
+    steps = max(1, min(args.steps, 5))
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        ctx.synchronize()
+        ev = _events(steps)
+        for e in ev:
+            e[0].record(stream)
+            fn()
+            e[1].record(stream)
+        ctx.synchronize()
+        return statistics.mean(e[0].elapsed_time(e[1]) for e in ev)
+
+    out = {"workload": f"mixing_layer{args.size}^3_{Wd}x{H}_m{m}_persp", "step": "the re-march step"}
+    for name, et in (("error_bounds_max", M.MAX_ERROR), ("error_bounds_rmse", M.RMSE),
+                     ("error_bounds_p90", M.ERROR_PERCENTILE)):
+        ep = M.ErrorReconstructionParameters(error_type=et, step_size=wl.rec.step_size, bias=wl.rec.bias)
+        ms = timed(lambda: ctx.stage_reconstruct_error(wl.camera, ep, Wd, H, m, idx, pm, b, eb))
+        out[name] = {"value": P / (ms * 1e-3) / 1e6, "unit": UNIT, "ms": ms}
+    utf = M.read_from_disk_uncertainty(wl.tf1d, wl.tf_step, M.RMSE)
+    t0 = time.perf_counter()
+    ctx.upload_uncertainty_tf(utf)
+    out["uncertainty_table_ms"] = (time.perf_counter() - t0) * 1e3
+    ctx.upload_tf(M.preintegrate(wl.tf1d, wl.tf_step).table)
+    for name, mode in (("interpolation", 0), ("convolution", 1)):
+        up = M.UncertaintyReconstructionParameters(rec=wl.rec, error_type=M.RMSE)
+        ms = timed(lambda: ctx.stage_reconstruct_uncertainty(wl.camera, up, mode, Wd, H, m, wl.domain_min,
+                                                             wl.domain_max, idx, pm, b, eb, rgba))
+        out[f"uncertainty_{name}"] = {"value": P / (ms * 1e-3) / 1e6, "unit": UNIT, "ms": ms}
+    ms = timed(lambda: ctx.stage_reconstruct(wl.camera, wl.rec, Wd, H, m, wl.domain_min, wl.domain_max, idx, pm, b,
+                                             rgba))
+    out["plain_reconstruct"] = {"value": P / (ms * 1e-3) / 1e6, "unit": UNIT, "ms": ms}
+    # the oracle (the reference's CPU method) on every 64th row of the same image
+    index = idx.cpu().numpy().view(np.uint32)
+    data = cm[:int(index[-1])].cpu().numpy()
+    bounds = b.cpu().numpy().view(np.uint16)
+    ep = M.ErrorReconstructionParameters(error_type=M.RMSE, step_size=wl.rec.step_size, bias=wl.rec.bias)
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    O.reconstruct_error(wl.camera, ep, wl.volume, wl.domain_min, wl.domain_max, Wd, H, m, index, data, False, 0, None,
+                        bounds, "f32", nthreads=threads, rows=(0, H, 8))
+    cpu_s = time.perf_counter() - t0
+    rays = Wd * len(range(0, H, 8))
+    out["cpu_oracle_rmse"] = {"value": rays / cpu_s / 1e6, "unit": UNIT, "threads": threads,
+                              "sample": f"rows y = 0 mod 8 ({rays} rays, {cpu_s:.1f} s)", "kind": "port"}
+    ctx.close()
+    return out
+
+
 def precision_errors(args, local):
     """Max and RMS errors of the moments, the transmittance and the RGBA of both arithmetic forms against the FP64
     oracle of the same method, on every 8th row of a 128 x 128 image of the default workload (its volume and
@@ -843,7 +923,7 @@ def main():
 
         _, _, local = dist_info()
         torch.cuda.set_device(local)
-        fn = {"diff": run_diff, "sph": run_sph, "large": run_large}[args.section]
+        fn = {"diff": run_diff, "sph": run_sph, "large": run_large, "uncertainty": run_uncertainty}[args.section]
         print(json.dumps({args.section: fn(args, local)}), flush=True)
     else:
         run_ours(args)

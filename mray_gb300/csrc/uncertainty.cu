@@ -35,6 +35,25 @@ __device__ __forceinline__ float to_phase(float t, float t_near, float range)
     return (float)((double)__fdiv_rn(__fsub_rn(t, t_near), range) * kPiD - kPiD);
 }
 
+// The same phase without FP64 (GB300 runs FP64 at 1/64 of the FP32 rate and this is evaluated per sample):
+// M_PI * q - M_PI = M_PI (q - 1) with q - 1 split exactly into s + e (two-sum) and the double M_PI split exactly
+// into three floats, the leading product exact by FMA; the float result equals the reference's except where the
+// exact value lies within about 2^-48 of a float rounding boundary.
+constexpr float kPi1 = (float)kPiD;
+constexpr float kPi2 = (float)(kPiD - (double)kPi1);
+constexpr float kPi3 = (float)((kPiD - (double)kPi1) - (double)kPi2);
+__device__ __forceinline__ float to_phase_ff(float t, float t_near, float range)
+{
+    const float q = __fdiv_rn(__fsub_rn(t, t_near), range);
+    const float s = __fadd_rn(q, -1.f);
+    const float bb = __fsub_rn(s, q);
+    const float e = __fadd_rn(__fsub_rn(q, __fsub_rn(s, bb)), __fsub_rn(-1.f, bb));
+    const float h = __fmul_rn(s, kPi1);
+    const float l = __fmaf_rn(s, kPi1, -h);
+    const float small = __fmaf_rn(s, kPi2, __fmaf_rn(e, kPi1, __fmaf_rn(s, kPi3, __fmaf_rn(e, kPi2, l))));
+    return __fadd_rn(h, small);
+}
+
 // ---- error measures (src/error_measures.h:30-229) -------------------------------------------------------------
 
 struct ErrMax
@@ -63,14 +82,17 @@ struct ErrRmse
 // only the three middle markers move.  All indices are compile-time constants, so the state stays in registers.
 struct ErrPercentile
 {
-    float q;
+    float q, q_half, q_mid; // q, q / 2 and (1 + q) / 2: the constant marker increments of update
     int init_num = 0;
     float h[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
     int pos[5] = {0, 0, 0, 0, 0};
     float des[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
 
     // ErrorPercentile(float p) : q(p / 100.f); built on the host and passed to the kernel as the initial state
-    __host__ __device__ explicit ErrPercentile(int percentile) : q((float)percentile / 100.f) {}
+    __host__ __device__ explicit ErrPercentile(int percentile)
+        : q((float)percentile / 100.f), q_half(q / 2.0f), q_mid((1.0f + q) / 2.f)
+    {
+    }
 
     __device__ __forceinline__ static void swap(float &a, float &b)
     {
@@ -193,9 +215,9 @@ struct ErrPercentile
         for (int k = 0; k < 5; ++k)
             if (k >= move_idx)
                 pos[k] += 1;
-        des[1] = __fadd_rn(des[1], __fdiv_rn(q, 2.0f));
+        des[1] = __fadd_rn(des[1], q_half);
         des[2] = __fadd_rn(des[2], q);
-        des[3] = __fadd_rn(des[3], __fdiv_rn(__fadd_rn(1.0f, q), 2.f));
+        des[3] = __fadd_rn(des[3], q_mid);
         des[4] = __fadd_rn(des[4], 1.0f);
         adjust_one<1>();
         adjust_one<2>();
@@ -287,7 +309,7 @@ __global__ void __launch_bounds__(128) error_bound_kernel(const ErrorDev a, cons
                     atomicExch(a.error_flag, 1);
                     break;
                 }
-                const float fs = mese_density<MAXM>(lam2, lam0, to_phase(t, t_near, range), lo, span);
+                const float fs = mese_density<MAXM>(lam2, lam0, to_phase_ff(t, t_near, range), lo, span);
                 const float ref = map_density(volume_sample(vol, __fadd_rn(o[0], __fmul_rn(t, d[0])),
                                                             __fadd_rn(o[1], __fmul_rn(t, d[1])),
                                                             __fadd_rn(o[2], __fmul_rn(t, d[2]))),
