@@ -181,6 +181,11 @@ int mraygb_reconstruct_error(mraygb_context *ctx, const mraygb_camera *cam, cons
 int mraygb_upload_uncertainty_tf(mraygb_context *ctx, const float *tf1d_rgba256, float step_size, int error_type,
                                  float *h_table);
 
+/* A 256 x 256 RGBA uncertainty table given whole ([y][x], the layout of TransferFunction::data,
+ * src/transfer_function.h:30-34), for callers that hold read_from_disk_uncertainty's result already (the seam
+ * reconstruct_uncertainty_convolution_device takes the table, src/moment_raymarcher.cuh:84-86). */
+int mraygb_upload_uncertainty_table(mraygb_context *ctx, const float *table_rgba256x256);
+
 /* reconstruct_uncertainty_interpolation (mode 0) and reconstruct_uncertainty_convolution (mode 1)
  * (src/moment_raymarcher.cpp:562-717, GPU :755-950) with the error bounds of mraygb_reconstruct_error.  Mode 0
  * marches the density lerp(clamp(rho - e), clamp(rho + e), bound_interpolation) (ErrorBoundInterpolator,

@@ -28,7 +28,7 @@ EXPORTS = [
     "mraygb_stage_dequantize_prediction_coding", "mraygb_stage_compact_noalloc", "mraygb_diff_forward",
     "mraygb_diff_backward", "mraygb_create_quantization_table", "mraygb_stage_create_quantization_table",
     "mraygb_reconstruct_error", "mraygb_stage_reconstruct_error", "mraygb_upload_uncertainty_tf",
-    "mraygb_reconstruct_uncertainty", "mraygb_stage_reconstruct_uncertainty",
+    "mraygb_reconstruct_uncertainty", "mraygb_stage_reconstruct_uncertainty", "mraygb_upload_uncertainty_table",
 ]
 
 _lock = threading.Lock()
@@ -85,6 +85,7 @@ def _declare(L):
     L.mraygb_reconstruct_error.argtypes = [vp, P(Camera), EP, i, i, i, vp, vp, u64, vp, i, i, vp, vp, vp]
     L.mraygb_stage_reconstruct_error.argtypes = [vp, P(Camera), EP, i, i, i, vp, vp, vp, vp, vp]
     L.mraygb_upload_uncertainty_tf.argtypes = [vp, vp, C.c_float, i, vp]
+    L.mraygb_upload_uncertainty_table.argtypes = [vp, vp]
     L.mraygb_reconstruct_uncertainty.argtypes = [vp, P(Camera), UP, i, i, i, i, f3, f3, vp, vp, u64, vp, vp, i, i, vp,
                                                  vp, vp]
     L.mraygb_stage_reconstruct_uncertainty.argtypes = [vp, P(Camera), UP, i, i, i, i, f3, f3, vp, vp, vp, vp, vp]

@@ -1419,6 +1419,20 @@ int mraygb_upload_uncertainty_tf(mraygb_context *ctx, const float *tf1d_rgba256,
     return MRAYGB_OK;
 }
 
+int mraygb_upload_uncertainty_table(mraygb_context *ctx, const float *table_rgba256x256)
+{
+    CHECK_CTX();
+    if (!table_rgba256x256)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "NULL uncertainty table");
+    CK(ctx->unc_table.reserve(256 * 256 * sizeof(float4)), "uncertainty table allocation");
+    CK(cudaMemcpyAsync(ctx->unc_table.ptr, table_rgba256x256, 256 * 256 * sizeof(float4), cudaMemcpyHostToDevice,
+                       ctx->stream),
+       "uncertainty table upload");
+    CK(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+    ctx->has_unc_table = true;
+    return MRAYGB_OK;
+}
+
 int mraygb_stage_reconstruct_uncertainty(mraygb_context *ctx, const mraygb_camera *cam,
                                          const mraygb_uncertainty_params *up, int mode, int width, int height, int m,
                                          const float domain_min[3], const float domain_max[3],

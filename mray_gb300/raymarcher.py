@@ -355,6 +355,13 @@ class Context:
                                                          _hptr(table)))
         return table
 
+    def upload_uncertainty_table(self, table) -> None:
+        """A whole 256 x 256 RGBA uncertainty table ([y][x]) as the convolution renderer's table."""
+        t = np.ascontiguousarray(table, dtype=np.float32)
+        if t.shape != (256, 256, 4):
+            raise ValueError("uncertainty table must be 256 x 256 x 4")
+        self._check(self._L.mraygb_upload_uncertainty_table(self._h, _hptr(t)))
+
     def reconstruct_uncertainty(self, cam: Camera, up: UncertaintyReconstructionParameters, mode: int,
                                 mi: MomentImageHost, img: Optional[ColorImageHost] = None) -> ColorImageHost:
         """mode 0: reconstruct_uncertainty_interpolation with the transfer function of ``upload_tf``; mode 1:

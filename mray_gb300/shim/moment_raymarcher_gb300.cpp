@@ -193,6 +193,126 @@ void reconstruct_device(cut::Camera cam, const MomentImageHost &mi, const Transf
                              reinterpret_cast<uint8_t *>(cimg.rgba.data())));
 }
 
+namespace
+{
+
+mraygb_error_params to_c(const ErrorReconstructionParameters &p)
+{
+    mraygb_error_params o{};
+    o.error_type = p.error_type;
+    o.error_percentile = p.error_percentile;
+    o.bias = p.bias;
+    o.data_min = p.data_min;
+    o.data_max = p.data_max;
+    o.step_size = p.step_size;
+    o.compress = p.compress;
+    o.entropy_coding = p.entropy_coding;
+    o.quantization_bits = p.quantization_bits;
+    return o;
+}
+
+mraygb_uncertainty_params to_c(const UncertaintyReconstructionParameters &p)
+{
+    mraygb_uncertainty_params o{};
+    o.rec = to_c(p.rec);
+    o.bound_interpolation = p.bound_interpolation;
+    o.error_type = p.error_type;
+    return o;
+}
+
+// the moment image's u16 arrays as the C ABI takes them
+struct ImageArrays
+{
+    std::vector<uint16_t> bounds, cp;
+    explicit ImageArrays(const MomentImageHost &mi)
+    {
+        for (const auto &b : mi.bounds)
+        {
+            bounds.push_back(b.lower);
+            bounds.push_back(b.upper);
+        }
+        for (const auto &p : mi.coding_params)
+        {
+            cp.push_back(p.param1);
+            cp.push_back(p.param2);
+        }
+    }
+};
+
+void error_uploaded(const cut::Camera &cam, MomentImageHost &mi, const ErrorReconstructionParameters &params)
+{
+    const auto c = to_c(cam);
+    const auto e = to_c(params);
+    ImageArrays arr(mi);
+    mi.error_bounds.resize(size_t(mi.width) * mi.height);
+    check(mraygb_reconstruct_error(context(), &c, &e, mi.width, mi.height, mi.num_moments,
+                                   mi.is_compact ? mi.index.data() : nullptr, mi.data.data(), mi.data.size(),
+                                   arr.bounds.empty() ? nullptr : arr.bounds.data(), mi.prediction_code,
+                                   mi.coding_warp, arr.cp.empty() ? nullptr : arr.cp.data(), mi.error_bounds.data(),
+                                   nullptr));
+}
+
+void uncertainty(const cut::Camera &cam, const MomentImageHost &mi, ColorImageHost &cimg,
+                 const UncertaintyReconstructionParameters &params, int mode)
+{
+    const auto c = to_c(cam);
+    const auto u = to_c(params);
+    ImageArrays arr(mi);
+    const float dmin[3] = {mi.domain.min.x, mi.domain.min.y, mi.domain.min.z};
+    const float dmax[3] = {mi.domain.max.x, mi.domain.max.y, mi.domain.max.z};
+    check(mraygb_reconstruct_uncertainty(context(), &c, &u, mode, mi.width, mi.height, mi.num_moments, dmin, dmax,
+                                         mi.is_compact ? mi.index.data() : nullptr, mi.data.data(), mi.data.size(),
+                                         arr.bounds.empty() ? nullptr : arr.bounds.data(), mi.error_bounds.data(),
+                                         mi.prediction_code, mi.coding_warp, arr.cp.empty() ? nullptr : arr.cp.data(),
+                                         nullptr, reinterpret_cast<uint8_t *>(cimg.rgba.data())));
+}
+
+} // namespace
+
+// reconstruct_error_device (src/moment_raymarcher.cuh:73-76) for both volume types: fills mi.error_bounds
+void reconstruct_error_device(cut::Camera cam, const RegularGrid &volume, MomentImageHost &mi,
+                              const ErrorReconstructionParameters &params)
+{
+    if (volume.type != RegularGrid::DataType::F32)
+    {
+        std::fprintf(stderr, "mraygb: only float grids are supported\n");
+        std::terminate();
+    }
+    const float dmin[3] = {volume.domain.min.x, volume.domain.min.y, volume.domain.min.z};
+    const float dmax[3] = {volume.domain.max.x, volume.domain.max.y, volume.domain.max.z};
+    check(mraygb_upload_grid(context(), volume.data.data(), volume.size.x, volume.size.y, volume.size.z, dmin, dmax,
+                             0));
+    error_uploaded(cam, mi, params);
+}
+
+void reconstruct_error_device(cut::Camera cam, const Particles &volume, MomentImageHost &mi,
+                              const ErrorReconstructionParameters &params)
+{
+    const float dmin[3] = {volume.domain.min.x, volume.domain.min.y, volume.domain.min.z};
+    const float dmax[3] = {volume.domain.max.x, volume.domain.max.y, volume.domain.max.z};
+    check(mraygb_upload_particles(context(), volume.x.data(), volume.y.data(), volume.z.data(),
+                                  volume.values.data(), volume.size(), volume.smoothing_length, dmin, dmax, 0));
+    error_uploaded(cam, mi, params);
+}
+
+// reconstruct_uncertainty_interpolation_device / _convolution_device (src/moment_raymarcher.cuh:78-86); the
+// single-scattering overload stays with the reference's launcher (single scattering is not on this path)
+void reconstruct_uncertainty_interpolation_device(cut::Camera cam, const MomentImageHost &mi,
+                                                  const TransferFunction &tf, ColorImageHost &cimg,
+                                                  const UncertaintyReconstructionParameters &params)
+{
+    check(mraygb_upload_tf(context(), reinterpret_cast<const float *>(tf.data.data())));
+    uncertainty(cam, mi, cimg, params, 0);
+}
+
+void reconstruct_uncertainty_convolution_device(cut::Camera cam, const MomentImageHost &mi, const TransferFunction &tf,
+                                                ColorImageHost &cimg,
+                                                const UncertaintyReconstructionParameters &params)
+{
+    check(mraygb_upload_uncertainty_table(context(), reinterpret_cast<const float *>(tf.data.data())));
+    uncertainty(cam, mi, cimg, params, 1);
+}
+
 // create_quantization_table (src/measure_coding_error.cpp:374-438) over the C ABI: the same table for the same
 // (already sampled) image, installed as the reference's global prediction-coding table.  measure_coding_error.cpp
 // also holds the offline curve study that main.cpp:770 calls, so this is a second name: main.cpp:322 calls it in

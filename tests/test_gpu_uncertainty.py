@@ -194,3 +194,22 @@ def test_uncertainty_errors(gpu_context):
         assert e.value.status == 6
     finally:
         fresh.close()
+
+
+def test_uncertainty_table_given_whole(gpu_context):
+    """mraygb_upload_uncertainty_table (the table read_from_disk_uncertainty returns, as the reference's convolution
+    seam takes it) renders the same image as the table built on the device."""
+    import mray_gb300 as M
+
+    wl = small_ml(64, 48, 16)
+    ref = O.workload_generate(wl, "f32")
+    ep = M.ErrorReconstructionParameters(error_type=M.MAX_ERROR, step_size=wl.rec.step_size, bias=wl.rec.bias)
+    _, eb = _oracle_errors(wl, ref, ep, "f32")
+    mi = _host_image(M, wl, ref)
+    mi.error_bounds = eb.reshape(-1).copy()
+    up = M.UncertaintyReconstructionParameters(rec=wl.rec, error_type=M.MAX_ERROR)
+    gpu_context.upload_uncertainty_tf(M.read_from_disk_uncertainty(wl.tf1d, wl.tf_step, M.MAX_ERROR))
+    built = gpu_context.reconstruct_uncertainty(wl.camera, up, 1, mi).rgba_float.copy()
+    gpu_context.upload_uncertainty_table(O.uncertainty_tf(wl.tf1d, wl.tf_step, M.MAX_ERROR))
+    given = gpu_context.reconstruct_uncertainty(wl.camera, up, 1, mi).rgba_float
+    assert np.array_equal(built, given)  # the box table is bit-exact, so the images are too
