@@ -9,6 +9,8 @@
  *   mraygb_reconstruction_params  <- ReconstructionParameters (src/parameters.h:231-247)
  *   mraygb_error_params           <- ErrorReconstructionParameters (src/parameters.h:124-137)
  *   mraygb_uncertainty_params     <- UncertaintyReconstructionParameters (src/parameters.h:319-325)
+ *   mraygb_single_scattering_params <- SingleScatteringParameters (src/parameters.h:173-193)
+ *   mraygb_reference_params       <- ReferenceParameters (src/parameters.h:339-350)
  *
  * C++ `bool` members are stored as uint8_t (same size and alignment under the
  * Itanium and AAPCS64 ABIs).  No CUDA or torch types appear here.
@@ -107,6 +109,38 @@ typedef struct mraygb_uncertainty_params
     float bound_interpolation; /* 0.5 */
     int32_t error_type;        /* 1 = MRAYGB_ERROR_RMSE */
 } mraygb_uncertainty_params;
+
+/* SingleScatteringParameters (src/parameters.h:173-193), same defaults.  The direction is used as given (the
+ * reference does not normalise it). */
+typedef struct mraygb_single_scattering_params
+{
+    uint8_t enable;           /* 0 */
+    uint8_t use_cache;        /* 1 (the cached form is not on this path; the reference renderer marches) */
+    uint8_t pad0[2];
+    int32_t cache_size_x;     /* 128 */
+    int32_t cache_size_y;     /* 128 */
+    int32_t cache_size_z;     /* 128 */
+    float step_size_factor;   /* 1.0 */
+    float henyey_greenstein_g; /* 0.0 */
+    float direction_x;        /* 0.0 */
+    float direction_y;        /* -1.0 */
+    float direction_z;        /* 0.1 */
+    float intensity_r;        /* 1.0 */
+    float intensity_g;        /* 1.0 */
+    float intensity_b;        /* 1.0 */
+} mraygb_single_scattering_params;
+
+/* ReferenceParameters (src/parameters.h:339-350), same defaults. */
+typedef struct mraygb_reference_params
+{
+    float step_size;             /* 1.0 */
+    float medium_emission;       /* 0.1 */
+    float medium_scattering;     /* 0.1 */
+    float early_ray_termination; /* 0.95 */
+    float data_min;              /* 0.0 */
+    float data_max;              /* 1.0 */
+    mraygb_single_scattering_params ss;
+} mraygb_reference_params;
 
 /* Coding warps (src/coding_params.h:35-42). */
 enum

@@ -210,3 +210,66 @@ class UncertaintyReconstructionParameters(C.Structure):
             if not hasattr(self, k):
                 raise AttributeError(k)
             setattr(self, k, v)
+
+
+class SingleScatteringParameters(C.Structure):
+    """``SingleScatteringParameters`` (parameters.h:173-193) with the reference's defaults."""
+
+    _fields_ = [
+        ("enable", C.c_uint8),
+        ("use_cache", C.c_uint8),
+        ("pad0", C.c_uint8 * 2),
+        ("cache_size_x", C.c_int32),
+        ("cache_size_y", C.c_int32),
+        ("cache_size_z", C.c_int32),
+        ("step_size_factor", C.c_float),
+        ("henyey_greenstein_g", C.c_float),
+        ("direction_x", C.c_float),
+        ("direction_y", C.c_float),
+        ("direction_z", C.c_float),
+        ("intensity_r", C.c_float),
+        ("intensity_g", C.c_float),
+        ("intensity_b", C.c_float),
+    ]
+
+    def __init__(self, **kw):
+        super().__init__()
+        self.enable = 0
+        self.use_cache = 1
+        self.cache_size_x = self.cache_size_y = self.cache_size_z = 128
+        self.step_size_factor = 1.0
+        self.henyey_greenstein_g = 0.0
+        self.direction_x, self.direction_y, self.direction_z = 0.0, -1.0, 0.1
+        self.intensity_r = self.intensity_g = self.intensity_b = 1.0
+        for k, v in kw.items():
+            if not hasattr(self, k):
+                raise AttributeError(k)
+            setattr(self, k, v)
+
+
+class ReferenceParameters(C.Structure):
+    """``ReferenceParameters`` (parameters.h:339-350) with the reference's defaults."""
+
+    _fields_ = [
+        ("step_size", C.c_float),
+        ("medium_emission", C.c_float),
+        ("medium_scattering", C.c_float),
+        ("early_ray_termination", C.c_float),
+        ("data_min", C.c_float),
+        ("data_max", C.c_float),
+        ("ss", SingleScatteringParameters),
+    ]
+
+    def __init__(self, **kw):
+        super().__init__()
+        self.step_size = 1.0
+        self.medium_emission = 0.1
+        self.medium_scattering = 0.1
+        self.early_ray_termination = 0.95
+        self.data_min = 0.0
+        self.data_max = 1.0
+        self.ss = SingleScatteringParameters()
+        for k, v in kw.items():
+            if not hasattr(self, k):
+                raise AttributeError(k)
+            setattr(self, k, v)

@@ -151,7 +151,11 @@ typedef struct oracle_options
                                               const uint32_t *index, const R *data, int prediction_code,           \
                                               int coding_warp, const uint16_t *coding_params,                      \
                                               const uint16_t *bounds, const uint16_t *error_bounds, const R *T,    \
-                                              R *rgba, const oracle_options *opt);
+                                              R *rgba, const oracle_options *opt);                         \
+    /* reference direct volume rendering (moment_raymarcher.cpp:45-79)                                      */     \
+    void oracle_generate_reference_##SFX(const mraygb_camera *cam, const mraygb_reference_params *rp,             \
+                                         const oracle_grid *grid, const oracle_particles *parts, int width,        \
+                                         int height, const R *T, R *rgba, const oracle_options *opt);
 
 ORACLE_DECL(float, f32)
 ORACLE_DECL(double, f64)

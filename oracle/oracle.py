@@ -158,6 +158,10 @@ def _declare(L):
         getattr(L, f"oracle_reconstruct_uncertainty_{sfx}").argtypes = [
             C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float * 3, C.c_float * 3, C.c_void_p,
             C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    for sfx in ("f32", "f64"):
+        getattr(L, f"oracle_generate_reference_{sfx}").argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                                   C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                                                   C.c_void_p]
     L.oracle_set_rounded_trig.argtypes = [C.c_int]
     L.oracle_set_rounded_trig.restype = None
     L.oracle_sample_moment_image.restype = C.c_uint64
@@ -464,6 +468,23 @@ def reconstruct_uncertainty(cam, up, mode, width, height, m, dmin, dmax, index, 
         C.byref(cam), C.byref(up), int(mode), width, height, m, (C.c_float * 3)(*dmin), (C.c_float * 3)(*dmax),
         _ptr(idx), _ptr(d), int(prediction_code), int(coding_warp), _ptr(cp), _ptr(b), _ptr(eb), _ptr(t), _ptr(out),
         C.byref(o))
+    return out
+
+
+def generate_reference(cam, rp, volume, dmin, dmax, width, height, tf_table, precision="f32", nthreads=0,
+                       rows=None, particles=None):
+    """reference_host: direct volume rendering of the volume (a grid, or ``particles`` when given) with the
+    preintegrated row; float RGBA[H,W,4]."""
+    L = lib()
+    dt = _dt(precision)
+    g, keep = (_grid(volume, dmin, dmax) if particles is None else (None, None))
+    t = np.ascontiguousarray(tf_table, dtype=dt)
+    out = np.zeros((height, width, 4), dtype=dt)
+    o = options(nthreads, rows)
+    getattr(L, f"oracle_generate_reference_{precision}")(
+        C.byref(cam), C.byref(rp), C.byref(g) if g is not None else None,
+        particles.handle if particles is not None else None, width, height, _ptr(t), _ptr(out), C.byref(o))
+    del keep
     return out
 
 

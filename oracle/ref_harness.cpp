@@ -13,6 +13,7 @@
 #include "moment_raymarcher.h"
 #include "raymarch_generate.h"
 #include "raymarch_reconstruct.h"
+#include "raymarch_reference.h"
 #include "moment_compaction.h"
 #include "moment_image.h"
 #include "moment_image_sample.h"
@@ -117,6 +118,31 @@ MomentImageHost make_mi(int w, int h, int m, const uint32_t *index, const float 
     if (dmin)
         mi.domain = to_range(dmin, dmax);
     return mi;
+}
+
+ReferenceParameters to_ref(const mraygb_reference_params *r)
+{
+    ReferenceParameters p;
+    p.step_size = r->step_size;
+    p.medium_emission = r->medium_emission;
+    p.medium_scattering = r->medium_scattering;
+    p.early_ray_termination = r->early_ray_termination;
+    p.data_min = r->data_min;
+    p.data_max = r->data_max;
+    p.ss.enable = r->ss.enable != 0;
+    p.ss.use_cache = r->ss.use_cache != 0;
+    p.ss.cache_size_x = r->ss.cache_size_x;
+    p.ss.cache_size_y = r->ss.cache_size_y;
+    p.ss.cache_size_z = r->ss.cache_size_z;
+    p.ss.step_size_factor = r->ss.step_size_factor;
+    p.ss.henyey_greenstein_g = r->ss.henyey_greenstein_g;
+    p.ss.direction_x = r->ss.direction_x;
+    p.ss.direction_y = r->ss.direction_y;
+    p.ss.direction_z = r->ss.direction_z;
+    p.ss.intensity_r = r->ss.intensity_r;
+    p.ss.intensity_g = r->ss.intensity_g;
+    p.ss.intensity_b = r->ss.intensity_b;
+    return p;
 }
 
 ErrorReconstructionParameters to_err(const mraygb_error_params *e)
@@ -506,6 +532,46 @@ int ref_reconstruct_uncertainty_float(const mraygb_camera *c, const mraygb_uncer
                     color = reconstruct_ray_uncertainty_tf(ray, mi.domain, cam.znear, bound_rec, tf, ss, params.rec);
                 }
             }
+            float *o = out + 4 * (size_t(y) * w + x);
+            o[0] = color.x;
+            o[1] = color.y;
+            o[2] = color.z;
+            o[3] = color.w;
+        }
+    return 0;
+}
+
+/* generate_reference (moment_raymarcher.cpp:74-80 -> reference_host :45-61) over a float grid: u8 RGBA. */
+int ref_generate_reference_u8(const mraygb_camera *c, const mraygb_reference_params *r, const float *vol, int nx,
+                              int ny, int nz, const float *dmin, const float *dmax, int w, int h, const float *tf_row,
+                              uint8_t *out)
+{
+    RegularGrid grid(Vec3i(nx, ny, nz), to_range(dmin, dmax), std::vector<float>(vol, vol + size_t(nx) * ny * nz),
+                     RegularGrid::DataType::F32);
+    auto tf = make_tf(tf_row);
+    ColorImageHost img(w, h);
+    generate_reference(to_camera(c), tf, grid, img, to_ref(r));
+    std::memcpy(out, img.rgba.data(), 4 * size_t(w) * h);
+    return 0;
+}
+
+/* The per-pixel body of reference_host (reference_ray with SingleScatteringBruteForce) keeping the float colour. */
+int ref_generate_reference_float(const mraygb_camera *c, const mraygb_reference_params *r, const float *vol, int nx,
+                                 int ny, int nz, const float *dmin, const float *dmax, int w, int h,
+                                 const float *tf_row, float *out)
+{
+    RegularGrid grid(Vec3i(nx, ny, nz), to_range(dmin, dmax), std::vector<float>(vol, vol + size_t(nx) * ny * nz),
+                     RegularGrid::DataType::F32);
+    auto tf = make_tf(tf_row);
+    auto cam = to_camera(c);
+    auto params = to_ref(r);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int y = 0; y < h; ++y)
+        for (int x = 0; x < w; ++x)
+        {
+            Vec2f ndc(x / static_cast<float>(w) * 2.f - 1.f, y / static_cast<float>(h) * 2.f - 1.f);
+            Vec4f color = reference_ray(grid, cut::get_eye_ray(cam, ndc), cam.znear, tf, SingleScatteringBruteForce{},
+                                        params);
             float *o = out + 4 * (size_t(y) * w + x);
             o[0] = color.x;
             o[1] = color.y;

@@ -21,6 +21,8 @@ on seeded inputs and stores inputs and outputs as small .npz files:
                       pairs (measure_coding_error.cpp needs HDF5, so the harness composes its loop from the
                       reference's own sample_moment_image, transform_dequantization_real, decode and
                       exponentialToTrigonometricMoments)
+  reference_dvr.npz   generate_reference's direct volume rendering of the Marschner-Lobb volume, without and with
+                      brute-force single scattering
   uncertainty.npz     error bounds of reconstruct_error (max, RMSE, P^2 percentile at 90 and 50), rows of the two
                       uncertainty tables of read_from_disk_uncertainty and the float colours of the interpolation
                       and convolution renderers on the Marschner-Lobb pipeline image
@@ -67,6 +69,7 @@ def declare(ref):
     ref.ref_uncertainty_tf.argtypes = [vp, f, i, vp]
     ref.ref_reconstruct_uncertainty_float.argtypes = [vp, vp, i, i, i, i, vp, vp, u64, vp, vp, i, i, vp, vp, vp, vp,
                                                       vp]
+    ref.ref_generate_reference_float.argtypes = [vp, vp, vp, i, i, i, vp, vp, i, i, vp, vp]
     ref.ref_sample_moment_image.restype = u64
     ref.ref_sample_moment_image.argtypes = [C.c_int, C.c_int, C.c_int, vp, vp, u64, C.c_int, vp, vp]
     ref.ref_coding_errors.restype = C.c_uint32
@@ -495,6 +498,30 @@ def uncertainty(ref):
     return out
 
 
+def reference_dvr(ref):
+    """generate_reference (direct volume rendering of the volume itself) without and with brute-force single
+    scattering, float colours from the reference's own reference_ray on the Marschner-Lobb volume."""
+    from mray_gb300.types import ReferenceParameters, SingleScatteringParameters
+
+    out = {}
+    wl = W.ml_workload(n=64, width=48, height=40, num_moments=16, seed=11, name="golden_ml")
+    vol = np.ascontiguousarray(wl.volume)
+    nz, ny, nx = vol.shape
+    dmin, dmax = f32(*wl.domain_min), f32(*wl.domain_max)
+    row = np.zeros((256, 4), np.float32)
+    ref.ref_preintegrate(P(np.ascontiguousarray(wl.tf1d, np.float32)), C.c_float(wl.tf_step), P(row))
+    cases = {"plain": dict(enable=0), "ss": dict(enable=1, henyey_greenstein_g=0.3, step_size_factor=2.0,
+                                                   direction_x=0.3, direction_y=-1.0, direction_z=0.2)}
+    for name, ss in cases.items():
+        rp = ReferenceParameters(step_size=wl.rec.step_size, medium_emission=1.0, early_ray_termination=0.99,
+                                 medium_scattering=0.5, ss=SingleScatteringParameters(**ss))
+        rgba = np.zeros((wl.height, wl.width, 4), np.float32)
+        ref.ref_generate_reference_float(C.byref(wl.camera), C.byref(rp), P(vol), nx, ny, nz, P(dmin), P(dmax),
+                                         wl.width, wl.height, P(row), P(rgba))
+        out[f"{name}_rgba"] = rgba
+    return out
+
+
 def main():
     ref = O.ref_lib()
     if ref is None:
@@ -510,6 +537,7 @@ def main():
     np.savez_compressed(os.path.join(HERE, "particles.npz"), **particles(ref))
     np.savez_compressed(os.path.join(HERE, "quant_curve.npz"), **quant_curve(ref))
     np.savez_compressed(os.path.join(HERE, "uncertainty.npz"), **uncertainty(ref))
+    np.savez_compressed(os.path.join(HERE, "reference_dvr.npz"), **reference_dvr(ref))
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

@@ -37,13 +37,16 @@ def test_library_exports_every_declared_symbol():
 def test_struct_layouts_match_the_c_header(tmp_path):
     """sizeof / offsetof of the POD mirrors as gcc lays out include/mraygb_types.h, against the ctypes mirrors."""
     from mray_gb300.types import (Camera, ErrorReconstructionParameters, GenerationParameters,
-                                  ReconstructionParameters, UncertaintyReconstructionParameters)
+                                  ReconstructionParameters, ReferenceParameters, SingleScatteringParameters,
+                                  UncertaintyReconstructionParameters)
 
     src = tmp_path / "layout.c"
     classes = {"mraygb_camera": Camera, "mraygb_generation_params": GenerationParameters,
                "mraygb_reconstruction_params": ReconstructionParameters,
                "mraygb_error_params": ErrorReconstructionParameters,
-               "mraygb_uncertainty_params": UncertaintyReconstructionParameters}
+               "mraygb_uncertainty_params": UncertaintyReconstructionParameters,
+               "mraygb_single_scattering_params": SingleScatteringParameters,
+               "mraygb_reference_params": ReferenceParameters}
     fields = {st: [f[0] for f in cls._fields_] for st, cls in classes.items()}
     lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{ROOT}/include/mraygb_types.h"', 'int main(){']
     for st, fl in fields.items():

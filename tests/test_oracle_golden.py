@@ -449,3 +449,22 @@ def test_error_bounds_and_uncertainty_bit_exact():
     # the P^2 estimate moves with the percentile and stays below the maximum on average
     pct50, pct90 = g["pc0_eb2_50"].astype(float), g["pc0_eb2_90"].astype(float)
     assert pct50.mean() < pct90.mean() <= g["pc0_eb0_90"].astype(float).mean()
+
+
+# ---- reference direct volume rendering (raymarch_reference.h) ------------------------------------------------------
+
+def test_reference_dvr_bit_exact():
+    from mray_gb300.types import ReferenceParameters, SingleScatteringParameters
+
+    g = load("reference_dvr.npz")
+    wl = W.ml_workload(n=64, width=48, height=40, num_moments=16, seed=11, name="golden_ml")
+    row = O.preintegrate(wl.tf1d, wl.tf_step)
+    cases = {"plain": dict(enable=0), "ss": dict(enable=1, henyey_greenstein_g=0.3, step_size_factor=2.0,
+                                                   direction_x=0.3, direction_y=-1.0, direction_z=0.2)}
+    for name, ss in cases.items():
+        rp = ReferenceParameters(step_size=wl.rec.step_size, medium_emission=1.0, early_ray_termination=0.99,
+                                 medium_scattering=0.5, ss=SingleScatteringParameters(**ss))
+        rgba = O.generate_reference(wl.camera, rp, wl.volume, wl.domain_min, wl.domain_max, wl.width, wl.height, row)
+        assert np.array_equal(rgba, g[f"{name}_rgba"]), name
+    # in-scattered light brightens the image where the medium scatters
+    assert g["ss_rgba"][..., :3].mean() > g["plain_rgba"][..., :3].mean()
