@@ -830,6 +830,13 @@ def run_uncertainty(args, local):
     ms = timed(lambda: ctx.stage_reconstruct(wl.camera, wl.rec, Wd, H, m, wl.domain_min, wl.domain_max, idx, pm, b,
                                              rgba))
     out["plain_reconstruct"] = {"value": P / (ms * 1e-3) / 1e6, "unit": UNIT, "ms": ms}
+    # the reference direct volume rendering of the same volume (the ground truth of the moment path), at the
+    # generation step
+    rp = M.ReferenceParameters(step_size=wl.gen.step_size, medium_emission=wl.rec.medium_emission,
+                               early_ray_termination=wl.rec.early_ray_termination, data_min=wl.gen.data_min,
+                               data_max=wl.gen.data_max)
+    ms = timed(lambda: ctx.stage_generate_reference(wl.camera, rp, Wd, H, rgba))
+    out["reference_dvr"] = {"value": P / (ms * 1e-3) / 1e6, "unit": UNIT, "ms": ms}
     # the oracle (the reference's CPU method) on every 64th row of the same image
     index = idx.cpu().numpy().view(np.uint32)
     data = cm[:int(index[-1])].cpu().numpy()

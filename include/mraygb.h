@@ -200,6 +200,14 @@ int mraygb_reconstruct_uncertainty(mraygb_context *ctx, const mraygb_camera *cam
                                    int prediction_code, int coding_warp, const uint16_t *h_coding_params,
                                    float *h_rgba, uint8_t *h_rgba8);
 
+/* generate_reference (src/moment_raymarcher.cpp:64-80; GPU src/moment_raymarcher.cu:65-114): direct volume
+ * rendering of the volume uploaded last with the transfer function of mraygb_upload_tf (reference_ray,
+ * src/raymarch_reference.h:93-160), the ground truth of the moment path.  With rp->ss.enable and a positive
+ * medium_scattering every sample marches a secondary ray towards the light (the brute-force transmittance of
+ * raymarch_reference.h:40-75; the cached form is not on this path).  Outputs as mraygb_reconstruct. */
+int mraygb_generate_reference(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_reference_params *rp,
+                              int width, int height, float *h_rgba, uint8_t *h_rgba8);
+
 /* ---- stage API: device pointers, ordered on the context stream ------------------------------------------ */
 
 /* Per-ray moments over the uploaded grid (generate_ray, src/raymarch_generate.h:69-148, driven as
@@ -259,6 +267,10 @@ int mraygb_stage_reconstruct_uncertainty(mraygb_context *ctx, const mraygb_camer
                                          int num_moments, const float domain_min[3], const float domain_max[3],
                                          const uint32_t *d_index, const float *d_pmoments, const uint16_t *d_bounds,
                                          const uint16_t *d_error_bounds, float *d_rgba);
+
+/* mraygb_generate_reference into device memory: d_rgba W*H*4 floats. */
+int mraygb_stage_generate_reference(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_reference_params *rp,
+                                    int width, int height, float *d_rgba);
 
 /* Compaction that allocates nothing, for callers that must not call cudaMalloc / cudaFree while they work:
  * renderers and services that reserve all device memory up front in their own pool or arena (where an

@@ -6,12 +6,13 @@ grid and transfer-function containers) and calls the C ABI through ctypes.
 """
 from .types import (CODING_WARP_DEFAULT_TRANSFORMED, CODING_WARP_NONE, ERROR_PERCENTILE, MAX_ERROR, RMSE, Camera,
                     ErrorReconstructionParameters, GenerationParameters, ReconstructionParameters,
-                    UncertaintyReconstructionParameters)
+                    ReferenceParameters, SingleScatteringParameters, UncertaintyReconstructionParameters)
 from .raymarcher import (MAX_MOMENTS, PRECISION_COMPENSATED_FF_MESE, PRECISION_COMPENSATED_FP64_MESE, PRECISION_FP32, ColorImageHost, Context,
                          MomentImageHost, Particles, RegularGrid, TransferFunction, default_context, default_quantization_table,
                          generate, preintegrate, quantize_prediction_coding, reconstruct,
                          create_quantization_table, UncertaintyTransferFunction, read_from_disk_uncertainty,
-                         reconstruct_error, reconstruct_uncertainty_interpolation, reconstruct_uncertainty_convolution)
+                         reconstruct_error, reconstruct_uncertainty_interpolation, reconstruct_uncertainty_convolution,
+                         generate_reference)
 from ._lib import MrayError
 
 __all__ = [
@@ -21,5 +22,6 @@ __all__ = [
     "PRECISION_COMPENSATED_FP64_MESE", "PRECISION_COMPENSATED_FF_MESE", "MAX_MOMENTS",
     "ErrorReconstructionParameters", "UncertaintyReconstructionParameters", "MAX_ERROR", "RMSE", "ERROR_PERCENTILE",
     "UncertaintyTransferFunction", "read_from_disk_uncertainty", "reconstruct_error",
-    "reconstruct_uncertainty_interpolation", "reconstruct_uncertainty_convolution",
+    "reconstruct_uncertainty_interpolation", "reconstruct_uncertainty_convolution", "generate_reference",
+    "ReferenceParameters", "SingleScatteringParameters",
 ]

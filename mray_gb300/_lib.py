@@ -9,7 +9,7 @@ import os
 import threading
 
 from .types import (Camera, ErrorReconstructionParameters, GenerationParameters, ReconstructionParameters,
-                    UncertaintyReconstructionParameters)
+                    ReferenceParameters, UncertaintyReconstructionParameters)
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libmraygb.so")
@@ -29,6 +29,7 @@ EXPORTS = [
     "mraygb_diff_backward", "mraygb_create_quantization_table", "mraygb_stage_create_quantization_table",
     "mraygb_reconstruct_error", "mraygb_stage_reconstruct_error", "mraygb_upload_uncertainty_tf",
     "mraygb_reconstruct_uncertainty", "mraygb_stage_reconstruct_uncertainty", "mraygb_upload_uncertainty_table",
+    "mraygb_generate_reference", "mraygb_stage_generate_reference",
 ]
 
 _lock = threading.Lock()
@@ -86,6 +87,8 @@ def _declare(L):
     L.mraygb_stage_reconstruct_error.argtypes = [vp, P(Camera), EP, i, i, i, vp, vp, vp, vp, vp]
     L.mraygb_upload_uncertainty_tf.argtypes = [vp, vp, C.c_float, i, vp]
     L.mraygb_upload_uncertainty_table.argtypes = [vp, vp]
+    L.mraygb_generate_reference.argtypes = [vp, P(Camera), P(ReferenceParameters), i, i, vp, vp]
+    L.mraygb_stage_generate_reference.argtypes = [vp, P(Camera), P(ReferenceParameters), i, i, vp]
     L.mraygb_reconstruct_uncertainty.argtypes = [vp, P(Camera), UP, i, i, i, i, f3, f3, vp, vp, u64, vp, vp, i, i, vp,
                                                  vp, vp]
     L.mraygb_stage_reconstruct_uncertainty.argtypes = [vp, P(Camera), UP, i, i, i, i, f3, f3, vp, vp, vp, vp, vp]

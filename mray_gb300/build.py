@@ -37,6 +37,7 @@ SOURCES = [
     ("coding.cu", ["--fmad=false"]),
     ("quant_curve.cu", ["--fmad=false"]),
     ("uncertainty.cu", ["--fmad=false"]),
+    ("reference.cu", []),
     ("api.cpp", ["-x", "cu"]),
 ]
 

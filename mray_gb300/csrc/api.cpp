@@ -568,6 +568,43 @@ int run_uncertainty(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_
     return MRAYGB_OK;
 }
 
+int validate_reference(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_reference_params *rp)
+{
+    if (!cam || !rp)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "NULL camera or parameters");
+    if (!(rp->step_size > 0.f))
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "step_size must be > 0 (got %g)", (double)rp->step_size);
+    if (rp->ss.enable && !(rp->ss.step_size_factor > 0.f))
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "single-scattering step_size_factor must be > 0 (got %g)",
+                    (double)rp->ss.step_size_factor);
+    if (ctx->volume == mraygb_context::NONE)
+        return fail(ctx, MRAYGB_NO_VOLUME, "no volume uploaded");
+    if (!ctx->has_tf)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "no transfer function uploaded");
+    return MRAYGB_OK;
+}
+
+int run_reference(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_reference_params *rp, int width,
+                  int height, float *d_rgba, uint8_t *d_rgba8)
+{
+    const DeviceCamera dc = to_device_camera(*cam);
+    ReferenceArgs a;
+    a.cam = &dc;
+    a.width = width;
+    a.height = height;
+    a.rp = rp;
+    a.tf = ctx->tf.as<float4>();
+    a.rgba = d_rgba;
+    a.rgba8 = d_rgba8;
+    if (ctx->volume == mraygb_context::PARTICLES)
+        CK(launch_reference_particles(particle_view(ctx), a, ctx->error_flag.as<int>(), ctx->stream),
+           "reference launch");
+    else
+        CK(launch_reference_grid(grid_view(ctx), a, ctx->error_flag.as<int>(), ctx->stream), "reference launch");
+    ctx->launches += 1;
+    return MRAYGB_OK;
+}
+
 int validate_rec(mraygb_context *ctx, const mraygb_reconstruction_params *rp)
 {
     if (!rp)
@@ -1417,6 +1454,49 @@ int mraygb_upload_uncertainty_tf(mraygb_context *ctx, const float *tf1d_rgba256,
     CK(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
     ctx->has_unc_table = true;
     return MRAYGB_OK;
+}
+
+// ---- reference direct volume rendering ------------------------------------------------------------------------
+
+int mraygb_stage_generate_reference(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_reference_params *rp,
+                                    int width, int height, float *d_rgba)
+{
+    CHECK_CTX();
+    int rc = check_image(ctx, width, height, 1);
+    if (rc)
+        return rc;
+    if ((rc = validate_reference(ctx, cam, rp)))
+        return rc;
+    if (!d_rgba)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "NULL colour buffer");
+    return run_reference(ctx, cam, rp, width, height, d_rgba, nullptr);
+}
+
+int mraygb_generate_reference(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_reference_params *rp,
+                              int width, int height, float *h_rgba, uint8_t *h_rgba8)
+{
+    CHECK_CTX();
+    int rc = check_image(ctx, width, height, 1);
+    if (rc)
+        return rc;
+    if ((rc = validate_reference(ctx, cam, rp)))
+        return rc;
+    if (!h_rgba && !h_rgba8)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "no output");
+    const size_t P = (size_t)width * (size_t)height;
+    CK(ctx->rgba.reserve(P * 4 * sizeof(float)), "colour buffer allocation");
+    if (h_rgba8)
+        CK(ctx->rgba8.reserve(P * 4), "u8 colour buffer allocation");
+    if ((rc = run_reference(ctx, cam, rp, width, height, ctx->rgba.as<float>(),
+                            h_rgba8 ? ctx->rgba8.as<uint8_t>() : nullptr)))
+        return rc;
+    if (h_rgba)
+        CK(cudaMemcpyAsync(h_rgba, ctx->rgba.ptr, P * 4 * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream),
+           "colour download");
+    if (h_rgba8)
+        CK(cudaMemcpyAsync(h_rgba8, ctx->rgba8.ptr, P * 4, cudaMemcpyDeviceToHost, ctx->stream), "u8 colour download");
+    CK(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+    return check_device_error_flag(ctx);
 }
 
 int mraygb_upload_uncertainty_table(mraygb_context *ctx, const float *table_rgba256x256)

@@ -105,6 +105,20 @@ struct UncertaintyArgs
 };
 cudaError_t launch_uncertainty(const UncertaintyArgs &a, int *error_flag, cudaStream_t stream);
 
+// reference.cu: direct volume rendering of the resident volume (the ground truth)
+struct ReferenceArgs
+{
+    const DeviceCamera *cam;
+    int width, height;
+    const mraygb_reference_params *rp;
+    const float4 *tf; // preintegrated row
+    float *rgba;      // W*H float4 or null
+    uint8_t *rgba8;   // W*H uchar4 or null
+};
+cudaError_t launch_reference_grid(const GridView &grid, const ReferenceArgs &a, int *error_flag, cudaStream_t stream);
+cudaError_t launch_reference_particles(const ParticleView &parts, const ReferenceArgs &a, int *error_flag,
+                                       cudaStream_t stream);
+
 // quant_curve.cu: the data-dependent quantization table's error means for every (index, bits) pair
 // scratch bytes for an sx x sy sample, bits bmin .. bmin + nb - 1, rows_per_pass moment indices per pass
 size_t quant_curve_scratch_bytes(int sx, int sy, int m, int nb, size_t rows_per_pass);

@@ -22,7 +22,7 @@ import numpy as np
 
 from . import _lib
 from .types import (Camera, ErrorReconstructionParameters, GenerationParameters, ReconstructionParameters,
-                    UncertaintyReconstructionParameters)
+                    ReferenceParameters, UncertaintyReconstructionParameters)
 
 PRECISION_FP32 = 0
 PRECISION_COMPENSATED_FP64_MESE = 1
@@ -380,6 +380,18 @@ class Context:
                                                            _hptr(img.rgba)))
         return img
 
+    def generate_reference(self, cam: Camera, rp: ReferenceParameters, width: int, height: int,
+                           img: Optional[ColorImageHost] = None) -> ColorImageHost:
+        """generate_reference (moment_raymarcher.cpp:64-80) over the volume and transfer function uploaded last."""
+        img = img or ColorImageHost(width, height)
+        self._check(self._L.mraygb_generate_reference(self._h, C.byref(cam), C.byref(rp), width, height,
+                                                      _hptr(img.rgba_float), _hptr(img.rgba)))
+        return img
+
+    def stage_generate_reference(self, cam, rp, width, height, rgba):
+        self._check(self._L.mraygb_stage_generate_reference(self._h, C.byref(cam), C.byref(rp), width, height,
+                                                            _dptr(rgba)))
+
     def quantize_prediction_coding(self, mi: MomentImageHost, table) -> np.ndarray:
         """quantize_prediction_coding(mi, table) (moment_quantization.cpp:239-276): the packed code bytes."""
         if not mi.is_compact:
@@ -597,3 +609,13 @@ def reconstruct_uncertainty_convolution(cam: Camera, mi: MomentImageHost, tf: Un
     ctx = context or default_context()
     ctx.upload_uncertainty_tf(tf)
     ctx.reconstruct_uncertainty(cam, params, 1, mi, img)
+
+
+def generate_reference(cam: Camera, tf: TransferFunction, volume, img: ColorImageHost, params: ReferenceParameters,
+                       context: Optional[Context] = None) -> None:
+    """generate_reference(cam, tf, volume, img, params) (moment_raymarcher.h, moment_raymarcher.cpp:64-80): direct
+    volume rendering of a RegularGrid or Particles into ``img``."""
+    ctx = context or default_context()
+    _upload_volume(ctx, volume)
+    ctx.upload_tf(tf.table)
+    ctx.generate_reference(cam, params, img.width, img.height, img)

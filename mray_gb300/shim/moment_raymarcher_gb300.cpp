@@ -269,6 +269,72 @@ void uncertainty(const cut::Camera &cam, const MomentImageHost &mi, ColorImageHo
 
 } // namespace
 
+namespace
+{
+
+mraygb_reference_params to_c(const ReferenceParameters &p)
+{
+    mraygb_reference_params o{};
+    o.step_size = p.step_size;
+    o.medium_emission = p.medium_emission;
+    o.medium_scattering = p.medium_scattering;
+    o.early_ray_termination = p.early_ray_termination;
+    o.data_min = p.data_min;
+    o.data_max = p.data_max;
+    o.ss.enable = p.ss.enable;
+    o.ss.use_cache = p.ss.use_cache;
+    o.ss.cache_size_x = p.ss.cache_size_x;
+    o.ss.cache_size_y = p.ss.cache_size_y;
+    o.ss.cache_size_z = p.ss.cache_size_z;
+    o.ss.step_size_factor = p.ss.step_size_factor;
+    o.ss.henyey_greenstein_g = p.ss.henyey_greenstein_g;
+    o.ss.direction_x = p.ss.direction_x;
+    o.ss.direction_y = p.ss.direction_y;
+    o.ss.direction_z = p.ss.direction_z;
+    o.ss.intensity_r = p.ss.intensity_r;
+    o.ss.intensity_g = p.ss.intensity_g;
+    o.ss.intensity_b = p.ss.intensity_b;
+    return o;
+}
+
+void reference_uploaded(const cut::Camera &cam, const TransferFunction &tf, ColorImageHost &img,
+                        const ReferenceParameters &params)
+{
+    check(mraygb_upload_tf(context(), reinterpret_cast<const float *>(tf.data.data())));
+    const auto c = to_c(cam);
+    const auto r = to_c(params);
+    check(mraygb_generate_reference(context(), &c, &r, img.width, img.height, nullptr,
+                                    reinterpret_cast<uint8_t *>(img.rgba.data())));
+}
+
+} // namespace
+
+// generate_reference_device (src/moment_raymarcher.cuh:38-41) for both volume types
+void generate_reference_device(cut::Camera cam, const RegularGrid &volume, const TransferFunction &tf,
+                               ColorImageHost &img, const ReferenceParameters &params)
+{
+    if (volume.type != RegularGrid::DataType::F32)
+    {
+        std::fprintf(stderr, "mraygb: only float grids are supported\n");
+        std::terminate();
+    }
+    const float dmin[3] = {volume.domain.min.x, volume.domain.min.y, volume.domain.min.z};
+    const float dmax[3] = {volume.domain.max.x, volume.domain.max.y, volume.domain.max.z};
+    check(mraygb_upload_grid(context(), volume.data.data(), volume.size.x, volume.size.y, volume.size.z, dmin, dmax,
+                             0));
+    reference_uploaded(cam, tf, img, params);
+}
+
+void generate_reference_device(cut::Camera cam, const Particles &volume, const TransferFunction &tf,
+                               ColorImageHost &img, const ReferenceParameters &params)
+{
+    const float dmin[3] = {volume.domain.min.x, volume.domain.min.y, volume.domain.min.z};
+    const float dmax[3] = {volume.domain.max.x, volume.domain.max.y, volume.domain.max.z};
+    check(mraygb_upload_particles(context(), volume.x.data(), volume.y.data(), volume.z.data(),
+                                  volume.values.data(), volume.size(), volume.smoothing_length, dmin, dmax, 0));
+    reference_uploaded(cam, tf, img, params);
+}
+
 // reconstruct_error_device (src/moment_raymarcher.cuh:73-76) for both volume types: fills mi.error_bounds
 void reconstruct_error_device(cut::Camera cam, const RegularGrid &volume, MomentImageHost &mi,
                               const ErrorReconstructionParameters &params)
