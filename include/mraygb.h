@@ -204,9 +204,46 @@ int mraygb_reconstruct_uncertainty(mraygb_context *ctx, const mraygb_camera *cam
  * rendering of the volume uploaded last with the transfer function of mraygb_upload_tf (reference_ray,
  * src/raymarch_reference.h:93-160), the ground truth of the moment path.  With rp->ss.enable and a positive
  * medium_scattering every sample marches a secondary ray towards the light (the brute-force transmittance of
- * raymarch_reference.h:40-75; the cached form is not on this path).  Outputs as mraygb_reconstruct. */
+ * raymarch_reference.h:40-75; the cache is mraygb_generate_reference_reconstructed_ss).  Outputs as
+ * mraygb_reconstruct. */
 int mraygb_generate_reference(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_reference_params *rp,
                               int width, int height, float *h_rgba, uint8_t *h_rgba8);
+
+/* ---- single scattering: the transmittance cache ----------------------------------------------------------
+ * The cache is a float grid of rp->ss.cache_size_x * _y * _z voxels (x fastest) over the domain of the light's
+ * moment image, held by the context (SingleScatteringCacheHost, src/single_scattering_cache.h:33-59).  A
+ * reconstruction with rp->ss.enable, rp->ss.use_cache and a positive medium_scattering samples it (trilinear,
+ * RegularGrid::sample) at every sample for the in-scattered light T_ss * henyey_greenstein * intensity
+ * (inscattering, src/raymarch_reconstruct.h:36-46 and 112-125); the marched form (use_cache = 0) returns
+ * MRAYGB_NOT_SUPPORTED. */
+
+/* reconstruct_single_scattering_cache(ss, tf, params) (src/moment_raymarcher.cpp:217-258): the moment image
+ * rendered from the light (SingleScatteringImageHost::img, given by its members as in mraygb_reconstruct, the
+ * light's camera light_cam) is prepared and re-marched with the transfer function of mraygb_upload_tf at
+ * rp->step_size; every sample writes exp(-tau) into the voxel int((q - min) / (max - min) * size) of its position
+ * q (ScatterGridHost::scatter, src/scatter_grid.h:54-66).  Where several samples reach a voxel the result is that
+ * of the reference's loop run sequentially: the last pixel in row-major order, and its last sample there, wins
+ * (the reference's parallel loop leaves the order open).  Voxels no sample reaches hold 0.  The cache becomes the
+ * context's; h_cache (cache_size_x*y*z floats) receives a copy, or may be NULL. */
+int mraygb_reconstruct_single_scattering_cache(mraygb_context *ctx, const mraygb_camera *light_cam,
+                                               const mraygb_reconstruction_params *rp, int width, int height,
+                                               int num_moments, const float domain_min[3], const float domain_max[3],
+                                               const uint32_t *h_index, const float *h_data, uint64_t data_size,
+                                               const uint16_t *h_bounds, int prediction_code, int coding_warp,
+                                               const uint16_t *h_coding_params, float *h_cache);
+
+/* A cache made elsewhere (SingleScatteringCacheHost(RegularGrid)): nx*ny*nz floats, x fastest, on the box
+ * [dmin, dmax]; host pointer, or device pointer when data_on_device != 0 (copied). */
+int mraygb_upload_single_scattering_cache(mraygb_context *ctx, const float *data, int nx, int ny, int nz,
+                                          const float dmin[3], const float dmax[3], int data_on_device);
+
+/* generate_reference_reconstructed_ss (src/moment_raymarcher.cpp:259-281): generate_reference of the volume
+ * uploaded last with ref_from_rec_params(rp) (src/parameters.h:379-390), the in-scattered light's transmittance
+ * sampled from the context's cache at each sample (compute_transmittance, src/raymarch_reference.h:77-86) instead
+ * of marched.  Outputs as mraygb_reconstruct. */
+int mraygb_generate_reference_reconstructed_ss(mraygb_context *ctx, const mraygb_camera *cam,
+                                               const mraygb_reconstruction_params *rp, int width, int height,
+                                               float *h_rgba, uint8_t *h_rgba8);
 
 /* ---- stage API: device pointers, ordered on the context stream ------------------------------------------ */
 
@@ -271,6 +308,20 @@ int mraygb_stage_reconstruct_uncertainty(mraygb_context *ctx, const mraygb_camer
 /* mraygb_generate_reference into device memory: d_rgba W*H*4 floats. */
 int mraygb_stage_generate_reference(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_reference_params *rp,
                                     int width, int height, float *d_rgba);
+
+/* mraygb_reconstruct_single_scattering_cache from the light image's multipliers (mraygb_stage_prepare_moments)
+ * in device memory; d_cache receives the cache (cache_size_x*y*z floats) or may be NULL. */
+int mraygb_stage_reconstruct_single_scattering_cache(mraygb_context *ctx, const mraygb_camera *light_cam,
+                                                     const mraygb_reconstruction_params *rp, int width, int height,
+                                                     int num_moments, const float domain_min[3],
+                                                     const float domain_max[3], const uint32_t *d_index,
+                                                     const float *d_pmoments, const uint16_t *d_bounds,
+                                                     float *d_cache);
+
+/* mraygb_generate_reference_reconstructed_ss into device memory: d_rgba W*H*4 floats. */
+int mraygb_stage_generate_reference_reconstructed_ss(mraygb_context *ctx, const mraygb_camera *cam,
+                                                     const mraygb_reconstruction_params *rp, int width, int height,
+                                                     float *d_rgba);
 
 /* Compaction that allocates nothing, for callers that must not call cudaMalloc / cudaFree while they work:
  * renderers and services that reserve all device memory up front in their own pool or arena (where an

@@ -62,8 +62,29 @@ typedef struct mraygb_generation_params
     float transform_bound_eps;     /* 0.01 */
 } mraygb_generation_params;
 
-/* ReconstructionParameters (src/parameters.h:231-247), same defaults.  The
- * single-scattering block is out of scope; ss_enable must be 0. */
+/* SingleScatteringParameters (src/parameters.h:173-193), same defaults.  The direction is used as given (the
+ * reference does not normalise it). */
+typedef struct mraygb_single_scattering_params
+{
+    uint8_t enable;           /* 0 */
+    uint8_t use_cache;        /* 1 (reconstruction samples the transmittance cache; 0, the marched form, is
+                                 not supported) */
+    uint8_t pad0[2];
+    int32_t cache_size_x;     /* 128 */
+    int32_t cache_size_y;     /* 128 */
+    int32_t cache_size_z;     /* 128 */
+    float step_size_factor;   /* 1.0 */
+    float henyey_greenstein_g; /* 0.0 */
+    float direction_x;        /* 0.0 */
+    float direction_y;        /* -1.0 */
+    float direction_z;        /* 0.1 */
+    float intensity_r;        /* 1.0 */
+    float intensity_g;        /* 1.0 */
+    float intensity_b;        /* 1.0 */
+} mraygb_single_scattering_params;
+
+/* ReconstructionParameters (src/parameters.h:231-247), same defaults and the
+ * same layout (the single-scattering block starts at byte 36). */
 typedef struct mraygb_reconstruction_params
 {
     float bias;                    /* 1e-6 */
@@ -75,8 +96,8 @@ typedef struct mraygb_reconstruction_params
     float step_size;               /* 0.01 */
     float step_size_write_samples; /* 1.5 (unused on this path) */
     uint8_t use_truncated_fourier; /* 0 (must be 0: MESE only) */
-    uint8_t ss_enable;             /* 0 (must be 0) */
-    uint8_t pad0[2];
+    uint8_t pad0[3];
+    mraygb_single_scattering_params ss;
 } mraygb_reconstruction_params;
 
 /* Error measures of the per-pixel error bound (src/common.h:152-157). */
@@ -109,26 +130,6 @@ typedef struct mraygb_uncertainty_params
     float bound_interpolation; /* 0.5 */
     int32_t error_type;        /* 1 = MRAYGB_ERROR_RMSE */
 } mraygb_uncertainty_params;
-
-/* SingleScatteringParameters (src/parameters.h:173-193), same defaults.  The direction is used as given (the
- * reference does not normalise it). */
-typedef struct mraygb_single_scattering_params
-{
-    uint8_t enable;           /* 0 */
-    uint8_t use_cache;        /* 1 (the cached form is not on this path; the reference renderer marches) */
-    uint8_t pad0[2];
-    int32_t cache_size_x;     /* 128 */
-    int32_t cache_size_y;     /* 128 */
-    int32_t cache_size_z;     /* 128 */
-    float step_size_factor;   /* 1.0 */
-    float henyey_greenstein_g; /* 0.0 */
-    float direction_x;        /* 0.0 */
-    float direction_y;        /* -1.0 */
-    float direction_z;        /* 0.1 */
-    float intensity_r;        /* 1.0 */
-    float intensity_g;        /* 1.0 */
-    float intensity_b;        /* 1.0 */
-} mraygb_single_scattering_params;
 
 /* ReferenceParameters (src/parameters.h:339-350), same defaults. */
 typedef struct mraygb_reference_params

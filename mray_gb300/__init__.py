@@ -12,7 +12,8 @@ from .raymarcher import (MAX_MOMENTS, PRECISION_COMPENSATED_FF_MESE, PRECISION_C
                          generate, preintegrate, quantize_prediction_coding, reconstruct,
                          create_quantization_table, UncertaintyTransferFunction, read_from_disk_uncertainty,
                          reconstruct_error, reconstruct_uncertainty_interpolation, reconstruct_uncertainty_convolution,
-                         generate_reference)
+                         generate_reference, SingleScatteringImageHost, SingleScatteringCacheHost,
+                         reconstruct_single_scattering_cache, generate_reference_reconstructed_ss)
 from ._lib import MrayError
 
 __all__ = [
@@ -23,5 +24,6 @@ __all__ = [
     "ErrorReconstructionParameters", "UncertaintyReconstructionParameters", "MAX_ERROR", "RMSE", "ERROR_PERCENTILE",
     "UncertaintyTransferFunction", "read_from_disk_uncertainty", "reconstruct_error",
     "reconstruct_uncertainty_interpolation", "reconstruct_uncertainty_convolution", "generate_reference",
-    "ReferenceParameters", "SingleScatteringParameters",
+    "ReferenceParameters", "SingleScatteringParameters", "SingleScatteringImageHost", "SingleScatteringCacheHost",
+    "reconstruct_single_scattering_cache", "generate_reference_reconstructed_ss",
 ]

@@ -29,7 +29,9 @@ EXPORTS = [
     "mraygb_diff_backward", "mraygb_create_quantization_table", "mraygb_stage_create_quantization_table",
     "mraygb_reconstruct_error", "mraygb_stage_reconstruct_error", "mraygb_upload_uncertainty_tf",
     "mraygb_reconstruct_uncertainty", "mraygb_stage_reconstruct_uncertainty", "mraygb_upload_uncertainty_table",
-    "mraygb_generate_reference", "mraygb_stage_generate_reference",
+    "mraygb_generate_reference", "mraygb_stage_generate_reference", "mraygb_reconstruct_single_scattering_cache",
+    "mraygb_stage_reconstruct_single_scattering_cache", "mraygb_upload_single_scattering_cache",
+    "mraygb_generate_reference_reconstructed_ss", "mraygb_stage_generate_reference_reconstructed_ss",
 ]
 
 _lock = threading.Lock()
@@ -89,6 +91,12 @@ def _declare(L):
     L.mraygb_upload_uncertainty_table.argtypes = [vp, vp]
     L.mraygb_generate_reference.argtypes = [vp, P(Camera), P(ReferenceParameters), i, i, vp, vp]
     L.mraygb_stage_generate_reference.argtypes = [vp, P(Camera), P(ReferenceParameters), i, i, vp]
+    L.mraygb_reconstruct_single_scattering_cache.argtypes = [vp, P(Camera), RP, i, i, i, f3, f3, vp, vp, u64, vp, i,
+                                                             i, vp, vp]
+    L.mraygb_stage_reconstruct_single_scattering_cache.argtypes = [vp, P(Camera), RP, i, i, i, f3, f3, vp, vp, vp, vp]
+    L.mraygb_upload_single_scattering_cache.argtypes = [vp, vp, i, i, i, f3, f3, i]
+    L.mraygb_generate_reference_reconstructed_ss.argtypes = [vp, P(Camera), RP, i, i, vp, vp]
+    L.mraygb_stage_generate_reference_reconstructed_ss.argtypes = [vp, P(Camera), RP, i, i, vp]
     L.mraygb_reconstruct_uncertainty.argtypes = [vp, P(Camera), UP, i, i, i, i, f3, f3, vp, vp, u64, vp, vp, i, i, vp,
                                                  vp, vp]
     L.mraygb_stage_reconstruct_uncertainty.argtypes = [vp, P(Camera), UP, i, i, i, i, f3, f3, vp, vp, vp, vp, vp]

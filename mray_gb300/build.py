@@ -38,6 +38,7 @@ SOURCES = [
     ("quant_curve.cu", ["--fmad=false"]),
     ("uncertainty.cu", ["--fmad=false"]),
     ("reference.cu", []),
+    ("scattering.cu", []),
     ("api.cpp", ["-x", "cu"]),
 ]
 

@@ -95,6 +95,14 @@ struct mraygb_context
     // table (resident) and the 1D table it is built from
     DeviceBuffer error_bounds, errors, unc_table, unc_tf1d;
     bool has_unc_table = false;
+    // the single-scattering transmittance cache as a float grid behind a point-sampled texture (as the volume), the
+    // per-voxel keys of its build and its linear copy
+    cudaArray_t ss_array = nullptr;
+    cudaTextureObject_t ss_tex = 0;
+    int ss_size[3] = {0, 0, 0};
+    float ss_dmin[3] = {0, 0, 0}, ss_dmax[3] = {0, 0, 0};
+    bool has_ss_cache = false;
+    DeviceBuffer ss_keys, ss_linear;
 };
 
 namespace
@@ -189,6 +197,34 @@ void release_grid(mraygb_context *ctx)
     ctx->grid_tex = 0;
     ctx->grid_array = nullptr;
     ctx->nx = ctx->ny = ctx->nz = 0;
+}
+
+void release_ss_cache(mraygb_context *ctx)
+{
+    if (ctx->ss_tex)
+        cudaDestroyTextureObject(ctx->ss_tex);
+    if (ctx->ss_array)
+        cudaFreeArray(ctx->ss_array);
+    ctx->ss_tex = 0;
+    ctx->ss_array = nullptr;
+    ctx->ss_size[0] = ctx->ss_size[1] = ctx->ss_size[2] = 0;
+    ctx->has_ss_cache = false;
+}
+
+GridView ss_cache_view(const mraygb_context *ctx)
+{
+    GridView g;
+    g.tex = ctx->ss_tex;
+    g.nx = ctx->ss_size[0];
+    g.ny = ctx->ss_size[1];
+    g.nz = ctx->ss_size[2];
+    for (int i = 0; i < 3; ++i)
+    {
+        g.dmin[i] = ctx->ss_dmin[i];
+        g.dmax[i] = ctx->ss_dmax[i];
+        g.ext[i] = ctx->ss_dmax[i] - ctx->ss_dmin[i];
+    }
+    return g;
 }
 
 int check_device_error_flag(mraygb_context *ctx)
@@ -310,6 +346,14 @@ int run_reconstruct(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_
     a.ert = rp->early_ray_termination;
     a.rgba = d_rgba;
     a.rgba8 = d_rgba8;
+    GridView cache;
+    if (!diff_form && rp->ss.enable && rp->medium_scattering > 0.0f && ctx->has_ss_cache)
+    {
+        cache = ss_cache_view(ctx);
+        a.ss_cache = &cache;
+        a.ss = &rp->ss;
+        a.scattering = rp->medium_scattering;
+    }
     CK(launch_reconstruct(a, ctx->error_flag.as<int>(), ctx->stream), "reconstruct kernel launch");
     ctx->launches += 1;
     return MRAYGB_OK;
@@ -522,8 +566,10 @@ int validate_uncertainty(mraygb_context *ctx, const mraygb_uncertainty_params *u
         return fail(ctx, MRAYGB_INVALID_ARGUMENT, "step_size must be > 0 (got %g)", (double)rp->step_size);
     if (rp->use_truncated_fourier)
         return fail(ctx, MRAYGB_NOT_SUPPORTED, "truncated Fourier reconstruction is not part of this path");
-    if (rp->ss_enable)
-        return fail(ctx, MRAYGB_NOT_SUPPORTED, "single scattering is not part of this path");
+    if (rp->ss.enable && rp->medium_scattering > 0.0f)
+        return fail(ctx, MRAYGB_NOT_SUPPORTED,
+                    "uncertainty rendering with single scattering (the reference marches the light's moment image, "
+                    "not the cache) is not supported");
     if (mode != 0 && mode != 1)
         return fail(ctx, MRAYGB_INVALID_ARGUMENT, "mode %d: 0 = interpolation, 1 = convolution", mode);
     if (mode == 0 && !ctx->has_tf)
@@ -585,7 +631,7 @@ int validate_reference(mraygb_context *ctx, const mraygb_camera *cam, const mray
 }
 
 int run_reference(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_reference_params *rp, int width,
-                  int height, float *d_rgba, uint8_t *d_rgba8)
+                  int height, float *d_rgba, uint8_t *d_rgba8, bool use_cache = false)
 {
     const DeviceCamera dc = to_device_camera(*cam);
     ReferenceArgs a;
@@ -596,12 +642,31 @@ int run_reference(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_re
     a.tf = ctx->tf.as<float4>();
     a.rgba = d_rgba;
     a.rgba8 = d_rgba8;
+    const GridView cache = ss_cache_view(ctx);
+    if (use_cache)
+        a.ss_cache = &cache;
     if (ctx->volume == mraygb_context::PARTICLES)
         CK(launch_reference_particles(particle_view(ctx), a, ctx->error_flag.as<int>(), ctx->stream),
            "reference launch");
     else
         CK(launch_reference_grid(grid_view(ctx), a, ctx->error_flag.as<int>(), ctx->stream), "reference launch");
     ctx->launches += 1;
+    return MRAYGB_OK;
+}
+
+// the single-scattering block of a reconstruction: only the cached form, and only with a cache built or uploaded
+int validate_rec_ss(mraygb_context *ctx, const mraygb_reconstruction_params *rp)
+{
+    if (!rp->ss.enable || !(rp->medium_scattering > 0.0f))
+        return MRAYGB_OK;
+    if (!rp->ss.use_cache)
+        return fail(ctx, MRAYGB_NOT_SUPPORTED,
+                    "single scattering marched through the light's moment image (ss.use_cache = 0) is not supported; "
+                    "use the transmittance cache");
+    if (!ctx->has_ss_cache)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT,
+                    "single scattering needs a transmittance cache (mraygb_reconstruct_single_scattering_cache or "
+                    "mraygb_upload_single_scattering_cache)");
     return MRAYGB_OK;
 }
 
@@ -613,11 +678,9 @@ int validate_rec(mraygb_context *ctx, const mraygb_reconstruction_params *rp)
         return fail(ctx, MRAYGB_INVALID_ARGUMENT, "step_size must be > 0 (got %g)", (double)rp->step_size);
     if (rp->use_truncated_fourier)
         return fail(ctx, MRAYGB_NOT_SUPPORTED, "truncated Fourier reconstruction is not part of this path");
-    if (rp->ss_enable)
-        return fail(ctx, MRAYGB_NOT_SUPPORTED, "single scattering is not part of this path");
     if (!ctx->has_tf)
         return fail(ctx, MRAYGB_INVALID_ARGUMENT, "no transfer function uploaded");
-    return MRAYGB_OK;
+    return validate_rec_ss(ctx, rp);
 }
 
 } // namespace
@@ -662,6 +725,7 @@ void mraygb_destroy(mraygb_context *ctx)
     if (ctx->stream)
         cudaStreamSynchronize(ctx->stream);
     release_grid(ctx);
+    release_ss_cache(ctx);
     DeviceBuffer *bufs[] = {&ctx->particle_pts, &ctx->particle_cells,
                             &ctx->tf,       &ctx->moments,       &ctx->counts,
                             &ctx->index,   &ctx->compact,  &ctx->bounds,        &ctx->coding_params,
@@ -670,7 +734,7 @@ void mraygb_destroy(mraygb_context *ctx)
                             &ctx->bits,    &ctx->bit_offset, &ctx->scan_scratch64, &ctx->packed,
                             &ctx->adj_lambda, &ctx->adj_bounds, &ctx->qc_scratch, &ctx->qc_means,
                             &ctx->qc_index, &ctx->qc_data, &ctx->error_bounds, &ctx->errors, &ctx->unc_table,
-                            &ctx->unc_tf1d};
+                            &ctx->unc_tf1d, &ctx->ss_keys, &ctx->ss_linear};
     for (DeviceBuffer *b : bufs)
         b->release();
     if (ctx->own_stream)
@@ -1499,6 +1563,275 @@ int mraygb_generate_reference(mraygb_context *ctx, const mraygb_camera *cam, con
     return check_device_error_flag(ctx);
 }
 
+// ---- single scattering: the transmittance cache ---------------------------------------------------------------
+
+namespace
+{
+
+int check_texture3d(mraygb_context *ctx, int nx, int ny, int nz, const char *what)
+{
+    if (nx <= 0 || ny <= 0 || nz <= 0)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "%s of %d x %d x %d voxels", what, nx, ny, nz);
+    int max3d[3] = {0, 0, 0};
+    cudaDeviceGetAttribute(&max3d[0], cudaDevAttrMaxTexture3DWidth, ctx->device);
+    cudaDeviceGetAttribute(&max3d[1], cudaDevAttrMaxTexture3DHeight, ctx->device);
+    cudaDeviceGetAttribute(&max3d[2], cudaDevAttrMaxTexture3DDepth, ctx->device);
+    if (nx > max3d[0] || ny > max3d[1] || nz > max3d[2])
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "%s %d x %d x %d exceeds the 3D texture limits %d x %d x %d", what, nx,
+                    ny, nz, max3d[0], max3d[1], max3d[2]);
+    return MRAYGB_OK;
+}
+
+// the cache's array and texture for nx x ny x nz voxels (kept while the size stays), filled from `src`
+int store_ss_cache(mraygb_context *ctx, const float *src, int nx, int ny, int nz, const float dmin[3],
+                   const float dmax[3], cudaMemcpyKind kind)
+{
+    if (!(ctx->ss_array && ctx->ss_size[0] == nx && ctx->ss_size[1] == ny && ctx->ss_size[2] == nz))
+    {
+        release_ss_cache(ctx);
+        const cudaChannelFormatDesc desc = cudaCreateChannelDesc<float>();
+        CK(cudaMalloc3DArray(&ctx->ss_array, &desc, make_cudaExtent(nx, ny, nz)), "cache allocation");
+        cudaResourceDesc res;
+        std::memset(&res, 0, sizeof(res));
+        res.resType = cudaResourceTypeArray;
+        res.res.array.array = ctx->ss_array;
+        cudaTextureDesc td;
+        std::memset(&td, 0, sizeof(td));
+        td.addressMode[0] = td.addressMode[1] = td.addressMode[2] = cudaAddressModeClamp;
+        td.filterMode = cudaFilterModePoint;
+        td.readMode = cudaReadModeElementType;
+        td.normalizedCoords = 0;
+        CK(cudaCreateTextureObject(&ctx->ss_tex, &res, &td, nullptr), "cache texture");
+        ctx->ss_size[0] = nx;
+        ctx->ss_size[1] = ny;
+        ctx->ss_size[2] = nz;
+    }
+    ctx->has_ss_cache = false;
+    cudaMemcpy3DParms cp;
+    std::memset(&cp, 0, sizeof(cp));
+    cp.srcPtr = make_cudaPitchedPtr(const_cast<float *>(src), (size_t)nx * sizeof(float), nx, ny);
+    cp.dstArray = ctx->ss_array;
+    cp.extent = make_cudaExtent(nx, ny, nz);
+    cp.kind = kind;
+    CK(cudaMemcpy3DAsync(&cp, ctx->stream), "cache copy");
+    for (int i = 0; i < 3; ++i)
+    {
+        ctx->ss_dmin[i] = dmin[i];
+        ctx->ss_dmax[i] = dmax[i];
+    }
+    ctx->has_ss_cache = true;
+    return MRAYGB_OK;
+}
+
+int validate_ss_cache(mraygb_context *ctx, const mraygb_camera *light_cam, const mraygb_reconstruction_params *rp,
+                      const float dmin[3], const float dmax[3])
+{
+    if (!light_cam || !rp || !dmin || !dmax)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "NULL argument");
+    if (!(rp->step_size > 0.f))
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "step_size must be > 0 (got %g)", (double)rp->step_size);
+    if (rp->use_truncated_fourier)
+        return fail(ctx, MRAYGB_NOT_SUPPORTED, "truncated Fourier reconstruction is not part of this path");
+    for (int i = 0; i < 3; ++i)
+        if (!(dmax[i] > dmin[i]))
+            return fail(ctx, MRAYGB_INVALID_ARGUMENT, "empty domain along axis %d", i);
+    if (!ctx->has_tf)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "no transfer function uploaded");
+    return check_texture3d(ctx, rp->ss.cache_size_x, rp->ss.cache_size_y, rp->ss.cache_size_z,
+                           "single-scattering cache");
+}
+
+int run_ss_cache(mraygb_context *ctx, const mraygb_camera *light_cam, const mraygb_reconstruction_params *rp,
+                 int width, int height, int m, const float dmin[3], const float dmax[3], const uint32_t *d_index,
+                 const float *d_pm, const uint16_t *d_bounds, float *d_cache)
+{
+    const int cx = rp->ss.cache_size_x, cy = rp->ss.cache_size_y, cz = rp->ss.cache_size_z;
+    const size_t nvox = (size_t)cx * (size_t)cy * (size_t)cz;
+    CK(ctx->ss_keys.reserve(nvox * sizeof(unsigned long long)), "cache key allocation");
+    if (!d_cache)
+    {
+        CK(ctx->ss_linear.reserve(nvox * sizeof(float)), "cache allocation");
+        d_cache = ctx->ss_linear.as<float>();
+    }
+    const DeviceCamera dc = to_device_camera(*light_cam);
+    SsCacheArgs a;
+    a.cam = &dc;
+    a.width = width;
+    a.height = height;
+    a.m = m;
+    for (int i = 0; i < 3; ++i)
+    {
+        a.dmin[i] = dmin[i];
+        a.dmax[i] = dmax[i];
+    }
+    a.index = d_index;
+    a.pmoments = d_pm;
+    a.bounds = d_bounds;
+    a.tf = ctx->tf.as<float4>();
+    a.step = rp->step_size;
+    a.cx = cx;
+    a.cy = cy;
+    a.cz = cz;
+    a.keys = ctx->ss_keys.as<unsigned long long>();
+    a.cache = d_cache;
+    CK(launch_ss_cache(a, ctx->error_flag.as<int>(), ctx->stream), "single-scattering cache launch");
+    ctx->launches += 2;
+    return store_ss_cache(ctx, d_cache, cx, cy, cz, dmin, dmax, cudaMemcpyDeviceToDevice);
+}
+
+} // namespace
+
+int mraygb_upload_single_scattering_cache(mraygb_context *ctx, const float *data, int nx, int ny, int nz,
+                                          const float dmin[3], const float dmax[3], int data_on_device)
+{
+    CHECK_CTX();
+    if (!data || !dmin || !dmax)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "NULL argument");
+    int rc = check_texture3d(ctx, nx, ny, nz, "single-scattering cache");
+    if (rc)
+        return rc;
+    for (int i = 0; i < 3; ++i)
+        if (!(dmax[i] > dmin[i]))
+            return fail(ctx, MRAYGB_INVALID_ARGUMENT, "empty domain along axis %d", i);
+    if ((rc = store_ss_cache(ctx, data, nx, ny, nz, dmin, dmax,
+                             data_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice)))
+        return rc;
+    if (!data_on_device)
+        CK(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+    return MRAYGB_OK;
+}
+
+int mraygb_stage_reconstruct_single_scattering_cache(mraygb_context *ctx, const mraygb_camera *light_cam,
+                                                     const mraygb_reconstruction_params *rp, int width, int height,
+                                                     int m, const float domain_min[3], const float domain_max[3],
+                                                     const uint32_t *d_index, const float *d_pmoments,
+                                                     const uint16_t *d_bounds, float *d_cache)
+{
+    CHECK_CTX();
+    int rc = check_image(ctx, width, height, m);
+    if (rc)
+        return rc;
+    if ((rc = validate_ss_cache(ctx, light_cam, rp, domain_min, domain_max)))
+        return rc;
+    if (!d_pmoments)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "NULL multipliers");
+    return run_ss_cache(ctx, light_cam, rp, width, height, m, domain_min, domain_max, d_index, d_pmoments, d_bounds,
+                        d_cache);
+}
+
+int mraygb_reconstruct_single_scattering_cache(mraygb_context *ctx, const mraygb_camera *light_cam,
+                                               const mraygb_reconstruction_params *rp, int width, int height, int m,
+                                               const float domain_min[3], const float domain_max[3],
+                                               const uint32_t *h_index, const float *h_data, uint64_t data_size,
+                                               const uint16_t *h_bounds, int prediction_code, int coding_warp,
+                                               const uint16_t *h_coding_params, float *h_cache)
+{
+    CHECK_CTX();
+    int rc = check_image(ctx, width, height, m);
+    if (rc)
+        return rc;
+    if ((rc = validate_ss_cache(ctx, light_cam, rp, domain_min, domain_max)))
+        return rc;
+    const uint32_t *d_index;
+    const uint16_t *d_bounds, *d_cp;
+    if ((rc = upload_moment_image(ctx, width, height, m, h_index, h_data, data_size, h_bounds, prediction_code,
+                                  coding_warp, h_coding_params, &d_index, &d_bounds, &d_cp)))
+        return rc;
+    if ((rc = run_prepare(ctx, width, height, m, d_index, ctx->compact.as<float>(), prediction_code, coding_warp,
+                          d_cp, rp->bias, ctx->pmoments.as<float>())))
+        return rc;
+    if ((rc = run_ss_cache(ctx, light_cam, rp, width, height, m, domain_min, domain_max, d_index,
+                           ctx->pmoments.as<float>(), d_bounds, nullptr)))
+        return rc;
+    if (h_cache)
+    {
+        const size_t nvox = (size_t)rp->ss.cache_size_x * rp->ss.cache_size_y * rp->ss.cache_size_z;
+        CK(cudaMemcpyAsync(h_cache, ctx->ss_linear.ptr, nvox * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream),
+           "cache download");
+    }
+    CK(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+    return check_device_error_flag(ctx);
+}
+
+namespace
+{
+
+// ref_from_rec_params (src/parameters.h:379-390)
+mraygb_reference_params ref_from_rec(const mraygb_reconstruction_params &r)
+{
+    mraygb_reference_params o{};
+    o.step_size = r.step_size;
+    o.medium_emission = r.medium_emission;
+    o.medium_scattering = r.medium_scattering;
+    o.early_ray_termination = r.early_ray_termination;
+    o.data_min = r.data_min;
+    o.data_max = r.data_max;
+    o.ss = r.ss;
+    return o;
+}
+
+int validate_reference_cached(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_reconstruction_params *rp)
+{
+    if (!rp)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "reconstruction parameters are NULL");
+    const mraygb_reference_params ref = ref_from_rec(*rp);
+    int rc = validate_reference(ctx, cam, &ref);
+    if (rc)
+        return rc;
+    if (rp->ss.enable && rp->medium_scattering > 0.0f && !ctx->has_ss_cache)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT,
+                    "single scattering needs a transmittance cache (mraygb_reconstruct_single_scattering_cache or "
+                    "mraygb_upload_single_scattering_cache)");
+    return MRAYGB_OK;
+}
+
+} // namespace
+
+int mraygb_stage_generate_reference_reconstructed_ss(mraygb_context *ctx, const mraygb_camera *cam,
+                                                     const mraygb_reconstruction_params *rp, int width, int height,
+                                                     float *d_rgba)
+{
+    CHECK_CTX();
+    int rc = check_image(ctx, width, height, 1);
+    if (rc)
+        return rc;
+    if ((rc = validate_reference_cached(ctx, cam, rp)))
+        return rc;
+    if (!d_rgba)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "NULL colour buffer");
+    const mraygb_reference_params ref = ref_from_rec(*rp);
+    return run_reference(ctx, cam, &ref, width, height, d_rgba, nullptr, true);
+}
+
+int mraygb_generate_reference_reconstructed_ss(mraygb_context *ctx, const mraygb_camera *cam,
+                                               const mraygb_reconstruction_params *rp, int width, int height,
+                                               float *h_rgba, uint8_t *h_rgba8)
+{
+    CHECK_CTX();
+    int rc = check_image(ctx, width, height, 1);
+    if (rc)
+        return rc;
+    if ((rc = validate_reference_cached(ctx, cam, rp)))
+        return rc;
+    if (!h_rgba && !h_rgba8)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "no output");
+    const mraygb_reference_params ref = ref_from_rec(*rp);
+    const size_t P = (size_t)width * (size_t)height;
+    CK(ctx->rgba.reserve(P * 4 * sizeof(float)), "colour buffer allocation");
+    if (h_rgba8)
+        CK(ctx->rgba8.reserve(P * 4), "u8 colour buffer allocation");
+    if ((rc = run_reference(ctx, cam, &ref, width, height, ctx->rgba.as<float>(),
+                            h_rgba8 ? ctx->rgba8.as<uint8_t>() : nullptr, true)))
+        return rc;
+    if (h_rgba)
+        CK(cudaMemcpyAsync(h_rgba, ctx->rgba.ptr, P * 4 * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream),
+           "colour download");
+    if (h_rgba8)
+        CK(cudaMemcpyAsync(h_rgba8, ctx->rgba8.ptr, P * 4, cudaMemcpyDeviceToHost, ctx->stream), "u8 colour download");
+    CK(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+    return check_device_error_flag(ctx);
+}
+
 int mraygb_upload_uncertainty_table(mraygb_context *ctx, const float *table_rgba256x256)
 {
     CHECK_CTX();
@@ -1601,6 +1934,8 @@ int validate_diff(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_ge
         return fail(ctx, MRAYGB_INVALID_ARGUMENT, "the differentiation form supports up to 64 moments (got %d)", m);
     if (!(rp->step_size > 0.f))
         return fail(ctx, MRAYGB_INVALID_ARGUMENT, "reconstruction step_size must be > 0");
+    if (rp->ss.enable && rp->medium_scattering > 0.0f)
+        return fail(ctx, MRAYGB_NOT_SUPPORTED, "the differentiation form has no single scattering");
     if (ctx->volume == mraygb_context::NONE)
         return fail(ctx, MRAYGB_NO_VOLUME, "no volume uploaded");
     return MRAYGB_OK;

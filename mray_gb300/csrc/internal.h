@@ -114,6 +114,8 @@ struct ReferenceArgs
     const float4 *tf; // preintegrated row
     float *rgba;      // W*H float4 or null
     uint8_t *rgba8;   // W*H uchar4 or null
+    // single scattering from the transmittance cache instead of the brute-force march (null: brute force)
+    const GridView *ss_cache = nullptr;
 };
 cudaError_t launch_reference_grid(const GridView &grid, const ReferenceArgs &a, int *error_flag, cudaStream_t stream);
 cudaError_t launch_reference_particles(const ParticleView &parts, const ReferenceArgs &a, int *error_flag,
@@ -170,8 +172,30 @@ struct ReconArgs
     const float4 *bounds4 = nullptr;
     // the differentiation form's density and transfer function (exact atan, cubic B-spline row)
     int diff_form = 0;
+    // single scattering from the transmittance cache (null: none): in-scattered light of intensity ss->intensity
+    // and phase function ss->henyey_greenstein_g, weighted by the medium's scattering coefficient
+    const GridView *ss_cache = nullptr;
+    const mraygb_single_scattering_params *ss = nullptr;
+    float scattering = 0.f;
 };
 cudaError_t launch_reconstruct(const ReconArgs &a, int *error_flag, cudaStream_t stream);
+
+// scattering.cu: the single-scattering transmittance cache of a light moment image (prepared moments)
+struct SsCacheArgs
+{
+    const DeviceCamera *cam; // the light's camera
+    int width, height, m;
+    float dmin[3], dmax[3]; // the image's domain, also the cache's
+    const uint32_t *index;
+    const float *pmoments;
+    const uint16_t *bounds;
+    const float4 *tf;
+    float step;
+    int cx, cy, cz;
+    unsigned long long *keys; // cx*cy*cz scratch
+    float *cache;             // cx*cy*cz floats, x fastest
+};
+cudaError_t launch_ss_cache(const SsCacheArgs &a, int *error_flag, cudaStream_t stream);
 
 // adjoint.cu: the differentiation form's adjoints (non-compact images, float bounds, linear transfer function)
 struct ReconAdjArgs

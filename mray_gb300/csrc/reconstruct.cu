@@ -1,5 +1,5 @@
-// Bounded-MESE re-march: one thread per pixel (reconstruct_ray with MESEReconstruction and no single
-// scattering, src/raymarch_reconstruct.h:127-200 and src/reconstruction_techniques.h:72-96; driven per pixel
+// Bounded-MESE re-march: one thread per pixel (reconstruct_ray with MESEReconstruction, without single
+// scattering or with the transmittance cache, src/raymarch_reconstruct.h:127-200 and src/reconstruction_techniques.h:72-96; driven per pixel
 // as reconstruct_host / reconstruct_moments_kernel, src/moment_raymarcher.cpp:283-327, .cu:339-384).
 //
 // Per sample the density is rho(p) = lo + (hi - lo) (fast_atan(S(p)) / pi + 1/2) with the Lagrange series
@@ -39,10 +39,16 @@ struct ReconDev
     uint8_t *rgba8;
     const float4 *bounds4;
     int *error_flag;
+    // single scattering: the transmittance cache, the light direction, intensity, phase asymmetry and the medium's
+    // scattering coefficient
+    GridView cache;
+    float light[3], intensity[3], hg_g, scattering;
 };
 
 // DIFF: the differentiation form (float bounds read by the caller's choice, exact atan, B-spline transfer function)
-template <int MAXM, bool DIFF>
+// SS: in-scattered light from the transmittance cache (inscattering with SingleScatteringCache,
+// src/raymarch_reconstruct.h:36-46 and 112-125)
+template <int MAXM, bool DIFF, bool SS>
 __global__ void __launch_bounds__(128) reconstruct_kernel(const ReconDev a)
 {
     __shared__ float4 s_tf[256];
@@ -116,6 +122,7 @@ __global__ void __launch_bounds__(128) reconstruct_kernel(const ReconDev a)
             const float est = range / a.step;
             const int cap = (est < 1.6e9f ? (int)(1.25f * est) : 2000000000) + 64;
             float L0 = 0.f, L1 = 0.f, L2 = 0.f, alpha = 0.f, T = 1.f, tau = 0.f;
+            const float pf = SS ? henyey_greenstein_ray(d, a.light, a.hg_g) : 0.f;
             float fs = DIFF ? mese_density_exact<MAXM>(lam2, lam0, p, lo, span)
                             : mese_density<MAXM>(lam2, lam0, p, lo, span);
             int it = 0;
@@ -131,9 +138,29 @@ __global__ void __launch_bounds__(128) reconstruct_kernel(const ReconDev a)
                 const float bs = DIFF ? mese_density_exact<MAXM>(lam2, lam0, p, lo, span)
                                       : mese_density<MAXM>(lam2, lam0, p, lo, span);
                 const float4 s = DIFF ? tf_sample_bspline(s_tf, bspline_tap(fs)) : tf_sample(s_tf, fs, bs);
-                L0 += (a.emission * s.x) * T;
-                L1 += (a.emission * s.y) * T;
-                L2 += (a.emission * s.z) * T;
+                if (SS)
+                {
+                    // L += (Le + Ls sigma_s) T with Ls = T_ss pf intensity, T_ss the cache at ray.origin + t ray.dir
+                    const float T_ss = grid_sample(a.cache, __fadd_rn(o[0], __fmul_rn(t, d[0])),
+                                                   __fadd_rn(o[1], __fmul_rn(t, d[1])),
+                                                   __fadd_rn(o[2], __fmul_rn(t, d[2])));
+                    const float tp = __fmul_rn(T_ss, pf);
+                    L0 = __fadd_rn(L0, __fmul_rn(__fadd_rn(__fmul_rn(a.emission, s.x),
+                                                           __fmul_rn(__fmul_rn(tp, a.intensity[0]), a.scattering)),
+                                                 T));
+                    L1 = __fadd_rn(L1, __fmul_rn(__fadd_rn(__fmul_rn(a.emission, s.y),
+                                                           __fmul_rn(__fmul_rn(tp, a.intensity[1]), a.scattering)),
+                                                 T));
+                    L2 = __fadd_rn(L2, __fmul_rn(__fadd_rn(__fmul_rn(a.emission, s.z),
+                                                           __fmul_rn(__fmul_rn(tp, a.intensity[2]), a.scattering)),
+                                                 T));
+                }
+                else
+                {
+                    L0 += (a.emission * s.x) * T;
+                    L1 += (a.emission * s.y) * T;
+                    L2 += (a.emission * s.z) * T;
+                }
                 tau += s.w;
                 T = expf(-tau);
                 alpha = 1.f - T;
@@ -161,14 +188,16 @@ __global__ void __launch_bounds__(128) reconstruct_kernel(const ReconDev a)
     }
 }
 
-template <int MAXM> void launch_m(const ReconDev &a, bool diff, cudaStream_t stream)
+template <int MAXM> void launch_m(const ReconDev &a, bool diff, bool ss, cudaStream_t stream)
 {
     dim3 block(16, 8);
     dim3 grid((a.width + 15) / 16, (a.height + 7) / 8);
     if (diff)
-        reconstruct_kernel<MAXM, true><<<grid, block, 0, stream>>>(a);
+        reconstruct_kernel<MAXM, true, false><<<grid, block, 0, stream>>>(a);
+    else if (ss)
+        reconstruct_kernel<MAXM, false, true><<<grid, block, 0, stream>>>(a);
     else
-        reconstruct_kernel<MAXM, false><<<grid, block, 0, stream>>>(a);
+        reconstruct_kernel<MAXM, false, false><<<grid, block, 0, stream>>>(a);
 }
 
 } // namespace
@@ -196,19 +225,30 @@ cudaError_t launch_reconstruct(const ReconArgs &r, int *error_flag, cudaStream_t
     a.rgba8 = r.rgba8;
     a.bounds4 = r.bounds4;
     a.error_flag = error_flag;
+    // inscattering only where the medium scatters (raymarch_reconstruct.h:176-179)
+    const bool ss = r.ss_cache && r.ss && r.scattering > 0.0f && r.diff_form == 0;
+    a.cache = ss ? *r.ss_cache : GridView{};
+    a.scattering = r.scattering;
+    a.light[0] = ss ? r.ss->direction_x : 0.f;
+    a.light[1] = ss ? r.ss->direction_y : 0.f;
+    a.light[2] = ss ? r.ss->direction_z : 0.f;
+    a.intensity[0] = ss ? r.ss->intensity_r : 0.f;
+    a.intensity[1] = ss ? r.ss->intensity_g : 0.f;
+    a.intensity[2] = ss ? r.ss->intensity_b : 0.f;
+    a.hg_g = ss ? r.ss->henyey_greenstein_g : 0.f;
     const bool lin = r.diff_form != 0;
     if (r.m <= 8)
-        launch_m<8>(a, lin, stream);
+        launch_m<8>(a, lin, ss, stream);
     else if (r.m <= 16)
-        launch_m<16>(a, lin, stream);
+        launch_m<16>(a, lin, ss, stream);
     else if (r.m <= 32)
-        launch_m<32>(a, lin, stream);
+        launch_m<32>(a, lin, ss, stream);
     else if (r.m <= 64)
-        launch_m<64>(a, lin, stream);
+        launch_m<64>(a, lin, ss, stream);
     else if (r.m <= 128)
-        launch_m<128>(a, lin, stream);
+        launch_m<128>(a, lin, ss, stream);
     else
-        launch_m<256>(a, lin, stream);
+        launch_m<256>(a, lin, ss, stream);
     return cudaGetLastError();
 }
 

@@ -177,6 +177,17 @@ __device__ __forceinline__ float mese_density_exact(const float (&lam2)[MAXM], f
     return (atanf(s) * 0.318309886f + 0.5f) * span + lo;
 }
 
+// henyey_greenstein (src/cut/phase_functions.h:33-36) at cos_theta = dot(-ray.dir, light_dir); the reference's CPU
+// build divides by pow of the float arguments promoted to double, so the division is in double
+__device__ __forceinline__ float henyey_greenstein_ray(const float d[3], const float light[3], float g)
+{
+    const float cos_theta =
+        __fadd_rn(__fadd_rn(__fmul_rn(-d[0], light[0]), __fmul_rn(-d[1], light[1])), __fmul_rn(-d[2], light[2]));
+    const float num = __fmul_rn(__fsub_rn(1.f, __fmul_rn(g, g)), 0.07957747154594766788f);
+    const float base = __fsub_rn(__fadd_rn(1.f, __fmul_rn(g, g)), __fmul_rn(__fmul_rn(2.f, g), cos_theta));
+    return (float)((double)num / pow((double)base, 1.5));
+}
+
 // d fast_atan / dt: fast_atan is t P(t^2) for |t| <= 1 and pi/2 - P(1/t^2) / |t| (odd) beyond, with P the
 // polynomial above; the derivative is Q(y) = P(y) + 2 y P'(y) at y = t^2, or Q(1/t^2) / t^2.
 __device__ __forceinline__ float fast_atan_derivative(float t)

@@ -2,8 +2,9 @@
 // src/moment_raymarcher.cu:65-114) with reference_ray (src/raymarch_reference.h:93-160): the ground-truth image the
 // moment path approximates, marched through the volume itself with the preintegrated transfer function.  With
 // single scattering enabled every sample marches a secondary ray towards the light (the brute-force transmittance
-// of raymarch_reference.h:40-75); the Henyey-Greenstein phase function depends on the eye ray only and is
-// evaluated once per ray.
+// of raymarch_reference.h:40-75), or samples the transmittance cache of a light moment image
+// (generate_reference_reconstructed_ss, src/moment_raymarcher.cpp:259-281); the Henyey-Greenstein phase function
+// depends on the eye ray only and is evaluated once per ray.
 //
 // One thread per pixel in 16 x 8 tiles over the resident volume (grid texture or SPH particles); the transfer
 // function row in shared memory, sampled as TransferFunction::sample does (src/transfer_function.h:44-59).  Sample
@@ -28,6 +29,8 @@ struct ReferenceDev
     float *rgba;
     uint8_t *rgba8;
     int *error_flag;
+    bool has_cache;
+    GridView cache;
 };
 
 __device__ __forceinline__ int march_cap(float range, float step)
@@ -72,7 +75,8 @@ __device__ float transmittance(const V &vol, const float o[3], const float d[3],
     return expf(-__fmul_rn(tau, rp.ss.step_size_factor));
 }
 
-template <class V, bool SS> __global__ void __launch_bounds__(128) reference_kernel(const ReferenceDev a, const V vol)
+// SS: 0 no single scattering, 1 brute-force transmittance, 2 the transmittance cache
+template <class V, int SS> __global__ void __launch_bounds__(128) reference_kernel(const ReferenceDev a, const V vol)
 {
     __shared__ float4 s_tf[256];
     for (int i = threadIdx.x + threadIdx.y * blockDim.x; i < 256; i += blockDim.x * blockDim.y)
@@ -94,18 +98,7 @@ template <class V, bool SS> __global__ void __launch_bounds__(128) reference_ker
     {
         const float light[3] = {rp.ss.direction_x, rp.ss.direction_y, rp.ss.direction_z};
         const float to_light[3] = {-light[0], -light[1], -light[2]};
-        float pf = 0.f;
-        if (SS)
-        {
-            // henyey_greenstein (src/cut/phase_functions.h:33-36) at dot(-ray.dir, light_dir); the reference's CPU
-            // build divides by the double pow
-            const float g = rp.ss.henyey_greenstein_g;
-            const float cos_theta =
-                __fadd_rn(__fadd_rn(__fmul_rn(-d[0], light[0]), __fmul_rn(-d[1], light[1])), __fmul_rn(-d[2], light[2]));
-            const float num = __fmul_rn(__fsub_rn(1.f, __fmul_rn(g, g)), 0.07957747154594766788f);
-            const float base = __fsub_rn(__fadd_rn(1.f, __fmul_rn(g, g)), __fmul_rn(__fmul_rn(2.f, g), cos_theta));
-            pf = (float)((double)num / pow((double)base, 1.5));
-        }
+        const float pf = SS != 0 ? henyey_greenstein_ray(d, light, rp.ss.henyey_greenstein_g) : 0.f;
         const float step = rp.step_size;
         const int cap = march_cap(__fsub_rn(t_far, t_near), step);
         float L0 = 0.f, L1 = 0.f, L2 = 0.f, alpha = 0.f, T = 1.f, tau = 0.f;
@@ -133,9 +126,12 @@ template <class V, bool SS> __global__ void __launch_bounds__(128) reference_ker
                 s = make_float4(0.f, 1.f, 0.f, 0.05f);
             float ls0 = 0.f, ls1 = 0.f, ls2 = 0.f;
             const float sigma_s = rp.medium_scattering;
-            if (SS)
+            if (SS != 0)
             {
-                const float T_ss = transmittance(vol, p, to_light, s_tf, rp, a.error_flag);
+                // compute_transmittance: the brute-force march, or the cache sampled at the sample position
+                // (raymarch_reference.h:77-86)
+                const float T_ss = SS == 1 ? transmittance(vol, p, to_light, s_tf, rp, a.error_flag)
+                                           : grid_sample(a.cache, p[0], p[1], p[2]);
                 const float tp = __fmul_rn(T_ss, pf);
                 ls0 = __fmul_rn(tp, rp.ss.intensity_r);
                 ls1 = __fmul_rn(tp, rp.ss.intensity_g);
@@ -174,10 +170,12 @@ template <class V> cudaError_t launch_reference_v(const ReferenceDev &a, const V
 {
     const dim3 block(16, 8), grid((a.width + 15) / 16, (a.height + 7) / 8);
     const bool ss = a.rp.ss.enable && a.rp.medium_scattering > 0.0f;
-    if (ss)
-        reference_kernel<V, true><<<grid, block, 0, stream>>>(a, vol);
+    if (ss && a.has_cache)
+        reference_kernel<V, 2><<<grid, block, 0, stream>>>(a, vol);
+    else if (ss)
+        reference_kernel<V, 1><<<grid, block, 0, stream>>>(a, vol);
     else
-        reference_kernel<V, false><<<grid, block, 0, stream>>>(a, vol);
+        reference_kernel<V, 0><<<grid, block, 0, stream>>>(a, vol);
     return cudaGetLastError();
 }
 
@@ -192,6 +190,8 @@ ReferenceDev reference_args(const ReferenceArgs &r, int *error_flag)
     a.rgba = r.rgba;
     a.rgba8 = r.rgba8;
     a.error_flag = error_flag;
+    a.has_cache = r.ss_cache != nullptr;
+    a.cache = r.ss_cache ? *r.ss_cache : GridView{};
     return a;
 }
 

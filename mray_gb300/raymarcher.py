@@ -177,6 +177,23 @@ class MomentImageHost:
         return (np.float32(b[0]) / np.float32(65535.0), np.float32(b[1]) / np.float32(65535.0))
 
 
+class SingleScatteringImageHost:
+    """SingleScatteringImageHost (single_scattering_image.h:50-106): the light's camera and the moment image
+    rendered from it (generate with that camera)."""
+
+    def __init__(self, cam: Camera, img: "MomentImageHost"):
+        self.cam = cam
+        self.img = img
+
+
+class SingleScatteringCacheHost:
+    """SingleScatteringCacheHost (single_scattering_cache.h:33-59): the transmittance towards the light as a
+    RegularGrid (float32 [z, y, x] over the light image's domain)."""
+
+    def __init__(self, cache: RegularGrid):
+        self.cache = cache
+
+
 class ColorImageHost:
     """ColorImageHost: u8 RGBA as the reference stores it, plus ``rgba_float`` (the colour before the store)."""
 
@@ -392,6 +409,54 @@ class Context:
         self._check(self._L.mraygb_stage_generate_reference(self._h, C.byref(cam), C.byref(rp), width, height,
                                                             _dptr(rgba)))
 
+    # ---- single scattering: the transmittance cache ----
+    def reconstruct_single_scattering_cache(self, light_cam: Camera, rp: ReconstructionParameters,
+                                            mi: MomentImageHost, return_cache: bool = True):
+        """reconstruct_single_scattering_cache(ss, tf, params) (moment_raymarcher.cpp:217-258) of the light's
+        moment image with the transfer function uploaded last.  The cache stays in the context for
+        reconstruct / generate_reference_reconstructed_ss; returns it as float32 [z, y, x] (or None)."""
+        data, index, bounds, cp = self._image_arrays(mi)
+        ss = rp.ss
+        cache = np.zeros((ss.cache_size_z, ss.cache_size_y, ss.cache_size_x), dtype=np.float32) \
+            if return_cache else None
+        self._check(self._L.mraygb_reconstruct_single_scattering_cache(
+            self._h, C.byref(light_cam), C.byref(rp), mi.width, mi.height, mi.num_moments, _f3(mi.domain_min),
+            _f3(mi.domain_max), _hptr(index), _hptr(data), data.size, _hptr(bounds), int(mi.prediction_code),
+            int(mi.coding_warp), _hptr(cp), _hptr(cache)))
+        return cache
+
+    def stage_reconstruct_single_scattering_cache(self, light_cam, rp, width, height, num_moments, domain_min,
+                                                  domain_max, index, pmoments, bounds, cache=None):
+        self._check(self._L.mraygb_stage_reconstruct_single_scattering_cache(
+            self._h, C.byref(light_cam), C.byref(rp), width, height, num_moments, _f3(domain_min), _f3(domain_max),
+            _dptr(index), _dptr(pmoments), _dptr(bounds), _dptr(cache)))
+
+    def upload_single_scattering_cache(self, cache, domain_min, domain_max) -> None:
+        """A transmittance cache made elsewhere: float32 [z, y, x] (numpy array or CUDA tensor) on the box."""
+        if hasattr(cache, "data_ptr"):
+            nz, ny, nx = cache.shape
+            self._check(self._L.mraygb_upload_single_scattering_cache(self._h, _dptr(cache), nx, ny, nz,
+                                                                      _f3(domain_min), _f3(domain_max), 1))
+        else:
+            c = np.ascontiguousarray(cache, dtype=np.float32)
+            nz, ny, nx = c.shape
+            self._check(self._L.mraygb_upload_single_scattering_cache(self._h, _hptr(c), nx, ny, nz,
+                                                                      _f3(domain_min), _f3(domain_max), 0))
+
+    def generate_reference_reconstructed_ss(self, cam: Camera, rp: ReconstructionParameters, width: int,
+                                            height: int, img: Optional[ColorImageHost] = None) -> ColorImageHost:
+        """generate_reference_reconstructed_ss (moment_raymarcher.cpp:259-281) over the volume, transfer function
+        and transmittance cache of the context."""
+        img = img or ColorImageHost(width, height)
+        self._check(self._L.mraygb_generate_reference_reconstructed_ss(self._h, C.byref(cam), C.byref(rp), width,
+                                                                       height, _hptr(img.rgba_float),
+                                                                       _hptr(img.rgba)))
+        return img
+
+    def stage_generate_reference_reconstructed_ss(self, cam, rp, width, height, rgba):
+        self._check(self._L.mraygb_stage_generate_reference_reconstructed_ss(self._h, C.byref(cam), C.byref(rp),
+                                                                             width, height, _dptr(rgba)))
+
     def quantize_prediction_coding(self, mi: MomentImageHost, table) -> np.ndarray:
         """quantize_prediction_coding(mi, table) (moment_quantization.cpp:239-276): the packed code bytes."""
         if not mi.is_compact:
@@ -568,11 +633,38 @@ def default_quantization_table(num_moments: int, num_bits: int) -> np.ndarray:
 
 
 def reconstruct(cam: Camera, mi: MomentImageHost, tf: TransferFunction, img: ColorImageHost,
-                params: ReconstructionParameters, context: Optional[Context] = None) -> None:
-    """reconstruct(cam, mi, tf, img, params) (moment_raymarcher.h:61-64): fills ``img`` in place."""
+                params: ReconstructionParameters, context: Optional[Context] = None,
+                ss: Optional[SingleScatteringImageHost] = None) -> None:
+    """reconstruct(cam, mi, tf, img, params) and, with ``ss``, reconstruct(cam, mi, tf, img, ss, params)
+    (moment_raymarcher.h:61-64, moment_raymarcher.cpp:329-351): fills ``img`` in place.  With ``ss`` the
+    transmittance cache of the light's image is built first and sampled for the in-scattered light."""
     ctx = context or default_context()
     ctx.upload_tf(tf.table)
+    if ss is not None:
+        ctx.reconstruct_single_scattering_cache(ss.cam, params, ss.img, return_cache=False)
     ctx.reconstruct(cam, params, mi, img)
+
+
+def reconstruct_single_scattering_cache(ss: SingleScatteringImageHost, tf: TransferFunction,
+                                        params: ReconstructionParameters,
+                                        context: Optional[Context] = None) -> SingleScatteringCacheHost:
+    """reconstruct_single_scattering_cache(ss, tf, params) (moment_raymarcher.cpp:217-258)."""
+    ctx = context or default_context()
+    ctx.upload_tf(tf.table)
+    cache = ctx.reconstruct_single_scattering_cache(ss.cam, params, ss.img)
+    return SingleScatteringCacheHost(RegularGrid(cache, ss.img.domain_min, ss.img.domain_max))
+
+
+def generate_reference_reconstructed_ss(cam: Camera, tf: TransferFunction, volume, img: ColorImageHost,
+                                        ss: SingleScatteringImageHost, params: ReconstructionParameters,
+                                        context: Optional[Context] = None) -> None:
+    """generate_reference_reconstructed_ss(cam, tf, volume, img, ss, params) (moment_raymarcher.cpp:259-281): the
+    reference renderer with the single-scattering transmittance of the light image's cache."""
+    ctx = context or default_context()
+    ctx.upload_tf(tf.table)
+    ctx.reconstruct_single_scattering_cache(ss.cam, params, ss.img, return_cache=False)
+    _upload_volume(ctx, volume)
+    ctx.generate_reference_reconstructed_ss(cam, params, img.width, img.height, img)
 
 
 def _upload_volume(ctx: Context, volume) -> None:

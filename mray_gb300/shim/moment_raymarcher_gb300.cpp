@@ -83,6 +83,25 @@ mraygb_generation_params to_c(const GenerationParameters &p)
     return o;
 }
 
+mraygb_single_scattering_params to_c(const SingleScatteringParameters &p)
+{
+    mraygb_single_scattering_params o{};
+    o.enable = p.enable;
+    o.use_cache = p.use_cache;
+    o.cache_size_x = p.cache_size_x;
+    o.cache_size_y = p.cache_size_y;
+    o.cache_size_z = p.cache_size_z;
+    o.step_size_factor = p.step_size_factor;
+    o.henyey_greenstein_g = p.henyey_greenstein_g;
+    o.direction_x = p.direction_x;
+    o.direction_y = p.direction_y;
+    o.direction_z = p.direction_z;
+    o.intensity_r = p.intensity_r;
+    o.intensity_g = p.intensity_g;
+    o.intensity_b = p.intensity_b;
+    return o;
+}
+
 mraygb_reconstruction_params to_c(const ReconstructionParameters &p)
 {
     mraygb_reconstruction_params o{};
@@ -95,7 +114,7 @@ mraygb_reconstruction_params to_c(const ReconstructionParameters &p)
     o.step_size = p.step_size;
     o.step_size_write_samples = p.step_size_write_samples;
     o.use_truncated_fourier = p.use_truncated_fourier;
-    o.ss_enable = p.ss.enable;
+    o.ss = to_c(p.ss);
     return o;
 }
 
@@ -281,19 +300,7 @@ mraygb_reference_params to_c(const ReferenceParameters &p)
     o.early_ray_termination = p.early_ray_termination;
     o.data_min = p.data_min;
     o.data_max = p.data_max;
-    o.ss.enable = p.ss.enable;
-    o.ss.use_cache = p.ss.use_cache;
-    o.ss.cache_size_x = p.ss.cache_size_x;
-    o.ss.cache_size_y = p.ss.cache_size_y;
-    o.ss.cache_size_z = p.ss.cache_size_z;
-    o.ss.step_size_factor = p.ss.step_size_factor;
-    o.ss.henyey_greenstein_g = p.ss.henyey_greenstein_g;
-    o.ss.direction_x = p.ss.direction_x;
-    o.ss.direction_y = p.ss.direction_y;
-    o.ss.direction_z = p.ss.direction_z;
-    o.ss.intensity_r = p.ss.intensity_r;
-    o.ss.intensity_g = p.ss.intensity_g;
-    o.ss.intensity_b = p.ss.intensity_b;
+    o.ss = to_c(p.ss);
     return o;
 }
 
@@ -361,8 +368,87 @@ void reconstruct_error_device(cut::Camera cam, const Particles &volume, MomentIm
     error_uploaded(cam, mi, params);
 }
 
+namespace
+{
+
+// The transmittance cache of the light's image (reconstruct_single_scattering_cache_device in the reference's
+// launchers), kept in the context for the call that follows.
+void ss_cache_uploaded(const SingleScatteringImageHost &ss, const ReconstructionParameters &params)
+{
+    const auto lc = to_c(ss.cam);
+    const auto r = to_c(params);
+    const MomentImageHost &mi = ss.img;
+    const float dmin[3] = {mi.domain.min.x, mi.domain.min.y, mi.domain.min.z};
+    const float dmax[3] = {mi.domain.max.x, mi.domain.max.y, mi.domain.max.z};
+    ImageArrays arr(mi);
+    check(mraygb_reconstruct_single_scattering_cache(
+        context(), &lc, &r, mi.width, mi.height, mi.num_moments, dmin, dmax, mi.is_compact ? mi.index.data() : nullptr,
+        mi.data.data(), mi.data.size(), arr.bounds.empty() ? nullptr : arr.bounds.data(), mi.prediction_code,
+        mi.coding_warp, arr.cp.empty() ? nullptr : arr.cp.data(), nullptr));
+}
+
+void reference_cached_uploaded(const cut::Camera &cam, const TransferFunction &tf, ColorImageHost &img,
+                               const SingleScatteringImageHost &ss, const ReconstructionParameters &params)
+{
+    check(mraygb_upload_tf(context(), reinterpret_cast<const float *>(tf.data.data())));
+    ss_cache_uploaded(ss, params);
+    const auto c = to_c(cam);
+    const auto r = to_c(params);
+    check(mraygb_generate_reference_reconstructed_ss(context(), &c, &r, img.width, img.height, nullptr,
+                                                     reinterpret_cast<uint8_t *>(img.rgba.data())));
+}
+
+} // namespace
+
+// reconstruct_device with a SingleScatteringImageHost (src/moment_raymarcher.cuh:56-57): the cache of the light's
+// image, then the re-march sampling it (params.ss.use_cache; the marched form returns MRAYGB_NOT_SUPPORTED)
+void reconstruct_device(cut::Camera cam, const MomentImageHost &mi, const TransferFunction &tf, ColorImageHost &cimg,
+                        const SingleScatteringImageHost &ss, const ReconstructionParameters &params)
+{
+    check(mraygb_upload_tf(context(), reinterpret_cast<const float *>(tf.data.data())));
+    ss_cache_uploaded(ss, params);
+    const auto c = to_c(cam);
+    const auto r = to_c(params);
+    const float dmin[3] = {mi.domain.min.x, mi.domain.min.y, mi.domain.min.z};
+    const float dmax[3] = {mi.domain.max.x, mi.domain.max.y, mi.domain.max.z};
+    ImageArrays arr(mi);
+    check(mraygb_reconstruct(context(), &c, &r, mi.width, mi.height, mi.num_moments, dmin, dmax,
+                             mi.is_compact ? mi.index.data() : nullptr, mi.data.data(), mi.data.size(),
+                             arr.bounds.empty() ? nullptr : arr.bounds.data(), mi.prediction_code, mi.coding_warp,
+                             arr.cp.empty() ? nullptr : arr.cp.data(), nullptr,
+                             reinterpret_cast<uint8_t *>(cimg.rgba.data())));
+}
+
+// generate_reference_reconstructed_ss_device (src/moment_raymarcher.cuh:59-64) for both volume types
+void generate_reference_reconstructed_ss_device(cut::Camera cam, const TransferFunction &tf, const RegularGrid &volume,
+                                                ColorImageHost &img, const SingleScatteringImageHost &ss,
+                                                const ReconstructionParameters &params)
+{
+    if (volume.type != RegularGrid::DataType::F32)
+    {
+        std::fprintf(stderr, "mraygb: only float grids are supported\n");
+        std::terminate();
+    }
+    const float dmin[3] = {volume.domain.min.x, volume.domain.min.y, volume.domain.min.z};
+    const float dmax[3] = {volume.domain.max.x, volume.domain.max.y, volume.domain.max.z};
+    check(mraygb_upload_grid(context(), volume.data.data(), volume.size.x, volume.size.y, volume.size.z, dmin, dmax,
+                             0));
+    reference_cached_uploaded(cam, tf, img, ss, params);
+}
+
+void generate_reference_reconstructed_ss_device(cut::Camera cam, const TransferFunction &tf, const Particles &volume,
+                                                ColorImageHost &img, const SingleScatteringImageHost &ss,
+                                                const ReconstructionParameters &params)
+{
+    const float dmin[3] = {volume.domain.min.x, volume.domain.min.y, volume.domain.min.z};
+    const float dmax[3] = {volume.domain.max.x, volume.domain.max.y, volume.domain.max.z};
+    check(mraygb_upload_particles(context(), volume.x.data(), volume.y.data(), volume.z.data(),
+                                  volume.values.data(), volume.size(), volume.smoothing_length, dmin, dmax, 0));
+    reference_cached_uploaded(cam, tf, img, ss, params);
+}
+
 // reconstruct_uncertainty_interpolation_device / _convolution_device (src/moment_raymarcher.cuh:78-86); the
-// single-scattering overload stays with the reference's launcher (single scattering is not on this path)
+// single-scattering overload stays with the reference's launcher (it marches the light's image, not the cache)
 void reconstruct_uncertainty_interpolation_device(cut::Camera cam, const MomentImageHost &mi,
                                                   const TransferFunction &tf, ColorImageHost &cimg,
                                                   const UncertaintyReconstructionParameters &params)

@@ -122,9 +122,45 @@ class GenerationParameters(C.Structure):
             setattr(self, k, v)
 
 
+class SingleScatteringParameters(C.Structure):
+    """``SingleScatteringParameters`` (parameters.h:173-193) with the reference's defaults."""
+
+    _fields_ = [
+        ("enable", C.c_uint8),
+        ("use_cache", C.c_uint8),
+        ("pad0", C.c_uint8 * 2),
+        ("cache_size_x", C.c_int32),
+        ("cache_size_y", C.c_int32),
+        ("cache_size_z", C.c_int32),
+        ("step_size_factor", C.c_float),
+        ("henyey_greenstein_g", C.c_float),
+        ("direction_x", C.c_float),
+        ("direction_y", C.c_float),
+        ("direction_z", C.c_float),
+        ("intensity_r", C.c_float),
+        ("intensity_g", C.c_float),
+        ("intensity_b", C.c_float),
+    ]
+
+    def __init__(self, **kw):
+        super().__init__()
+        self.enable = 0
+        self.use_cache = 1
+        self.cache_size_x = self.cache_size_y = self.cache_size_z = 128
+        self.step_size_factor = 1.0
+        self.henyey_greenstein_g = 0.0
+        self.direction_x, self.direction_y, self.direction_z = 0.0, -1.0, 0.1
+        self.intensity_r = self.intensity_g = self.intensity_b = 1.0
+        for k, v in kw.items():
+            if not hasattr(self, k):
+                raise AttributeError(k)
+            setattr(self, k, v)
+
+
 class ReconstructionParameters(C.Structure):
-    """``ReconstructionParameters`` (parameters.h:231-247) with the reference's defaults; single scattering
-    and the truncated-Fourier variant are not part of this path and must stay 0."""
+    """``ReconstructionParameters`` (parameters.h:231-247) with the reference's defaults and layout; the
+    truncated-Fourier variant is not part of this path and must stay 0.  Single scattering (``ss.enable``) samples
+    the transmittance cache of the context (``reconstruct_single_scattering_cache``)."""
 
     _fields_ = [
         ("bias", C.c_float),
@@ -136,8 +172,8 @@ class ReconstructionParameters(C.Structure):
         ("step_size", C.c_float),
         ("step_size_write_samples", C.c_float),
         ("use_truncated_fourier", C.c_uint8),
-        ("ss_enable", C.c_uint8),
-        ("pad0", C.c_uint8 * 2),
+        ("pad0", C.c_uint8 * 3),
+        ("ss", SingleScatteringParameters),
     ]
 
     def __init__(self, **kw):
@@ -151,7 +187,7 @@ class ReconstructionParameters(C.Structure):
         self.step_size = 0.01
         self.step_size_write_samples = 1.5
         self.use_truncated_fourier = 0
-        self.ss_enable = 0
+        self.ss = SingleScatteringParameters()
         for k, v in kw.items():
             if not hasattr(self, k):
                 raise AttributeError(k)
@@ -206,41 +242,6 @@ class UncertaintyReconstructionParameters(C.Structure):
         self.rec = ReconstructionParameters()
         self.bound_interpolation = 0.5
         self.error_type = RMSE
-        for k, v in kw.items():
-            if not hasattr(self, k):
-                raise AttributeError(k)
-            setattr(self, k, v)
-
-
-class SingleScatteringParameters(C.Structure):
-    """``SingleScatteringParameters`` (parameters.h:173-193) with the reference's defaults."""
-
-    _fields_ = [
-        ("enable", C.c_uint8),
-        ("use_cache", C.c_uint8),
-        ("pad0", C.c_uint8 * 2),
-        ("cache_size_x", C.c_int32),
-        ("cache_size_y", C.c_int32),
-        ("cache_size_z", C.c_int32),
-        ("step_size_factor", C.c_float),
-        ("henyey_greenstein_g", C.c_float),
-        ("direction_x", C.c_float),
-        ("direction_y", C.c_float),
-        ("direction_z", C.c_float),
-        ("intensity_r", C.c_float),
-        ("intensity_g", C.c_float),
-        ("intensity_b", C.c_float),
-    ]
-
-    def __init__(self, **kw):
-        super().__init__()
-        self.enable = 0
-        self.use_cache = 1
-        self.cache_size_x = self.cache_size_y = self.cache_size_z = 128
-        self.step_size_factor = 1.0
-        self.henyey_greenstein_g = 0.0
-        self.direction_x, self.direction_y, self.direction_z = 0.0, -1.0, 0.1
-        self.intensity_r = self.intensity_g = self.intensity_b = 1.0
         for k, v in kw.items():
             if not hasattr(self, k):
                 raise AttributeError(k)

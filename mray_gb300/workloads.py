@@ -103,6 +103,19 @@ def ortho_camera(seed: int, center=(0.0, 0.0, 0.0), half_extent: float = math.sq
     return Camera.orthographic_camera(pos, right * half_extent, up * half_extent, d)
 
 
+def light_camera(direction, center=(0.0, 0.0, 0.0), half_extent: float = math.sqrt(3.0),
+                 distance: float = 3.0) -> Camera:
+    """An orthographic camera looking along ``direction``: the light of single scattering, whose image is the
+    SingleScatteringImage and whose direction is SingleScatteringParameters' light direction
+    (parse_ss_params, src/parameters.h:219-226)."""
+    d = _unit(direction)
+    helper = np.array([0.0, 0.0, 1.0]) if abs(d[2]) < 0.9 else np.array([1.0, 0.0, 0.0])
+    right = _unit(np.cross(d, helper))
+    up = _unit(np.cross(right, d))
+    pos = np.asarray(center, dtype=np.float64) - distance * d
+    return Camera.orthographic_camera(pos, right * half_extent, up * half_extent, d)
+
+
 def look_at_transform(eye, target, up=(0.0, 0.0, 1.0)) -> np.ndarray:
     """Camera->world matrix (row-major) for a camera at ``eye`` looking at ``target``; the camera looks
     along -z in camera space (src/cut/raytracing.h:39-49)."""

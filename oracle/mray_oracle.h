@@ -79,6 +79,9 @@ typedef struct oracle_options
     const void *bounds_in;
     /* generate only: columns col_begin, col_begin + col_step, ... below col_end (col_end <= 0: the width) */
     int col_begin, col_end, col_step;
+    /* reconstruct and generate_reference: the single-scattering transmittance cache (NULL: none; generate_reference
+     * then marches the transmittance when rp->ss.enable) */
+    const oracle_grid *ss_cache;
 } oracle_options;
 
 #define ORACLE_DECL(R, SFX)                                                                                         \
@@ -102,6 +105,11 @@ typedef struct oracle_options
                                   const float domain_max[3], const uint32_t *index, const R *pmoments,               \
                                   const uint16_t *bounds, const R *tf_table, R *rgba,                                 \
                                   const oracle_options *opt);                                                        \
+    /* the single-scattering transmittance cache of a light image, sequential (moment_raymarcher.cpp:217-258) */   \
+    void oracle_ss_cache_##SFX(const mraygb_camera *light_cam, const mraygb_reconstruction_params *rp, int width,    \
+                               int height, int num_moments, const float domain_min[3], const float domain_max[3],    \
+                               const uint32_t *index, const R *pmoments, const uint16_t *bounds,                     \
+                               const R *tf_table, float *cache);                                                     \
     /* MESE primitives (mese/MESE_dynamic.h)                                                                  */    \
     void oracle_trig_to_exp_##SFX(int n, const R *trig, R *exp_out /* 2n */);                                     \
     void oracle_exp_to_trig_##SFX(int n, const R *exp_in /* 2n */, R *trig_out /* 2n */);                         \

@@ -28,7 +28,8 @@ fp = np.ctypeslib.ndpointer
 class Options(C.Structure):
     _fields_ = [("exact_atan", C.c_int), ("nthreads", C.c_int), ("row_begin", C.c_int), ("row_end", C.c_int),
                 ("row_step", C.c_int), ("tf_bspline", C.c_int), ("bounds_out", C.c_void_p),
-                ("bounds_in", C.c_void_p), ("col_begin", C.c_int), ("col_end", C.c_int), ("col_step", C.c_int)]
+                ("bounds_in", C.c_void_p), ("col_begin", C.c_int), ("col_end", C.c_int), ("col_step", C.c_int),
+                ("ss_cache", C.c_void_p)]
 
 
 class Grid(C.Structure):
@@ -159,6 +160,9 @@ def _declare(L):
             C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float * 3, C.c_float * 3, C.c_void_p,
             C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     for sfx in ("f32", "f64"):
+        getattr(L, f"oracle_ss_cache_{sfx}").argtypes = [
+            P(Camera), P(ReconstructionParameters), C.c_int, C.c_int, C.c_int, C.c_float * 3, C.c_float * 3,
+            C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         getattr(L, f"oracle_generate_reference_{sfx}").argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                                                    C.c_int, C.c_int, C.c_void_p, C.c_void_p,
                                                                    C.c_void_p]
@@ -393,11 +397,37 @@ def prepare_moments(width, height, m, index, data, prediction_code=False, coding
     return out[:d.size]
 
 
+def ss_cache(light_cam, rp, width, height, m, dmin, dmax, index, pmoments, bounds, tf_table, precision="f32"):
+    """reconstruct_single_scattering_cache, run sequentially: the transmittance cache of a light image's
+    multipliers, float32[cache_size_z, cache_size_y, cache_size_x] over [dmin, dmax]."""
+    L = lib()
+    dt = _dt(precision)
+    pm = np.ascontiguousarray(pmoments, dtype=dt)
+    idx = None if index is None else np.ascontiguousarray(index, dtype=np.uint32)
+    b = None if bounds is None else np.ascontiguousarray(bounds, dtype=np.uint16)
+    t = np.ascontiguousarray(tf_table, dtype=dt)
+    out = np.zeros((rp.ss.cache_size_z, rp.ss.cache_size_y, rp.ss.cache_size_x), dtype=np.float32)
+    getattr(L, f"oracle_ss_cache_{precision}")(C.byref(light_cam), C.byref(rp), width, height, m,
+                                               (C.c_float * 3)(*dmin), (C.c_float * 3)(*dmax), _ptr(idx), _ptr(pm),
+                                               _ptr(b), _ptr(t), _ptr(out))
+    return out
+
+
+def _cache_option(o, cache):
+    """cache = (values[z, y, x], dmin, dmax) or None; returns what must stay alive while the call runs."""
+    if cache is None:
+        return None
+    g, keep = _grid(*cache)
+    o.ss_cache = C.addressof(g)
+    return g, keep
+
+
 def reconstruct(cam, rp, width, height, m, dmin, dmax, index, pmoments, bounds, tf_table, precision="f32",
-                nthreads=0, rows=None, exact_atan=False, tf_bspline=False, float_bounds=None):
+                nthreads=0, rows=None, exact_atan=False, tf_bspline=False, float_bounds=None, cache=None):
     """reconstruct_host with float RGBA: returns rgba[H,W,4].  tf_bspline / float_bounds select the
     differentiation form (transfer-function row as a cubic B-spline in the front density; unquantized
-    bounds[H,W,2])."""
+    bounds[H,W,2]).  cache = (values[z, y, x], dmin, dmax): single scattering from that transmittance cache when
+    rp.ss.enable."""
     L = lib()
     dt = _dt(precision)
     pm = np.ascontiguousarray(pmoments, dtype=dt)
@@ -409,9 +439,11 @@ def reconstruct(cam, rp, width, height, m, dmin, dmax, index, pmoments, bounds, 
     o.tf_bspline = int(tf_bspline)
     bf = None if float_bounds is None else np.ascontiguousarray(float_bounds, dtype=dt)
     o.bounds_in = None if bf is None else bf.ctypes.data
+    keep = _cache_option(o, cache)
     getattr(L, f"oracle_reconstruct_{precision}")(C.byref(cam), C.byref(rp), width, height, m,
                                                   (C.c_float * 3)(*dmin), (C.c_float * 3)(*dmax), _ptr(idx),
                                                   _ptr(pm), _ptr(b), _ptr(t), _ptr(out), C.byref(o))
+    del keep
     return out
 
 
@@ -472,20 +504,31 @@ def reconstruct_uncertainty(cam, up, mode, width, height, m, dmin, dmax, index, 
 
 
 def generate_reference(cam, rp, volume, dmin, dmax, width, height, tf_table, precision="f32", nthreads=0,
-                       rows=None, particles=None):
+                       rows=None, particles=None, cache=None):
     """reference_host: direct volume rendering of the volume (a grid, or ``particles`` when given) with the
-    preintegrated row; float RGBA[H,W,4]."""
+    preintegrated row; float RGBA[H,W,4].  cache = (values[z, y, x], dmin, dmax): the single-scattering
+    transmittance from that cache instead of the brute-force march (generate_reference_reconstructed_ss)."""
     L = lib()
     dt = _dt(precision)
     g, keep = (_grid(volume, dmin, dmax) if particles is None else (None, None))
     t = np.ascontiguousarray(tf_table, dtype=dt)
     out = np.zeros((height, width, 4), dtype=dt)
     o = options(nthreads, rows)
+    keep_cache = _cache_option(o, cache)
     getattr(L, f"oracle_generate_reference_{precision}")(
         C.byref(cam), C.byref(rp), C.byref(g) if g is not None else None,
         particles.handle if particles is not None else None, width, height, _ptr(t), _ptr(out), C.byref(o))
-    del keep
+    del keep, keep_cache
     return out
+
+
+def ref_from_rec(rp):
+    """ref_from_rec_params (parameters.h:379-390)."""
+    from mray_gb300.types import ReferenceParameters
+
+    return ReferenceParameters(step_size=rp.step_size, medium_emission=rp.medium_emission,
+                               medium_scattering=rp.medium_scattering, early_ray_termination=rp.early_ray_termination,
+                               data_min=rp.data_min, data_max=rp.data_max, ss=rp.ss)
 
 
 def preintegrate(tf1d, step_size):

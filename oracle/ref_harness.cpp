@@ -26,6 +26,10 @@
 #include "color_image.h"
 #include "volume.h"
 #include "cut/raytracing.h"
+#include "single_scattering_image.h"
+#include "single_scattering_cache.h"
+
+#include <omp.h>
 
 #include <cstring>
 
@@ -72,6 +76,8 @@ GenerationParameters to_gen(const mraygb_generation_params *g)
     return p;
 }
 
+SingleScatteringParameters to_ss(const mraygb_single_scattering_params &s);
+
 ReconstructionParameters to_rec(const mraygb_reconstruction_params *r)
 {
     ReconstructionParameters p;
@@ -84,6 +90,7 @@ ReconstructionParameters to_rec(const mraygb_reconstruction_params *r)
     p.step_size = r->step_size;
     p.step_size_write_samples = r->step_size_write_samples;
     p.use_truncated_fourier = r->use_truncated_fourier != 0;
+    p.ss = to_ss(r->ss);
     return p;
 }
 
@@ -118,6 +125,25 @@ MomentImageHost make_mi(int w, int h, int m, const uint32_t *index, const float 
     if (dmin)
         mi.domain = to_range(dmin, dmax);
     return mi;
+}
+
+SingleScatteringParameters to_ss(const mraygb_single_scattering_params &s)
+{
+    SingleScatteringParameters p;
+    p.enable = s.enable != 0;
+    p.use_cache = s.use_cache != 0;
+    p.cache_size_x = s.cache_size_x;
+    p.cache_size_y = s.cache_size_y;
+    p.cache_size_z = s.cache_size_z;
+    p.step_size_factor = s.step_size_factor;
+    p.henyey_greenstein_g = s.henyey_greenstein_g;
+    p.direction_x = s.direction_x;
+    p.direction_y = s.direction_y;
+    p.direction_z = s.direction_z;
+    p.intensity_r = s.intensity_r;
+    p.intensity_g = s.intensity_g;
+    p.intensity_b = s.intensity_b;
+    return p;
 }
 
 ReferenceParameters to_ref(const mraygb_reference_params *r)
@@ -572,6 +598,133 @@ int ref_generate_reference_float(const mraygb_camera *c, const mraygb_reference_
             Vec2f ndc(x / static_cast<float>(w) * 2.f - 1.f, y / static_cast<float>(h) * 2.f - 1.f);
             Vec4f color = reference_ray(grid, cut::get_eye_ray(cam, ndc), cam.znear, tf, SingleScatteringBruteForce{},
                                         params);
+            float *o = out + 4 * (size_t(y) * w + x);
+            o[0] = color.x;
+            o[1] = color.y;
+            o[2] = color.z;
+            o[3] = color.w;
+        }
+    return 0;
+}
+
+/* ---- single scattering from the transmittance cache ---- */
+
+// defined in moment_raymarcher.cpp:217-258 without a header declaration
+extern "C++" SingleScatteringCacheHost reconstruct_single_scattering_cache(const SingleScatteringImageHost &ss,
+                                                                           const TransferFunction &tf,
+                                                                           const ReconstructionParameters &params);
+
+/* reconstruct_single_scattering_cache (moment_raymarcher.cpp:217-258) on one OpenMP thread, so that its racing
+ * writes come in the loop's order; out: cache_size_z*y*x floats. */
+int ref_ss_cache(const mraygb_camera *light, const mraygb_reconstruction_params *r, int w, int h, int m,
+                 const uint32_t *index, const float *data, uint64_t data_size, const uint16_t *bounds,
+                 int prediction_code, int coding_warp, const uint16_t *coding_params, const float *dmin,
+                 const float *dmax, const float *tf_row, float *out)
+{
+    auto mi = make_mi(w, h, m, index, data, data_size, bounds, prediction_code, coding_warp, coding_params, dmin,
+                      dmax);
+    SingleScatteringImageHost ss(to_camera(light), mi);
+    auto tf = make_tf(tf_row);
+    const int threads = omp_get_max_threads();
+    omp_set_num_threads(1);
+    auto cache = reconstruct_single_scattering_cache(ss, tf, to_rec(r));
+    omp_set_num_threads(threads);
+    const Vec3i sz = cache.cache.size;
+    for (int z = 0; z < sz.z; ++z)
+        for (int y = 0; y < sz.y; ++y)
+            for (int x = 0; x < sz.x; ++x)
+                out[(size_t(z) * sz.y + y) * sz.x + x] = cache.cache.get(x, y, z);
+    return 0;
+}
+
+SingleScatteringCacheHost make_cache(const float *cache, int cx, int cy, int cz, const float *cmin, const float *cmax)
+{
+    return SingleScatteringCacheHost(RegularGrid(Vec3i(cx, cy, cz), to_range(cmin, cmax),
+                                                 std::vector<float>(cache, cache + size_t(cx) * cy * cz),
+                                                 RegularGrid::DataType::F32));
+}
+
+/* The per-pixel body of reconstruct_host with a SingleScatteringCacheHost (moment_raymarcher.cpp:283-327) keeping
+ * the float colour. */
+int ref_reconstruct_cached_float(const mraygb_camera *c, const mraygb_reconstruction_params *r, int w, int h, int m,
+                                 const uint32_t *index, const float *data, uint64_t data_size, const uint16_t *bounds,
+                                 int prediction_code, int coding_warp, const uint16_t *coding_params,
+                                 const float *dmin, const float *dmax, const float *tf_row, const float *cache, int cx,
+                                 int cy, int cz, const float *cmin, const float *cmax, float *out_rgba)
+{
+    auto mi = make_mi(w, h, m, index, data, data_size, bounds, prediction_code, coding_warp, coding_params, dmin,
+                      dmax);
+    auto tf = make_tf(tf_row);
+    auto cam = to_camera(c);
+    auto params = to_rec(r);
+    auto ss = make_cache(cache, cx, cy, cz, cmin, cmax);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int y = 0; y < h; ++y)
+        for (int x = 0; x < w; ++x)
+        {
+            Vec2f ndc(x / static_cast<float>(w) * 2.f - 1.f, y / static_cast<float>(h) * 2.f - 1.f);
+            Vec4f color;
+            if (mi.get_num_moments(x, y) == 0)
+                color = reconstruct_zero_ray(tf);
+            else
+            {
+                auto pm = mi.prepare_moments(x, y, params.bias);
+                MESEReconstructionDefault rec(pm.size(), pm.data(), mi.get_bounds(x, y));
+                color = reconstruct_ray(cut::get_eye_ray(cam, ndc), mi.domain, cam.znear, rec, tf, ss, params);
+            }
+            float *o = out_rgba + 4 * (size_t(y) * w + x);
+            o[0] = color.x;
+            o[1] = color.y;
+            o[2] = color.z;
+            o[3] = color.w;
+        }
+    return 0;
+}
+
+/* reconstruct(cam, mi, tf, img, ss, params) (moment_raymarcher.cpp:339-351) end to end, u8 RGBA, the cache built
+ * on one OpenMP thread. */
+int ref_reconstruct_ss_u8(const mraygb_camera *c, const mraygb_reconstruction_params *r, int w, int h, int m,
+                          const uint32_t *index, const float *data, uint64_t data_size, const uint16_t *bounds,
+                          int prediction_code, int coding_warp, const uint16_t *coding_params, const float *dmin,
+                          const float *dmax, const mraygb_camera *light, int lw, int lh, int lm,
+                          const uint32_t *lindex, const float *ldata, uint64_t ldata_size, const uint16_t *lbounds,
+                          int lprediction_code, int lcoding_warp, const uint16_t *lcoding_params, const float *tf_row,
+                          uint8_t *out_rgba8)
+{
+    auto mi = make_mi(w, h, m, index, data, data_size, bounds, prediction_code, coding_warp, coding_params, dmin,
+                      dmax);
+    auto lmi = make_mi(lw, lh, lm, lindex, ldata, ldata_size, lbounds, lprediction_code, lcoding_warp, lcoding_params,
+                       dmin, dmax);
+    SingleScatteringImageHost ss(to_camera(light), lmi);
+    auto tf = make_tf(tf_row);
+    ColorImageHost img(w, h);
+    const int threads = omp_get_max_threads();
+    omp_set_num_threads(1);
+    reconstruct(to_camera(c), mi, tf, img, ss, to_rec(r));
+    omp_set_num_threads(threads);
+    std::memcpy(out_rgba8, img.rgba.data(), 4 * size_t(w) * h);
+    return 0;
+}
+
+/* The per-pixel body of generate_reference_reconstructed_ss (moment_raymarcher.cpp:259-281: reference_host with
+ * the cache and ref_from_rec_params) keeping the float colour. */
+int ref_generate_reference_cached_float(const mraygb_camera *c, const mraygb_reconstruction_params *r,
+                                        const float *vol, int nx, int ny, int nz, const float *dmin, const float *dmax,
+                                        int w, int h, const float *tf_row, const float *cache, int cx, int cy, int cz,
+                                        const float *cmin, const float *cmax, float *out)
+{
+    RegularGrid grid(Vec3i(nx, ny, nz), to_range(dmin, dmax), std::vector<float>(vol, vol + size_t(nx) * ny * nz),
+                     RegularGrid::DataType::F32);
+    auto tf = make_tf(tf_row);
+    auto cam = to_camera(c);
+    auto params = ref_from_rec_params(to_rec(r));
+    auto ss = make_cache(cache, cx, cy, cz, cmin, cmax);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int y = 0; y < h; ++y)
+        for (int x = 0; x < w; ++x)
+        {
+            Vec2f ndc(x / static_cast<float>(w) * 2.f - 1.f, y / static_cast<float>(h) * 2.f - 1.f);
+            Vec4f color = reference_ray(grid, cut::get_eye_ray(cam, ndc), cam.znear, tf, ss, params);
             float *o = out + 4 * (size_t(y) * w + x);
             o[0] = color.x;
             o[1] = color.y;

@@ -70,6 +70,13 @@ def declare(ref):
     ref.ref_reconstruct_uncertainty_float.argtypes = [vp, vp, i, i, i, i, vp, vp, u64, vp, vp, i, i, vp, vp, vp, vp,
                                                       vp]
     ref.ref_generate_reference_float.argtypes = [vp, vp, vp, i, i, i, vp, vp, i, i, vp, vp]
+    ref.ref_ss_cache.argtypes = [vp, vp, i, i, i, vp, vp, u64, vp, i, i, vp, vp, vp, vp, vp]
+    ref.ref_reconstruct_cached_float.argtypes = [vp, vp, i, i, i, vp, vp, u64, vp, i, i, vp, vp, vp, vp, vp, i, i, i,
+                                                 vp, vp, vp]
+    ref.ref_reconstruct_ss_u8.argtypes = [vp, vp, i, i, i, vp, vp, u64, vp, i, i, vp, vp, vp, vp, i, i, i, vp, vp,
+                                          u64, vp, i, i, vp, vp, vp]
+    ref.ref_generate_reference_cached_float.argtypes = [vp, vp, vp, i, i, i, vp, vp, i, i, vp, vp, i, i, i, vp, vp,
+                                                        vp]
     ref.ref_sample_moment_image.restype = u64
     ref.ref_sample_moment_image.argtypes = [C.c_int, C.c_int, C.c_int, vp, vp, u64, C.c_int, vp, vp]
     ref.ref_coding_errors.restype = C.c_uint32
@@ -522,6 +529,69 @@ def reference_dvr(ref):
     return out
 
 
+def _ref_image(ref, cam, gen, vol, dmin, dmax, Wd, H, m):
+    """generate() through the reference: (index, data, bounds, coding params or None)."""
+    nz, ny, nx = vol.shape
+    data = np.zeros(Wd * H * m, np.float32)
+    index = np.zeros(Wd * H + 1, np.uint32)
+    bounds = np.zeros(2 * Wd * H, np.uint16)
+    cp = np.zeros(2 * m, np.uint16)
+    size = C.c_uint64()
+    flags = np.zeros(4, np.int32)
+    ref.ref_generate_grid(C.byref(cam), C.byref(gen), P(vol), nx, ny, nz, P(dmin), P(dmax), Wd, H, m, P(data),
+                          P(index), P(bounds), P(cp), C.byref(size), P(flags))
+    return index, data[:size.value].copy(), bounds, (cp[:2 * (m - 1)].copy() if gen.prediction_coding else None)
+
+
+def single_scattering(ref):
+    """Single scattering from the transmittance cache: the cache of a light image (reconstruct_single_scattering_
+    cache on one thread, so that its racing writes come in the loop's order), the re-march sampling it
+    (reconstruct_host with the cache, float and the whole reconstruct(..., ss, ...) as u8) and the reference
+    renderer sampling it (generate_reference_reconstructed_ss), all from the reference's own code."""
+    from mray_gb300.types import GenerationParameters, ReconstructionParameters, SingleScatteringParameters
+
+    out = {}
+    wl = W.ml_workload(n=64, width=48, height=40, num_moments=16, seed=11, name="golden_ml")
+    vol = np.ascontiguousarray(wl.volume)
+    nz, ny, nx = vol.shape
+    dmin, dmax = f32(*wl.domain_min), f32(*wl.domain_max)
+    row = np.zeros((256, 4), np.float32)
+    ref.ref_preintegrate(P(np.ascontiguousarray(wl.tf1d, np.float32)), C.c_float(wl.tf_step), P(row))
+    # the eye image (compact, bounds) and the light image (compact, bounds, prediction coded, threshold 0.01)
+    m = wl.num_moments
+    eye = _ref_image(ref, wl.camera, wl.gen, vol, dmin, dmax, wl.width, wl.height, m)
+    light = W.light_camera((0.3, -1.0, 0.2))
+    lw, lh = 40, 36
+    lgen = GenerationParameters(step_size=wl.gen.step_size, error_threshold=0.01, bias=wl.gen.bias, compact_image=1,
+                                prediction_coding=1, transform_to_bounds=1, transform_bound_eps=0.005)
+    lim = _ref_image(ref, light, lgen, vol, dmin, dmax, lw, lh, m)
+    ssp = SingleScatteringParameters(enable=1, use_cache=1, cache_size_x=24, cache_size_y=20, cache_size_z=16,
+                                     henyey_greenstein_g=0.3, direction_x=light.dir[0], direction_y=light.dir[1],
+                                     direction_z=light.dir[2], intensity_r=0.9, intensity_g=0.8, intensity_b=0.7)
+    rp = ReconstructionParameters(step_size=wl.rec.step_size, bias=wl.rec.bias, medium_emission=1.0,
+                                  medium_scattering=0.5, early_ray_termination=0.99, ss=ssp)
+    cs = (ssp.cache_size_z, ssp.cache_size_y, ssp.cache_size_x)
+    cache = np.zeros(cs, np.float32)
+    ref.ref_ss_cache(C.byref(light), C.byref(rp), lw, lh, m, P(lim[0]), P(lim[1]), lim[1].size, P(lim[2]), 1, 0,
+                     P(lim[3]), P(dmin), P(dmax), P(row), P(cache))
+    rgba = np.zeros((wl.height, wl.width, 4), np.float32)
+    ref.ref_reconstruct_cached_float(C.byref(wl.camera), C.byref(rp), wl.width, wl.height, m, P(eye[0]), P(eye[1]),
+                                     eye[1].size, P(eye[2]), 0, 0, None, P(dmin), P(dmax), P(row), P(cache),
+                                     ssp.cache_size_x, ssp.cache_size_y, ssp.cache_size_z, P(dmin), P(dmax), P(rgba))
+    u8 = np.zeros((wl.height, wl.width, 4), np.uint8)
+    ref.ref_reconstruct_ss_u8(C.byref(wl.camera), C.byref(rp), wl.width, wl.height, m, P(eye[0]), P(eye[1]),
+                              eye[1].size, P(eye[2]), 0, 0, None, P(dmin), P(dmax), C.byref(light), lw, lh, m,
+                              P(lim[0]), P(lim[1]), lim[1].size, P(lim[2]), 1, 0, P(lim[3]), P(row), P(u8))
+    refss = np.zeros((wl.height, wl.width, 4), np.float32)
+    ref.ref_generate_reference_cached_float(C.byref(wl.camera), C.byref(rp), P(vol), nx, ny, nz, P(dmin), P(dmax),
+                                            wl.width, wl.height, P(row), P(cache), ssp.cache_size_x, ssp.cache_size_y,
+                                            ssp.cache_size_z, P(dmin), P(dmax), P(refss))
+    out.update(eye_index=eye[0], eye_data=eye[1], eye_bounds=eye[2], light_index=lim[0], light_data=lim[1],
+               light_bounds=lim[2], light_coding_params=lim[3], light_shape=np.array([lw, lh, m], np.int32),
+               cache=cache, rgba=rgba, rgba8=u8, reference_rgba=refss)
+    return out
+
+
 def main():
     ref = O.ref_lib()
     if ref is None:
@@ -538,6 +608,7 @@ def main():
     np.savez_compressed(os.path.join(HERE, "quant_curve.npz"), **quant_curve(ref))
     np.savez_compressed(os.path.join(HERE, "uncertainty.npz"), **uncertainty(ref))
     np.savez_compressed(os.path.join(HERE, "reference_dvr.npz"), **reference_dvr(ref))
+    np.savez_compressed(os.path.join(HERE, "single_scattering.npz"), **single_scattering(ref))
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

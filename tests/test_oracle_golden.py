@@ -468,3 +468,69 @@ def test_reference_dvr_bit_exact():
         assert np.array_equal(rgba, g[f"{name}_rgba"]), name
     # in-scattered light brightens the image where the medium scatters
     assert g["ss_rgba"][..., :3].mean() > g["plain_rgba"][..., :3].mean()
+
+
+# ---- single scattering from the transmittance cache (moment_raymarcher.cpp:217-351) ---------------------------------
+
+def test_single_scattering_cache_bit_exact():
+    """The cache of the light image (the reference's loop on one thread: the last write to a voxel wins), the
+    re-march sampling it (float and the whole reconstruct(..., ss, ...) as u8) and the reference renderer sampling
+    it, against the reference's own code."""
+    from helpers import single_scattering_case
+
+    g = load("single_scattering.npz")
+    wl, light, rp = single_scattering_case()
+    lw, lh, m = (int(v) for v in g["light_shape"])
+    row = O.preintegrate(wl.tf1d, wl.tf_step)
+    dmin, dmax = wl.domain_min, wl.domain_max
+    lpm = O.prepare_moments(lw, lh, m, g["light_index"], g["light_data"], True, 0, g["light_coding_params"], rp.bias)
+    cache = O.ss_cache(light, rp, lw, lh, m, dmin, dmax, g["light_index"], lpm, g["light_bounds"], row)
+    assert np.array_equal(cache, g["cache"])
+    epm = O.prepare_moments(wl.width, wl.height, m, g["eye_index"], g["eye_data"], bias=rp.bias)
+    rgba = O.reconstruct(wl.camera, rp, wl.width, wl.height, m, dmin, dmax, g["eye_index"], epm, g["eye_bounds"], row,
+                         cache=(cache, dmin, dmax))
+    assert np.array_equal(rgba, g["rgba"])
+    assert np.array_equal(O.rgba_to_u8(rgba), g["rgba8"])
+    ref = O.generate_reference(wl.camera, O.ref_from_rec(rp), wl.volume, dmin, dmax, wl.width, wl.height, row,
+                               cache=(cache, dmin, dmax))
+    assert np.array_equal(ref, g["reference_rgba"])
+    # the in-scattered light is there: without single scattering the image is darker
+    rp.ss.enable = 0
+    plain = O.reconstruct(wl.camera, rp, wl.width, wl.height, m, dmin, dmax, g["eye_index"], epm, g["eye_bounds"],
+                          row)
+    assert g["rgba"][..., :3].mean() > plain[..., :3].mean()
+    # a transmittance in (0, 1] everywhere the light image reaches
+    assert 0.0 < cache.min() and cache.max() <= 1.0
+
+
+def test_single_scattering_cache_last_write_wins():
+    """Many light pixels per voxel (a 3 x 2 x 4 cache): the rows decide in order.  Where one row of the light image
+    writes, its values replace the earlier rows'; the other voxels keep the earlier rows' values."""
+    from helpers import single_scattering_case
+
+    g = load("single_scattering.npz")
+    wl, light, rp = single_scattering_case(cache_size=(3, 2, 4))
+    lw, lh, m = (int(v) for v in g["light_shape"])
+    row = O.preintegrate(wl.tf1d, wl.tf_step)
+    lpm = O.prepare_moments(lw, lh, m, g["light_index"], g["light_data"], True, 0, g["light_coding_params"], rp.bias)
+    full = O.ss_cache(light, rp, lw, lh, m, wl.domain_min, wl.domain_max, g["light_index"], lpm, g["light_bounds"],
+                      row)
+    idx = g["light_index"].astype(np.int64)
+
+    def rows(r0, r1):
+        """the light image with only rows r0 .. r1 - 1 kept (the other pixels empty)"""
+        keep = idx.copy()
+        keep[:r0 * lw + 1] = idx[r0 * lw]
+        keep[r1 * lw + 1:] = idx[r1 * lw]
+        return O.ss_cache(light, rp, lw, lh, m, wl.domain_min, wl.domain_max, keep.astype(np.uint32), lpm,
+                          g["light_bounds"], row)
+
+    r = lh // 2
+    upto, before, only = rows(0, r + 1), rows(0, r), rows(r, r + 1)
+    hit = only != 0
+    assert hit.any() and not hit.all()
+    # where row r writes, its values win over the earlier rows'; elsewhere the earlier rows' stay
+    assert np.array_equal(upto[hit], only[hit])
+    assert np.array_equal(upto[~hit], before[~hit])
+    assert not np.array_equal(before[hit], only[hit])
+    assert np.array_equal(rows(0, lh), full)
