@@ -55,7 +55,8 @@ def parse():
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the differentiation-form, SPH and FP64-error sections")
     ap.add_argument("--sph-particles", type=int, default=16_000_000)
-    ap.add_argument("--section", default="all", choices=["all", "diff", "sph", "large", "uncertainty"],
+    ap.add_argument("--section", default="all",
+                    choices=["all", "diff", "sph", "large", "uncertainty", "scattering"],
                     help="diff / sph: run only that section and print its JSON (for profiling)")
     return ap.parse_args()
 
@@ -394,6 +395,7 @@ def run_ours(args):
         extras["sph"] = run_sph(args, local)
         extras["large"] = run_large(args, local)
         extras["uncertainty"] = run_uncertainty(args, local)
+        extras["single_scattering"] = run_scattering(args, local)
         extras["errors_vs_fp64"] = precision_errors(args, local)
 
     if rank == 0:
@@ -854,6 +856,110 @@ def run_uncertainty(args, local):
     return out
 
 
+def run_scattering(args, local):
+    """Single scattering from the transmittance cache on the default workload (512^3 mixing layer, 1024^2 eye image,
+    m = 64), with the reference's single-scattering settings (eval/turbine/turbine_single_scattering.json): a 512^2
+    light image with 50 moments (compact, bounds, prediction coded, error threshold 0.01) along an oblique light, a
+    256 x 128 x 128 cache, emission 0.6, scattering 0.35, intensity 0.28.  Per launch: the cache build (its march
+    over the light image, the decode and the copy into the sampled array), the re-march with and without
+    in-scattering and the reference renderer sampling the cache.  The oracle's cache loop (one thread, as the
+    reference's result is defined) on every 32nd row of the light image beside them."""
+    import torch
+
+    import mray_gb300 as M
+    from mray_gb300 import workloads as W
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    wl = workload(args)
+    Wd, H, m = wl.width, wl.height, wl.num_moments
+    P = Wd * H
+    lw = lh = max(64, args.image // 2)
+    lm = min(50, m)
+    LP = lw * lh
+    light = W.light_camera((0.3, -1.0, 0.2), center=(0.5, 0.5, 0.5), half_extent=0.9, distance=2.0)
+    ssp = M.SingleScatteringParameters(enable=1, use_cache=1, cache_size_x=256, cache_size_y=128, cache_size_z=128,
+                                       step_size_factor=4.0, direction_x=light.dir[0], direction_y=light.dir[1],
+                                       direction_z=light.dir[2], intensity_r=0.28, intensity_g=0.28,
+                                       intensity_b=0.28)
+    rp = M.ReconstructionParameters(step_size=wl.rec.step_size, bias=wl.rec.bias, medium_emission=0.6,
+                                    medium_scattering=0.35, early_ray_termination=wl.rec.early_ray_termination,
+                                    ss=ssp)
+    lgen = M.GenerationParameters(step_size=wl.gen.step_size, error_threshold=0.01, bias=wl.gen.bias, compact_image=1,
+                                  prediction_coding=1, transform_to_bounds=1, transform_bound_eps=0.005)
+    ctx = M.Context(local)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    ctx.upload_grid(torch.from_numpy(wl.volume).cuda(), wl.domain_min, wl.domain_max)
+    ctx.upload_tf(M.preintegrate(wl.tf1d, wl.tf_step).table)
+    # the light image through the host API (generation, compaction, prediction coding), then prepared on the device
+    lmi = ctx.generate(light, lgen, lw, lh, lm)
+    l_idx = torch.from_numpy(lmi.index.view(np.int32)).cuda()
+    l_data = torch.from_numpy(lmi.data).cuda()
+    l_b = torch.from_numpy(lmi.bounds.reshape(-1).view(np.int16)).cuda()
+    l_cp = torch.from_numpy(lmi.coding_params.view(np.int16)).cuda()
+    l_pm = torch.empty_like(l_data)
+    ctx.stage_prepare_moments(lw, lh, lm, l_idx, l_data, l_pm, prediction_code=True, coding_warp=0, coding_params=l_cp,
+                              bias=rp.bias)
+    # the eye image
+    mo = torch.empty(P * m, device="cuda")
+    b = torch.empty(2 * P, dtype=torch.int16, device="cuda")
+    c = torch.empty(P, dtype=torch.int32, device="cuda")
+    idx = torch.empty(P + 1, dtype=torch.int32, device="cuda")
+    cm = torch.empty(P * m, device="cuda")
+    pm = torch.empty(P * m, device="cuda")
+    rgba = torch.empty(P * 4, device="cuda")
+    ctx.stage_generate_moments(wl.camera, wl.gen, Wd, H, m, mo, b, c)
+    ctx.stage_compact(Wd, H, m, c, mo, idx, cm)
+    ctx.stage_prepare_moments(Wd, H, m, idx, cm, pm, bias=wl.rec.bias)
+    steps = max(1, min(args.steps, 5))
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        ctx.synchronize()
+        ev = _events(steps)
+        for e in ev:
+            e[0].record(stream)
+            fn()
+            e[1].record(stream)
+        ctx.synchronize()
+        return statistics.mean(e[0].elapsed_time(e[1]) for e in ev)
+
+    out = {"workload": f"mixing_layer{args.size}^3_{Wd}x{H}_m{m}_persp; light {lw}x{lh} m{lm} ortho; cache 256x128x128",
+           "step": "the re-march step"}
+    d_cache = torch.empty(128 * 128 * 256, device="cuda")
+    ms = timed(lambda: ctx.stage_reconstruct_single_scattering_cache(light, rp, lw, lh, lm, wl.domain_min,
+                                                                     wl.domain_max, l_idx, l_pm, l_b, d_cache))
+    out["cache_build"] = {"value": LP / (ms * 1e-3) / 1e6, "unit": UNIT, "ms": ms,
+                          "written_voxels": float((d_cache > 0).float().mean().item())}
+    ms = timed(lambda: ctx.stage_reconstruct(wl.camera, rp, Wd, H, m, wl.domain_min, wl.domain_max, idx, pm, b, rgba))
+    out["reconstruct_single_scattering"] = {"value": P / (ms * 1e-3) / 1e6, "unit": UNIT, "ms": ms}
+    rp.ss.enable = 0
+    ms = timed(lambda: ctx.stage_reconstruct(wl.camera, rp, Wd, H, m, wl.domain_min, wl.domain_max, idx, pm, b, rgba))
+    out["reconstruct_plain"] = {"value": P / (ms * 1e-3) / 1e6, "unit": UNIT, "ms": ms}
+    rp.ss.enable = 1
+    ms = timed(lambda: ctx.stage_generate_reference_reconstructed_ss(wl.camera, rp, Wd, H, rgba))
+    out["reference_reconstructed_ss"] = {"value": P / (ms * 1e-3) / 1e6, "unit": UNIT, "ms": ms}
+    # the oracle's cache loop on every 32nd row of the light image (the others left empty)
+    index = lmi.index.astype(np.int64)
+    keep = np.repeat(np.arange(lh) % 32 == 0, lw)
+    counts = np.diff(index) * keep
+    sample_index = np.concatenate([[0], np.cumsum(counts)]).astype(np.uint32)
+    lpm = l_pm.cpu().numpy()
+    sample_pm = np.concatenate([lpm[index[p]:index[p + 1]] for p in np.nonzero(keep)[0]]) if keep.any() else lpm[:0]
+    bounds = lmi.bounds.reshape(-1)
+    row = M.preintegrate(wl.tf1d, wl.tf_step).table
+    t0 = time.perf_counter()
+    O.ss_cache(light, rp, lw, lh, lm, wl.domain_min, wl.domain_max, sample_index, sample_pm, bounds, row)
+    cpu_s = time.perf_counter() - t0
+    rays = int(keep.sum())
+    out["cpu_oracle_cache"] = {"value": rays / cpu_s / 1e6, "unit": UNIT, "threads": 1,
+                               "sample": f"light rows y = 0 mod 32 ({rays} rays, {cpu_s:.1f} s)", "kind": "port"}
+    ctx.close()
+    return out
+
+
 def precision_errors(args, local):
     """Max and RMS errors of the moments, the transmittance and the RGBA of both arithmetic forms against the FP64
     oracle of the same method, on every 8th row of a 128 x 128 image of the default workload (its volume and
@@ -930,7 +1036,8 @@ def main():
 
         _, _, local = dist_info()
         torch.cuda.set_device(local)
-        fn = {"diff": run_diff, "sph": run_sph, "large": run_large, "uncertainty": run_uncertainty}[args.section]
+        fn = {"diff": run_diff, "sph": run_sph, "large": run_large, "uncertainty": run_uncertainty,
+              "scattering": run_scattering}[args.section]
         print(json.dumps({args.section: fn(args, local)}), flush=True)
     else:
         run_ours(args)
