@@ -56,7 +56,7 @@ def parse():
                     help="skip the differentiation-form, SPH and FP64-error sections")
     ap.add_argument("--sph-particles", type=int, default=16_000_000)
     ap.add_argument("--section", default="all",
-                    choices=["all", "diff", "sph", "large", "uncertainty", "scattering"],
+                    choices=["all", "diff", "sph", "large", "uncertainty", "scattering", "file"],
                     help="diff / sph: run only that section and print its JSON (for profiling)")
     return ap.parse_args()
 
@@ -396,6 +396,7 @@ def run_ours(args):
         extras["large"] = run_large(args, local)
         extras["uncertainty"] = run_uncertainty(args, local)
         extras["single_scattering"] = run_scattering(args, local)
+        extras["file_format"] = run_file_format(args, local)
         extras["errors_vs_fp64"] = precision_errors(args, local)
 
     if rank == 0:
@@ -960,6 +961,45 @@ def run_scattering(args, local):
     return out
 
 
+def run_file_format(args, local):
+    """The moment-image file format on the default workload's image (1024^2, m = 64, compact, prediction coded):
+    write_moment_image / load_moment_image in memory with LZ4-compressed sections, the payload as packed 10-bit codes
+    (table [16, 10, ...]) and as the entropy coder's streams.  Quantization runs on the GPU, LZ4 and the arithmetic
+    coder on the host (the streams in parallel over the host threads)."""
+    import torch
+
+    import mray_gb300 as M
+
+    wl = workload(args)
+    Wd, H, m = wl.width, wl.height, wl.num_moments
+    ctx = M.Context(local)
+    ctx.set_stream(torch.cuda.current_stream())
+    ctx.upload_grid(torch.from_numpy(wl.volume).cuda(), wl.domain_min, wl.domain_max)
+    gen = wl.gen
+    gen.prediction_coding = 1
+    mi = ctx.generate(wl.camera, gen, Wd, H, m)
+    mi.domain_min, mi.domain_max = wl.domain_min, wl.domain_max
+    table = np.array([16] + [10] * (m - 1), np.uint8)
+    raw_mb = mi.data.size * 4 / 1e6
+    out = {"workload": f"mixing_layer{args.size}^3_{Wd}x{H}_m{m}_persp prediction coded",
+           "moments_MB": raw_mb, "host_threads": os.cpu_count()}
+    reps = max(1, min(args.steps, 3))
+    for name, entropy in (("packed_10bit_lz4", False), ("entropy_coded_lz4", True)):
+        blob = ctx.encode_moment_image(mi, True, 10, entropy, table)
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            blob = ctx.encode_moment_image(mi, True, 10, entropy, table)
+        enc = (time.perf_counter() - t0) / reps
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            back, _ = ctx.decode_moment_image(blob)
+        dec = (time.perf_counter() - t0) / reps
+        out[name] = {"file_MB": len(blob) / 1e6, "write_ms": enc * 1e3, "read_ms": dec * 1e3,
+                     "write_moments_GB_s": raw_mb / 1e3 / enc, "read_moments_GB_s": raw_mb / 1e3 / dec}
+    ctx.close()
+    return out
+
+
 def precision_errors(args, local):
     """Max and RMS errors of the moments, the transmittance and the RGBA of both arithmetic forms against the FP64
     oracle of the same method, on every 8th row of a 128 x 128 image of the default workload (its volume and
@@ -1037,7 +1077,7 @@ def main():
         _, _, local = dist_info()
         torch.cuda.set_device(local)
         fn = {"diff": run_diff, "sph": run_sph, "large": run_large, "uncertainty": run_uncertainty,
-              "scattering": run_scattering}[args.section]
+              "scattering": run_scattering, "file": run_file_format}[args.section]
         print(json.dumps({args.section: fn(args, local)}), flush=True)
     else:
         run_ours(args)

@@ -245,6 +245,50 @@ int mraygb_generate_reference_reconstructed_ss(mraygb_context *ctx, const mraygb
                                                const mraygb_reconstruction_params *rp, int width, int height,
                                                float *h_rgba, uint8_t *h_rgba8);
 
+/* ---- the moment-image file format ------------------------------------------------------------------------
+ * write_moment_image / load_moment_image (src/moment_image_io.cpp:291-529) with the entropy coder of
+ * src/moment_image_coding.cpp:98-234: the same bytes for the same image and options, except that compressed
+ * sections are LZ4 blocks of this library's encoder (any LZ4 decoder reads them; LZ4_compress_default would choose
+ * other matches).  Quantization and dequantization of the payload run on the GPU; LZ4 and the arithmetic coder
+ * (one stream per moment index, on host threads) on the host.  `quant_table` (num_moments bytes) stands for the
+ * reference's global prediction-coding table (moment_quantization.cpp:166-223): NULL = none set, so the header's
+ * table flag is 0 and prediction codes use [16, bits, bits, ...]; entropy coding of a prediction-coded image needs
+ * it.  Entropy coding needs table entries of 1..14 bits for moment indices >= 1. */
+
+/* Encodes the image into a buffer held by the context; *h_bytes receives its size.  mraygb_copy_encoded copies it
+ * out (capacity >= the size). */
+int mraygb_encode_moment_image(mraygb_context *ctx, const mraygb_moment_image *mi, int compress,
+                               int quantization_bits, int entropy_coding, const uint8_t *quant_table,
+                               uint64_t *h_bytes);
+int mraygb_copy_encoded(mraygb_context *ctx, uint8_t *out, uint64_t capacity);
+
+/* Decodes a file held in memory.  With mi->data NULL only the shape, flags, data_size and has_* fields are filled
+ * (and the table, when the file holds one: *has_quant_table = 1 and num_moments bytes into quant_table if it is not
+ * NULL); call again with index (compact images), data and the arrays the file holds.  A static image written with
+ * compression and quantization cannot be read (the reference's writer puts a byte before its block that its reader
+ * does not expect): MRAYGB_NOT_SUPPORTED. */
+int mraygb_decode_moment_image(mraygb_context *ctx, const uint8_t *bytes, uint64_t n, mraygb_moment_image *mi,
+                               uint8_t *quant_table, int *has_quant_table);
+
+/* The same through files (write_moment_image(mi, filename, compress, quantizationBits, entropy_coding) and
+ * load_moment_image(filename)); loading reads the file on each call. */
+int mraygb_write_moment_image(mraygb_context *ctx, const char *path, const mraygb_moment_image *mi, int compress,
+                              int quantization_bits, int entropy_coding, const uint8_t *quant_table);
+int mraygb_load_moment_image(mraygb_context *ctx, const char *path, mraygb_moment_image *mi, uint8_t *quant_table,
+                             int *has_quant_table);
+
+/* Host-only pieces of the format (no context, no GPU): an LZ4 block of n bytes (returns its size, 0 when it does
+ * not fit in cap) and back (returns the decoded size, -1 for a malformed block); the entropy-coded payload of u16
+ * codes in the layout of the moment data (index: W*H+1 offsets; the size into *h_bytes, the bytes when out holds
+ * them) and back (returns MRAYGB_OK or MRAYGB_INVALID_ARGUMENT for a malformed payload).  threads <= 0: all host
+ * threads. */
+uint64_t mraygb_lz4_compress(const uint8_t *src, uint64_t n, uint8_t *dst, uint64_t cap);
+int64_t mraygb_lz4_decompress(const uint8_t *src, uint64_t n, uint8_t *dst, uint64_t cap);
+int mraygb_entropy_encode(int width, int height, int num_moments, const uint32_t *index, const uint16_t *codes,
+                          const uint8_t *table, int threads, uint8_t *out, uint64_t capacity, uint64_t *h_bytes);
+int mraygb_entropy_decode(const uint8_t *bytes, uint64_t n, int width, int height, int num_moments,
+                          const uint32_t *index, const uint8_t *table, int threads, uint16_t *codes);
+
 /* ---- stage API: device pointers, ordered on the context stream ------------------------------------------ */
 
 /* Per-ray moments over the uploaded grid (generate_ray, src/raymarch_generate.h:69-148, driven as

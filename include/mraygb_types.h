@@ -11,6 +11,7 @@
  *   mraygb_uncertainty_params     <- UncertaintyReconstructionParameters (src/parameters.h:319-325)
  *   mraygb_single_scattering_params <- SingleScatteringParameters (src/parameters.h:173-193)
  *   mraygb_reference_params       <- ReferenceParameters (src/parameters.h:339-350)
+ *   mraygb_moment_image           <- MomentImageHost (src/moment_image.h:33-147), as arrays
  *
  * C++ `bool` members are stored as uint8_t (same size and alignment under the
  * Itanium and AAPCS64 ABIs).  No CUDA or torch types appear here.
@@ -142,6 +143,26 @@ typedef struct mraygb_reference_params
     float data_max;              /* 1.0 */
     mraygb_single_scattering_params ss;
 } mraygb_reference_params;
+
+/* MomentImageHost (src/moment_image.h:33-147) as plain arrays, for the file-format calls.  Writing reads the
+ * arrays given (NULL = the image has none; index is required when is_compact); loading fills the scalar fields and
+ * the has_* flags first, then the arrays the caller provides. */
+typedef struct mraygb_moment_image
+{
+    int32_t width, height, num_moments;
+    uint8_t is_compact, prediction_code;
+    uint8_t has_bounds, has_error_bounds; /* loading: the file holds them */
+    uint8_t has_coding_params;            /* loading: the file holds them */
+    uint8_t pad0[3];
+    int32_t coding_warp;
+    float domain_min[3], domain_max[3];
+    uint64_t data_size;      /* floats in data (compact: index[W*H]; else W*H*num_moments) */
+    uint32_t *index;         /* W*H + 1 offsets when is_compact */
+    float *data;             /* data_size floats */
+    uint16_t *bounds;        /* 2*W*H (lower, upper) */
+    uint16_t *error_bounds;  /* W*H */
+    uint16_t *coding_params; /* 2*(num_moments - 1) (param1, param2) */
+} mraygb_moment_image;
 
 /* Coding warps (src/coding_params.h:35-42). */
 enum

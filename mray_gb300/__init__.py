@@ -13,7 +13,9 @@ from .raymarcher import (MAX_MOMENTS, PRECISION_COMPENSATED_FF_MESE, PRECISION_C
                          create_quantization_table, UncertaintyTransferFunction, read_from_disk_uncertainty,
                          reconstruct_error, reconstruct_uncertainty_interpolation, reconstruct_uncertainty_convolution,
                          generate_reference, SingleScatteringImageHost, SingleScatteringCacheHost,
-                         reconstruct_single_scattering_cache, generate_reference_reconstructed_ss)
+                         reconstruct_single_scattering_cache, generate_reference_reconstructed_ss,
+                         write_moment_image, load_moment_image, lz4_compress, lz4_decompress, entropy_encode,
+                         entropy_decode)
 from ._lib import MrayError
 
 __all__ = [
@@ -25,5 +27,6 @@ __all__ = [
     "UncertaintyTransferFunction", "read_from_disk_uncertainty", "reconstruct_error",
     "reconstruct_uncertainty_interpolation", "reconstruct_uncertainty_convolution", "generate_reference",
     "ReferenceParameters", "SingleScatteringParameters", "SingleScatteringImageHost", "SingleScatteringCacheHost",
-    "reconstruct_single_scattering_cache", "generate_reference_reconstructed_ss",
+    "reconstruct_single_scattering_cache", "generate_reference_reconstructed_ss", "write_moment_image",
+    "load_moment_image", "lz4_compress", "lz4_decompress", "entropy_encode", "entropy_decode",
 ]

@@ -8,8 +8,8 @@ import ctypes as C
 import os
 import threading
 
-from .types import (Camera, ErrorReconstructionParameters, GenerationParameters, ReconstructionParameters,
-                    ReferenceParameters, UncertaintyReconstructionParameters)
+from .types import (Camera, ErrorReconstructionParameters, GenerationParameters, MomentImageArrays,
+                    ReconstructionParameters, ReferenceParameters, UncertaintyReconstructionParameters)
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libmraygb.so")
@@ -32,6 +32,9 @@ EXPORTS = [
     "mraygb_generate_reference", "mraygb_stage_generate_reference", "mraygb_reconstruct_single_scattering_cache",
     "mraygb_stage_reconstruct_single_scattering_cache", "mraygb_upload_single_scattering_cache",
     "mraygb_generate_reference_reconstructed_ss", "mraygb_stage_generate_reference_reconstructed_ss",
+    "mraygb_encode_moment_image", "mraygb_copy_encoded", "mraygb_decode_moment_image", "mraygb_write_moment_image",
+    "mraygb_load_moment_image", "mraygb_lz4_compress", "mraygb_lz4_decompress", "mraygb_entropy_encode",
+    "mraygb_entropy_decode",
 ]
 
 _lock = threading.Lock()
@@ -99,11 +102,24 @@ def _declare(L):
     L.mraygb_stage_generate_reference_reconstructed_ss.argtypes = [vp, P(Camera), RP, i, i, vp]
     L.mraygb_reconstruct_uncertainty.argtypes = [vp, P(Camera), UP, i, i, i, i, f3, f3, vp, vp, u64, vp, vp, i, i, vp,
                                                  vp, vp]
+    MI = P(MomentImageArrays)
+    L.mraygb_encode_moment_image.argtypes = [vp, MI, i, i, i, vp, P(u64)]
+    L.mraygb_copy_encoded.argtypes = [vp, vp, u64]
+    L.mraygb_decode_moment_image.argtypes = [vp, vp, u64, MI, vp, P(i)]
+    L.mraygb_write_moment_image.argtypes = [vp, C.c_char_p, MI, i, i, i, vp]
+    L.mraygb_load_moment_image.argtypes = [vp, C.c_char_p, MI, vp, P(i)]
+    L.mraygb_lz4_compress.argtypes = [vp, u64, vp, u64]
+    L.mraygb_lz4_decompress.argtypes = [vp, u64, vp, u64]
+    L.mraygb_entropy_encode.argtypes = [i, i, i, vp, vp, vp, i, vp, u64, P(u64)]
+    L.mraygb_entropy_decode.argtypes = [vp, u64, i, i, i, vp, vp, i, vp]
     L.mraygb_stage_reconstruct_uncertainty.argtypes = [vp, P(Camera), UP, i, i, i, i, f3, f3, vp, vp, vp, vp, vp]
-    special = ("mraygb_destroy", "mraygb_last_error", "mraygb_get_stream", "mraygb_kernel_launches")
+    special = ("mraygb_destroy", "mraygb_last_error", "mraygb_get_stream", "mraygb_kernel_launches",
+               "mraygb_lz4_compress", "mraygb_lz4_decompress")
     for name in EXPORTS:
         if name not in special:
             getattr(L, name).restype = C.c_int
+    L.mraygb_lz4_compress.restype = u64
+    L.mraygb_lz4_decompress.restype = C.c_int64
 
 
 def load(build_if_missing: bool = True):

@@ -39,6 +39,9 @@ SOURCES = [
     ("uncertainty.cu", ["--fmad=false"]),
     ("reference.cu", []),
     ("scattering.cu", []),
+    ("lz4_block.cpp", []),
+    ("arith_coder.cpp", ["-Xcompiler", "-ffp-contract=off"]),
+    ("moment_file.cpp", []),
     ("api.cpp", ["-x", "cu"]),
 ]
 
@@ -81,7 +84,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(lambda s: _compile(s[0], s[1], verbose), SOURCES))
     tmp = LIB_PATH + ".tmp"
-    cmd = [nvcc(), *ARCH, "-shared", "-cudart", "static", "-o", tmp, *objs]
+    cmd = [nvcc(), *ARCH, "-shared", "-cudart", "static", "-o", tmp, *objs, "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -13,12 +13,15 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include <cuda_runtime.h>
 
 #include "device_common.cuh"
 #include "internal.h"
+#include "lz4_block.h"
+#include "moment_file.h"
 
 using namespace mraygb;
 
@@ -103,6 +106,9 @@ struct mraygb_context
     float ss_dmin[3] = {0, 0, 0}, ss_dmax[3] = {0, 0, 0};
     bool has_ss_cache = false;
     DeviceBuffer ss_keys, ss_linear;
+    // the moment-image file format: the last encoded file and the codes of the entropy coder
+    std::vector<uint8_t> encoded;
+    DeviceBuffer file_codes;
 };
 
 namespace
@@ -734,7 +740,7 @@ void mraygb_destroy(mraygb_context *ctx)
                             &ctx->bits,    &ctx->bit_offset, &ctx->scan_scratch64, &ctx->packed,
                             &ctx->adj_lambda, &ctx->adj_bounds, &ctx->qc_scratch, &ctx->qc_means,
                             &ctx->qc_index, &ctx->qc_data, &ctx->error_bounds, &ctx->errors, &ctx->unc_table,
-                            &ctx->unc_tf1d, &ctx->ss_keys, &ctx->ss_linear};
+                            &ctx->unc_tf1d, &ctx->ss_keys, &ctx->ss_linear, &ctx->file_codes};
     for (DeviceBuffer *b : bufs)
         b->release();
     if (ctx->own_stream)
@@ -1830,6 +1836,555 @@ int mraygb_generate_reference_reconstructed_ss(mraygb_context *ctx, const mraygb
         CK(cudaMemcpyAsync(h_rgba8, ctx->rgba8.ptr, P * 4, cudaMemcpyDeviceToHost, ctx->stream), "u8 colour download");
     CK(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
     return check_device_error_flag(ctx);
+}
+
+// ---- the moment-image file format ------------------------------------------------------------------------------
+
+namespace
+{
+
+constexpr float kPlainLo = (float)(-1.0 / 3.14159265358979323846); // quantize(..., -1.0 / M_PI, 1.0 / M_PI)
+constexpr float kPlainHi = (float)(1.0 / 3.14159265358979323846);
+
+int host_threads()
+{
+    const unsigned t = std::thread::hardware_concurrency();
+    return t ? (int)t : 1;
+}
+
+// the bits of each moment index: the prediction-coding table (given, else [16, bits, ...],
+// get_prediction_coding_quantization_table, moment_quantization.cpp:186-203) or `bits` for every index
+std::vector<uint8_t> payload_table(const mraygb_moment_image &mi, int bits, const uint8_t *quant_table)
+{
+    std::vector<uint8_t> t((size_t)mi.num_moments, (uint8_t)bits);
+    if (mi.prediction_code)
+    {
+        if (quant_table)
+            std::memcpy(t.data(), quant_table, t.size());
+        else if (!t.empty())
+            t[0] = 16;
+    }
+    return t;
+}
+
+int check_file_image(mraygb_context *ctx, const mraygb_moment_image *mi, int bits, int entropy,
+                     const uint8_t *quant_table)
+{
+    if (!mi)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "NULL moment image");
+    if (mi->width <= 0 || mi->height <= 0 || mi->width > 65535 || mi->height > 65535)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "image size %dx%d outside 1..65535", mi->width, mi->height);
+    if (mi->num_moments < 1 || mi->num_moments > 255)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "num_moments %d outside 1..255 (the file stores it in a byte)",
+                    mi->num_moments);
+    if (bits < 1 || bits > 32)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "quantization bits %d outside 1..32", bits);
+    if (!mi->data)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "NULL moment data");
+    const size_t P = (size_t)mi->width * (size_t)mi->height;
+    if (mi->is_compact)
+    {
+        if (!mi->index)
+            return fail(ctx, MRAYGB_INVALID_ARGUMENT, "a compact image needs its index");
+        for (size_t p = 0; p < P; ++p)
+            if (mi->index[p + 1] < mi->index[p] || mi->index[p + 1] - mi->index[p] > (uint32_t)mi->num_moments)
+                return fail(ctx, MRAYGB_INVALID_ARGUMENT, "pixel %zu holds %lld moments (0..%d)", p,
+                            (long long)mi->index[p + 1] - (long long)mi->index[p], mi->num_moments);
+        if (mi->data_size < mi->index[P])
+            return fail(ctx, MRAYGB_INVALID_ARGUMENT, "data_size %llu is below the index's %u",
+                        (unsigned long long)mi->data_size, mi->index[P]);
+    }
+    else
+    {
+        if (mi->prediction_code)
+            return fail(ctx, MRAYGB_INVALID_ARGUMENT, "prediction coding needs a compact image");
+        if (entropy)
+            return fail(ctx, MRAYGB_NOT_SUPPORTED, "the entropy coder writes compact images only");
+        if (mi->data_size < P * (size_t)mi->num_moments)
+            return fail(ctx, MRAYGB_INVALID_ARGUMENT, "a static image needs W*H*m floats");
+    }
+    if (entropy)
+    {
+        if (mi->prediction_code && !quant_table)
+            return fail(ctx, MRAYGB_INVALID_ARGUMENT,
+                        "entropy coding of a prediction-coded image needs the quantization table");
+        const std::vector<uint8_t> t = payload_table(*mi, bits, quant_table);
+        for (int l = 1; l < mi->num_moments; ++l)
+            if (t[l] < 1 || t[l] > 14)
+                return fail(ctx, MRAYGB_INVALID_ARGUMENT,
+                            "entropy coding takes 1..14 bits per code (moment index %d has %d)", l, (int)t[l]);
+    }
+    return MRAYGB_OK;
+}
+
+// the payload of a compact image: floats, packed codes or entropy-coded streams (write_moment_image,
+// moment_image_io.cpp:398-436)
+int compact_payload(mraygb_context *ctx, const mraygb_moment_image &mi, int bits, int entropy,
+                    const uint8_t *quant_table, std::vector<uint8_t> &payload)
+{
+    const int P = mi.width * mi.height;
+    const int m = mi.num_moments;
+    const size_t nd = mi.index[P];
+    if (!entropy && bits == 32)
+    {
+        payload.resize(nd * sizeof(float));
+        if (nd)
+            std::memcpy(payload.data(), mi.data, nd * sizeof(float));
+        return MRAYGB_OK;
+    }
+    const std::vector<uint8_t> table = payload_table(mi, bits, quant_table);
+    const float lo1 = mi.prediction_code ? 0.f : kPlainLo, hi1 = mi.prediction_code ? 1.f : kPlainHi;
+    CK(ctx->index.reserve(((size_t)P + 1) * sizeof(uint32_t)), "index buffer allocation");
+    CK(ctx->compact.reserve((nd ? nd : 1) * sizeof(float)), "moment buffer allocation");
+    CK(cudaMemcpyAsync(ctx->index.ptr, mi.index, ((size_t)P + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                       ctx->stream),
+       "index upload");
+    if (nd)
+        CK(cudaMemcpyAsync(ctx->compact.ptr, mi.data, nd * sizeof(float), cudaMemcpyHostToDevice, ctx->stream),
+           "moment upload");
+    const uint8_t *d_table;
+    const uint32_t *d_prefix;
+    int rc = upload_table(ctx, m, table.data(), &d_table, &d_prefix);
+    if (rc)
+        return rc;
+    if (entropy)
+    {
+        // u16 codes on the device, the arithmetic coder on host threads
+        CK(ctx->file_codes.reserve((nd ? nd : 1) * sizeof(uint16_t)), "code buffer allocation");
+        CK(launch_symbols(P, ctx->index.as<uint32_t>(), ctx->compact.as<float>(), d_table, lo1, hi1,
+                          ctx->file_codes.as<uint16_t>(), ctx->stream),
+           "code launch");
+        ctx->launches += 1;
+        std::vector<uint16_t> codes(nd ? nd : 1);
+        CK(cudaMemcpyAsync(codes.data(), ctx->file_codes.ptr, nd * sizeof(uint16_t), cudaMemcpyDeviceToHost,
+                           ctx->stream),
+           "code download");
+        CK(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+        payload = entropy_encode(mi.width, mi.height, m, mi.index, codes.data(), table.data(), host_threads());
+        return MRAYGB_OK;
+    }
+    uint64_t total_bits = 0;
+    if ((rc = run_bit_offsets(ctx, P, ctx->index.as<uint32_t>(), d_prefix, &total_bits)))
+        return rc;
+    const uint64_t word_bytes = ((total_bits + 31) / 32) * 4;
+    CK(ctx->packed.reserve(word_bytes ? word_bytes : 4), "packed buffer allocation");
+    if (word_bytes)
+        CK(cudaMemsetAsync(ctx->packed.ptr, 0, word_bytes, ctx->stream), "clearing the packed buffer");
+    CK(launch_pack(P, ctx->index.as<uint32_t>(), ctx->compact.as<float>(), d_table, d_prefix,
+                   ctx->bit_offset.as<unsigned long long>(), ctx->packed.as<uint32_t>(), ctx->stream, lo1, hi1),
+       "pack launch");
+    ctx->launches += 1;
+    payload.resize(total_bits / 8); // pack_bits emits whole bytes only
+    if (!payload.empty())
+        CK(cudaMemcpyAsync(payload.data(), ctx->packed.ptr, payload.size(), cudaMemcpyDeviceToHost, ctx->stream),
+           "packed download");
+    CK(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+    return MRAYGB_OK;
+}
+
+// write_static_image (moment_image_io.cpp:438-491): the payload follows the sections without a size prefix
+int static_payload(mraygb_context *ctx, const mraygb_moment_image &mi, int compress, int bits,
+                   std::vector<uint8_t> &out)
+{
+    const size_t count = (size_t)mi.width * (size_t)mi.height * (size_t)mi.num_moments;
+    const uint8_t *raw = reinterpret_cast<const uint8_t *>(mi.data);
+    if (!compress)
+    {
+        out.insert(out.end(), raw, raw + count * sizeof(float));
+        return MRAYGB_OK;
+    }
+    if (bits == 32)
+    {
+        std::vector<uint8_t> block(count * sizeof(float));
+        const size_t r = lz4_compress(raw, count * sizeof(float), block.data(), block.size());
+        if (r == 0 || r >= block.size())
+            out.insert(out.end(), raw, raw + count); // (sic) the reference writes one byte per float here
+        else
+            out.insert(out.end(), block.begin(), block.begin() + (long)r);
+        return MRAYGB_OK;
+    }
+    // the bits byte, then the byte-aligned codes as one LZ4 block (its capacity, four times the codes, always holds it)
+    out.push_back((uint8_t)bits);
+    const size_t code_bytes = count * (size_t)((bits + 7) / 8);
+    CK(ctx->compact.reserve((count ? count : 1) * sizeof(float)), "moment buffer allocation");
+    CK(ctx->packed.reserve(code_bytes ? code_bytes : 4), "code buffer allocation");
+    if (count)
+    {
+        CK(cudaMemcpyAsync(ctx->compact.ptr, mi.data, count * sizeof(float), cudaMemcpyHostToDevice, ctx->stream),
+           "moment upload");
+        CK(launch_static_quantize(count, mi.num_moments, ctx->compact.as<float>(), bits, kPlainLo, kPlainHi,
+                                  ctx->packed.as<uint8_t>(), ctx->stream),
+           "quantize launch");
+        ctx->launches += 1;
+    }
+    std::vector<uint8_t> codes(code_bytes);
+    if (code_bytes)
+        CK(cudaMemcpyAsync(codes.data(), ctx->packed.ptr, code_bytes, cudaMemcpyDeviceToHost, ctx->stream),
+           "code download");
+    CK(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+    std::vector<uint8_t> block(code_bytes * 4 + 16);
+    const size_t r = lz4_compress(codes.data(), code_bytes, block.data(), code_bytes * 4);
+    if (r == 0 || r >= code_bytes * 4)
+        out.insert(out.end(), codes.begin(), codes.end());
+    else
+        out.insert(out.end(), block.begin(), block.begin() + (long)r);
+    return MRAYGB_OK;
+}
+
+int encode_file(mraygb_context *ctx, const mraygb_moment_image *mi, int compress, int bits, int entropy,
+                const uint8_t *quant_table, std::vector<uint8_t> &out)
+{
+    int rc = check_file_image(ctx, mi, bits, entropy, quant_table);
+    if (rc)
+        return rc;
+    const size_t P = (size_t)mi->width * (size_t)mi->height;
+    const int m = mi->num_moments;
+    FileHeader h;
+    h.width = (uint16_t)mi->width;
+    h.height = (uint16_t)mi->height;
+    h.moments = (uint8_t)m;
+    h.coding_warp = (uint8_t)mi->coding_warp;
+    h.bits = (uint8_t)((bits & 0xff) | (entropy ? 64 : 0) | (quant_table ? 128 : 0));
+    h.flags = (uint8_t)((compress ? 1 : 0) | (mi->is_compact ? 2 : 0) | (mi->prediction_code ? 4 : 0) |
+                        (mi->bounds ? 16 : 0) | (mi->error_bounds ? 32 : 0) | (mi->coding_params ? 128 : 0));
+    for (int i = 0; i < 3; ++i)
+    {
+        h.dmin[i] = mi->domain_min[i];
+        h.dmax[i] = mi->domain_max[i];
+    }
+    out.clear();
+    put_header(out, h);
+    if (quant_table)
+        put_section(out, quant_table, (size_t)m, compress != 0);
+    if (mi->is_compact)
+    {
+        std::vector<uint8_t> counts(P);
+        for (size_t p = 0; p < P; ++p)
+            counts[p] = (uint8_t)(mi->index[p + 1] - mi->index[p]);
+        put_section(out, counts.data(), P, compress != 0);
+    }
+    if (mi->bounds)
+        put_section(out, reinterpret_cast<const uint8_t *>(mi->bounds), P * 4, compress != 0);
+    if (mi->error_bounds)
+        put_section(out, reinterpret_cast<const uint8_t *>(mi->error_bounds), P * 2, compress != 0);
+    if (mi->coding_params)
+        put_section(out, reinterpret_cast<const uint8_t *>(mi->coding_params), (size_t)(m - 1) * 4, compress != 0);
+    if (!mi->is_compact)
+        return static_payload(ctx, *mi, compress, bits, out);
+    std::vector<uint8_t> payload;
+    if ((rc = compact_payload(ctx, *mi, bits, entropy, quant_table, payload)))
+        return rc;
+    put_section(out, payload.data(), payload.size(), compress != 0);
+    return MRAYGB_OK;
+}
+
+int decode_file(mraygb_context *ctx, const uint8_t *file, size_t n, mraygb_moment_image *mi, uint8_t *quant_table,
+                int *has_quant_table)
+{
+    if (!file || !mi)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "NULL argument");
+    FileHeader h;
+    if (!get_header(file, n, h))
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "the file is shorter than its header");
+    const bool sizes_only = mi->data == nullptr;
+    const int W = h.width, H = h.height, m = h.moments;
+    const size_t P = (size_t)W * (size_t)H;
+    const bool compressed = h.compressed();
+    const int bits = h.quantization_bits();
+    if (W == 0 || H == 0 || m == 0)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "empty image %dx%d with %d moments in the header", W, H, m);
+    if (bits < 1 || bits > 32)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "quantization bits %d in the header (1..32)", bits);
+    mi->width = W;
+    mi->height = H;
+    mi->num_moments = m;
+    mi->coding_warp = h.coding_warp;
+    mi->is_compact = h.compact();
+    mi->prediction_code = h.prediction_coded();
+    mi->has_bounds = h.has_bounds();
+    mi->has_error_bounds = h.has_error_bounds();
+    mi->has_coding_params = h.has_coding_params();
+    for (int i = 0; i < 3; ++i)
+    {
+        mi->domain_min[i] = h.dmin[i];
+        mi->domain_max[i] = h.dmax[i];
+    }
+    size_t pos = kFileHeaderBytes;
+    std::vector<uint8_t> table((size_t)m, 0);
+    if (has_quant_table)
+        *has_quant_table = h.has_table() ? 1 : 0;
+    if (h.has_table())
+    {
+        if (!get_section(file, n, &pos, (size_t)m, compressed, table.data()))
+            return fail(ctx, MRAYGB_INVALID_ARGUMENT, "truncated quantization table");
+        if (quant_table)
+            std::memcpy(quant_table, table.data(), (size_t)m);
+    }
+    std::vector<uint32_t> index;
+    if (h.compact())
+    {
+        std::vector<uint8_t> counts(P, 0);
+        if (!get_section(file, n, &pos, P, compressed, counts.data()))
+            return fail(ctx, MRAYGB_INVALID_ARGUMENT, "truncated index");
+        index.resize(P + 1);
+        uint64_t sum = 0;
+        for (size_t p = 0; p < P; ++p)
+        {
+            if (counts[p] > m)
+                return fail(ctx, MRAYGB_INVALID_ARGUMENT, "pixel %zu holds %d moments, the header %d", p,
+                            (int)counts[p], m);
+            index[p] = (uint32_t)sum;
+            sum += counts[p];
+        }
+        if (sum >= (1ull << 32))
+            return fail(ctx, MRAYGB_INVALID_ARGUMENT, "the index exceeds u32");
+        index[P] = (uint32_t)sum;
+        mi->data_size = sum;
+    }
+    else
+    {
+        if (h.prediction_coded())
+            return fail(ctx, MRAYGB_INVALID_ARGUMENT, "a static image cannot be prediction coded");
+        mi->data_size = (uint64_t)P * (uint64_t)m;
+    }
+    if (sizes_only)
+        return MRAYGB_OK;
+    if (h.compact() && !mi->index)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "NULL index for a compact image");
+    if ((h.has_bounds() && !mi->bounds) || (h.has_error_bounds() && !mi->error_bounds) ||
+        (h.has_coding_params() && !mi->coding_params))
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "the file holds bounds, error bounds or coding parameters the "
+                                                  "call gives no buffer for");
+    if (h.compact())
+        std::memcpy(mi->index, index.data(), (P + 1) * sizeof(uint32_t));
+    if (h.has_bounds())
+    {
+        std::memset(mi->bounds, 0, P * 4);
+        if (!get_section(file, n, &pos, P * 4, compressed, reinterpret_cast<uint8_t *>(mi->bounds)))
+            return fail(ctx, MRAYGB_INVALID_ARGUMENT, "truncated bounds");
+    }
+    if (h.has_error_bounds())
+    {
+        std::memset(mi->error_bounds, 0, P * 2);
+        if (!get_section(file, n, &pos, P * 2, compressed, reinterpret_cast<uint8_t *>(mi->error_bounds)))
+            return fail(ctx, MRAYGB_INVALID_ARGUMENT, "truncated error bounds");
+    }
+    if (h.has_coding_params())
+    {
+        std::memset(mi->coding_params, 0, (size_t)(m - 1) * 4);
+        if (!get_section(file, n, &pos, (size_t)(m - 1) * 4, compressed,
+                         reinterpret_cast<uint8_t *>(mi->coding_params)))
+            return fail(ctx, MRAYGB_INVALID_ARGUMENT, "truncated coding parameters");
+    }
+    const size_t nd = (size_t)mi->data_size;
+    std::memset(mi->data, 0, nd * sizeof(float));
+    if (!h.compact())
+    {
+        // read_static_image (moment_image_io.cpp:197-252)
+        if (!compressed)
+        {
+            if (n - pos < nd * sizeof(float))
+                return fail(ctx, MRAYGB_INVALID_ARGUMENT, "truncated moment data");
+            std::memcpy(mi->data, file + pos, nd * sizeof(float));
+            return MRAYGB_OK;
+        }
+        if (bits < 32)
+            return fail(ctx, MRAYGB_NOT_SUPPORTED,
+                        "a compressed, quantized static image: the reference's writer puts the bits before the block "
+                        "and its reader decodes from that byte");
+        if (lz4_decompress(file + pos, n - pos, reinterpret_cast<uint8_t *>(mi->data), nd * sizeof(float)) < 0)
+            return fail(ctx, MRAYGB_INVALID_ARGUMENT, "malformed LZ4 block");
+        return MRAYGB_OK;
+    }
+    // read_moment_image (moment_image_io.cpp:158-185)
+    std::vector<uint8_t> bytes;
+    if (!get_payload(file, n, &pos, nd * 4, compressed, bytes))
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "truncated moment payload");
+    const bool entropy = h.entropy_coded();
+    if (!entropy && bits == 32)
+    {
+        std::memcpy(mi->data, bytes.data(), std::min(bytes.size(), nd * sizeof(float)));
+        return MRAYGB_OK;
+    }
+    mraygb_moment_image shape = *mi;
+    if (entropy && h.prediction_coded() && !h.has_table())
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "an entropy-coded prediction-coded image without its table");
+    const std::vector<uint8_t> bit_table = payload_table(shape, bits, h.has_table() ? table.data() : nullptr);
+    const float lo1 = h.prediction_coded() ? 0.f : kPlainLo, hi1 = h.prediction_coded() ? 1.f : kPlainHi;
+    if (entropy)
+        for (int l = 1; l < m; ++l)
+            if (bit_table[l] < 1 || bit_table[l] > 14)
+                return fail(ctx, MRAYGB_INVALID_ARGUMENT, "entropy-coded moment index %d with %d bits", l,
+                            (int)bit_table[l]);
+    const int iP = (int)P;
+    CK(ctx->index.reserve((P + 1) * sizeof(uint32_t)), "index buffer allocation");
+    CK(ctx->compact.reserve((nd ? nd : 1) * sizeof(float)), "moment buffer allocation");
+    CK(cudaMemcpyAsync(ctx->index.ptr, index.data(), (P + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->stream),
+       "index upload");
+    const uint8_t *d_table;
+    const uint32_t *d_prefix;
+    int rc = upload_table(ctx, m, bit_table.data(), &d_table, &d_prefix);
+    if (rc)
+        return rc;
+    if (entropy)
+    {
+        std::vector<uint16_t> codes(nd ? nd : 1, 0);
+        if (!entropy_decode(bytes.data(), bytes.size(), W, H, m, index.data(), bit_table.data(), codes.data(),
+                            host_threads()))
+            return fail(ctx, MRAYGB_INVALID_ARGUMENT, "malformed entropy-coded payload");
+        CK(ctx->file_codes.reserve((nd ? nd : 1) * sizeof(uint16_t)), "code buffer allocation");
+        CK(cudaMemcpyAsync(ctx->file_codes.ptr, codes.data(), nd * sizeof(uint16_t), cudaMemcpyHostToDevice,
+                           ctx->stream),
+           "code upload");
+        CK(launch_desymbols(iP, ctx->index.as<uint32_t>(), ctx->file_codes.as<uint16_t>(), d_table, lo1, hi1,
+                            ctx->compact.as<float>(), ctx->stream),
+           "dequantize launch");
+        ctx->launches += 1;
+    }
+    else
+    {
+        uint64_t total_bits = 0;
+        if ((rc = run_bit_offsets(ctx, iP, ctx->index.as<uint32_t>(), d_prefix, &total_bits)))
+            return rc;
+        CK(ctx->packed.reserve(bytes.size() ? bytes.size() : 1), "packed buffer allocation");
+        if (!bytes.empty())
+            CK(cudaMemcpyAsync(ctx->packed.ptr, bytes.data(), bytes.size(), cudaMemcpyHostToDevice, ctx->stream),
+               "packed upload");
+        CK(launch_unpack(iP, ctx->index.as<uint32_t>(), d_table, d_prefix, ctx->bit_offset.as<unsigned long long>(),
+                         ctx->packed.as<uint8_t>(), bytes.size(), ctx->compact.as<float>(), ctx->stream, lo1, hi1),
+           "unpack launch");
+        ctx->launches += 1;
+    }
+    if (nd)
+        CK(cudaMemcpyAsync(mi->data, ctx->compact.ptr, nd * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream),
+           "moment download");
+    CK(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+    return MRAYGB_OK;
+}
+
+} // namespace
+
+int mraygb_encode_moment_image(mraygb_context *ctx, const mraygb_moment_image *mi, int compress,
+                               int quantization_bits, int entropy_coding, const uint8_t *quant_table,
+                               uint64_t *h_bytes)
+{
+    CHECK_CTX();
+    if (!h_bytes)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "NULL size output");
+    int rc = encode_file(ctx, mi, compress, quantization_bits, entropy_coding, quant_table, ctx->encoded);
+    if (rc)
+    {
+        ctx->encoded.clear();
+        return rc;
+    }
+    *h_bytes = ctx->encoded.size();
+    return MRAYGB_OK;
+}
+
+int mraygb_copy_encoded(mraygb_context *ctx, uint8_t *out, uint64_t capacity)
+{
+    CHECK_CTX();
+    if (!out || capacity < ctx->encoded.size())
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "the buffer holds %llu bytes, %llu needed",
+                    (unsigned long long)capacity, (unsigned long long)ctx->encoded.size());
+    if (!ctx->encoded.empty())
+        std::memcpy(out, ctx->encoded.data(), ctx->encoded.size());
+    return MRAYGB_OK;
+}
+
+int mraygb_decode_moment_image(mraygb_context *ctx, const uint8_t *bytes, uint64_t n, mraygb_moment_image *mi,
+                               uint8_t *quant_table, int *has_quant_table)
+{
+    CHECK_CTX();
+    return decode_file(ctx, bytes, (size_t)n, mi, quant_table, has_quant_table);
+}
+
+int mraygb_write_moment_image(mraygb_context *ctx, const char *path, const mraygb_moment_image *mi, int compress,
+                              int quantization_bits, int entropy_coding, const uint8_t *quant_table)
+{
+    CHECK_CTX();
+    if (!path)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "NULL path");
+    std::vector<uint8_t> bytes;
+    int rc = encode_file(ctx, mi, compress, quantization_bits, entropy_coding, quant_table, bytes);
+    if (rc)
+        return rc;
+    FILE *f = std::fopen(path, "wb");
+    if (!f)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "cannot open %s for writing", path);
+    const size_t w = bytes.empty() ? 0 : std::fwrite(bytes.data(), 1, bytes.size(), f);
+    const bool ok = std::fclose(f) == 0 && w == bytes.size();
+    return ok ? MRAYGB_OK : fail(ctx, MRAYGB_INVALID_ARGUMENT, "cannot write %s", path);
+}
+
+int mraygb_load_moment_image(mraygb_context *ctx, const char *path, mraygb_moment_image *mi, uint8_t *quant_table,
+                             int *has_quant_table)
+{
+    CHECK_CTX();
+    if (!path)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "NULL path");
+    FILE *f = std::fopen(path, "rb");
+    if (!f)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "cannot open %s", path);
+    std::vector<uint8_t> bytes;
+    uint8_t chunk[1 << 16];
+    size_t r;
+    while ((r = std::fread(chunk, 1, sizeof(chunk), f)) > 0)
+        bytes.insert(bytes.end(), chunk, chunk + r);
+    std::fclose(f);
+    return decode_file(ctx, bytes.data(), bytes.size(), mi, quant_table, has_quant_table);
+}
+
+uint64_t mraygb_lz4_compress(const uint8_t *src, uint64_t n, uint8_t *dst, uint64_t cap)
+{
+    if ((!src && n) || !dst || n >= (1ull << 31))
+        return 0;
+    return lz4_compress(src, (size_t)n, dst, (size_t)cap);
+}
+
+int64_t mraygb_lz4_decompress(const uint8_t *src, uint64_t n, uint8_t *dst, uint64_t cap)
+{
+    if (!src || (!dst && cap))
+        return -1;
+    return lz4_decompress(src, (size_t)n, dst, (size_t)cap);
+}
+
+int mraygb_entropy_encode(int width, int height, int num_moments, const uint32_t *index, const uint16_t *codes,
+                          const uint8_t *table, int threads, uint8_t *out, uint64_t capacity, uint64_t *h_bytes)
+{
+    if (width <= 0 || height <= 0 || num_moments < 1 || num_moments > 255 || !index || !codes || !table || !h_bytes)
+        return MRAYGB_INVALID_ARGUMENT;
+    for (int l = 1; l < num_moments; ++l)
+        if (table[l] < 1 || table[l] > 14)
+            return MRAYGB_INVALID_ARGUMENT;
+    const size_t P = (size_t)width * (size_t)height;
+    for (size_t p = 0; p < P; ++p)
+        if (index[p + 1] < index[p] || index[p + 1] - index[p] > (uint32_t)num_moments)
+            return MRAYGB_INVALID_ARGUMENT;
+    const std::vector<uint8_t> bytes =
+        entropy_encode(width, height, num_moments, index, codes, table, threads > 0 ? threads : host_threads());
+    *h_bytes = bytes.size();
+    if (out && capacity >= bytes.size() && !bytes.empty())
+        std::memcpy(out, bytes.data(), bytes.size());
+    return MRAYGB_OK;
+}
+
+int mraygb_entropy_decode(const uint8_t *bytes, uint64_t n, int width, int height, int num_moments,
+                          const uint32_t *index, const uint8_t *table, int threads, uint16_t *codes)
+{
+    if (!bytes || width <= 0 || height <= 0 || num_moments < 1 || num_moments > 255 || !index || !table || !codes)
+        return MRAYGB_INVALID_ARGUMENT;
+    for (int l = 1; l < num_moments; ++l)
+        if (table[l] < 1 || table[l] > 14)
+            return MRAYGB_INVALID_ARGUMENT;
+    const size_t P = (size_t)width * (size_t)height;
+    for (size_t p = 0; p < P; ++p)
+        if (index[p + 1] < index[p] || index[p + 1] - index[p] > (uint32_t)num_moments)
+            return MRAYGB_INVALID_ARGUMENT;
+    return entropy_decode(bytes, (size_t)n, width, height, num_moments, index, table, codes,
+                          threads > 0 ? threads : host_threads())
+               ? MRAYGB_OK
+               : MRAYGB_INVALID_ARGUMENT;
 }
 
 int mraygb_upload_uncertainty_table(mraygb_context *ctx, const float *table_rgba256x256)

@@ -1,0 +1,177 @@
+// The floating-point adaptive arithmetic coder (see arith_coder.h).  Built with -ffp-contract=off: a fused
+// multiply-add in `base + length * cdf` would change the stream.
+
+#include "arith_coder.h"
+
+namespace mraygb
+{
+
+namespace
+{
+
+constexpr double kOut = 65536.0;               // sixteen bits leave the interval per renormalisation step
+constexpr double kMinLength = 1.0 / 65536.0;   // renormalise once the interval is this short
+constexpr double kLsb = 1.0 / 16777216.0 / 16777216.0; // 2^-48, the weight of the last code bit
+constexpr double kLeakage = 2.0 * kLsb;        // taken off every interval, so rounding never widens it
+constexpr unsigned kMaxTotal = 1u << 17;       // counts are halved once their sum passes this
+
+} // namespace
+
+AdaptiveModel::AdaptiveModel(unsigned symbols) : n_(symbols), count_(symbols, 1u), cdf_(symbols, 0.0)
+{
+    // uniform start: the rebuild adds the first period (n) to the total of the n unit counts
+    period_ = n_;
+    rebuild();
+    until_ = period_ = (n_ + 6) >> 1;
+}
+
+void AdaptiveModel::rebuild()
+{
+    total_ += period_;
+    if (total_ > kMaxTotal)
+    {
+        total_ = 0;
+        for (unsigned k = 0; k < n_; ++k)
+        {
+            count_[k] = (count_[k] + 1) >> 1;
+            total_ += count_[k];
+        }
+    }
+    const double scale = 1.0 / double(total_);
+    unsigned below = 0;
+    for (unsigned k = 0; k < n_; ++k)
+    {
+        cdf_[k] = scale * below;
+        below += count_[k];
+    }
+    period_ = (5 * period_) >> 2;
+    const unsigned longest = (n_ + 6) << 3;
+    if (period_ > longest)
+        period_ = longest;
+    until_ = period_;
+}
+
+void ArithEncoder::carry()
+{
+    base_ -= 1.0;
+    // add one to the bytes already out: trailing 0xff become 0, the first other byte grows by one
+    size_t i = out_.size();
+    while (i > 0 && out_[i - 1] == 0xffu)
+        out_[--i] = 0;
+    if (i > 0)
+        ++out_[i - 1];
+}
+
+void ArithEncoder::renormalize()
+{
+    do
+    {
+        base_ *= kOut;
+        const unsigned a = unsigned(base_);
+        out_.push_back((uint8_t)(a >> 8));
+        out_.push_back((uint8_t)(a & 0xffu));
+        base_ -= double(a);
+        length_ *= kOut;
+    } while (length_ <= kMinLength);
+}
+
+void ArithEncoder::put(unsigned s, AdaptiveModel &m)
+{
+    const double top = (s == m.n_ - 1) ? base_ + length_ : base_ + length_ * m.cdf_[s + 1];
+    base_ += length_ * m.cdf_[s];
+    length_ = top - base_;
+    if (base_ >= 1.0)
+        carry();
+    length_ -= kLeakage;
+    if (length_ <= kMinLength)
+        renormalize();
+    m.seen(s);
+}
+
+std::vector<uint8_t> &ArithEncoder::finish()
+{
+    // as few final bytes as identify a point of the interval
+    const unsigned lo = unsigned(kOut * base_);
+    const unsigned hi = unsigned(kOut * (base_ + length_));
+    unsigned last;
+    if (hi - lo < 2)
+    {
+        base_ += 0.5 * kMinLength;
+        last = 3;
+    }
+    else if ((hi >> 8) - (lo >> 8) < 2)
+    {
+        base_ += kMinLength;
+        last = 2;
+    }
+    else
+    {
+        base_ += 256.0 * kMinLength;
+        last = 1;
+    }
+    if (base_ >= 1.0)
+        carry();
+    do
+    {
+        base_ *= 256.0;
+        const unsigned a = unsigned(base_);
+        out_.push_back((uint8_t)a);
+        base_ -= double(a);
+    } while (--last);
+    return out_;
+}
+
+ArithDecoder::ArithDecoder(const uint8_t *bytes, size_t n) : bytes_(bytes), n_(n)
+{
+    for (size_t k = 0; k < 6; ++k)
+        value_ = 256.0 * value_ + kLsb * byte(k);
+}
+
+void ArithDecoder::renormalize()
+{
+    do
+    {
+        base_ *= kOut;
+        const unsigned a = unsigned(base_);
+        base_ -= double(a);
+        value_ = (kOut * value_ - double(a)) + kLsb * (256.0 * double(byte(pos_)) + double(byte(pos_ + 1)));
+        pos_ += 2;
+        length_ *= kOut;
+    } while (length_ <= kMinLength);
+}
+
+unsigned ArithDecoder::get(AdaptiveModel &m)
+{
+    // bisection for the symbol whose sub-interval holds the code value
+    unsigned s = 0, hi_s = m.n_, mid = hi_s >> 1;
+    double lo = base_, hi = base_ + length_;
+    const double target = value_ + kLsb;
+    do
+    {
+        const double z = base_ + length_ * m.cdf_[mid];
+        if (z > target)
+        {
+            hi = z;
+            hi_s = mid;
+        }
+        else
+        {
+            lo = z;
+            s = mid;
+        }
+    } while ((mid = (s + hi_s) >> 1) != s);
+    base_ = lo;
+    length_ = hi - lo;
+    if (base_ >= 1.0)
+    {
+        base_ -= 1.0;
+        value_ -= 1.0;
+    }
+    length_ -= kLeakage;
+    if (length_ <= kMinLength)
+        renormalize();
+    m.seen(s);
+    return s;
+}
+
+} // namespace mraygb

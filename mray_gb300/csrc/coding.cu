@@ -8,6 +8,8 @@
 //   quantize / dequantize              src/moment_quantization.cpp:37-66
 //   quantize_prediction_coding         src/moment_quantization.cpp:239-276 with pack_bits :92-114
 //   dequantize_prediction_coding       src/moment_quantization.cpp:278-332 with unpack_bits :135-160
+//   quantize / dequantize (plain)      src/moment_quantization.cpp:340-407, fixed bits, [-1/pi, 1/pi]
+//   entropy coder symbols              src/moment_image_coding.cpp:110-143
 //
 // Layout: one warp per pixel (lanes take the moment indices l = lane, lane + 32, ...), so reads of the compact
 // moment buffer are coalesced.  Codes are OR-ed into a zeroed u32 word stream at their bit offsets (pixel
@@ -136,22 +138,24 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
     }
 }
 
-__device__ __forceinline__ uint32_t quantize_code(float value, int bits)
+// quantize(value, bits, lo, hi) / dequantize (src/moment_quantization.cpp:37-66); prediction codes use [0, 1],
+// the plain quantizer [0, 1] for the zeroth moment and [-1/pi, 1/pi] for the others
+__device__ __forceinline__ uint32_t quantize_code(float value, int bits, float lo = 0.f, float hi = 1.f)
 {
-    value = clampf(value, 0.f, 1.f);
+    value = clampf(value, lo, hi);
     if (bits == 32)
         return __float_as_uint(value);
-    const float norm = (value - 0.f) / (1.f - 0.f);
+    const float norm = (value - lo) / (hi - lo);
     const uint32_t q = (uint32_t)(norm * (float)((1 << bits) - 1));
     return q & (uint32_t)((1u << bits) - 1u);
 }
 
-__device__ __forceinline__ float dequantize_code(uint32_t q, int bits)
+__device__ __forceinline__ float dequantize_code(uint32_t q, int bits, float lo = 0.f, float hi = 1.f)
 {
     if (bits == 32)
-        return clampf(__uint_as_float(q), 0.f, 1.f);
+        return clampf(__uint_as_float(q), lo, hi);
     const float norm = (float)q / (float)((1 << bits) - 1);
-    return norm * (1.f - 0.f) + 0.f;
+    return norm * (hi - lo) + lo;
 }
 
 __global__ void pixel_bits_kernel(int num_pixels, const uint32_t *__restrict__ index,
@@ -166,7 +170,7 @@ __global__ void pixel_bits_kernel(int num_pixels, const uint32_t *__restrict__ i
 __global__ void __launch_bounds__(kWarpsPerBlock * 32)
     pack_kernel(int num_pixels, const uint32_t *__restrict__ index, const float *__restrict__ data,
                 const uint8_t *__restrict__ table, const uint32_t *__restrict__ prefix_bits,
-                const unsigned long long *__restrict__ bit_offset, uint32_t *__restrict__ words)
+                const unsigned long long *__restrict__ bit_offset, float lo1, float hi1, uint32_t *__restrict__ words)
 {
     const int lane = threadIdx.x & 31;
     const int gw = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
@@ -179,7 +183,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
         for (int l = lane; l < n; l += 32)
         {
             const int b = table[l];
-            const uint32_t code = quantize_code(data[idx + l], b);
+            const uint32_t code = l ? quantize_code(data[idx + l], b, lo1, hi1) : quantize_code(data[idx], b);
             const unsigned long long pos = base + prefix_bits[l];
             const size_t w = (size_t)(pos >> 5);
             const int sh = (int)(pos & 31);
@@ -193,7 +197,8 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
 __global__ void __launch_bounds__(kWarpsPerBlock * 32)
     unpack_kernel(int num_pixels, const uint32_t *__restrict__ index, const uint8_t *__restrict__ table,
                   const uint32_t *__restrict__ prefix_bits, const unsigned long long *__restrict__ bit_offset,
-                  const uint8_t *__restrict__ bytes, unsigned long long num_bytes, float *__restrict__ data)
+                  const uint8_t *__restrict__ bytes, unsigned long long num_bytes, float lo1, float hi1,
+                  float *__restrict__ data)
 {
     const int lane = threadIdx.x & 31;
     const int gw = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
@@ -220,8 +225,57 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
                 acc >>= (pos & 7);
                 q = (uint32_t)(b == 32 ? acc : (acc & ((1ull << b) - 1ull)));
             }
-            data[idx + l] = dequantize_code(q, b);
+            data[idx + l] = l ? dequantize_code(q, b, lo1, hi1) : dequantize_code(q, b);
         }
+    }
+}
+
+// one u16 symbol per moment for the entropy coder, in the layout of the moment data: quantize(value, table[l], ...)
+// with the ranges above (the zeroth moment's code is cast to u16 as the reference stores it)
+__global__ void __launch_bounds__(kWarpsPerBlock * 32)
+    symbols_kernel(int num_pixels, const uint32_t *__restrict__ index, const float *__restrict__ data,
+                   const uint8_t *__restrict__ table, float lo1, float hi1, uint16_t *__restrict__ symbols)
+{
+    const int lane = threadIdx.x & 31;
+    const int gw = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
+    const int nw = gridDim.x * kWarpsPerBlock;
+    for (int p = gw; p < num_pixels; p += nw)
+    {
+        const size_t idx = index[p];
+        const int n = (int)(index[p + 1] - index[p]);
+        for (int l = lane; l < n; l += 32)
+            symbols[idx + l] = (uint16_t)(l ? quantize_code(data[idx + l], table[l], lo1, hi1)
+                                            : quantize_code(data[idx], table[0]));
+    }
+}
+
+__global__ void __launch_bounds__(kWarpsPerBlock * 32)
+    desymbols_kernel(int num_pixels, const uint32_t *__restrict__ index, const uint16_t *__restrict__ symbols,
+                     const uint8_t *__restrict__ table, float lo1, float hi1, float *__restrict__ data)
+{
+    const int lane = threadIdx.x & 31;
+    const int gw = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
+    const int nw = gridDim.x * kWarpsPerBlock;
+    for (int p = gw; p < num_pixels; p += nw)
+    {
+        const size_t idx = index[p];
+        const int n = (int)(index[p + 1] - index[p]);
+        for (int l = lane; l < n; l += 32)
+            data[idx + l] = l ? dequantize_code(symbols[idx + l], table[l], lo1, hi1)
+                              : dequantize_code(symbols[idx], table[0]);
+    }
+}
+
+// the byte-aligned quantizer of images without compaction (quantize(moments, m, bits), moment_quantization.cpp:
+// 464-485 with append :409-433): value i of the W*H*m array as (bits + 7) / 8 little-endian bytes
+__global__ void static_quantize_kernel(size_t count, int m, const float *__restrict__ data, int bits, int nbytes,
+                                       float lo1, float hi1, uint8_t *__restrict__ out)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x)
+    {
+        const uint32_t q = (i % (size_t)m) ? quantize_code(data[i], bits, lo1, hi1) : quantize_code(data[i], bits);
+        for (int k = 0; k < nbytes; ++k)
+            out[i * (size_t)nbytes + k] = (uint8_t)(q >> (8 * k));
     }
 }
 
@@ -264,19 +318,45 @@ cudaError_t launch_pixel_bits(int num_pixels, const uint32_t *index, const uint3
 
 cudaError_t launch_pack(int num_pixels, const uint32_t *index, const float *data, const uint8_t *table,
                         const uint32_t *prefix_bits, const unsigned long long *bit_offset, uint32_t *words,
-                        cudaStream_t stream)
+                        cudaStream_t stream, float lo1, float hi1)
 {
     pack_kernel<<<grid_for(num_pixels), kWarpsPerBlock * 32, 0, stream>>>(num_pixels, index, data, table, prefix_bits,
-                                                                            bit_offset, words);
+                                                                            bit_offset, lo1, hi1, words);
     return cudaGetLastError();
 }
 
 cudaError_t launch_unpack(int num_pixels, const uint32_t *index, const uint8_t *table, const uint32_t *prefix_bits,
                           const unsigned long long *bit_offset, const uint8_t *bytes, unsigned long long num_bytes,
-                          float *data, cudaStream_t stream)
+                          float *data, cudaStream_t stream, float lo1, float hi1)
 {
     unpack_kernel<<<grid_for(num_pixels), kWarpsPerBlock * 32, 0, stream>>>(num_pixels, index, table, prefix_bits,
-                                                                              bit_offset, bytes, num_bytes, data);
+                                                                              bit_offset, bytes, num_bytes, lo1, hi1,
+                                                                              data);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_symbols(int num_pixels, const uint32_t *index, const float *data, const uint8_t *table, float lo1,
+                           float hi1, uint16_t *symbols, cudaStream_t stream)
+{
+    symbols_kernel<<<grid_for(num_pixels), kWarpsPerBlock * 32, 0, stream>>>(num_pixels, index, data, table, lo1, hi1,
+                                                                               symbols);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_desymbols(int num_pixels, const uint32_t *index, const uint16_t *symbols, const uint8_t *table,
+                             float lo1, float hi1, float *data, cudaStream_t stream)
+{
+    desymbols_kernel<<<grid_for(num_pixels), kWarpsPerBlock * 32, 0, stream>>>(num_pixels, index, symbols, table, lo1,
+                                                                                 hi1, data);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_static_quantize(size_t count, int m, const float *data, int bits, float lo1, float hi1,
+                                   uint8_t *out, cudaStream_t stream)
+{
+    const size_t want = (count + 255) / 256;
+    const int blocks = (int)(want < 152 * 16 ? (want ? want : 1) : 152 * 16);
+    static_quantize_kernel<<<blocks, 256, 0, stream>>>(count, m, data, bits, (bits + 7) / 8, lo1, hi1, out);
     return cudaGetLastError();
 }
 

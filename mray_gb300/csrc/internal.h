@@ -148,12 +148,22 @@ cudaError_t launch_coding_warp(int num_pixels, const uint32_t *index, float *dat
                                const float *params, cudaStream_t stream);
 cudaError_t launch_pixel_bits(int num_pixels, const uint32_t *index, const uint32_t *prefix_bits,
                               unsigned long long *bits, cudaStream_t stream);
+// codes of moment index l >= 1 over [lo1, hi1] (prediction codes: [0, 1]; the plain quantizer: [-1/pi, 1/pi]); the
+// zeroth moment over [0, 1]
 cudaError_t launch_pack(int num_pixels, const uint32_t *index, const float *data, const uint8_t *table,
                         const uint32_t *prefix_bits, const unsigned long long *bit_offset, uint32_t *words,
-                        cudaStream_t stream);
+                        cudaStream_t stream, float lo1 = 0.f, float hi1 = 1.f);
 cudaError_t launch_unpack(int num_pixels, const uint32_t *index, const uint8_t *table, const uint32_t *prefix_bits,
                           const unsigned long long *bit_offset, const uint8_t *bytes, unsigned long long num_bytes,
-                          float *data, cudaStream_t stream);
+                          float *data, cudaStream_t stream, float lo1 = 0.f, float hi1 = 1.f);
+// u16 codes in the layout of the moment data, for the entropy coder, and back
+cudaError_t launch_symbols(int num_pixels, const uint32_t *index, const float *data, const uint8_t *table, float lo1,
+                           float hi1, uint16_t *symbols, cudaStream_t stream);
+cudaError_t launch_desymbols(int num_pixels, const uint32_t *index, const uint16_t *symbols, const uint8_t *table,
+                             float lo1, float hi1, float *data, cudaStream_t stream);
+// byte-aligned codes of an image without compaction (count = W*H*m values)
+cudaError_t launch_static_quantize(size_t count, int m, const float *data, int bits, float lo1, float hi1,
+                                   uint8_t *out, cudaStream_t stream);
 
 // reconstruct.cu
 struct ReconArgs

@@ -21,7 +21,8 @@ from typing import Optional
 import numpy as np
 
 from . import _lib
-from .types import (Camera, ErrorReconstructionParameters, GenerationParameters, ReconstructionParameters,
+from .types import (Camera, ErrorReconstructionParameters, GenerationParameters, MomentImageArrays,
+                    ReconstructionParameters,
                     ReferenceParameters, UncertaintyReconstructionParameters)
 
 PRECISION_FP32 = 0
@@ -409,6 +410,53 @@ class Context:
         self._check(self._L.mraygb_stage_generate_reference(self._h, C.byref(cam), C.byref(rp), width, height,
                                                             _dptr(rgba)))
 
+    # ---- the moment-image file format ----
+    def encode_moment_image(self, mi: MomentImageHost, compress: bool, quantization_bits: int,
+                            entropy_coding: bool = False, table=None) -> bytes:
+        """The bytes write_moment_image(mi, filename, compress, quantizationBits, entropy_coding) writes
+        (moment_image_io.cpp:510-529); ``table`` stands for the reference's global prediction-coding table."""
+        arrs, keep = _image_arrays_c(mi)
+        t = None if table is None else np.ascontiguousarray(table, dtype=np.uint8)
+        n = C.c_uint64()
+        self._check(self._L.mraygb_encode_moment_image(self._h, C.byref(arrs), int(compress), int(quantization_bits),
+                                                       int(entropy_coding), _hptr(t), C.byref(n)))
+        out = np.zeros(max(n.value, 1), dtype=np.uint8)
+        self._check(self._L.mraygb_copy_encoded(self._h, _hptr(out), out.size))
+        del keep
+        return out[:n.value].tobytes()
+
+    def decode_moment_image(self, data: bytes):
+        """load_moment_image on bytes (moment_image_io.cpp:291-310): (MomentImageHost, table or None)."""
+        buf = np.frombuffer(data, dtype=np.uint8)
+        arrs = MomentImageArrays()
+        has_table = C.c_int()
+        table = np.zeros(256, dtype=np.uint8)
+        self._check(self._L.mraygb_decode_moment_image(self._h, _hptr(buf), buf.size, C.byref(arrs), _hptr(table),
+                                                       C.byref(has_table)))
+        mi, keep = _image_from_c(arrs)
+        self._check(self._L.mraygb_decode_moment_image(self._h, _hptr(buf), buf.size, C.byref(arrs), None, None))
+        del keep
+        return mi, (table[:mi.num_moments].copy() if has_table.value else None)
+
+    def write_moment_image(self, filename: str, mi: MomentImageHost, compress: bool, quantization_bits: int,
+                           entropy_coding: bool = False, table=None) -> None:
+        arrs, keep = _image_arrays_c(mi)
+        t = None if table is None else np.ascontiguousarray(table, dtype=np.uint8)
+        self._check(self._L.mraygb_write_moment_image(self._h, str(filename).encode(), C.byref(arrs), int(compress),
+                                                      int(quantization_bits), int(entropy_coding), _hptr(t)))
+        del keep
+
+    def load_moment_image(self, filename: str):
+        arrs = MomentImageArrays()
+        has_table = C.c_int()
+        table = np.zeros(256, dtype=np.uint8)
+        path = str(filename).encode()
+        self._check(self._L.mraygb_load_moment_image(self._h, path, C.byref(arrs), _hptr(table), C.byref(has_table)))
+        mi, keep = _image_from_c(arrs)
+        self._check(self._L.mraygb_load_moment_image(self._h, path, C.byref(arrs), None, None))
+        del keep
+        return mi, (table[:mi.num_moments].copy() if has_table.value else None)
+
     # ---- single scattering: the transmittance cache ----
     def reconstruct_single_scattering_cache(self, light_cam: Camera, rp: ReconstructionParameters,
                                             mi: MomentImageHost, return_cache: bool = True):
@@ -587,6 +635,98 @@ class Context:
                                                  _dptr(grad_volume)))
 
 
+def _image_arrays_c(mi: MomentImageHost):
+    """The mraygb_moment_image view of a MomentImageHost, and the arrays that must stay alive while it is used."""
+    a = MomentImageArrays()
+    a.width, a.height, a.num_moments = mi.width, mi.height, mi.num_moments
+    a.is_compact, a.prediction_code, a.coding_warp = int(mi.is_compact), int(mi.prediction_code), int(mi.coding_warp)
+    for i in range(3):
+        a.domain_min[i], a.domain_max[i] = mi.domain_min[i], mi.domain_max[i]
+    data = np.ascontiguousarray(mi.data, dtype=np.float32)
+    index = np.ascontiguousarray(mi.index, dtype=np.uint32) if mi.is_compact else None
+    bounds = np.ascontiguousarray(mi.bounds, dtype=np.uint16) if mi.bounds is not None else None
+    eb = np.ascontiguousarray(mi.error_bounds, dtype=np.uint16) if mi.error_bounds is not None else None
+    cp = np.ascontiguousarray(mi.coding_params, dtype=np.uint16) if mi.coding_params is not None else None
+    a.data_size = data.size
+    a.index, a.data = _addr(index), _addr(data)
+    a.bounds, a.error_bounds, a.coding_params = _addr(bounds), _addr(eb), _addr(cp)
+    return a, (data, index, bounds, eb, cp)
+
+
+def _addr(a):
+    return None if a is None else a.ctypes.data
+
+
+def _image_from_c(a: MomentImageArrays):
+    """A MomentImageHost with the arrays a decoded header asks for, pointed to by ``a``."""
+    mi = MomentImageHost(a.width, a.height, a.num_moments, bool(a.is_compact), bool(a.has_bounds))
+    mi.is_compact, mi.prediction_code, mi.coding_warp = bool(a.is_compact), bool(a.prediction_code), a.coding_warp
+    mi.domain_min = tuple(float(a.domain_min[i]) for i in range(3))
+    mi.domain_max = tuple(float(a.domain_max[i]) for i in range(3))
+    mi.data = np.zeros(a.data_size, dtype=np.float32)
+    if not mi.is_compact:
+        mi.index = None
+    if a.has_error_bounds:
+        mi.add_error_bounds()
+    mi.coding_params = np.zeros(2 * (mi.num_moments - 1), dtype=np.uint16) if a.has_coding_params else None
+    a.index, a.data = _addr(mi.index), _addr(mi.data)
+    a.bounds, a.error_bounds, a.coding_params = _addr(mi.bounds), _addr(mi.error_bounds), _addr(mi.coding_params)
+    return mi, None
+
+
+def lz4_compress(data: bytes) -> bytes:
+    """An LZ4 block of ``data`` (the compression of the file format's sections)."""
+    L = _lib.load()
+    src = np.frombuffer(data, dtype=np.uint8)
+    cap = src.size + src.size // 255 + 16
+    dst = np.zeros(cap, dtype=np.uint8)
+    n = L.mraygb_lz4_compress(_hptr(src) if src.size else None, src.size, _hptr(dst), cap)
+    if n == 0:
+        raise _lib.MrayError(1, "LZ4 block does not fit")
+    return dst[:n].tobytes()
+
+
+def lz4_decompress(block: bytes, size: int) -> bytes:
+    L = _lib.load()
+    src = np.frombuffer(block, dtype=np.uint8)
+    dst = np.zeros(max(size, 1), dtype=np.uint8)
+    r = L.mraygb_lz4_decompress(_hptr(src), src.size, _hptr(dst), size)
+    if r < 0:
+        raise _lib.MrayError(1, "malformed LZ4 block")
+    return dst[:r].tobytes()
+
+
+def entropy_encode(width: int, height: int, num_moments: int, index, codes, table, threads: int = 0) -> bytes:
+    """The entropy-coded payload (moment_image_coding.cpp:206-221) of u16 codes in the layout of the moment data."""
+    L = _lib.load()
+    idx = np.ascontiguousarray(index, dtype=np.uint32)
+    c = np.ascontiguousarray(codes, dtype=np.uint16)
+    t = np.ascontiguousarray(table, dtype=np.uint8)
+    n = C.c_uint64()
+    st = L.mraygb_entropy_encode(width, height, num_moments, _hptr(idx), _hptr(c), _hptr(t), threads, None, 0,
+                                 C.byref(n))
+    if st:
+        raise _lib.MrayError(st, "entropy_encode: invalid arguments")
+    out = np.zeros(max(n.value, 1), dtype=np.uint8)
+    L.mraygb_entropy_encode(width, height, num_moments, _hptr(idx), _hptr(c), _hptr(t), threads, _hptr(out), out.size,
+                            C.byref(n))
+    return out[:n.value].tobytes()
+
+
+def entropy_decode(payload: bytes, width: int, height: int, num_moments: int, index, table,
+                   threads: int = 0) -> np.ndarray:
+    L = _lib.load()
+    buf = np.frombuffer(payload, dtype=np.uint8)
+    idx = np.ascontiguousarray(index, dtype=np.uint32)
+    t = np.ascontiguousarray(table, dtype=np.uint8)
+    codes = np.zeros(max(int(idx[-1]), 1), dtype=np.uint16)
+    st = L.mraygb_entropy_decode(_hptr(buf), buf.size, width, height, num_moments, _hptr(idx), _hptr(t), threads,
+                                 _hptr(codes))
+    if st:
+        raise _lib.MrayError(st, "malformed entropy-coded payload")
+    return codes[:int(idx[-1])]
+
+
 _default: dict = {}
 
 
@@ -643,6 +783,18 @@ def reconstruct(cam: Camera, mi: MomentImageHost, tf: TransferFunction, img: Col
     if ss is not None:
         ctx.reconstruct_single_scattering_cache(ss.cam, params, ss.img, return_cache=False)
     ctx.reconstruct(cam, params, mi, img)
+
+
+def write_moment_image(mi: MomentImageHost, filename: str, compress: bool, quantization_bits: int,
+                       entropy_coding: bool = False, table=None, context: Optional[Context] = None) -> None:
+    """write_moment_image(mi, filename, compress, quantizationBits, entropy_coding) (moment_image_io.h:32-33);
+    ``table``: the prediction-coding table the reference keeps globally (set_prediction_coding_quantization_table)."""
+    (context or default_context()).write_moment_image(filename, mi, compress, quantization_bits, entropy_coding, table)
+
+
+def load_moment_image(filename: str, context: Optional[Context] = None):
+    """load_moment_image(filename) (moment_image_io.h:30): (MomentImageHost, the table the file holds or None)."""
+    return (context or default_context()).load_moment_image(filename)
 
 
 def reconstruct_single_scattering_cache(ss: SingleScatteringImageHost, tf: TransferFunction,

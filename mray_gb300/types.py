@@ -274,3 +274,28 @@ class ReferenceParameters(C.Structure):
             if not hasattr(self, k):
                 raise AttributeError(k)
             setattr(self, k, v)
+
+
+class MomentImageArrays(C.Structure):
+    """``mraygb_moment_image``: a MomentImageHost (moment_image.h:33-147) as plain arrays for the file-format calls."""
+
+    _fields_ = [
+        ("width", C.c_int32),
+        ("height", C.c_int32),
+        ("num_moments", C.c_int32),
+        ("is_compact", C.c_uint8),
+        ("prediction_code", C.c_uint8),
+        ("has_bounds", C.c_uint8),
+        ("has_error_bounds", C.c_uint8),
+        ("has_coding_params", C.c_uint8),
+        ("pad0", C.c_uint8 * 3),
+        ("coding_warp", C.c_int32),
+        ("domain_min", C.c_float * 3),
+        ("domain_max", C.c_float * 3),
+        ("data_size", C.c_uint64),
+        ("index", C.c_void_p),
+        ("data", C.c_void_p),
+        ("bounds", C.c_void_p),
+        ("error_bounds", C.c_void_p),
+        ("coding_params", C.c_void_p),
+    ]

@@ -144,6 +144,8 @@ def _declare(L):
     L.oracle_quantize.argtypes = [C.c_float, C.c_int, C.c_float, C.c_float]
     L.oracle_dequantize.restype = C.c_float
     L.oracle_dequantize.argtypes = [C.c_uint32, C.c_int, C.c_float, C.c_float]
+    L.LZ4_compress_default.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int]
+    L.LZ4_decompress_safe.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int]
     L.oracle_quantize_prediction_coding.restype = C.c_uint64
     L.oracle_quantize_prediction_coding.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                                     C.c_void_p]
@@ -306,6 +308,42 @@ def quantize_prediction_coding(width, height, m, index, data, table):
     out = np.zeros(max(n, 1), dtype=np.uint8)
     L.oracle_quantize_prediction_coding(width, height, m, _ptr(idx), _ptr(d), _ptr(t), _ptr(out))
     return out[:n]
+
+
+def entropy_codes(width, height, m, index, data, table, prediction_code):
+    """The symbols the reference's entropy coder codes (moment_image_coding.cpp:110-143), as u16 in the layout of
+    the moment data: quantize(value, table[l], 0, 1) for the zeroth moment and for prediction codes, else over
+    [-1/pi, 1/pi]."""
+    L = lib()
+    idx = np.asarray(index, dtype=np.int64)
+    d = np.asarray(data, dtype=np.float32)
+    lo = np.float32(0.0) if prediction_code else np.float32(-1.0 / np.pi)
+    hi = np.float32(1.0) if prediction_code else np.float32(1.0 / np.pi)
+    out = np.zeros(d.size, dtype=np.uint16)
+    for p in range(width * height):
+        for l in range(int(idx[p + 1] - idx[p])):
+            a, b = (0.0, 1.0) if l == 0 else (float(lo), float(hi))
+            out[idx[p] + l] = L.oracle_quantize(float(d[idx[p] + l]), int(table[l]), a, b) & 0xffff
+    return out
+
+
+def lz4_compress(data: bytes) -> bytes:
+    """The oracle's own LZ4 block encoder (oracle/lz4_ref.c)."""
+    L = lib()
+    src = np.frombuffer(data, dtype=np.uint8)
+    cap = src.size + src.size // 255 + 16
+    dst = np.zeros(cap, dtype=np.uint8)
+    n = L.LZ4_compress_default(_ptr(src) if src.size else None, _ptr(dst), src.size, cap)
+    return dst[:n].tobytes()
+
+
+def lz4_decompress(block: bytes, size: int):
+    """The oracle's LZ4 block decoder: the bytes, or None for a malformed block."""
+    L = lib()
+    src = np.frombuffer(block, dtype=np.uint8)
+    dst = np.zeros(max(size, 1), dtype=np.uint8)
+    r = L.LZ4_decompress_safe(_ptr(src), _ptr(dst), src.size, size)
+    return None if r < 0 else dst[:r].tobytes()
 
 
 def dequantize_prediction_coding(width, height, m, index, table, packed, size):

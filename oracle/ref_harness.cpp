@@ -28,6 +28,8 @@
 #include "cut/raytracing.h"
 #include "single_scattering_image.h"
 #include "single_scattering_cache.h"
+#include "moment_image_io.h"
+#include "moment_image_coding.h"
 
 #include <omp.h>
 
@@ -732,6 +734,92 @@ int ref_generate_reference_cached_float(const mraygb_camera *c, const mraygb_rec
             o[3] = color.w;
         }
     return 0;
+}
+
+/* ---- the moment-image file format (moment_image_io.cpp, moment_image_coding.cpp) ---- */
+
+namespace
+{
+MomentImageHost file_image(int w, int h, int m, int compact, int pc, int warp, const float *dmin, const float *dmax,
+                           const uint32_t *index, const float *data, uint64_t data_size, const uint16_t *bounds,
+                           const uint16_t *error_bounds, const uint16_t *coding_params)
+{
+    auto mi = make_mi(w, h, m, compact ? index : nullptr, data, data_size, bounds, pc, warp, coding_params, dmin, dmax);
+    if (error_bounds)
+        mi.error_bounds.assign(error_bounds, error_bounds + size_t(w) * h);
+    return mi;
+}
+} // namespace
+
+/* write_moment_image (moment_image_io.cpp:510-529); table: installed as the global prediction-coding table first
+ * (set_prediction_coding_quantization_table; NULL leaves the global state as it is, and once set it stays set) */
+int ref_write_moment_image(const char *path, int w, int h, int m, int compact, int pc, int warp, const float *dmin,
+                           const float *dmax, const uint32_t *index, const float *data, uint64_t data_size,
+                           const uint16_t *bounds, const uint16_t *error_bounds, const uint16_t *coding_params,
+                           int compress, int bits, int entropy, const uint8_t *table)
+{
+    auto mi = file_image(w, h, m, compact, pc, warp, dmin, dmax, index, data, data_size, bounds, error_bounds,
+                         coding_params);
+    if (table)
+        moment_quantization::set_prediction_coding_quantization_table(std::vector<Byte>(table, table + m));
+    write_moment_image(mi, std::string(path), compress != 0, (Byte)bits, entropy != 0);
+    return 0;
+}
+
+/* load_moment_image (moment_image_io.cpp:291-310).  info: w, h, m, compact, pc, warp, has bounds, has error
+ * bounds, has coding params; with data NULL only info, domain (6 floats) and *data_size are written. */
+int ref_load_moment_image(const char *path, int *info, float *domain, uint64_t *data_size, uint32_t *index,
+                          float *data, uint16_t *bounds, uint16_t *error_bounds, uint16_t *coding_params)
+{
+    auto mi = load_moment_image(std::string(path));
+    info[0] = mi.width;
+    info[1] = mi.height;
+    info[2] = mi.num_moments;
+    info[3] = mi.is_compact;
+    info[4] = mi.prediction_code;
+    info[5] = mi.coding_warp;
+    info[6] = mi.has_bounds();
+    info[7] = mi.has_error_bounds();
+    info[8] = mi.has_coding_params();
+    domain[0] = mi.domain.min.x;
+    domain[1] = mi.domain.min.y;
+    domain[2] = mi.domain.min.z;
+    domain[3] = mi.domain.max.x;
+    domain[4] = mi.domain.max.y;
+    domain[5] = mi.domain.max.z;
+    *data_size = mi.data.size();
+    if (!data)
+        return 0;
+    std::memcpy(data, mi.data.data(), mi.data.size() * sizeof(float));
+    if (mi.is_compact && index)
+        std::memcpy(index, mi.index.data(), mi.index.size() * sizeof(uint32_t));
+    if (mi.has_bounds() && bounds)
+        for (size_t i = 0; i < mi.bounds.size(); ++i)
+        {
+            bounds[2 * i] = mi.bounds[i].lower;
+            bounds[2 * i + 1] = mi.bounds[i].upper;
+        }
+    if (mi.has_error_bounds() && error_bounds)
+        std::memcpy(error_bounds, mi.error_bounds.data(), mi.error_bounds.size() * sizeof(uint16_t));
+    if (mi.has_coding_params() && coding_params)
+        for (size_t i = 0; i < mi.coding_params.size(); ++i)
+        {
+            coding_params[2 * i] = mi.coding_params[i].param1;
+            coding_params[2 * i + 1] = mi.coding_params[i].param2;
+        }
+    return 0;
+}
+
+/* entropy_encode (moment_image_coding.cpp:206-221) of a compact image with the table given; returns the size, the
+ * bytes when out holds them */
+uint64_t ref_entropy_encode(int w, int h, int m, const uint32_t *index, const float *data, uint64_t data_size, int pc,
+                            const uint8_t *table, uint8_t *out, uint64_t capacity)
+{
+    auto mi = make_mi(w, h, m, index, data, data_size, nullptr, pc, 1, nullptr, nullptr, nullptr);
+    auto bytes = entropy_encode(mi, std::vector<Byte>(table, table + m));
+    if (out && capacity >= bytes.size())
+        std::memcpy(out, bytes.data(), bytes.size());
+    return bytes.size();
 }
 
 /* ---- MESE primitives (mese/MESE_dynamic.h) ---- */

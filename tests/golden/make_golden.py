@@ -71,6 +71,10 @@ def declare(ref):
                                                       vp]
     ref.ref_generate_reference_float.argtypes = [vp, vp, vp, i, i, i, vp, vp, i, i, vp, vp]
     ref.ref_ss_cache.argtypes = [vp, vp, i, i, i, vp, vp, u64, vp, i, i, vp, vp, vp, vp, vp]
+    ref.ref_write_moment_image.argtypes = [C.c_char_p, i, i, i, i, i, i, vp, vp, vp, vp, u64, vp, vp, vp, i, i, i, vp]
+    ref.ref_load_moment_image.argtypes = [C.c_char_p, vp, vp, vp, vp, vp, vp, vp, vp]
+    ref.ref_entropy_encode.restype = u64
+    ref.ref_entropy_encode.argtypes = [i, i, i, vp, vp, u64, i, vp, vp, u64]
     ref.ref_reconstruct_cached_float.argtypes = [vp, vp, i, i, i, vp, vp, u64, vp, i, i, vp, vp, vp, vp, vp, i, i, i,
                                                  vp, vp, vp]
     ref.ref_reconstruct_ss_u8.argtypes = [vp, vp, i, i, i, vp, vp, u64, vp, i, i, vp, vp, vp, vp, i, i, i, vp, vp,
@@ -592,6 +596,85 @@ def single_scattering(ref):
     return out
 
 
+FILE_CASES = [
+    # name, image, compress, bits, entropy, install the table first (once set, the reference keeps it)
+    ("pc_raw", "pc", 0, 32, 0, False), ("pc_raw_lz4", "pc", 1, 32, 0, False), ("pc_q10", "pc", 0, 10, 0, False),
+    ("pc_q10_lz4", "pc", 1, 10, 0, False), ("plain_raw", "plain", 0, 32, 0, False),
+    ("plain_q12", "plain", 0, 12, 0, False), ("plain_q12_lz4", "plain", 1, 12, 0, False),
+    ("plain_ac10", "plain", 0, 10, 1, False), ("plain_ac10_lz4", "plain", 1, 10, 1, False),
+    ("static_raw", "static", 0, 32, 0, False), ("static_lz4", "static", 1, 32, 0, False),
+    ("static_q16_lz4", "static", 1, 16, 0, False),
+    ("pc_table", "pc", 0, 10, 0, True), ("pc_table_ac", "pc", 0, 10, 1, True), ("pc_table_ac_lz4", "pc", 1, 10, 1, True),
+    ("plain_q12_table", "plain", 0, 12, 0, True),
+]
+FILE_TABLE = [16, 14, 13, 12, 11, 10, 10, 9, 8, 7, 6, 5]
+
+
+def file_format(ref):
+    """Moment-image files written by the reference's write_moment_image (its LZ4 calls served by oracle/lz4_ref.c)
+    and read back by its load_moment_image, for compact images with and without prediction coding and a static
+    image, raw, quantized, entropy coded, with and without compression and the global quantization table; and the
+    entropy-coded payloads on their own."""
+    import tempfile
+
+    wl = W.ml_workload(n=64, width=20, height=16, num_moments=12, seed=11, name="golden_file")
+    vol = np.ascontiguousarray(wl.volume)
+    dmin, dmax = f32(*wl.domain_min), f32(*wl.domain_max)
+    Wd, H, m = wl.width, wl.height, wl.num_moments
+    P_ = Wd * H
+    rng = np.random.default_rng(7)
+    images = {}
+    wl.gen.prediction_coding = 1
+    images["pc"] = _ref_image(ref, wl.camera, wl.gen, vol, dmin, dmax, Wd, H, m)
+    wl.gen.prediction_coding = 0
+    images["plain"] = _ref_image(ref, wl.camera, wl.gen, vol, dmin, dmax, Wd, H, m)
+    wl.gen.compact_image = 0
+    wl.gen.transform_to_bounds = 0
+    st = _ref_image(ref, wl.camera, wl.gen, vol, dmin, dmax, Wd, H, m)
+    images["static"] = (None, np.ascontiguousarray(st[1][:P_ * m]), None, None)
+    error_bounds = rng.integers(0, 65536, P_).astype(np.uint16)
+    out = {"shape": np.array([Wd, H, m], np.int32), "domain": np.stack([dmin, dmax]),
+           "table": np.array(FILE_TABLE, np.uint8), "error_bounds": error_bounds}
+    for k, (index, data, bounds, cp) in images.items():
+        out[f"{k}_data"] = data
+        if index is not None:
+            out[f"{k}_index"], out[f"{k}_bounds"] = index, bounds
+        if cp is not None:
+            out[f"{k}_coding_params"] = cp
+    table = np.array(FILE_TABLE, np.uint8)
+    with tempfile.TemporaryDirectory() as tmp:
+        for name, kind, compress, bits, entropy, use_table in FILE_CASES:
+            index, data, bounds, cp = images[kind]
+            path = os.path.join(tmp, name + ".mom").encode()
+            eb = error_bounds if kind == "plain" else None
+            ref.ref_write_moment_image(path, Wd, H, m, int(index is not None), int(kind == "pc"), 0, P(dmin),
+                                       P(dmax), P(index), P(data), data.size, P(bounds), P(eb), P(cp), compress,
+                                       bits, entropy, P(table) if use_table else None)
+            with open(path, "rb") as f:
+                out[f"file_{name}"] = np.frombuffer(f.read(), np.uint8).copy()
+            if name == "static_q16_lz4":
+                continue  # the reference's reader decodes this one from the wrong byte
+            info = np.zeros(9, np.int32)
+            dom = np.zeros(6, np.float32)
+            size = C.c_uint64()
+            ref.ref_load_moment_image(path, P(info), P(dom), C.byref(size), None, None, None, None, None)
+            d = np.zeros(size.value, np.float32)
+            idx = np.zeros(P_ + 1, np.uint32)
+            b = np.zeros(2 * P_, np.uint16)
+            e = np.zeros(P_, np.uint16)
+            c = np.zeros(2 * (m - 1), np.uint16)
+            ref.ref_load_moment_image(path, P(info), P(dom), C.byref(size), P(idx), P(d), P(b), P(e), P(c))
+            out[f"loaded_{name}_info"], out[f"loaded_{name}_data"] = info, d
+    # the entropy-coded payloads alone
+    for kind, pc, tab in (("plain", 0, np.full(m, 10, np.uint8)), ("pc", 1, table)):
+        index, data = images[kind][0], images[kind][1]
+        n = ref.ref_entropy_encode(Wd, H, m, P(index), P(data), data.size, pc, P(tab), None, 0)
+        buf = np.zeros(n, np.uint8)
+        ref.ref_entropy_encode(Wd, H, m, P(index), P(data), data.size, pc, P(tab), P(buf), n)
+        out[f"entropy_{kind}"], out[f"entropy_{kind}_table"] = buf, tab
+    return out
+
+
 def main():
     ref = O.ref_lib()
     if ref is None:
@@ -609,6 +692,7 @@ def main():
     np.savez_compressed(os.path.join(HERE, "uncertainty.npz"), **uncertainty(ref))
     np.savez_compressed(os.path.join(HERE, "reference_dvr.npz"), **reference_dvr(ref))
     np.savez_compressed(os.path.join(HERE, "single_scattering.npz"), **single_scattering(ref))
+    np.savez_compressed(os.path.join(HERE, "file_format.npz"), **file_format(ref))
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))
