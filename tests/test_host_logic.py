@@ -36,7 +36,7 @@ def test_library_exports_every_declared_symbol():
 
 def test_struct_layouts_match_the_c_header(tmp_path):
     """sizeof / offsetof of the POD mirrors as gcc lays out include/mraygb_types.h, against the ctypes mirrors."""
-    from mray_gb300.types import (Camera, ErrorReconstructionParameters, GenerationParameters,
+    from mray_gb300.types import (Camera, ErrorReconstructionParameters, GenerationParameters, MomentImageArrays,
                                   ReconstructionParameters, ReferenceParameters, SingleScatteringParameters,
                                   UncertaintyReconstructionParameters)
 
@@ -46,7 +46,7 @@ def test_struct_layouts_match_the_c_header(tmp_path):
                "mraygb_error_params": ErrorReconstructionParameters,
                "mraygb_uncertainty_params": UncertaintyReconstructionParameters,
                "mraygb_single_scattering_params": SingleScatteringParameters,
-               "mraygb_reference_params": ReferenceParameters}
+               "mraygb_reference_params": ReferenceParameters, "mraygb_moment_image": MomentImageArrays}
     fields = {st: [f[0] for f in cls._fields_] for st, cls in classes.items()}
     lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{ROOT}/include/mraygb_types.h"', 'int main(){']
     for st, fl in fields.items():
