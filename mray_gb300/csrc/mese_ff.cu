@@ -133,10 +133,10 @@ __device__ __forceinline__ void pixel_span_ff(const uint32_t *index, int m, int 
 }
 
 // ---- one pixel per group of G lanes -----------------------------------------------------------------------
-// The arrays of a pixel (x, E, sol as float pairs) live in shared memory; the G lanes of its group split every
-// sum (lane r takes the indices = r mod G, each with its own compensated accumulator) and combine the partial
-// sums with butterfly shuffles, and split the Levinson update by index pairs.  Per pixel 10 floats per moment of
-// shared memory.
+// The arrays of a pixel (E and the solution as float pairs; x in the solution's space while it is not yet used)
+// live in shared memory; the G lanes of its group split every sum (lane r takes the indices = r mod G, each with
+// its own compensated accumulator) and combine the partial sums with butterfly shuffles, and split the Levinson
+// update by index pairs.  Per pixel 8 floats per moment of shared memory.
 
 // G = 8 lanes per pixel (measured at 64 moments: 3.36 ms per 512^2 launch; 4 lanes, with one shuffle level less
 // per sum but half the warps per SM for the same shared memory, 4.60 ms)
@@ -160,9 +160,38 @@ template <int G> __device__ __forceinline__ void group_reduce(Dot &d)
     }
 }
 
+// two compensated partial sums of the group combined with about half the shuffles of two group_reduce calls: at the
+// first level the even lane of each pair keeps `a` and takes its partner's `a`, the odd lane does the same with `b`;
+// the remaining levels reduce within each parity; a last exchange between the lanes of each pair gives every lane
+// both sums.  The combination tree of each sum, and so its result, is group_reduce's.
+template <int G> __device__ __forceinline__ void group_reduce2(Dot &a, Dot &b, int r)
+{
+    const bool even = (r & 1) == 0;
+    float ks = even ? a.s : b.s, kc = even ? a.c : b.c;
+    const float ss = even ? b.s : a.s, sc = even ? b.c : a.c;
+#pragma unroll
+    for (int o = 1; o < G; o <<= 1)
+    {
+        const float s2 = __shfl_xor_sync(0xffffffffu, o == 1 ? ss : ks, o);
+        const float c2 = __shfl_xor_sync(0xffffffffu, o == 1 ? sc : kc, o);
+        const ff t = two_sum(ks, s2);
+        ks = t.hi;
+        kc = __fadd_rn(__fadd_rn(kc, c2), t.lo);
+    }
+    const float os = __shfl_xor_sync(0xffffffffu, ks, 1);
+    const float oc = __shfl_xor_sync(0xffffffffu, kc, 1);
+    a.s = even ? ks : os;
+    a.c = even ? kc : oc;
+    b.s = even ? os : ks;
+    b.c = even ? oc : kc;
+}
+
+// per pixel: E (4 floats per moment), then one region of 4 floats per moment that holds x (2) during the
+// exponential moments, the solution (4) during Levinson's recursion and in the tail the rounded polynomial (2) and
+// the autocorrelation (2)
 template <int MAXM> struct FfLayout
 {
-    static constexpr int floats_per_pixel = MAXM * 10; // E, sol (4 floats per moment), x (2)
+    static constexpr int floats_per_pixel = MAXM * 8;
 };
 
 // the pair update of Levinson's recursion on the solution divided by prod_j f_j (see the kernel): for the pairs
@@ -220,7 +249,7 @@ __global__ void __launch_bounds__(128) prepare_ff_kernel(int num_pixels, int m, 
     float *base = smem_ff + (size_t)slot * FfLayout<MAXM>::floats_per_pixel;
     cff *E = reinterpret_cast<cff *>(base);
     cff *sol = E + MAXM;
-    ff *x = reinterpret_cast<ff *>(sol + MAXM);
+    ff *x = reinterpret_cast<ff *>(sol); // standard coding: dead once the exponential moments are done
 
     size_t idx = 0;
     int n = 0;
@@ -265,8 +294,7 @@ __global__ void __launch_bounds__(128) prepare_ff_kernel(int num_pixels, int m, 
                 ar.add(sc, e.re);
                 ai.add(sc, e.im);
             }
-            group_reduce<kGroup>(ar);
-            group_reduce<kGroup>(ai);
+            group_reduce2<kGroup>(ar, ai, r);
             if (r == 0)
             {
                 const float2 w2 = c_two_pi_over_l_ff[l];
@@ -276,6 +304,7 @@ __global__ void __launch_bounds__(128) prepare_ff_kernel(int num_pixels, int m, 
             }
             __syncwarp();
         }
+        __syncwarp(); // every lane is done with x before the solution takes its space
         if (r == 0)
         {
             E[0].re = {2.f * E[0].re.hi, 2.f * E[0].re.lo};
@@ -300,8 +329,7 @@ __global__ void __launch_bounds__(128) prepare_ff_kernel(int num_pixels, int m, 
                     ui.add(a.re, b.im);
                     ui.add(a.im, b.re);
                 }
-            group_reduce<kGroup>(ur);
-            group_reduce<kGroup>(ui);
+            group_reduce2<kGroup>(ur, ui, r);
             cff u = {ff_mul(F, ur.result()), ff_mul(F, ui.result())};
             Dot a2d;
             a2d.add(u.re, u.re);
@@ -326,26 +354,10 @@ __global__ void __launch_bounds__(128) prepare_ff_kernel(int num_pixels, int m, 
     else
     {
         // transform_dequantization_real: code_0 = 2 e^{i (pi c_0 - pi/2)} / (4 pi), code_l = w_l axis / |axis| with
-        // axis = i code_0 and w_l the inverse warp of the input; x holds w_l, the factor is formed per use
+        // axis = i code_0 and w_l the inverse warp of the input (formed per step, below)
         double cp, sp;
         sincos(3.141592653589793 * (double)(n > 0 ? in[0] : 0.f) - 1.5707963267948966, &sp, &cp);
         const ff fre = ff_from_double(-sp), fim = ff_from_double(cp); // axis / |axis| = i e^{i phi}
-        for (int i = 1 + r; i < nw; i += kGroup)
-        {
-            const float c = i < n ? in[i] : 0.f;
-            ff w;
-            if (coding_warp == 0)
-            {
-                // prediction_coding_inv_warp: c p1 2 - p0
-                const ff cp1 = ff_mul_f({c, 0.f}, s_params[(i - 1) * 2 + 1]);
-                w = ff_add({2.f * cp1.hi, 2.f * cp1.lo}, {-s_params[(i - 1) * 2], 0.f});
-            }
-            else
-            {
-                w = two_sum(2.f * c, -1.f);
-            }
-            x[i] = w;
-        }
         if (r == 0)
         {
             E[0].re = ff_from_double(0.15915494309189535 * cp);
@@ -368,9 +380,19 @@ __global__ void __launch_bounds__(128) prepare_ff_kernel(int num_pixels, int m, 
                 gi.add(a.re, b.im);
                 gi.add(a.im, b.re);
             }
-            group_reduce<kGroup>(gr);
-            group_reduce<kGroup>(gi);
-            const ff w = x[l];
+            group_reduce2<kGroup>(gr, gi, r);
+            const float c = l < n ? in[l] : 0.f;
+            ff w;
+            if (coding_warp == 0)
+            {
+                // prediction_coding_inv_warp: c p1 2 - p0
+                const ff cp1 = ff_mul_f({c, 0.f}, s_params[(l - 1) * 2 + 1]);
+                w = ff_add({2.f * cp1.hi, 2.f * cp1.lo}, {-s_params[(l - 1) * 2], 0.f});
+            }
+            else
+            {
+                w = two_sum(2.f * c, -1.f);
+            }
             cff u = {ff_mul(w, fre), ff_mul(w, fim)};
             Dot a2d;
             a2d.add(u.re, u.re);
@@ -397,19 +419,32 @@ __global__ void __launch_bounds__(128) prepare_ff_kernel(int num_pixels, int m, 
             __syncwarp();
         }
     }
-    // sol = F shat
-    for (int i = r; i < nw; i += kGroup)
-        sol[i] = {ff_mul(F, sol[i].re), ff_mul(F, sol[i].im)};
+    // the tail in FP32 on the rounded values (lagrange_from_poly): P = 2 pi sol with sol = F shat, and the
+    // exponential moments with E_0 halved; then the autocorrelation a_q and the correlation.  P is formed in
+    // registers, then stored over the solution (the first half of its region), a_q in the second half.
+    constexpr int kPer = (MAXM + kGroup - 1) / kGroup;
+    float pre[kPer], pim[kPer];
+#pragma unroll
+    for (int k = 0; k < kPer; ++k)
+    {
+        const int i = r + k * kGroup;
+        if (i < nw)
+        {
+            pre[k] = 6.28318531f * ff_round(ff_mul(F, sol[i].re));
+            pim[k] = 6.28318531f * ff_round(ff_mul(F, sol[i].im));
+        }
+    }
     __syncwarp();
-
-    // the tail in FP32 on the rounded values (lagrange_from_poly): P = 2 pi sol and the exponential moments with
-    // E_0 halved, as float complex in the space of x; then the autocorrelation a_q and the correlation
-    cx<float> *Pf = reinterpret_cast<cx<float> *>(x);
-    for (int i = r; i < nw; i += kGroup)
-        Pf[i] = {6.28318531f * ff_round(sol[i].re), 6.28318531f * ff_round(sol[i].im)};
+    cx<float> *Pf = reinterpret_cast<cx<float> *>(sol);
+#pragma unroll
+    for (int k = 0; k < kPer; ++k)
+    {
+        const int i = r + k * kGroup;
+        if (i < nw)
+            Pf[i] = {pre[k], pim[k]};
+    }
     __syncwarp();
-    // a_q into sol's space (as float complex), E rounded into E's second half-space is not needed: read E directly
-    cx<float> *A = reinterpret_cast<cx<float> *>(sol);
+    cx<float> *A = Pf + MAXM;
     for (int q = r; q < nw; q += kGroup)
     {
         float ar = 0.f, ai = 0.f;
