@@ -211,6 +211,35 @@ def test_reference_with_cache(gpu_context):
     assert np.abs(img2.rgba_float - ref).max() <= REF_TOL
 
 
+def test_reference_with_cache_over_particles(gpu_context):
+    """generate_reference_reconstructed_ss over SPH particles: the renderer samples the particles and the cache of a
+    light image rendered from them."""
+    import mray_gb300 as M
+    from mray_gb300 import workloads as Wl
+
+    swl = Wl.sph_workload(n=100_000, h=1.0 / 48, width=40, height=32, num_moments=12, seed=9)
+    light = Wl.light_camera((0.3, -1.0, 0.2), center=(0.5, 0.5, 0.5), half_extent=0.9, distance=2.0)
+    ssp = M.SingleScatteringParameters(enable=1, use_cache=1, cache_size_x=20, cache_size_y=18, cache_size_z=16,
+                                       henyey_greenstein_g=-0.2, direction_x=light.dir[0], direction_y=light.dir[1],
+                                       direction_z=light.dir[2])
+    rp = M.ReconstructionParameters(step_size=swl.rec.step_size, bias=swl.rec.bias, medium_emission=1.0,
+                                    medium_scattering=0.5, early_ray_termination=0.99, data_min=swl.gen.data_min,
+                                    data_max=swl.gen.data_max, ss=ssp)
+    tf = M.preintegrate(swl.tf1d, swl.tf_step)
+    gpu_context.upload_tf(tf.table)
+    gpu_context.upload_particles(swl.x, swl.y, swl.z, swl.v, swl.h, swl.domain_min, swl.domain_max)
+    lmi = gpu_context.generate(light, swl.gen, 48, 48, swl.num_moments)
+    lmi.domain_min, lmi.domain_max = swl.domain_min, swl.domain_max
+    cache = gpu_context.reconstruct_single_scattering_cache(light, rp, lmi)
+    assert 0.0 < cache.max() <= 1.0
+    img = gpu_context.generate_reference_reconstructed_ss(swl.camera, rp, swl.width, swl.height)
+    parts = O.ParticleSet(swl.x, swl.y, swl.z, swl.v, swl.h, swl.domain_min, swl.domain_max)
+    ref = O.generate_reference(swl.camera, O.ref_from_rec(rp), None, swl.domain_min, swl.domain_max, swl.width,
+                               swl.height, tf.table, particles=parts, cache=(cache, swl.domain_min, swl.domain_max))
+    assert ref[..., 3].mean() > 0.05
+    assert np.abs(img.rgba_float - ref).max() <= REF_TOL
+
+
 def test_disabled_or_no_scattering_is_the_plain_march(gpu_context):
     """ss.enable = 0, or a medium that does not scatter: no in-scattering (raymarch_reconstruct.h:176-179), the
     plain re-march bit for bit, with a cache resident or not."""
