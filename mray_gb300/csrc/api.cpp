@@ -2264,6 +2264,21 @@ int decode_file(mraygb_context *ctx, const uint8_t *file, size_t n, mraygb_momen
 
 } // namespace
 
+// host allocations and threads of the file format report failure as a status, never as an exception across the C ABI
+#define HOST_GUARD(body)                                                                                            \
+    try                                                                                                             \
+    {                                                                                                               \
+        body                                                                                                        \
+    }                                                                                                               \
+    catch (const std::bad_alloc &)                                                                                  \
+    {                                                                                                               \
+        return fail(ctx, MRAYGB_OUT_OF_MEMORY, "host allocation failed");                                          \
+    }                                                                                                               \
+    catch (const std::exception &e_)                                                                                \
+    {                                                                                                               \
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "host failure: %s", e_.what());                                   \
+    }
+
 int mraygb_encode_moment_image(mraygb_context *ctx, const mraygb_moment_image *mi, int compress,
                                int quantization_bits, int entropy_coding, const uint8_t *quant_table,
                                uint64_t *h_bytes)
@@ -2271,7 +2286,8 @@ int mraygb_encode_moment_image(mraygb_context *ctx, const mraygb_moment_image *m
     CHECK_CTX();
     if (!h_bytes)
         return fail(ctx, MRAYGB_INVALID_ARGUMENT, "NULL size output");
-    int rc = encode_file(ctx, mi, compress, quantization_bits, entropy_coding, quant_table, ctx->encoded);
+    int rc;
+    HOST_GUARD(rc = encode_file(ctx, mi, compress, quantization_bits, entropy_coding, quant_table, ctx->encoded);)
     if (rc)
     {
         ctx->encoded.clear();
@@ -2296,7 +2312,7 @@ int mraygb_decode_moment_image(mraygb_context *ctx, const uint8_t *bytes, uint64
                                uint8_t *quant_table, int *has_quant_table)
 {
     CHECK_CTX();
-    return decode_file(ctx, bytes, (size_t)n, mi, quant_table, has_quant_table);
+    HOST_GUARD(return decode_file(ctx, bytes, (size_t)n, mi, quant_table, has_quant_table);)
 }
 
 int mraygb_write_moment_image(mraygb_context *ctx, const char *path, const mraygb_moment_image *mi, int compress,
@@ -2306,7 +2322,8 @@ int mraygb_write_moment_image(mraygb_context *ctx, const char *path, const mrayg
     if (!path)
         return fail(ctx, MRAYGB_INVALID_ARGUMENT, "NULL path");
     std::vector<uint8_t> bytes;
-    int rc = encode_file(ctx, mi, compress, quantization_bits, entropy_coding, quant_table, bytes);
+    int rc;
+    HOST_GUARD(rc = encode_file(ctx, mi, compress, quantization_bits, entropy_coding, quant_table, bytes);)
     if (rc)
         return rc;
     FILE *f = std::fopen(path, "wb");
@@ -2327,12 +2344,22 @@ int mraygb_load_moment_image(mraygb_context *ctx, const char *path, mraygb_momen
     if (!f)
         return fail(ctx, MRAYGB_INVALID_ARGUMENT, "cannot open %s", path);
     std::vector<uint8_t> bytes;
-    uint8_t chunk[1 << 16];
-    size_t r;
-    while ((r = std::fread(chunk, 1, sizeof(chunk), f)) > 0)
-        bytes.insert(bytes.end(), chunk, chunk + r);
+    bool read_ok = true;
+    try
+    {
+        uint8_t chunk[1 << 16];
+        size_t r;
+        while ((r = std::fread(chunk, 1, sizeof(chunk), f)) > 0)
+            bytes.insert(bytes.end(), chunk, chunk + r);
+    }
+    catch (const std::exception &)
+    {
+        read_ok = false;
+    }
     std::fclose(f);
-    return decode_file(ctx, bytes.data(), bytes.size(), mi, quant_table, has_quant_table);
+    if (!read_ok)
+        return fail(ctx, MRAYGB_OUT_OF_MEMORY, "host allocation failed reading %s", path);
+    HOST_GUARD(return decode_file(ctx, bytes.data(), bytes.size(), mi, quant_table, has_quant_table);)
 }
 
 uint64_t mraygb_lz4_compress(const uint8_t *src, uint64_t n, uint8_t *dst, uint64_t cap)
@@ -2361,12 +2388,19 @@ int mraygb_entropy_encode(int width, int height, int num_moments, const uint32_t
     for (size_t p = 0; p < P; ++p)
         if (index[p + 1] < index[p] || index[p + 1] - index[p] > (uint32_t)num_moments)
             return MRAYGB_INVALID_ARGUMENT;
-    const std::vector<uint8_t> bytes =
-        entropy_encode(width, height, num_moments, index, codes, table, threads > 0 ? threads : host_threads());
-    *h_bytes = bytes.size();
-    if (out && capacity >= bytes.size() && !bytes.empty())
-        std::memcpy(out, bytes.data(), bytes.size());
-    return MRAYGB_OK;
+    try
+    {
+        const std::vector<uint8_t> bytes =
+            entropy_encode(width, height, num_moments, index, codes, table, threads > 0 ? threads : host_threads());
+        *h_bytes = bytes.size();
+        if (out && capacity >= bytes.size() && !bytes.empty())
+            std::memcpy(out, bytes.data(), bytes.size());
+        return MRAYGB_OK;
+    }
+    catch (const std::exception &)
+    {
+        return MRAYGB_OUT_OF_MEMORY;
+    }
 }
 
 int mraygb_entropy_decode(const uint8_t *bytes, uint64_t n, int width, int height, int num_moments,
@@ -2381,10 +2415,17 @@ int mraygb_entropy_decode(const uint8_t *bytes, uint64_t n, int width, int heigh
     for (size_t p = 0; p < P; ++p)
         if (index[p + 1] < index[p] || index[p + 1] - index[p] > (uint32_t)num_moments)
             return MRAYGB_INVALID_ARGUMENT;
-    return entropy_decode(bytes, (size_t)n, width, height, num_moments, index, table, codes,
-                          threads > 0 ? threads : host_threads())
-               ? MRAYGB_OK
-               : MRAYGB_INVALID_ARGUMENT;
+    try
+    {
+        return entropy_decode(bytes, (size_t)n, width, height, num_moments, index, table, codes,
+                              threads > 0 ? threads : host_threads())
+                   ? MRAYGB_OK
+                   : MRAYGB_INVALID_ARGUMENT;
+    }
+    catch (const std::exception &)
+    {
+        return MRAYGB_OUT_OF_MEMORY;
+    }
 }
 
 int mraygb_upload_uncertainty_table(mraygb_context *ctx, const float *table_rgba256x256)
