@@ -164,6 +164,18 @@ int check_image(mraygb_context *ctx, int width, int height, int m)
     return MRAYGB_OK;
 }
 
+void set_extent(GridView &g, const float dmin[3], const float dmax[3])
+{
+    for (int i = 0; i < 3; ++i)
+    {
+        g.dmin[i] = dmin[i];
+        g.dmax[i] = dmax[i];
+        g.ext[i] = dmax[i] - dmin[i];
+        g.ext_pow2[i] = is_pow2_divisor(g.ext[i]) ? 1 : 0;
+        g.inv_ext[i] = g.ext_pow2[i] ? 1.0f / g.ext[i] : 0.f;
+    }
+}
+
 GridView grid_view(const mraygb_context *ctx)
 {
     GridView g;
@@ -171,12 +183,7 @@ GridView grid_view(const mraygb_context *ctx)
     g.nx = ctx->nx;
     g.ny = ctx->ny;
     g.nz = ctx->nz;
-    for (int i = 0; i < 3; ++i)
-    {
-        g.dmin[i] = ctx->dmin[i];
-        g.dmax[i] = ctx->dmax[i];
-        g.ext[i] = ctx->dmax[i] - ctx->dmin[i];
-    }
+    set_extent(g, ctx->dmin, ctx->dmax);
     return g;
 }
 
@@ -224,12 +231,7 @@ GridView ss_cache_view(const mraygb_context *ctx)
     g.nx = ctx->ss_size[0];
     g.ny = ctx->ss_size[1];
     g.nz = ctx->ss_size[2];
-    for (int i = 0; i < 3; ++i)
-    {
-        g.dmin[i] = ctx->ss_dmin[i];
-        g.dmax[i] = ctx->ss_dmax[i];
-        g.ext[i] = ctx->ss_dmax[i] - ctx->ss_dmin[i];
-    }
+    set_extent(g, ctx->ss_dmin, ctx->ss_dmax);
     return g;
 }
 

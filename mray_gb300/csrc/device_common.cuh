@@ -10,6 +10,7 @@
 //   map_density                    src/parameters.h:31-34
 #pragma once
 
+#include <cmath>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -57,7 +58,26 @@ struct GridView
     float dmin[3];
     float ext[3]; // dmax - dmin, rounded as the reference rounds it
     float dmax[3];
+    // where ext is a power of two, x / ext is x * (1 / ext) exactly (both are the correctly rounded x 2^-k)
+    float inv_ext[3];
+    int ext_pow2[3];
 };
+
+// exactly x / d: a multiply by the exact reciprocal where d is a power of two (`pow2` uniform across the launch)
+__device__ __forceinline__ float div_exact(float x, float d, float inv, int pow2)
+{
+    return pow2 ? __fmul_rn(x, inv) : __fdiv_rn(x, d);
+}
+
+// host side: whether d is +-2^k with a normal reciprocal
+inline bool is_pow2_divisor(float d)
+{
+    if (!(d != 0.f) || d != d || d - d != 0.f)
+        return false;
+    int e = 0;
+    const float mant = std::frexp(d < 0.f ? -d : d, &e);
+    return mant == 0.5f && e > -125 && e < 127;
+}
 
 // cut::min / cut::max (src/cut/cuda_math.h:77-85): ternaries, so NaN handling matches the reference
 __device__ __forceinline__ float rmin(float a, float b) { return (a < b) ? a : b; }
@@ -146,7 +166,7 @@ __device__ __forceinline__ GridPoint grid_point(const GridView &g, float px, flo
 #pragma unroll
     for (int i = 0; i < 3; ++i)
     {
-        float np = __fdiv_rn(__fsub_rn(p[i], g.dmin[i]), g.ext[i]);
+        float np = div_exact(__fsub_rn(p[i], g.dmin[i]), g.ext[i], g.inv_ext[i], g.ext_pow2[i]);
         float ip = __fmul_rn(np, (float)sz[i]);
         q.fl[i] = floorf(ip);
         q.a[i] = __fsub_rn(ip, q.fl[i]);
@@ -302,6 +322,12 @@ __device__ __forceinline__ float volume_sample(const ParticleView &v, float x, f
 __device__ __forceinline__ float map_density(float s, float dmin, float dmax)
 {
     return rclamp(__fdiv_rn(__fsub_rn(s, dmin), __fsub_rn(dmax, dmin)), 0.f, 1.f);
+}
+
+// map_density with the span dmax - dmin, its reciprocal and whether it is a power of two precomputed
+__device__ __forceinline__ float map_density(float s, float dmin, float span, float inv_span, int span_pow2)
+{
+    return rclamp(div_exact(__fsub_rn(s, dmin), span, inv_span, span_pow2), 0.f, 1.f);
 }
 
 // float((double)x - M_PI) without double arithmetic: x - pi with pi split into two floats (exact two-sum of

@@ -43,6 +43,8 @@ template <class V> struct GenArgs
     int width, height, m;
     float step;
     float data_min, data_max;
+    float data_span, data_inv_span; // data_max - data_min and its reciprocal
+    int data_span_pow2;             // the span is a power of two: the mapping's division is a multiply
     float bound_eps;
     int transform_to_bounds;
     int compact_image;
@@ -102,7 +104,7 @@ template <class V, int NJ, bool KAHAN> __device__ __forceinline__ void generate_
         const float f0 = map_density(volume_sample(a.vol, __fadd_rn(o[0], __fmul_rn(t, d[0])),
                                                  __fadd_rn(o[1], __fmul_rn(t, d[1])),
                                                  __fadd_rn(o[2], __fmul_rn(t, d[2]))),
-                                     a.data_min, a.data_max);
+                                     a.data_min, a.data_span, a.data_inv_span, a.data_span_pow2);
         blo = rmin(blo, f0);
         bhi = rmax(bhi, f0);
         f_tail = f0;
@@ -144,7 +146,7 @@ template <class V, int NJ, bool KAHAN> __device__ __forceinline__ void generate_
             f_my = map_density(volume_sample(a.vol, __fadd_rn(o[0], __fmul_rn(my_t, d[0])),
                                            __fadd_rn(o[1], __fmul_rn(my_t, d[1])),
                                            __fadd_rn(o[2], __fmul_rn(my_t, d[2]))),
-                               a.data_min, a.data_max);
+                               a.data_min, a.data_span, a.data_inv_span, a.data_span_pow2);
             blo = rmin(blo, f_my);
             bhi = rmax(bhi, f_my);
         }
@@ -243,7 +245,7 @@ template <class V, int NJ, bool KAHAN> __device__ __forceinline__ void generate_
         f_far = map_density(volume_sample(a.vol, __fadd_rn(o[0], __fmul_rn(t_far, d[0])),
                                         __fadd_rn(o[1], __fmul_rn(t_far, d[1])),
                                         __fadd_rn(o[2], __fmul_rn(t_far, d[2]))),
-                            a.data_min, a.data_max);
+                            a.data_min, a.data_span, a.data_inv_span, a.data_span_pow2);
         blo = rmin(blo, f_far);
         bhi = rmax(bhi, f_far);
     }
@@ -388,6 +390,9 @@ cudaError_t launch_generate(const V &vol, const DeviceCamera &cam, const mraygb_
     a.step = gp.step_size;
     a.data_min = gp.data_min;
     a.data_max = gp.data_max;
+    a.data_span = gp.data_max - gp.data_min;
+    a.data_span_pow2 = is_pow2_divisor(a.data_span) ? 1 : 0;
+    a.data_inv_span = a.data_span_pow2 ? 1.0f / a.data_span : 0.f;
     a.bound_eps = gp.transform_bound_eps;
     a.transform_to_bounds = gp.transform_to_bounds ? 1 : 0;
     a.compact_image = gp.compact_image ? 1 : 0;
