@@ -310,17 +310,23 @@ def run_ours(args):
         if ev is not None:
             ev[1].record(stream)
         ctx.stage_compact(W, H, m, d_c, d_mo, d_idx, d_cm)
+        if ev is not None:
+            ev[3].record(stream)
         ctx.stage_prepare_moments(W, H, m, d_idx, d_cm, d_pm, bias=wl.rec.bias)
+        if ev is not None:
+            ev[4].record(stream)
         ctx.stage_reconstruct(wl.camera, wl.rec, W, H, m, wl.domain_min, wl.domain_max, d_idx, d_pm, d_b, d_rgba)
         if ev is not None:
             ev[2].record(stream)
+
+    stage_ms = {}
 
     def timed_loop(precision):
         ctx.precision = precision
         for _ in range(args.warmup):
             step()
         ctx.synchronize()
-        evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+        evs = [[torch.cuda.Event(enable_timing=True) for _ in range(5)] for _ in range(args.steps)]
         if dist:
             dist.barrier()
         torch.cuda.synchronize()
@@ -336,6 +342,11 @@ def run_ours(args):
         launches = ctx.kernel_launches - launches0
         step_ms = [e[0].elapsed_time(e[2]) for e in evs]
         gen_ms = [e[0].elapsed_time(e[1]) for e in evs]
+        stage_ms[precision] = {
+            "generate": statistics.mean(gen_ms),
+            "compaction": statistics.mean(e[1].elapsed_time(e[3]) for e in evs),
+            "prepare": statistics.mean(e[3].elapsed_time(e[4]) for e in evs),
+            "reconstruct": statistics.mean(e[4].elapsed_time(e[2]) for e in evs)}
         return sum(step_ms), statistics.mean(gen_ms), launches, wall
 
     # the plain FP32 form and the FP64 precision form first (reported beside the headline), then the headline
@@ -381,6 +392,18 @@ def run_ours(args):
                          "note": "method FLOPs 4(m-1)+24 per sample (FMA = 2) against the nominal FP32 issue rate "
                                  "152 SMs x 128 lanes x 2 at the max SM clock; the binding roof of this method"}}
 
+    # every stage of the step: its own Mrays/s and its compulsory bytes against the measured HBM peak (the kernels
+    # are issue bound on FP32 arithmetic, so these fractions are small by the method's nature)
+    nd = int(d_idx[-1].item())
+    stage_bytes = {"generate": gen_bytes, "compaction": P * m * 4 + nd * 4 + 8 * P,
+                   "prepare": 2 * nd * 4 + 4 * P, "reconstruct": nd * 4 + 24 * P}
+    stages = {}
+    for name, prec in (("plain_fp32", M.PRECISION_FP32), ("precision_form_fp64", M.PRECISION_COMPENSATED_FP64_MESE),
+                       ("precision_form", M.PRECISION_COMPENSATED_FF_MESE)):
+        stages[name] = {k: {"ms": v, "Mrays_s": P / (v * 1e-3) / 1e6,
+                            "hbm_frac": stage_bytes[k] / (v * 1e-3) / 1e9 / hbm_peak,
+                            "algorithmic_bytes": stage_bytes[k]} for k, v in stage_ms[prec].items()}
+
     e2e = None
     if not args.no_e2e:
         e2e = run_e2e(args, ctx, wl, dist)
@@ -413,7 +436,8 @@ def run_ours(args):
                 "precision_form_fp64": {"value": fp64_value, "unit": UNIT, "ms_per_step": fp64_max / args.steps,
                                         "note": "the same pass with the MESE preparation in native FP64"},
                 "precision_over_plain": value / plain_value,
-                "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
+                "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "stages": stages, "cpu_baseline": cpu,
+                "clocks": clocks,
                 "wall_s_timed": wall, **extras}
         print(json.dumps(line), flush=True)
     ctx.close()
