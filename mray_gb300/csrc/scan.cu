@@ -130,6 +130,38 @@ __global__ void compact_copy_kernel(size_t total, int m, const uint32_t *__restr
     }
 }
 
+// m a multiple of 4, W*H*m < 2^32 (the u32 moment index) and both buffers 16-byte aligned: four consecutive moments
+// of one pixel per thread, one 16-byte load, a 32-bit division for the pixel, a 16-byte store where the
+// destination element is aligned
+__global__ void compact_copy4_kernel(uint32_t total4, uint32_t m, const uint32_t *__restrict__ counts,
+                                     const uint32_t *__restrict__ index, const float4 *__restrict__ moments,
+                                     float *__restrict__ compact)
+{
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < total4; q += gridDim.x * blockDim.x)
+    {
+        const uint32_t e = q * 4u;
+        const uint32_t p = e / m;
+        const uint32_t j = e - p * m;
+        const uint32_t n = counts[p];
+        if (j >= n)
+            continue;
+        const float4 v = moments[q];
+        const size_t d = (size_t)index[p] + j;
+        if (j + 4u <= n && (d & 3u) == 0)
+            *reinterpret_cast<float4 *>(compact + d) = v;
+        else
+        {
+            compact[d] = v.x;
+            if (j + 1u < n)
+                compact[d + 1] = v.y;
+            if (j + 2u < n)
+                compact[d + 2] = v.z;
+            if (j + 3u < n)
+                compact[d + 3] = v.w;
+        }
+    }
+}
+
 } // namespace
 
 size_t scan_scratch_words(size_t n)
@@ -189,6 +221,16 @@ cudaError_t launch_compact_copy(int num_pixels, int m, const uint32_t *counts, c
     if (total == 0)
         return cudaSuccess;
     const int block = 256;
+    if (m % 4 == 0 && total < (1ull << 32) && ((reinterpret_cast<uintptr_t>(moments) | reinterpret_cast<uintptr_t>(compact)) & 15u) == 0)
+    {
+        const size_t total4 = total / 4;
+        size_t blocks = (total4 + block - 1) / block;
+        if (blocks > 152 * 64)
+            blocks = 152 * 64;
+        compact_copy4_kernel<<<(unsigned)blocks, block, 0, stream>>>(
+            (uint32_t)total4, (uint32_t)m, counts, index, reinterpret_cast<const float4 *>(moments), compact);
+        return cudaGetLastError();
+    }
     size_t blocks = (total + block - 1) / block;
     if (blocks > 152 * 64)
         blocks = 152 * 64;
