@@ -49,6 +49,22 @@ void AdaptiveModel::rebuild()
     if (period_ > longest)
         period_ = longest;
     until_ = period_;
+    if (buckets_)
+        index_buckets();
+}
+
+void AdaptiveModel::index_buckets()
+{
+    const unsigned nb = 1u << kBucketBits;
+    bucket_.resize(nb + 1);
+    unsigned s = 0;
+    for (unsigned b = 0; b <= nb; ++b)
+    {
+        const double x = double(b) / double(nb);
+        while (s + 1 < n_ && cdf_[s + 1] <= x)
+            ++s;
+        bucket_[b] = s;
+    }
 }
 
 void ArithEncoder::carry()
@@ -142,24 +158,26 @@ void ArithDecoder::renormalize()
 
 unsigned ArithDecoder::get(AdaptiveModel &m)
 {
-    // bisection for the symbol whose sub-interval holds the code value
-    unsigned s = 0, hi_s = m.n_, mid = hi_s >> 1;
-    double lo = base_, hi = base_ + length_;
-    const double target = value_ + kLsb;
-    do
+    // the symbol s with z(s) <= value + lsb < z(s + 1), z(k) = base + length * cdf[k] (z(n) = base + length): the
+    // coder's bisection finds the same s, since z strictly grows with k, and ends with base = z(s) and
+    // length = z(s + 1) - z(s) as computed here.  The model's bucket table gives the starting guess.
+    if (!m.buckets_)
     {
-        const double z = base_ + length_ * m.cdf_[mid];
-        if (z > target)
-        {
-            hi = z;
-            hi_s = mid;
-        }
-        else
-        {
-            lo = z;
-            s = mid;
-        }
-    } while ((mid = (s + hi_s) >> 1) != s);
+        m.buckets_ = true;
+        m.index_buckets();
+    }
+    const double target = value_ + kLsb;
+    const unsigned nb = 1u << AdaptiveModel::kBucketBits;
+    double r = (target - base_) / length_;
+    r = r < 0.0 ? 0.0 : (r > 1.0 ? 1.0 : r);
+    unsigned s = m.bucket_[(unsigned)(r * nb)];
+    auto z = [&](unsigned k) { return k >= m.n_ ? base_ + length_ : base_ + length_ * m.cdf_[k]; };
+    while (s > 0 && z(s) > target)
+        --s;
+    while (s + 1 < m.n_ && z(s + 1) <= target)
+        ++s;
+    const double lo = s == 0 ? base_ : z(s);
+    const double hi = z(s + 1);
     base_ = lo;
     length_ = hi - lo;
     if (base_ >= 1.0)

@@ -34,9 +34,15 @@ class AdaptiveModel
         if (--until_ == 0)
             rebuild();
     }
+    // decoder only: bucket[b] = the symbol whose cumulative interval holds b / 2^kBucketBits (a starting point for
+    // the search; the decision itself uses the coder's own comparisons)
+    void index_buckets();
+    static constexpr int kBucketBits = 12;
     unsigned n_, total_ = 0, period_ = 0, until_ = 0;
+    bool buckets_ = false;
     std::vector<unsigned> count_;
     std::vector<double> cdf_;
+    std::vector<unsigned> bucket_;
 };
 
 class ArithEncoder
