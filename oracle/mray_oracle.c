@@ -1,6 +1,6 @@
 /*
  * ORACLE — test infrastructure only.  CPU restatement of the reference (TobiasRp/mray) moment-image hot path,
- * used by tests/ as the checker and by bench.py as the timed CPU baseline.  Never linked into the product.
+ * used by tests/ to check the product and by bench.py as the timed CPU baseline.  Never linked into the product.
  *
  * Build: see oracle/Makefile (gcc -O2 -ffp-contract=off -fopenmp; contraction must stay off so that the f32
  * body reproduces the reference's separately rounded float operations on both x86-64 and aarch64).

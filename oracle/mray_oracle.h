@@ -14,7 +14,7 @@
  *           built with -ffp-contract=off so that it reproduces the
  *           reference's compiled CPU path;
  *   *_f64 : the same method evaluated in double precision with exact
- *           constants (the FP64 oracle the new precision form is judged
+ *           constants (the FP64 oracle the new precision form is compared
  *           against).
  * Each function cites the reference file:line it follows.
  */
