@@ -160,6 +160,10 @@ def test_reconstruct_with_cache(gpu_context):
     ok = rgba_agreement(img.rgba_float, r32, march("f64"), TOL)
     assert ok.mean() >= 0.998, f"{(~ok).sum()} pixels"
     assert np.mean(np.abs(img.rgba.astype(int) - g["rgba8"].astype(int)) <= 1) >= 0.999
+    # the same cache uploaded from device memory gives the same image
+    gpu_context.upload_single_scattering_cache(torch.from_numpy(g["cache"].copy()).cuda(), wl.domain_min,
+                                               wl.domain_max)
+    assert np.array_equal(gpu_context.reconstruct(wl.camera, rp, emi).rgba_float, img.rgba_float)
     # the in-scattered light is there
     rp.ss.enable = 0
     plain = gpu_context.reconstruct(wl.camera, rp, emi)
