@@ -105,6 +105,8 @@ typedef struct oracle_options
                                   const float domain_max[3], const uint32_t *index, const R *pmoments,               \
                                   const uint16_t *bounds, const R *tf_table, R *rgba,                                 \
                                   const oracle_options *opt);                                                        \
+    /* an error measure fed value by value, error() after each update (error_measures.h:30-229)               */   \
+    void oracle_error_stream_##SFX(int type, int percentile, int n, const R *values, R *out);                      \
     /* the single-scattering transmittance cache of a light image, sequential (moment_raymarcher.cpp:217-258) */   \
     void oracle_ss_cache_##SFX(const mraygb_camera *light_cam, const mraygb_reconstruction_params *rp, int width,    \
                                int height, int num_moments, const float domain_min[3], const float domain_max[3],    \

@@ -162,6 +162,7 @@ def _declare(L):
             C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float * 3, C.c_float * 3, C.c_void_p,
             C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     for sfx in ("f32", "f64"):
+        getattr(L, f"oracle_error_stream_{sfx}").argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
         getattr(L, f"oracle_ss_cache_{sfx}").argtypes = [
             P(Camera), P(ReconstructionParameters), C.c_int, C.c_int, C.c_int, C.c_float * 3, C.c_float * 3,
             C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
@@ -433,6 +434,16 @@ def prepare_moments(width, height, m, index, data, prediction_code=False, coding
     getattr(L, f"oracle_prepare_moments_{precision}")(width, height, m, _ptr(idx), _ptr(d), int(prediction_code),
                                                       coding_warp, _ptr(cp), bias, _ptr(out), C.byref(o))
     return out[:d.size]
+
+
+def error_stream(error_type, percentile, values, precision="f32"):
+    """ErrorMax / ErrorRMSE / ErrorPercentile (error_measures.h) fed update(0, v) for each value: error() after
+    each update."""
+    L = lib()
+    v = np.ascontiguousarray(values, dtype=_dt(precision))
+    out = np.zeros(v.size, dtype=_dt(precision))
+    getattr(L, f"oracle_error_stream_{precision}")(int(error_type), int(percentile), v.size, _ptr(v), _ptr(out))
+    return out
 
 
 def ss_cache(light_cam, rp, width, height, m, dmin, dmax, index, pmoments, bounds, tf_table, precision="f32"):

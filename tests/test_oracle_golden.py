@@ -534,3 +534,21 @@ def test_single_scattering_cache_last_write_wins():
     assert np.array_equal(upto[~hit], before[~hit])
     assert not np.array_equal(before[hit], only[hit])
     assert np.array_equal(rows(0, lh), full)
+
+
+# ---- tests/test_error_measures.cpp ------------------------------------------------------------------------------
+
+def test_p2_percentile_worked_example():
+    """The reference's own check of its P-squared median (tests/test_error_measures.cpp:29-87, the worked example of
+    Jain and Chlamtac, with the paper's typo corrected as the reference does): the estimate after each of updates
+    6..20 within 0.01."""
+    values = [0.02, 0.15, 0.74, 3.39, 0.83, 22.37, 10.15, 15.43, 38.62, 15.92, 34.60, 10.28, 1.47, 0.40, 0.05, 11.39,
+              0.27, 0.42, 0.09, 11.37]
+    expected = [0.74, 0.74, 2.18, 4.75, 4.75, 9.28, 9.28, 9.28, 9.28, 6.3, 6.3, 6.3, 6.3, 4.44, 4.44]
+    for precision in ("f32", "f64"):
+        est = O.error_stream(2, 50, np.array(values, np.float32), precision)
+        assert np.allclose(est[5:], expected, atol=0.01), (precision, est[5:])
+    # max and RMSE on the same stream
+    v = np.array(values, np.float32)
+    assert O.error_stream(0, 50, v)[-1] == v.max()
+    assert abs(O.error_stream(1, 50, v, "f64")[-1] - np.sqrt(np.mean(v.astype(np.float64) ** 2))) < 1e-12
