@@ -672,6 +672,17 @@ def file_format(ref):
         buf = np.zeros(n, np.uint8)
         ref.ref_entropy_encode(Wd, H, m, P(index), P(data), data.size, pc, P(tab), P(buf), n)
         out[f"entropy_{kind}"], out[f"entropy_{kind}_table"] = buf, tab
+    # the reference's own coding test (tests/test_moment_image_coding.cpp:30-64): a 16 x 16 ramp x / 16 in all ten
+    # moments, prediction coded, table [16, 11, ...]
+    rw, rm = 16, 10
+    ramp = np.repeat((np.arange(rw, dtype=np.float32) / np.float32(rw))[None, :, None], rw, axis=0)
+    ramp = np.ascontiguousarray(np.repeat(ramp, rm, axis=2).reshape(-1))
+    ridx = np.arange(0, rw * rw * rm + 1, rm, dtype=np.uint32)
+    rtab = np.array([16] + [11] * (rm - 1), np.uint8)
+    n = ref.ref_entropy_encode(rw, rw, rm, P(ridx), P(ramp), ramp.size, 1, P(rtab), None, 0)
+    buf = np.zeros(n, np.uint8)
+    ref.ref_entropy_encode(rw, rw, rm, P(ridx), P(ramp), ramp.size, 1, P(rtab), P(buf), n)
+    out["entropy_ramp"], out["entropy_ramp_data"], out["entropy_ramp_table"] = buf, ramp, rtab
     return out
 
 

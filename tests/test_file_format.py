@@ -128,3 +128,21 @@ def test_reference_file_headers(g):
     assert g["file_static_raw"][6] == 0 and g["file_static_raw"][7] == 32
     assert g["file_pc_table_ac"][7] == 10 | 64 | 128  # and the table follows the header
     assert g["file_plain_q12_table"][7] == 12 | 128  # the global table is written for a plain image too
+
+
+def test_reference_coding_test_ramp(g, M):
+    """The reference's own entropy-coding test (tests/test_moment_image_coding.cpp:30-64): a 16 x 16 ramp in ten
+    prediction-coded moments, table [16, 11, ...]; the payload equals the reference's coder's and decodes to within
+    0.1 of the input, as that test asks (here: to the quantizer's own resolution)."""
+    data, table = g["entropy_ramp_data"], g["entropy_ramp_table"]
+    Wd = H = 16
+    m = 10
+    index = np.arange(0, Wd * H * m + 1, m, dtype=np.uint32)
+    codes = O.entropy_codes(Wd, H, m, index, data, table, True)
+    payload = M.entropy_encode(Wd, H, m, index, codes, table)
+    assert payload == g["entropy_ramp"].tobytes()
+    back = M.entropy_decode(payload, Wd, H, m, index, table)
+    L = O.lib()
+    dec = np.array([L.oracle_dequantize(int(back[i]), int(table[i % m]), 0.0, 1.0) for i in range(back.size)])
+    assert np.abs(dec - data).max() <= 0.1
+    assert np.abs(dec - data)[np.arange(back.size) % m > 0].max() <= 1.0 / (2 ** 11 - 1)
