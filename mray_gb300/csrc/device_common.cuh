@@ -380,10 +380,10 @@ __device__ __forceinline__ void seg_coeffs(int j, float h, float &alpha, float &
     beta = num / ((float)j * x);
 }
 
-// Kahan-compensated accumulation of `v` into (sum, comp)
-__device__ __forceinline__ void kahan_add(float &sum, float &comp, float v)
+// Kahan-compensated accumulation into (sum, comp) of a term y that already has the compensation taken off
+// (y = v - comp, formed by the caller, e.g. as the first FMA of a partial sum)
+__device__ __forceinline__ void kahan_add_corrected(float &sum, float &comp, float y)
 {
-    float y = __fsub_rn(v, comp);
     float t = __fadd_rn(sum, y);
     comp = __fsub_rn(__fsub_rn(t, sum), y);
     sum = t;

@@ -23,7 +23,8 @@
 // z_k^q z_k^{4i} by complex rotation, so no moment is more than 16 rotations from a fresh sincos.
 //
 // Two arithmetic forms: plain FP32 sums, or per-round partial sums added with Kahan compensation
-// (MRAYGB_PRECISION_COMPENSATED_FP64_MESE).
+// (MRAYGB_PRECISION_COMPENSATED_FP64_MESE; the partial starts from minus the compensation, which saves Kahan's
+// separate correction step).
 
 #include "device_common.cuh"
 #include "internal.h"
@@ -189,16 +190,17 @@ template <class V, int NJ, bool KAHAN> __device__ __forceinline__ void generate_
         {
             if (KAHAN)
             {
-                float pc = Ss[0] * w[0].x;
-                float pd = Ds[0] * w[0].y;
+                // the partial sum starts from minus the compensation, so it is already Kahan's corrected term
+                float pc = fmaf(Ss[0], w[0].x, -Ck[i]);
+                float pd = fmaf(Ds[0], w[0].y, -Dk[i]);
 #pragma unroll
                 for (int s = 1; s < 4; ++s)
                 {
                     pc = fmaf(Ss[s], w[s].x, pc);
                     pd = fmaf(Ds[s], w[s].y, pd);
                 }
-                kahan_add(C[i], Ck[i], pc);
-                kahan_add(Dc[i], Dk[i], pd);
+                kahan_add_corrected(C[i], Ck[i], pc);
+                kahan_add_corrected(Dc[i], Dk[i], pd);
             }
             else
             {
