@@ -308,6 +308,14 @@ int mraygb_stage_compact(mraygb_context *ctx, int width, int height, int num_mom
                          const float *d_moments, uint32_t *d_index, float *d_compact, uint64_t capacity,
                          uint64_t *h_total);
 
+/* cosf / sinf as the MESE algebra evaluates them on the device: the zeroth-moment phase of
+ * trigonometricToExponentialMoments (src/mese/MESE_dynamic.h:38-40) and of transform_dequantization_real
+ * (src/moment_prediction_coding.h:103-104), which the reference takes from the host C library.  For every float
+ * x in [-pi, pi] the results equal the C library's of the machine that built this library, bit for bit (a
+ * double-precision evaluation corrected by a table generated from that library at build time); outside that
+ * interval, the double-precision functions rounded to float.  n floats of d_x in, d_sin and d_cos out. */
+int mraygb_stage_libm_sincosf(mraygb_context *ctx, const float *d_x, float *d_sin, float *d_cos, uint64_t n);
+
 /* MomentImageDevice::prediction_encode (src/moment_image_device.cu:166-195; host form
  * MomentImageHost::prediction_encode, src/moment_image.cpp:96-152) in place on a compact image: bias lerp,
  * trigonometric -> exponential moments, Levinson-style encode, projection to the real line, coding parameters
@@ -374,10 +382,12 @@ int mraygb_stage_generate_reference_reconstructed_ss(mraygb_context *ctx, const 
  * context: it runs on the current device and on `stream` (a cudaStream_t, NULL for the default stream), and
  * the scan's block sums live in a fixed device array of 16448 words (64 KiB) that each GPU loading the library
  * holds until the process exits.  Limit: W * H <= 16,777,216 pixels (4096 x 4096); larger images return
- * MRAYGB_INVALID_ARGUMENT.  The first call on a device looks up the array's device address (set-up), so make
- * that first call before any stream capture.  All calls share the array: calls that overlap on the GPU race on
- * it and must be ordered by the caller.  Failures are reported by the return code only (there is no context to
- * hold a message). */
+ * MRAYGB_INVALID_ARGUMENT.  The first call on a device looks up the array's device address (set-up) and keeps
+ * it for the life of the process: after cudaDeviceReset, or with a non-primary driver context current on that
+ * device, the kept address is not valid, so such callers must not use this entry point.  Every call reads the
+ * compact size back and waits for `stream`, so it blocks the calling thread and cannot be used inside stream
+ * capture.  All calls share the array: calls that overlap on the GPU race on it and must be ordered by the
+ * caller.  Failures are reported by the return code only (there is no context to hold a message). */
 int mraygb_stage_compact_noalloc(void *stream, int width, int height, int num_moments, const uint32_t *d_counts,
                                  const float *d_moments, uint32_t *d_index, float *d_compact, uint64_t capacity,
                                  uint64_t *h_total);

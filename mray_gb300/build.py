@@ -42,8 +42,17 @@ SOURCES = [
     ("lz4_block.cpp", []),
     ("arith_coder.cpp", ["-Xcompiler", "-ffp-contract=off"]),
     ("moment_file.cpp", []),
+    ("libm_trig_host.cpp", []),
     ("api.cpp", ["-x", "cu"]),
 ]
+
+# The sinf / cosf exception table (csrc/libm_trig_core.h): generated by running the host C library over every float
+# of [-pi, pi], then linked into the library as a read-only blob.
+TRIG_GEN_SRC = os.path.join(CSRC, "libm_trig_gen.cpp")
+TRIG_GEN = os.path.join(BUILD_DIR, "libm_trig_gen")
+TRIG_TABLE = os.path.join(BUILD_DIR, "libm_trig_table.bin")
+TRIG_ASM = os.path.join(BUILD_DIR, "libm_trig_table.S")
+TRIG_OBJ = os.path.join(BUILD_DIR, "libm_trig_table.o")
 
 
 def nvcc() -> str:
@@ -66,6 +75,40 @@ def _compile(src: str, extra: list[str], verbose: bool) -> str:
     return obj
 
 
+def _host_cxx() -> str:
+    for cand in (os.environ.get("CXX"), shutil.which("g++"), shutil.which("c++")):
+        if cand:
+            return cand
+    raise RuntimeError("no host C++ compiler found (g++)")
+
+
+def _run(cmd: list[str], what: str) -> None:
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"{what} failed:\n{r.stdout}\n{r.stderr}")
+
+
+def _trig_table() -> str:
+    """Compile and run the table generator; assemble the table into an object file."""
+    _run([_host_cxx(), "-O2", "-std=c++17", "-ffp-contract=off", "-pthread", TRIG_GEN_SRC, "-o", TRIG_GEN],
+         "compiling libm_trig_gen")
+    _run([TRIG_GEN, TRIG_TABLE], "generating the sinf / cosf table")
+    with open(TRIG_ASM, "w") as f:
+        f.write("\t.section .rodata.mraygb_libm_trig,\"a\"\n"
+                "\t.balign 16\n"
+                "\t.globl mraygb_libm_trig_table_begin\n"
+                "\t.hidden mraygb_libm_trig_table_begin\n"
+                "mraygb_libm_trig_table_begin:\n"
+                f"\t.incbin \"{TRIG_TABLE}\"\n"
+                "\t.globl mraygb_libm_trig_table_end\n"
+                "\t.hidden mraygb_libm_trig_table_end\n"
+                "mraygb_libm_trig_table_end:\n"
+                "\t.section .note.GNU-stack,\"\",%progbits\n")
+    cc = os.environ.get("CC") or shutil.which("gcc") or "cc"
+    _run([cc, "-c", TRIG_ASM, "-o", TRIG_OBJ], "assembling the sinf / cosf table")
+    return TRIG_OBJ
+
+
 def _stale() -> bool:
     if not os.path.exists(LIB_PATH):
         return True
@@ -81,8 +124,10 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if not force and not _stale():
         return LIB_PATH
     os.makedirs(BUILD_DIR, exist_ok=True)
-    with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
+    with cf.ThreadPoolExecutor(max_workers=len(SOURCES) + 1) as ex:
+        table = ex.submit(_trig_table)
         objs = list(ex.map(lambda s: _compile(s[0], s[1], verbose), SOURCES))
+        objs.append(table.result())
     tmp = LIB_PATH + ".tmp"
     cmd = [nvcc(), *ARCH, "-shared", "-cudart", "static", "-o", tmp, *objs, "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)

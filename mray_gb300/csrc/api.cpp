@@ -1033,6 +1033,16 @@ int mraygb_stage_reconstruct(mraygb_context *ctx, const mraygb_camera *cam, cons
                            d_rgba, d_rgba8);
 }
 
+int mraygb_stage_libm_sincosf(mraygb_context *ctx, const float *d_x, float *d_sin, float *d_cos, uint64_t n)
+{
+    CHECK_CTX();
+    if (n > 0 && (!d_x || !d_sin || !d_cos))
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "NULL argument");
+    CK(launch_libm_sincosf(n, d_x, d_sin, d_cos, ctx->stream), "libm_sincosf");
+    ctx->launches += n > 0 ? 1 : 0;
+    return MRAYGB_OK;
+}
+
 int mraygb_stage_prediction_encode(mraygb_context *ctx, int width, int height, int m, const uint32_t *d_index,
                                    float *d_data, uint64_t data_size, int coding_warp, float bias,
                                    uint16_t *d_coding_params)

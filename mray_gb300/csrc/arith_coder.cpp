@@ -1,6 +1,19 @@
 // The floating-point adaptive arithmetic coder (see arith_coder.h).  Built with -ffp-contract=off: a fused
 // multiply-add in `base + length * cdf` would change the stream.
 
+// Attribution.  The coding steps restate the FastAC arithmetic coder, whose notice reads:
+//
+//   Fast arithmetic coding implementation -> double-precision floating-point arithmetic, Version 1.00, April 25,
+//   2004.  WARNING: The only purpose of this program is to demonstrate the basic principles of arithmetic coding.
+//   It is provided as is, without any express or implied warranty, without even the warranty of fitness for any
+//   particular purpose, or that the implementations are correct.  Permission to copy and redistribute this code is
+//   hereby granted, provided that this warning and copyright notices are not removed or altered.
+//   Copyright (c) 2004 by Amir Said (said@ieee.org) & William A. Pearlman (pearlw@ecse.rpi.edu)
+//
+//   The method is described in: Lossless Compression Handbook, ed. K. Sayood, Chapter 5: Arithmetic Coding
+//   (A. Said), pp. 101-152, Academic Press, 2003; and A. Said, Introduction to Arithmetic Coding - Theory and
+//   Practice, HP Labs report HPL-2004-76.
+
 #include "arith_coder.h"
 
 namespace mraygb

@@ -9,7 +9,9 @@
 //
 // The array is reached from the host through cudaGetSymbolAddress, once per device, with that device current
 // (the host-side name of a __device__ array is only a stand-in, not a device address).  The first call on a
-// device does that set-up.  All calls share the one array and the scan overwrites every word it reads, so no
+// device does that set-up and the address is kept for the process: it belongs to the device's primary context,
+// so it is not valid after cudaDeviceReset or under another driver context on the same device.  Each call reads
+// the compact size back and waits for its stream, so no call can be captured into a CUDA graph.  All calls share the one array and the scan overwrites every word it reads, so no
 // clearing is needed; two calls that overlap on the GPU (different streams, or different host threads on the
 // same device) race on the array and must be ordered by the caller.
 

@@ -45,8 +45,19 @@ cudaError_t launch_particle_sort(uint32_t n, uint32_t total, uint32_t *keys, uin
 cudaError_t launch_particle_gather(uint64_t n, const uint32_t *order, const float *x, const float *y, const float *z,
                                    const float *v, float4 *pts, cudaStream_t stream);
 
+// libm_trig_host.cpp: the device copy of the sinf / cosf exception table (libm_trig_core.h)
+struct LibmTrigTable
+{
+    const uint32_t *offsets; // n_buckets + 1
+    const uint16_t *entries;
+};
+// the table of the current device, uploaded on first use (thread safe)
+cudaError_t libm_trig_device_table(LibmTrigTable *out);
+
 // mese.cu
 cudaError_t mese_init_constants();
+// cosf / sinf of the MESE algebra (the host C library's results) over n floats
+cudaError_t launch_libm_sincosf(uint64_t n, const float *x, float *s, float *c, cudaStream_t stream);
 // determine_best_number_moments for every pixel whose count is non-zero (error threshold > 0)
 cudaError_t launch_count_moments(int num_pixels, int m, float error_threshold, const float *moments,
                                  uint32_t *counts, cudaStream_t stream);
@@ -54,12 +65,12 @@ cudaError_t launch_count_moments(int num_pixels, int m, float error_threshold, c
 cudaError_t launch_prediction_encode(int num_pixels, int m, const uint32_t *index, float *data, float bias,
                                      cudaStream_t stream);
 // mese_f64.cu: the FP64 preparation
-cudaError_t mese_f64_init_constants();
+cudaError_t mese_f64_init_constants(const LibmTrigTable &trig);
 cudaError_t launch_prepare_f64(int num_pixels, int m, const uint32_t *index, const float *data, int prediction_code,
                                int coding_warp, const uint16_t *coding_params, float bias, float *pmoments,
                                cudaStream_t stream);
 // mese_ff.cu: the float-float preparation
-cudaError_t mese_ff_init_constants();
+cudaError_t mese_ff_init_constants(const LibmTrigTable &trig);
 cudaError_t launch_prepare_ff(int num_pixels, int m, const uint32_t *index, const float *data, int prediction_code,
                               int coding_warp, const uint16_t *coding_params, float bias, float *pmoments,
                               cudaStream_t stream);
@@ -122,6 +133,7 @@ cudaError_t launch_reference_particles(const ParticleView &parts, const Referenc
                                        cudaStream_t stream);
 
 // quant_curve.cu: the data-dependent quantization table's error means for every (index, bits) pair
+cudaError_t quant_curve_init_constants(const LibmTrigTable &trig);
 // scratch bytes for an sx x sy sample, bits bmin .. bmin + nb - 1, rows_per_pass moment indices per pass
 size_t quant_curve_scratch_bytes(int sx, int sy, int m, int nb, size_t rows_per_pass);
 // d_means[(idx - 1) * nb + (b - bmin)] for idx in [1, m): the mean rRMSE of quantizing moment idx to b bits

@@ -139,6 +139,18 @@ __global__ void __launch_bounds__(BLOCK) prediction_encode_kernel(int num_pixels
         d[l] = cmulc((cx<float>)code[l], inv_axis).x;
 }
 
+__global__ void libm_sincosf_kernel(uint64_t n, const float *__restrict__ x, float *__restrict__ s,
+                                    float *__restrict__ c)
+{
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    {
+        float sv, cv;
+        libm_sincosf(x[i], &sv, &cv);
+        s[i] = sv;
+        c[i] = cv;
+    }
+}
+
 template <int MAXM>
 cudaError_t launch_count_t(int num_pixels, int m, float thr, const float *moments, uint32_t *counts,
                            cudaStream_t stream)
@@ -174,12 +186,28 @@ cudaError_t launch_encode_t(int num_pixels, int m, const uint32_t *index, float 
 
 cudaError_t mese_init_constants()
 {
-    cudaError_t e = init_tables();
+    LibmTrigTable trig;
+    cudaError_t e = libm_trig_device_table(&trig);
     if (e != cudaSuccess)
         return e;
-    if ((e = mese_ff_init_constants()) != cudaSuccess)
+    if ((e = init_tables()) != cudaSuccess)
         return e;
-    return mese_f64_init_constants();
+    if ((e = set_libm_trig_constants(trig)) != cudaSuccess)
+        return e;
+    if ((e = mese_ff_init_constants(trig)) != cudaSuccess)
+        return e;
+    if ((e = quant_curve_init_constants(trig)) != cudaSuccess)
+        return e;
+    return mese_f64_init_constants(trig);
+}
+
+cudaError_t launch_libm_sincosf(uint64_t n, const float *x, float *s, float *c, cudaStream_t stream)
+{
+    if (n == 0)
+        return cudaSuccess;
+    const uint64_t blocks = (n + 255) / 256;
+    libm_sincosf_kernel<<<(unsigned)(blocks < 152 * 16 ? blocks : 152 * 16), 256, 0, stream>>>(n, x, s, c);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_count_moments(int num_pixels, int m, float thr, const float *moments, uint32_t *counts,

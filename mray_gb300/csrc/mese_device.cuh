@@ -1,9 +1,9 @@
 // Per-pixel bounded-MESE algebra on the device, generic over float / double and over the array type.
 //
 // The float instantiation performs the reference's operations in the reference's order (these kernels are
-// compiled without FMA contraction), so its results differ from the reference's CPU build only where CUDA's
-// cosf / sinf round differently from the C library's.  The double instantiation is the same method in FP64
-// with exact constants (the precision form).
+// compiled without FMA contraction), and its cosf / sinf return the host C library's results
+// (libm_trig_core.h), so its results equal the reference's CPU build bit for bit.  The double instantiation is
+// the same method in FP64 with exact constants (the precision form).
 //
 // Arrays are accessed through an index operator only: the kernels pass thread-strided views of shared memory
 // (element k of thread t at k * BLOCK + t, so a warp reading element k touches 32 consecutive words).
@@ -21,6 +21,8 @@
 #pragma once
 
 #include <cuda_runtime.h>
+
+#include "libm_trig.cuh"
 
 namespace mraygb
 {
@@ -59,7 +61,7 @@ template <> struct MeseConst<double>
     static constexpr double rrmse_tie = 1e-8;
 };
 
-__device__ __forceinline__ void dsincos(float x, float *s, float *c) { sincosf(x, s, c); }
+__device__ __forceinline__ void dsincos(float x, float *s, float *c) { libm_sincosf(x, s, c); }
 __device__ __forceinline__ void dsincos(double x, double *s, double *c) { sincos(x, s, c); }
 __device__ __forceinline__ float dsqrt(float x) { return sqrtf(x); }
 __device__ __forceinline__ double dsqrt(double x) { return sqrt(x); }

@@ -5,7 +5,11 @@
 namespace mraygb
 {
 
-cudaError_t mese_f64_init_constants() { return init_tables(); }
+cudaError_t mese_f64_init_constants(const LibmTrigTable &trig)
+{
+    cudaError_t e = set_libm_trig_constants(trig);
+    return e != cudaSuccess ? e : init_tables();
+}
 
 cudaError_t launch_prepare_f64(int num_pixels, int m, const uint32_t *index, const float *data, int prediction_code,
                                int coding_warp, const uint16_t *coding_params, float bias, float *pmoments,

@@ -503,8 +503,11 @@ cudaError_t launch_ff_m(int num_pixels, int m, const uint32_t *index, const floa
 
 } // namespace
 
-cudaError_t mese_ff_init_constants()
+cudaError_t mese_ff_init_constants(const LibmTrigTable &trig)
 {
+    cudaError_t e = set_libm_trig_constants(trig);
+    if (e != cudaSuccess)
+        return e;
     float2 t[256];
     t[0] = make_float2(0.f, 0.f);
     for (int l = 1; l < 256; ++l)

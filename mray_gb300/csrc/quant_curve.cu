@@ -19,8 +19,8 @@
 // The search itself (a few hundred comparisons) then runs on the host over the table of means.
 //
 // The per-pixel arithmetic is the reference CPU build's, operation for operation (this file is compiled without
-// FMA contraction; divisions and square roots are IEEE-rounded, cos / sin / atan2 correctly rounded): the results
-// differ from it only where the C library's cosf / sinf do not round correctly.  The reference's CUDA build sums the errors with
+// FMA contraction; divisions and square roots are IEEE-rounded, cosf / sinf return the C library's results
+// (libm_trig_core.h), atan2 is the double function rounded to float).  The reference's CUDA build sums the errors with
 // thrust::reduce (a different order) over a count that leaves out the last pixel when it is non-empty
 // (exclusive scan, measure_coding_error.cu:190-197); the CPU build's sequential mean over every non-empty pixel
 // is the one followed here.
@@ -68,17 +68,14 @@ template <int MAXM> __device__ __forceinline__ void load_params(const QcArgs &a,
 
 // transform_dequantization_real (moment_prediction_coding.h:97-118) for code 0: the first code and the factor
 // that maps every later real residual onto the axis perpendicular to it (the operations of pc_dequant_real).
-// The reference's cosf / sinf come from the C library, which rounds correctly on all but a few percent of these
-// arguments; the rRMSE is a difference of nearly equal moments, so one ulp in the first code moves a pixel's error
-// by up to ~1e-2 relative at 16 bits.  The correctly rounded values (the double functions rounded to float; one
-// call per pixel) keep the device on the library's results wherever the library rounds correctly.
+// The rRMSE is a difference of nearly equal moments, so one ulp in the first code moves a pixel's error by up to
+// ~1e-2 relative at 16 bits: cosf / sinf must return the C library's results (libm_sincosf).
 __device__ __forceinline__ void dequant_head(float c0, cx<float> &code0, cx<float> &factor)
 {
     using K = MeseConst<float>;
     const float phase = K::pi * c0 - K::half_pi;
-    double sd, cd;
-    sincos((double)phase, &sd, &cd);
-    const float s = (float)sd, c = (float)cd;
+    float s, c;
+    libm_sincosf(phase, &s, &c);
     code0 = cscale(2.f * K::inv_4pi, mk(c, s));
     const cx<float> axis = mk(-code0.y, code0.x);
     const float len = dsqrt(cabs2(axis));
@@ -300,6 +297,8 @@ cudaError_t run_curve(const QcArgs &base, size_t rows_per_pass, cudaStream_t str
 }
 
 } // namespace
+
+cudaError_t quant_curve_init_constants(const LibmTrigTable &trig) { return set_libm_trig_constants(trig); }
 
 size_t quant_curve_scratch_bytes(int sx, int sy, int m, int nb, size_t rows_per_pass)
 {

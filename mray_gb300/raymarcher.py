@@ -585,6 +585,10 @@ class Context:
                                                  _dptr(index), _dptr(compact), int(capacity), C.byref(total)))
         return int(total.value)
 
+    def stage_libm_sincosf(self, x, s, c):
+        """cosf / sinf of the MESE algebra on device float32 tensors (the host C library's results on [-pi, pi])."""
+        self._check(self._L.mraygb_stage_libm_sincosf(self._h, _dptr(x), _dptr(s), _dptr(c), int(x.numel())))
+
     def stage_prediction_encode(self, width, height, num_moments, index, data, data_size, coding_warp=0,
                                 bias=1e-4, coding_params=None):
         self._check(self._L.mraygb_stage_prediction_encode(self._h, width, height, num_moments, _dptr(index),

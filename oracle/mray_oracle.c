@@ -452,6 +452,17 @@ void oracle_preintegrate(const float *tf1d, float step_size, float *table)
     }
 }
 
+/* cosf / sinf of trigonometricToExponentialMoments (mese/MESE_dynamic.h:38-40): the C library's */
+void oracle_libm_sincosf(uint64_t n, const float *x, float *s, float *c)
+{
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < (int64_t)n; ++i)
+    {
+        c[i] = cosf(x[i]);
+        s[i] = sinf(x[i]);
+    }
+}
+
 /* ColorImageHost::set_color / rgba8_t (color_image.h:41-47, 60-65) */
 void oracle_rgba_to_u8(uint64_t num_pixels, const float *rgba, uint8_t *out)
 {

@@ -129,6 +129,8 @@ typedef struct oracle_options
     void oracle_transform_dequantization_real_##SFX(int n, const R *in, R *code, int warp, const R *params);      \
     /* moment compaction (moment_compaction.h)                                                                 */   \
     int oracle_determine_best_number_moments_##SFX(int n, const R *moments, R error_threshold);                  \
+    void oracle_count_moments_##SFX(int num_pixels, int m, const R *moments, const uint32_t *counts_in,          \
+                                    R error_threshold, uint32_t *counts_out, int nthreads);                        \
     void oracle_evaluate_unknown_moments_##SFX(int n, const R *exp_in, int max_moments, R *new_exp);              \
     void oracle_exponential_to_bounded_moments_##SFX(int n, const R *exp_in, R *bounded, int known);             \
     R oracle_rmse_##SFX(int n, int m, const R *pred /* complex */, const R *target);                              \
@@ -219,6 +221,10 @@ void oracle_preintegrate(const float *tf1d, float step_size, float *table);
 
 /* ColorImageHost::set_color: clamp and truncate to u8 (color_image.h:41-47, 60-65). */
 void oracle_rgba_to_u8(uint64_t num_pixels, const float *rgba, uint8_t *out);
+
+/* The C library's cosf / sinf over n floats (OpenMP), as trigonometricToExponentialMoments calls them
+ * (mese/MESE_dynamic.h:38-40). */
+void oracle_libm_sincosf(uint64_t n, const float *x, float *s, float *c);
 
 /* euler_exp as the reference's CPU build resolves it (complex_algebra.h:155-158). */
 void oracle_euler_exp_f32(float x, float out[2]);

@@ -44,9 +44,11 @@ def build(force: bool = False) -> None:
 
 
 def build_ref() -> bool:
-    """Compile the reference's own CPU path into oracle/_ref (only where the reference sources exist)."""
-    src = os.environ.get("MRAY_REFERENCE_SRC", "/root/reference/src")
-    if not os.path.isdir(src):
+    """Compile the reference's own CPU path into oracle/_ref (only where the reference sources were staged)."""
+    from stage_reference import reference_src
+
+    src = reference_src()
+    if src is None:
         return False
     subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={src}"], check=True)
     return os.path.exists(REF_LIB_PATH)
@@ -116,6 +118,9 @@ def _declare(L):
         getattr(L, f"oracle_fast_atan_{sfx}").argtypes = [R]
         getattr(L, f"oracle_determine_best_number_moments_{sfx}").argtypes = [C.c_int, C.c_void_p, R]
         getattr(L, f"oracle_determine_best_number_moments_{sfx}").restype = C.c_int
+        getattr(L, f"oracle_count_moments_{sfx}").argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, R,
+                                                              C.c_void_p, C.c_int]
+        getattr(L, f"oracle_count_moments_{sfx}").restype = None
         getattr(L, f"oracle_rmse_{sfx}").argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p]
         getattr(L, f"oracle_rmse_{sfx}").restype = R
         getattr(L, f"oracle_transform_quantization_real_{sfx}").argtypes = [C.c_int, C.c_void_p, R, C.c_void_p]
@@ -169,6 +174,8 @@ def _declare(L):
         getattr(L, f"oracle_generate_reference_{sfx}").argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                                                    C.c_int, C.c_int, C.c_void_p, C.c_void_p,
                                                                    C.c_void_p]
+    L.oracle_libm_sincosf.argtypes = [C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.oracle_libm_sincosf.restype = None
     L.oracle_set_rounded_trig.argtypes = [C.c_int]
     L.oracle_set_rounded_trig.restype = None
     L.oracle_sample_moment_image.restype = C.c_uint64
@@ -291,6 +298,28 @@ def prediction_encode(width, height, m, index, data, coding_warp=0, bias=1e-4, n
     return d, cp[:2 * (m - 1)]
 
 
+def count_moments(moments, counts_in, error_threshold, precision="f32", nthreads=0):
+    """compute_num_moments with an error threshold: per pixel of moments[H, W, m] (or [P, m]) whose counts_in is
+    non-zero, determine_best_number_moments; returns u32 counts."""
+    L = lib()
+    m = moments.shape[-1]
+    mo = np.ascontiguousarray(moments, dtype=_dt(precision)).reshape(-1, m)
+    cin = np.ascontiguousarray(counts_in, dtype=np.uint32).reshape(-1)
+    out = np.zeros(mo.shape[0], dtype=np.uint32)
+    getattr(L, f"oracle_count_moments_{precision}")(mo.shape[0], m, _ptr(mo), _ptr(cin), error_threshold,
+                                                     _ptr(out), nthreads)
+    return out
+
+
+def libm_sincosf(x):
+    """The C library's (sinf(x), cosf(x)) for a float32 array."""
+    xs = np.ascontiguousarray(x, dtype=np.float32)
+    s = np.empty_like(xs)
+    c = np.empty_like(xs)
+    lib().oracle_libm_sincosf(xs.size, _ptr(xs), _ptr(s), _ptr(c))
+    return s, c
+
+
 def find_coding_transform_parameters(width, height, m, index, data):
     L = lib()
     d = np.ascontiguousarray(data, dtype=np.float32)
@@ -355,6 +384,31 @@ def dequantize_prediction_coding(width, height, m, index, table, packed, size):
                                           _ptr(np.ascontiguousarray(table, dtype=np.uint8)), _ptr(b), b.size,
                                           _ptr(out))
     return out[:size]
+
+
+def unpack_codes(width, height, m, index, table, packed):
+    """The integer codes of a packed prediction-coding stream (pack_bits, moment_quantization.cpp:92-114: LSB-first,
+    pixels in row-major order, moment index ascending), one per stored moment; -1 for a code cut off by the
+    dropped trailing partial byte."""
+    idx = np.asarray(index, dtype=np.int64)
+    counts = np.diff(idx)
+    tab = np.asarray(table, dtype=np.int64)
+    total = int(idx[-1])
+    starts = np.repeat(idx[:-1], counts)
+    l = np.arange(total, dtype=np.int64) - starts
+    widths = tab[l]
+    offs = np.zeros(total, dtype=np.int64)
+    if total:
+        offs[1:] = np.cumsum(widths)[:-1]
+    bits = np.unpackbits(np.asarray(packed, dtype=np.uint8), bitorder="little").astype(np.int64)
+    nbits = bits.size
+    codes = np.zeros(total, dtype=np.int64)
+    for k in range(int(tab.max()) if total else 0):
+        pos = offs + k
+        take = (k < widths) & (pos < nbits)
+        codes[take] |= bits[pos[take]] << k
+    codes[offs + widths > nbits] = -1
+    return codes
 
 
 def default_quantization_table(m, bits):

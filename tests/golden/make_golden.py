@@ -1,7 +1,7 @@
 """Writes the golden fixtures of tests/golden/ from the reference's OWN CPU implementation.
 
-The reference (TobiasRp/mray) is compiled from its sources by oracle/Makefile (`make ref`, sources under
-/root/reference/src) into oracle/_ref/libmrayref.so together with a small C-ABI harness.  This script calls it
+The reference (TobiasRp/mray) is compiled from its sources by oracle/Makefile (`make ref`, sources staged by
+oracle/stage_reference.py) into oracle/_ref/libmrayref.so together with a small C-ABI harness.  This script calls it
 on seeded inputs and stores inputs and outputs as small .npz files:
 
   known_answers.npz   the inputs of the reference's own unit tests (tests/test_mese.cpp, test_prediction_coding.cpp,

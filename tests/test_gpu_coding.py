@@ -1,7 +1,9 @@
 """GPU prediction coding, coding parameters, quantization and bit packing against the oracle.
 
-Bar: codes and packed bytes bit-identical to the reference's packer for the same prediction-coded floats;
-coding parameters (u16) identical; the encoded floats within 1e-5 absolute (only cosf / sinf rounding differs).
+Bar: from the same input moments, the prediction-coded floats, the u16 coding parameters, the 10-bit codes and
+the packed bytes are bit-identical to the reference's CPU arithmetic (the device performs its float operations in
+its order and takes cosf / sinf with the C library's results).  From the same volume, the moments themselves
+differ from the reference's in their last bits, so the end-to-end code mismatch is measured and bounded.
 """
 import numpy as np
 import pytest
@@ -49,16 +51,19 @@ def test_prediction_encode_matches_oracle(gpu_context, warp, ragged_seed):
     bias = 5e-5
     ours, cp = _encode_gpu(gpu_context, W, H, m, index, data, warp, bias)
     ref, cp_ref = O.prediction_encode(W, H, m, index, data, warp, bias)
-    assert np.abs(ours.astype(np.float64) - ref).max() <= 1e-5
+    # the encoded (and, with the default warp, warped) floats: bit for bit
+    assert np.array_equal(ours.view(np.uint32), ref.view(np.uint32)), \
+        f"{int((ours.view(np.uint32) != ref.view(np.uint32)).sum())} of {ref.size} floats differ"
     if warp == 0:
-        # the parameters come from exact min / max reductions of the encoded residuals
-        assert np.abs(cp.astype(int) - cp_ref.astype(int)).max() <= 1
-        assert np.mean(cp == cp_ref) >= 0.9
-    # 10-bit codes of the two encodings: differences only where a float sits on a code boundary
+        assert np.array_equal(cp, cp_ref)
+    # the 10-bit codes packed by the GPU equal the reference packer's codes of the reference's floats
     table = O.default_quantization_table(m, 10)
-    a = O.quantize_prediction_coding(W, H, m, index, ours, table)
+    d_out = torch.zeros(ours.size * 4 + 16, dtype=torch.uint8, device="cuda")
+    n = gpu_context.stage_quantize_prediction_coding(W, H, m, _dev(index.view(np.int32)), _dev(ours), table, d_out)
+    gpu_context.synchronize()
     b = O.quantize_prediction_coding(W, H, m, index, ref, table)
-    assert a.size == b.size
+    assert n == b.size
+    assert np.array_equal(d_out.cpu().numpy()[:n], b)
 
 
 TABLES = {
@@ -137,14 +142,18 @@ def test_dropin_generate_prediction_coded_then_reconstruct(gpu_context, warp):
         assert np.abs(mi.coding_params.astype(int) - ref["coding_params"].astype(int)).max() <= 1
     # the encoding amplifies the moments' last-bit differences (the reference's FP32 rounding) by the
     # prediction coding's Levinson recursion; with the same input moments it is the reference's arithmetic
-    # (test_prediction_encode_matches_oracle)
+    # bit for bit (test_prediction_encode_matches_oracle)
     assert np.abs(mi.data.astype(np.float64) - ref["data"]).max() <= 2e-3
     table = M.default_quantization_table(wl.num_moments, 10)
     codes = M.quantize_prediction_coding(mi, table, context=gpu_context)
     codes_ref = O.quantize_prediction_coding(wl.width, wl.height, wl.num_moments, ref["index"], ref["data"], table)
     assert codes.size == codes_ref.size
-    # end-to-end byte agreement of the packed 10-bit codes
-    assert np.mean(codes == codes_ref) >= 0.98
+    # end to end (volume -> codes): the fraction of 10-bit codes that differ
+    a = O.unpack_codes(wl.width, wl.height, wl.num_moments, ref["index"], table, codes)
+    b = O.unpack_codes(wl.width, wl.height, wl.num_moments, ref["index"], table, codes_ref)
+    frac = float(np.mean(a != b))
+    print(f"end-to-end 10-bit code mismatch (warp {warp}): {frac:.4%} of {a.size} codes")
+    assert frac <= 0.02
     # reconstruct from the prediction-coded image (prepare_moments_from_pred_coding)
     tf = M.preintegrate(wl.tf1d, wl.tf_step)
     img = M.ColorImageHost(wl.width, wl.height)
@@ -182,5 +191,5 @@ def test_prepare_from_prediction_coding_same_input(gpu_context):
     rgba_ref = O.reconstruct(wl.camera, wl.rec, W, H, m, wl.domain_min, wl.domain_max, ref["index"], pm_ref,
                              ref["bounds"], tf, "f32")
     assert np.abs(rgba - rgba_ref).max() <= 1e-3
-    # the multipliers themselves: only cosf / sinf rounding differs from the reference's arithmetic
-    assert np.abs(pm - pm_ref).max() <= 1e-4 * max(1.0, float(np.abs(pm_ref).max()))
+    # the multipliers themselves: the reference's arithmetic, bit for bit
+    assert np.array_equal(pm.view(np.uint32), pm_ref.view(np.uint32))

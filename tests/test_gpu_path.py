@@ -169,11 +169,13 @@ def test_prepare_and_reconstruct_from_same_moments(gpu_context, case):
     # two FP32 evaluations of an ill-conditioned series can land on either side of each other by chance (the
     # 64-moment mixing layer: multipliers of 1e4..1e6 that cancel)
     assert ok.mean() >= (0.998 if m <= 31 else 0.995), f"{(~ok).sum()} pixels neither within 1e-3 of the reference nor closer to FP64"
-    # 2. the multipliers: the reference's arithmetic, so only cosf / sinf rounding differs
+    # 2. the multipliers: the reference's arithmetic operation by operation, bit for bit
     gpu_context.stage_reconstruct(wl.camera, wl.rec, W, H, m, wl.domain_min, wl.domain_max, d_idx, d_pm, d_b, d_rgba)
     gpu_context.synchronize()
     rgba2 = d_rgba.cpu().numpy().reshape(H, W, 4)
     pm = d_pm.cpu().numpy()
+    assert np.array_equal(pm.view(np.uint32), pm_ref.view(np.uint32)), \
+        f"{int((pm.view(np.uint32) != pm_ref.view(np.uint32)).sum())} of {pm.size} multipliers differ"
     ok2 = rgba_agreement(rgba2, oracle_march(pm, "f32"), oracle_march(pm, "f64"), RGBA_TOL)
     assert ok2.mean() >= (0.998 if m <= 31 else 0.995), f"{(~ok2).sum()} pixels"
     if m <= 31:

@@ -1,16 +1,18 @@
 """The reference-side shims (mray_gb300/shim/) compile against the reference's own headers: the drop-in seams
-type-check.  Runs only where the reference sources are present."""
+type-check.  Runs only where the reference sources were staged (oracle/stage_reference.py)."""
 import os
 import shutil
 import subprocess
 
 import pytest
 
+from stage_reference import reference_src
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = "/root/reference/src"
+REF = reference_src()
 
 
-@pytest.mark.skipif(not os.path.isdir(REF), reason="reference sources not present")
+@pytest.mark.skipif(REF is None, reason="reference sources not staged")
 @pytest.mark.parametrize("shim", ["moment_raymarcher_gb300.cpp", "moment_image_io_gb300.cpp"])
 def test_shim_compiles_against_reference_headers(tmp_path, shim):
     cuda_inc = "/usr/local/cuda/include"
