@@ -82,6 +82,10 @@ int mraygb_synchronize(mraygb_context *ctx);
 int mraygb_set_precision(mraygb_context *ctx, int precision);
 /* Number of this library's kernels launched by the context so far. */
 uint64_t mraygb_kernel_launches(const mraygb_context *ctx);
+/* The FP32 roof the marching kernels are measured against: the rate of a chain of fused multiply-adds with no
+ * memory traffic on every SM of the context's device (two launches of about 10 ms on the context's stream, the
+ * second timed with CUDA events), in TFLOP/s (an FMA counts as two).  No counterpart in the reference. */
+int mraygb_measure_fp32_rate(mraygb_context *ctx, double *h_tflops);
 
 /* ---- resident inputs ------------------------------------------------------------------------------------ */
 
@@ -140,6 +144,14 @@ int mraygb_reconstruct(mraygb_context *ctx, const mraygb_camera *cam, const mray
 int mraygb_quantize_prediction_coding(mraygb_context *ctx, int width, int height, int num_moments,
                                       const uint32_t *h_index, const float *h_data, uint64_t data_size,
                                       const uint8_t *h_table, uint8_t *h_out, uint64_t capacity, uint64_t *h_nbytes);
+
+/* dequantize_prediction_coding (src/moment_quantization.cpp:278-332 with unpack_bits :116-152) for a compact image
+ * in host memory: the packed codes (num_bytes, as the quantizer wrote them) back to values in [0, 1], written to
+ * h_data (data_size = index[W*H] floats), which the reconstruction then reads as the prediction-coded moments
+ * (load_moment_image does this for a quantized file, src/moment_image_io.cpp). */
+int mraygb_dequantize_prediction_coding(mraygb_context *ctx, int width, int height, int num_moments,
+                                        const uint32_t *h_index, const uint8_t *h_table, const uint8_t *h_bytes,
+                                        uint64_t num_bytes, float *h_data, uint64_t data_size);
 
 /* create_quantization_table (src/measure_coding_error.cpp:374-438) as main.cpp:318-327 runs it before the codes
  * are written: on the sample_moment_image (src/moment_image_sample.h:33-62) of a compact, prediction-coded

@@ -34,7 +34,8 @@ EXPORTS = [
     "mraygb_generate_reference_reconstructed_ss", "mraygb_stage_generate_reference_reconstructed_ss",
     "mraygb_encode_moment_image", "mraygb_copy_encoded", "mraygb_decode_moment_image", "mraygb_write_moment_image",
     "mraygb_load_moment_image", "mraygb_lz4_compress", "mraygb_lz4_decompress", "mraygb_entropy_encode",
-    "mraygb_entropy_decode", "mraygb_stage_libm_sincosf",
+    "mraygb_entropy_decode", "mraygb_stage_libm_sincosf", "mraygb_dequantize_prediction_coding",
+    "mraygb_measure_fp32_rate",
 ]
 
 _lock = threading.Lock()
@@ -77,6 +78,8 @@ def _declare(L):
                                            C.c_float * 3, vp, vp, vp, vp, vp]
     u64 = C.c_uint64
     L.mraygb_quantize_prediction_coding.argtypes = [vp, i, i, i, vp, vp, u64, vp, vp, u64, P(u64)]
+    L.mraygb_dequantize_prediction_coding.argtypes = [vp, i, i, i, vp, vp, vp, u64, vp, u64]
+    L.mraygb_measure_fp32_rate.argtypes = [vp, P(C.c_double)]
     L.mraygb_stage_libm_sincosf.argtypes = [vp, vp, vp, vp, u64]
     L.mraygb_stage_prediction_encode.argtypes = [vp, i, i, i, vp, vp, u64, i, C.c_float, vp]
     L.mraygb_stage_quantize_prediction_coding.argtypes = [vp, i, i, i, vp, vp, vp, vp, u64, P(u64)]

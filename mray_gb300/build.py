@@ -43,6 +43,7 @@ SOURCES = [
     ("arith_coder.cpp", ["-Xcompiler", "-ffp-contract=off"]),
     ("moment_file.cpp", []),
     ("libm_trig_host.cpp", []),
+    ("fp32_rate.cu", []),
     ("api.cpp", ["-x", "cu"]),
 ]
 

@@ -1033,6 +1033,19 @@ int mraygb_stage_reconstruct(mraygb_context *ctx, const mraygb_camera *cam, cons
                            d_rgba, d_rgba8);
 }
 
+int mraygb_measure_fp32_rate(mraygb_context *ctx, double *h_tflops)
+{
+    CHECK_CTX();
+    if (!h_tflops)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "NULL argument");
+    int sms = 0;
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device), "cudaDeviceGetAttribute");
+    CK(ctx->pmoments.reserve(fp32_rate_scratch_floats(sms) * sizeof(float)), "scratch allocation");
+    CK(measure_fp32_rate(sms, ctx->stream, ctx->pmoments.as<float>(), h_tflops), "FP32 rate kernel");
+    ctx->launches += 2;
+    return MRAYGB_OK;
+}
+
 int mraygb_stage_libm_sincosf(mraygb_context *ctx, const float *d_x, float *d_sin, float *d_cos, uint64_t n)
 {
     CHECK_CTX();
@@ -1312,6 +1325,39 @@ int mraygb_quantize_prediction_coding(mraygb_context *ctx, int width, int height
         if (nbytes)
             CK(cudaMemcpyAsync(h_out, ctx->packed.ptr, nbytes, cudaMemcpyDeviceToHost, ctx->stream), "packed download");
     }
+    CK(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+    return MRAYGB_OK;
+}
+
+int mraygb_dequantize_prediction_coding(mraygb_context *ctx, int width, int height, int m, const uint32_t *h_index,
+                                        const uint8_t *h_table, const uint8_t *h_bytes, uint64_t num_bytes,
+                                        float *h_data, uint64_t data_size)
+{
+    CHECK_CTX();
+    int rc = check_image(ctx, width, height, m);
+    if (rc)
+        return rc;
+    if (!h_index || !h_table || (!h_bytes && num_bytes) || (!h_data && data_size))
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "NULL argument");
+    const size_t P = (size_t)width * (size_t)height;
+    if ((uint64_t)h_index[P] != data_size)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "data_size %llu differs from the index's total %u",
+                    (unsigned long long)data_size, h_index[P]);
+    CK(ctx->index.reserve((P + 1) * sizeof(uint32_t)), "index buffer allocation");
+    CK(ctx->compact.reserve((data_size ? data_size : 1) * sizeof(float)), "moment buffer allocation");
+    CK(ctx->packed.reserve(num_bytes ? num_bytes : 1), "packed buffer allocation");
+    CK(cudaMemcpyAsync(ctx->index.ptr, h_index, (P + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->stream),
+       "index upload");
+    if (num_bytes)
+        CK(cudaMemcpyAsync(ctx->packed.ptr, h_bytes, num_bytes, cudaMemcpyHostToDevice, ctx->stream),
+           "packed upload");
+    if ((rc = mraygb_stage_dequantize_prediction_coding(ctx, width, height, m, ctx->index.as<uint32_t>(), h_table,
+                                                        ctx->packed.as<uint8_t>(), num_bytes,
+                                                        ctx->compact.as<float>())))
+        return rc;
+    if (data_size)
+        CK(cudaMemcpyAsync(h_data, ctx->compact.ptr, data_size * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream),
+           "moment download");
     CK(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
     return MRAYGB_OK;
 }

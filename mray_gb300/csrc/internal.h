@@ -54,6 +54,10 @@ struct LibmTrigTable
 // the table of the current device, uploaded on first use (thread safe)
 cudaError_t libm_trig_device_table(LibmTrigTable *out);
 
+// fp32_rate.cu: the measured FP32 FMA rate (TFLOP/s) of the current device
+size_t fp32_rate_scratch_floats(int sm_count);
+cudaError_t measure_fp32_rate(int sm_count, cudaStream_t stream, float *scratch, double *tflops);
+
 // mese.cu
 cudaError_t mese_init_constants();
 // cosf / sinf of the MESE algebra (the host C library's results) over n floats

@@ -514,15 +514,34 @@ class Context:
             raise ValueError("the quantization table needs one entry per moment index")
         data = np.ascontiguousarray(mi.data, dtype=np.float32)
         index = np.ascontiguousarray(mi.index, dtype=np.uint32)
+        # the packed size from the counts: whole bytes of sum_p sum_{l < n_p} table[l]
+        cum = np.concatenate([[0], np.cumsum(t[:mi.num_moments].astype(np.int64))])
+        nbytes = int(cum[np.diff(index.astype(np.int64))].sum()) // 8
+        out = np.empty(max(nbytes, 1), dtype=np.uint8)
         n = C.c_uint64()
-        self._check(self._L.mraygb_quantize_prediction_coding(self._h, mi.width, mi.height, mi.num_moments,
-                                                              _hptr(index), _hptr(data), data.size, _hptr(t), None,
-                                                              0, C.byref(n)))
-        out = np.zeros(max(n.value, 1), dtype=np.uint8)
         self._check(self._L.mraygb_quantize_prediction_coding(self._h, mi.width, mi.height, mi.num_moments,
                                                               _hptr(index), _hptr(data), data.size, _hptr(t),
                                                               _hptr(out), out.size, C.byref(n)))
         return out[:n.value]
+
+    def dequantize_prediction_coding(self, mi: MomentImageHost, table, qs) -> None:
+        """dequantize_prediction_coding(mi, table, qs) (moment_quantization.cpp:278-332): the codes back into
+        mi.data (values in [0, 1]; the image keeps its index and coding parameters)."""
+        if not mi.is_compact:
+            raise ValueError("dequantize_prediction_coding needs a compact moment image")
+        t = np.ascontiguousarray(table, dtype=np.uint8)
+        if t.size < mi.num_moments:
+            raise ValueError("the quantization table needs one entry per moment index")
+        index = np.ascontiguousarray(mi.index, dtype=np.uint32)
+        q = np.ascontiguousarray(qs, dtype=np.uint8)
+        size = int(index[-1])
+        data = mi.data if (isinstance(mi.data, np.ndarray) and mi.data.dtype == np.float32 and mi.data.size >= size
+                           and mi.data.flags.c_contiguous) else np.empty(size, dtype=np.float32)
+        data = data[:size]
+        self._check(self._L.mraygb_dequantize_prediction_coding(self._h, mi.width, mi.height, mi.num_moments,
+                                                                _hptr(index), _hptr(t), _hptr(q), q.size,
+                                                                _hptr(data), size))
+        mi.data = data
 
     def create_quantization_table(self, mi: MomentImageHost, start_bits: int, sampling: int = 0,
                                   return_means: bool = False):
@@ -584,6 +603,12 @@ class Context:
         self._check(self._L.mraygb_stage_compact(self._h, width, height, num_moments, _dptr(counts), _dptr(moments),
                                                  _dptr(index), _dptr(compact), int(capacity), C.byref(total)))
         return int(total.value)
+
+    def measure_fp32_rate(self) -> float:
+        """The FP32 FMA roof of the device in TFLOP/s (mraygb_measure_fp32_rate)."""
+        v = C.c_double()
+        self._check(self._L.mraygb_measure_fp32_rate(self._h, C.byref(v)))
+        return float(v.value)
 
     def stage_libm_sincosf(self, x, s, c):
         """cosf / sinf of the MESE algebra on device float32 tensors (the host C library's results on [-pi, pi])."""
@@ -759,6 +784,11 @@ def generate(cam: Camera, volume, mi: MomentImageHost, params: GenerationParamet
 def quantize_prediction_coding(mi: MomentImageHost, table, context: Optional[Context] = None) -> np.ndarray:
     """moment_quantization::quantize_prediction_coding(mi, table) on the GPU."""
     return (context or default_context()).quantize_prediction_coding(mi, table)
+
+
+def dequantize_prediction_coding(mi: MomentImageHost, table, qs, context: Optional[Context] = None) -> None:
+    """moment_quantization::dequantize_prediction_coding(mi, table, qs) on the GPU (into mi.data)."""
+    (context or default_context()).dequantize_prediction_coding(mi, table, qs)
 
 
 def create_quantization_table(img: MomentImageHost, start_bits: int, context: Optional[Context] = None,

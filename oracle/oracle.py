@@ -17,10 +17,12 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 REF_LIB_PATH = os.path.join(HERE, "_ref", "libmrayref.so")
+REF_REL_LIB_PATH = os.path.join(HERE, "_ref", "libmrayref_release.so")
 
 _lock = threading.Lock()
 _lib = None
 _ref = None
+_ref_rel = None
 
 fp = np.ctypeslib.ndpointer
 
@@ -50,7 +52,8 @@ def build_ref() -> bool:
     src = reference_src()
     if src is None:
         return False
-    subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={src}"], check=True)
+    jobs = str(min(16, os.cpu_count() or 1))
+    subprocess.run(["make", "-s", "-j", jobs, "-C", HERE, "ref", "refrel", f"REF={src}"], check=True)
     return os.path.exists(REF_LIB_PATH)
 
 
@@ -73,6 +76,61 @@ def ref_lib():
                 return None
             _ref = C.CDLL(REF_LIB_PATH)
         return _ref
+
+
+def ref_release_lib():
+    """The reference's own CPU code built with its Release flags (timing only), or None where it cannot be built."""
+    global _ref_rel
+    with _lock:
+        if _ref_rel is None:
+            if not os.path.exists(REF_REL_LIB_PATH) and not build_ref():
+                return None
+            if not os.path.exists(REF_REL_LIB_PATH):
+                return None
+            L = C.CDLL(REF_REL_LIB_PATH)
+            from mray_gb300.types import Camera, GenerationParameters, ReconstructionParameters
+
+            L.ref_grid_create.restype = C.c_void_p
+            L.ref_grid_create.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+            L.ref_grid_destroy.argtypes = [C.c_void_p]
+            L.ref_grid_destroy.restype = None
+            L.ref_pipeline_rows.restype = C.c_int64
+            L.ref_pipeline_rows.argtypes = [C.c_void_p, C.POINTER(Camera), C.POINTER(GenerationParameters),
+                                            C.POINTER(ReconstructionParameters), C.c_int, C.c_int, C.c_int, C.c_int,
+                                            C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+            _ref_rel = L
+        return _ref_rel
+
+
+class RefPipeline:
+    """The reference's own generate -> compaction -> prediction coding -> quantize / dequantize -> reconstruct flow
+    (Release build) over row samples of an image, on a grid held between calls (timing of the CPU baseline)."""
+
+    def __init__(self, volume, dmin, dmax):
+        self.L = ref_release_lib()
+        if self.L is None:
+            raise OSError("the reference's CPU path is not built (its sources are not staged)")
+        self._vol = np.ascontiguousarray(volume, dtype=np.float32)
+        nz, ny, nx = self._vol.shape
+        dmn = np.asarray(dmin, dtype=np.float32)
+        dmx = np.asarray(dmax, dtype=np.float32)
+        self.handle = self.L.ref_grid_create(_ptr(self._vol), nx, ny, nz, _ptr(dmn), _ptr(dmx))
+        self._vol = None
+
+    def rows(self, cam, gen, rec, width, height, m, row0, row_step, table, tf_row, rgba=None):
+        t = np.ascontiguousarray(table, dtype=np.uint8) if table is not None else None
+        row = np.ascontiguousarray(tf_row, dtype=np.float32)
+        return int(self.L.ref_pipeline_rows(self.handle, C.byref(cam), C.byref(gen), C.byref(rec), width, height, m,
+                                            row0, row_step, _ptr(t) if t is not None else None, _ptr(row),
+                                            _ptr(rgba) if rgba is not None else None))
+
+    def close(self):
+        if self.handle:
+            self.L.ref_grid_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        self.close()
 
 
 class ParticleSet:

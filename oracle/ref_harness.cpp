@@ -255,6 +255,99 @@ int ref_generate_grid(const mraygb_camera *c, const mraygb_generation_params *g,
     return 0;
 }
 
+/* A RegularGrid held between calls (the CPU baseline times the path, not the copy of the volume). */
+void *ref_grid_create(const float *vol, int nx, int ny, int nz, const float *dmin, const float *dmax)
+{
+    return new RegularGrid(Vec3i(nx, ny, nz), to_range(dmin, dmax),
+                           std::vector<float>(vol, vol + size_t(nx) * ny * nz), RegularGrid::DataType::F32);
+}
+void ref_grid_destroy(void *grid) { delete static_cast<RegularGrid *>(grid); }
+
+/* The generate and reconstruct flows of main.cpp (generate() with compaction and prediction coding, the codes of
+ * quantize_prediction_coding with `table`, dequantize_prediction_coding, reconstruct()) restricted to the rows
+ * y = row0 (mod row_step) of a W x H image, with the reference's own code: the per-pixel body of generate_host
+ * (moment_raymarcher.cpp:129-157: generate_ray and compute_num_moments) on the sampled rows, then
+ * MomentImageHost::compact and prediction_encode (the other pixels hold no moments), the quantizer and its inverse,
+ * and the per-pixel body of reconstruct_host (moment_raymarcher.cpp:296-325) on the sampled rows.  OpenMP over the
+ * sampled pixels (the reference's loops go over rows, which a sample of a few rows would leave to a few threads).
+ * out_rgba: W*H*4 floats or nullptr; returns the number of sampled rays. */
+int64_t ref_pipeline_rows(const void *grid_handle, const mraygb_camera *c, const mraygb_generation_params *g,
+                          const mraygb_reconstruction_params *r, int w, int h, int m, int row0, int row_step,
+                          const uint8_t *table, const float *tf_row, float *out_rgba)
+{
+    const RegularGrid &grid = *static_cast<const RegularGrid *>(grid_handle);
+    auto gp = to_gen(g);
+    auto params = to_rec(r);
+    auto cam = to_camera(c);
+    MomentImageHost img(w, h, m, gp.compact_image, gp.transform_to_bounds);
+    img.domain = grid.domain;
+    const int nrows = row0 < h ? (h - 1 - row0) / row_step + 1 : 0;
+#pragma omp parallel for schedule(dynamic, 8)
+    for (int64_t i = 0; i < int64_t(nrows) * w; ++i)
+    {
+        const int y = row0 + int(i / w) * row_step;
+        const int x = int(i % w);
+        {
+            Vec2f ndc(x / static_cast<float>(w) * 2.f - 1.f, y / static_cast<float>(h) * 2.f - 1.f);
+            auto idx = img.get_idx(x, y);
+            vector<float> trig_moments(m, 0.0f);
+            auto b = generate_ray(grid, get_eye_ray(cam, ndc), cam.znear, trig_moments.data(), &img.data[idx], m, gp);
+            if (img.has_bounds())
+                img.bounds[y * w + x] = b;
+            if (gp.compact_image)
+            {
+                vector<float_complex> t0(m), t1(m), t2(m);
+                compute_num_moments(img, x, y, gp.error_threshold, t0.data(), t1.data(), t2.data());
+            }
+        }
+    }
+    // the rows not sampled hold no moments
+    if (gp.compact_image)
+        for (int y = 0; y < h; ++y)
+            if (y < row0 || (y - row0) % row_step != 0)
+                for (int x = 0; x < w; ++x)
+                    img.index[y * w + x] = 0;
+    if (gp.compact_image)
+        img.compact();
+    if (gp.prediction_coding)
+        img.prediction_encode(gp.coding_warp, gp.bias);
+    if (table && gp.prediction_coding)
+    {
+        std::vector<Byte> t(table, table + m);
+        auto qs = moment_quantization::quantize_prediction_coding(img, t);
+        moment_quantization::dequantize_prediction_coding(img, t, qs);
+    }
+    auto tf = make_tf(tf_row);
+    NoSingleScattering ss;
+#pragma omp parallel for schedule(dynamic, 8)
+    for (int64_t i = 0; i < int64_t(nrows) * w; ++i)
+    {
+        const int y = row0 + int(i / w) * row_step;
+        const int x = int(i % w);
+        {
+            Vec2f ndc(x / static_cast<float>(w) * 2.f - 1.f, y / static_cast<float>(h) * 2.f - 1.f);
+            Vec4f color;
+            if (img.get_num_moments(x, y) == 0)
+                color = reconstruct_zero_ray(tf);
+            else
+            {
+                auto pm = img.prepare_moments(x, y, params.bias);
+                MESEReconstructionDefault rec(pm.size(), pm.data(), img.get_bounds(x, y));
+                color = reconstruct_ray(cut::get_eye_ray(cam, ndc), img.domain, cam.znear, rec, tf, ss, params);
+            }
+            if (out_rgba)
+            {
+                float *o = out_rgba + 4 * (size_t(y) * w + x);
+                o[0] = color.x;
+                o[1] = color.y;
+                o[2] = color.z;
+                o[3] = color.w;
+            }
+        }
+    }
+    return int64_t(nrows) * w;
+}
+
 /* Particles::sample (volume.cpp:83-94) at npts points, with the grid Particles builds (volume.cpp:55-81). */
 int ref_particles_sample(const float *x, const float *y, const float *z, const float *v, uint64_t n, float h,
                          const float *dmin, const float *dmax, const float *pts, uint64_t npts, float *out)

@@ -148,12 +148,25 @@ def test_dropin_generate_prediction_coded_then_reconstruct(gpu_context, warp):
     codes = M.quantize_prediction_coding(mi, table, context=gpu_context)
     codes_ref = O.quantize_prediction_coding(wl.width, wl.height, wl.num_moments, ref["index"], ref["data"], table)
     assert codes.size == codes_ref.size
-    # end to end (volume -> codes): the fraction of 10-bit codes that differ
-    a = O.unpack_codes(wl.width, wl.height, wl.num_moments, ref["index"], table, codes)
-    b = O.unpack_codes(wl.width, wl.height, wl.num_moments, ref["index"], table, codes_ref)
-    frac = float(np.mean(a != b))
-    print(f"end-to-end 10-bit code mismatch (warp {warp}): {frac:.4%} of {a.size} codes")
-    assert frac <= 0.02
+    # end to end (volume -> codes): the moments differ from the reference's FP32 moments in their last bits, and a
+    # code flips wherever that carries an encoded value across a code boundary.  Both code streams are compared with
+    # the codes the reference's FP32 encoding gives for the FP64 moments rounded to float (pixels whose u16 bounds
+    # agree in both precisions): ours must agree with those at least as often as the reference's do.
+    W, H, m = wl.width, wl.height, wl.num_moments
+    m64, b64, _ = O.generate_moments(wl.camera, wl.gen, wl.volume, wl.domain_min, wl.domain_max, W, H, m, "f64")
+    counts = np.diff(ref["index"].astype(np.int64))
+    data64 = m64.reshape(-1, m)[counts > 0].reshape(-1).astype(np.float32)
+    enc64, _ = O.prediction_encode(W, H, m, ref["index"], data64, warp, wl.gen.bias)
+    codes_exact = O.quantize_prediction_coding(W, H, m, ref["index"], enc64, table)
+    a, b, e = (O.unpack_codes(W, H, m, ref["index"], table, c) for c in (codes, codes_ref, codes_exact))
+    pix_same = np.all(b64.reshape(-1, 2) == ref["bounds"].reshape(-1, 2), axis=-1)
+    same = np.repeat(pix_same, counts)
+    ours_vs_ref = float(np.mean(a != b))
+    ours_vs_exact = float(np.mean((a != e)[same]))
+    ref_vs_exact = float(np.mean((b != e)[same]))
+    print(f"10-bit codes differing (warp {warp}, {a.size} codes): ours vs reference {ours_vs_ref:.3%}, ours vs "
+          f"exact {ours_vs_exact:.3%}, reference vs exact {ref_vs_exact:.3%}")
+    assert ours_vs_exact <= ref_vs_exact + 0.002
     # reconstruct from the prediction-coded image (prepare_moments_from_pred_coding)
     tf = M.preintegrate(wl.tf1d, wl.tf_step)
     img = M.ColorImageHost(wl.width, wl.height)
