@@ -20,7 +20,8 @@
 // Layout: a warp holds 8 rays (quads).  Per round the 4 lanes of a quad each march one sample (the four
 // consecutive t values are computed by every lane with the reference's sequential float adds), exchange
 // (f_{k-1}+f_k, f_k-f_{k-1}, z_k) with shuffles, and each lane accumulates the moments j = q + 4i it owns:
-// z_k^q z_k^{4i} by complex rotation, so no moment is more than 16 rotations from a fresh sincos.
+// z_k^j by the three-term recurrence in j (steps of four) from z_k^q and z_k^(q+4), so no moment is more than
+// 15 steps from a fresh sincos (largest error of the trigonometric values 6e-5, where sin(4 p_m) is near 0).
 //
 // Two arithmetic forms: plain FP32 sums, or per-round partial sums added with Kahan compensation
 // (MRAYGB_PRECISION_COMPENSATED_FP64_MESE; the partial starts from minus the compensation, which saves Kahan's
@@ -165,8 +166,11 @@ template <class V, int NJ, bool KAHAN> __device__ __forceinline__ void generate_
             z = {cs, -sn};
         }
 
-        float Ss[4], Ds[4];
-        cf w[4], v[4];
+        // Per sample s the lane needs z_s^j for its moments j = q + 4i.  Both parts of z^j satisfy the three-term
+        // recurrence x_{j+4} = 2 cos(4 theta) x_j - x_{j-4} (Chebyshev in steps of four), one FMA per part and
+        // moment instead of a complex rotation's four operations; the recurrence starts from z^q and z^(q+4).
+        float Ss[4], Ds[4], c4[4];
+        cf wa[4], wb[4];
 #pragma unroll
         for (int s = 0; s < 4; ++s)
         {
@@ -177,12 +181,14 @@ template <class V, int NJ, bool KAHAN> __device__ __forceinline__ void generate_
             zs.y = __shfl_sync(kFull, z.y, qbase + s);
             const cf z2 = csq(zs);
             const cf z3 = cmul(z2, zs);
-            v[s] = csq(z2);
+            const cf z4 = csq(z2);
             cf u = {1.f, 0.f};
             u = (q == 1) ? zs : u;
             u = (q == 2) ? z2 : u;
             u = (q == 3) ? z3 : u;
-            w[s] = u;
+            wa[s] = u;
+            wb[s] = cmul(u, z4);
+            c4[s] = 2.f * z4.x;
         }
 
 #pragma unroll
@@ -191,13 +197,13 @@ template <class V, int NJ, bool KAHAN> __device__ __forceinline__ void generate_
             if (KAHAN)
             {
                 // the partial sum starts from minus the compensation, so it is already Kahan's corrected term
-                float pc = fmaf(Ss[0], w[0].x, -Ck[i]);
-                float pd = fmaf(Ds[0], w[0].y, -Dk[i]);
+                float pc = fmaf(Ss[0], wa[0].x, -Ck[i]);
+                float pd = fmaf(Ds[0], wa[0].y, -Dk[i]);
 #pragma unroll
                 for (int s = 1; s < 4; ++s)
                 {
-                    pc = fmaf(Ss[s], w[s].x, pc);
-                    pd = fmaf(Ds[s], w[s].y, pd);
+                    pc = fmaf(Ss[s], wa[s].x, pc);
+                    pd = fmaf(Ds[s], wa[s].y, pd);
                 }
                 kahan_add_corrected(C[i], Ck[i], pc);
                 kahan_add_corrected(Dc[i], Dk[i], pd);
@@ -207,15 +213,19 @@ template <class V, int NJ, bool KAHAN> __device__ __forceinline__ void generate_
 #pragma unroll
                 for (int s = 0; s < 4; ++s)
                 {
-                    C[i] = fmaf(Ss[s], w[s].x, C[i]);
-                    Dc[i] = fmaf(Ds[s], w[s].y, Dc[i]);
+                    C[i] = fmaf(Ss[s], wa[s].x, C[i]);
+                    Dc[i] = fmaf(Ds[s], wa[s].y, Dc[i]);
                 }
             }
             if (i + 1 < NJ)
             {
 #pragma unroll
                 for (int s = 0; s < 4; ++s)
-                    w[s] = cmul(w[s], v[s]);
+                {
+                    const cf next = {fmaf(c4[s], wb[s].x, -wa[s].x), fmaf(c4[s], wb[s].y, -wa[s].y)};
+                    wa[s] = wb[s];
+                    wb[s] = next;
+                }
             }
         }
 

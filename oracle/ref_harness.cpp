@@ -33,6 +33,7 @@
 
 #include <omp.h>
 
+#include <chrono>
 #include <cstring>
 
 /* defined in transfer_function.cpp without a header declaration */
@@ -346,6 +347,43 @@ int64_t ref_pipeline_rows(const void *grid_handle, const mraygb_camera *c, const
         }
     }
     return int64_t(nrows) * w;
+}
+
+/* Wall-clock milliseconds of the reference's own generate() and reconstruct() calls (moment_raymarcher.cpp:
+ * 168-183, 329-337) on a grid held between calls, as main.cpp's --generate / --reconstruct make them: a fresh
+ * MomentImageHost per generate (outside the timing), then reconstruct of the image generate returned.  They
+ * dispatch to whatever generate_device / reconstruct_device the library was linked with: the reference's
+ * moment_raymarcher.cu (Makefile refcuda) or the drop-in shim over libmraygb.so (Makefile shim).  out_ms holds
+ * 2 * steps values (generate, reconstruct per step); out_rgba8 (W*H*4 bytes, or nullptr) the last colours. */
+int ref_time_flow(const void *grid_handle, const mraygb_camera *c, const mraygb_generation_params *g,
+                  const mraygb_reconstruction_params *r, int w, int h, int m, const float *tf_row, int warmup,
+                  int steps, double *out_ms, uint8_t *out_rgba8, uint64_t *out_data_size)
+{
+    const RegularGrid &grid = *static_cast<const RegularGrid *>(grid_handle);
+    auto gp = to_gen(g);
+    auto params = to_rec(r);
+    auto cam = to_camera(c);
+    auto tf = make_tf(tf_row);
+    ColorImageHost cimg(w, h);
+    for (int i = 0; i < warmup + steps; ++i)
+    {
+        MomentImageHost img(w, h, m, gp.compact_image, gp.transform_to_bounds);
+        const auto t0 = std::chrono::steady_clock::now();
+        generate(cam, grid, img, gp);
+        const auto t1 = std::chrono::steady_clock::now();
+        reconstruct(cam, img, tf, cimg, params);
+        const auto t2 = std::chrono::steady_clock::now();
+        if (i >= warmup)
+        {
+            out_ms[2 * (i - warmup)] = std::chrono::duration<double, std::milli>(t1 - t0).count();
+            out_ms[2 * (i - warmup) + 1] = std::chrono::duration<double, std::milli>(t2 - t1).count();
+        }
+        if (out_data_size)
+            *out_data_size = img.data.size();
+    }
+    if (out_rgba8)
+        std::memcpy(out_rgba8, cimg.rgba.data(), 4 * size_t(w) * h);
+    return 0;
 }
 
 /* Particles::sample (volume.cpp:83-94) at npts points, with the grid Particles builds (volume.cpp:55-81). */

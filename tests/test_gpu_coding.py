@@ -124,6 +124,28 @@ def test_quantize_host_api_matches_reference_packer(gpu_context):
     assert np.array_equal(ours, O.quantize_prediction_coding(W, H, m, index, mi.data, table))
 
 
+def test_dequantize_host_api_matches_reference_unpacker(gpu_context):
+    """mraygb_dequantize_prediction_coding (dequantize_prediction_coding on host buffers): the oracle's floats."""
+    import mray_gb300 as M
+
+    W, H, m, index, data = _ragged_image(6)
+    table = M.default_quantization_table(m, 10)
+    vals = np.random.default_rng(6).uniform(0.0, 1.0, size=data.size).astype(np.float32)
+    packed = O.quantize_prediction_coding(W, H, m, index, vals, table)
+    mi = M.MomentImageHost(W, H, m, True)
+    mi.is_compact, mi.prediction_code = True, True
+    mi.index, mi.data = index, np.zeros(data.size, np.float32)
+    M.dequantize_prediction_coding(mi, table, packed, context=gpu_context)
+    ref = O.dequantize_prediction_coding(W, H, m, index, table, packed, data.size)
+    assert np.array_equal(mi.data, ref)
+
+
+def test_measured_fp32_rate_is_plausible(gpu_context):
+    """The FP32 FMA roof: within the GB300's nominal 152 SMs x 128 lanes x 2 FLOP x 2.07 GHz = 80.6 TFLOP/s."""
+    rate = gpu_context.measure_fp32_rate()
+    assert 20.0 < rate < 85.0, rate
+
+
 @pytest.mark.parametrize("warp", [0, 1])
 def test_dropin_generate_prediction_coded_then_reconstruct(gpu_context, warp):
     """generate with prediction_coding (the reference's default), codes at 10 bits, reconstruct from the
