@@ -726,6 +726,8 @@ def refcuda_worker(args, local):
     import torch
 
     from mray_gb300.types import Camera, GenerationParameters, ReconstructionParameters
+
+    O = _oracle()  # puts oracle/ on the path
     from stage_reference import reference_src
 
     src = reference_src()
@@ -751,7 +753,6 @@ def refcuda_worker(args, local):
     dmx = np.asarray(hl.domain_max, np.float32)
     grid = L.ref_grid_create(vol.ctypes.data, hl.n, hl.n, hl.n, dmn.ctypes.data, dmx.ctypes.data)
     del vol
-    O = _oracle()
     row = O.preintegrate(hl.tf1d, hl.tf_step)
     steps = max(1, min(args.steps, 3))
     ms = np.zeros(2 * steps, np.float64)

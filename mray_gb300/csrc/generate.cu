@@ -23,7 +23,7 @@
 // z_k^j by the three-term recurrence in j (steps of four) from z_k^q and z_k^(q+4), so no moment is more than
 // 15 steps from a fresh sincos (largest error of the trigonometric values 6e-5, where sin(4 p_m) is near 0).
 //
-// Two arithmetic forms: plain FP32 sums, or per-round partial sums added with Kahan compensation
+// Two arithmetic forms: plain FP32 sums, or per-round partial sums of C added with Kahan compensation
 // (MRAYGB_PRECISION_COMPENSATED_FP64_MESE; the partial starts from minus the compensation, which saves Kahan's
 // separate correction step).
 
@@ -83,14 +83,13 @@ template <class V, int NJ, bool KAHAN> __device__ __forceinline__ void generate_
         hit = hit && (t_far > 0.f);
     }
 
-    float C[NJ], Dc[NJ], Ck[NJ], Dk[NJ];
+    float C[NJ], Dc[NJ], Ck[NJ];
 #pragma unroll
     for (int i = 0; i < NJ; ++i)
     {
         C[i] = 0.f;
         Dc[i] = 0.f;
         Ck[i] = 0.f;
-        Dk[i] = 0.f;
     }
 
     float blo = 1.f, bhi = 0.f;
@@ -196,17 +195,17 @@ template <class V, int NJ, bool KAHAN> __device__ __forceinline__ void generate_
         {
             if (KAHAN)
             {
-                // the partial sum starts from minus the compensation, so it is already Kahan's corrected term
+                // the partial sum starts from minus the compensation, so it is already Kahan's corrected term.
+                // Only C is compensated: D enters moment j through beta_j(h) ~ j h^2 / 3, at most a few percent of
+                // alpha_j(h) ~ h, so its rounding is that much smaller in the moment.
                 float pc = fmaf(Ss[0], wa[0].x, -Ck[i]);
-                float pd = fmaf(Ds[0], wa[0].y, -Dk[i]);
 #pragma unroll
                 for (int s = 1; s < 4; ++s)
-                {
                     pc = fmaf(Ss[s], wa[s].x, pc);
-                    pd = fmaf(Ds[s], wa[s].y, pd);
-                }
                 kahan_add_corrected(C[i], Ck[i], pc);
-                kahan_add_corrected(Dc[i], Dk[i], pd);
+#pragma unroll
+                for (int s = 0; s < 4; ++s)
+                    Dc[i] = fmaf(Ds[s], wa[s].y, Dc[i]);
             }
             else
             {

@@ -102,8 +102,6 @@ __global__ void __launch_bounds__(BLOCK) count_moments_kernel(int num_pixels, in
 
 // MomentImageHost::prediction_encode, per-pixel part (moment_image.cpp:103-126): bias lerp, trigonometric ->
 // exponential moments, encode, projection of the residuals to the real line; in place
-// MomentImageHost::prediction_encode, per-pixel part (moment_image.cpp:103-126): bias lerp, trigonometric ->
-// exponential moments, encode, projection of the residuals to the real line; in place
 template <int MAXM, int BLOCK>
 __global__ void __launch_bounds__(BLOCK) prediction_encode_kernel(int num_pixels, int m,
                                                                   const uint32_t *__restrict__ index,
@@ -126,17 +124,16 @@ __global__ void __launch_bounds__(BLOCK) prediction_encode_kernel(int num_pixels
         d[i] = (1 - bias) * d[i] + bias * 0.0f;
     cx<float> *base = reinterpret_cast<cx<float> *>(smem);
     const Strided<cx<float>, BLOCK> e{base + threadIdx.x};
-    const Strided<cx<float>, BLOCK> code{base + MAXM * BLOCK + threadIdx.x};
-    const Strided<cx<float>, BLOCK> poly{base + 2 * MAXM * BLOCK + threadIdx.x};
+    const Strided<cx<float>, BLOCK> poly{base + MAXM * BLOCK + threadIdx.x};
     trig_to_exp<float>(n, e, d, two_pi_over_l<float>());
-    pc_encode<float>(n, e, code, poly);
-    // transform_quantization_real (moment_prediction_coding.h:81-92): out[0] = c_0 stays d[0]
-    const cx<float> c0 = code[0];
+    // transform_quantization_real (moment_prediction_coding.h:81-92) on the code as encode produces it: out[0] =
+    // c_0 stays d[0]; the axis comes from code_0 = e_0.  The trigonometric moments in d are no longer read once
+    // the exponential moments exist, so each residual can overwrite its moment at once (no code array).
+    const cx<float> c0 = e[0];
     const cx<float> axis = mk(-c0.y, c0.x);
     const float len = sqrtf(cabs2(axis));
     const cx<float> inv_axis = cdiv(mk(len, 0.f), axis);
-    for (int l = 1; l < n; ++l)
-        d[l] = cmulc((cx<float>)code[l], inv_axis).x;
+    pc_encode<float>(n, e, poly, [&](int l, cx<float> code_l) { d[l] = cmulc(code_l, inv_axis).x; });
 }
 
 __global__ void libm_sincosf_kernel(uint64_t n, const float *__restrict__ x, float *__restrict__ s,
@@ -170,12 +167,16 @@ cudaError_t launch_count_t(int num_pixels, int m, float thr, const float *moment
 template <int MAXM>
 cudaError_t launch_encode_t(int num_pixels, int m, const uint32_t *index, float *data, float bias, cudaStream_t stream)
 {
-    constexpr int per = smem_per_thread<float, MAXM, 3, 0>();
+    constexpr int per = smem_per_thread<float, MAXM, 2, 0>();
     constexpr int block = block_for<per>();
     constexpr int bytes = per * block;
     cudaError_t e = cudaFuncSetAttribute(prediction_encode_kernel<MAXM, block>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (e != cudaSuccess)
+        return e;
+    // the whole shared-memory carveout: the resident pixels are what this latency-bound kernel lives on
+    if ((e = cudaFuncSetAttribute(prediction_encode_kernel<MAXM, block>,
+                                  cudaFuncAttributePreferredSharedMemoryCarveout, 100)) != cudaSuccess)
         return e;
     prediction_encode_kernel<MAXM, block><<<(num_pixels + block - 1) / block, block, bytes, stream>>>(
         num_pixels, m, index, data, bias);

@@ -184,10 +184,10 @@ __device__ void lagrange_from_poly(int n, const A &poly, const A &e, const O &ac
     }
 }
 
-// encode (moment_prediction_coding.h:123-158)
-template <typename T, typename A> __device__ void pc_encode(int n, const A &e, const A &code, const A &poly)
+// encode (moment_prediction_coding.h:123-158).  code[0] = e[0]; code[l] for l >= 1 goes to sink(l, code_l) as
+// soon as it is known (the caller stores or transforms it; nothing later reads it back).
+template <typename T, typename A, typename Sink> __device__ void pc_encode(int n, const A &e, const A &poly, Sink &&sink)
 {
-    code[0] = (cx<T>)e[0];
     poly[0] = mk<T>(T(1) / ((cx<T>)e[0]).x, 0);
     bool invalid = false;
     for (int l = 1; l < n; ++l)
@@ -195,7 +195,7 @@ template <typename T, typename A> __device__ void pc_encode(int n, const A &e, c
         cx<T> u = mk<T>(0, 0);
         for (int k = 0; k < l; ++k)
             u = cadd(u, cmulc((cx<T>)poly[k], (cx<T>)e[l - k]));
-        code[l] = u;
+        sink(l, u);
         T a2 = cabs2(u);
         if (invalid || a2 >= T(1))
         {
@@ -207,16 +207,17 @@ template <typename T, typename A> __device__ void pc_encode(int n, const A &e, c
     }
 }
 
-// decode (moment_prediction_coding.h:163-208)
-template <typename T, typename A> __device__ void pc_decode(int n, const A &code, const A &e, const A &poly)
+// decode (moment_prediction_coding.h:163-208); code(l) yields code l (each is asked for once, in order)
+template <typename T, typename A, typename Code>
+__device__ void pc_decode_from(int n, Code &&code, const A &e, const A &poly)
 {
     using K = MeseConst<T>;
-    e[0] = (cx<T>)code[0];
+    e[0] = code(0);
     poly[0] = mk<T>(T(1) / ((cx<T>)e[0]).x, 0);
     bool invalid = false;
     for (int l = 1; l < n; ++l)
     {
-        cx<T> u = code[l];
+        cx<T> u = code(l);
         T a2 = cabs2(u);
         if (invalid || a2 >= (T(1) - K::eps_decode))
         {
@@ -232,6 +233,11 @@ template <typename T, typename A> __device__ void pc_decode(int n, const A &code
     }
 }
 
+template <typename T, typename A> __device__ void pc_decode(int n, const A &code, const A &e, const A &poly)
+{
+    pc_decode_from<T>(n, [&](int l) { return (cx<T>)code[l]; }, e, poly);
+}
+
 // prediction_coding_inv_warp; params are the dequantized u16 coding parameters
 template <typename T> __device__ __forceinline__ T pc_inv_warp(int l, T x, int warp, const float *p)
 {
@@ -240,22 +246,30 @@ template <typename T> __device__ __forceinline__ T pc_inv_warp(int l, T x, int w
     return x * T(2) - T(1);
 }
 
-// transform_dequantization_real
-template <typename T, typename A>
-__device__ void pc_dequant_real(int n, const float *in, const A &out, int warp, const float *params)
+// transform_dequantization_real, one code at a time: code 0 and the factor that maps every later real residual
+// onto the axis perpendicular to it
+template <typename T> struct PcDequant
 {
-    using K = MeseConst<T>;
-    const T c0 = T(in[0]);
-    const T phase = K::pi * c0 - K::half_pi;
-    T s, c;
-    dsincos(phase, &s, &c);
-    const cx<T> o0 = cscale(T(2) * K::inv_4pi, mk(c, s));
-    out[0] = o0;
-    const cx<T> axis = mk(-o0.y, o0.x);
-    const T len = dsqrt(cabs2(axis));
-    const cx<T> factor = cdivr(axis, len);
-    for (int l = 1; l < n; ++l)
-        out[l] = cscale(pc_inv_warp<T>(l, T(in[l]), warp, params), factor);
-}
+    const float *in;
+    int warp;
+    const float *params;
+    cx<T> o0, factor;
+    __device__ PcDequant(const float *in_, int warp_, const float *params_) : in(in_), warp(warp_), params(params_)
+    {
+        using K = MeseConst<T>;
+        const T c0 = T(in[0]);
+        const T phase = K::pi * c0 - K::half_pi;
+        T s, c;
+        dsincos(phase, &s, &c);
+        o0 = cscale(T(2) * K::inv_4pi, mk(c, s));
+        const cx<T> axis = mk(-o0.y, o0.x);
+        const T len = dsqrt(cabs2(axis));
+        factor = cdivr(axis, len);
+    }
+    __device__ cx<T> operator()(int l) const
+    {
+        return l == 0 ? o0 : cscale(pc_inv_warp<T>(l, T(in[l]), warp, params), factor);
+    }
+};
 
 } // namespace mraygb

@@ -40,17 +40,17 @@ template <typename T, int MAXM, int NC, int NR> constexpr int smem_per_thread()
 }
 
 // Lagrange multipliers (prepare_moments_from_std_coding / prepare_moments_from_pred_coding).  Arrays live in
-// thread-strided shared memory: code (prediction-coded input only), e (exponential moments), poly (Levinson
-// solution) and the real accumulators of the correlation.
+// thread-strided shared memory: e (exponential moments), poly (Levinson solution) and the real accumulators of the
+// correlation; prediction codes are dequantized one at a time as the decode reads them.
 template <typename T, int MAXM, int BLOCK, bool PC, typename CArr, typename RArr>
-__device__ __forceinline__ void prepare_pixel(int n, const float *in, const CArr &e, const CArr &poly, const CArr &code,
+__device__ __forceinline__ void prepare_pixel(int n, const float *in, const CArr &e, const CArr &poly,
                                               const RArr &acc, int coding_warp, const float *params, float bias,
                                               float *out)
 {
     if (PC)
     {
-        pc_dequant_real<T>(n, in, code, coding_warp, params);
-        pc_decode<T>(n, code, e, poly);
+        // the codes are dequantized as the decode asks for them (transform_dequantization_real, then decode)
+        pc_decode_from<T>(n, PcDequant<T>(in, coding_warp, params), e, poly);
     }
     else
     {
@@ -100,17 +100,16 @@ __global__ void __launch_bounds__(BLOCK) prepare_kernel(int num_pixels, int m, c
         cx<T> *base = reinterpret_cast<cx<T> *>(smem);
         const Strided<cx<T>, BLOCK> e{base + threadIdx.x};
         const Strided<cx<T>, BLOCK> poly{base + MAXM * BLOCK + threadIdx.x};
-        const Strided<cx<T>, BLOCK> code{base + 2 * MAXM * BLOCK + threadIdx.x};
-        const Strided<T, BLOCK> acc{reinterpret_cast<T *>(base + (PC ? 3 : 2) * MAXM * BLOCK) + threadIdx.x};
-        prepare_pixel<T, MAXM, BLOCK, PC>(n, data + idx, e, poly, code, acc, coding_warp, s_params, bias, out + idx);
+        const Strided<T, BLOCK> acc{reinterpret_cast<T *>(base + 2 * MAXM * BLOCK) + threadIdx.x};
+        prepare_pixel<T, MAXM, BLOCK, PC>(n, data + idx, e, poly, acc, coding_warp, s_params, bias, out + idx);
     }
     else
     {
-        cx<T> ae[MAXM], apoly[MAXM], acode[PC ? MAXM : 1];
+        cx<T> ae[MAXM], apoly[MAXM];
         T aacc[MAXM];
-        const Strided<cx<T>, 1> e{ae}, poly{apoly}, code{acode};
+        const Strided<cx<T>, 1> e{ae}, poly{apoly};
         const Strided<T, 1> acc{aacc};
-        prepare_pixel<T, MAXM, BLOCK, PC>(n, data + idx, e, poly, code, acc, coding_warp, s_params, bias, out + idx);
+        prepare_pixel<T, MAXM, BLOCK, PC>(n, data + idx, e, poly, acc, coding_warp, s_params, bias, out + idx);
     }
 }
 
@@ -133,7 +132,7 @@ cudaError_t launch_prepare_pc(int num_pixels, int m, const uint32_t *index, cons
                               const uint16_t *cp, float bias, float *out, cudaStream_t stream)
 {
     constexpr bool smem = sizeof(T) == 4;
-    constexpr int per = smem_per_thread<T, MAXM, PC ? 3 : 2, 1>();
+    constexpr int per = smem_per_thread<T, MAXM, 2, 1>();
     constexpr int block = smem ? block_for<per>() : 128;
     constexpr int bytes = smem ? per * block : 0;
     if (smem)
@@ -141,6 +140,10 @@ cudaError_t launch_prepare_pc(int num_pixels, int m, const uint32_t *index, cons
         cudaError_t e = cudaFuncSetAttribute(prepare_kernel<T, MAXM, block, PC, smem>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
         if (e != cudaSuccess)
+            return e;
+        // the whole shared-memory carveout: resident pixels are what this latency-bound kernel lives on
+        if ((e = cudaFuncSetAttribute(prepare_kernel<T, MAXM, block, PC, smem>,
+                                      cudaFuncAttributePreferredSharedMemoryCarveout, 100)) != cudaSuccess)
             return e;
     }
     const int grid = (num_pixels + block - 1) / block;
