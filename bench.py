@@ -783,10 +783,21 @@ def run_reference_cuda(args):
         cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--section", "refcuda-worker", "--worker", which,
                "--steps", str(args.steps), "--size", str(args.size), "--image", str(args.image), "--moments",
                str(args.moments), "--modes", str(args.modes), "--bits", str(args.bits)]
+        env = dict(os.environ)
+        if which == "shim":
+            env["MRAYGB_SHIM_TIMING"] = "1"
         try:
-            r = subprocess.run(cmd, capture_output=True, text=True, timeout=900)
+            r = subprocess.run(cmd, capture_output=True, text=True, timeout=900, env=env)
             res = json.loads(r.stdout.strip().splitlines()[-1])["refcuda-worker"] if r.returncode == 0 else \
                 {"unavailable": f"exit {r.returncode}: {r.stderr[-400:]}"}
+            if which == "shim" and r.returncode == 0:
+                # mean of each phase the shim reports, over the calls after the warm-up
+                phases = {}
+                for ln in r.stderr.splitlines():
+                    if ln.startswith("mraygb shim "):
+                        head, ms = ln[len("mraygb shim "):].rsplit(" ", 2)[0], float(ln.rsplit(" ", 2)[1])
+                        phases.setdefault(head, []).append(ms)
+                res["shim_phases_ms"] = {k: statistics.mean(v[1:] if len(v) > 1 else v) for k, v in phases.items()}
         except (subprocess.TimeoutExpired, ValueError, IndexError, KeyError) as e:
             res = {"unavailable": f"{type(e).__name__}: {str(e)[-300:]}"}
         out["reference_cuda" if which == "cuda" else "ours_through_shim"] = res

@@ -95,6 +95,11 @@ template <class V, int NJ, bool KAHAN> __device__ __forceinline__ void generate_
     float blo = 1.f, bhi = 0.f;
     float pti = 0.f, pss = 0.f;
     float f_tail = 0.f;
+    // The sums run over the density minus a baseline (the ray's first sample): over the phase interval [-pi, 0] a
+    // constant density c contributes exactly c pi to the zeroth integral and nothing to the others, so it is added
+    // back in closed form.  The sums then scale with the ray's density range instead of its level, and so do their
+    // rounding errors (which the bounds transform divides by that range).
+    float base = 0.f;
     float p_tail = -kPiF;
     float t = t_near;
     const float step = a.step;
@@ -109,6 +114,7 @@ template <class V, int NJ, bool KAHAN> __device__ __forceinline__ void generate_
         blo = rmin(blo, f0);
         bhi = rmax(bhi, f0);
         f_tail = f0;
+        base = f0;
     }
     const float half_pss = 0.5f * pss;
     // A ray ends by itself after about (t_far - t_near) / step samples; the cap only guards a step too small to
@@ -158,7 +164,7 @@ template <class V, int NJ, bool KAHAN> __device__ __forceinline__ void generate_
         cf z = {1.f, 0.f};
         if (my_valid)
         {
-            S = f_left + f_my;
+            S = __fsub_rn(f_left, base) + __fsub_rn(f_my, base);
             D = f_my - f_left;
             float sn, cs;
             sincosf(p_my - half_pss, &sn, &cs);
@@ -290,7 +296,7 @@ template <class V, int NJ, bool KAHAN> __device__ __forceinline__ void generate_
         return;
     }
 
-    const float sL = f_tail + f_far;
+    const float sL = __fsub_rn(f_tail, base) + __fsub_rn(f_far, base);
     const float dL = f_far - f_tail;
     const float hL = -0.5f * p_tail;
     float snL, csL;
@@ -324,12 +330,13 @@ template <class V, int NJ, bool KAHAN> __device__ __forceinline__ void generate_
             seg_coeffs(j, h, al, be);
             seg_coeffs(j, hL, alL, beL);
             const float trig = al * C[i] + be * Dc[i] + (alL * sL * wL.x + beL * dL * wL.y);
-            const float raw = __fmul_rn(trig, kMInvPi);
+            // the baseline's share: c for the zeroth moment (exactly c pi / pi), zero for the others
+            const float rel = __fmul_rn(trig, kMInvPi);
             float val;
             if (a.transform_to_bounds)
-                val = (j == 0) ? (float)((double)__fsub_rn(raw, lo) * inv) : (float)((double)raw * inv);
+                val = (j == 0) ? (float)(((double)base - (double)lo + (double)rel) * inv) : (float)((double)rel * inv);
             else
-                val = raw;
+                val = (j == 0) ? __fadd_rn(base, rel) : rel;
             out[j] = val;
             if (j == 0)
                 m0 = val;

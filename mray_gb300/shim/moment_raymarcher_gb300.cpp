@@ -9,7 +9,9 @@
 #include "moment_raymarcher.cuh"
 #include "moment_quantization.h"
 
+#include <chrono>
 #include <cstdio>
+#include <cstdlib>
 #include <exception>
 #include <mutex>
 
@@ -31,6 +33,28 @@ mraygb_context *context()
     });
     return ctx;
 }
+
+// MRAYGB_SHIM_TIMING=1 prints the wall time of each phase of the seam calls to stderr (a maintainer's view of
+// where a generate / reconstruct call spends its time: copies, conversions, the library's own work)
+struct PhaseTimer
+{
+    const char *call;
+    bool on;
+    std::chrono::steady_clock::time_point t;
+    explicit PhaseTimer(const char *c) : call(c), on(std::getenv("MRAYGB_SHIM_TIMING") != nullptr)
+    {
+        t = std::chrono::steady_clock::now();
+    }
+    void mark(const char *phase)
+    {
+        if (!on)
+            return;
+        const auto now = std::chrono::steady_clock::now();
+        std::fprintf(stderr, "mraygb shim %s: %s %.2f ms\n", call, phase,
+                     std::chrono::duration<double, std::milli>(now - t).count());
+        t = now;
+    }
+};
 
 void check(int status)
 {
@@ -127,6 +151,7 @@ namespace
 void generate_uploaded(const cut::Camera &cam, const Range<Vec3f> &domain, MomentImageHost &img,
                        const GenerationParameters &params)
 {
+    PhaseTimer timer("generate");
     const auto c = to_c(cam);
     const auto g = to_c(params);
     img.domain = domain;
@@ -137,16 +162,19 @@ void generate_uploaded(const cut::Camera &cam, const Range<Vec3f> &domain, Momen
         img.bounds.resize(size_t(img.width) * img.height);
     std::vector<uint16_t> bounds(params.transform_to_bounds ? 2 * size_t(img.width) * img.height : 0);
     std::vector<uint16_t> cp(img.num_moments > 1 ? 2 * size_t(img.num_moments - 1) : 1);
+    timer.mark("host buffers");
     uint64_t size = 0;
     check(mraygb_generate(context(), &c, &g, img.width, img.height, img.num_moments, img.data.data(),
                           params.compact_image ? img.index.data() : nullptr,
                           params.transform_to_bounds ? bounds.data() : nullptr, cp.data(), &size));
+    timer.mark("mraygb_generate");
     img.data.resize(size);
     for (size_t i = 0; i < img.bounds.size() && !bounds.empty(); ++i)
     {
         img.bounds[i].lower = bounds[2 * i];
         img.bounds[i].upper = bounds[2 * i + 1];
     }
+    timer.mark("bounds conversion");
     img.is_compact = params.compact_image;
     img.prediction_code = params.prediction_coding;
     img.coding_warp = static_cast<CodingWarpType>(params.coding_warp);
@@ -168,8 +196,10 @@ void generate_device(cut::Camera cam, const RegularGrid &volume, MomentImageHost
     }
     const float dmin[3] = {volume.domain.min.x, volume.domain.min.y, volume.domain.min.z};
     const float dmax[3] = {volume.domain.max.x, volume.domain.max.y, volume.domain.max.z};
+    PhaseTimer timer("generate_device");
     check(mraygb_upload_grid(context(), volume.data.data(), volume.size.x, volume.size.y, volume.size.z, dmin, dmax,
                              0));
+    timer.mark("mraygb_upload_grid");
     generate_uploaded(cam, volume.domain, img, params);
 }
 
@@ -187,6 +217,7 @@ void reconstruct_device(cut::Camera cam, const MomentImageHost &mi, const Transf
                         const ReconstructionParameters &params)
 {
     // preintegrate() / read_from_disk() tables have 256 equal rows; the first row is the whole table
+    PhaseTimer timer("reconstruct_device");
     check(mraygb_upload_tf(context(), reinterpret_cast<const float *>(tf.data.data())));
     const auto c = to_c(cam);
     const auto r = to_c(params);
@@ -205,11 +236,13 @@ void reconstruct_device(cut::Camera cam, const MomentImageHost &mi, const Transf
         cp.push_back(p.param2);
     }
     static_assert(sizeof(ColorImageHost::rgba8_t) == 4, "rgba8_t is four bytes");
+    timer.mark("tf upload and bounds conversion");
     check(mraygb_reconstruct(context(), &c, &r, mi.width, mi.height, mi.num_moments, dmin, dmax,
                              mi.is_compact ? mi.index.data() : nullptr, mi.data.data(), mi.data.size(),
                              bounds.empty() ? nullptr : bounds.data(), mi.prediction_code, mi.coding_warp,
                              cp.empty() ? nullptr : cp.data(), nullptr,
                              reinterpret_cast<uint8_t *>(cimg.rgba.data())));
+    timer.mark("mraygb_reconstruct");
 }
 
 namespace
