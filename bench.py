@@ -1030,14 +1030,9 @@ def run_sph(args, local):
     from mray_gb300 import workloads as W
 
     n = args.sph_particles
-    h = 1.0 / 256
-    x, y, z, v = W.sph_particles(n, seed=31)
-    wl = W.sph_workload(n=64, h=h, width=SECTION_IMAGE, height=SECTION_IMAGE, num_moments=SECTION_M, seed=31)
-    rng = np.random.default_rng(38)
-    smp = v[rng.integers(0, n, size=100000)]
-    wl.gen.data_min, wl.gen.data_max = float(np.percentile(smp, 1)), float(np.percentile(smp, 99))
-    dmin = (float(x.min()), float(y.min()), float(z.min()))
-    dmax = (float(x.max()), float(y.max()), float(z.max()))
+    wl = W.sph_cluster_workload(n=n, width=SECTION_IMAGE, height=SECTION_IMAGE, num_moments=SECTION_M, seed=31)
+    x, y, z, v, h = wl.x, wl.y, wl.z, wl.v, wl.h
+    dmin, dmax = wl.domain_min, wl.domain_max
     Wd, H, m = wl.width, wl.height, wl.num_moments
     P = Wd * H
     ctx = M.Context(local)

@@ -330,6 +330,18 @@ __device__ __forceinline__ float map_density(float s, float dmin, float span, fl
     return rclamp(div_exact(__fsub_rn(s, dmin), span, inv_span, span_pow2), 0.f, 1.f);
 }
 
+// Every float t of [0, t_far] plus step is exact when step is a multiple of the float spacing at t_far (the largest
+// spacing a sample t < t_far has): the lowest set bit of step's significand at or above t_far's last place.
+__device__ __forceinline__ bool exact_steps(float step, float t_far)
+{
+    const uint32_t sb = __float_as_uint(step), fb = __float_as_uint(t_far);
+    const int es = (int)((sb >> 23) & 0xffu), ef = (int)((fb >> 23) & 0xffu);
+    if (es == 0 || es == 0xff || ef == 0xff)
+        return false; // subnormal, infinite or NaN step; infinite t_far
+    const uint32_t sig = (sb & 0x7fffffu) | 0x800000u;
+    return es + (__ffs(sig) - 1) >= ef;
+}
+
 // float((double)x - M_PI) without double arithmetic: x - pi with pi split into two floats (exact two-sum of
 // x and -pi_hi, then the low part), the same value the reference's double expression rounds to.
 __device__ __forceinline__ float sub_pi(float x)

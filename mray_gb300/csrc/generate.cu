@@ -95,10 +95,14 @@ template <class V, int NJ, bool KAHAN> __device__ __forceinline__ void generate_
     float blo = 1.f, bhi = 0.f;
     float pti = 0.f, pss = 0.f;
     float f_tail = 0.f;
-    // The sums run over the density minus a baseline (the ray's first sample): over the phase interval [-pi, 0] a
-    // constant density c contributes exactly c pi to the zeroth integral and nothing to the others, so it is added
-    // back in closed form.  The sums then scale with the ray's density range instead of its level, and so do their
-    // rounding errors (which the bounds transform divides by that range).
+    // The sums run over the density minus a baseline c, and c's share is added back in closed form: over the phase
+    // interval [-pi, 0] a constant contributes exactly c to the zeroth moment and nothing to the others.  The sums
+    // then scale with the ray's density range instead of its level, and so do their rounding errors, which the
+    // bounds transform divides by that range.  The closed form holds only where the segments [p - pss, p] tile
+    // [-pi, 0], i.e. where every t += step is exact: step a multiple of the float spacing at t_far.  Elsewhere (a
+    // step such as 1/192) t drifts by a constant amount per step, a constant density covers slightly more or less
+    // than pi, and the ray runs with c = 0.  c is the midrange of the first sample and 16 coarse samples spread
+    // over the ray (four per lane of the quad); it only chooses the split, not the integrals.
     float base = 0.f;
     float p_tail = -kPiF;
     float t = t_near;
@@ -114,7 +118,25 @@ template <class V, int NJ, bool KAHAN> __device__ __forceinline__ void generate_
         blo = rmin(blo, f0);
         bhi = rmax(bhi, f0);
         f_tail = f0;
-        base = f0;
+        if (exact_steps(step, t_far))
+        {
+            float cmin = f0, cmax = f0;
+            const float len = __fsub_rn(t_far, t_near);
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+            {
+                const float tc = t_near + len * ((float)(4 * i + q) + 0.5f) * (1.f / 16.f);
+                const float fc = map_density(volume_sample(a.vol, o[0] + tc * d[0], o[1] + tc * d[1], o[2] + tc * d[2]),
+                                             a.data_min, a.data_span, a.data_inv_span, a.data_span_pow2);
+                cmin = rmin(cmin, fc);
+                cmax = rmax(cmax, fc);
+            }
+            cmin = rmin(cmin, __shfl_xor_sync(0xfu << qbase, cmin, 1));
+            cmax = rmax(cmax, __shfl_xor_sync(0xfu << qbase, cmax, 1));
+            cmin = rmin(cmin, __shfl_xor_sync(0xfu << qbase, cmin, 2));
+            cmax = rmax(cmax, __shfl_xor_sync(0xfu << qbase, cmax, 2));
+            base = 0.5f * (cmin + cmax);
+        }
     }
     const float half_pss = 0.5f * pss;
     // A ray ends by itself after about (t_far - t_near) / step samples; the cap only guards a step too small to
@@ -330,7 +352,7 @@ template <class V, int NJ, bool KAHAN> __device__ __forceinline__ void generate_
             seg_coeffs(j, h, al, be);
             seg_coeffs(j, hL, alL, beL);
             const float trig = al * C[i] + be * Dc[i] + (alL * sL * wL.x + beL * dL * wL.y);
-            // the baseline's share: c for the zeroth moment (exactly c pi / pi), zero for the others
+            // the baseline's share: c for the zeroth moment, nothing for the others
             const float rel = __fmul_rn(trig, kMInvPi);
             float val;
             if (a.transform_to_bounds)

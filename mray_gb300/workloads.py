@@ -304,3 +304,21 @@ def sph_workload(n: int = 20000, h: float = 1.0 / 32, width: int = 64, height: i
     name = name or f"sph{n}_h{h:g}_{width}x{height}_m{num_moments}"
     return ParticleWorkload(name, x, y, z, v, h, dmin, dmax, width, height, num_moments, cam, gen, rec,
                             transfer_function(seed + 1), tf_step=0.05)
+
+
+def sph_cluster_workload(n: int = 16_000_000, h: float = 1.0 / 256, width: int = 1024, height: int = 1024,
+                         num_moments: int = 64, seed: int = 31) -> ParticleWorkload:
+    """The SPH configuration: n particles (70 % uniform, 30 % in 200 seeded Gaussian clusters, LogNormal(0, 0.5)
+    values) with one smoothing length h (the reference's particle grid: 1 / h cells per unit, 256^3 at h = 1/256),
+    perspective view of the unit cube, 64 moments, step h / 2; data_min / data_max at the 1st / 99th percentiles of
+    a seeded sample of 100000 values."""
+    wl = sph_workload(n=64, h=h, width=width, height=height, num_moments=num_moments, seed=seed)
+    x, y, z, v = sph_particles(n, seed)
+    rng = np.random.default_rng(seed + 7)
+    smp = v[rng.integers(0, n, size=min(n, 100000))]
+    wl.gen.data_min, wl.gen.data_max = float(np.percentile(smp, 1)), float(np.percentile(smp, 99))
+    wl.x, wl.y, wl.z, wl.v = x, y, z, v
+    wl.domain_min = (float(x.min()), float(y.min()), float(z.min()))
+    wl.domain_max = (float(x.max()), float(y.max()), float(z.max()))
+    wl.name = f"sph{n}_h1/{round(1 / h)}_{width}x{height}_m{num_moments}_persp"
+    return wl

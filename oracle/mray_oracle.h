@@ -82,6 +82,13 @@ typedef struct oracle_options
     /* reconstruct and generate_reference: the single-scattering transmittance cache (NULL: none; generate_reference
      * then marches the transmittance when rp->ss.enable) */
     const oracle_grid *ss_cache;
+    /* reconstruct only: added to every reconstructed density before the transfer-function lookup (0: the method).
+     * The reference's CPU sampling of the table (transfer_function.h:44-59) takes the texel pair from the front
+     * density and the blend weight from the back density's fractional part, so the colour jumps where a density
+     * crosses a multiple of 1/256; a small offset shows which pixels sit on such a jump. */
+    double density_offset;
+    /* reconstruct only: per-pixel offsets (W*H of R) used instead of density_offset when not NULL */
+    const void *density_offsets;
 } oracle_options;
 
 #define ORACLE_DECL(R, SFX)                                                                                         \

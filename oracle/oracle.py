@@ -31,7 +31,7 @@ class Options(C.Structure):
     _fields_ = [("exact_atan", C.c_int), ("nthreads", C.c_int), ("row_begin", C.c_int), ("row_end", C.c_int),
                 ("row_step", C.c_int), ("tf_bspline", C.c_int), ("bounds_out", C.c_void_p),
                 ("bounds_in", C.c_void_p), ("col_begin", C.c_int), ("col_end", C.c_int), ("col_step", C.c_int),
-                ("ss_cache", C.c_void_p)]
+                ("ss_cache", C.c_void_p), ("density_offset", C.c_double), ("density_offsets", C.c_void_p)]
 
 
 class Grid(C.Structure):
@@ -584,11 +584,13 @@ def _cache_option(o, cache):
 
 
 def reconstruct(cam, rp, width, height, m, dmin, dmax, index, pmoments, bounds, tf_table, precision="f32",
-                nthreads=0, rows=None, exact_atan=False, tf_bspline=False, float_bounds=None, cache=None):
+                nthreads=0, rows=None, exact_atan=False, tf_bspline=False, float_bounds=None, cache=None,
+                density_offset=0.0):
     """reconstruct_host with float RGBA: returns rgba[H,W,4].  tf_bspline / float_bounds select the
     differentiation form (transfer-function row as a cubic B-spline in the front density; unquantized
     bounds[H,W,2]).  cache = (values[z, y, x], dmin, dmax): single scattering from that transmittance cache when
-    rp.ss.enable."""
+    rp.ss.enable.  density_offset (a scalar, or one value per pixel [H, W]) is added to every reconstructed density (a
+    probe of the colour's sensitivity to the densities; 0 is the method)."""
     L = lib()
     dt = _dt(precision)
     pm = np.ascontiguousarray(pmoments, dtype=dt)
@@ -600,6 +602,12 @@ def reconstruct(cam, rp, width, height, m, dmin, dmax, index, pmoments, bounds, 
     o.tf_bspline = int(tf_bspline)
     bf = None if float_bounds is None else np.ascontiguousarray(float_bounds, dtype=dt)
     o.bounds_in = None if bf is None else bf.ctypes.data
+    offs = None
+    if np.ndim(density_offset) == 0:
+        o.density_offset = float(density_offset)
+    else:
+        offs = np.ascontiguousarray(np.broadcast_to(density_offset, (height, width)), dtype=dt)
+        o.density_offsets = offs.ctypes.data
     keep = _cache_option(o, cache)
     getattr(L, f"oracle_reconstruct_{precision}")(C.byref(cam), C.byref(rp), width, height, m,
                                                   (C.c_float * 3)(*dmin), (C.c_float * 3)(*dmax), _ptr(idx),
@@ -751,12 +759,14 @@ def preintegrate_r(tf1d, step_size, precision="f64"):
 
 
 def diff_forward(cam, gp, rp, volume, dmin, dmax, width, height, m, tf_table, precision="f64", nthreads=0,
-                 exact_atan=True):
+                 exact_atan=True, rows=None):
     """The differentiation form's forward on the CPU: generate without compaction, unquantized bounds,
     Lagrange multipliers, re-march with exact atan and the transfer-function row as a cubic B-spline in the
-    front density.  Returns rgba[H,W,4] in the working precision."""
+    front density.  Returns rgba[H,W,4] in the working precision; with rows = (begin, end, step) only those rows
+    (the others stay zero)."""
     moments, _, _, bf = generate_moments(cam, gp, volume, dmin, dmax, width, height, m, precision, nthreads,
-                                         float_bounds=True)
-    pm = prepare_moments(width, height, m, None, moments.reshape(-1), False, 1, None, rp.bias, precision, nthreads)
+                                         rows=rows, float_bounds=True)
+    pm = prepare_moments(width, height, m, None, moments.reshape(-1), False, 1, None, rp.bias, precision, nthreads,
+                         rows=rows)
     return reconstruct(cam, rp, width, height, m, dmin, dmax, None, pm, None, tf_table, precision, nthreads,
-                       exact_atan=exact_atan, tf_bspline=True, float_bounds=bf)
+                       rows=rows, exact_atan=exact_atan, tf_bspline=True, float_bounds=bf)

@@ -263,6 +263,8 @@ void *ref_grid_create(const float *vol, int nx, int ny, int nz, const float *dmi
                            std::vector<float>(vol, vol + size_t(nx) * ny * nz), RegularGrid::DataType::F32);
 }
 void ref_grid_destroy(void *grid) { delete static_cast<RegularGrid *>(grid); }
+/* the grid's own sample buffer (RegularGrid::data, the std::vector the reference's loaders fill) */
+const float *ref_grid_data(const void *grid) { return static_cast<const RegularGrid *>(grid)->data.data(); }
 
 /* The generate and reconstruct flows of main.cpp (generate() with compaction and prediction coding, the codes of
  * quantize_prediction_coding with `table`, dequantize_prediction_coding, reconstruct()) restricted to the rows

@@ -14,6 +14,7 @@ import numpy as np
 import pytest
 
 import oracle as O
+from helpers import GpuRender, pick_parameters as _pick, richardson as _richardson
 
 torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
@@ -23,38 +24,6 @@ def _workload(n=40, width=40, height=36, m=16, seed=11):
     from mray_gb300 import workloads as W
 
     return W.diff_workload(n=n, width=width, height=height, num_moments=m, seed=seed)
-
-
-class GpuRender:
-    """The GPU forward / backward of one workload on fixed device buffers."""
-
-    def __init__(self, ctx, wl):
-        self.ctx, self.wl = ctx, wl
-        W, H, m = wl.width, wl.height, wl.num_moments
-        self.moments = torch.empty(W * H * m, device="cuda")
-        self.bounds4 = torch.empty(W * H * 4, device="cuda")
-        self.pm = torch.empty(W * H * m, device="cuda")
-        self.rgba = torch.empty((H, W, 4), device="cuda")
-
-    def forward(self, volume, table):
-        wl = self.wl
-        self.vol = torch.from_numpy(np.ascontiguousarray(volume, dtype=np.float32)).cuda()
-        self.tab = torch.from_numpy(np.ascontiguousarray(table, dtype=np.float32)).cuda()
-        self.ctx.upload_grid(self.vol, wl.domain_min, wl.domain_max)
-        self.ctx.diff_forward(wl.camera, wl.gen, wl.rec, wl.width, wl.height, wl.num_moments, self.tab, self.moments,
-                              self.bounds4, self.pm, self.rgba)
-        self.ctx.synchronize()
-        return self.rgba.cpu().numpy().astype(np.float64)
-
-    def backward(self, grad_rgba, volume_grad=True):
-        wl = self.wl
-        g = torch.from_numpy(np.ascontiguousarray(grad_rgba, dtype=np.float32)).cuda()
-        gtf = torch.zeros((256, 4), device="cuda")
-        gvol = torch.zeros_like(self.vol) if volume_grad else None
-        self.ctx.diff_backward(wl.camera, wl.gen, wl.rec, wl.width, wl.height, wl.num_moments, self.tab, self.moments,
-                               self.bounds4, self.pm, self.rgba, g, gtf, gvol)
-        self.ctx.synchronize()
-        return gtf.cpu().numpy().astype(np.float64), (gvol.cpu().numpy().astype(np.float64) if volume_grad else None)
 
 
 def _oracle_rgba(wl, volume, table):
@@ -85,15 +54,6 @@ def _fd64(wl, volume, table, weights, params, eps=2.0 ** -10):
     return np.array([_richardson(loss, wl, t64, kind, idx, eps) for kind, idx in params])
 
 
-def _pick(rng, grad_vol, grad_tf, n_tf, n_vox):
-    """Seeded parameters whose gradient is not negligible (above 1 % of the largest of its kind)."""
-    tf_ok = np.argwhere(np.abs(grad_tf) > 1e-2 * np.abs(grad_tf).max())
-    vox_ok = np.argwhere(np.abs(grad_vol) > 1e-2 * np.abs(grad_vol).max())
-    params = [("tf", tuple(tf_ok[i])) for i in rng.choice(len(tf_ok), n_tf, replace=False)]
-    params += [("vox", tuple(vox_ok[i])) for i in rng.choice(len(vox_ok), n_vox, replace=False)]
-    return params
-
-
 @pytest.mark.parametrize("m", [16, 31])
 def test_adjoint_against_fp64_reference_gradient(gpu_context, m):
     wl, _ = _workload(m=m)
@@ -116,26 +76,6 @@ def _l2_setup(ctx):
     R = GpuRender(ctx, wl)
     target = R.forward(wl.volume, O.preintegrate(target_tf, wl.tf_step))
     return wl, table, R, target
-
-
-def _perturbed(wl, table, kind, idx, delta):
-    v, t = wl.volume, table
-    if kind == "vox":
-        v = wl.volume.copy()
-        v[idx] += np.float32(delta)
-    else:
-        t = table.copy()
-        t[idx] += delta
-    return v, t
-
-
-def _richardson(loss, wl, table, kind, idx, eps):
-    """Central differences at eps and 2 eps combined as (4 D(eps) - D(2 eps)) / 3, which removes their eps^2
-    truncation term: voxels near where rays enter the volume change the image strongly enough that D(1e-3) alone
-    is off by a few 1e-3."""
-    def d(e):
-        return (loss(*_perturbed(wl, table, kind, idx, e)) - loss(*_perturbed(wl, table, kind, idx, -e))) / (2 * e)
-    return (4.0 * d(eps) - d(2 * eps)) / 3.0
 
 
 def test_l2_adjoint_against_fp64_central_differences(gpu_context):

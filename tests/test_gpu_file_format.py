@@ -156,6 +156,15 @@ def test_large_image_round_trips(gpu_context):
                            (np.array([16] + [14, 12, 11] + [10] * 20 + [8] * 40, np.uint8), True)):
         packed = O.quantize_prediction_coding(wl.width, wl.height, 64, mi.index, mi.data, table)
         want = O.dequantize_prediction_coding(wl.width, wl.height, 64, mi.index, table, packed, mi.data.size)
+        if entropy:
+            # the packed stream drops its trailing partial byte (pack_bits, moment_quantization.cpp:92-114), so the
+            # last code or two read back as 0 there; the entropy coder keeps every code whole
+            cut = np.flatnonzero(O.unpack_codes(wl.width, wl.height, 64, mi.index, table, packed) < 0)
+            syms = O.entropy_codes(wl.width, wl.height, 64, mi.index, mi.data, table, True)
+            last = mi.index[np.searchsorted(mi.index, cut, side="right") - 1]
+            want = want.copy()
+            for i, l in zip(cut, cut - last):
+                want[i] = O.lib().oracle_dequantize(int(syms[i]), int(table[l]), 0.0, 1.0)
         for compress in (False, True):
             blob = gpu_context.encode_moment_image(mi, compress, 10, entropy, table)
             back, t = gpu_context.decode_moment_image(blob)
