@@ -619,7 +619,10 @@ def run_e2e(args, ctx, hl, dist):
     P = W * H
     ctx.precision = M.PRECISION_COMPENSATED_FF_MESE
     vol_np = hl.volume.numpy() if hasattr(hl.volume, "numpy") else hl.volume
-    grid = M.RegularGrid(vol_np, hl.domain_min, hl.domain_max)
+    # the step's input in pinned host memory, as the reference's pinned-host uploads would hold it
+    vol_pinned = torch.empty(vol_np.shape, dtype=torch.float32).pin_memory().numpy()
+    vol_pinned[...] = vol_np
+    grid = M.RegularGrid(vol_pinned, hl.domain_min, hl.domain_max)
     mi = M.MomentImageHost(W, H, m, True, True)
     data_full = torch.empty(P * m, dtype=torch.float32).pin_memory().numpy()
     mi.index = torch.empty(P + 1, dtype=torch.int32).pin_memory().numpy().view(np.uint32)

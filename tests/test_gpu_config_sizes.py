@@ -19,7 +19,7 @@ import numpy as np
 import pytest
 
 import oracle as O
-from helpers import fp64_sensitivity, moment_rel_err, rgba_agreement
+from helpers import fp32_density_bound, fp64_sensitivity, moment_rel_err, rgba_agreement
 
 torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
@@ -244,9 +244,9 @@ def test_config3_adjoint_against_gpu_central_differences(gpu_context):
     assert rel.max() <= 1e-2, f"max rel err {rel.max():.3e} at {params[int(rel.argmax())]}"
 
 
-def _colour(wl, mo, bo, co, precision, rows, sensitivity=False):
+def _colour(wl, mo, bo, co, precision, rows, sensitivity=False, delta=1e-5):
     """Compaction, multipliers and re-march of the given moments in the given precision on the sampled rows (and,
-    when asked, the FP64 colour's sensitivity to a +-1e-5 shift of the densities)."""
+    when asked, the FP64 colour's sensitivity to a +-delta shift of the densities, delta a scalar or per pixel)."""
     W, H, m = wl.width, wl.height, wl.num_moments
     idx, _ = O.compact(co, mo.astype(np.float32))
     data = mo.reshape(-1, m)[co.reshape(-1) > 0].reshape(-1)
@@ -256,7 +256,8 @@ def _colour(wl, mo, bo, co, precision, rows, sensitivity=False):
                          rows=rows)
     if not sensitivity:
         return rgba
-    return rgba, fp64_sensitivity(wl.camera, wl.rec, W, H, m, wl.domain_min, wl.domain_max, idx, pm, bo, tf, rows)
+    return rgba, fp64_sensitivity(wl.camera, wl.rec, W, H, m, wl.domain_min, wl.domain_max, idx, pm, bo, tf, rows,
+                                  delta=delta)
 
 
 def test_config5_sph_sampled_rows(gpu_context):
@@ -264,7 +265,8 @@ def test_config5_sph_sampled_rows(gpu_context):
     so 256^3 cells; 1024^2 perspective, 64 moments) on every 64th row (16 rows of 1024 pixels): the GPU bins the
     particles and renders the whole image, the oracle bins them the reference's way and renders the sampled rows.
     Bars: bounds and counts exact; moments within 1e-4 of the reference's FP32 moments widened by its own FP32 error,
-    and no further from the FP64 oracle than that; every sampled pixel's colour within the RGBA bar."""
+    and no further from the FP64 oracle than that; every sampled pixel's colour within the RGBA bar, its jump clause
+    with a density shift of the size of the FP32 errors of the moments and of the MESE series."""
     import mray_gb300 as M
     from mray_gb300 import workloads as W_
 
@@ -311,9 +313,18 @@ def test_config5_sph_sampled_rows(gpu_context):
     same = hit & np.all(b32 == b64, axis=-1)
     err64 = moment_rel_err(mo, m64, m64[..., 0])
     assert np.all(err64[same] <= 1e-4 + own[same]), f"max excess vs f64 {(err64 - own)[same].max():.3e}"
+    # The jump clause of the RGBA bar with a density shift per pixel of the larger of: our moments' distance from
+    # FP64 (relative to m_0, times the density span), and how far any FP32 evaluation of the MESE series can move
+    # the density (helpers.fp32_density_bound from the reference's FP32 multipliers: ~1e-5 on most pixels, up to
+    # a few 1e-2 on the 1 % whose multipliers reach 1e4 and cancel).
+    span = (b64[..., 1].astype(np.float64) - b64[..., 0]) / 65535.0
+    idx32, _ = O.compact(c32, m32)
+    pm32 = O.prepare_moments(W, H, m, idx32, m32.reshape(-1, m)[c32.reshape(-1) > 0].reshape(-1), False, 1, None,
+                             wl.rec.bias, "f32", rows=rows)
+    delta = np.maximum(fp32_density_bound(W, H, m, idx32, pm32, b32), np.where(same, err64 * span, 0.0))
     err64, own64 = err64[same], own[same]
     rgba32 = _colour(wl, m32, b32, c32, "f32", rows)
-    rgba64, sens = _colour(wl, m64, b64, c64, "f64", rows, sensitivity=True)
+    rgba64, sens = _colour(wl, m64, b64, c64, "f64", rows, sensitivity=True, delta=delta)
     ok = rgba_agreement(rgba[sel], rgba32[sel], rgba64[sel], RGBA_TOL, sens[sel])
     d64 = np.abs(rgba[sel].astype(np.float64) - rgba64[sel]).max(axis=-1)
     d32 = np.abs(rgba32[sel].astype(np.float64) - rgba64[sel]).max(axis=-1)
