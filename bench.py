@@ -1104,6 +1104,30 @@ def run_sph(args, local):
 
     ms = timed(fwd_bwd)
     out["diff_fwd_tf_adjoint"] = {"value": P / (ms * 1e-3) / 1e6, "unit": UNIT, "ms": ms}
+
+    # the configuration's own text: a smoothing length per particle (0.005-0.02) with the Wendland C2 kernel, a
+    # variant the reference does not have (parity unpinned: checked against the oracle's restatement)
+    wv = W.sph_wendland_workload(n=n, width=Wd, height=H, num_moments=m, seed=31)
+    hs = torch.from_numpy(wv.h).cuda()
+    e = _events(1)[0]
+    e[0].record(stream)
+    ctx.upload_particles_h(*xs[:4], hs, dmin, dmax)
+    e[1].record(stream)
+    ctx.synchronize()
+    build_ms = e[0].elapsed_time(e[1])
+    wl.gen.compact_image = 1
+    saved = (wl.gen.step_size, wl.rec.step_size, args.steps, args.warmup)
+    wl.gen.step_size, wl.rec.step_size = wv.gen.step_size, wv.rec.step_size
+    args.steps, args.warmup = 1, 1
+    ms = timed(fwd)
+    wl.gen.step_size, wl.rec.step_size, args.steps, args.warmup = saved
+    out["wendland_variant"] = {
+        "workload": wv.name, "grid_build_ms": build_ms,
+        "particles": f"{n} particles as above, smoothing length per particle uniform in [0.005, 0.02], Wendland C2 "
+                     "kernel, grid cell size = the largest smoothing length, step 2^-9",
+        "parity": "unpinned: the reference has no per-particle smoothing length; checked against the oracle's "
+                  "restatement (tests/test_gpu_particles.py, tests/test_oracle_wendland.py)",
+        "fwd_fp32": {"value": P / (ms * 1e-3) / 1e6, "unit": UNIT, "ms": ms}}
     ctx.close()
     return out
 

@@ -105,6 +105,16 @@ int mraygb_upload_grid(mraygb_context *ctx, const float *data, int nx, int ny, i
 int mraygb_upload_particles(mraygb_context *ctx, const float *x, const float *y, const float *z, const float *v,
                             uint64_t n, float h, const float dmin[3], const float dmax[3], int data_on_device);
 
+/* SPH particles with a smoothing length per particle h[i] (n floats, host or device like x, y, z, v; each finite
+ * and > 0) and the Wendland C2 kernel W(q) ~ (1 - q)^4 (1 + 4q) / h^3 for q = r / h < 1: a variant that the
+ * reference does not have (its Particles carry one smoothing length and the cubic spline), so its parity is
+ * checked against the oracle's restatement only.  The grid is the reference's grid with the largest h as its cell
+ * size; samples are sum W v / sum W over the 27 neighbour cells, as the reference's sampler normalises.
+ * Generation (mraygb_generate / mraygb_stage_generate_moments) samples it; the error-bound and reference
+ * renderers return MRAYGB_NOT_SUPPORTED for it. */
+int mraygb_upload_particles_h(mraygb_context *ctx, const float *x, const float *y, const float *z, const float *v,
+                              const float *h, uint64_t n, const float dmin[3], const float dmax[3], int data_on_device);
+
 /* The transfer-function table that reconstruction samples: 256 RGBA float entries of one row of
  * TransferFunction::data (src/transfer_function.h:30-60).  read_from_disk / preintegrate build tables whose
  * 256 rows are all equal (src/transfer_function.cpp:46-97), so one row is the whole table. */

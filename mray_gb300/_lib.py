@@ -20,7 +20,7 @@ STATUS = {0: "OK", 1: "INVALID_ARGUMENT", 2: "OUT_OF_MEMORY", 3: "CUDA_ERROR", 4
 # every symbol include/mraygb.h declares
 EXPORTS = [
     "mraygb_create", "mraygb_destroy", "mraygb_last_error", "mraygb_set_stream", "mraygb_get_stream",
-    "mraygb_synchronize", "mraygb_set_precision", "mraygb_kernel_launches", "mraygb_upload_grid", "mraygb_upload_particles",
+    "mraygb_synchronize", "mraygb_set_precision", "mraygb_kernel_launches", "mraygb_upload_grid", "mraygb_upload_particles", "mraygb_upload_particles_h",
     "mraygb_upload_tf",
     "mraygb_generate", "mraygb_reconstruct", "mraygb_stage_generate_moments", "mraygb_stage_compact",
     "mraygb_stage_prepare_moments", "mraygb_stage_reconstruct", "mraygb_quantize_prediction_coding",
@@ -66,6 +66,7 @@ def _declare(L):
     L.mraygb_kernel_launches.restype = C.c_uint64
     L.mraygb_upload_grid.argtypes = [vp, vp, i, i, i, C.c_float * 3, C.c_float * 3, i]
     L.mraygb_upload_particles.argtypes = [vp, vp, vp, vp, vp, C.c_uint64, C.c_float, C.c_float * 3, C.c_float * 3, i]
+    L.mraygb_upload_particles_h.argtypes = [vp, vp, vp, vp, vp, vp, C.c_uint64, C.c_float * 3, C.c_float * 3, i]
     L.mraygb_upload_tf.argtypes = [vp, vp]
     L.mraygb_generate.argtypes = [vp, P(Camera), P(GenerationParameters), i, i, i, vp, vp, vp, vp,
                                   P(C.c_uint64)]

@@ -82,6 +82,9 @@ struct mraygb_context
     DeviceBuffer particle_pts, particle_cells;
     ParticleGridParams particle_grid{};
     uint64_t num_particles = 0;
+    // per-particle smoothing lengths with the Wendland C2 kernel (mraygb_upload_particles_h): (1/h, 1/h^3) per record
+    DeviceBuffer particle_inv_h;
+    bool particle_wendland = false;
     DeviceBuffer tf;
     bool has_tf = false;
 
@@ -187,6 +190,8 @@ GridView grid_view(const mraygb_context *ctx)
     return g;
 }
 
+ParticleHView particle_h_view(const mraygb_context *ctx);
+
 ParticleView particle_view(const mraygb_context *ctx)
 {
     ParticleView v;
@@ -198,6 +203,14 @@ ParticleView particle_view(const mraygb_context *ctx)
         v.dmin[i] = ctx->dmin[i];
         v.dmax[i] = ctx->dmax[i];
     }
+    return v;
+}
+
+ParticleHView particle_h_view(const mraygb_context *ctx)
+{
+    ParticleHView v;
+    static_cast<ParticleView &>(v) = particle_view(ctx);
+    v.inv_h = ctx->particle_inv_h.as<float2>();
     return v;
 }
 
@@ -269,7 +282,11 @@ int run_generate_moments(mraygb_context *ctx, const mraygb_camera *cam, const mr
 {
     const DeviceCamera dc = to_device_camera(*cam);
     const bool kahan = ctx->precision != MRAYGB_PRECISION_FP32;
-    if (ctx->volume == mraygb_context::PARTICLES)
+    if (ctx->volume == mraygb_context::PARTICLES && ctx->particle_wendland)
+        CK(launch_generate_particles_h(particle_h_view(ctx), dc, *gp, width, height, m, kahan, d_moments, d_bounds,
+                                       d_counts, d_bounds4, ctx->error_flag.as<int>(), ctx->stream),
+           "generate kernel launch");
+    else if (ctx->volume == mraygb_context::PARTICLES)
         CK(launch_generate_particles(particle_view(ctx), dc, *gp, width, height, m, kahan, d_moments, d_bounds,
                                      d_counts, d_bounds4, ctx->error_flag.as<int>(), ctx->stream),
            "generate kernel launch");
@@ -555,6 +572,8 @@ int run_error_bounds(mraygb_context *ctx, const mraygb_camera *cam, const mraygb
     a.percentile = ep->error_percentile;
     a.error_bounds = d_error_bounds;
     a.errors = d_errors;
+    if (ctx->volume == mraygb_context::PARTICLES && ctx->particle_wendland)
+        return fail(ctx, MRAYGB_NOT_SUPPORTED, "error bounds over particles with per-particle smoothing lengths");
     if (ctx->volume == mraygb_context::PARTICLES)
         CK(launch_error_bounds_particles(particle_view(ctx), a, ep->error_type, ctx->error_flag.as<int>(), ctx->stream),
            "error bound launch");
@@ -653,6 +672,8 @@ int run_reference(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_re
     const GridView cache = ss_cache_view(ctx);
     if (use_cache)
         a.ss_cache = &cache;
+    if (ctx->volume == mraygb_context::PARTICLES && ctx->particle_wendland)
+        return fail(ctx, MRAYGB_NOT_SUPPORTED, "the reference renderer over particles with per-particle smoothing lengths");
     if (ctx->volume == mraygb_context::PARTICLES)
         CK(launch_reference_particles(particle_view(ctx), a, ctx->error_flag.as<int>(), ctx->stream),
            "reference launch");
@@ -839,15 +860,21 @@ int mraygb_upload_grid(mraygb_context *ctx, const float *data, int nx, int ny, i
     return MRAYGB_OK;
 }
 
-int mraygb_upload_particles(mraygb_context *ctx, const float *x, const float *y, const float *z, const float *v,
-                            uint64_t n, float h, const float dmin[3], const float dmax[3], int data_on_device)
+namespace
+{
+
+// the particle upload of both forms: one smoothing length h (hs == NULL, the reference's), or one per particle
+// (hs, Wendland C2; the grid's cell size is then the largest of them)
+int upload_particles(mraygb_context *ctx, const float *x, const float *y, const float *z, const float *v,
+                     const float *hs, uint64_t n, float h, const float dmin[3], const float dmax[3],
+                     int data_on_device)
 {
     CHECK_CTX();
     if (!x || !y || !z || !v || !dmin || !dmax)
         return fail(ctx, MRAYGB_INVALID_ARGUMENT, "NULL particle array or domain");
     if (n == 0 || n > (1ull << 31))
         return fail(ctx, MRAYGB_INVALID_ARGUMENT, "particle count %llu outside 1..2^31", (unsigned long long)n);
-    if (!(h > 0.f) || !std::isfinite(h))
+    if (!hs && (!(h > 0.f) || !std::isfinite(h)))
         return fail(ctx, MRAYGB_INVALID_ARGUMENT, "smoothing length must be finite and > 0 (got %g)", (double)h);
     for (int i = 0; i < 3; ++i)
         if (!(dmax[i] > dmin[i]))
@@ -868,19 +895,35 @@ int mraygb_upload_particles(mraygb_context *ctx, const float *x, const float *y,
         }
     } release{{&stage, &keys, &keys_alt, &vals, &vals_alt, &counts, &hist, &hist_scan, &minmax}};
 
-    const float *dx = x, *dy = y, *dz = z, *dv = v;
+    const int arrays = hs ? 5 : 4;
+    const float *dx = x, *dy = y, *dz = z, *dv = v, *dh = hs;
     if (!data_on_device)
     {
-        CK(stage.reserve(4 * n * sizeof(float)), "particle staging allocation");
+        CK(stage.reserve(arrays * n * sizeof(float)), "particle staging allocation");
         float *s = stage.as<float>();
-        const float *src[4] = {x, y, z, v};
-        for (int k = 0; k < 4; ++k)
+        const float *src[5] = {x, y, z, v, hs};
+        for (int k = 0; k < arrays; ++k)
             CK(cudaMemcpyAsync(s + k * n, src[k], n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream),
                "particle upload");
         dx = s;
         dy = s + n;
         dz = s + 2 * n;
         dv = s + 3 * n;
+        dh = hs ? s + 4 * n : nullptr;
+    }
+    if (dh)
+    {
+        // the largest smoothing length sets the cell size; every one must be finite and > 0
+        CK(minmax.reserve(2 * sizeof(unsigned int)), "particle scratch allocation");
+        CK(launch_particle_h_range(n, dh, minmax.as<unsigned int>(), ctx->stream), "smoothing length kernel");
+        unsigned int hr[2];
+        CK(cudaMemcpyAsync(hr, minmax.ptr, sizeof(hr), cudaMemcpyDeviceToHost, ctx->stream),
+           "reading the smoothing lengths");
+        CK(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+        ctx->launches += 1;
+        if (hr[1])
+            return fail(ctx, MRAYGB_INVALID_ARGUMENT, "%u smoothing lengths are not finite and > 0", hr[1]);
+        std::memcpy(&h, &hr[0], sizeof(float));
     }
 
     // 1. bounding box of the particles -> grid parameters (createGridFromDomain)
@@ -936,6 +979,18 @@ int mraygb_upload_particles(mraygb_context *ctx, const float *x, const float *y,
     CK(launch_particle_gather(n, order, dx, dy, dz, dv, ctx->particle_pts.as<float4>(), ctx->stream),
        "particle gather kernel");
     launches += 1;
+    if (dh)
+    {
+        CK(ctx->particle_inv_h.reserve(n * sizeof(float2)), "smoothing length allocation");
+        CK(launch_particle_gather_h(n, order, dh, ctx->particle_inv_h.as<float2>(), ctx->stream),
+           "smoothing length gather kernel");
+        launches += 1;
+    }
+    else
+    {
+        ctx->particle_inv_h.release();
+    }
+    ctx->particle_wendland = dh != nullptr;
     CK(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
     ctx->launches += (uint64_t)launches;
 
@@ -949,6 +1004,22 @@ int mraygb_upload_particles(mraygb_context *ctx, const float *x, const float *y,
     ctx->volume = mraygb_context::PARTICLES;
     release_grid(ctx);
     return MRAYGB_OK;
+}
+
+} // namespace
+
+int mraygb_upload_particles(mraygb_context *ctx, const float *x, const float *y, const float *z, const float *v,
+                            uint64_t n, float h, const float dmin[3], const float dmax[3], int data_on_device)
+{
+    return upload_particles(ctx, x, y, z, v, nullptr, n, h, dmin, dmax, data_on_device);
+}
+
+int mraygb_upload_particles_h(mraygb_context *ctx, const float *x, const float *y, const float *z, const float *v,
+                              const float *h, uint64_t n, const float dmin[3], const float dmax[3], int data_on_device)
+{
+    if (ctx && !h)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "NULL smoothing length array");
+    return upload_particles(ctx, x, y, z, v, h, n, 0.f, dmin, dmax, data_on_device);
 }
 
 int mraygb_upload_tf(mraygb_context *ctx, const float *table)

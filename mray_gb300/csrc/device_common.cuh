@@ -309,6 +309,67 @@ __device__ __forceinline__ float particle_sample(const ParticleView &v, float px
     return value;
 }
 
+// SPH particles with a smoothing length per particle and the Wendland C2 kernel (this build's variant: the
+// reference's particles carry one smoothing length and the cubic spline).  The grid is the reference's grid with
+// the largest smoothing length as its cell size, so the 27 cells around a point hold every particle whose support
+// (radius h_i, as the reference's radius test uses h) contains it.  Per record (1 / h_i, 1 / h_i^3).
+struct ParticleHView : ParticleView
+{
+    const float2 *inv_h;
+};
+
+// W(q) h^3 up to the constant 21 / (2 pi), which the normalised sum cancels: (1 - q)^4 (1 + 4 q) for q < 1
+__device__ __forceinline__ float wendland_c2(float q)
+{
+    const float u = __fsub_rn(1.f, q);
+    const float u2 = __fmul_rn(u, u);
+    return __fmul_rn(__fmul_rn(u2, u2), __fadd_rn(__fmul_rn(4.f, q), 1.f));
+}
+
+// sum_i W(|p - x_i|, h_i) v_i / sum_i W(|p - x_i|, h_i) over the 27 cells in z, y, x order and the cells' order
+__device__ __forceinline__ float particle_sample_h(const ParticleHView &v, float px, float py, float pz)
+{
+    const float p[3] = {px, py, pz};
+    const int s[3] = {v.g.sx, v.g.sy, v.g.sz};
+    int lo[3], hi[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+    {
+        int c = (int)__fmul_rn(__fsub_rn(p[k], v.g.gmin[k]), v.g.inv_cell);
+        c = c < -2 ? -2 : (c > s[k] + 1 ? s[k] + 1 : c);
+        lo[k] = c - 1 > 0 ? c - 1 : 0;
+        hi[k] = c + 2 < s[k] ? c + 2 : s[k];
+    }
+    float value = 0.f, wsum = 0.f;
+    for (int z = lo[2]; z < hi[2]; ++z)
+        for (int y = lo[1]; y < hi[1]; ++y)
+            for (int x = lo[0]; x < hi[0]; ++x)
+            {
+                const uint32_t cell = particle_cell_index(v.g, x, y, z);
+                const uint32_t b = __ldg(v.cell_start + cell), e = __ldg(v.cell_start + cell + 1);
+                for (uint32_t i = b; i < e; ++i)
+                {
+                    const float4 q = __ldg(v.pts + i);
+                    const float dx = __fsub_rn(px, q.x), dy = __fsub_rn(py, q.y), dz = __fsub_rn(pz, q.z);
+                    const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+                    if (d2 < v.g.r2)
+                    {
+                        const float2 ih = __ldg(v.inv_h + i);
+                        const float r = __fmul_rn(__fsqrt_rn(d2), ih.x);
+                        if (r < 1.f)
+                        {
+                            const float w = __fmul_rn(wendland_c2(r), ih.y);
+                            wsum = __fadd_rn(wsum, w);
+                            value = __fadd_rn(value, __fmul_rn(w, q.w));
+                        }
+                    }
+                }
+            }
+    if (wsum != 0.f)
+        value = __fdiv_rn(value, wsum);
+    return value;
+}
+
 // the two volumes behind one generate kernel: the ray box and one sample
 __device__ __forceinline__ float volume_sample(const GridView &g, float x, float y, float z)
 {
@@ -317,6 +378,10 @@ __device__ __forceinline__ float volume_sample(const GridView &g, float x, float
 __device__ __forceinline__ float volume_sample(const ParticleView &v, float x, float y, float z)
 {
     return particle_sample(v, x, y, z);
+}
+__device__ __forceinline__ float volume_sample(const ParticleHView &v, float x, float y, float z)
+{
+    return particle_sample_h(v, x, y, z);
 }
 
 __device__ __forceinline__ float map_density(float s, float dmin, float dmax)

@@ -398,6 +398,12 @@ __global__ void __launch_bounds__(128) generate_particles_kernel(const GenArgs<P
     generate_quads<ParticleView, NJ, KAHAN>(a);
 }
 
+template <int NJ, bool KAHAN>
+__global__ void __launch_bounds__(128) generate_particles_h_kernel(const GenArgs<ParticleHView> a)
+{
+    generate_quads<ParticleHView, NJ, KAHAN>(a);
+}
+
 template <int NJ, bool KAHAN> void launch_kernel(const GenArgs<GridView> &a, dim3 grid, cudaStream_t stream)
 {
     generate_grid_kernel<NJ, KAHAN><<<grid, 128, 0, stream>>>(a);
@@ -405,6 +411,10 @@ template <int NJ, bool KAHAN> void launch_kernel(const GenArgs<GridView> &a, dim
 template <int NJ, bool KAHAN> void launch_kernel(const GenArgs<ParticleView> &a, dim3 grid, cudaStream_t stream)
 {
     generate_particles_kernel<NJ, KAHAN><<<grid, 128, 0, stream>>>(a);
+}
+template <int NJ, bool KAHAN> void launch_kernel(const GenArgs<ParticleHView> &a, dim3 grid, cudaStream_t stream)
+{
+    generate_particles_h_kernel<NJ, KAHAN><<<grid, 128, 0, stream>>>(a);
 }
 
 template <int NJ, class V> void launch_nj(const GenArgs<V> &a, bool kahan, cudaStream_t stream)
@@ -474,6 +484,15 @@ cudaError_t launch_generate_particles(const ParticleView &parts, const DeviceCam
                                       const mraygb_generation_params &gp, int width, int height, int m, bool kahan,
                                       float *moments, uint16_t *bounds, uint32_t *counts, float4 *bounds4,
                                       int *error_flag, cudaStream_t stream)
+{
+    return launch_generate(parts, cam, gp, width, height, m, kahan, moments, bounds, counts, bounds4, error_flag,
+                           stream);
+}
+
+cudaError_t launch_generate_particles_h(const ParticleHView &parts, const DeviceCamera &cam,
+                                        const mraygb_generation_params &gp, int width, int height, int m, bool kahan,
+                                        float *moments, uint16_t *bounds, uint32_t *counts, float4 *bounds4,
+                                        int *error_flag, cudaStream_t stream)
 {
     return launch_generate(parts, cam, gp, width, height, m, kahan, moments, bounds, counts, bounds4, error_flag,
                            stream);

@@ -11,6 +11,7 @@ namespace mraygb
 
 struct GridView;
 struct ParticleView;
+struct ParticleHView;
 struct ParticleGridParams;
 struct DeviceCamera;
 
@@ -23,6 +24,10 @@ cudaError_t launch_generate_particles(const ParticleView &parts, const DeviceCam
                                       const mraygb_generation_params &gp, int width, int height, int m, bool kahan,
                                       float *moments, uint16_t *bounds, uint32_t *counts, float4 *bounds4,
                                       int *error_flag, cudaStream_t stream);
+cudaError_t launch_generate_particles_h(const ParticleHView &parts, const DeviceCamera &cam,
+                                        const mraygb_generation_params &gp, int width, int height, int m, bool kahan,
+                                        float *moments, uint16_t *bounds, uint32_t *counts, float4 *bounds4,
+                                        int *error_flag, cudaStream_t stream);
 
 // particles.cu: the particle grid build
 ParticleGridParams particle_grid_params(const float mn[3], const float mx[3], float h);
@@ -42,6 +47,11 @@ cudaError_t launch_particle_sort(uint32_t n, uint32_t total, uint32_t *keys, uin
                                  uint32_t *vals_alt, uint32_t *hist, uint32_t *hist_scan, uint32_t *scan_scratch,
                                  uint32_t **sorted_vals, cudaStream_t stream, int *launches);
 // pts[i] = (x, y, z, v)[order[i]]
+// per-particle smoothing lengths: out2 = (bits of the largest valid h, count of h not finite and > 0); the records'
+// (1 / h, 1 / h^3) in sorted order
+cudaError_t launch_particle_h_range(uint64_t n, const float *h, unsigned int *out2, cudaStream_t stream);
+cudaError_t launch_particle_gather_h(uint64_t n, const uint32_t *order, const float *h, float2 *inv_h,
+                                     cudaStream_t stream);
 cudaError_t launch_particle_gather(uint64_t n, const uint32_t *order, const float *x, const float *y, const float *z,
                                    const float *v, float4 *pts, cudaStream_t stream);
 

@@ -187,6 +187,40 @@ __global__ void gather_kernel(uint64_t n, const uint32_t *__restrict__ order, co
     }
 }
 
+// per-particle smoothing lengths: the largest (its bits: h > 0, so the float order is the integer order) and a
+// count of those that are not finite and > 0
+__global__ void h_range_kernel(uint64_t n, const float *__restrict__ h, unsigned int *__restrict__ out2)
+{
+    unsigned int mx = 0, bad = 0;
+    for (uint64_t i = (uint64_t)blockIdx.x * kThreads + threadIdx.x; i < n; i += (uint64_t)gridDim.x * kThreads)
+    {
+        const float v = h[i];
+        if (v > 0.f && v <= 3.402823466e38f)
+            mx = max(mx, __float_as_uint(v));
+        else
+            ++bad;
+    }
+    mx = __reduce_max_sync(0xffffffffu, mx);
+    bad = __reduce_add_sync(0xffffffffu, bad);
+    if ((threadIdx.x & 31) == 0)
+    {
+        atomicMax(out2, mx);
+        if (bad)
+            atomicAdd(out2 + 1, bad);
+    }
+}
+
+// (1 / h, 1 / h^3) of every record, in the records' (sorted) order
+__global__ void gather_h_kernel(uint64_t n, const uint32_t *__restrict__ order, const float *__restrict__ h,
+                                float2 *__restrict__ inv_h)
+{
+    for (uint64_t i = (uint64_t)blockIdx.x * kThreads + threadIdx.x; i < n; i += (uint64_t)gridDim.x * kThreads)
+    {
+        const float v = h[order[i]];
+        inv_h[i] = make_float2(__fdiv_rn(1.f, v), __fdiv_rn(1.f, __fmul_rn(__fmul_rn(v, v), v)));
+    }
+}
+
 unsigned grid_blocks(uint64_t n)
 {
     const uint64_t b = (n + kThreads - 1) / kThreads;
@@ -279,6 +313,22 @@ cudaError_t launch_particle_sort(uint32_t n, uint32_t total, uint32_t *keys, uin
     }
     *sorted_vals = vin;
     return cudaSuccess;
+}
+
+cudaError_t launch_particle_h_range(uint64_t n, const float *h, unsigned int *out2, cudaStream_t stream)
+{
+    cudaError_t e = cudaMemsetAsync(out2, 0, 2 * sizeof(unsigned int), stream);
+    if (e != cudaSuccess)
+        return e;
+    h_range_kernel<<<grid_blocks(n), kThreads, 0, stream>>>(n, h, out2);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_particle_gather_h(uint64_t n, const uint32_t *order, const float *h, float2 *inv_h,
+                                     cudaStream_t stream)
+{
+    gather_h_kernel<<<grid_blocks(n), kThreads, 0, stream>>>(n, order, h, inv_h);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_particle_gather(uint64_t n, const uint32_t *order, const float *x, const float *y, const float *z,

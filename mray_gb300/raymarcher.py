@@ -296,6 +296,21 @@ class Context:
         self._check(self._L.mraygb_upload_particles(self._h, *ptrs, n, float(smoothing_length), _f3(domain_min),
                                                     _f3(domain_max), on_device))
 
+    def upload_particles_h(self, x, y, z, v, h, domain_min, domain_max) -> None:
+        """SPH particles with a smoothing length per particle (five float32 arrays: numpy arrays or CUDA tensors)
+        and the Wendland C2 kernel (mraygb_upload_particles_h); they replace an uploaded volume."""
+        if hasattr(x, "data_ptr"):
+            n = x.numel()
+            ptrs = [_dptr(a) for a in (x, y, z, v, h)]
+            on_device = 1
+        else:
+            arrs = [np.ascontiguousarray(a, dtype=np.float32) for a in (x, y, z, v, h)]
+            n = arrs[0].size
+            ptrs = [_hptr(a) for a in arrs]
+            on_device = 0
+        self._check(self._L.mraygb_upload_particles_h(self._h, *ptrs, n, _f3(domain_min), _f3(domain_max),
+                                                      on_device))
+
     def upload_tf(self, table) -> None:
         t = np.ascontiguousarray(table, dtype=np.float32)
         if t.shape != (256, 4):

@@ -306,6 +306,21 @@ def sph_workload(n: int = 20000, h: float = 1.0 / 32, width: int = 64, height: i
                             transfer_function(seed + 1), tf_step=0.05)
 
 
+def sph_wendland_workload(n: int = 16_000_000, h_range=(0.005, 0.02), width: int = 1024, height: int = 1024,
+                          num_moments: int = 64, seed: int = 31) -> ParticleWorkload:
+    """The SPH configuration as its text states it, a variant the reference does not have: the particles of
+    :func:`sph_cluster_workload` with a seeded smoothing length per particle, uniform in ``h_range``, and the Wendland
+    C2 kernel (``Context.upload_particles_h``).  Step 2^-9, below half the smallest smoothing length; ``h`` holds the
+    per-particle array."""
+    wl = sph_cluster_workload(n=n, h=1.0 / 256, width=width, height=height, num_moments=num_moments, seed=seed)
+    rng = np.random.default_rng(seed + 11)
+    wl.h = rng.uniform(h_range[0], h_range[1], size=n).astype(np.float32)
+    wl.gen.step_size = 2.0 ** -9
+    wl.rec.step_size = 2.0 ** -9
+    wl.name = f"sph{n}_wendland_h{h_range[0]:g}-{h_range[1]:g}_{width}x{height}_m{num_moments}_persp"
+    return wl
+
+
 def sph_cluster_workload(n: int = 16_000_000, h: float = 1.0 / 256, width: int = 1024, height: int = 1024,
                          num_moments: int = 64, seed: int = 31) -> ParticleWorkload:
     """The SPH configuration: n particles (70 % uniform, 30 % in 200 seeded Gaussian clusters, LogNormal(0, 0.5)

@@ -87,8 +87,30 @@ static int cmp_cell_key(const void *a, const void *b)
     return x->index < y->index ? -1 : (x->index > y->index ? 1 : 0);
 }
 
+static oracle_particles *particles_build(const float *x, const float *y, const float *z, const float *v,
+                                         const float *hs, uint64_t n, float h, const float dmin[3],
+                                         const float dmax[3]);
+
 oracle_particles *oracle_particles_create(const float *x, const float *y, const float *z, const float *v, uint64_t n,
                                           float h, const float dmin[3], const float dmax[3])
+{
+    return particles_build(x, y, z, v, NULL, n, h, dmin, dmax);
+}
+
+oracle_particles *oracle_particles_create_h(const float *x, const float *y, const float *z, const float *v,
+                                            const float *hs, uint64_t n, const float dmin[3], const float dmax[3])
+{
+    if (n == 0 || !hs)
+        return NULL;
+    float h = hs[0];
+    for (uint64_t i = 1; i < n; ++i)
+        h = hs[i] > h ? hs[i] : h;
+    return particles_build(x, y, z, v, hs, n, h, dmin, dmax);
+}
+
+static oracle_particles *particles_build(const float *x, const float *y, const float *z, const float *v,
+                                         const float *hs, uint64_t n, float h, const float dmin[3],
+                                         const float dmax[3])
 {
     if (n == 0)
         return NULL;
@@ -142,6 +164,7 @@ oracle_particles *oracle_particles_create(const float *x, const float *y, const 
     P->y = (float *)malloc(sizeof(float) * n);
     P->z = (float *)malloc(sizeof(float) * n);
     P->v = (float *)malloc(sizeof(float) * n);
+    P->hh = hs ? (float *)malloc(sizeof(float) * n) : NULL;
     P->cell_start = (uint32_t *)calloc((size_t)P->total + 1, sizeof(uint32_t));
     for (uint64_t i = 0; i < n; ++i)
     {
@@ -150,6 +173,8 @@ oracle_particles *oracle_particles_create(const float *x, const float *y, const 
         P->y[i] = y[j];
         P->z[i] = z[j];
         P->v[i] = v[j];
+        if (hs)
+            P->hh[i] = hs[j];
         P->cell_start[keys[i].cell + 1] += 1;
     }
     for (uint32_t c = 0; c < P->total; ++c)
@@ -166,6 +191,7 @@ void oracle_particles_destroy(oracle_particles *P)
     free(P->y);
     free(P->z);
     free(P->v);
+    free(P->hh);
     free(P->cell_start);
     free(P);
 }

@@ -52,10 +52,16 @@ typedef struct oracle_particles
     int sx, sy, sz, tz;
     uint32_t total;
     uint32_t *cell_start; /* total + 1 */
+    float *hh;            /* per-particle smoothing lengths, sorted like x (Wendland C2 variant), or NULL */
 } oracle_particles;
 
 oracle_particles *oracle_particles_create(const float *x, const float *y, const float *z, const float *v, uint64_t n,
                                           float h, const float dmin[3], const float dmax[3]);
+/* The variant with a smoothing length per particle and the Wendland C2 kernel (not in the reference, whose
+ * particles carry one smoothing length): the same grid with the largest h as its cell size; a particle contributes
+ * (1 - q)^4 (1 + 4q) / h^3 at q = r / h < 1 (and r^2 below the largest h squared, the cells' radius test). */
+oracle_particles *oracle_particles_create_h(const float *x, const float *y, const float *z, const float *v,
+                                            const float *h, uint64_t n, const float dmin[3], const float dmax[3]);
 void oracle_particles_destroy(oracle_particles *p);
 /* cell order of the grid (UniformGridDevice::getIndexFromCell, particle_grid.cuh:64-83) */
 uint32_t oracle_particles_cell_index(const oracle_particles *p, int cx, int cy, int cz);

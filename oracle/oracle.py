@@ -137,13 +137,21 @@ class ParticleSet:
     """oracle_particles: the reference's uniform particle grid built by the oracle (owns its C memory)."""
 
     def __init__(self, x, y, z, v, h, dmin, dmax):
+        """h: one smoothing length (the reference's particles), or one per particle (the Wendland C2 variant)."""
         L = lib()
         self._keep = [np.ascontiguousarray(a, dtype=np.float32) for a in (x, y, z, v)]
         self.n = self._keep[0].size
-        self.h = float(h)
         self.dmin, self.dmax = tuple(dmin), tuple(dmax)
-        self.handle = L.oracle_particles_create(*[_ptr(a) for a in self._keep], self.n, self.h,
-                                                (C.c_float * 3)(*dmin), (C.c_float * 3)(*dmax))
+        if np.ndim(h) == 0:
+            self.h = float(h)
+            self.handle = L.oracle_particles_create(*[_ptr(a) for a in self._keep], self.n, self.h,
+                                                    (C.c_float * 3)(*dmin), (C.c_float * 3)(*dmax))
+        else:
+            hs = np.ascontiguousarray(h, dtype=np.float32)
+            self._keep.append(hs)
+            self.h = float(hs.max())
+            self.handle = L.oracle_particles_create_h(*[_ptr(a) for a in self._keep], self.n,
+                                                      (C.c_float * 3)(*dmin), (C.c_float * 3)(*dmax))
         if not self.handle:
             raise ValueError("no particles")
 
@@ -189,6 +197,9 @@ def _declare(L):
     L.oracle_particles_create.restype = C.c_void_p
     L.oracle_particles_create.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_float,
                                           C.c_float * 3, C.c_float * 3]
+    L.oracle_particles_create_h.restype = C.c_void_p
+    L.oracle_particles_create_h.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64,
+                                            C.c_float * 3, C.c_float * 3]
     L.oracle_particles_destroy.argtypes = [C.c_void_p]
     for sfx, R in (("f32", C.c_float), ("f64", C.c_double)):
         f = getattr(L, f"oracle_generate_moments_particles_{sfx}")

@@ -25,9 +25,16 @@ def _gpu_particle_moments(ctx, x, y, z, v, h, dmin, dmax, cam, gen, W, H, m, pre
     import mray_gb300 as M
 
     ctx.precision = precision
+    per_particle = np.ndim(h) > 0
     if on_device:
-        arrs = [torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).cuda() for a in (x, y, z, v)]
-        ctx.upload_particles(*arrs, h, dmin, dmax)
+        arrs = [torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).cuda()
+                for a in ((x, y, z, v, h) if per_particle else (x, y, z, v))]
+        if per_particle:
+            ctx.upload_particles_h(*arrs, dmin, dmax)
+        else:
+            ctx.upload_particles(*arrs, h, dmin, dmax)
+    elif per_particle:
+        ctx.upload_particles_h(x, y, z, v, h, dmin, dmax)
     else:
         ctx.upload_particles(x, y, z, v, h, dmin, dmax)
     mo = torch.zeros(W * H * m, dtype=torch.float32, device="cuda")
@@ -148,3 +155,49 @@ def test_particle_upload_errors(gpu_context):
     mo = torch.zeros(16, dtype=torch.float32, device="cuda")
     with pytest.raises(M.MrayError, match="NO_VOLUME"):
         gpu_context.stage_generate_moments(mi_cam, gp, 4, 4, 1, mo, None, None)
+
+
+def _wendland_case(n=30000, seed=41, W=48, H=40, m=16):
+    """The per-particle smoothing-length variant on a small case: clustered particles, h uniform in [0.03, 0.06]
+    (about six particles per cell of the 0.06 grid), step 2^-6."""
+    from mray_gb300 import workloads as W_
+
+    wl = W_.sph_workload(n=n, h=0.06, width=W, height=H, num_moments=m, seed=seed)
+    wl.h = np.random.default_rng(seed).uniform(0.03, 0.06, size=n).astype(np.float32)
+    wl.gen.step_size = 2.0 ** -6
+    return wl
+
+
+@pytest.mark.parametrize("on_device", [False, True])
+def test_wendland_variant_matches_oracle(gpu_context, on_device):
+    """The Wendland C2 variant with a smoothing length per particle (parity unpinned: the reference has no such
+    form; the oracle's restatement, oracle_particles_create_h, is the check): bounds and counts exact, moments
+    within the particle path's bar against the oracle's FP32 and FP64 evaluations."""
+    wl = _wendland_case()
+    _check_against_oracle(gpu_context, wl.x, wl.y, wl.z, wl.v, wl.h, wl.domain_min, wl.domain_max, wl.camera,
+                          wl.gen, wl.width, wl.height, wl.num_moments, on_device=on_device)
+
+
+def test_wendland_variant_kahan_and_unsupported_paths(gpu_context):
+    import mray_gb300 as M
+
+    wl = _wendland_case(n=12000, seed=43, W=33, H=17, m=31)
+    _check_against_oracle(gpu_context, wl.x, wl.y, wl.z, wl.v, wl.h, wl.domain_min, wl.domain_max, wl.camera,
+                          wl.gen, wl.width, wl.height, wl.num_moments, precision=M.PRECISION_COMPENSATED_FF_MESE)
+    # smoothing lengths must be finite and > 0
+    for bad in (0.0, -0.01, np.nan, np.inf):
+        h = wl.h.copy()
+        h[17] = bad
+        with pytest.raises(M.MrayError) as e:
+            gpu_context.upload_particles_h(wl.x, wl.y, wl.z, wl.v, h, wl.domain_min, wl.domain_max)
+        assert e.value.status == 1
+    # the renderers without a per-particle form say so
+    gpu_context.upload_particles_h(wl.x, wl.y, wl.z, wl.v, wl.h, wl.domain_min, wl.domain_max)
+    rgba = torch.zeros(wl.width * wl.height * 4, device="cuda")
+    gpu_context.upload_tf(O.preintegrate(wl.tf1d, wl.tf_step))
+    from mray_gb300.types import ReferenceParameters
+
+    rp = ReferenceParameters(step_size=wl.gen.step_size, data_min=wl.gen.data_min, data_max=wl.gen.data_max)
+    with pytest.raises(M.MrayError) as e:
+        gpu_context.stage_generate_reference(wl.camera, rp, wl.width, wl.height, rgba)
+    assert e.value.status == 6
