@@ -631,12 +631,13 @@ def run_e2e(args, ctx, hl, dist):
     img.rgba_float = torch.empty(P * 4, dtype=torch.float32).pin_memory().numpy().reshape(H, W, 4)
     img.rgba = torch.empty(P * 4, dtype=torch.uint8).pin_memory().numpy().reshape(H, W, 4)
     tf = M.preintegrate(hl.tf1d, hl.tf_step)
+    codes = torch.empty(P * m * 2 + 8, dtype=torch.uint8).pin_memory().numpy()  # 16 bits per value at most
     sizes = {}
 
     def one():
         mi.data = data_full
         M.generate(hl.camera, grid, mi, hl.gen, context=ctx)
-        qs = M.quantize_prediction_coding(mi, hl.table, context=ctx)
+        qs = M.quantize_prediction_coding(mi, hl.table, context=ctx, out=codes)
         M.dequantize_prediction_coding(mi, hl.table, qs, context=ctx)
         M.reconstruct(hl.camera, mi, tf, img, hl.rec, context=ctx)
         sizes["moments"], sizes["codes"] = mi.data.size, qs.size

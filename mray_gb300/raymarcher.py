@@ -520,8 +520,9 @@ class Context:
         self._check(self._L.mraygb_stage_generate_reference_reconstructed_ss(self._h, C.byref(cam), C.byref(rp),
                                                                              width, height, _dptr(rgba)))
 
-    def quantize_prediction_coding(self, mi: MomentImageHost, table) -> np.ndarray:
-        """quantize_prediction_coding(mi, table) (moment_quantization.cpp:239-276): the packed code bytes."""
+    def quantize_prediction_coding(self, mi: MomentImageHost, table, out: Optional[np.ndarray] = None) -> np.ndarray:
+        """quantize_prediction_coding(mi, table) (moment_quantization.cpp:239-276): the packed code bytes, as a view
+        of ``out`` (a caller's uint8 buffer, e.g. pinned, of at least the packed size) or of a new array."""
         if not mi.is_compact:
             raise ValueError("quantize_prediction_coding needs a compact moment image")
         t = np.ascontiguousarray(table, dtype=np.uint8)
@@ -529,10 +530,12 @@ class Context:
             raise ValueError("the quantization table needs one entry per moment index")
         data = np.ascontiguousarray(mi.data, dtype=np.float32)
         index = np.ascontiguousarray(mi.index, dtype=np.uint32)
-        # the packed size from the counts: whole bytes of sum_p sum_{l < n_p} table[l]
-        cum = np.concatenate([[0], np.cumsum(t[:mi.num_moments].astype(np.int64))])
-        nbytes = int(cum[np.diff(index.astype(np.int64))].sum()) // 8
-        out = np.empty(max(nbytes, 1), dtype=np.uint8)
+        if out is None:
+            # an upper bound of the packed size (every stored value at the widest code); the library reports the
+            # exact size and the copy back touches only those bytes
+            out = np.empty(max((data.size * int(t[:mi.num_moments].max()) + 7) // 8, 1), dtype=np.uint8)
+        elif out.dtype != np.uint8 or not out.flags.c_contiguous:
+            raise ValueError("out must be a contiguous uint8 array")
         n = C.c_uint64()
         self._check(self._L.mraygb_quantize_prediction_coding(self._h, mi.width, mi.height, mi.num_moments,
                                                               _hptr(index), _hptr(data), data.size, _hptr(t),
@@ -796,9 +799,10 @@ def generate(cam: Camera, volume, mi: MomentImageHost, params: GenerationParamet
     assert out is mi
 
 
-def quantize_prediction_coding(mi: MomentImageHost, table, context: Optional[Context] = None) -> np.ndarray:
-    """moment_quantization::quantize_prediction_coding(mi, table) on the GPU."""
-    return (context or default_context()).quantize_prediction_coding(mi, table)
+def quantize_prediction_coding(mi: MomentImageHost, table, context: Optional[Context] = None,
+                               out: Optional[np.ndarray] = None) -> np.ndarray:
+    """moment_quantization::quantize_prediction_coding(mi, table) on the GPU (``out``: an optional caller buffer)."""
+    return (context or default_context()).quantize_prediction_coding(mi, table, out)
 
 
 def dequantize_prediction_coding(mi: MomentImageHost, table, qs, context: Optional[Context] = None) -> None:
