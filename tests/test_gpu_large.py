@@ -129,3 +129,33 @@ def test_large_quantization_table(large, gpu_context):
     seen = np.isfinite(ref_means)
     assert np.array_equal(means[seen], ref_means[seen])
     assert table.tolist() == ref_table.tolist()
+
+
+def test_large_codes_end_to_end_sampled(large):
+    """Volume -> 10-bit codes on the sampled pixels of the large configuration: the codes of the GPU's moments, of
+    the reference's FP32 moments (oracle) and of the FP64 moments rounded to float, each prediction coded with the
+    reference's encoder (bit-exact with the GPU's on the same moments, test above) and quantized with the fixed
+    table.  The warp is the plain one (CODING_WARP_NONE), so every pixel's codes depend on its own moments only.
+    Ours must agree with the codes of the FP64 moments at least as often as the reference's do."""
+    g = large
+    sel = (slice(ROWS[0], ROWS[1], ROWS[2]), slice(COLS[0], COLS[1], COLS[2]))
+    ref_m, ref_b, ref_c = O.generate_moments(g["cam"], g["gen"], g["vol"], g["dmin"], g["dmax"], WIDTH, HEIGHT, M_MOM,
+                                             "f32", rows=ROWS, cols=COLS)
+    m64, b64, _ = O.generate_moments(g["cam"], g["gen"], g["vol"], g["dmin"], g["dmax"], WIDTH, HEIGHT, M_MOM, "f64",
+                                     rows=ROWS, cols=COLS)
+    keep = (ref_c[sel] > 0) & np.all(ref_b[sel] == b64[sel], axis=-1)
+    n = int(keep.sum())
+    assert n > 256
+    index = np.arange(n + 1, dtype=np.uint32) * M_MOM
+    codes = []
+    for mom in (g["moments"][sel][keep], ref_m[sel][keep], m64[sel][keep].astype(np.float32)):
+        enc, _ = O.prediction_encode(n, 1, M_MOM, index, mom.reshape(-1), 1, g["gen"].bias)
+        packed = O.quantize_prediction_coding(n, 1, M_MOM, index, enc, g["table"])
+        codes.append(O.unpack_codes(n, 1, M_MOM, index, g["table"], packed))
+    ours, ref, exact = codes
+    ours_vs_exact = float(np.mean(ours != exact))
+    ref_vs_exact = float(np.mean(ref != exact))
+    print(f"large configuration, {n} sampled pixels: 10-bit codes differing from those of the FP64 moments, ours "
+          f"{ours_vs_exact:.3%}, the reference's FP32 {ref_vs_exact:.3%}; ours against the reference's "
+          f"{float(np.mean(ours != ref)):.3%}")
+    assert ours_vs_exact <= ref_vs_exact + 0.002
