@@ -387,7 +387,8 @@ template <class V, int NJ, bool KAHAN> __device__ __forceinline__ void generate_
     }
 }
 
-template <int NJ, bool KAHAN> __global__ void __launch_bounds__(128) generate_grid_kernel(const GenArgs<GridView> a)
+template <int NJ, bool KAHAN>
+__global__ void __launch_bounds__(128) generate_grid_kernel(const GenArgs<GridView> a)
 {
     generate_quads<GridView, NJ, KAHAN>(a);
 }
@@ -403,6 +404,29 @@ __global__ void __launch_bounds__(128) generate_particles_h_kernel(const GenArgs
 {
     generate_quads<ParticleHView, NJ, KAHAN>(a);
 }
+
+// The compensated instantiations at five blocks per SM: 96 registers, the Kahan terms kept with a few bytes of
+// spill (9.84 ms against 10.6 at the four blocks of their unbounded 120-128 registers, 512^3 / 1024^2 / m = 64).
+// The plain ones keep the unbounded allocation (96 registers for the grid, 72 with some spill for particles, seven
+// blocks): a stated minimum gives them 110-128 registers, or spills, and measured slower.
+#define MRAYGB_KAHAN_5_BLOCKS(NAME, VIEW, NJ)                                                                       \
+    template <> __global__ void __launch_bounds__(128, 5) NAME<NJ, true>(const GenArgs<VIEW> a)                      \
+    {                                                                                                              \
+        generate_quads<VIEW, NJ, true>(a);                                                                         \
+    }
+#define MRAYGB_KAHAN_5_BLOCKS_ALL(NAME, VIEW)                                                                       \
+    MRAYGB_KAHAN_5_BLOCKS(NAME, VIEW, 1)                                                                           \
+    MRAYGB_KAHAN_5_BLOCKS(NAME, VIEW, 2)                                                                           \
+    MRAYGB_KAHAN_5_BLOCKS(NAME, VIEW, 4)                                                                           \
+    MRAYGB_KAHAN_5_BLOCKS(NAME, VIEW, 8)                                                                           \
+    MRAYGB_KAHAN_5_BLOCKS(NAME, VIEW, 16)                                                                          \
+    MRAYGB_KAHAN_5_BLOCKS(NAME, VIEW, 32)                                                                          \
+    MRAYGB_KAHAN_5_BLOCKS(NAME, VIEW, 64)
+MRAYGB_KAHAN_5_BLOCKS_ALL(generate_grid_kernel, GridView)
+MRAYGB_KAHAN_5_BLOCKS_ALL(generate_particles_kernel, ParticleView)
+MRAYGB_KAHAN_5_BLOCKS_ALL(generate_particles_h_kernel, ParticleHView)
+#undef MRAYGB_KAHAN_5_BLOCKS_ALL
+#undef MRAYGB_KAHAN_5_BLOCKS
 
 template <int NJ, bool KAHAN> void launch_kernel(const GenArgs<GridView> &a, dim3 grid, cudaStream_t stream)
 {
