@@ -765,8 +765,6 @@ def refcuda_worker(args, local):
     L.ref_time_flow(grid, C.byref(hl.camera), C.byref(hl.gen), C.byref(hl.rec), hl.width, hl.height, hl.num_moments,
                     row.ctypes.data, 1, steps, ms.ctypes.data, rgba8.ctypes.data, C.byref(size))
     gen_ms, rec_ms = float(ms[0::2].mean()), float(ms[1::2].mean())
-    np.save(os.path.join(ROOT, "gpurun_out" if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "_work",
-                         f"refcuda_{args.worker}_rgba8.npy"), rgba8[::8, ::8])
     return {"generate_ms": gen_ms, "reconstruct_ms": rec_ms, "steps": steps, "moment_floats": int(size.value),
             "Mrays_s": hl.width * hl.height / ((gen_ms + rec_ms) * 1e-3) / 1e6, "rgba8_mean": float(rgba8.mean())}
 
