@@ -13,8 +13,9 @@
 // Memory: none of the three adjoints keeps a per-sample tape.  The re-march adjoint replays the forward march
 // and uses the final radiance of the forward pass for the suffix sums of front-to-back compositing (d L / d tau_k
 // needs the radiance gathered behind sample k, which is the final radiance minus the radiance so far); the
-// generation adjoint replays the sample positions; the preparation adjoint runs Levinson's recursion backwards by
-// inverting each update (old_k = new_k + u conj(new_{j-k})), so it stores only the reflection coefficients.
+// generation adjoint replays the sample positions; the preparation adjoint reads two arrays per pixel that the
+// forward preparation kept (the Levinson solution and the exponential moments, 2m complex values) and needs no
+// recursion run backwards (see prepare_adjoint_kernel).
 
 #include "device_common.cuh"
 #include "internal.h"
@@ -95,18 +96,19 @@ struct TfGradCache
 // memory, lane l adding to copy l mod kTfCopies: neighbouring rays sample similar densities at the same step, and
 // shared-memory atomics on one address from many lanes of a warp serialize.
 constexpr int kTfCopies = 8;
+constexpr int kTfCopyStride = 256;
 
 template <int MAXM> __global__ void __launch_bounds__(128, 4) reconstruct_adjoint_kernel(const ReconAdjDev a)
 {
     __shared__ float4 s_tf[256];
-    extern __shared__ float4 s_gall[]; // kTfCopies * 256 (dynamic: above the 48 KiB of static shared memory)
+    extern __shared__ float4 s_gall[]; // kTfCopies * kTfCopyStride (dynamic: above the 48 KiB of static shared memory)
     const int tid = threadIdx.x + threadIdx.y * blockDim.x;
     for (int i = tid; i < 256; i += blockDim.x * blockDim.y)
         s_tf[i] = a.tf[i];
-    for (int i = tid; i < kTfCopies * 256; i += blockDim.x * blockDim.y)
+    for (int i = tid; i < kTfCopies * kTfCopyStride; i += blockDim.x * blockDim.y)
         s_gall[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     __syncthreads();
-    float4 *s_g = s_gall + (tid % kTfCopies) * 256;
+    float4 *s_g = s_gall + (tid % kTfCopies) * kTfCopyStride;
 
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
@@ -159,7 +161,9 @@ template <int MAXM> __global__ void __launch_bounds__(128, 4) reconstruct_adjoin
                     atomicExch(a.error_flag, 1);
                     break;
                 }
-                const float S = mese_series<MAXM>(lam2, lam0, pc);
+                bool pos;
+                const float dl = reinsch_lambda(pc, pos);
+                const float S = mese_series_reinsch<MAXM>(lam2, lam0, pos, dl);
                 const float r = atanf(S) * 0.318309886f + 0.5f;
                 const float fs = r * span + lo;
                 const BSplineTap k = bspline_tap(fs);
@@ -183,28 +187,39 @@ template <int MAXM> __global__ void __launch_bounds__(128, 4) reconstruct_adjoin
                 const float gfs = dt.x * gs.x + dt.y * gs.y + dt.z * gs.z + dt.w * gs.w;
                 glo = fmaf(gfs, 1.f - r, glo);
                 ghi = fmaf(gfs, r, ghi);
-                const float gS = gfs * span * 0.318309886f / fmaf(S, S, 1.f);
+                const float gS = __fdividef(gfs * span * 0.318309886f, fmaf(S, S, 1.f));
                 glam[0] += gS;
                 // cos(l pc) for l >= 1 by Reinsch's modification of the three-term recurrence (stable where pc
-                // nears 0 or -pi, the two ends of every ray): with d = -4 sin^2(pc / 2) while cos pc > 0,
+                // nears 0 or -pi, the two ends of every ray), with the series' own d: with d = -4 sin^2(pc / 2)
+                // while cos pc > 0,
                 //   e_{l+1} = e_l + d c_l,  c_{l+1} = c_l + e_{l+1}      (e_l = c_l - c_{l-1}),
                 // and with d = 4 cos^2(pc / 2) otherwise,
-                //   e_{l+1} = d c_l - e_l,  c_{l+1} = e_{l+1} - c_l      (e_l = c_l + c_{l-1})
+                //   e_{l+1} = d c_l - e_l,  c_{l+1} = e_{l+1} - c_l      (e_l = c_l + c_{l-1});
+                // one loop per branch, so each step is one FMA and one add besides the accumulation
                 {
-                    float sh, ch;
-                    sincosf(0.5f * pc, &sh, &ch);
-                    const bool pos = fabsf(pc) < 1.5707963267948966f;
-                    const float sg = pos ? 1.f : -1.f;
-                    const float d = pos ? -4.f * sh * sh : 4.f * ch * ch;
-                    float e = 0.5f * d;
-                    float c = e + sg; // cos pc: 1 + d/2, or d/2 - 1
+                    float e = 0.5f * dl;
                     const float g2 = 2.f * gS;
-#pragma unroll
-                    for (int l = 1; l < MAXM; ++l)
+                    if (pos)
                     {
-                        glam[l] = fmaf(g2, c, glam[l]);
-                        e = fmaf(d, c, sg * e);
-                        c = fmaf(sg, c, e);
+                        float c = e + 1.f; // cos pc = 1 + d/2
+#pragma unroll
+                        for (int l = 1; l < MAXM; ++l)
+                        {
+                            glam[l] = fmaf(g2, c, glam[l]);
+                            e = fmaf(dl, c, e);
+                            c = c + e;
+                        }
+                    }
+                    else
+                    {
+                        float c = e - 1.f; // cos pc = d/2 - 1
+#pragma unroll
+                        for (int l = 1; l < MAXM; ++l)
+                        {
+                            glam[l] = fmaf(g2, c, glam[l]);
+                            e = fmaf(dl, c, -e);
+                            c = e - c;
+                        }
                     }
                 }
                 t = __fadd_rn(t, a.step);
@@ -228,7 +243,7 @@ template <int MAXM> __global__ void __launch_bounds__(128, 4) reconstruct_adjoin
 #pragma unroll
         for (int c = 1; c < kTfCopies; ++c)
         {
-            const float4 w = s_gall[c * 256 + i];
+            const float4 w = s_gall[c * kTfCopyStride + i];
             v.x += w.x;
             v.y += w.y;
             v.z += w.z;
@@ -249,256 +264,258 @@ template <int MAXM> __global__ void __launch_bounds__(128, 4) reconstruct_adjoin
 // preparation adjoint (prepare_moments_from_std_coding -> prepareMESELagrange, src/moment_preparation.h:55-64,
 // src/mese/MESE_dynamic.h:35-211)
 // ------------------------------------------------------------------------------------------------------------
-
-struct C2
-{
-    float x, y;
-};
-__device__ __forceinline__ C2 c2(float x, float y) { return {x, y}; }
-__device__ __forceinline__ C2 operator+(C2 a, C2 b) { return {a.x + b.x, a.y + b.y}; }
-__device__ __forceinline__ C2 operator-(C2 a, C2 b) { return {a.x - b.x, a.y - b.y}; }
-__device__ __forceinline__ C2 operator*(C2 a, C2 b) { return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x}; }
-__device__ __forceinline__ C2 operator*(float s, C2 a) { return {s * a.x, s * a.y}; }
-__device__ __forceinline__ C2 conj(C2 a) { return {a.x, -a.y}; }
-__device__ __forceinline__ float abs2(C2 a) { return a.x * a.x + a.y * a.y; }
-
-// Complex adjoints are carried as d L / d re + i d L / d im.  For w = a b: a_bar += w_bar conj(b); for w = conj(c) u:
-// c_bar += conj(w_bar) u, u_bar += w_bar c.
 //
-// One thread per pixel, the arrays (2 KiB at 32 moments) in local memory: measured faster (1.44 ms per 512^2 launch
-// at m = 31) than the same kernel with its arrays in shared memory, one lane per pixel (1.80 ms: fewer resident
-// threads) or one pixel per group of 8 lanes (1.93 ms: the per-step reductions and syncs of the sequential
-// recursions cost more than the split of their O(n) bodies saves).
-template <int MAXM>
-__global__ void __launch_bounds__(64) prepare_adjoint_kernel(int num_pixels, int m, const float *__restrict__ moments,
-                                                             float bias, const float *grad_lambda,
-                                                             float *grad_moments)
+// The forward per pixel, with x the Levinson solution, P = 2 pi x, E the exponential moments and Eh = E with its
+// zeroth halved (the arrays the forward kept):
+//   A_q = sum_j P_j conj(P_{j+q}),  acc_k = sum_{q>=k} Im(A_q Eh_{q-k}),  lambda_k = acc_k / (pi P_0)
+// and x = T^-1 e_0 for the Hermitian Toeplitz matrix T of E (diagonal Re E_0), restricted to its leading nn x nn
+// block when Levinson's Herglotz check latched at step nn (x is then zero from nn on and independent of E_d,
+// d >= nn).  The reverse sweep needs no recursion run backwards:
+// * Levinson: with gsol the adjoint of x, y = T^-1 gsol and dT = -y x^H, which sums along the diagonals to
+//   E_d: -sum_c (y_{c+d} conj(x_c) + conj(y_c) x_{c+d}) (d >= 1) and -sum_c Re(y_c conj(x_c)) (d = 0, real).
+//   T^-1 comes from x itself (Gohberg-Semencul): T^-1 = (L(x) L(x)^H - L(v) L(v)^H) / x_0 with L(.) the lower
+//   triangular Toeplitz matrix of a vector and v = (0, conj(x_{nn-1}), ..., conj(x_1)), four triangular products.
+// * Exponential moments: E = E_0 exp(2 pi i X(z)) as power series with X(z) = sum_{k>=1} x'_k z^k (x' the biased
+//   moments; E_l = (2 pi i / l) sum_{j<l} (l - j) x'_{l-j} E_j is its recurrence), so dE_l / dx'_k = 2 pi i E_{l-k}
+//   (k >= 1) and dE_l / dphi = i E_l, phi = pi x'_0 - pi / 2 (with E_0 undoubled).
+// Every step is then a correlation or a triangular product: lane r of a warp forms output r (and r + 32) by a
+// loop over the pixel's arrays in shared memory, padded with zeros so every lane runs the same loop.
+//
+// Complex adjoints are carried as d L / d re + i d L / d im.
+
+__device__ __forceinline__ float2 cmul2(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+// a conj(b)
+__device__ __forceinline__ float2 cmulcj(float2 a, float2 b) { return make_float2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y); }
+__device__ __forceinline__ void cacc(float2 &s, float2 v)
 {
-    const int pix = blockIdx.x * blockDim.x + threadIdx.x;
+    s.x += v.x;
+    s.y += v.y;
+}
+
+__device__ __forceinline__ float warp_sum(float v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v += __shfl_xor_sync(kFull, v, o);
+    return v;
+}
+
+// per warp in shared memory (complex values as float2), M = MAXM
+template <int M> struct PrepAdjSmem
+{
+    float2 xp[3 * M]; // P at offset M, zeros on both sides
+    float2 eh[2 * M]; // Eh at offset M, zeros below
+    float2 ww[2 * M]; // v (in P's scale) at offset M, zeros below
+    float2 a[2 * M];  // A, then y; zeros above
+    float2 ga[M];     // adjoint of A
+    float2 gp[M];     // adjoint of P
+    float2 ge[M];     // adjoint of Eh, then of the undoubled E
+    float4 t[M];      // L(P)^H gP and L(v)^H gP
+    float gc[M];      // d loss / d lambda, then d loss / d acc
+};
+
+constexpr int kPrepAdjWarps = 4;
+
+template <int MAXM>
+__global__ void __launch_bounds__(32 * kPrepAdjWarps) prepare_adjoint_kernel(int num_pixels, int m,
+                                                                             const float2 *__restrict__ keep,
+                                                                             float bias, const float *grad_lambda,
+                                                                             float *grad_moments)
+{
+    __shared__ PrepAdjSmem<MAXM> s_all[kPrepAdjWarps];
+    PrepAdjSmem<MAXM> &s = s_all[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
+    const int pix = blockIdx.x * kPrepAdjWarps + (threadIdx.x >> 5);
     if (pix >= num_pixels)
-        return;
+        return; // whole warps
+    constexpr float kPi = 3.14159265358979f;
+    constexpr float kTwoPi = 6.283185307179586f;
+    constexpr int M = MAXM;
     const int n = m < MAXM ? m : MAXM;
     const size_t idx = (size_t)pix * (size_t)m;
-    float gl[MAXM];
+    const float2 *kp = keep + 2 * idx;
+    const float2 z2 = make_float2(0.f, 0.f);
+
     bool any = false;
-    for (int k = 0; k < n; ++k)
+    int last = -1;
+#pragma unroll
+    for (int i = 0; i < MAXM / 32; ++i)
     {
-        gl[k] = grad_lambda[idx + k];
-        any |= gl[k] != 0.f;
+        const int k = lane + 32 * i;
+        const float g = k < n ? grad_lambda[idx + k] : 0.f;
+        any |= g != 0.f;
+        const float2 pk = k < n ? kp[k] : z2;
+        if (pk.x != 0.f || pk.y != 0.f)
+            last = k;
+        s.xp[k] = z2;
+        s.xp[M + k] = pk;
+        s.xp[2 * M + k] = z2;
+        s.eh[k] = z2;
+        s.eh[M + k] = k < n ? kp[m + k] : z2;
+        s.ww[k] = z2;
+        s.a[M + k] = z2;
+        s.gc[k] = g;
     }
-    if (!any)
+    if (!__any_sync(kFull, any))
     {
-        for (int k = 0; k < n; ++k)
+        for (int k = lane; k < n; k += 32)
             grad_moments[idx + k] = 0.f;
         return;
     }
-    constexpr float kPi = 3.14159265358979f;
-    constexpr float kInv4Pi = 0.0795774715459477f;
+    // the leading block Levinson solved: past the last non-zero entry of x every step latched
+    const int nn = __reduce_max_sync(kFull, last) + 1;
+    __syncwarp();
 
-    // ---- forward, keeping what the reverse sweep needs ----
-    float xm[MAXM];
-    C2 E[MAXM], sol[MAXM], uu[MAXM];
-    uint32_t latched[(MAXM + 31) / 32];
-    for (int i = 0; i < (MAXM + 31) / 32; ++i)
-        latched[i] = 0u;
-    xm[0] = (1.f - bias) * moments[idx] + bias * 0.5f;
-    for (int i = 1; i < n; ++i)
-        xm[i] = (1.f - bias) * moments[idx + i];
-    // trigonometricToExponentialMoments (E[0] un-doubled inside the recurrence)
-    const float phi = kPi * xm[0] - 0.5f * kPi;
-    float sphi, cphi;
-    sincosf(phi, &sphi, &cphi);
-    E[0] = c2(kInv4Pi * cphi, kInv4Pi * sphi);
-    for (int l = 1; l < n; ++l)
+    // A_q
+#pragma unroll
+    for (int i = 0; i < MAXM / 32; ++i)
     {
-        C2 acc = c2(0.f, 0.f);
-        for (int j = 0; j < l; ++j)
-            acc = acc + (float(l - j) * xm[l - j]) * E[j];
-        const float w = (float)(6.283185307179586 / (double)l);
-        E[l] = c2(-w * acc.y, w * acc.x);
+        const int q = lane + 32 * i;
+        float2 acc = z2;
+        for (int j = 0; j < n; ++j)
+            cacc(acc, cmulcj(s.xp[M + j], s.xp[M + j + q]));
+        s.a[q] = q < n ? acc : z2;
     }
-    E[0] = 2.f * E[0];
-    // levinsonsAlgorithm with the invalid latch
-    sol[0] = c2(1.f / E[0].x, 0.f);
-    bool invalid = false;
-    for (int j = 1; j < n; ++j)
+    __syncwarp();
+    // d loss / d norm = sum_k glambda_k acc_k
+    float gn = 0.f;
+#pragma unroll
+    for (int i = 0; i < MAXM / 32; ++i)
     {
-        C2 u = c2(0.f, 0.f);
-        if (!invalid)
-            for (int k = 0; k < j; ++k)
-                u = u + sol[k] * E[j - k];
-        float a2 = abs2(u);
-        if (invalid || a2 >= 1.f)
+        const int k = lane + 32 * i;
+        float acc = 0.f;
+        for (int d = 0; d < n; ++d)
         {
-            u = c2(0.f, 0.f);
-            a2 = 0.f;
-            invalid = true;
-            latched[j >> 5] |= 1u << (j & 31);
+            const float2 av = s.a[k + d], e = s.eh[M + d];
+            acc += av.x * e.y + av.y * e.x;
         }
-        uu[j] = u;
-        const float f = 1.f / (1.f - a2);
-        const float s0 = sol[0].x;
-        int k = 1, kk = j - 1;
-        for (; k < kk; ++k, --kk)
-        {
-            const C2 p = sol[k], q = sol[kk];
-            sol[k] = f * (p - conj(q) * u);
-            sol[kk] = f * (q - conj(p) * u);
-        }
-        if (k == kk)
-        {
-            const C2 p = sol[k];
-            sol[k] = f * (p - conj(p) * u);
-        }
-        sol[j] = f * ((-s0) * u);
-        sol[0] = c2(f * s0, 0.f);
+        gn += s.gc[k] * acc;
     }
-    // P = 2 pi sol; Eh = E with Eh[0] = E[0] / 2; a_q = sum_j P_j conj(P_{j+q}); acc_k = sum_{q>=k} Im(a_q Eh_{q-k})
-    constexpr float kTwoPi = 6.283185307179586f;
-    C2 A[MAXM];
-    float accv[MAXM];
-    for (int q = 0; q < n; ++q)
-    {
-        C2 s = c2(0.f, 0.f);
-        for (int j = 0; j + q < n; ++j)
-            s = s + (kTwoPi * sol[j]) * conj(kTwoPi * sol[j + q]);
-        A[q] = s;
-    }
-    for (int k = 0; k < n; ++k)
-    {
-        float s = 0.f;
-        for (int q = k; q < n; ++q)
-        {
-            const C2 e = (q - k == 0) ? 0.5f * E[0] : E[q - k];
-            s += A[q].x * e.y + A[q].y * e.x;
-        }
-        accv[k] = s;
-    }
-    const float P0 = kTwoPi * sol[0].x;
+    gn = warp_sum(gn);
+    const float P0 = s.xp[M].x;
     const float norm = 1.f / (kPi * P0);
-
-    // ---- reverse ----
-    // lambda_k = norm acc_k
-    float gnorm = 0.f;
-    for (int k = 0; k < n; ++k)
+    __syncwarp();
+#pragma unroll
+    for (int i = 0; i < MAXM / 32; ++i)
+        s.gc[lane + 32 * i] *= norm;
+    __syncwarp();
+    // acc_k = sum_q Im(A_q Eh_{q-k}): gA_q += gacc_k (Eh_{q-k}.y, Eh_{q-k}.x), gEh_d += gacc_k (A_{k+d}.y, A_{k+d}.x)
+#pragma unroll
+    for (int i = 0; i < MAXM / 32; ++i)
     {
-        gnorm += gl[k] * accv[k];
-        gl[k] *= norm; // now d / d acc_k
+        const int q = lane + 32 * i;
+        float2 gA = z2, gE = z2;
+        for (int k = 0; k < n; ++k)
+        {
+            const float g = s.gc[k];
+            const float2 e = s.eh[M + q - k], av = s.a[k + q];
+            gA.x += g * e.y;
+            gA.y += g * e.x;
+            gE.x += g * av.y;
+            gE.y += g * av.x;
+        }
+        s.ga[q] = gA;
+        s.ge[q] = gE;
     }
-    // acc_k = sum_{q>=k} Im(A_q Eh_{q-k}): A_bar_q += acc_bar_k (Eh.y, Eh.x); Eh_bar_{q-k} += acc_bar_k (A.y, A.x)
-    C2 gE[MAXM], gP[MAXM];
-    for (int i = 0; i < n; ++i)
+    __syncwarp();
+    // A_q = sum_j P_j conj(P_{j+q}): gP_j += gA_q P_{j+q} + conj(gA_q) P_{j-q}; P_0 also through the norm
+#pragma unroll
+    for (int i = 0; i < MAXM / 32; ++i)
     {
-        gE[i] = c2(0.f, 0.f);
-        gP[i] = c2(0.f, 0.f);
+        const int j = lane + 32 * i;
+        float2 g = z2;
+        for (int q = 0; q < n; ++q)
+        {
+            const float2 gA = s.ga[q];
+            cacc(g, cmul2(gA, s.xp[M + j + q]));
+            cacc(g, cmulcj(s.xp[M + j - q], gA));
+        }
+        if (j == 0)
+            g.x -= gn * norm / P0;
+        s.gp[j] = j < nn ? g : z2;
+        // v_i = conj(x_{nn-i}), 1 <= i < nn (in P's scale)
+        if (j >= 1 && j < nn)
+        {
+            const float2 p = s.xp[M + nn - j];
+            s.ww[M + j] = make_float2(p.x, -p.y);
+        }
+        else
+            s.ww[M + j] = z2;
     }
-    for (int q = 0; q < n; ++q)
+    __syncwarp();
+    // Levinson: gsol = 2 pi gP, y = T^-1 gsol = (L(P) L(P)^H gP - L(v) L(v)^H gP) / P_0
+#pragma unroll
+    for (int i = 0; i < MAXM / 32; ++i)
     {
-        C2 gA = c2(0.f, 0.f);
-        for (int k = 0; k <= q; ++k)
+        const int r = lane + 32 * i;
+        float2 t1 = z2, t2 = z2;
+        for (int c = 0; c < nn; ++c)
         {
-            const C2 e = (q - k == 0) ? 0.5f * E[0] : E[q - k];
-            gA = gA + gl[k] * c2(e.y, e.x);
-            gE[q - k] = gE[q - k] + gl[k] * c2(A[q].y, A[q].x);
+            const float2 g = s.gp[c];
+            cacc(t1, cmulcj(g, s.xp[M + c - r]));
+            cacc(t2, cmulcj(g, s.ww[M + c - r]));
         }
-        // A_q = sum_j P_j conj(P_{j+q})
-        for (int j = 0; j + q < n; ++j)
-        {
-            const C2 pj = kTwoPi * sol[j], pq = kTwoPi * sol[j + q];
-            gP[j] = gP[j] + gA * pq;
-            gP[j + q] = gP[j + q] + conj(gA) * pj;
-        }
+        s.t[r] = r < nn ? make_float4(t1.x, t1.y, t2.x, t2.y) : make_float4(0.f, 0.f, 0.f, 0.f);
     }
-    gP[0].x += gnorm * (-norm / P0);
-    gE[0] = 0.5f * gE[0]; // Eh[0] = E[0] / 2
-    // sol_bar = 2 pi P_bar (reuse gP)
-    for (int i = 0; i < n; ++i)
-        gP[i] = kTwoPi * gP[i];
-
-    // Levinson backwards: sol holds the state after step j, gP its adjoint
-    for (int j = n - 1; j >= 1; --j)
+    __syncwarp();
+    const float inv_p0 = 1.f / P0;
+#pragma unroll
+    for (int i = 0; i < MAXM / 32; ++i)
     {
-        const C2 u = uu[j];
-        const float a2 = abs2(u);
-        const float f = 1.f / (1.f - a2);
-        // f_bar = sum_k Re(conj(s_bar_k) new_k) / f
-        float gf = 0.f;
-        for (int k = 0; k <= j; ++k)
-            gf += gP[k].x * sol[k].x + gP[k].y * sol[k].y;
-        gf /= f;
-        // old_k = new_k + u conj(new_{j-k}), k = 0..j-1 (pairs in place)
+        const int r = lane + 32 * i;
+        float2 y = z2;
+        for (int c = 0; c < nn; ++c)
         {
-            int k = 0, kk = j;
-            for (; k < kk; ++k, --kk)
-            {
-                const C2 p = sol[k], q = sol[kk];
-                sol[k] = p + u * conj(q);
-                sol[kk] = q + u * conj(p);
-            }
-            if (k == kk)
-            {
-                const C2 p = sol[k];
-                sol[k] = p + u * conj(p);
-            }
-            sol[j] = c2(0.f, 0.f);
+            const float4 tc = s.t[c];
+            const float2 p = s.xp[M + r - c], v = s.ww[M + r - c];
+            cacc(y, cmul2(p, make_float2(tc.x, tc.y)));
+            const float2 vt = cmul2(v, make_float2(tc.z, tc.w));
+            y.x -= vt.x;
+            y.y -= vt.y;
         }
-        // v_bar = f s_bar; u_bar = -f sum_{k=1..j} s_bar_k old_{j-k}; old_bar_i = f s_bar_i - conj(f s_bar_{j-i}) u
-        C2 gu = c2(0.f, 0.f);
-        for (int k = 1; k <= j; ++k)
-            gu = gu - (f * gP[k]) * sol[j - k];
-        {
-            int i = 0, ii = j;
-            for (; i < ii; ++i, --ii)
-            {
-                const C2 vi = f * gP[i], vii = f * gP[ii];
-                gP[i] = vi - conj(vii) * u;
-                gP[ii] = vii - conj(vi) * u; // ii = j: old_j is the constant 0, its adjoint is dropped below
-            }
-            if (i == ii)
-            {
-                const C2 vi = f * gP[i];
-                gP[i] = vi - conj(vi) * u;
-            }
-            gP[j] = c2(0.f, 0.f);
-        }
-        if (!((latched[j >> 5] >> (j & 31)) & 1u))
-        {
-            // f = 1 / (1 - |u|^2): d f / d u = 2 f^2 u
-            gu = gu + (2.f * gf * f * f) * u;
-            // u = sum_{k<j} old_k E_{j-k}
-            for (int k = 0; k < j; ++k)
-            {
-                const C2 ok = sol[k];
-                gP[k] = gP[k] + gu * conj(E[j - k]);
-                gE[j - k] = gE[j - k] + gu * conj(ok);
-            }
-        }
+        s.a[r] = r < nn ? make_float2(y.x * inv_p0, y.y * inv_p0) : z2; // A is no longer read
     }
-    // sol_0 = 1 / E_0.x (real)
-    gE[0].x += -gP[0].x / (E[0].x * E[0].x);
-
-    // trigonometricToExponentialMoments backwards: E[0] = 2 e_0
-    float gx[MAXM];
-    for (int i = 0; i < n; ++i)
-        gx[i] = 0.f;
-    E[0] = 0.5f * E[0];
-    gE[0] = 2.f * gE[0];
-    for (int l = n - 1; l >= 1; --l)
+    __syncwarp();
+    // dT = -y x^H onto E (x = P / 2 pi); the total adjoint of the undoubled E: gE'_0 = gEh_0 + 2 gE_0(T), gE'_d = gEh_d
+    // + gE_d(T)
+    constexpr float kInv2Pi = 0.15915494309189535f;
+#pragma unroll
+    for (int i = 0; i < MAXM / 32; ++i)
     {
-        const float w = (float)(6.283185307179586 / (double)l);
-        // E_l = (i w) acc: acc_bar = E_bar_l (-i w)
-        const C2 gacc = c2(gE[l].y * w, -gE[l].x * w);
-        for (int j = 0; j < l; ++j)
+        const int d = lane + 32 * i;
+        float2 lev = z2;
+        for (int c = 0; c < nn; ++c)
         {
-            const float sc = float(l - j) * xm[l - j];
-            gE[j] = gE[j] + sc * gacc;
-            gx[l - j] += float(l - j) * (gacc.x * E[j].x + gacc.y * E[j].y);
+            const float2 pc = s.xp[M + c], yc = s.a[c];
+            cacc(lev, cmulcj(s.a[c + d], pc));
+            cacc(lev, cmulcj(s.xp[M + c + d], yc));
         }
+        float2 g = s.ge[d];
+        if (d == 0)
+            g.x -= kInv2Pi * lev.x; // 2 * (-(1/2pi) Re sum y_c conj(x_c)) / 2: lev.x counts the sum twice
+        else if (d < nn)
+        {
+            g.x -= kInv2Pi * lev.x;
+            g.y -= kInv2Pi * lev.y;
+        }
+        s.ge[d] = g;
     }
-    // e_0 = (cos phi, sin phi) / (4 pi), phi = pi x_0 - pi / 2
-    gx[0] += kPi * kInv4Pi * (-gE[0].x * sphi + gE[0].y * cphi);
-    for (int i = 0; i < n; ++i)
-        grad_moments[idx + i] = (1.f - bias) * gx[i];
+    __syncwarp();
+    // moments: gx_k = -2 pi sum_{l>=k} Im(conj(gE'_l) E'_{l-k}) (k >= 1), gx_0 = pi dphi = -pi sum_l Im(conj(gE'_l) E'_l)
+    const float omb = 1.f - bias;
+#pragma unroll
+    for (int i = 0; i < MAXM / 32; ++i)
+    {
+        const int k = lane + 32 * i;
+        float acc = 0.f;
+        for (int l = 0; l < n; ++l)
+        {
+            const float2 g = s.ge[l], e = s.eh[M + l - k];
+            acc += g.x * e.y - g.y * e.x;
+        }
+        if (k < n)
+            grad_moments[idx + k] = omb * (k == 0 ? -kPi * acc : -kTwoPi * acc);
+    }
 }
 
 // ------------------------------------------------------------------------------------------------------------
@@ -695,7 +712,9 @@ template <int NJ> __global__ void __launch_bounds__(128) generate_adjoint_kernel
             sincosf(p_my - h, &sn, &cs);
             z = {cs, -sn};
         }
-        // partial A, B of the four segments over this lane's moments
+        // partial A, B of the four segments over this lane's moments j = q + 4i: both parts of z^j follow the
+        // three-term recurrence x_{j+4} = 2 cos(4 theta) x_j - x_{j-4} from z^q and z^(q+4), one FMA per part and
+        // moment (the forward's scheme) instead of a complex rotation's four operations
         float As[4], Bs[4];
 #pragma unroll
         for (int s = 0; s < 4; ++s)
@@ -709,6 +728,8 @@ template <int NJ> __global__ void __launch_bounds__(128) generate_adjoint_kernel
             w = (q == 1) ? zs : w;
             w = (q == 2) ? z2 : w;
             w = (q == 3) ? cmul(z2, zs) : w;
+            cf wn = cmul(w, v);
+            const float c4 = 2.f * v.x;
             float A = 0.f, B = 0.f;
 #pragma unroll
             for (int i = 0; i < NJ; ++i)
@@ -717,7 +738,11 @@ template <int NJ> __global__ void __launch_bounds__(128) generate_adjoint_kernel
                 A = fmaf(ca[i], w.x, A);
                 B = fmaf(-cb[i], w.y, B);
                 if (i + 1 < NJ)
-                    w = cmul(w, v);
+                {
+                    const cf next = {fmaf(c4, wn.x, -w.x), fmaf(c4, wn.y, -w.y)};
+                    w = wn;
+                    wn = next;
+                }
             }
             As[s] = A;
             Bs[s] = B;
@@ -856,7 +881,7 @@ template <int NJ> __global__ void __launch_bounds__(128) generate_adjoint_kernel
 
 template <int MAXM> cudaError_t launch_recon_adj(const ReconAdjDev &a, cudaStream_t stream)
 {
-    const int bytes = kTfCopies * 256 * (int)sizeof(float4);
+    const int bytes = kTfCopies * kTfCopyStride * (int)sizeof(float4);
     cudaError_t e =
         cudaFuncSetAttribute(reconstruct_adjoint_kernel<MAXM>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (e != cudaSuccess)
@@ -868,10 +893,11 @@ template <int MAXM> cudaError_t launch_recon_adj(const ReconAdjDev &a, cudaStrea
 }
 
 template <int MAXM>
-cudaError_t launch_prep_adj(int P, int m, const float *moments, float bias, const float *gl, float *gm,
+cudaError_t launch_prep_adj(int P, int m, const float2 *keep, float bias, const float *gl, float *gm,
                             cudaStream_t stream)
 {
-    prepare_adjoint_kernel<MAXM><<<(P + 63) / 64, 64, 0, stream>>>(P, m, moments, bias, gl, gm);
+    prepare_adjoint_kernel<MAXM><<<(P + kPrepAdjWarps - 1) / kPrepAdjWarps, 32 * kPrepAdjWarps, 0, stream>>>(
+        P, m, keep, bias, gl, gm);
     return cudaGetLastError();
 }
 
@@ -916,16 +942,12 @@ cudaError_t launch_reconstruct_adjoint(const ReconAdjArgs &r, int *error_flag, c
     return launch_recon_adj<64>(a, stream);
 }
 
-cudaError_t launch_prepare_adjoint(int num_pixels, int m, const float *moments, float bias, const float *grad_lambda,
+cudaError_t launch_prepare_adjoint(int num_pixels, int m, const float2 *keep, float bias, const float *grad_lambda,
                                    float *grad_moments, cudaStream_t stream)
 {
-    if (m <= 8)
-        return launch_prep_adj<8>(num_pixels, m, moments, bias, grad_lambda, grad_moments, stream);
-    if (m <= 16)
-        return launch_prep_adj<16>(num_pixels, m, moments, bias, grad_lambda, grad_moments, stream);
     if (m <= 32)
-        return launch_prep_adj<32>(num_pixels, m, moments, bias, grad_lambda, grad_moments, stream);
-    return launch_prep_adj<64>(num_pixels, m, moments, bias, grad_lambda, grad_moments, stream);
+        return launch_prep_adj<32>(num_pixels, m, keep, bias, grad_lambda, grad_moments, stream);
+    return launch_prep_adj<64>(num_pixels, m, keep, bias, grad_lambda, grad_moments, stream);
 }
 
 cudaError_t launch_generate_adjoint(const GridView &grid, float *grad_volume, const DeviceCamera &cam,

@@ -93,8 +93,16 @@ struct mraygb_context
     DeviceBuffer error_flag;
     // prediction coding and quantization
     DeviceBuffer coding_partial, coding_params_f, table, bits, bit_offset, scan_scratch64, packed;
-    // adjoint work buffers of the differentiation form
-    DeviceBuffer adj_lambda, adj_bounds;
+    // adjoint work buffers of the differentiation form; diff_keep: the preparation's Levinson solution and
+    // exponential moments (2m float2 per pixel) for the buffers and sizes in diff_key, valid while diff_key.valid
+    DeviceBuffer adj_lambda, adj_bounds, diff_keep;
+    struct
+    {
+        bool valid = false;
+        const float *moments = nullptr, *pmoments = nullptr;
+        int width = 0, height = 0, m = 0;
+        float bias = 0.f;
+    } diff_key;
     // the quantization curve: per-sample moments and errors, the means, the uploaded sample of the host call
     DeviceBuffer qc_scratch, qc_means, qc_index, qc_data;
     // error bounds and uncertainty rendering: the bounds and errors of the host calls, the 256 x 256 uncertainty
@@ -340,6 +348,18 @@ int run_prepare(mraygb_context *ctx, int width, int height, int m, const uint32_
         CK(launch_prepare(width * height, m, d_index, d_data, prediction_code, coding_warp, d_coding_params, bias,
                           ctx->precision != MRAYGB_PRECISION_FP32, d_out, ctx->stream),
            "prepare kernel launch");
+    ctx->launches += 1;
+    return MRAYGB_OK;
+}
+
+// the differentiation form's FP32 preparation of W*H*m moments, keeping its arrays in ctx->diff_keep
+int run_prepare_keep(mraygb_context *ctx, int width, int height, int m, const float *d_moments, float bias,
+                     float *d_out)
+{
+    const size_t P = (size_t)width * (size_t)height;
+    CK(ctx->diff_keep.reserve(P * 2 * (size_t)m * sizeof(float2)), "preparation buffer allocation");
+    CK(launch_prepare_keep((int)P, m, d_moments, bias, d_out, ctx->diff_keep.as<float2>(), ctx->stream),
+       "prepare kernel launch");
     ctx->launches += 1;
     return MRAYGB_OK;
 }
@@ -761,7 +781,7 @@ void mraygb_destroy(mraygb_context *ctx)
                             &ctx->pmoments, &ctx->rgba,    &ctx->rgba8,         &ctx->scan_scratch,
                             &ctx->error_flag, &ctx->coding_partial, &ctx->coding_params_f, &ctx->table,
                             &ctx->bits,    &ctx->bit_offset, &ctx->scan_scratch64, &ctx->packed,
-                            &ctx->adj_lambda, &ctx->adj_bounds, &ctx->qc_scratch, &ctx->qc_means,
+                            &ctx->adj_lambda, &ctx->adj_bounds, &ctx->diff_keep, &ctx->qc_scratch, &ctx->qc_means,
                             &ctx->qc_index, &ctx->qc_data, &ctx->error_bounds, &ctx->errors, &ctx->unc_table,
                             &ctx->unc_tf1d, &ctx->ss_keys, &ctx->ss_linear, &ctx->file_codes};
     for (DeviceBuffer *b : bufs)
@@ -2687,10 +2707,22 @@ int mraygb_diff_forward(mraygb_context *ctx, const mraygb_camera *cam, const mra
                               reinterpret_cast<float4 *>(d_bounds4));
     if (rc)
         return rc;
-    rc = run_prepare(ctx, width, height, m, nullptr, d_moments, 0, MRAYGB_CODING_WARP_NONE, nullptr, rp->bias,
-                     d_pmoments);
-    if (rc)
-        return rc;
+    ctx->diff_key.valid = false;
+    if (ctx->precision == MRAYGB_PRECISION_FP32)
+    {
+        // the FP32 multipliers, keeping what the preparation adjoint reads
+        rc = run_prepare_keep(ctx, width, height, m, d_moments, rp->bias, d_pmoments);
+        if (rc)
+            return rc;
+        ctx->diff_key = {true, d_moments, d_pmoments, width, height, m, rp->bias};
+    }
+    else
+    {
+        rc = run_prepare(ctx, width, height, m, nullptr, d_moments, 0, MRAYGB_CODING_WARP_NONE, nullptr, rp->bias,
+                         d_pmoments);
+        if (rc)
+            return rc;
+    }
     return run_reconstruct(ctx, cam, rp, width, height, m, ctx->dmin, ctx->dmax, nullptr, d_pmoments, nullptr, d_rgba,
                            nullptr, reinterpret_cast<const float4 *>(d_bounds4),
                            reinterpret_cast<const float4 *>(d_tf), 1);
@@ -2717,6 +2749,21 @@ int mraygb_diff_backward(mraygb_context *ctx, const mraygb_camera *cam, const mr
     const size_t P = (size_t)width * (size_t)height;
     CK(ctx->adj_lambda.reserve(P * (size_t)m * sizeof(float)), "adjoint buffer allocation");
     CK(ctx->adj_bounds.reserve(P * sizeof(float2)), "adjoint buffer allocation");
+    if (d_grad_volume)
+    {
+        const auto &k = ctx->diff_key;
+        if (!(k.valid && k.moments == d_moments && k.pmoments == d_pmoments && k.width == width &&
+              k.height == height && k.m == m && k.bias == rp->bias))
+        {
+            // the last forward kept nothing for these buffers (another precision form, or other buffers since):
+            // run the FP32 preparation again for its arrays, its multipliers into the adjoint buffer (overwritten
+            // below by the re-march adjoint)
+            rc = run_prepare_keep(ctx, width, height, m, d_moments, rp->bias, ctx->adj_lambda.as<float>());
+            if (rc)
+                return rc;
+            ctx->diff_key.valid = false;
+        }
+    }
     const DeviceCamera dc = to_device_camera(*cam);
     ReconAdjArgs a;
     a.cam = &dc;
@@ -2743,8 +2790,8 @@ int mraygb_diff_backward(mraygb_context *ctx, const mraygb_camera *cam, const mr
     ctx->launches += 1;
     if (!d_grad_volume)
         return MRAYGB_OK;
-    CK(launch_prepare_adjoint((int)P, m, d_moments, rp->bias, ctx->adj_lambda.as<float>(), ctx->adj_lambda.as<float>(),
-                              ctx->stream),
+    CK(launch_prepare_adjoint((int)P, m, ctx->diff_keep.as<float2>(), rp->bias, ctx->adj_lambda.as<float>(),
+                              ctx->adj_lambda.as<float>(), ctx->stream),
        "preparation adjoint launch");
     CK(launch_generate_adjoint(grid_view(ctx), d_grad_volume, dc, *gp, width, height, m, d_moments,
                                reinterpret_cast<const float4 *>(d_bounds4), ctx->adj_lambda.as<float>(),

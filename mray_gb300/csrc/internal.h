@@ -249,8 +249,12 @@ struct ReconAdjArgs
     float4 *grad_tf;
 };
 cudaError_t launch_reconstruct_adjoint(const ReconAdjArgs &a, int *error_flag, cudaStream_t stream);
-// d loss / d moments from d loss / d Lagrange multipliers (grad_moments may alias grad_lambda)
-cudaError_t launch_prepare_adjoint(int num_pixels, int m, const float *moments, float bias, const float *grad_lambda,
+// the FP32 multipliers of W*H*m moments (m <= 64) and, per pixel, the 2m float2 that the preparation adjoint reads
+cudaError_t launch_prepare_keep(int num_pixels, int m, const float *data, float bias, float *pmoments, float2 *keep,
+                                cudaStream_t stream);
+// d loss / d moments from d loss / d Lagrange multipliers and the arrays launch_prepare_keep kept (grad_moments may
+// alias grad_lambda)
+cudaError_t launch_prepare_adjoint(int num_pixels, int m, const float2 *keep, float bias, const float *grad_lambda,
                                    float *grad_moments, cudaStream_t stream);
 // d loss / d voxel density, accumulated into grad_volume
 cudaError_t launch_generate_adjoint(const GridView &grid, float *grad_volume, const DeviceCamera &cam,

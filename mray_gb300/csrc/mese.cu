@@ -183,7 +183,63 @@ cudaError_t launch_encode_t(int num_pixels, int m, const uint32_t *index, float 
     return cudaGetLastError();
 }
 
+// The differentiation form's preparation: the FP32 kernel's arithmetic on the uncompacted W*H*m image (so the same
+// multipliers), and in `keep` the two arrays of each pixel that the preparation adjoint reads, as 2m float2: P = 2 pi
+// x with x the Levinson solution (exactly zero from a latched step on, where the Herglotz check failed), then the
+// exponential moments with the zeroth halved.  Both are what lagrange_from_poly leaves in the pixel's arrays.
+template <int MAXM, int BLOCK>
+__global__ void __launch_bounds__(BLOCK) prepare_keep_kernel(int num_pixels, int m, const float *__restrict__ data,
+                                                             float bias, float *__restrict__ out,
+                                                             float2 *__restrict__ keep)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int p = blockIdx.x * BLOCK + threadIdx.x;
+    if (p >= num_pixels)
+        return;
+    const int n = m < MAXM ? m : MAXM;
+    const size_t idx = (size_t)p * (size_t)m;
+    cx<float> *base = reinterpret_cast<cx<float> *>(smem);
+    const Strided<cx<float>, BLOCK> e{base + threadIdx.x};
+    const Strided<cx<float>, BLOCK> poly{base + MAXM * BLOCK + threadIdx.x};
+    const Strided<float, BLOCK> acc{reinterpret_cast<float *>(base + 2 * MAXM * BLOCK) + threadIdx.x};
+    prepare_pixel<float, MAXM, BLOCK, false>(n, data + idx, e, poly, acc, 0, nullptr, bias, out + idx);
+    float2 *kp = keep + 2 * idx;
+    for (int k = 0; k < n; ++k)
+    {
+        const cx<float> a = poly[k], b = e[k];
+        kp[k] = make_float2(a.x, a.y);
+        kp[m + k] = make_float2(b.x, b.y);
+    }
+}
+
+template <int MAXM>
+cudaError_t launch_keep_t(int num_pixels, int m, const float *data, float bias, float *out, float2 *keep,
+                          cudaStream_t stream)
+{
+    constexpr int per = smem_per_thread<float, MAXM, 2, 1>();
+    constexpr int block = block_for<per>();
+    constexpr int bytes = per * block;
+    cudaError_t e = cudaFuncSetAttribute(prepare_keep_kernel<MAXM, block>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         bytes);
+    if (e != cudaSuccess)
+        return e;
+    if ((e = cudaFuncSetAttribute(prepare_keep_kernel<MAXM, block>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                  100)) != cudaSuccess)
+        return e;
+    prepare_keep_kernel<MAXM, block><<<(num_pixels + block - 1) / block, block, bytes, stream>>>(num_pixels, m, data,
+                                                                                              bias, out, keep);
+    return cudaGetLastError();
+}
+
 } // namespace
+
+cudaError_t launch_prepare_keep(int num_pixels, int m, const float *data, float bias, float *pmoments, float2 *keep,
+                                cudaStream_t stream)
+{
+    if (m <= 32)
+        return launch_keep_t<32>(num_pixels, m, data, bias, pmoments, keep, stream);
+    return launch_keep_t<64>(num_pixels, m, data, bias, pmoments, keep, stream);
+}
 
 cudaError_t mese_init_constants()
 {

@@ -138,13 +138,20 @@ __device__ __forceinline__ float4 tf_bspline_derivative(const float4 *T, const B
 //   cos(theta) > 0 : lam = -4 sin^2(theta/2),  u <- u + d,  d <- a_k + lam u + d
 //   cos(theta) <= 0: lam =  4 cos^2(theta/2),  u <- d - u,  d <- a_k + lam u - d
 //   S = d - (lam / 2) u
-template <int MAXM> __device__ __forceinline__ float mese_series(const float (&lam2)[MAXM], float lam0, float pc)
+// (reinsch_lambda gives lam and the branch; a caller that runs a second recurrence at the same theta takes them
+// once)
+__device__ __forceinline__ float reinsch_lambda(float pc, bool &pos)
 {
     float sh, ch;
     sincosf(0.5f * pc, &sh, &ch);
-    const bool pos = fabsf(pc) < 1.5707963267948966f; // cos(pc) > 0
+    pos = fabsf(pc) < 1.5707963267948966f; // cos(pc) > 0
+    return pos ? -4.f * sh * sh : 4.f * ch * ch;
+}
+
+template <int MAXM>
+__device__ __forceinline__ float mese_series_reinsch(const float (&lam2)[MAXM], float lam0, bool pos, float lam)
+{
     const float sg = pos ? 1.f : -1.f;
-    const float lam = pos ? -4.f * sh * sh : 4.f * ch * ch;
     float u = 0.f, d = 0.f;
 #pragma unroll
     for (int l = MAXM - 1; l >= 1; --l)
@@ -155,6 +162,13 @@ template <int MAXM> __device__ __forceinline__ float mese_series(const float (&l
     u = fmaf(sg, u, d);
     d = fmaf(lam, u, fmaf(sg, d, lam0));
     return fmaf(-0.5f * lam, u, d);
+}
+
+template <int MAXM> __device__ __forceinline__ float mese_series(const float (&lam2)[MAXM], float lam0, float pc)
+{
+    bool pos;
+    const float lam = reinsch_lambda(pc, pos);
+    return mese_series_reinsch<MAXM>(lam2, lam0, pos, lam);
 }
 
 // the bounded density at phase p: lo + span (atan(S) / pi + 1/2) (MESEReconstruction::reconstruct,

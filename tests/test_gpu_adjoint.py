@@ -121,6 +121,33 @@ def test_l2_adjoint_against_gpu_central_differences(gpu_context):
     assert rel.max() <= 1e-2, f"max rel err {rel.max():.3e} at {params[int(rel.argmax())]}"
 
 
+def test_preparation_adjoint_without_the_kept_arrays(gpu_context):
+    """The forward keeps the preparation's Levinson solution and exponential moments for the backward on the same
+    buffers.  A backward on buffers of an earlier forward (another forward ran since) and a backward after a
+    forward in the float-float precision form prepare them again: the first must give the gradients of the kept
+    path (up to the order of the float atomics), the second those of its own multipliers (within 1e-3 of the FP32
+    forward's gradients)."""
+    import mray_gb300 as M
+
+    wl, _ = _workload(m=31)
+    table = O.preintegrate(wl.tf1d, wl.tf_step)
+    weights = np.random.default_rng(9).standard_normal((wl.height, wl.width, 4))
+    R1, R2 = GpuRender(gpu_context, wl), GpuRender(gpu_context, wl)
+    R1.forward(wl.volume, table)
+    gtf, gvol = R1.backward(weights)
+    R2.forward(wl.volume, table)
+    gtf2, gvol2 = R1.backward(weights)
+    assert np.allclose(gvol2, gvol, rtol=1e-5, atol=1e-6 * np.abs(gvol).max())
+    assert np.allclose(gtf2, gtf, rtol=1e-5, atol=1e-6 * np.abs(gtf).max())
+    gpu_context.precision = M.PRECISION_COMPENSATED_FF_MESE
+    try:
+        R1.forward(wl.volume, table)
+        _, gvol3 = R1.backward(weights)
+    finally:
+        gpu_context.precision = M.PRECISION_FP32
+    assert np.abs(gvol3 - gvol).max() <= 1e-3 * np.abs(gvol).max()
+
+
 def test_autograd_function_and_tf1d_chain(gpu_context):
     """torch.autograd.Function: the same gradients as the direct calls, and through preintegrate_table to the 1D
     extinction / emission entries."""
