@@ -50,6 +50,16 @@ struct ReconAdjDev
     int *error_flag;
 };
 
+// The transfer-function gradient of a block is accumulated in kTfCopies copies of the 256-entry row in shared
+// memory, lane l adding to copy l mod kTfCopies: neighbouring rays sample similar densities at the same step, and
+// shared-memory atomics on one address from many lanes of a warp serialize.  Row and gradient are held as one float
+// table per channel (scalar loads and atomics: lanes whose entries differ by less than 32 never share a bank; the
+// float4 entries of a gather conflicted whenever two entries of a quarter-warp were 8 apart), the tables of the
+// copies kTfCopyStride = 257 floats apart (copy c's channel ch at (4 c + ch) * 257), so the lanes that add to the same
+// entry in their own copies fall into different banks.
+constexpr int kTfCopies = 8;
+constexpr int kTfCopyStride = 257;
+
 // accumulates the B-spline weights times g into the shared transfer-function gradient through a cache of the
 // last four entries: consecutive samples of a ray mostly fall between the same knots
 struct TfGradCache
@@ -57,7 +67,8 @@ struct TfGradCache
     int base = -1000;
     float4 acc[4];
 
-    __device__ __forceinline__ void flush(float4 *s_g)
+    // s_g: this lane's copy, channel c at c * kTfCopyStride
+    __device__ __forceinline__ void flush(float *s_g)
     {
         if (base <= -1000)
             return;
@@ -65,13 +76,13 @@ struct TfGradCache
         for (int j = 0; j < 4; ++j)
         {
             const int x = min(max(base - 1 + j, 0), 255);
-            atomicAdd(&s_g[x].x, acc[j].x);
-            atomicAdd(&s_g[x].y, acc[j].y);
-            atomicAdd(&s_g[x].z, acc[j].z);
-            atomicAdd(&s_g[x].w, acc[j].w);
+            atomicAdd(&s_g[x], acc[j].x);
+            atomicAdd(&s_g[kTfCopyStride + x], acc[j].y);
+            atomicAdd(&s_g[2 * kTfCopyStride + x], acc[j].z);
+            atomicAdd(&s_g[3 * kTfCopyStride + x], acc[j].w);
         }
     }
-    __device__ __forceinline__ void add(float4 *s_g, const BSplineTap &k, float4 g)
+    __device__ __forceinline__ void add(float *s_g, const BSplineTap &k, float4 g)
     {
         if (k.i != base)
         {
@@ -92,23 +103,24 @@ struct TfGradCache
     }
 };
 
-// The transfer-function gradient of a block is accumulated in kTfCopies copies of the 256-entry table in shared
-// memory, lane l adding to copy l mod kTfCopies: neighbouring rays sample similar densities at the same step, and
-// shared-memory atomics on one address from many lanes of a warp serialize.
-constexpr int kTfCopies = 8;
-constexpr int kTfCopyStride = 256;
 
 template <int MAXM> __global__ void __launch_bounds__(128, 4) reconstruct_adjoint_kernel(const ReconAdjDev a)
 {
-    __shared__ float4 s_tf[256];
-    extern __shared__ float4 s_gall[]; // kTfCopies * kTfCopyStride (dynamic: above the 48 KiB of static shared memory)
+    __shared__ float s_tf[4 * 256]; // channel c of entry i at c * 256 + i
+    extern __shared__ float s_gall[]; // kTfCopies * 4 * kTfCopyStride (dynamic: above the 48 KiB of static memory)
     const int tid = threadIdx.x + threadIdx.y * blockDim.x;
     for (int i = tid; i < 256; i += blockDim.x * blockDim.y)
-        s_tf[i] = a.tf[i];
-    for (int i = tid; i < kTfCopies * kTfCopyStride; i += blockDim.x * blockDim.y)
-        s_gall[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    {
+        const float4 v = a.tf[i];
+        s_tf[i] = v.x;
+        s_tf[256 + i] = v.y;
+        s_tf[512 + i] = v.z;
+        s_tf[768 + i] = v.w;
+    }
+    for (int i = tid; i < kTfCopies * 4 * kTfCopyStride; i += blockDim.x * blockDim.y)
+        s_gall[i] = 0.f;
     __syncthreads();
-    float4 *s_g = s_gall + (tid % kTfCopies) * kTfCopyStride;
+    float *s_g = s_gall + (tid % kTfCopies) * 4 * kTfCopyStride;
 
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
@@ -168,7 +180,7 @@ template <int MAXM> __global__ void __launch_bounds__(128, 4) reconstruct_adjoin
                 const float fs = r * span + lo;
                 const BSplineTap k = bspline_tap(fs);
                 float4 s, dt;
-                tf_bspline_value_derivative(s_tf, k, s, dt);
+                tf_bspline_value_derivative_soa(s_tf, k, s, dt);
                 // d loss / d sample: emission terms see T before this step, extinction the radiance behind it
                 float4 gs;
                 gs.x = g.x * a.emission * T;
@@ -237,26 +249,15 @@ template <int MAXM> __global__ void __launch_bounds__(128, 4) reconstruct_adjoin
     }
     cache.flush(s_g);
     __syncthreads();
-    for (int i = tid; i < 256; i += blockDim.x * blockDim.y)
+    for (int i = tid; i < 4 * 256; i += blockDim.x * blockDim.y)
     {
-        float4 v = s_gall[i];
+        const int ch = i >> 8, e = i & 255;
+        float v = 0.f;
 #pragma unroll
-        for (int c = 1; c < kTfCopies; ++c)
-        {
-            const float4 w = s_gall[c * kTfCopyStride + i];
-            v.x += w.x;
-            v.y += w.y;
-            v.z += w.z;
-            v.w += w.w;
-        }
-        if (v.x != 0.f)
-            atomicAdd(&a.grad_tf[i].x, v.x);
-        if (v.y != 0.f)
-            atomicAdd(&a.grad_tf[i].y, v.y);
-        if (v.z != 0.f)
-            atomicAdd(&a.grad_tf[i].z, v.z);
-        if (v.w != 0.f)
-            atomicAdd(&a.grad_tf[i].w, v.w);
+        for (int c = 0; c < kTfCopies; ++c)
+            v += s_gall[(4 * c + ch) * kTfCopyStride + e];
+        if (v != 0.f)
+            atomicAdd(reinterpret_cast<float *>(a.grad_tf + e) + ch, v);
     }
 }
 
@@ -292,6 +293,12 @@ __device__ __forceinline__ void cacc(float2 &s, float2 v)
     s.y += v.y;
 }
 
+// two consecutive complex values (an even index of a 16-byte aligned array) in one shared-memory load: the operand
+// every lane reads at the same index comes in pairs, halving those loads
+__device__ __forceinline__ float4 ld_pair(const float2 *p) { return *reinterpret_cast<const float4 *>(p); }
+__device__ __forceinline__ float2 lo2(float4 v) { return make_float2(v.x, v.y); }
+__device__ __forceinline__ float2 hi2(float4 v) { return make_float2(v.z, v.w); }
+
 __device__ __forceinline__ float warp_sum(float v)
 {
 #pragma unroll
@@ -300,7 +307,8 @@ __device__ __forceinline__ float warp_sum(float v)
     return v;
 }
 
-// per warp in shared memory (complex values as float2), M = MAXM
+// per warp in shared memory (complex values as float2), M = MAXM (even: the loops below step over index pairs and read
+// one entry past an odd bound, which every array holds as zero)
 template <int M> struct PrepAdjSmem
 {
     float2 xp[3 * M]; // P at offset M, zeros on both sides
@@ -372,8 +380,12 @@ __global__ void __launch_bounds__(32 * kPrepAdjWarps) prepare_adjoint_kernel(int
     {
         const int q = lane + 32 * i;
         float2 acc = z2;
-        for (int j = 0; j < n; ++j)
-            cacc(acc, cmulcj(s.xp[M + j], s.xp[M + j + q]));
+        for (int j = 0; j < n; j += 2)
+        {
+            const float4 pj = ld_pair(&s.xp[M + j]);
+            cacc(acc, cmulcj(lo2(pj), s.xp[M + j + q]));
+            cacc(acc, cmulcj(hi2(pj), s.xp[M + j + 1 + q]));
+        }
         s.a[q] = q < n ? acc : z2;
     }
     __syncwarp();
@@ -384,10 +396,12 @@ __global__ void __launch_bounds__(32 * kPrepAdjWarps) prepare_adjoint_kernel(int
     {
         const int k = lane + 32 * i;
         float acc = 0.f;
-        for (int d = 0; d < n; ++d)
+        for (int d = 0; d < n; d += 2)
         {
-            const float2 av = s.a[k + d], e = s.eh[M + d];
-            acc += av.x * e.y + av.y * e.x;
+            const float4 e = ld_pair(&s.eh[M + d]);
+            const float2 a0 = s.a[k + d], a1 = s.a[k + d + 1];
+            acc += a0.x * e.y + a0.y * e.x;
+            acc += a1.x * e.w + a1.y * e.z;
         }
         gn += s.gc[k] * acc;
     }
@@ -405,17 +419,18 @@ __global__ void __launch_bounds__(32 * kPrepAdjWarps) prepare_adjoint_kernel(int
     {
         const int q = lane + 32 * i;
         float2 gA = z2, gE = z2;
-        for (int k = 0; k < n; ++k)
+        for (int k = 0; k < n; k += 2)
         {
-            const float g = s.gc[k];
-            const float2 e = s.eh[M + q - k], av = s.a[k + q];
-            gA.x += g * e.y;
-            gA.y += g * e.x;
-            gE.x += g * av.y;
-            gE.y += g * av.x;
+            const float2 g = *reinterpret_cast<const float2 *>(&s.gc[k]);
+            const float2 e0 = s.eh[M + q - k], e1 = s.eh[M + q - k - 1];
+            const float2 a0 = s.a[k + q], a1 = s.a[k + q + 1];
+            gA.x += g.x * e0.y + g.y * e1.y;
+            gA.y += g.x * e0.x + g.y * e1.x;
+            gE.x += g.x * a0.y + g.y * a1.y;
+            gE.y += g.x * a0.x + g.y * a1.x;
         }
-        s.ga[q] = gA;
-        s.ge[q] = gE;
+        s.ga[q] = q < n ? gA : z2;
+        s.ge[q] = q < n ? gE : z2;
     }
     __syncwarp();
     // A_q = sum_j P_j conj(P_{j+q}): gP_j += gA_q P_{j+q} + conj(gA_q) P_{j-q}; P_0 also through the norm
@@ -424,11 +439,13 @@ __global__ void __launch_bounds__(32 * kPrepAdjWarps) prepare_adjoint_kernel(int
     {
         const int j = lane + 32 * i;
         float2 g = z2;
-        for (int q = 0; q < n; ++q)
+        for (int q = 0; q < n; q += 2)
         {
-            const float2 gA = s.ga[q];
-            cacc(g, cmul2(gA, s.xp[M + j + q]));
-            cacc(g, cmulcj(s.xp[M + j - q], gA));
+            const float4 gA = ld_pair(&s.ga[q]);
+            cacc(g, cmul2(lo2(gA), s.xp[M + j + q]));
+            cacc(g, cmulcj(s.xp[M + j - q], lo2(gA)));
+            cacc(g, cmul2(hi2(gA), s.xp[M + j + q + 1]));
+            cacc(g, cmulcj(s.xp[M + j - q - 1], hi2(gA)));
         }
         if (j == 0)
             g.x -= gn * norm / P0;
@@ -449,11 +466,13 @@ __global__ void __launch_bounds__(32 * kPrepAdjWarps) prepare_adjoint_kernel(int
     {
         const int r = lane + 32 * i;
         float2 t1 = z2, t2 = z2;
-        for (int c = 0; c < nn; ++c)
+        for (int c = 0; c < nn; c += 2)
         {
-            const float2 g = s.gp[c];
-            cacc(t1, cmulcj(g, s.xp[M + c - r]));
-            cacc(t2, cmulcj(g, s.ww[M + c - r]));
+            const float4 g = ld_pair(&s.gp[c]);
+            cacc(t1, cmulcj(lo2(g), s.xp[M + c - r]));
+            cacc(t2, cmulcj(lo2(g), s.ww[M + c - r]));
+            cacc(t1, cmulcj(hi2(g), s.xp[M + c + 1 - r]));
+            cacc(t2, cmulcj(hi2(g), s.ww[M + c + 1 - r]));
         }
         s.t[r] = r < nn ? make_float4(t1.x, t1.y, t2.x, t2.y) : make_float4(0.f, 0.f, 0.f, 0.f);
     }
@@ -484,11 +503,13 @@ __global__ void __launch_bounds__(32 * kPrepAdjWarps) prepare_adjoint_kernel(int
     {
         const int d = lane + 32 * i;
         float2 lev = z2;
-        for (int c = 0; c < nn; ++c)
+        for (int c = 0; c < nn; c += 2)
         {
-            const float2 pc = s.xp[M + c], yc = s.a[c];
-            cacc(lev, cmulcj(s.a[c + d], pc));
-            cacc(lev, cmulcj(s.xp[M + c + d], yc));
+            const float4 pc = ld_pair(&s.xp[M + c]), yc = ld_pair(&s.a[c]);
+            cacc(lev, cmulcj(s.a[c + d], lo2(pc)));
+            cacc(lev, cmulcj(s.xp[M + c + d], lo2(yc)));
+            cacc(lev, cmulcj(s.a[c + d + 1], hi2(pc)));
+            cacc(lev, cmulcj(s.xp[M + c + d + 1], hi2(yc)));
         }
         float2 g = s.ge[d];
         if (d == 0)
@@ -508,10 +529,12 @@ __global__ void __launch_bounds__(32 * kPrepAdjWarps) prepare_adjoint_kernel(int
     {
         const int k = lane + 32 * i;
         float acc = 0.f;
-        for (int l = 0; l < n; ++l)
+        for (int l = 0; l < n; l += 2)
         {
-            const float2 g = s.ge[l], e = s.eh[M + l - k];
-            acc += g.x * e.y - g.y * e.x;
+            const float4 g = ld_pair(&s.ge[l]);
+            const float2 e0 = s.eh[M + l - k], e1 = s.eh[M + l + 1 - k];
+            acc += g.x * e0.y - g.y * e0.x;
+            acc += g.z * e1.y - g.w * e1.x;
         }
         if (k < n)
             grad_moments[idx + k] = omb * (k == 0 ? -kPi * acc : -kTwoPi * acc);
@@ -708,8 +731,10 @@ template <int NJ> __global__ void __launch_bounds__(128) generate_adjoint_kernel
                               __fadd_rn(o[2], __fmul_rn(my_t, d[2])));
             s_my = grid_blend(a.grid, q_my);
             f_my = map_density(s_my, a.data_min, a.data_max);
+            // the segment's phase factor only weighs the gradient (no forward value is replayed from it): the
+            // hardware sine and cosine (absolute error about 4e-7 on [-pi - h, 0]) are accurate enough for it
             float sn, cs;
-            sincosf(p_my - h, &sn, &cs);
+            __sincosf(p_my - h, &sn, &cs);
             z = {cs, -sn};
         }
         // partial A, B of the four segments over this lane's moments j = q + 4i: both parts of z^j follow the
@@ -881,7 +906,7 @@ template <int NJ> __global__ void __launch_bounds__(128) generate_adjoint_kernel
 
 template <int MAXM> cudaError_t launch_recon_adj(const ReconAdjDev &a, cudaStream_t stream)
 {
-    const int bytes = kTfCopies * kTfCopyStride * (int)sizeof(float4);
+    const int bytes = kTfCopies * 4 * kTfCopyStride * (int)sizeof(float);
     cudaError_t e =
         cudaFuncSetAttribute(reconstruct_adjoint_kernel<MAXM>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (e != cudaSuccess)

@@ -186,29 +186,41 @@ cudaError_t launch_encode_t(int num_pixels, int m, const uint32_t *index, float 
 // The differentiation form's preparation: the FP32 kernel's arithmetic on the uncompacted W*H*m image (so the same
 // multipliers), and in `keep` the two arrays of each pixel that the preparation adjoint reads, as 2m float2: P = 2 pi
 // x with x the Levinson solution (exactly zero from a latched step on, where the Herglotz check failed), then the
-// exponential moments with the zeroth halved.  Both are what lagrange_from_poly leaves in the pixel's arrays.
+// exponential moments with the zeroth halved.  Both are what lagrange_from_poly leaves in the pixel's arrays.  The
+// arrays' stride is BLOCK + 1 elements, so that the block's copy-out (one pixel's elements in a row, then the next
+// pixel's: the block's kept arrays are one contiguous run) reads shared memory with at most two-way conflicts and
+// writes global memory coalesced.
+template <int MAXM, int BLOCK> constexpr int keep_smem_bytes()
+{
+    return MAXM * (BLOCK + 1) * (2 * (int)sizeof(cx<float>) + (int)sizeof(float));
+}
+
 template <int MAXM, int BLOCK>
 __global__ void __launch_bounds__(BLOCK) prepare_keep_kernel(int num_pixels, int m, const float *__restrict__ data,
                                                              float bias, float *__restrict__ out,
                                                              float2 *__restrict__ keep)
 {
     extern __shared__ __align__(16) unsigned char smem[];
+    constexpr int S = BLOCK + 1;
     const int p = blockIdx.x * BLOCK + threadIdx.x;
-    if (p >= num_pixels)
-        return;
     const int n = m < MAXM ? m : MAXM;
-    const size_t idx = (size_t)p * (size_t)m;
     cx<float> *base = reinterpret_cast<cx<float> *>(smem);
-    const Strided<cx<float>, BLOCK> e{base + threadIdx.x};
-    const Strided<cx<float>, BLOCK> poly{base + MAXM * BLOCK + threadIdx.x};
-    const Strided<float, BLOCK> acc{reinterpret_cast<float *>(base + 2 * MAXM * BLOCK) + threadIdx.x};
-    prepare_pixel<float, MAXM, BLOCK, false>(n, data + idx, e, poly, acc, 0, nullptr, bias, out + idx);
-    float2 *kp = keep + 2 * idx;
-    for (int k = 0; k < n; ++k)
+    const Strided<cx<float>, S> e{base + threadIdx.x};
+    const Strided<cx<float>, S> poly{base + MAXM * S + threadIdx.x};
+    const Strided<float, S> acc{reinterpret_cast<float *>(base + 2 * MAXM * S) + threadIdx.x};
+    if (p < num_pixels)
+        prepare_pixel<float, MAXM, BLOCK, false>(n, data + (size_t)p * (size_t)m, e, poly, acc, 0, nullptr, bias,
+                                                 out + (size_t)p * (size_t)m);
+    __syncthreads();
+    const int p0 = blockIdx.x * BLOCK;
+    const int np = min(BLOCK, num_pixels - p0);
+    const int per = 2 * n;
+    float2 *dst = keep + (size_t)p0 * (size_t)per;
+    for (int i = threadIdx.x; i < np * per; i += BLOCK)
     {
-        const cx<float> a = poly[k], b = e[k];
-        kp[k] = make_float2(a.x, a.y);
-        kp[m + k] = make_float2(b.x, b.y);
+        const int t = i / per, k = i - t * per;
+        const cx<float> v = k < n ? base[MAXM * S + k * S + t] : base[(k - n) * S + t];
+        dst[i] = make_float2(v.x, v.y);
     }
 }
 
@@ -216,9 +228,8 @@ template <int MAXM>
 cudaError_t launch_keep_t(int num_pixels, int m, const float *data, float bias, float *out, float2 *keep,
                           cudaStream_t stream)
 {
-    constexpr int per = smem_per_thread<float, MAXM, 2, 1>();
-    constexpr int block = block_for<per>();
-    constexpr int bytes = per * block;
+    constexpr int block = block_for<smem_per_thread<float, MAXM, 2, 1>()>();
+    constexpr int bytes = keep_smem_bytes<MAXM, block>();
     cudaError_t e = cudaFuncSetAttribute(prepare_keep_kernel<MAXM, block>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          bytes);
     if (e != cudaSuccess)

@@ -115,6 +115,31 @@ __device__ __forceinline__ void tf_bspline_value_derivative(const float4 *T, con
     }
 }
 
+// the same from one float table per channel (channel c of entry i at c * 256 + i): the same operations
+__device__ __forceinline__ void tf_bspline_value_derivative_soa(const float *T, const BSplineTap &k, float4 &val,
+                                                                float4 &dval)
+{
+    const float t = k.t, s = 1.f - t;
+    const float d[4] = {-128.f * s * s, 128.f * (3.f * t * t - 4.f * t), 128.f * (-3.f * t * t + 2.f * t + 1.f),
+                        128.f * t * t};
+    val = make_float4(0.f, 0.f, 0.f, 0.f);
+    dval = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+    {
+        const int i = bspline_entry(k, j);
+        const float4 e = make_float4(T[i], T[256 + i], T[512 + i], T[768 + i]);
+        val.x = fmaf(k.w[j], e.x, val.x);
+        val.y = fmaf(k.w[j], e.y, val.y);
+        val.z = fmaf(k.w[j], e.z, val.z);
+        val.w = fmaf(k.w[j], e.w, val.w);
+        dval.x = fmaf(d[j], e.x, dval.x);
+        dval.y = fmaf(d[j], e.y, dval.y);
+        dval.z = fmaf(d[j], e.z, dval.z);
+        dval.w = fmaf(d[j], e.w, dval.w);
+    }
+}
+
 // d tf_sample_bspline / d fs (256 d / d u)
 __device__ __forceinline__ float4 tf_bspline_derivative(const float4 *T, const BSplineTap &k)
 {
