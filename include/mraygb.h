@@ -438,14 +438,17 @@ int mraygb_stage_reconstruct(mraygb_context *ctx, const mraygb_camera *cam, cons
  * transform_to_bounds = 1; m <= 64), Lagrange multipliers in the context's precision form, re-march with the
  * transfer-function row d_tf (256 RGBA floats).  Writes d_moments (W*H*m), d_bounds4 (W*H*4: lo, hi and the
  * samples' min, max), d_pmoments (W*H*m) and d_rgba (W*H*4), which the backward reads.  16-byte aligned float4
- * buffers. */
+ * buffers.  In the FP32 precision form the context also keeps, for these buffers, the preparation's Levinson
+ * solution and exponential moments (W*H*2m complex floats), which the backward's preparation adjoint reads. */
 int mraygb_diff_forward(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_generation_params *gp,
                         const mraygb_reconstruction_params *rp, int width, int height, int m, const float *d_tf,
                         float *d_moments, float *d_bounds4, float *d_pmoments, float *d_rgba);
 
 /* Adjoint of mraygb_diff_forward for the loss gradient d_grad_rgba (W*H*4): adds d loss / d transfer-function row
  * to d_grad_tf (256*4) and, when d_grad_volume is not NULL (regular grids only), d loss / d voxel density to
- * d_grad_volume (nx*ny*nz).  The forward's buffers must be unchanged. */
+ * d_grad_volume (nx*ny*nz).  The forward's buffers must be unchanged.  When the context's kept preparation arrays
+ * belong to other buffers (another forward ran since, or the forward ran in another precision form), the volume
+ * gradient first runs the FP32 preparation of d_moments again to rebuild them. */
 int mraygb_diff_backward(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_generation_params *gp,
                          const mraygb_reconstruction_params *rp, int width, int height, int m, const float *d_tf,
                          const float *d_moments, const float *d_bounds4, const float *d_pmoments, const float *d_rgba,
