@@ -428,11 +428,24 @@ int mraygb_stage_reconstruct(mraygb_context *ctx, const mraygb_camera *cam, cons
                              const uint16_t *d_bounds, float *d_rgba, uint8_t *d_rgba8);
 
 /* ---- differentiation form -------------------------------------------------------------------------------
- * No counterpart in the reference.  The moment-image method with three changes that make an image-space loss
- * piecewise smooth in the volume and the transfer function: no compaction (every pixel keeps m moments), the
- * re-march reads the unquantized per-pixel density bounds, and the transfer-function row is sampled linearly in
- * the front density with the texture convention of the reference's GPU path (TransferFunctionDevice::sample,
- * src/transfer_function_device.cuh:30-65).  All buffers are device pointers on the context's stream. */
+ * No counterpart in the reference.  The moment-image method with four changes that make an image-space loss
+ * smooth almost everywhere in the volume and the transfer function: no compaction (every pixel keeps m moments),
+ * the re-march reads the unquantized per-pixel density bounds, the MESE density uses the exact arctangent, and the
+ * transfer-function row is sampled in the front density at the texel centres of the reference's GPU texture
+ * (TransferFunctionDevice::sample, src/transfer_function_device.cuh:30-65: u = 256 fs - 1/2, clamp to edge), as a
+ * uniform cubic B-spline (the default: the loss is then smooth where a density crosses an entry) or linearly, the
+ * GPU path's own interpolation with exact weights (mraygb_set_diff_tf_sampling).  All buffers are device pointers
+ * on the context's stream. */
+
+enum
+{
+    MRAYGB_DIFF_TF_BSPLINE = 0, /* the row as a uniform cubic B-spline in the front density */
+    MRAYGB_DIFF_TF_LINEAR = 1   /* the row linear in the front density (the reference's GPU sampling) */
+};
+
+/* Selects the differentiation form's transfer-function sampling for the later forward and backward calls of the
+ * context (MRAYGB_DIFF_TF_BSPLINE by default).  A backward must run with the sampling of its forward. */
+int mraygb_set_diff_tf_sampling(mraygb_context *ctx, int sampling);
 
 /* Forward over the volume uploaded last: generate (gp->compact_image = 0, prediction_coding = 0,
  * transform_to_bounds = 1; m <= 64), Lagrange multipliers in the context's precision form, re-march with the

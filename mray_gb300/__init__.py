@@ -7,7 +7,7 @@ grid and transfer-function containers) and calls the C ABI through ctypes.
 from .types import (CODING_WARP_DEFAULT_TRANSFORMED, CODING_WARP_NONE, ERROR_PERCENTILE, MAX_ERROR, RMSE, Camera,
                     ErrorReconstructionParameters, GenerationParameters, ReconstructionParameters,
                     ReferenceParameters, SingleScatteringParameters, UncertaintyReconstructionParameters)
-from .raymarcher import (MAX_MOMENTS, PRECISION_COMPENSATED_FF_MESE, PRECISION_COMPENSATED_FP64_MESE, PRECISION_FP32, ColorImageHost, Context,
+from .raymarcher import (DIFF_TF_BSPLINE, DIFF_TF_LINEAR, MAX_MOMENTS, PRECISION_COMPENSATED_FF_MESE, PRECISION_COMPENSATED_FP64_MESE, PRECISION_FP32, ColorImageHost, Context,
                          MomentImageHost, Particles, RegularGrid, TransferFunction, default_context, default_quantization_table,
                          generate, preintegrate, quantize_prediction_coding, dequantize_prediction_coding,
                          reconstruct,
@@ -23,7 +23,8 @@ __all__ = [
     "Camera", "GenerationParameters", "ReconstructionParameters", "CODING_WARP_DEFAULT_TRANSFORMED",
     "CODING_WARP_NONE", "ColorImageHost", "Context", "MomentImageHost", "Particles", "RegularGrid", "TransferFunction",
     "default_context", "default_quantization_table", "create_quantization_table", "quantize_prediction_coding", "dequantize_prediction_coding", "generate", "preintegrate", "reconstruct", "MrayError", "PRECISION_FP32",
-    "PRECISION_COMPENSATED_FP64_MESE", "PRECISION_COMPENSATED_FF_MESE", "MAX_MOMENTS",
+    "PRECISION_COMPENSATED_FP64_MESE", "PRECISION_COMPENSATED_FF_MESE", "MAX_MOMENTS", "DIFF_TF_BSPLINE",
+    "DIFF_TF_LINEAR",
     "ErrorReconstructionParameters", "UncertaintyReconstructionParameters", "MAX_ERROR", "RMSE", "ERROR_PERCENTILE",
     "UncertaintyTransferFunction", "read_from_disk_uncertainty", "reconstruct_error",
     "reconstruct_uncertainty_interpolation", "reconstruct_uncertainty_convolution", "generate_reference",

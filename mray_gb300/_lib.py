@@ -35,7 +35,7 @@ EXPORTS = [
     "mraygb_encode_moment_image", "mraygb_copy_encoded", "mraygb_decode_moment_image", "mraygb_write_moment_image",
     "mraygb_load_moment_image", "mraygb_lz4_compress", "mraygb_lz4_decompress", "mraygb_entropy_encode",
     "mraygb_entropy_decode", "mraygb_stage_libm_sincosf", "mraygb_dequantize_prediction_coding",
-    "mraygb_measure_fp32_rate",
+    "mraygb_measure_fp32_rate", "mraygb_set_diff_tf_sampling",
 ]
 
 _lock = threading.Lock()
@@ -62,6 +62,7 @@ def _declare(L):
     L.mraygb_get_stream.restype = vp
     L.mraygb_synchronize.argtypes = [vp]
     L.mraygb_set_precision.argtypes = [vp, i]
+    L.mraygb_set_diff_tf_sampling.argtypes = [vp, i]
     L.mraygb_kernel_launches.argtypes = [vp]
     L.mraygb_kernel_launches.restype = C.c_uint64
     L.mraygb_upload_grid.argtypes = [vp, vp, i, i, i, C.c_float * 3, C.c_float * 3, i]

@@ -2,8 +2,10 @@
 adjoint (the CUDA kernels behind mraygb_diff_forward / mraygb_diff_backward).
 
 The differentiated method is the moment-image path (generate -> Lagrange multipliers -> MESE re-march) without
-compaction, with the unquantized per-pixel density bounds and with the transfer-function row sampled linearly
-in the front density.  Gradients flow to the transfer-function row (256 x RGBA, the preintegrated table) and to
+compaction, with the unquantized per-pixel density bounds, the exact arctangent and the transfer-function row
+sampled in the front density as a cubic B-spline (``RenderSpec.tf_sampling = DIFF_TF_BSPLINE``, the default) or
+linearly as the reference's GPU texture samples it (``DIFF_TF_LINEAR``).  Gradients flow to the transfer-function
+row (256 x RGBA, the preintegrated table) and to
 the voxel densities; ``preintegrate_table`` builds that row from a 1D transfer function with torch operations, so
 gradients reach the 1D extinction (alpha) and emission (rgb) tables through ordinary autograd.
 """
@@ -14,7 +16,7 @@ from typing import Optional
 
 import torch
 
-from .raymarcher import Context, default_context
+from .raymarcher import DIFF_TF_BSPLINE, Context, default_context
 from .types import Camera, GenerationParameters, ReconstructionParameters
 
 
@@ -38,6 +40,7 @@ class RenderSpec:
     domain_min: tuple
     domain_max: tuple
     context: Optional[Context] = None
+    tf_sampling: int = DIFF_TF_BSPLINE
 
     def ctx(self) -> Context:
         return self.context or default_context(torch.cuda.current_device())
@@ -57,6 +60,7 @@ class MomentRender(torch.autograd.Function):
         bounds4 = torch.empty(W * H * 4, dtype=torch.float32, device=dev)
         pmoments = torch.empty(W * H * m, dtype=torch.float32, device=dev)
         rgba = torch.empty((H, W, 4), dtype=torch.float32, device=dev)
+        ctx.diff_tf_sampling = spec.tf_sampling
         ctx.diff_forward(spec.camera, spec.gen, spec.rec, W, H, m, tf, moments, bounds4, pmoments, rgba)
         fctx.save_for_backward(vol, tf, moments, bounds4, pmoments, rgba)
         fctx.spec = spec
@@ -74,6 +78,7 @@ class MomentRender(torch.autograd.Function):
         g = grad_rgba.contiguous().float()
         grad_tf = torch.zeros_like(tf)
         grad_vol = torch.zeros_like(vol) if fctx.need_volume else None
+        ctx.diff_tf_sampling = spec.tf_sampling
         ctx.diff_backward(spec.camera, spec.gen, spec.rec, W, H, m, tf, moments, bounds4, pmoments, rgba, g, grad_tf,
                           grad_vol)
         return grad_vol, grad_tf, None

@@ -47,6 +47,7 @@ struct ReconAdjDev
     float *grad_lambda;     // W*H*m
     float2 *grad_bounds;    // W*H (d/d lo, d/d hi)
     float4 *grad_tf;        // 256, accumulated
+    int tf_linear;          // the row linear in the front density instead of the cubic B-spline
     int *error_flag;
 };
 
@@ -178,9 +179,9 @@ template <int MAXM> __global__ void __launch_bounds__(128, 4) reconstruct_adjoin
                 const float S = mese_series_reinsch<MAXM>(lam2, lam0, pos, dl);
                 const float r = atanf(S) * 0.318309886f + 0.5f;
                 const float fs = r * span + lo;
-                const BSplineTap k = bspline_tap(fs);
+                const BSplineTap k = diff_tf_tap(fs, a.tf_linear);
                 float4 s, dt;
-                tf_bspline_value_derivative_soa(s_tf, k, s, dt);
+                tf_bspline_value_derivative_soa(s_tf, k, s, dt, a.tf_linear);
                 // d loss / d sample: emission terms see T before this step, extinction the radiance behind it
                 float4 gs;
                 gs.x = g.x * a.emission * T;
@@ -957,6 +958,7 @@ cudaError_t launch_reconstruct_adjoint(const ReconAdjArgs &r, int *error_flag, c
     a.grad_lambda = r.grad_lambda;
     a.grad_bounds = r.grad_bounds;
     a.grad_tf = r.grad_tf;
+    a.tf_linear = r.tf_linear;
     a.error_flag = error_flag;
     if (r.m <= 8)
         return launch_recon_adj<8>(a, stream);

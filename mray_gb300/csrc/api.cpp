@@ -64,6 +64,8 @@ struct mraygb_context
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
     int precision = MRAYGB_PRECISION_FP32;
+    // the differentiation form's transfer-function row: MRAYGB_DIFF_TF_BSPLINE or MRAYGB_DIFF_TF_LINEAR
+    int diff_tf_sampling = MRAYGB_DIFF_TF_BSPLINE;
     std::string error;
     uint64_t launches = 0;
 
@@ -386,6 +388,7 @@ int run_reconstruct(mraygb_context *ctx, const mraygb_camera *cam, const mraygb_
     a.tf = d_tf ? d_tf : ctx->tf.as<float4>();
     a.bounds4 = d_bounds4;
     a.diff_form = diff_form;
+    a.diff_tf_linear = diff_form && ctx->diff_tf_sampling == MRAYGB_DIFF_TF_LINEAR;
     a.step = rp->step_size;
     a.emission = rp->medium_emission;
     a.ert = rp->early_ray_termination;
@@ -816,6 +819,15 @@ int mraygb_set_precision(mraygb_context *ctx, int precision)
         precision != MRAYGB_PRECISION_COMPENSATED_FF_MESE)
         return fail(ctx, MRAYGB_INVALID_ARGUMENT, "unknown precision form %d", precision);
     ctx->precision = precision;
+    return MRAYGB_OK;
+}
+
+int mraygb_set_diff_tf_sampling(mraygb_context *ctx, int sampling)
+{
+    CHECK_CTX();
+    if (sampling != MRAYGB_DIFF_TF_BSPLINE && sampling != MRAYGB_DIFF_TF_LINEAR)
+        return fail(ctx, MRAYGB_INVALID_ARGUMENT, "unknown transfer-function sampling %d", sampling);
+    ctx->diff_tf_sampling = sampling;
     return MRAYGB_OK;
 }
 
@@ -2786,6 +2798,7 @@ int mraygb_diff_backward(mraygb_context *ctx, const mraygb_camera *cam, const mr
     a.grad_lambda = ctx->adj_lambda.as<float>();
     a.grad_bounds = ctx->adj_bounds.as<float2>();
     a.grad_tf = reinterpret_cast<float4 *>(d_grad_tf);
+    a.tf_linear = ctx->diff_tf_sampling == MRAYGB_DIFF_TF_LINEAR;
     CK(launch_reconstruct_adjoint(a, ctx->error_flag.as<int>(), ctx->stream), "re-march adjoint launch");
     ctx->launches += 1;
     if (!d_grad_volume)

@@ -206,8 +206,10 @@ struct ReconArgs
     uint8_t *rgba8;
     // per-pixel (lo, hi, ., .) float bounds instead of the u16 ones
     const float4 *bounds4 = nullptr;
-    // the differentiation form's density and transfer function (exact atan, cubic B-spline row)
+    // the differentiation form's density and transfer function (exact atan, cubic B-spline row; with diff_tf_linear
+    // the row linear in the front density)
     int diff_form = 0;
+    int diff_tf_linear = 0;
     // single scattering from the transmittance cache (null: none): in-scattered light of intensity ss->intensity
     // and phase function ss->henyey_greenstein_g, weighted by the medium's scattering coefficient
     const GridView *ss_cache = nullptr;
@@ -247,6 +249,7 @@ struct ReconAdjArgs
     float *grad_lambda;
     float2 *grad_bounds;
     float4 *grad_tf;
+    int tf_linear = 0; // the transfer-function row linear in the front density instead of the cubic B-spline
 };
 cudaError_t launch_reconstruct_adjoint(const ReconAdjArgs &a, int *error_flag, cudaStream_t stream);
 // the FP32 multipliers of W*H*m moments (m <= 64) and, per pixel, the 2m float2 that the preparation adjoint reads

@@ -38,6 +38,7 @@ struct ReconDev
     float *rgba;
     uint8_t *rgba8;
     const float4 *bounds4;
+    int diff_tf_linear;
     int *error_flag;
     // single scattering: the transmittance cache, the light direction, intensity, phase asymmetry and the medium's
     // scattering coefficient
@@ -45,7 +46,8 @@ struct ReconDev
     float light[3], intensity[3], hg_g, scattering;
 };
 
-// DIFF: the differentiation form (float bounds read by the caller's choice, exact atan, B-spline transfer function)
+// DIFF: the differentiation form (float bounds read by the caller's choice, exact atan, the transfer-function row
+// as a cubic B-spline or, with a.diff_tf_linear, linear in the front density)
 // SS: in-scattered light from the transmittance cache (inscattering with SingleScatteringCache,
 // src/raymarch_reconstruct.h:36-46 and 112-125)
 template <int MAXM, bool DIFF, bool SS>
@@ -78,7 +80,7 @@ __global__ void __launch_bounds__(128) reconstruct_kernel(const ReconDev a)
     if (n == 0)
     {
         // reconstruct_zero_ray (src/raymarch_reconstruct.h:127-131)
-        const float4 z = DIFF ? tf_sample_bspline(s_tf, bspline_tap(0.f)) : tf_sample(s_tf, 0.f, 0.f);
+        const float4 z = DIFF ? tf_sample_bspline(s_tf, diff_tf_tap(0.f, a.diff_tf_linear)) : tf_sample(s_tf, 0.f, 0.f);
         out = make_float4(z.x, z.y, z.z, 0.f);
     }
     else
@@ -137,7 +139,7 @@ __global__ void __launch_bounds__(128) reconstruct_kernel(const ReconDev a)
                 p = __fadd_rn(p, phase_step);
                 const float bs = DIFF ? mese_density_exact<MAXM>(lam2, lam0, p, lo, span)
                                       : mese_density<MAXM>(lam2, lam0, p, lo, span);
-                const float4 s = DIFF ? tf_sample_bspline(s_tf, bspline_tap(fs)) : tf_sample(s_tf, fs, bs);
+                const float4 s = DIFF ? tf_sample_bspline(s_tf, diff_tf_tap(fs, a.diff_tf_linear)) : tf_sample(s_tf, fs, bs);
                 if (SS)
                 {
                     // L += (Le + Ls sigma_s) T with Ls = T_ss pf intensity, T_ss the cache at ray.origin + t ray.dir
@@ -224,6 +226,7 @@ cudaError_t launch_reconstruct(const ReconArgs &r, int *error_flag, cudaStream_t
     a.rgba = r.rgba;
     a.rgba8 = r.rgba8;
     a.bounds4 = r.bounds4;
+    a.diff_tf_linear = r.diff_tf_linear;
     a.error_flag = error_flag;
     // inscattering only where the medium scatters (raymarch_reconstruct.h:176-179)
     const bool ss = r.ss_cache && r.ss && r.scattering > 0.0f && r.diff_form == 0;

@@ -76,6 +76,27 @@ __device__ __forceinline__ BSplineTap bspline_tap(float fs)
 
 __device__ __forceinline__ int bspline_entry(const BSplineTap &k, int j) { return min(max(k.i - 1 + j, 0), 255); }
 
+// The same row sampled linearly in the front density with the texel convention of the reference's GPU texture
+// (TransferFunctionDevice::sample, src/transfer_function_device.cuh:30-65: u = 256 fs - 1/2, clamp to edge) as a tap
+// of the same four-entry window: entries i and i + 1 with weights 1 - t and t (the outer two weigh 0).  Exact float
+// weights, not the texture unit's 8-bit fractions.
+__device__ __forceinline__ BSplineTap linear_tap(float fs)
+{
+    BSplineTap k;
+    const float u = fs * 256.f - 0.5f;
+    const float fl = floorf(u);
+    k.t = u - fl;
+    k.i = (int)fl;
+    k.w[0] = 0.f;
+    k.w[1] = 1.f - k.t;
+    k.w[2] = k.t;
+    k.w[3] = 0.f;
+    return k;
+}
+
+// the differentiation form's tap of either transfer-function row
+__device__ __forceinline__ BSplineTap diff_tf_tap(float fs, bool linear) { return linear ? linear_tap(fs) : bspline_tap(fs); }
+
 __device__ __forceinline__ float4 tf_sample_bspline(const float4 *T, const BSplineTap &k)
 {
     float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -115,13 +136,21 @@ __device__ __forceinline__ void tf_bspline_value_derivative(const float4 *T, con
     }
 }
 
-// the same from one float table per channel (channel c of entry i at c * 256 + i): the same operations
+// the same from one float table per channel (channel c of entry i at c * 256 + i): the same operations; with
+// `linear` the tap is linear_tap's and the derivative d / d fs = 256 (T[i + 1] - T[i])
 __device__ __forceinline__ void tf_bspline_value_derivative_soa(const float *T, const BSplineTap &k, float4 &val,
-                                                                float4 &dval)
+                                                                float4 &dval, bool linear = false)
 {
     const float t = k.t, s = 1.f - t;
-    const float d[4] = {-128.f * s * s, 128.f * (3.f * t * t - 4.f * t), 128.f * (-3.f * t * t + 2.f * t + 1.f),
-                        128.f * t * t};
+    float d[4] = {-128.f * s * s, 128.f * (3.f * t * t - 4.f * t), 128.f * (-3.f * t * t + 2.f * t + 1.f),
+                  128.f * t * t};
+    if (linear)
+    {
+        d[0] = 0.f;
+        d[1] = -256.f;
+        d[2] = 256.f;
+        d[3] = 0.f;
+    }
     val = make_float4(0.f, 0.f, 0.f, 0.f);
     dval = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll

@@ -29,6 +29,9 @@ PRECISION_FP32 = 0
 PRECISION_COMPENSATED_FP64_MESE = 1
 PRECISION_COMPENSATED_FF_MESE = 2
 MAX_MOMENTS = 255
+# the differentiation form's transfer-function row (mraygb_set_diff_tf_sampling)
+DIFF_TF_BSPLINE = 0
+DIFF_TF_LINEAR = 1
 
 
 def _dptr(x) -> Optional[int]:
@@ -250,6 +253,16 @@ class Context:
     def precision(self, value: int):
         self._check(self._L.mraygb_set_precision(self._h, int(value)))
         self._precision = int(value)
+
+    @property
+    def diff_tf_sampling(self) -> int:
+        """The differentiation form's transfer-function row: DIFF_TF_BSPLINE (default) or DIFF_TF_LINEAR."""
+        return getattr(self, "_diff_tf_sampling", DIFF_TF_BSPLINE)
+
+    @diff_tf_sampling.setter
+    def diff_tf_sampling(self, value: int):
+        self._check(self._L.mraygb_set_diff_tf_sampling(self._h, int(value)))
+        self._diff_tf_sampling = int(value)
 
     def set_stream(self, stream) -> None:
         """Orders later work on ``stream``: a torch.cuda.Stream (torch's default stream included), a cudaStream_t as

@@ -76,8 +76,9 @@ typedef struct oracle_options
     int row_step;     /* process every row_step-th row (<=0: 1)           */
     /* The differentiation form (a variant of the method whose loss is smooth almost everywhere in its inputs;
      * combine with exact_atan = 1):
-     *   tf_bspline : reconstruct samples the transfer function row as a uniform cubic B-spline in the front
-     *                density, knots at the texel centres of the reference's GPU texture (u = 256 fs - 1/2);
+     *   tf_bspline : 1: reconstruct samples the transfer function row as a uniform cubic B-spline in the front
+     *                density, knots at the texel centres of the reference's GPU texture (u = 256 fs - 1/2); 2:
+     *                linearly in the front density at those texel centres (the texture's sampling, exact weights);
      *   bounds_out : generate writes the per-pixel density bounds (lo, hi) unquantized, 2*W*H of R;
      *   bounds_in  : reconstruct reads (lo, hi) from here (2*W*H of R) instead of the u16 bounds. */
     int tf_bspline;

@@ -598,8 +598,8 @@ def reconstruct(cam, rp, width, height, m, dmin, dmax, index, pmoments, bounds, 
                 nthreads=0, rows=None, exact_atan=False, tf_bspline=False, float_bounds=None, cache=None,
                 density_offset=0.0):
     """reconstruct_host with float RGBA: returns rgba[H,W,4].  tf_bspline / float_bounds select the
-    differentiation form (transfer-function row as a cubic B-spline in the front density; unquantized
-    bounds[H,W,2]).  cache = (values[z, y, x], dmin, dmax): single scattering from that transmittance cache when
+    differentiation form (transfer-function row as a cubic B-spline in the front density, or with tf_bspline = 2
+    linear in it; unquantized bounds[H,W,2]).  cache = (values[z, y, x], dmin, dmax): single scattering from that transmittance cache when
     rp.ss.enable.  density_offset (a scalar, or one value per pixel [H, W]) is added to every reconstructed density (a
     probe of the colour's sensitivity to the densities; 0 is the method)."""
     L = lib()
@@ -770,14 +770,14 @@ def preintegrate_r(tf1d, step_size, precision="f64"):
 
 
 def diff_forward(cam, gp, rp, volume, dmin, dmax, width, height, m, tf_table, precision="f64", nthreads=0,
-                 exact_atan=True, rows=None):
+                 exact_atan=True, rows=None, tf_linear=False):
     """The differentiation form's forward on the CPU: generate without compaction, unquantized bounds,
     Lagrange multipliers, re-march with exact atan and the transfer-function row as a cubic B-spline in the
-    front density.  Returns rgba[H,W,4] in the working precision; with rows = (begin, end, step) only those rows
-    (the others stay zero)."""
+    front density (with tf_linear: linear in it, the GPU texture's sampling with exact weights).  Returns
+    rgba[H,W,4] in the working precision; with rows = (begin, end, step) only those rows (the others stay zero)."""
     moments, _, _, bf = generate_moments(cam, gp, volume, dmin, dmax, width, height, m, precision, nthreads,
                                          rows=rows, float_bounds=True)
     pm = prepare_moments(width, height, m, None, moments.reshape(-1), False, 1, None, rp.bias, precision, nthreads,
                          rows=rows)
     return reconstruct(cam, rp, width, height, m, dmin, dmax, None, pm, None, tf_table, precision, nthreads,
-                       rows=rows, exact_atan=exact_atan, tf_bspline=True, float_bounds=bf)
+                       rows=rows, exact_atan=exact_atan, tf_bspline=2 if tf_linear else 1, float_bounds=bf)

@@ -9,6 +9,8 @@ a cubic B-spline in the front density.  Two checks of the gradients:
   * under the configuration's L2 loss (target rendered with a perturbed transfer function) on 32 seeded parameters
     (16 transfer-function entries, 16 voxels): against central differences (eps about 1e-3) of the FP64 oracle,
     and against central differences (eps = 1e-3) of the FP32 GPU forward itself on the strong parameters.
+The transfer-function row linear in the front density (the reference's GPU sampling) is checked the same way
+against the oracle's FP64 form of that sampling.
 """
 import numpy as np
 import pytest
@@ -121,6 +123,76 @@ def test_l2_adjoint_against_gpu_central_differences(gpu_context):
     assert rel.max() <= 1e-2, f"max rel err {rel.max():.3e} at {params[int(rel.argmax())]}"
 
 
+def _linear(ctx):
+    import mray_gb300 as M
+
+    class _Linear:
+        def __enter__(self):
+            ctx.diff_tf_sampling = M.DIFF_TF_LINEAR
+
+        def __exit__(self, *exc):
+            ctx.diff_tf_sampling = M.DIFF_TF_BSPLINE
+
+    return _Linear()
+
+
+def _oracle_rgba_linear(wl, volume, table):
+    return O.diff_forward(wl.camera, wl.gen, wl.rec, volume, wl.domain_min, wl.domain_max, wl.width, wl.height,
+                          wl.num_moments, table, "f64", tf_linear=True)
+
+
+def test_linear_tf_forward_matches_oracle(gpu_context):
+    """The transfer-function row sampled linearly in the front density (the reference's GPU texture sampling, exact
+    weights): the forward against the oracle's FP32 and FP64 forms of the same sampling, and different from the
+    B-spline row's image."""
+    wl, _ = _workload(m=31)
+    table = O.preintegrate(wl.tf1d, wl.tf_step)
+    R = GpuRender(gpu_context, wl)
+    spline = R.forward(wl.volume, table)
+    with _linear(gpu_context):
+        rgba = R.forward(wl.volume, table)
+    ref32 = O.diff_forward(wl.camera, wl.gen, wl.rec, wl.volume, wl.domain_min, wl.domain_max, wl.width, wl.height,
+                           wl.num_moments, table, "f32", tf_linear=True)
+    ref64 = _oracle_rgba_linear(wl, wl.volume, table)
+    assert np.abs(rgba - ref32).max() <= 1e-3
+    assert np.abs(rgba - ref64).max() <= 1e-3
+    # the two rows render differently (the smooth table makes the difference small): the linear image is far closer to
+    # the oracle's linear image than to the B-spline one
+    assert np.abs(rgba - spline).max() > 10.0 * np.abs(rgba - ref64).max()
+
+
+def test_linear_tf_adjoint_against_fp64_central_differences(gpu_context):
+    """Gradients with the linear row against central differences (eps = 2^-10, Richardson-combined with 2 eps) of
+    the FP64 oracle of the same sampling, under a random linear image loss.  The loss is smooth in the table entries
+    (they enter the emission linearly and the transmittance through exp), but an entry's gradient sums the hat weights
+    1 - |256 fs - 1/2 - i| of its samples, which move by 256 times the FP32 forward's density error (the B-spline's
+    weights by at most half as much): 16 entries within 2e-3 relative (most within 3e-4).  In a voxel the loss has
+    a kink wherever one of the many samples whose reconstructed density the voxel moves crosses a texel centre, and
+    central differences over eps cross some of them: 8 voxels within 1e-2 relative."""
+    wl, _ = _workload(m=16)
+    table = O.preintegrate(wl.tf1d, wl.tf_step)
+    rng = np.random.default_rng(29)
+    weights = rng.standard_normal((wl.height, wl.width, 4))
+    R = GpuRender(gpu_context, wl)
+    with _linear(gpu_context):
+        R.forward(wl.volume, table)
+        gtf, gvol = R.backward(weights)
+    params = _pick(rng, gvol, gtf, 16, 8)
+    t64 = table.astype(np.float64)
+
+    def loss(v, t):
+        return float((weights * _oracle_rgba_linear(wl, v, t)).sum())
+
+    fd = np.array([_richardson(loss, wl, t64, kind, idx, 2.0 ** -10) for kind, idx in params])
+    ad = np.array([gtf[idx] if kind == "tf" else gvol[idx] for kind, idx in params])
+    rel = np.abs(ad - fd) / np.abs(fd)
+    is_tf = np.array([kind == "tf" for kind, _ in params])
+    print(f"linear row: tf max rel err {rel[is_tf].max():.2e} (median {np.median(rel[is_tf]):.1e}), voxels "
+          f"{rel[~is_tf].max():.2e}")
+    assert rel[is_tf].max() <= 2e-3, f"tf: max rel err {rel[is_tf].max():.3e}: ad {ad[is_tf]} fd {fd[is_tf]}"
+    assert rel[~is_tf].max() <= 1e-2, f"voxels: max rel err {rel[~is_tf].max():.3e}: ad {ad[~is_tf]} fd {fd[~is_tf]}"
+
+
 def test_preparation_adjoint_without_the_kept_arrays(gpu_context):
     """The forward keeps the preparation's Levinson solution and exponential moments for the backward on the same
     buffers.  A backward on buffers of an earlier forward (another forward ran since) and a backward after a
@@ -183,6 +255,8 @@ def test_diff_form_argument_errors(gpu_context):
     wl, _ = _workload(m=8)
     R = GpuRender(gpu_context, wl)
     R.forward(wl.volume, O.preintegrate(wl.tf1d, wl.tf_step))
+    with pytest.raises(M.MrayError, match="INVALID_ARGUMENT"):
+        gpu_context.diff_tf_sampling = 7
     wl.gen.compact_image = 1
     with pytest.raises(M.MrayError, match="INVALID_ARGUMENT"):
         R.forward(wl.volume, O.preintegrate(wl.tf1d, wl.tf_step))
