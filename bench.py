@@ -653,6 +653,28 @@ def run_e2e(args, ctx, hl, dist):
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
     (dt,) = reduce_max([dt], dist, "cuda")
+
+    # where the time of a step goes: three more steps (after the timed ones) with a clock around each call, the
+    # volume upload apart from the generate call (each call returns with its copies done)
+    phases = {"upload_grid": [], "generate": [], "quantize": [], "dequantize": [], "reconstruct": []}
+    for _ in range(3):
+        t = time.perf_counter()
+        mi.data = data_full
+        ctx.upload_grid(grid.data, grid.domain_min, grid.domain_max)
+        t, t_prev = time.perf_counter(), t
+        phases["upload_grid"].append(t - t_prev)
+        ctx.generate(hl.camera, hl.gen, W, H, m, out=mi)
+        t, t_prev = time.perf_counter(), t
+        phases["generate"].append(t - t_prev)
+        qs = M.quantize_prediction_coding(mi, hl.table, context=ctx, out=codes)
+        t, t_prev = time.perf_counter(), t
+        phases["quantize"].append(t - t_prev)
+        M.dequantize_prediction_coding(mi, hl.table, qs, context=ctx)
+        t, t_prev = time.perf_counter(), t
+        phases["dequantize"].append(t - t_prev)
+        M.reconstruct(hl.camera, mi, tf, img, hl.rec, context=ctx)
+        t, t_prev = time.perf_counter(), t
+        phases["reconstruct"].append(t - t_prev)
     world = dist.get_world_size() if dist else 1
     nd, nq = 4 * sizes["moments"], sizes["codes"]
     idx_b, cp_b = 4 * (P + 1), 4 * (m - 1)
@@ -663,6 +685,7 @@ def run_e2e(args, ctx, hl, dist):
     d2h = (nd + idx_b + 4 * P + cp_b) + nq + nd + (16 * P + 4 * P)
     return {"value": world * P * args.steps / dt / 1e6, "unit": UNIT, "ms_per_step": 1e3 * dt / args.steps,
             "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "steps": args.steps,
+            "phases_ms": {k: [round(1e3 * x, 2) for x in v] for k, v in phases.items()},
             "path": "mraygb_upload_grid + mraygb_generate, mraygb_quantize_prediction_coding, "
                     "mraygb_dequantize_prediction_coding, mraygb_upload_tf + mraygb_reconstruct on pinned host "
                     "buffers (the drop-in seams of generate_device / reconstruct_device and the reference's "

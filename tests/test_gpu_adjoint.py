@@ -72,6 +72,28 @@ def test_adjoint_against_fp64_reference_gradient(gpu_context, m):
     assert rel.max() <= 1e-3, f"max rel err {rel.max():.3e} at {params[int(rel.argmax())]}: ad {ad} fd {fd}"
 
 
+def test_adjoint_64_moments_against_fp64_reference_gradient(gpu_context):
+    """64 moments (two elements per lane in the preparation adjoint, the 64-moment instances of every adjoint
+    kernel) under a random linear image loss against central differences of the FP64 oracle: voxels within 1e-3
+    relative.  Table entries within 2e-3: an entry's gradient sums the B-spline weights of its samples, which move
+    with the FP32 forward's reconstructed densities, and at 64 moments the FP32 series (multipliers up to 1e4
+    cancelling to values of order one) moves those densities more than at 31 (at 31 moments 1e-3 holds above)."""
+    wl, _ = _workload(m=64)
+    table = O.preintegrate(wl.tf1d, wl.tf_step)
+    rng = np.random.default_rng(5)
+    weights = rng.standard_normal((wl.height, wl.width, 4))
+    R = GpuRender(gpu_context, wl)
+    R.forward(wl.volume, table)
+    gtf, gvol = R.backward(weights)
+    params = _pick(rng, gvol, gtf, 8, 8)
+    ad = np.array([gtf[idx] if kind == "tf" else gvol[idx] for kind, idx in params])
+    fd = _fd64(wl, wl.volume, table, weights, params)
+    rel = np.abs(ad - fd) / np.abs(fd)
+    is_tf = np.array([kind == "tf" for kind, _ in params])
+    assert rel[~is_tf].max() <= 1e-3, f"voxels: max rel err {rel[~is_tf].max():.3e}: ad {ad[~is_tf]} fd {fd[~is_tf]}"
+    assert rel[is_tf].max() <= 2e-3, f"tf: max rel err {rel[is_tf].max():.3e}: ad {ad[is_tf]} fd {fd[is_tf]}"
+
+
 def _l2_setup(ctx):
     wl, target_tf = _workload(n=48, width=48, height=40, m=31)
     table = O.preintegrate(wl.tf1d, wl.tf_step).astype(np.float64)
