@@ -189,9 +189,10 @@ def test_linear_tf_adjoint_against_fp64_central_differences(gpu_context):
     the FP64 oracle of the same sampling, under a random linear image loss.  The loss is smooth in the table entries
     (they enter the emission linearly and the transmittance through exp), but an entry's gradient sums the hat weights
     1 - |256 fs - 1/2 - i| of its samples, which move by 256 times the FP32 forward's density error (the B-spline's
-    weights by at most half as much): 16 entries within 2e-3 relative (most within 3e-4).  In a voxel the loss has
+    weights by at most half as much): 16 entries within 3e-3 relative (measured 1.8e-3 at worst, median 7e-5).  In a
+    voxel the loss has
     a kink wherever one of the many samples whose reconstructed density the voxel moves crosses a texel centre, and
-    central differences over eps cross some of them: 8 voxels within 1e-2 relative."""
+    central differences over eps cross some of them: 8 voxels within 1e-2 relative (measured 7.3e-3)."""
     wl, _ = _workload(m=16)
     table = O.preintegrate(wl.tf1d, wl.tf_step)
     rng = np.random.default_rng(29)
@@ -212,7 +213,7 @@ def test_linear_tf_adjoint_against_fp64_central_differences(gpu_context):
     is_tf = np.array([kind == "tf" for kind, _ in params])
     print(f"linear row: tf max rel err {rel[is_tf].max():.2e} (median {np.median(rel[is_tf]):.1e}), voxels "
           f"{rel[~is_tf].max():.2e}")
-    assert rel[is_tf].max() <= 2e-3, f"tf: max rel err {rel[is_tf].max():.3e}: ad {ad[is_tf]} fd {fd[is_tf]}"
+    assert rel[is_tf].max() <= 3e-3, f"tf: max rel err {rel[is_tf].max():.3e}: ad {ad[is_tf]} fd {fd[is_tf]}"
     assert rel[~is_tf].max() <= 1e-2, f"voxels: max rel err {rel[~is_tf].max():.3e}: ad {ad[~is_tf]} fd {fd[~is_tf]}"
 
 
