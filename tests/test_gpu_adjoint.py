@@ -190,9 +190,9 @@ def test_linear_tf_adjoint_against_fp64_central_differences(gpu_context):
     (they enter the emission linearly and the transmittance through exp), but an entry's gradient sums the hat weights
     1 - |256 fs - 1/2 - i| of its samples, which move by 256 times the FP32 forward's density error (the B-spline's
     weights by at most half as much): 16 entries within 3e-3 relative (measured 1.8e-3 at worst, median 7e-5).  In a
-    voxel the loss has
-    a kink wherever one of the many samples whose reconstructed density the voxel moves crosses a texel centre, and
-    central differences over eps cross some of them: 8 voxels within 1e-2 relative (measured 7.3e-3)."""
+    voxel the loss has a kink wherever one of the many samples whose reconstructed density the voxel moves crosses a
+    texel centre, and central differences over eps cross some of them: 8 voxels within 1e-2 relative (measured
+    7.3e-3)."""
     wl, _ = _workload(m=16)
     table = O.preintegrate(wl.tf1d, wl.tf_step)
     rng = np.random.default_rng(29)
