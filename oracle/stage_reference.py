@@ -1,8 +1,8 @@
 """ORACLE -- test infrastructure only.
 
-Stages the reference's sources into ``baseline/_ref/src`` (git-ignored, not gpurun-ignored), so that the machines
-that run the tests and the benchmark can compile the reference's own CPU path (``oracle/Makefile ref``) and its CUDA
-path (``oracle/Makefile refcuda``) from them.  The reference is only ever read from its checkout here; every other
+Stages the reference's sources into ``baseline/_ref/src`` (kept out of the repository's history, but copied with the
+working tree to the machines that run the tests and the benchmark), so that those machines can compile the
+reference's own CPU path (``oracle/Makefile ref``) and its CUDA path (``oracle/Makefile refcuda``) from them.  The reference is only ever read from its checkout here; every other
 file takes the staged copy (or ``MRAY_REFERENCE_SRC``).  Nothing is copied into the repository's history.
 """
 from __future__ import annotations
