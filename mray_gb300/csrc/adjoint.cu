@@ -8,7 +8,8 @@
 // reference's fast_atan jumps by 2.4e-5 at |t| = 1), and the transfer-function row is a uniform cubic B-spline in
 // the front density with knots at the texel centres of the reference's GPU texture (transfer_function_device.cuh).
 // A piecewise-linear row has a kink at every entry, dense enough that a 1e-3 change of one voxel crosses several
-// along a ray.
+// along a ray; it is still offered (tf_linear: the GPU texture's own interpolation, exact weights), as the same
+// four-entry tap with the outer two weights zero.
 //
 // Memory: none of the three adjoints keeps a per-sample tape.  The re-march adjoint replays the forward march
 // and uses the final radiance of the forward pass for the suffix sums of front-to-back compositing (d L / d tau_k
