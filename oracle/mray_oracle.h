@@ -156,6 +156,7 @@ typedef struct oracle_options
                                     R *t_near, R *t_far);                                                          \
     void oracle_tf_sample_##SFX(const R *tf_table, R fs, R bs, R out[4]);                                           \
     void oracle_tf_sample_bspline_##SFX(const R *tf_table, R fs, R out[4]);                                         \
+    void oracle_tf_sample_linear_##SFX(const R *tf_table, R fs, R out[4]);                                          \
     /* quantization curve (measure_coding_error.cpp:92-192, 357-438) on a compact prediction-coded image       */   \
     R oracle_measure_idx_error_##SFX(int width, int height, int num_moments, const uint32_t *index, const R *data, \
                                      int coding_warp, const uint16_t *coding_params, int idx, int b, R *errors,     \

@@ -194,6 +194,7 @@ def _declare(L):
         getattr(L, f"oracle_grid_sample_{sfx}").restype = R
         getattr(L, f"oracle_tf_sample_{sfx}").argtypes = [C.c_void_p, R, R, C.c_void_p]
         getattr(L, f"oracle_tf_sample_bspline_{sfx}").argtypes = [C.c_void_p, R, C.c_void_p]
+        getattr(L, f"oracle_tf_sample_linear_{sfx}").argtypes = [C.c_void_p, R, C.c_void_p]
     L.oracle_particles_create.restype = C.c_void_p
     L.oracle_particles_create.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_float,
                                           C.c_float * 3, C.c_float * 3]
@@ -709,6 +710,16 @@ def ref_from_rec(rp):
     return ReferenceParameters(step_size=rp.step_size, medium_emission=rp.medium_emission,
                                medium_scattering=rp.medium_scattering, early_ray_termination=rp.early_ray_termination,
                                data_min=rp.data_min, data_max=rp.data_max, ss=rp.ss)
+
+
+def tf_sample_diff(tf_table, fs, linear=False, precision="f64"):
+    """The differentiation form's transfer-function row at front density fs: the cubic B-spline or (linear) the
+    GPU texture's linear interpolation, both at the texel centres u = 256 fs - 1/2; RGBA."""
+    L = lib()
+    t = np.ascontiguousarray(tf_table, dtype=_dt(precision)).reshape(-1)
+    out = np.zeros(4, dtype=_dt(precision))
+    getattr(L, f"oracle_tf_sample_{'linear' if linear else 'bspline'}_{precision}")(_ptr(t), fs, _ptr(out))
+    return out
 
 
 def preintegrate(tf1d, step_size):
