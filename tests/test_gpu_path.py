@@ -44,6 +44,10 @@ CASES = [
     dict(kind="ml", width=40, height=40, m=1, seed=3),
     dict(kind="ml", width=33, height=17, m=64, seed=9),
     dict(kind="mix", width=48, height=40, m=64, n=96, seed=21),
+    # beyond 64 moments, up to the reference's limit of 255 (main.cpp:288-293): the 32- and 64-moment-per-lane
+    # generate instances and the 128- and 256-entry preparation and re-march instances
+    dict(kind="mix", width=24, height=20, m=128, n=64, seed=23),
+    dict(kind="mix", width=20, height=16, m=255, n=64, seed=29),
 ]
 
 
@@ -142,7 +146,8 @@ def _oracle_image(wl):
     return mi, tf
 
 
-@pytest.mark.parametrize("case", [CASES[0], CASES[1], CASES[3], CASES[4]], ids=lambda c: f"{c['kind']}-m{c['m']}")
+@pytest.mark.parametrize("case", [CASES[0], CASES[1], CASES[3], CASES[4], CASES[5], CASES[6]],
+                         ids=lambda c: f"{c['kind']}-m{c['m']}")
 def test_prepare_and_reconstruct_from_same_moments(gpu_context, case):
     """Same compact moment image in: GPU Lagrange multipliers and re-march against the oracle's."""
     wl = _case(case)
