@@ -66,6 +66,27 @@ def test_prediction_encode_matches_oracle(gpu_context, warp, ragged_seed):
     assert np.array_equal(d_out.cpu().numpy()[:n], b)
 
 
+@pytest.mark.parametrize("warp", [0, 1])
+@pytest.mark.parametrize("m", [1, 2, 64, 255])
+def test_prediction_encode_moment_counts(gpu_context, warp, m):
+    """The same bar at the ends of the moment range: one and two moments (no or one coding-parameter pair) and 64
+    and 255 (the reference's limit), on a compact image with random per-pixel counts."""
+    W, H, m, index, data = _ragged_image(seed=m, width=24, height=16, m=m)
+    ours, cp = _encode_gpu(gpu_context, W, H, m, index, data, warp, 5e-5)
+    ref, cp_ref = O.prediction_encode(W, H, m, index, data, warp, 5e-5)
+    assert np.array_equal(ours.view(np.uint32), ref.view(np.uint32)), \
+        f"{int((ours.view(np.uint32) != ref.view(np.uint32)).sum())} of {ref.size} floats differ"
+    if warp == 0:
+        assert np.array_equal(cp, cp_ref)
+    table = O.default_quantization_table(m, 10)
+    d_out = torch.zeros(ours.size * 4 + 16, dtype=torch.uint8, device="cuda")
+    n = gpu_context.stage_quantize_prediction_coding(W, H, m, _dev(index.view(np.int32)), _dev(ours), table, d_out)
+    gpu_context.synchronize()
+    b = O.quantize_prediction_coding(W, H, m, index, ref, table)
+    assert n == b.size
+    assert np.array_equal(d_out.cpu().numpy()[:n], b)
+
+
 TABLES = {
     "16_10": lambda m: O.default_quantization_table(m, 10),
     "16_12": lambda m: O.default_quantization_table(m, 12),
