@@ -42,7 +42,7 @@ def _case(kind, m):
 
 
 @pytest.mark.parametrize("thr", [0.01, 0.001])
-@pytest.mark.parametrize("m", [8, 31, 64])
+@pytest.mark.parametrize("m", [8, 31, 64, 128, 255])
 @pytest.mark.parametrize("kind", ["ml", "mixing"])
 def test_threshold_counts_match_oracle(gpu_context, kind, m, thr):
     wl = _case(kind, m)
