@@ -25,7 +25,7 @@ def _lambda_err(pm, pm64, index):
     return np.array(out)
 
 
-CASES = [("ml", 31), ("mix", 64)]
+CASES = [("ml", 31), ("mix", 64), ("mix", 128), ("mix", 255)]
 
 
 @pytest.mark.parametrize("form", ["fp64", "ff"])
@@ -53,8 +53,10 @@ def test_precision_prepare_matches_fp64_oracle(gpu_context, form, pc, kind, m):
     pm64 = O.prepare_moments(W, H, m, mi["index"], mi["data"], bool(pc), 0, cp, wl.rec.bias, "f64")
     err = _lambda_err(pm, pm64, mi["index"])
     # FP64: the same arithmetic up to contraction and the sincos of the first exponential moment; float-float:
-    # 48-bit steps, then the FP32 tail (about 1e-7 of the largest multiplier) and the float result
-    tol = 1e-6 if form == "fp64" else 2e-5
+    # 48-bit steps, then the FP32 tail and the float result.  The tail's correlations sum m products in FP32, so
+    # its rounding grows with m: the bar scales with m above 64 moments (measured at 255 moments: p99 5.5e-6, max
+    # 1.8e-5, against 2e-5 / 8e-5)
+    tol = 1e-6 if form == "fp64" else 2e-5 * max(1.0, m / 64.0)
     assert np.quantile(err, 0.99) <= tol / 4 and err.max() <= tol, f"p99 {np.quantile(err, .99):.2e} max {err.max():.2e}"
     # the FP32 preparation, for scale: the precision forms are far closer to FP64
     gpu_context.stage_prepare_moments(W, H, m, d_idx, d_data, d_pm, prediction_code=pc, coding_warp=0,
