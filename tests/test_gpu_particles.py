@@ -94,10 +94,12 @@ def test_particles_match_reference_fixture(gpu_context, prefix):
 
 
 @pytest.mark.parametrize("precision", [0, 1])
-def test_sph_workload_matches_oracle(gpu_context, precision):
+@pytest.mark.parametrize("m", [16, 128])
+def test_sph_workload_matches_oracle(gpu_context, precision, m):
     from mray_gb300 import workloads as W
 
-    wl = W.sph_workload(n=20000, h=1.0 / 32, width=64, height=56, num_moments=16, seed=31)
+    wl = W.sph_workload(n=20000, h=1.0 / 32, width=64 if m <= 64 else 32, height=56 if m <= 64 else 24,
+                        num_moments=m, seed=31)
     _check_against_oracle(gpu_context, wl.x, wl.y, wl.z, wl.v, wl.h, wl.domain_min, wl.domain_max, wl.camera,
                           wl.gen, wl.width, wl.height, wl.num_moments, precision=precision)
 
