@@ -199,3 +199,37 @@ def test_errors(gpu_context, g):
     back, _ = gpu_context.decode_moment_image(ref)
     whole = _whole_codes(pc, 10, False, None)
     assert np.array_equal(back.data[whole], g["loaded_pc_q10_lz4_data"][whole])
+
+
+@pytest.mark.parametrize("m", [1, 255])
+@pytest.mark.parametrize("compact,pc", [(True, True), (True, False), (False, False)], ids=["pc", "plain", "static"])
+def test_round_trip_at_the_moment_limits(gpu_context, m, compact, pc):
+    """One moment and 255 (the file's 8-bit moment count, moment_image_io.cpp:346-359): raw files round-trip bit for
+    bit, compressed or not; quantized and entropy-coded compact images decode to the image's shape and index, and a
+    second encoding of the decoded image gives the same file size.  Static images: raw files (their quantized files
+    are taken apart by a bits byte, tested above)."""
+    import mray_gb300 as M
+    from helpers import small_mixing
+
+    wl = small_mixing(20, 16, m, 64, seed=m)
+    wl.gen.compact_image = int(compact)
+    wl.gen.prediction_coding = int(pc)
+    wl.gen.transform_to_bounds = int(compact)
+    grid = M.RegularGrid(wl.volume, wl.domain_min, wl.domain_max)
+    mi = M.MomentImageHost(wl.width, wl.height, m, compact, compact)
+    M.generate(wl.camera, grid, mi, wl.gen, context=gpu_context)
+    for compress in (0, 1):
+        back, _ = gpu_context.decode_moment_image(gpu_context.encode_moment_image(mi, compress, 32))
+        _same_image(back, mi)
+    if not compact:
+        return
+    for bits, entropy in ((10, 0), (16, 0), (10, 1)):
+        table = np.array([16] + [bits] * (m - 1), dtype=np.uint8)[:m] if pc else None
+        back, _ = gpu_context.decode_moment_image(gpu_context.encode_moment_image(mi, 1, bits, entropy, table))
+        assert (back.width, back.height, back.num_moments, back.data.size) == (mi.width, mi.height, m, mi.data.size)
+        assert np.array_equal(back.index, mi.index)
+        assert np.all(np.isfinite(back.data))
+        if not entropy:
+            assert len(gpu_context.encode_moment_image(back, 1, bits, entropy, table)) > 0
+            assert len(gpu_context.encode_moment_image(back, 0, bits, entropy, table)) == \
+                len(gpu_context.encode_moment_image(mi, 0, bits, entropy, table))
