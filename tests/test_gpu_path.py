@@ -247,6 +247,37 @@ def test_dropin_generate_reconstruct_ml(gpu_context):
     assert np.mean(np.abs(img.rgba.astype(int) - O.rgba_to_u8(rgba32).astype(int)) <= 1) >= 0.999
 
 
+@pytest.mark.parametrize("prediction_coding", [0, 1])
+def test_dropin_empty_image(gpu_context, prediction_coding):
+    """A view that misses the volume: every count zero, an empty compact image, empty codes, and every pixel the
+    zero ray's colour (the transfer function at density 0 with alpha 0, reconstruct_zero_ray,
+    raymarch_reconstruct.h:127-131), as the oracle gives it."""
+    import mray_gb300 as M
+    from mray_gb300 import workloads as W
+
+    wl = small_mixing(24, 20, 16, 64, seed=3)
+    wl.camera = W.perspective_camera(eye=(3.0, 3.0, 3.0), target=(6.0, 6.0, 6.0), fov_deg=30.0)
+    wl.gen.prediction_coding = prediction_coding
+    wl.gen.quantization_bits = 10 if prediction_coding else 32
+    grid = M.RegularGrid(wl.volume, wl.domain_min, wl.domain_max)
+    mi = M.MomentImageHost(wl.width, wl.height, wl.num_moments, True, True)
+    M.generate(wl.camera, grid, mi, wl.gen, context=gpu_context)
+    ref = O.workload_generate(wl, "f32")
+    assert mi.data.size == 0 and np.all(mi.index == 0) and np.array_equal(mi.index, ref["index"])
+    if prediction_coding:
+        table = M.default_quantization_table(wl.num_moments, 10)
+        qs = M.quantize_prediction_coding(mi, table, context=gpu_context)
+        assert qs.size == 0
+        M.dequantize_prediction_coding(mi, table, qs, context=gpu_context)
+        assert mi.data.size == 0
+    tf = M.preintegrate(wl.tf1d, wl.tf_step)
+    img = M.ColorImageHost(wl.width, wl.height)
+    M.reconstruct(wl.camera, mi, tf, img, wl.rec, context=gpu_context)
+    rgba32 = O.workload_reconstruct(wl, ref, "f32")
+    assert np.array_equal(img.rgba_float, rgba32.astype(np.float32))
+    assert np.all(img.rgba_float[..., 3] == 0.0)
+
+
 def test_dropin_rejects_bad_arguments(gpu_context):
     import mray_gb300 as M
 
