@@ -56,7 +56,7 @@ def _fd64(wl, volume, table, weights, params, eps=2.0 ** -10):
     return np.array([_richardson(loss, wl, t64, kind, idx, eps) for kind, idx in params])
 
 
-@pytest.mark.parametrize("m", [16, 31])
+@pytest.mark.parametrize("m", [1, 8, 16, 31])
 def test_adjoint_against_fp64_reference_gradient(gpu_context, m):
     wl, _ = _workload(m=m)
     table = O.preintegrate(wl.tf1d, wl.tf_step)
