@@ -1033,6 +1033,12 @@ def run_diff(args, local):
     f_ms, f_l = timed(fwd)
     fb_ms, fb_l = timed(fwd_bwd)
     loss = float(((rgba - target) ** 2).sum())
+    # the same with the transfer-function row linear in the front density (the reference's GPU sampling)
+    ctx.diff_tf_sampling = M.DIFF_TF_LINEAR
+    ctx.diff_forward(wl.camera, wl.gen, wl.rec, Wd, H, m, ttab, mo, b4, pm, target)
+    lf_ms, _ = timed(fwd)
+    lfb_ms, _ = timed(fwd_bwd)
+    ctx.diff_tf_sampling = M.DIFF_TF_BSPLINE
     ctx.close()
     return {"workload": f"{wl.name}_ortho (256^3 Marschner-Lobb, 512x512, m=31, no compaction, ert 1)",
             "fwd": {"value": P / (f_ms * 1e-3) / 1e6, "unit": UNIT, "ms": f_ms, "gpu_launches_per_step": f_l},
@@ -1040,6 +1046,9 @@ def run_diff(args, local):
                             "gpu_launches_per_step": fb_l,
                             "gradients": "transfer-function row (256 x RGBA) and all 256^3 voxel densities"},
             "fwd_adjoint_over_fwd": fb_ms / f_ms, "loss": loss,
+            "linear_tf_row": {"fwd_ms": lf_ms, "fwd_adjoint_ms": lfb_ms, "fwd_adjoint_over_fwd": lfb_ms / lf_ms,
+                              "note": "the transfer-function row linear in the front density (mraygb_set_diff_tf_"
+                                      "sampling), target re-rendered with it"},
             "note": "forward = generate (no compaction) + FP32 Lagrange multipliers + re-march (exact atan, "
                     "B-spline transfer function); adjoint = re-march adjoint + preparation adjoint + generation "
                     "adjoint; the L2 residual and the gradient zeroing (torch) are inside the timed region"}
